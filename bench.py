@@ -1,0 +1,329 @@
+"""Benchmark: body-steps/s of the batched world step on one GB300.
+
+Workload: 4,096 independent worlds (body counts log-uniform in [16, 512],
+60/40 discs/rectangles, each with its own ground box and gravity U[5,15]),
+dt = 1/60, 8 solver iterations, one sub-step.  The scene is first advanced
+300 steps (untimed) so that the timed steps see settled piles with their
+full contact load, not bodies in free fall.  One "step" = one
+Solver.process-equivalent pass over all 4,096 worlds.
+
+value      body-steps/s with the state resident in HBM, CUDA events around
+           each step on the library's stream, L2 flushed (256 MiB write)
+           between steps outside the timed events.
+e2e        the same metric through the C ABI with host buffers: every step
+           writes the full state from pinned host memory, steps, and reads it
+           back (r2d_batch_write_state / process / read_state).
+roofline   algorithmic HBM bytes of the world-step kernel per step
+           (117 B per body-step: 77 B read, 40 B written) over its measured
+           time, against the measured copy bandwidth.
+cpu_baseline  the CPU oracle (the C++ restatement of the reference's step,
+           replaying the same constraint order) on this host's cores, from
+           the same settled state.
+
+--impl reference times that CPU step alone (the reference is Zig and cannot
+be built here) and prints its own line.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+SETTLE_STEPS = 300
+BYTES_READ = 77   # pos 8, angle 4, momentum 8, ang. momentum 4, force+torque 12, AABB 16, mass/inertia/mu/dims 20, kind 1, id 4
+BYTES_WRITE = 40  # pos 8, angle 4, momentum 8, ang. momentum 4, AABB 16
+METRIC = "body-steps/sec on 1 GB300, batched FP32 vs plain, at stated pos error vs FP64"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_from_profile():
+    p = os.path.join(REPO, "profiles", "world_step_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("bytes_per_body_step")
+    return None
+
+
+def cpu_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def settle_scene(sc, steps):
+    """Advance the scene `steps` steps on the CPU oracle (all host threads)."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+
+    _, state, st = O.batch_run(sc, steps, cpu_threads())
+    assert st == 0, st
+    return state.reshape(13, sc.nbodies)
+
+
+def oracle_time(sc, state, steps, threads):
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+
+    secs, _, st = O.batch_run(sc, steps, threads, state_in=state)
+    assert st == 0, st
+    return secs
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from resolve2d_gb300 import build as B
+    from resolve2d_gb300 import scenes
+
+    B.build_oracle()
+    sc = scenes.config3(seed=3)
+    threads = cpu_threads()
+    state = settle_scene(sc, SETTLE_STEPS)
+    # each step: one full pass over all 4,096 worlds
+    for _ in range(args.warmup):
+        oracle_time(sc, state, 1, threads)
+    secs = oracle_time(sc, state, args.steps, threads)
+    bsteps = sc.nbodies * args.steps
+    v = bsteps / secs
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "body-steps/s", "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded)",
+        "config": {"workload": "config3: 4096 worlds, counts log-uniform [16,512], dt 1/60, 8 iterations, settled 300 steps",
+                   "bodies": sc.nbodies, "worlds": sc.nworlds},
+        "cpu_baseline": {"value": v, "unit": "body-steps/s", "cores": threads, "kind": "port",
+                         "sample": f"all {sc.nworlds} worlds x {args.steps} steps from the settled state; "
+                                   "C++ restatement of Solver.process (Zig toolchain absent)"},
+        "e2e": {"value": v, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--plain-worlds", type=int, default=64,
+                    help="worlds stepped one per launch for the plain-path comparison")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    rank, world, local = dist_env()
+    import torch
+
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from resolve2d_gb300 import build as B
+    from resolve2d_gb300 import scenes
+    from resolve2d_gb300.engine import Batch, World
+
+    B.build_library()
+    sc = scenes.config3(seed=3 + rank)
+    stream = torch.cuda.current_stream()
+    batch = Batch.from_scene(sc, stream=stream.cuda_stream)
+    # settle (untimed): bring the worlds to their loaded state
+    for _ in range(SETTLE_STEPS):
+        batch.process(sc.dt, sc.sub_steps, sc.iters)
+    batch.sync()
+    settled = batch.read_state()
+    nb = sc.nbodies
+
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        batch.process(sc.dt, sc.sub_steps, sc.iters)
+    batch.sync()
+    batch.write_state(settled)
+    batch.sync()
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.zero_()
+        starts[k].record(stream)
+        batch.process(sc.dt, sc.sub_steps, sc.iters)
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    batch.sync()
+    ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    dev_s = sum(ms) / 1e3
+    if world > 1:
+        t = torch.tensor([dev_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dev_s = float(t.item())
+    clk = clocks.stop()
+    value = nb * args.steps * world / dev_s
+    launches = batch.launches_per_step() * args.steps
+
+    # end to end through the C ABI with pinned host buffers
+    host = torch.empty((13, nb), dtype=torch.float32).pin_memory()
+    host_np = host.numpy()
+    host_np[...] = settled
+    batch.write_state(host_np)
+    batch.sync()
+    e2e_steps = max(3, min(args.steps, 10))
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for _ in range(e2e_steps):
+        batch.write_state(host_np)
+        batch.process(sc.dt, sc.sub_steps, sc.iters)
+        batch.read_state(host_np)
+    batch.sync()
+    e2e_s = time.perf_counter() - t1
+    e2e_v = nb * e2e_steps / e2e_s
+
+    # plain path: the same worlds, one world per launch
+    plain = None
+    if args.plain_worlds > 0:
+        pw = min(args.plain_worlds, sc.nworlds)
+        worlds = [World.from_scene(sc.world(w), stream=stream.cuda_stream) for w in range(pw)]
+        for i, w in enumerate(worlds):  # first process plans the launch (untimed)
+            w.process(sc.dt, sc.sub_steps, sc.iters)
+            w.sync()
+            b0, b1 = sc.body_off[i], sc.body_off[i + 1]
+            w.write_state(np.ascontiguousarray(settled[:, b0:b1]))
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for w in worlds:
+            w.process(sc.dt, sc.sub_steps, sc.iters)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        nbp = int(sc.body_off[pw])
+        plain = nbp / (ev0.elapsed_time(ev1) / 1e3)
+        for w in worlds:
+            w.close()
+
+    peak, peak_src = measured_peaks()
+    step_s = dev_s / args.steps
+    achieved = (BYTES_READ + BYTES_WRITE) * nb / step_s / 1e9
+    traffic = traffic_from_profile()
+    line = {
+        "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * step_s, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": "config3: 4096 worlds, counts log-uniform [16,512], dt 1/60, 8 iterations, "
+                               "settled 300 steps", "bodies": nb, "worlds": sc.nworlds,
+                   "l2": "flushed between timed steps (256 MiB write outside the events)",
+                   "parallelism": f"replicas x{world}"},
+        "gpu_launches": launches,
+        "wall_s_timed_loop": wall,
+        "e2e": {"value": e2e_v, "unit": "body-steps/s", "h2d_bytes_per_step": 52 * nb, "d2h_bytes_per_step": 52 * nb},
+        "plain_one_world_per_launch": {"value": plain, "unit": "body-steps/s", "worlds": args.plain_worlds,
+                                       "batched_over_plain": (value / world) / plain if plain else None},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_src,
+                     "traffic": None if traffic is None else traffic * nb,
+                     "bytes_per_body_step": BYTES_READ + BYTES_WRITE},
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = cpu_threads()
+        sub_steps = 2
+        secs = oracle_time(sc, settled, sub_steps, threads)
+        line["cpu_baseline"] = {"value": nb * sub_steps / secs, "unit": "body-steps/s", "cores": threads,
+                                "kind": "port",
+                                "sample": f"all {sc.nworlds} worlds x {sub_steps} steps from the settled state "
+                                          "(C++ restatement of Solver.process; Zig toolchain absent)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,187 @@
+/*
+ * r2d_gb300.h -- C ABI of the GB300 step library (libr2d_gb300.so).
+ *
+ * It replaces the CPU step of nilsblix/resolve2d, Solver.process
+ * (src/core/lib.zig:189-251), behind plain pointers and sizes so that the
+ * reference's own host language can bind it (Zig `extern fn`; the binding a
+ * maintainer would add is shown in INTEGRATION.md).  Reference paths below
+ * are relative to the reference project.
+ *
+ * Conventions
+ *   - Every entry point returns an r2d_status (0 = success, negative = error).
+ *     Errors never abort; the reference's error unions map onto them:
+ *     error.InvalidRigidBodyId -> R2D_ERR_INVALID_BODY_ID,
+ *     error.OutOfMemory        -> R2D_ERR_OUT_OF_MEMORY.
+ *   - Host buffers are caller-owned; the library owns all device memory.
+ *   - Per-body arrays are field-major: field f of body i is at [f * n + i].
+ *   - Body ids are u32 (the reference's RigidBody.Id is u16,
+ *     src/core/Bodies/RigidBody.zig:15; u32 lets one world hold more bodies).
+ *   - One handle per host thread; calls on one handle are not reentrant.
+ *   - `stream` in r2d_config is a cudaStream_t (NULL = a stream the library
+ *     creates).  r2d_*_process only enqueues work; r2d_*_sync waits for it
+ *     and returns the first device-side error.
+ */
+#ifndef R2D_GB300_H
+#define R2D_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define R2D_API __attribute__((visibility("default")))
+#else
+#define R2D_API
+#endif
+
+typedef enum r2d_status {
+    R2D_OK = 0,
+    R2D_ERR_INVALID_ARGUMENT = -1,
+    R2D_ERR_INVALID_BODY_ID = -2, /* error.InvalidRigidBodyId (src/core/Constraints/DistanceJoint.zig:44-47) */
+    R2D_ERR_OUT_OF_MEMORY = -3,   /* error.OutOfMemory */
+    R2D_ERR_CUDA = -4,            /* a CUDA runtime call failed (see r2d_last_error_string) */
+    R2D_ERR_CAPACITY = -5,        /* a world outgrew the per-world capacity of its kernel class */
+    R2D_ERR_TIMEOUT = -6,         /* a bounded device-side wait gave up */
+    R2D_ERR_NONFINITE = -7,       /* an AABB coordinate is not a representable spatial-hash cell */
+    R2D_ERR_NO_DEVICE = -8        /* no CUDA device is visible */
+} r2d_status;
+
+/* Per-body state, f32 field-major [R2D_STATE_FIELDS][n]
+ * (RigidBody.Props, src/core/Bodies/RigidBody.zig:69-81, plus the body's
+ * stored AABB, RigidBody.zig:84, which the next frame's broadphase reads). */
+enum {
+    R2D_S_POS_X = 0, R2D_S_POS_Y, R2D_S_ANGLE,
+    R2D_S_MOM_X, R2D_S_MOM_Y, R2D_S_ANG_MOM,
+    R2D_S_FORCE_X, R2D_S_FORCE_Y, R2D_S_TORQUE,
+    R2D_S_AABB_X, R2D_S_AABB_Y, R2D_S_AABB_HW, R2D_S_AABB_HH,
+    R2D_STATE_FIELDS
+};
+
+/* Per-body constant properties, f32 field-major [R2D_PROP_FIELDS][n]:
+ * mass, inertia, mu, then radius (disc) or width, height (rectangle)
+ * (Disc.zig:8, Rectangle.zig:17-18). */
+enum { R2D_P_MASS = 0, R2D_P_INERTIA, R2D_P_MU, R2D_P_DIM0, R2D_P_DIM1, R2D_PROP_FIELDS };
+
+/* kind bits per body: RigidBody.Type (RigidBody.zig:28-31) and the static flag (:85) */
+enum { R2D_KIND_RECTANGLE = 1, R2D_KIND_STATIC = 2 };
+
+/* Constraint.Type (src/core/Constraints/Constraint.zig:15-20) */
+enum {
+    R2D_JOINT_DISTANCE = 0,
+    R2D_JOINT_OFFSET_DISTANCE = 1,
+    R2D_JOINT_FIXED_POSITION = 2,
+    R2D_JOINT_MOTOR = 3
+};
+
+/* Joint parameters, f32 [n][R2D_JOINT_PARAMS]:
+ *   [0] power_max [1] power_min [2] beta   (Constraint.Parameters, Constraint.zig:27-31)
+ *   distance:        [3] target_distance
+ *   offset distance: [3] r1.x [4] r1.y [5] r2.x [6] r2.y [7] target_distance
+ *   fixed position:  [3] target.x [4] target.y
+ *   motor:           [3] target_omega */
+enum { R2D_JOINT_PARAMS = 8 };
+
+/* Floats per manifold in r2d_*_get_manifolds:
+ *   [0..1] normal [2..3] tangent [4] friction [5] has point 0 [6] has point 1
+ *   [7] prev_angle_1 [8] prev_angle_2, then per point (12 floats, points 0 and 1):
+ *   pos.x pos.y (NaN: not kept on the device) ref_r.x ref_r.y inc_r.x inc_r.y
+ *   depth original_depth mass_n mass_t accumulated_pn accumulated_pt
+ *   (CollisionManifold / CollisionPoint, src/core/collision.zig:22-69). */
+enum { R2D_MANIFOLD_FLOATS = 33 };
+
+enum {
+    R2D_FLAG_DEBUG_TAPS = 1u /* keep manifolds and colours for r2d_*_get_manifolds */
+};
+
+typedef struct r2d_config {
+    /* Spatial hash cell width and bucket-table multiplier.  The reference
+     * hard-codes 4.0 and 2 * bodies (src/core/lib.zig:254-255) and ignores
+     * Solver.init's arguments (lib.zig:145); 0 selects those values. */
+    float spatialhash_cell_width;
+    uint32_t spatialhash_table_size_mult;
+    uint32_t flags;
+    void* stream;
+} r2d_config;
+
+/* ---------------------------------------------------------------------------
+ * One world: the drop-in for Solver (src/core/lib.zig:132-315) and the WASM
+ * exports solverInit / solverDeinit / solverProcess (src/wasm_root.zig:18-43).
+ * ------------------------------------------------------------------------- */
+typedef struct r2d_solver r2d_solver;
+
+/* Solver.init (lib.zig:145-157) / solverInit (wasm_root.zig:18-30) */
+R2D_API int r2d_solver_create(const r2d_config* cfg, r2d_solver** out);
+/* Solver.deinit (lib.zig:159-179) / solverDeinit (wasm_root.zig:32-37) */
+R2D_API int r2d_solver_destroy(r2d_solver* s);
+
+/* Replaces the body store (Solver.bodies, lib.zig:135) in its iteration
+ * order.  props [R2D_PROP_FIELDS][n], state [R2D_STATE_FIELDS][n].  With
+ * init_aabb != 0 every AABB is computed as RigidBody.updateAABB does when a
+ * body is created (Disc.zig:63-66, Rectangle.zig:71-86) and the AABB fields
+ * of `state` are ignored. */
+R2D_API int r2d_solver_set_bodies(r2d_solver* s, uint32_t n, const uint32_t* ids, const uint8_t* kind,
+                                  const float* props, const float* state, int init_aabb);
+/* Per-frame mirror of the dynamic state (host -> device, device -> host). */
+R2D_API int r2d_solver_write_state(r2d_solver* s, const float* state);
+R2D_API int r2d_solver_read_state(r2d_solver* s, float* state);
+/* Solver.force_generators (lib.zig:136): one DownwardsGravity per entry
+ * (src/core/Forces/DownwardsGravity.zig:19-39), at most 4. */
+R2D_API int r2d_solver_set_gravity(r2d_solver* s, uint32_t n, const float* g);
+/* Solver.constraints (lib.zig:139), EntityFactory.make*Joint (lib.zig:100-122).
+ * Ids refer to body ids; they are resolved at r2d_solver_process, which
+ * returns R2D_ERR_INVALID_BODY_ID (state untouched) for an unknown id. */
+R2D_API int r2d_solver_set_joints(r2d_solver* s, uint32_t n, const uint8_t* type, const uint32_t* id1,
+                                  const uint32_t* id2, const float* params);
+/* Solver.exclude_collision_pairs / EntityFactory.excludeCollisionPair
+ * (lib.zig:124-129): pairs [n][2] of body ids. */
+R2D_API int r2d_solver_set_exclusions(r2d_solver* s, uint32_t n, const uint32_t* pairs);
+/* Solver.process (lib.zig:189-251) / solverProcess (wasm_root.zig:39-43). */
+R2D_API int r2d_solver_process(r2d_solver* s, float dt, uint32_t sub_steps, uint32_t collision_iters);
+R2D_API int r2d_solver_sync(r2d_solver* s);
+/* Debug taps (need R2D_FLAG_DEBUG_TAPS): the last frame's manifolds
+ * (Solver.manifolds, lib.zig:137) with their contact colours.  keys [cap][2]
+ * are (reference, incident) body indices; data [cap][R2D_MANIFOLD_FLOATS]. */
+R2D_API int r2d_solver_num_manifolds(r2d_solver* s, uint32_t* out);
+R2D_API int r2d_solver_get_manifolds(r2d_solver* s, uint32_t cap, uint32_t* keys, float* data,
+                                     uint32_t* colours);
+R2D_API int r2d_solver_get_joint_colours(r2d_solver* s, uint32_t cap, uint32_t* colours);
+
+/* ---------------------------------------------------------------------------
+ * Many independent worlds stepped by one launch per kernel class.  No
+ * counterpart in the reference, which holds one global solver
+ * (src/wasm_root.zig:15); each world behaves exactly like one r2d_solver.
+ * ------------------------------------------------------------------------- */
+typedef struct r2d_batch r2d_batch;
+
+R2D_API int r2d_batch_create(const r2d_config* cfg, r2d_batch** out);
+R2D_API int r2d_batch_destroy(r2d_batch* b);
+/* Bodies of world w are [body_off[w], body_off[w+1]) of the concatenated
+ * arrays (same layouts as r2d_solver_set_bodies); gravity [nworlds] is one
+ * DownwardsGravity per world (0 = none). */
+R2D_API int r2d_batch_set_worlds(r2d_batch* b, uint32_t nworlds, const uint32_t* body_off, const uint32_t* ids,
+                                 const uint8_t* kind, const float* props, const float* state,
+                                 const float* gravity, int init_aabb);
+R2D_API int r2d_batch_write_state(r2d_batch* b, const float* state);
+R2D_API int r2d_batch_read_state(r2d_batch* b, float* state);
+R2D_API int r2d_batch_process(r2d_batch* b, float dt, uint32_t sub_steps, uint32_t collision_iters);
+R2D_API int r2d_batch_sync(r2d_batch* b);
+/* Kernel launches one r2d_batch_process enqueues (one per occupied size class). */
+R2D_API int r2d_batch_launches_per_step(r2d_batch* b, uint32_t* out);
+/* Per-world status of the last synced step (0 or an r2d_status). */
+R2D_API int r2d_batch_world_status(r2d_batch* b, int* status);
+/* Debug taps for world w (need R2D_FLAG_DEBUG_TAPS). */
+R2D_API int r2d_batch_num_manifolds(r2d_batch* b, uint32_t w, uint32_t* out);
+R2D_API int r2d_batch_get_manifolds(r2d_batch* b, uint32_t w, uint32_t cap, uint32_t* keys, float* data,
+                                    uint32_t* colours);
+
+/* Library information. */
+R2D_API const char* r2d_last_error_string(void);
+R2D_API int r2d_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* R2D_GB300_H */

@@ -1,0 +1,198 @@
+"""ctypes wrapper of the CPU oracle (r2d_oracle.hpp / oracle_capi.cpp).
+
+TEST INFRASTRUCTURE: imported only by tests/, __graft_entry__.smoke() and
+bench.py (its CPU baseline and --impl reference arm).  The product package
+never imports it.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "_build" / "libr2d_oracle.so"
+ORDER_REFERENCE, ORDER_COLOUR = 0, 1
+NSTATE, NPROP, MF = 13, 5, 33
+
+_u32p = C.POINTER(C.c_uint32)
+_u8p = C.POINTER(C.c_uint8)
+_f32p = C.POINTER(C.c_float)
+_f64p = C.POINTER(C.c_double)
+_i32p = C.POINTER(C.c_int)
+_P = C.c_void_p
+
+_SIG = {
+    "r2o_create": ([C.c_int], _P),
+    "r2o_destroy": ([_P], None),
+    "r2o_add_bodies": ([_P, C.c_uint32, _u32p, _u8p, _f32p], C.c_int),
+    "r2o_num_bodies": ([_P], C.c_uint32),
+    "r2o_add_gravity": ([_P, C.c_float], None),
+    "r2o_exclude_pair": ([_P, C.c_uint32, C.c_uint32], None),
+    "r2o_add_joints": ([_P, C.c_uint32, _u8p, _u32p, _u32p, _f32p], None),
+    "r2o_set_hash_config": ([_P, C.c_float, C.c_uint32], None),
+    "r2o_get_state": ([_P, _f32p], None),
+    "r2o_get_state_f64": ([_P, _f64p], None),
+    "r2o_set_state": ([_P, _f32p], None),
+    "r2o_get_props": ([_P, _f32p], None),
+    "r2o_process": ([_P, C.c_float, C.c_uint32, C.c_uint32, C.c_int], C.c_int),
+    "r2o_update_manifolds": ([_P, C.c_int], C.c_int),
+    "r2o_num_manifolds": ([_P], C.c_uint32),
+    "r2o_get_manifolds": ([_P, _u32p, _f32p], None),
+    "r2o_get_colours": ([_P, _u32p, _u32p], None),
+    "r2o_nmath_kat": ([_f32p, _f32p, _f32p], None),
+    "r2o_aabb_intersects": ([C.c_float] * 8, C.c_int),
+    "r2o_sincosf": ([C.c_uint32, _f32p, _f32p, _f32p], None),
+    "r2o_batch_run": ([C.c_int, C.c_uint32, _u32p, _u32p, _u8p, _f32p, _f32p, C.c_float, C.c_uint32,
+                       C.c_uint32, C.c_uint32, C.c_int, C.c_int, _f32p, _f32p, _i32p], C.c_double),
+}
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} is not built (make -C oracle)")
+        lib = C.CDLL(str(LIB_PATH))
+        for k, (a, r) in _SIG.items():
+            f = getattr(lib, k)
+            f.argtypes = a
+            f.restype = r
+        _lib = lib
+    return _lib
+
+
+def _p(a, t):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+class Oracle:
+    """One world of the CPU restatement (precision 32 = f32, 64 = FP64)."""
+
+    def __init__(self, precision: int = 32):
+        self.lib = load()
+        self.h = self.lib.r2o_create(precision)
+        self.precision = precision
+        self.nj = 0
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.lib.r2o_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+    @classmethod
+    def from_scene(cls, sc, precision: int = 32, world: int = 0) -> "Oracle":
+        if sc.nworlds != 1:
+            sc = sc.world(world)
+        o = cls(precision)
+        ids = np.ascontiguousarray(sc.ids, np.uint32)
+        kind = np.ascontiguousarray(sc.kind, np.uint8)
+        opt = np.ascontiguousarray(sc.opt, np.float32)
+        o.lib.r2o_add_bodies(o.h, ids.shape[0], _p(ids, C.c_uint32), _p(kind, C.c_uint8), _p(opt, C.c_float))
+        for g in np.atleast_1d(sc.gravity):
+            if g != 0:
+                o.lib.r2o_add_gravity(o.h, float(g))
+        if sc.jtype.size:
+            t = np.ascontiguousarray(sc.jtype, np.uint8)
+            a = np.ascontiguousarray(sc.jid1, np.uint32)
+            b = np.ascontiguousarray(sc.jid2, np.uint32)
+            p = np.ascontiguousarray(sc.jprm, np.float32)
+            o.lib.r2o_add_joints(o.h, t.shape[0], _p(t, C.c_uint8), _p(a, C.c_uint32), _p(b, C.c_uint32),
+                                 _p(p, C.c_float))
+            o.nj = int(t.shape[0])
+        for (x, y) in np.asarray(sc.xpairs).reshape(-1, 2):
+            o.lib.r2o_exclude_pair(o.h, int(x), int(y))
+        return o
+
+    @property
+    def n(self) -> int:
+        return int(self.lib.r2o_num_bodies(self.h))
+
+    def set_hash(self, cell: float, mult: int):
+        self.lib.r2o_set_hash_config(self.h, cell, mult)
+
+    def state(self) -> np.ndarray:
+        out = np.empty((NSTATE, self.n), np.float32)
+        self.lib.r2o_get_state(self.h, _p(out, C.c_float))
+        return out
+
+    def state64(self) -> np.ndarray:
+        out = np.empty((NSTATE, self.n), np.float64)
+        self.lib.r2o_get_state_f64(self.h, _p(out, C.c_double))
+        return out
+
+    def set_state(self, st: np.ndarray):
+        st = np.ascontiguousarray(st, np.float32)
+        self.lib.r2o_set_state(self.h, _p(st, C.c_float))
+
+    def props(self) -> np.ndarray:
+        out = np.empty((NPROP, self.n), np.float32)
+        self.lib.r2o_get_props(self.h, _p(out, C.c_float))
+        return out
+
+    def process(self, dt: float, sub_steps: int = 1, iters: int = 8, order: int = ORDER_COLOUR) -> int:
+        return int(self.lib.r2o_process(self.h, float(dt), int(sub_steps), int(iters), int(order)))
+
+    def update_manifolds(self, order: int = ORDER_COLOUR) -> int:
+        return int(self.lib.r2o_update_manifolds(self.h, int(order)))
+
+    def manifolds(self):
+        m = int(self.lib.r2o_num_manifolds(self.h))
+        k = np.zeros((m, 2), np.uint32)
+        d = np.zeros((m, MF), np.float32)
+        self.lib.r2o_get_manifolds(self.h, _p(k, C.c_uint32), _p(d, C.c_float))
+        return k, d
+
+    def colours(self):
+        m = int(self.lib.r2o_num_manifolds(self.h))
+        c = np.zeros(m, np.uint32)
+        j = np.zeros(max(self.nj, 1), np.uint32)
+        self.lib.r2o_get_colours(self.h, _p(c, C.c_uint32), _p(j, C.c_uint32))
+        return c, j[: self.nj]
+
+
+def batch_run(sc, steps: int, nthreads: int, precision: int = 32, order: int = ORDER_COLOUR, state_in=None):
+    """Step every world of a scene on host threads, optionally from a given
+    state ([13][n] field-major over all worlds); returns (seconds, state
+    [13][n], status)."""
+    lib = load()
+    off = np.ascontiguousarray(sc.body_off, np.uint32)
+    ids = np.ascontiguousarray(sc.ids, np.uint32)
+    kind = np.ascontiguousarray(sc.kind, np.uint8)
+    opt = np.ascontiguousarray(sc.opt, np.float32)
+    grav = np.ascontiguousarray(sc.gravity, np.float32)
+    state = np.zeros((NSTATE, sc.nbodies), np.float32)
+    sin = None if state_in is None else np.ascontiguousarray(state_in, np.float32)
+    status = C.c_int(0)
+    secs = lib.r2o_batch_run(precision, sc.nworlds, _p(off, C.c_uint32), _p(ids, C.c_uint32), _p(kind, C.c_uint8),
+                             _p(opt, C.c_float), _p(grav, C.c_float), float(sc.dt), sc.sub_steps, sc.iters,
+                             int(steps), int(order), int(nthreads), None if sin is None else _p(sin, C.c_float),
+                             _p(state, C.c_float), C.byref(status))
+    return float(secs), state, int(status.value)
+
+
+def nmath_kat(a, b) -> np.ndarray:
+    """[add2 xy, sub2 xy, multelem2 xy, divelem2 xy, dot2, cross2, length2sq(a), length2(a)]"""
+    a = np.ascontiguousarray(a, np.float32)
+    b = np.ascontiguousarray(b, np.float32)
+    out = np.zeros(12, np.float32)
+    load().r2o_nmath_kat(_p(a, C.c_float), _p(b, C.c_float), _p(out, C.c_float))
+    return out
+
+
+def aabb_intersects(s1, s2) -> bool:
+    return bool(load().r2o_aabb_intersects(*[float(v) for v in (*s1, *s2)]))
+
+
+def sincosf(x) -> tuple[np.ndarray, np.ndarray]:
+    x = np.ascontiguousarray(x, np.float32)
+    s = np.empty_like(x)
+    c = np.empty_like(x)
+    load().r2o_sincosf(x.size, _p(x, C.c_float), _p(s, C.c_float), _p(c, C.c_float))
+    return s, c

@@ -1,0 +1,751 @@
+/*
+ * r2d_capi.cu -- host runtime behind include/r2d_gb300.h.
+ *
+ * An Engine owns the device copy of one or many worlds (field-major state
+ * and properties in HBM, world descriptors, joints, exclusions) and steps
+ * them with the fused per-world kernel (r2d_world_kernel.cu).  Worlds are
+ * grouped into size classes; each class is one launch whose per-world
+ * shared-memory budget is sized from that class's capacities, so small
+ * worlds pack many CTAs per SM and large ones still fit.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/r2d_gb300.h"
+#include "r2d_sincos.h"
+#include "r2d_world.cuh"
+
+namespace r2d {
+cudaError_t launch_world_step(const StepParams& P, const Caps& C, int threads, cudaStream_t stream);
+cudaError_t world_step_occupancy(const Caps& C, int threads, int* blocks_per_sm);
+}  // namespace r2d
+
+using namespace r2d;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+#define CUDA_TRY(expr)                                                                       \
+    do {                                                                                     \
+        cudaError_t e_ = (expr);                                                             \
+        if (e_ != cudaSuccess) {                                                             \
+            if (e_ == cudaErrorMemoryAllocation) return fail(R2D_ERR_OUT_OF_MEMORY, #expr);  \
+            return fail(R2D_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+        }                                                                                    \
+    } while (0)
+
+template <class T>
+void dfree(T*& p) {
+    if (p) cudaFree((void*)p);
+    p = nullptr;
+}
+
+template <class T>
+cudaError_t dalloc(T*& p, size_t count) {
+    dfree(p);
+    if (count == 0) count = 1;
+    return cudaMalloc((void**)&p, count * sizeof(T));
+}
+
+uint32_t next_pow2(uint32_t v) {
+    uint32_t p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+// AABB of a freshly created body (Disc.zig:63-66, Rectangle.zig:71-86).
+void init_aabb(uint8_t kind, float x, float y, float angle, float d0, float d1, float out[4]) {
+    out[0] = x;
+    out[1] = y;
+    if (!(kind & K_RECT)) {
+        out[2] = d0;
+        out[3] = d0;
+        return;
+    }
+    float s, c;
+    r2d_sincosf(angle, &s, &c);
+    const float w = d0 / 2.0f, h = d1 / 2.0f;
+    const float lx[4] = {-w, -w, w, w}, ly[4] = {-h, h, h, -h};
+    float ew = 0.f, eh = 0.f;
+    for (int i = 0; i < 4; ++i) {
+        float rx = lx[i] * c - ly[i] * s;
+        float ry = lx[i] * s + ly[i] * c;
+        if (rx > ew) ew = rx;
+        if (ry > eh) eh = ry;
+    }
+    out[2] = ew;
+    out[3] = eh;
+}
+
+struct KClass {
+    Caps caps{};
+    int threads = 128;
+    std::vector<uint32_t> worlds;
+    uint32_t* d_list = nullptr;
+    uint32_t smem = 0;
+};
+
+struct Engine {
+    r2d_config cfg{};
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    float cell = 4.0f;
+    uint32_t table_mult = 2;
+
+    uint32_t nworlds = 0, nbodies = 0;
+    std::vector<WorldDesc> worlds_h;
+    std::vector<uint32_t> ids_h;
+    std::vector<uint8_t> kind_h;
+    std::vector<float> props_h;
+    std::vector<float> state_h;  // last uploaded (for capacity planning)
+
+    float* d_state = nullptr;
+    float* d_props = nullptr;
+    uint8_t* d_kind = nullptr;
+    uint32_t* d_ids = nullptr;
+    WorldDesc* d_worlds = nullptr;
+    int* d_status = nullptr;
+    int* d_err = nullptr;
+    int* h_err = nullptr;  // pinned
+
+    // joints / exclusions (resolved to world-local indices)
+    uint32_t njoints = 0, nexcl = 0;
+    uint8_t* d_jtype = nullptr;
+    uint16_t* d_jb1 = nullptr;
+    uint16_t* d_jb2 = nullptr;
+    float* d_jprm = nullptr;
+    uint32_t* d_excl = nullptr;
+
+    std::vector<KClass> classes;
+    bool plan_dirty = true;
+
+    // debug taps
+    DebugOut dbg{};
+    uint32_t* d_dbg_nman = nullptr;
+    uint32_t* d_dbg_keys = nullptr;
+    float* d_dbg_data = nullptr;
+    uint32_t* d_dbg_col = nullptr;
+    uint32_t* d_dbg_jcol = nullptr;
+
+    std::vector<int> status_h;
+    bool pending = false;
+
+    ~Engine() {
+        dfree(d_state); dfree(d_props); dfree(d_kind); dfree(d_ids); dfree(d_worlds);
+        dfree(d_status); dfree(d_err);
+        if (h_err) cudaFreeHost(h_err);
+        dfree(d_jtype); dfree(d_jb1); dfree(d_jb2); dfree(d_jprm); dfree(d_excl);
+        for (auto& c : classes) dfree(c.d_list);
+        dfree(d_dbg_nman); dfree(d_dbg_keys); dfree(d_dbg_data); dfree(d_dbg_col); dfree(d_dbg_jcol);
+        if (own_stream && stream) cudaStreamDestroy(stream);
+    }
+
+    int init(const r2d_config* c) {
+        if (c) cfg = *c;
+        int ndev = 0;
+        if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(R2D_ERR_NO_DEVICE, "no CUDA device");
+        cell = cfg.spatialhash_cell_width > 0.f ? cfg.spatialhash_cell_width : 4.0f;
+        table_mult = cfg.spatialhash_table_size_mult ? cfg.spatialhash_table_size_mult : 2u;
+        if (cfg.stream) {
+            stream = (cudaStream_t)cfg.stream;
+        } else {
+            CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+            own_stream = true;
+        }
+        CUDA_TRY(cudaMallocHost((void**)&h_err, sizeof(int)));
+        CUDA_TRY(dalloc(d_err, 1));
+        return R2D_OK;
+    }
+
+    int set_bodies(uint32_t nw, const uint32_t* body_off, const uint32_t* ids, const uint8_t* kind,
+                   const float* props, const float* state, const float* gravity, uint32_t ngrav_each,
+                   int do_init_aabb) {
+        const uint32_t n = body_off[nw];
+        for (uint32_t w = 0; w < nw; ++w)
+            if (body_off[w + 1] < body_off[w]) return fail(R2D_ERR_INVALID_ARGUMENT, "body_off not monotonic");
+        nworlds = nw;
+        nbodies = n;
+        ids_h.assign(ids, ids + n);
+        kind_h.assign(kind, kind + n);
+        props_h.assign(props, props + (size_t)P_NFIELDS * n);
+        state_h.assign(state, state + (size_t)S_NFIELDS * n);
+        if (do_init_aabb) {
+            for (uint32_t i = 0; i < n; ++i) {
+                float ab[4];
+                init_aabb(kind_h[i], state_h[(size_t)S_POS_X * n + i], state_h[(size_t)S_POS_Y * n + i],
+                          state_h[(size_t)S_ANGLE * n + i], props_h[(size_t)P_DIM0 * n + i],
+                          props_h[(size_t)P_DIM1 * n + i], ab);
+                for (int k = 0; k < 4; ++k) state_h[(size_t)(S_AABB_X + k) * n + i] = ab[k];
+            }
+        }
+        worlds_h.assign(nw, WorldDesc{});
+        for (uint32_t w = 0; w < nw; ++w) {
+            WorldDesc& d = worlds_h[w];
+            d.body_off = body_off[w];
+            d.n = body_off[w + 1] - body_off[w];
+            d.ngrav = 0;
+            for (uint32_t k = 0; k < ngrav_each && k < (uint32_t)MAX_GRAVITY; ++k) {
+                d.g[k] = gravity[(size_t)w * ngrav_each + k];
+                d.ngrav++;
+            }
+        }
+        CUDA_TRY(dalloc(d_state, (size_t)S_NFIELDS * n));
+        CUDA_TRY(dalloc(d_props, (size_t)P_NFIELDS * n));
+        CUDA_TRY(dalloc(d_kind, n));
+        CUDA_TRY(dalloc(d_ids, n));
+        CUDA_TRY(dalloc(d_status, nw));
+        CUDA_TRY(cudaMemcpyAsync(d_state, state_h.data(), sizeof(float) * S_NFIELDS * n, cudaMemcpyHostToDevice, stream));
+        CUDA_TRY(cudaMemcpyAsync(d_props, props_h.data(), sizeof(float) * P_NFIELDS * n, cudaMemcpyHostToDevice, stream));
+        CUDA_TRY(cudaMemcpyAsync(d_kind, kind_h.data(), n, cudaMemcpyHostToDevice, stream));
+        CUDA_TRY(cudaMemcpyAsync(d_ids, ids_h.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice, stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        plan_dirty = true;
+        return R2D_OK;
+    }
+
+    int write_state(const float* state) {
+        if (!d_state) return fail(R2D_ERR_INVALID_ARGUMENT, "no bodies");
+        CUDA_TRY(cudaMemcpyAsync(d_state, state, sizeof(float) * S_NFIELDS * nbodies, cudaMemcpyHostToDevice, stream));
+        return R2D_OK;
+    }
+
+    int read_state(float* state) {
+        if (!d_state) return fail(R2D_ERR_INVALID_ARGUMENT, "no bodies");
+        CUDA_TRY(cudaMemcpyAsync(state, d_state, sizeof(float) * S_NFIELDS * nbodies, cudaMemcpyDeviceToHost, stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        return R2D_OK;
+    }
+
+    // Joints / exclusions already resolved to world-local indices.
+    int set_constraints(const std::vector<uint32_t>& jworld, const std::vector<uint8_t>& jtype,
+                        const std::vector<uint16_t>& jb1, const std::vector<uint16_t>& jb2,
+                        const std::vector<float>& jprm, const std::vector<uint32_t>& xworld,
+                        const std::vector<uint32_t>& xkey) {
+        // joints are grouped per world in the order given (insertion order inside a world)
+        njoints = (uint32_t)jtype.size();
+        std::vector<uint32_t> order(njoints);
+        for (uint32_t j = 0; j < njoints; ++j) order[j] = j;
+        std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return jworld[a] < jworld[b]; });
+        std::vector<uint8_t> t(njoints);
+        std::vector<uint16_t> b1(njoints), b2(njoints);
+        std::vector<float> p((size_t)njoints * JOINT_PARAMS);
+        for (auto& d : worlds_h) {
+            d.joint_off = 0;
+            d.nj = 0;
+            d.excl_off = 0;
+            d.nexcl = 0;
+            d.flags &= ~W_DISC_ROTATION;
+        }
+        for (uint32_t k = 0; k < njoints; ++k) {
+            const uint32_t j = order[k];
+            t[k] = jtype[j];
+            b1[k] = jb1[j];
+            b2[k] = jb2[j];
+            std::copy(jprm.begin() + (size_t)j * JOINT_PARAMS, jprm.begin() + (size_t)(j + 1) * JOINT_PARAMS,
+                      p.begin() + (size_t)k * JOINT_PARAMS);
+            WorldDesc& d = worlds_h[jworld[j]];
+            if (d.nj == 0) d.joint_off = k;
+            d.nj++;
+            if (jtype[j] == J_OFFSET) d.flags |= W_DISC_ROTATION;
+        }
+        nexcl = (uint32_t)xkey.size();
+        std::vector<uint64_t> xs(nexcl);
+        for (uint32_t k = 0; k < nexcl; ++k) xs[k] = ((uint64_t)xworld[k] << 32) | xkey[k];
+        std::sort(xs.begin(), xs.end());
+        xs.erase(std::unique(xs.begin(), xs.end()), xs.end());
+        nexcl = (uint32_t)xs.size();
+        std::vector<uint32_t> xk(nexcl);
+        for (uint32_t k = 0; k < nexcl; ++k) {
+            const uint32_t w = (uint32_t)(xs[k] >> 32);
+            xk[k] = (uint32_t)xs[k];
+            WorldDesc& d = worlds_h[w];
+            if (d.nexcl == 0) d.excl_off = k;
+            d.nexcl++;
+        }
+        CUDA_TRY(dalloc(d_jtype, njoints));
+        CUDA_TRY(dalloc(d_jb1, njoints));
+        CUDA_TRY(dalloc(d_jb2, njoints));
+        CUDA_TRY(dalloc(d_jprm, (size_t)njoints * JOINT_PARAMS));
+        CUDA_TRY(dalloc(d_excl, nexcl));
+        if (njoints) {
+            CUDA_TRY(cudaMemcpyAsync(d_jtype, t.data(), njoints, cudaMemcpyHostToDevice, stream));
+            CUDA_TRY(cudaMemcpyAsync(d_jb1, b1.data(), 2 * njoints, cudaMemcpyHostToDevice, stream));
+            CUDA_TRY(cudaMemcpyAsync(d_jb2, b2.data(), 2 * njoints, cudaMemcpyHostToDevice, stream));
+            CUDA_TRY(cudaMemcpyAsync(d_jprm, p.data(), sizeof(float) * p.size(), cudaMemcpyHostToDevice, stream));
+        }
+        if (nexcl) CUDA_TRY(cudaMemcpyAsync(d_excl, xk.data(), 4 * nexcl, cudaMemcpyHostToDevice, stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        plan_dirty = true;
+        return R2D_OK;
+    }
+
+    // Capacity of a world class sized from the worlds it holds.
+    Caps caps_for(uint32_t nb, uint32_t max_nj, float rect_frac, uint32_t max_cells) const {
+        Caps c{};
+        c.nb = nb;
+        c.nm = std::min<uint32_t>(65535u, 3u * nb + 32u);
+        c.npt = std::min<uint32_t>(65535u, (uint32_t)std::ceil(c.nm * (1.0f + std::min(1.0f, rect_frac + 0.15f))) + 16u);
+        c.ne = std::min<uint32_t>(65535u, std::max<uint32_t>(4u * nb + 64u, max_cells * 3u / 2u + 64u));
+        c.np = std::min<uint32_t>(65535u, 4u * nb + 32u);
+        c.hs = next_pow2(2u * c.np);
+        c.nj = max_nj;
+        c.nt = table_mult * nb;
+        return c;
+    }
+
+    uint32_t cells_of(uint32_t i) const {
+        const uint32_t n = nbodies;
+        const float x = state_h[(size_t)S_AABB_X * n + i], y = state_h[(size_t)S_AABB_Y * n + i];
+        const float hw = state_h[(size_t)S_AABB_HW * n + i], hh = state_h[(size_t)S_AABB_HH * n + i];
+        // rotation can grow a rectangle's extents up to its half-diagonal
+        float r = hw > hh ? hw : hh;
+        if (kind_h[i] & K_RECT) {
+            const float d0 = props_h[(size_t)P_DIM0 * n + i], d1 = props_h[(size_t)P_DIM1 * n + i];
+            r = 0.5f * std::sqrt(d0 * d0 + d1 * d1);
+        }
+        (void)x;
+        (void)y;
+        const double span = std::floor(2.0 * r / cell) + 2.0;
+        const double c = span * span;
+        return c > 65535.0 ? 65535u : (uint32_t)c;
+    }
+
+    int plan() {
+        for (auto& c : classes) dfree(c.d_list);
+        classes.clear();
+        // size classes by body count: bounds in bodies
+        static const uint32_t bounds[] = {32, 64, 96, 128, 160, 192, 256, 320, 384, 448, 512, 640, 768, 1024};
+        const int nbnd = sizeof(bounds) / sizeof(bounds[0]);
+        std::vector<std::vector<uint32_t>> groups(nbnd);
+        for (uint32_t w = 0; w < nworlds; ++w) {
+            const uint32_t n = worlds_h[w].n;
+            int k = 0;
+            while (k < nbnd - 1 && n > bounds[k]) ++k;
+            if (n > bounds[nbnd - 1])
+                return fail(R2D_ERR_CAPACITY, "world " + std::to_string(w) + " has " + std::to_string(n) +
+                                                  " bodies; the fused kernel holds at most " +
+                                                  std::to_string(bounds[nbnd - 1]));
+            groups[k].push_back(w);
+        }
+        int dev = 0;
+        cudaGetDevice(&dev);
+        int smem_optin = 0;
+        cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        for (int k = 0; k < nbnd; ++k) {
+            if (groups[k].empty()) continue;
+            KClass kc;
+            uint32_t max_nj = 0, max_cells = 0;
+            float rect_frac = 0.f;
+            for (uint32_t w : groups[k]) {
+                const WorldDesc& d = worlds_h[w];
+                max_nj = std::max(max_nj, d.nj);
+                uint32_t rects = 0, cells = 0;
+                for (uint32_t i = d.body_off; i < d.body_off + d.n; ++i) {
+                    rects += (kind_h[i] & K_RECT) ? 1u : 0u;
+                    cells += cells_of(i);
+                }
+                max_cells = std::max(max_cells, cells);
+                if (d.n) rect_frac = std::max(rect_frac, (float)rects / (float)d.n);
+            }
+            kc.caps = caps_for(bounds[k], max_nj, rect_frac, max_cells);
+            kc.threads = bounds[k] <= 64 ? 64 : (bounds[k] <= 256 ? 128 : 256);
+            kc.smem = make_layout(kc.caps).total;
+            if ((int)kc.smem > smem_optin)
+                return fail(R2D_ERR_CAPACITY, "world class of " + std::to_string(bounds[k]) + " bodies needs " +
+                                                  std::to_string(kc.smem) + " B of shared memory");
+            // largest worlds first: the longest tasks start earliest
+            std::stable_sort(groups[k].begin(), groups[k].end(),
+                             [&](uint32_t a, uint32_t b) { return worlds_h[a].n > worlds_h[b].n; });
+            kc.worlds = groups[k];
+            CUDA_TRY(dalloc(kc.d_list, kc.worlds.size()));
+            CUDA_TRY(cudaMemcpyAsync(kc.d_list, kc.worlds.data(), 4 * kc.worlds.size(), cudaMemcpyHostToDevice, stream));
+            classes.push_back(std::move(kc));
+        }
+        CUDA_TRY(dalloc(d_worlds, nworlds));
+        CUDA_TRY(cudaMemcpyAsync(d_worlds, worlds_h.data(), sizeof(WorldDesc) * nworlds, cudaMemcpyHostToDevice, stream));
+        // debug taps
+        dbg = DebugOut{};
+        if (cfg.flags & R2D_FLAG_DEBUG_TAPS) {
+            uint32_t cap = 0, jcap = 0;
+            for (auto& c : classes) {
+                cap = std::max(cap, c.caps.nm);
+                jcap = std::max(jcap, c.caps.nj);
+            }
+            CUDA_TRY(dalloc(d_dbg_nman, nworlds));
+            CUDA_TRY(dalloc(d_dbg_keys, (size_t)nworlds * cap * 2));
+            CUDA_TRY(dalloc(d_dbg_data, (size_t)nworlds * cap * DEBUG_MF));
+            CUDA_TRY(dalloc(d_dbg_col, (size_t)nworlds * cap));
+            CUDA_TRY(dalloc(d_dbg_jcol, (size_t)nworlds * (jcap ? jcap : 1)));
+            CUDA_TRY(cudaMemsetAsync(d_dbg_nman, 0, 4 * nworlds, stream));
+            dbg.cap = cap;
+            dbg.nman = d_dbg_nman;
+            dbg.keys = d_dbg_keys;
+            dbg.data = d_dbg_data;
+            dbg.colour = d_dbg_col;
+            dbg.jcolour = d_dbg_jcol;
+            dbg.jcap = jcap;
+        }
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        plan_dirty = false;
+        return R2D_OK;
+    }
+
+    int process(float dt, uint32_t sub_steps, uint32_t iters) {
+        if (sub_steps == 0) return fail(R2D_ERR_INVALID_ARGUMENT, "sub_steps must be >= 1");
+        if (!d_state) return fail(R2D_ERR_INVALID_ARGUMENT, "no bodies");
+        if (plan_dirty) {
+            int st = plan();
+            if (st) return st;
+        }
+        if (!pending) CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), stream));
+        StepParams P{};
+        P.worlds = d_worlds;
+        P.state = d_state;
+        P.props = d_props;
+        P.kind = d_kind;
+        P.ids = d_ids;
+        P.nbodies = nbodies;
+        P.jtype = d_jtype;
+        P.jb1 = d_jb1;
+        P.jb2 = d_jb2;
+        P.jprm = d_jprm;
+        P.excl = d_excl;
+        P.world_status = d_status;
+        P.error_count = d_err;
+        P.dt = dt;
+        P.sub_steps = sub_steps;
+        P.iters = iters;
+        P.cell = cell;
+        P.table_mult = table_mult;
+        P.dbg = dbg;
+        for (auto& c : classes) {
+            P.world_list = c.d_list;
+            P.nlist = (uint32_t)c.worlds.size();
+            cudaError_t e = launch_world_step(P, c.caps, c.threads, stream);
+            if (e != cudaSuccess) return fail(R2D_ERR_CUDA, std::string("world step launch: ") + cudaGetErrorString(e));
+        }
+        pending = true;
+        return R2D_OK;
+    }
+
+    int sync() {
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        if (!pending) return R2D_OK;
+        pending = false;
+        CUDA_TRY(cudaMemcpy(h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost));
+        if (*h_err == 0) return R2D_OK;
+        status_h.resize(nworlds);
+        CUDA_TRY(cudaMemcpy(status_h.data(), d_status, sizeof(int) * nworlds, cudaMemcpyDeviceToHost));
+        for (uint32_t w = 0; w < nworlds; ++w)
+            if (status_h[w] != 0)
+                return fail(status_h[w], "world " + std::to_string(w) + " failed with status " +
+                                             std::to_string(status_h[w]));
+        return fail(R2D_ERR_CUDA, "device reported an error without a world status");
+    }
+
+    int world_status(int* out) {
+        int st = sync();
+        (void)st;
+        status_h.assign(nworlds, 0);
+        if (nworlds) CUDA_TRY(cudaMemcpy(status_h.data(), d_status, sizeof(int) * nworlds, cudaMemcpyDeviceToHost));
+        std::copy(status_h.begin(), status_h.end(), out);
+        return R2D_OK;
+    }
+
+    int num_manifolds(uint32_t w, uint32_t* out) {
+        if (!dbg.cap) return fail(R2D_ERR_INVALID_ARGUMENT, "debug taps are off (R2D_FLAG_DEBUG_TAPS)");
+        if (w >= nworlds) return fail(R2D_ERR_INVALID_ARGUMENT, "world index out of range");
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        CUDA_TRY(cudaMemcpy(out, d_dbg_nman + w, 4, cudaMemcpyDeviceToHost));
+        return R2D_OK;
+    }
+
+    int get_manifolds(uint32_t w, uint32_t cap, uint32_t* keys, float* data, uint32_t* colours) {
+        uint32_t m = 0;
+        int st = num_manifolds(w, &m);
+        if (st) return st;
+        m = std::min(m, std::min(cap, dbg.cap));
+        const size_t o = (size_t)w * dbg.cap;
+        if (keys) CUDA_TRY(cudaMemcpy(keys, d_dbg_keys + 2 * o, 8 * (size_t)m, cudaMemcpyDeviceToHost));
+        if (data) CUDA_TRY(cudaMemcpy(data, d_dbg_data + o * DEBUG_MF, 4 * (size_t)m * DEBUG_MF, cudaMemcpyDeviceToHost));
+        if (colours) CUDA_TRY(cudaMemcpy(colours, d_dbg_col + o, 4 * (size_t)m, cudaMemcpyDeviceToHost));
+        return R2D_OK;
+    }
+
+    int get_joint_colours(uint32_t w, uint32_t cap, uint32_t* colours) {
+        if (!dbg.cap) return fail(R2D_ERR_INVALID_ARGUMENT, "debug taps are off (R2D_FLAG_DEBUG_TAPS)");
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        const uint32_t m = std::min(std::min(cap, dbg.jcap), worlds_h[w].nj);
+        if (m) CUDA_TRY(cudaMemcpy(colours, d_dbg_jcol + (size_t)w * dbg.jcap, 4 * (size_t)m, cudaMemcpyDeviceToHost));
+        return R2D_OK;
+    }
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// single world
+// ---------------------------------------------------------------------------
+struct r2d_solver {
+    Engine eng;
+    std::vector<float> gravity;
+    std::vector<uint8_t> jtype;
+    std::vector<uint32_t> jid1, jid2;
+    std::vector<float> jprm;
+    std::vector<uint32_t> xpairs;
+    bool constraints_dirty = false;
+};
+
+struct r2d_batch {
+    Engine eng;
+};
+
+extern "C" {
+
+R2D_API int r2d_version(void) { return 1; }
+
+R2D_API const char* r2d_last_error_string(void) { return g_last_error.c_str(); }
+
+R2D_API int r2d_solver_create(const r2d_config* cfg, r2d_solver** out) {
+    if (!out) return fail(R2D_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    r2d_solver* s = new (std::nothrow) r2d_solver();
+    if (!s) return fail(R2D_ERR_OUT_OF_MEMORY, "host allocation");
+    int st = s->eng.init(cfg);
+    if (st) {
+        delete s;
+        return st;
+    }
+    *out = s;
+    return R2D_OK;
+}
+
+R2D_API int r2d_solver_destroy(r2d_solver* s) {
+    if (!s) return fail(R2D_ERR_INVALID_ARGUMENT, "solver is NULL");
+    cudaStreamSynchronize(s->eng.stream);
+    delete s;
+    return R2D_OK;
+}
+
+R2D_API int r2d_solver_set_bodies(r2d_solver* s, uint32_t n, const uint32_t* ids, const uint8_t* kind,
+                                  const float* props, const float* state, int init_aabb) {
+    if (!s || (n && (!ids || !kind || !props || !state))) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (n > 65535u) return fail(R2D_ERR_CAPACITY, "a world holds at most 65535 bodies");
+    const uint32_t off[2] = {0, n};
+    const float* g = s->gravity.empty() ? nullptr : s->gravity.data();
+    int st = s->eng.set_bodies(1, off, ids, kind, props, state, g, (uint32_t)s->gravity.size(), init_aabb);
+    if (st) return st;
+    s->constraints_dirty = true;
+    return R2D_OK;
+}
+
+R2D_API int r2d_solver_write_state(r2d_solver* s, const float* state) {
+    if (!s || !state) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
+    return s->eng.write_state(state);
+}
+
+R2D_API int r2d_solver_read_state(r2d_solver* s, float* state) {
+    if (!s || !state) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
+    return s->eng.read_state(state);
+}
+
+R2D_API int r2d_solver_set_gravity(r2d_solver* s, uint32_t n, const float* g) {
+    if (!s || (n && !g)) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (n > (uint32_t)MAX_GRAVITY) return fail(R2D_ERR_INVALID_ARGUMENT, "at most 4 gravity generators");
+    s->gravity.assign(g, g + n);
+    if (!s->eng.worlds_h.empty()) {
+        WorldDesc& d = s->eng.worlds_h[0];
+        d.ngrav = n;
+        for (uint32_t k = 0; k < n; ++k) d.g[k] = g[k];
+        s->eng.plan_dirty = true;
+    }
+    return R2D_OK;
+}
+
+R2D_API int r2d_solver_set_joints(r2d_solver* s, uint32_t n, const uint8_t* type, const uint32_t* id1,
+                                  const uint32_t* id2, const float* params) {
+    if (!s || (n && (!type || !id1 || !id2 || !params))) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
+    for (uint32_t j = 0; j < n; ++j)
+        if (type[j] > J_MOTOR) return fail(R2D_ERR_INVALID_ARGUMENT, "unknown joint type");
+    s->jtype.assign(type, type + n);
+    s->jid1.assign(id1, id1 + n);
+    s->jid2.assign(id2, id2 + n);
+    s->jprm.assign(params, params + (size_t)n * JOINT_PARAMS);
+    s->constraints_dirty = true;
+    return R2D_OK;
+}
+
+R2D_API int r2d_solver_set_exclusions(r2d_solver* s, uint32_t n, const uint32_t* pairs) {
+    if (!s || (n && !pairs)) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
+    s->xpairs.assign(pairs, pairs + 2 * (size_t)n);
+    s->constraints_dirty = true;
+    return R2D_OK;
+}
+
+static int solver_resolve(r2d_solver* s) {
+    Engine& e = s->eng;
+    std::unordered_map<uint32_t, uint32_t> idx;
+    idx.reserve(e.nbodies * 2 + 1);
+    for (uint32_t i = 0; i < e.nbodies; ++i) idx[e.ids_h[i]] = i;
+    const uint32_t nj = (uint32_t)s->jtype.size();
+    std::vector<uint32_t> jw(nj, 0);
+    std::vector<uint16_t> b1(nj), b2(nj);
+    for (uint32_t j = 0; j < nj; ++j) {
+        auto a = idx.find(s->jid1[j]);
+        if (a == idx.end()) return fail(R2D_ERR_INVALID_BODY_ID, "joint " + std::to_string(j) + " names an unknown body id");
+        b1[j] = (uint16_t)a->second;
+        b2[j] = b1[j];
+        if (s->jtype[j] == J_DISTANCE || s->jtype[j] == J_OFFSET) {
+            auto b = idx.find(s->jid2[j]);
+            if (b == idx.end())
+                return fail(R2D_ERR_INVALID_BODY_ID, "joint " + std::to_string(j) + " names an unknown body id");
+            b2[j] = (uint16_t)b->second;
+        }
+    }
+    const uint32_t nx = (uint32_t)(s->xpairs.size() / 2);
+    std::vector<uint32_t> xw, xk;
+    for (uint32_t k = 0; k < nx; ++k) {
+        auto a = idx.find(s->xpairs[2 * k]), b = idx.find(s->xpairs[2 * k + 1]);
+        if (a == idx.end() || b == idx.end()) continue;  // an exclusion of a missing body excludes nothing
+        const uint32_t lo = std::min(a->second, b->second), hi = std::max(a->second, b->second);
+        if (lo == hi) continue;
+        xw.push_back(0);
+        xk.push_back((lo << 16) | hi);
+    }
+    return e.set_constraints(jw, s->jtype, b1, b2, s->jprm, xw, xk);
+}
+
+R2D_API int r2d_solver_process(r2d_solver* s, float dt, uint32_t sub_steps, uint32_t collision_iters) {
+    if (!s) return fail(R2D_ERR_INVALID_ARGUMENT, "solver is NULL");
+    if (s->eng.nworlds == 0) return R2D_OK;  // no bodies: nothing to step
+    if (s->constraints_dirty) {
+        int st = solver_resolve(s);
+        if (st) return st;
+        s->constraints_dirty = false;
+    }
+    return s->eng.process(dt, sub_steps, collision_iters);
+}
+
+R2D_API int r2d_solver_sync(r2d_solver* s) {
+    if (!s) return fail(R2D_ERR_INVALID_ARGUMENT, "solver is NULL");
+    return s->eng.sync();
+}
+
+R2D_API int r2d_solver_num_manifolds(r2d_solver* s, uint32_t* out) {
+    if (!s || !out) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
+    return s->eng.num_manifolds(0, out);
+}
+
+R2D_API int r2d_solver_get_manifolds(r2d_solver* s, uint32_t cap, uint32_t* keys, float* data, uint32_t* colours) {
+    if (!s) return fail(R2D_ERR_INVALID_ARGUMENT, "solver is NULL");
+    return s->eng.get_manifolds(0, cap, keys, data, colours);
+}
+
+R2D_API int r2d_solver_get_joint_colours(r2d_solver* s, uint32_t cap, uint32_t* colours) {
+    if (!s || !colours) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
+    return s->eng.get_joint_colours(0, cap, colours);
+}
+
+// ---------------------------------------------------------------------------
+// batch
+// ---------------------------------------------------------------------------
+R2D_API int r2d_batch_create(const r2d_config* cfg, r2d_batch** out) {
+    if (!out) return fail(R2D_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    r2d_batch* b = new (std::nothrow) r2d_batch();
+    if (!b) return fail(R2D_ERR_OUT_OF_MEMORY, "host allocation");
+    int st = b->eng.init(cfg);
+    if (st) {
+        delete b;
+        return st;
+    }
+    *out = b;
+    return R2D_OK;
+}
+
+R2D_API int r2d_batch_destroy(r2d_batch* b) {
+    if (!b) return fail(R2D_ERR_INVALID_ARGUMENT, "batch is NULL");
+    cudaStreamSynchronize(b->eng.stream);
+    delete b;
+    return R2D_OK;
+}
+
+R2D_API int r2d_batch_set_worlds(r2d_batch* b, uint32_t nworlds, const uint32_t* body_off, const uint32_t* ids,
+                                 const uint8_t* kind, const float* props, const float* state, const float* gravity,
+                                 int init_aabb) {
+    if (!b || !body_off || (nworlds && (!gravity))) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
+    const uint32_t n = body_off[nworlds];
+    if (n && (!ids || !kind || !props || !state)) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
+    int st = b->eng.set_bodies(nworlds, body_off, ids, kind, props, state, gravity, 1, init_aabb);
+    if (st) return st;
+    for (auto& d : b->eng.worlds_h) {  // gravity 0 means no generator
+        if (d.g[0] == 0.f) d.ngrav = 0;
+    }
+    std::vector<uint32_t> e32;
+    std::vector<uint8_t> e8;
+    std::vector<uint16_t> e16;
+    std::vector<float> ef;
+    return b->eng.set_constraints(e32, e8, e16, e16, ef, e32, e32);
+}
+
+R2D_API int r2d_batch_write_state(r2d_batch* b, const float* state) {
+    if (!b || !state) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
+    return b->eng.write_state(state);
+}
+
+R2D_API int r2d_batch_read_state(r2d_batch* b, float* state) {
+    if (!b || !state) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
+    return b->eng.read_state(state);
+}
+
+R2D_API int r2d_batch_process(r2d_batch* b, float dt, uint32_t sub_steps, uint32_t collision_iters) {
+    if (!b) return fail(R2D_ERR_INVALID_ARGUMENT, "batch is NULL");
+    if (b->eng.nworlds == 0) return R2D_OK;
+    return b->eng.process(dt, sub_steps, collision_iters);
+}
+
+R2D_API int r2d_batch_sync(r2d_batch* b) {
+    if (!b) return fail(R2D_ERR_INVALID_ARGUMENT, "batch is NULL");
+    return b->eng.sync();
+}
+
+R2D_API int r2d_batch_launches_per_step(r2d_batch* b, uint32_t* out) {
+    if (!b || !out) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (b->eng.plan_dirty && b->eng.nworlds) {
+        int st = b->eng.plan();
+        if (st) return st;
+    }
+    *out = (uint32_t)b->eng.classes.size();
+    return R2D_OK;
+}
+
+R2D_API int r2d_batch_world_status(r2d_batch* b, int* status) {
+    if (!b || !status) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
+    return b->eng.world_status(status);
+}
+
+R2D_API int r2d_batch_num_manifolds(r2d_batch* b, uint32_t w, uint32_t* out) {
+    if (!b || !out) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
+    return b->eng.num_manifolds(w, out);
+}
+
+R2D_API int r2d_batch_get_manifolds(r2d_batch* b, uint32_t w, uint32_t cap, uint32_t* keys, float* data,
+                                    uint32_t* colours) {
+    if (!b) return fail(R2D_ERR_INVALID_ARGUMENT, "batch is NULL");
+    return b->eng.get_manifolds(w, cap, keys, data, colours);
+}
+
+}  // extern "C"

@@ -1,0 +1,333 @@
+/*
+ * r2d_device.cuh -- per-constraint and per-shape device arithmetic of the
+ * resolve2d step, written for structure-of-arrays state.
+ *
+ * Every function reproduces one reference function's f32 arithmetic in the
+ * reference's evaluation order (paths relative to the reference project):
+ * the build compiles with --fmad=false and IEEE division / square root, so
+ * the results are the bits the reference's own formulas give.  Rotation
+ * values come from r2d_sincos.h; a body's sin/cos is computed once per
+ * angle and reused, which gives the same bits as the reference calling
+ * std.math.sin/cos at every rotate2 (src/core/nmath.zig:129-136).
+ */
+#pragma once
+
+#include <stdint.h>
+
+#include "r2d_colour.h"
+#include "r2d_sincos.h"
+
+namespace r2d {
+
+// ---- constants (src/core/simulation_constants.zig:3-22) ----
+constexpr float MIN_MANIFOLD_IMPULSE = 1e-4f;
+constexpr float BAUMGARTE = 0.02f;
+constexpr float BAUMGARTE_SLOP = 0.005f;
+constexpr float SAT_OVERLAP_THRESHOLD = 1e-4f;
+constexpr float COLLISION_MARGIN = 0.01f;
+constexpr float NMATH_WARN_DIVIDING_BELOW = 1e-3f;
+constexpr float AABB_EPS_OVERLAP = 0.01f;
+constexpr float CONSTRAINT_GRADIENT_DIVISION_LIMIT = 1e-4f;
+constexpr float ALLOWED_CONSTRAINT_VALUE = 1e-6f;
+
+#define R2D_DF __device__ __forceinline__
+
+struct f2 {
+    float x, y;
+};
+
+// ---- nmath (src/core/nmath.zig) ----
+R2D_DF f2 add2(f2 a, f2 b) { return {a.x + b.x, a.y + b.y}; }
+R2D_DF f2 sub2(f2 a, f2 b) { return {a.x - b.x, a.y - b.y}; }
+R2D_DF f2 scale2(f2 a, float s) { return {a.x * s, a.y * s}; }
+R2D_DF float dot2(f2 a, f2 b) { return a.x * b.x + a.y * b.y; }
+R2D_DF float cross2(f2 a, f2 b) { return a.x * b.y - a.y * b.x; }
+R2D_DF float length2(f2 a) { return sqrtf(dot2(a, a)); }
+R2D_DF f2 normalize2(f2 a) {  // nmath.zig:95-103
+    float len = length2(a);
+    if (len < NMATH_WARN_DIVIDING_BELOW) return {0.f, 0.f};
+    return scale2(a, 1.0f / len);
+}
+R2D_DF f2 negate2(f2 a) { return {-a.x, -a.y}; }
+R2D_DF f2 neg_by_mul(f2 a) { return {a.x * -1.0f, a.y * -1.0f}; }  // Vector2.negate (:48-51)
+R2D_DF f2 addmult2(f2 a, f2 b, float s) { return add2(a, scale2(b, s)); }
+R2D_DF bool approx_eql(float a, float b, float eps) { return a > b - eps && a < b + eps; }
+R2D_DF bool approx_eql2(f2 a, f2 b, float eps) {
+    return approx_eql(a.x, b.x, eps) && approx_eql(a.y, b.y, eps);
+}
+R2D_DF f2 rot(f2 a, float c, float s) { return {a.x * c - a.y * s, a.x * s + a.y * c}; }
+R2D_DF f2 cw90(f2 a) { return {a.y, -a.x}; }
+R2D_DF f2 ccw90(f2 a) { return {-a.y, a.x}; }
+
+// Zig @max / @min on floats: the non-NaN operand wins.
+R2D_DF float zmax(float a, float b) {
+    if (a != a) return b;
+    if (b != b) return a;
+    return a > b ? a : b;
+}
+R2D_DF float zmin(float a, float b) {
+    if (a != a) return b;
+    if (b != b) return a;
+    return a < b ? a : b;
+}
+R2D_DF float zclamp(float v, float lo, float hi) { return zmax(lo, zmin(v, hi)); }
+
+// ---- spatial hash (src/core/SpatialHash.zig:78-81) ----
+R2D_DF uint32_t cell_bucket(int64_t xi, int64_t yi, uint32_t table_size) {
+    uint64_t h = ((uint64_t)xi * 92837111ull) ^ ((uint64_t)yi * 689287499ull);
+    return (uint32_t)(h % (uint64_t)table_size);
+}
+
+// floor(c / cell) as the reference's @intFromFloat(@floor(..)) (SpatialHash.zig:93-96);
+// false when the value is not a representable cell index.
+R2D_DF bool cell_index(float c, float cell, int32_t* out) {
+    float v = floorf(c / cell);
+    if (!(v > -2.0e9f && v < 2.0e9f)) return false;
+    *out = (int32_t)v;
+    return true;
+}
+
+// ---- AABB (src/core/aabb.zig:12-19; Disc.zig:63-66; Rectangle.zig:71-86) ----
+R2D_DF bool aabb_intersects(f2 p1, float hw1, float hh1, f2 p2, float hw2, float hh2) {
+    float dx = fabsf(p2.x - p1.x);
+    float dy = fabsf(p2.y - p1.y);
+    return (dx <= (hw1 + hw2) + AABB_EPS_OVERLAP) && (dy <= (hh1 + hh2) + AABB_EPS_OVERLAP);
+}
+
+// Local rectangle vertices (Rectangle.zig:38-40): (-w,-h), (-w,h), (w,h), (w,-h).
+R2D_DF f2 rect_local(int i, float w, float h) {
+    return {(i < 2) ? -w : w, (i == 0 || i == 3) ? -h : h};
+}
+
+R2D_DF void rect_half_extents(float width, float height, float c, float s, float* hw, float* hh) {
+    const float w = width / 2.0f, h = height / 2.0f;
+    float ew = 0.f, eh = 0.f;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        f2 r = rot(rect_local(i, w, h), c, s);
+        if (r.x > ew) ew = r.x;
+        if (r.y > eh) eh = r.y;
+    }
+    *hw = ew;
+    *hh = eh;
+}
+
+// ---- narrowphase geometry ----
+// One body as the SAT sees it.  For a rectangle the world vertices
+// (Rectangle.zig:88-98) and edge normals (Rectangle.zig:132-151) are
+// computed once; the reference recomputes the same values at every use.
+struct Geo {
+    f2 pos;
+    float radius;  // disc
+    bool rect;
+    f2 wv[4];      // rectangle world vertices
+    f2 en[4];      // rectangle edge normals (ccw90 of the normalised edge)
+};
+
+R2D_DF void geo_make(Geo& g, f2 pos, bool rect, float d0, float d1, float c, float s) {
+    g.pos = pos;
+    g.rect = rect;
+    g.radius = d0;
+    if (!rect) return;
+    const float w = d0 / 2.0f, h = d1 / 2.0f;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) g.wv[i] = add2(rot(rect_local(i, w, h), c, s), pos);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) g.en[i] = ccw90(normalize2(sub2(g.wv[(i + 1) & 3], g.wv[i])));
+}
+
+// closestPoint (Disc.zig:80-84; Rectangle.zig:114-130 -- the nearest vertex)
+R2D_DF f2 closest_point(const Geo& g, f2 p) {
+    if (!g.rect) {
+        f2 n = normalize2(sub2(p, g.pos));
+        return addmult2(g.pos, n, g.radius);
+    }
+    float best = __int_as_float(0x7f800000);
+    f2 bp = p;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        f2 d = sub2(g.wv[i], p);
+        float d2 = dot2(d, d);
+        if (d2 < best) {
+            best = d2;
+            bp = g.wv[i];
+        }
+    }
+    return bp;
+}
+
+// projectAlongAxis (Disc.zig:92-97; Rectangle.zig:153-169)
+R2D_DF void project(const Geo& g, f2 n, float* lo, float* hi) {
+    if (!g.rect) {
+        float mid = dot2(g.pos, n);
+        *lo = mid - g.radius;
+        *hi = mid + g.radius;
+        return;
+    }
+    float l = __int_as_float(0x7f800000), h = __int_as_float(0xff800000);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        float d = dot2(g.wv[i], n);
+        if (d < l) l = d;
+        if (d > h) h = d;
+    }
+    *lo = l;
+    *hi = h;
+}
+
+struct SatState {
+    f2 normal;
+    float penetration;
+    uint32_t refid;
+    bool ref_is_first;  // key.ref_body == the body passed first to performNarrowSAT's o1
+};
+
+// overlapSAT (collision.zig:228-289) with `reference` = R, `incident` = I.
+R2D_DF bool overlap_sat(SatState& ret, const Geo& R, const Geo& I, bool r_is_o1) {
+    const float EPS = SAT_OVERLAP_THRESHOLD;
+    const int nn = R.rect ? 4 : 1;
+    f2 disc_axis = {0.f, 0.f};
+    if (!R.rect) disc_axis = normalize2(sub2(closest_point(I, R.pos), R.pos));  // Disc.zig:86-90
+    for (int it = 0; it < nn; ++it) {
+        f2 normal = R.rect ? R.en[it] : disc_axis;
+        bool flipped = false;
+        if (dot2(normal, sub2(I.pos, R.pos)) < 0.0f) {  // normalShouldFlipSAT (:221-226)
+            normal = neg_by_mul(normal);
+            flipped = true;
+        }
+        float p1lo, p1hi, p2lo, p2hi;
+        project(R, normal, &p1lo, &p1hi);
+        project(I, normal, &p2lo, &p2hi);
+        float d1 = p1hi - p2lo;
+        float d2 = p2hi - p1lo;
+        float d = zmin(d1, d2);
+        if (d <= -COLLISION_MARGIN) return false;
+        if (!flipped && approx_eql2(normal, ret.normal, EPS)) {
+            float tref = dot2(R.pos, normal);
+            float tinc = dot2(I.pos, normal);
+            if (tref < tinc - EPS) {
+                ret.penetration = d;
+                ret.normal = normal;
+                ret.refid = it;
+                ret.ref_is_first = r_is_o1;
+            }
+        }
+        if (!flipped && approx_eql2(normal, negate2(ret.normal), EPS)) {
+            f2 diff = sub2(I.pos, R.pos);
+            if (dot2(diff, normal) > dot2(diff, ret.normal) + EPS) {
+                ret.penetration = d;
+                ret.normal = normal;
+                ret.refid = it;
+                ret.ref_is_first = r_is_o1;
+            }
+        }
+        if (d + EPS < ret.penetration) {
+            ret.penetration = d;
+            ret.normal = normal;
+            ret.refid = it;
+            ret.ref_is_first = r_is_o1;
+        }
+    }
+    return true;
+}
+
+// performNarrowSAT (collision.zig:299-320): o1 = lower id.  The reference
+// leaves ret.normal/key undefined until the first axis writes them; the
+// start value here is normal (0,0), reference = o1, edge 0.
+R2D_DF bool perform_narrow_sat(const Geo& o1, const Geo& o2, SatState& ret) {
+    ret.normal = {0.f, 0.f};
+    ret.penetration = __int_as_float(0x7f800000);
+    ret.refid = 0;
+    ret.ref_is_first = true;
+    if (!overlap_sat(ret, o1, o2, true)) return false;
+    if (!overlap_sat(ret, o2, o1, false)) return false;
+    return true;
+}
+
+struct NewPoint {
+    f2 ref_r, inc_r;
+    float depth;
+};
+
+// CollisionPoint.init (collision.zig:38-51)
+R2D_DF NewPoint make_point(f2 pos, float depth, f2 ref_pos, f2 inc_pos, f2 normal) {
+    f2 middle = sub2(pos, scale2(normal, depth / 2.0f));
+    NewPoint p;
+    p.ref_r = sub2(middle, ref_pos);
+    p.inc_r = sub2(middle, inc_pos);
+    p.depth = depth;
+    return p;
+}
+
+// clipLineToLine (collision.zig:330-363): b clipped onto a.
+R2D_DF void clip_line_to_line(f2 aa, f2 ab, f2 ba, f2 bb, f2* p1o, f2* p2o) {
+    f2 delta_a = sub2(ab, aa);
+    float a_len = length2(delta_a);
+    f2 tang = scale2(delta_a, 1.0f / a_len);
+    f2 p1 = ba, p2 = bb;
+    {
+        float scalar = dot2(sub2(ba, aa), tang);
+        if (!(scalar > 0.0f && scalar < a_len)) {
+            f2 clos = scalar < 0.5f * a_len ? aa : ab;
+            f2 delta_p = sub2(ba, bb);
+            float t = -dot2(tang, sub2(bb, clos)) / dot2(tang, delta_p);
+            p1 = addmult2(bb, delta_p, t);
+        }
+    }
+    {
+        float scalar = dot2(sub2(bb, aa), tang);
+        if (!(scalar > 0.0f && scalar < a_len)) {
+            f2 clos = scalar < 0.5f * a_len ? aa : ab;
+            f2 delta_p = sub2(bb, ba);
+            float t = -dot2(tang, sub2(ba, clos)) / dot2(tang, delta_p);
+            p2 = addmult2(ba, delta_p, t);
+        }
+    }
+    *p1o = p1;
+    *p2o = p2;
+}
+
+// identifyCollisionPoints (Disc.zig:99-123; Rectangle.zig:171-211 with
+// clipAgainstEdge Disc.zig:125-130 / Rectangle.zig:213-238).  Returns the
+// number of points written (0..2).
+R2D_DF int identify_points(const Geo& ref, const Geo& inc, uint32_t refid, NewPoint out[2]) {
+    if (!ref.rect) {
+        f2 pos = closest_point(inc, ref.pos);
+        f2 normal = normalize2(sub2(closest_point(inc, ref.pos), ref.pos));
+        if (dot2(normal, sub2(inc.pos, ref.pos)) < 0.0f) normal = neg_by_mul(normal);
+        float dot = dot2(normal, sub2(pos, ref.pos));
+        float depth = dot - ref.radius;
+        out[0] = make_point(pos, depth, ref.pos, inc.pos, normal);
+        return 1;
+    }
+    const f2 ea = ref.wv[refid];
+    const f2 eb = ref.wv[(refid + 1) & 3];
+    const f2 ndir = ref.en[refid];
+    if (!inc.rect) {
+        f2 pos = addmult2(inc.pos, ndir, -inc.radius);
+        float dot = dot2(sub2(pos, ea), ndir);
+        out[0] = make_point(pos, dot, ref.pos, inc.pos, ndir);
+        return 1;
+    }
+    int best = -1;
+    float best_dot = __int_as_float(0x7f800000);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        float d = dot2(ndir, inc.en[i]);
+        if (d < best_dot) {
+            best_dot = d;
+            best = i;
+        }
+    }
+    if (best < 0) best = 0;  // every dot NaN: the reference reads an undefined edge
+    f2 pa, pb;
+    clip_line_to_line(ea, eb, inc.wv[best], inc.wv[(best + 1) & 3], &pa, &pb);
+    int n = 0;
+    float dot = dot2(sub2(pa, ea), ndir);
+    if (dot < COLLISION_MARGIN) out[n++] = make_point(pa, dot, ref.pos, inc.pos, ndir);
+    dot = dot2(sub2(pb, eb), ndir);
+    if (dot < COLLISION_MARGIN) out[n++] = make_point(pb, dot, ref.pos, inc.pos, ndir);
+    return n;
+}
+
+}  // namespace r2d

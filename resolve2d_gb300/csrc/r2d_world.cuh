@@ -1,0 +1,160 @@
+/*
+ * r2d_world.cuh -- data layout shared by the host runtime and the fused
+ * per-world step kernel.
+ */
+#pragma once
+
+#include <stdint.h>
+
+namespace r2d {
+
+// Field-major f32 state: field f of body g lives at state[f * nbodies + g].
+enum StateField : int {
+    S_POS_X = 0, S_POS_Y, S_ANGLE, S_MOM_X, S_MOM_Y, S_ANG_MOM,
+    S_FORCE_X, S_FORCE_Y, S_TORQUE, S_AABB_X, S_AABB_Y, S_AABB_HW, S_AABB_HH,
+    S_NFIELDS
+};
+enum PropField : int { P_MASS = 0, P_INERTIA, P_MU, P_DIM0, P_DIM1, P_NFIELDS };
+enum KindBits : uint8_t { K_RECT = 1, K_STATIC = 2, K_FORCED = 0x80 /* device-only: force/torque to clear */ };
+enum JointTypes : uint8_t { J_DISTANCE = 0, J_OFFSET = 1, J_FIXED = 2, J_MOTOR = 3 };
+enum WorldFlags : uint32_t { W_DISC_ROTATION = 2u };
+
+constexpr int MAX_GRAVITY = 4;
+constexpr int JOINT_PARAMS = 8;
+constexpr int DEBUG_MF = 33;     // floats per manifold in the debug dump (oracle layout)
+constexpr int MAX_COLOURS = 254; // colour 255 marks "not coloured yet"
+
+struct WorldDesc {
+    uint32_t body_off, n;
+    uint32_t joint_off, nj;
+    uint32_t excl_off, nexcl;
+    uint32_t ngrav, flags;
+    float g[MAX_GRAVITY];
+};
+
+// Per-world capacities of one kernel class; every buffer below is sized
+// from them, and a world that outgrows one is reported, never overrun.
+struct Caps {
+    uint32_t nb;   // bodies
+    uint32_t nm;   // manifolds
+    uint32_t npt;  // contact points
+    uint32_t ne;   // (cell, body) entries of the spatial hash
+    uint32_t np;   // candidate pairs that passed the AABB test
+    uint32_t hs;   // pair hash-set slots (power of two)
+    uint32_t nj;   // joints
+    uint32_t nt;   // spatial-hash buckets (table_mult * bodies)
+};
+
+// Byte offsets into the dynamic shared memory of one CTA.
+struct Layout {
+    // bodies (whole step)
+    uint32_t px, py, ang, mx, my, L, mass, inertia, inv_m, inv_i, cs, sn, ang_prev, tq, kind;
+    // manifolds + points (narrowphase .. end) -- aliased by the broadphase scratch
+    uint32_t ma, mb, mp0, mnp, mcol, nx, ny, fric;
+    uint32_t r1x, r1y, r2x, r2y, depth, odepth, mn, mt, apn, apt;
+    // broadphase scratch (inside the manifold region)
+    uint32_t ax, ay, ahw, ahh, rx0, ry0, rx1, ry1, bcnt, ebucket, ebody, eslot, sbody, table, hset;
+    // colouring scratch
+    uint32_t adj, adjl, prio;
+    // orders
+    uint32_t corder, coff, jorder, joff, jcol;
+    // pairs
+    uint32_t pairs;
+    uint32_t total;
+};
+
+__host__ __device__ inline uint32_t r2d_align(uint32_t x, uint32_t a) { return (x + a - 1) / a * a; }
+
+__host__ __device__ inline Layout make_layout(const Caps& c) {
+    Layout L{};
+    uint32_t o = 0;
+    auto take = [&](uint32_t bytes) {
+        uint32_t at = o;
+        o = r2d_align(o + bytes, 16);
+        return at;
+    };
+    const uint32_t nb4 = 4 * c.nb;
+    L.px = take(nb4); L.py = take(nb4); L.ang = take(nb4);
+    L.mx = take(nb4); L.my = take(nb4); L.L = take(nb4);
+    L.mass = take(nb4); L.inertia = take(nb4); L.inv_m = take(nb4); L.inv_i = take(nb4);
+    L.cs = take(nb4); L.sn = take(nb4); L.ang_prev = take(nb4); L.tq = take(nb4);
+    L.kind = take(c.nb);
+
+    // region X: manifolds + points, aliased by the broadphase scratch
+    const uint32_t xbase = o;
+    const uint32_t nm4 = 4 * c.nm, np4 = 4 * c.npt;
+    L.ma = take(2 * c.nm); L.mb = take(2 * c.nm); L.mp0 = take(2 * c.nm);
+    L.mnp = take(c.nm); L.mcol = take(c.nm);
+    L.nx = take(nm4); L.ny = take(nm4); L.fric = take(nm4);
+    L.r1x = take(np4); L.r1y = take(np4); L.r2x = take(np4); L.r2y = take(np4);
+    L.depth = take(np4); L.odepth = take(np4); L.mn = take(np4); L.mt = take(np4);
+    L.apn = take(np4); L.apt = take(np4);
+    const uint32_t xend_m = o;
+    o = xbase;
+    L.ax = take(nb4); L.ay = take(nb4); L.ahw = take(nb4); L.ahh = take(nb4);
+    L.rx0 = take(nb4); L.ry0 = take(nb4); L.rx1 = take(nb4); L.ry1 = take(nb4);
+    L.bcnt = take(4 * (c.nb + 1));
+    L.ebucket = take(4 * c.ne); L.ebody = take(2 * c.ne); L.eslot = take(2 * c.ne);
+    L.sbody = take(2 * c.ne);
+    L.table = take(4 * (c.nt + 2));
+    L.hset = take(4 * c.hs);
+    const uint32_t xend_bp = o;
+    o = xend_m > xend_bp ? xend_m : xend_bp;
+
+    // colouring scratch
+    const uint32_t ncon = c.nm > c.nj ? c.nm : c.nj;
+    L.adj = take(4 * (c.nb + 1));
+    L.adjl = take(2 * 2 * ncon);
+    L.prio = take(8 * ncon);
+    // orders
+    L.corder = take(2 * c.nm);
+    L.coff = take(2 * (MAX_COLOURS + 2));
+    L.jorder = take(2 * (c.nj ? c.nj : 1));
+    L.joff = take(2 * (MAX_COLOURS + 2));
+    L.jcol = take(c.nj ? c.nj : 1);
+    // pairs
+    L.pairs = take(4 * c.np);
+    L.total = o;
+    return L;
+}
+
+struct DebugOut {
+    uint32_t cap;        // manifolds per world slot (0 = no dump)
+    uint32_t* nman;      // [world]
+    uint32_t* keys;      // [world][cap][2]  (reference, incident) world-local indices
+    float* data;         // [world][cap][DEBUG_MF]
+    uint32_t* colour;    // [world][cap]
+    uint32_t* jcolour;   // [world][jcap]
+    uint32_t jcap;
+};
+
+struct StepParams {
+    const WorldDesc* worlds;
+    const uint32_t* world_list;  // worlds handled by this launch
+    uint32_t nlist;
+    float* state;                // [S_NFIELDS][nbodies]
+    const float* props;          // [P_NFIELDS][nbodies]
+    const uint8_t* kind;         // [nbodies]
+    const uint32_t* ids;         // [nbodies]
+    uint32_t nbodies;
+    const uint8_t* jtype;        // [njoints]
+    const uint16_t* jb1;         // world-local body index
+    const uint16_t* jb2;
+    const float* jprm;           // [njoints][JOINT_PARAMS]
+    const uint32_t* excl;        // sorted (lo << 16 | hi) per world
+    int* world_status;           // [nworlds]
+    int* error_count;
+    float dt;
+    uint32_t sub_steps, iters;
+    float cell;
+    uint32_t table_mult;
+    DebugOut dbg;
+};
+
+enum DeviceStatus : int {
+    DS_OK = 0,
+    DS_CAPACITY = -5,
+    DS_NONFINITE = -7,
+};
+
+}  // namespace r2d

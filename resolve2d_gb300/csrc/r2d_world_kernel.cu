@@ -1,0 +1,881 @@
+/*
+ * r2d_world_kernel.cu -- one CTA steps one whole world: the body state is
+ * loaded into shared memory once, and the spatial-hash broadphase
+ * (src/core/SpatialHash.zig), the SAT narrowphase and manifold build
+ * (src/core/collision.zig:221-363, Bodies/*.zig), the constraint colouring,
+ * the substep loop of Solver.process (src/core/lib.zig:189-251: forces,
+ * velocities, prestep, joint + contact impulses, integration) and the state
+ * write-back all run from shared memory.  HBM sees each body's state once in
+ * and once out per step.
+ *
+ * Constraint order.  The reference solves joints then manifolds one at a
+ * time (lib.zig:226-236).  Here each set is coloured into body-disjoint
+ * batches (first-fit greedy in the priority order of r2d_colour.h, computed
+ * by Jones-Plassmann rounds), and one colour is solved per barrier phase.
+ * Inside a colour no two constraints share a non-static body, so the result
+ * equals the reference's per-constraint arithmetic replayed colour by colour.
+ * No floating-point atomics are used anywhere: every run is bit-reproducible.
+ */
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "r2d_device.cuh"
+#include "r2d_world.cuh"
+
+namespace r2d {
+
+template <int NT>
+__device__ uint32_t block_scan_excl(uint32_t* a, uint32_t n, uint32_t* wsum) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int NW = NT / 32;
+    const uint32_t per = (n + NT - 1) / NT;
+    const uint32_t beg = min(n, (uint32_t)tid * per), end = min(n, beg + per);
+    uint32_t s = 0;
+    for (uint32_t i = beg; i < end; ++i) s += a[i];
+    uint32_t x = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t v = lane < NW ? wsum[lane] : 0u;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v += y;
+        }
+        if (lane < NW) wsum[lane] = v;
+    }
+    __syncthreads();
+    uint32_t run = (warp ? wsum[warp - 1] : 0u) + x - s;
+    const uint32_t total = wsum[NW - 1];
+    for (uint32_t i = beg; i < end; ++i) {
+        uint32_t v = a[i];
+        a[i] = run;
+        run += v;
+    }
+    __syncthreads();
+    return total;
+}
+
+__device__ __forceinline__ bool hs_insert(uint32_t* hs, uint32_t mask, uint32_t key, int* err) {
+    uint32_t h = (key * 0x9E3779B1u) ^ (key >> 15);
+    for (uint32_t probe = 0; probe <= mask; ++probe) {
+        uint32_t slot = (h + probe) & mask;
+        uint32_t prev = atomicCAS(&hs[slot], 0xFFFFFFFFu, key);
+        if (prev == 0xFFFFFFFFu) return true;
+        if (prev == key) return false;
+    }
+    *err = DS_CAPACITY;
+    return false;
+}
+
+__device__ __forceinline__ bool excluded(const uint32_t* ex, uint32_t n, uint32_t key) {
+    uint32_t lo = 0, hi = n;
+    while (lo < hi) {
+        uint32_t mid = (lo + hi) >> 1;
+        uint32_t v = __ldg(ex + mid);
+        if (v == key) return true;
+        if (v < key) lo = mid + 1;
+        else hi = mid;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void set_err(int* s_err, int code) { atomicCAS(s_err, 0, code); }
+
+// First colour not marked in the 256-bit set; 255 when all of 0..253 are taken.
+__device__ __forceinline__ uint32_t first_free(const uint32_t bits[8]) {
+#pragma unroll
+    for (int wd = 0; wd < 8; ++wd) {
+        if (bits[wd] != 0xFFFFFFFFu) {
+            uint32_t c = wd * 32 + __ffs(~bits[wd]) - 1;
+            return c < (uint32_t)MAX_COLOURS ? c : 255u;
+        }
+    }
+    return 255u;
+}
+
+// Shared-memory views of one world.
+struct SW {
+    float *px, *py, *ang, *mx, *my, *L, *mass, *inertia, *inv_m, *inv_i, *cs, *sn, *ang_prev, *tq;
+    uint8_t* kind;
+    uint16_t *ma, *mb, *mp0;
+    uint8_t *mnp, *mcol;
+    float *nx, *ny, *fric;
+    float *r1x, *r1y, *r2x, *r2y, *depth, *odepth, *mn, *mt, *apn, *apt;
+};
+
+// CollisionManifold.calculateImpulses (collision.zig:135-218)
+__device__ __forceinline__ void solve_contact(const SW& s, uint32_t m, float h) {
+    const uint32_t a = s.ma[m], b = s.mb[m];
+    const bool sa = s.kind[a] & K_STATIC, sb = s.kind[b] & K_STATIC;
+    const float inv_m1 = s.inv_m[a], inv_m2 = s.inv_m[b];
+    const float inv_i1 = s.inv_i[a], inv_i2 = s.inv_i[b];
+    const f2 vlinear_1 = scale2(f2{s.mx[a], s.my[a]}, inv_m1);
+    const float omega1 = s.L[a] * inv_i1;
+    const f2 vlinear_2 = scale2(f2{s.mx[b], s.my[b]}, inv_m2);
+    const float omega2 = s.L[b] * inv_i2;
+    const f2 n = {s.nx[m], s.ny[m]};
+    const f2 t = cw90(n);
+    const float fr = s.fric[m];
+    f2 alp1 = {0.f, 0.f}, alp2 = {0.f, 0.f};
+    float arp1 = 0.f, arp2 = 0.f;
+    const uint32_t p0 = s.mp0[m], np = s.mnp[m];
+    for (uint32_t k = 0; k < np; ++k) {
+        const uint32_t p = p0 + k;
+        const float d = s.depth[p];
+        if (d >= 0.0f) {
+            s.apn[p] = 0.f;
+            s.apt[p] = 0.f;
+            continue;
+        }
+        const f2 r1 = {s.r1x[p], s.r1y[p]}, r2 = {s.r2x[p], s.r2y[p]};
+        const f2 v1 = add2(vlinear_1, f2{-r1.y * omega1, r1.x * omega1});
+        const f2 v2 = add2(vlinear_2, f2{-r2.y * omega2, r2.x * omega2});
+        const f2 dv = sub2(v1, v2);
+        const float bias = BAUMGARTE * zmax(0.0f, (-d) - BAUMGARTE_SLOP) / h;
+        float num = dot2(dv, n) + bias;
+        const float pn = num * s.mn[p];
+        if (pn < MIN_MANIFOLD_IMPULSE) continue;
+        num = dot2(dv, t);
+        const float pt = num * s.mt[p];
+        const float acc = s.apn[p];
+        const float nacc = zmax(0.0f, acc + pn);
+        const float applied_pn = nacc - acc;
+        s.apn[p] = nacc;
+        const float max_pt = fr * fabsf(nacc);
+        const float acct = s.apt[p];
+        const float nacct = zclamp(acct + pt, -max_pt, max_pt);
+        const float applied_pt = nacct - acct;
+        s.apt[p] = nacct;
+        const f2 dp = add2(scale2(n, applied_pn), scale2(t, applied_pt));
+        if (!sa) {
+            alp1 = sub2(alp1, dp);
+            arp1 -= cross2(r1, dp);
+        }
+        if (!sb) {
+            alp2 = add2(alp2, dp);
+            arp2 += cross2(r2, dp);
+        }
+    }
+    // A static body receives exactly +0 in the reference; its state is left alone.
+    if (!sa) {
+        s.mx[a] += alp1.x;
+        s.my[a] += alp1.y;
+        s.L[a] += arp1;
+    }
+    if (!sb) {
+        s.mx[b] += alp2.x;
+        s.my[b] += alp2.y;
+        s.L[b] += arp2;
+    }
+}
+
+// Constraint solve functions (src/core/Constraints/*.zig).
+__device__ __forceinline__ void solve_joint(const SW& s, uint8_t type, uint32_t i1, uint32_t i2,
+                                            const float* __restrict__ prm, float h) {
+    const float pmax = __ldg(prm + 0), pmin = __ldg(prm + 1), beta = __ldg(prm + 2);
+    if (type == J_DISTANCE) {  // DistanceJoint.zig:40-75
+        const float epsilon = CONSTRAINT_GRADIENT_DIVISION_LIMIT;
+        const float target = __ldg(prm + 3);
+        const bool st1 = s.kind[i1] & K_STATIC, st2 = s.kind[i2] & K_STATIC;
+        const float w1 = st1 ? 0.f : 1.0f / s.mass[i1];
+        const float w2 = st2 ? 0.f : 1.0f / s.mass[i2];
+        const f2 v1 = scale2(f2{s.mx[i1], s.my[i1]}, w1);
+        const f2 v2 = scale2(f2{s.mx[i2], s.my[i2]}, w2);
+        const f2 rel = sub2(v2, v1);
+        const f2 d = sub2(f2{s.px[i2], s.py[i2]}, f2{s.px[i1], s.py[i1]});
+        const f2 normal = normalize2(d);
+        const float dist_error = length2(d) - target;
+        const float pc = beta * dist_error / zmax(target, 0.001f);
+        float J = -(dot2(rel, normal) + pc) / (w1 + w2);
+        const float ndv = dot2(normal, rel);
+        const float den = 1.0f / zmax(fabsf(ndv), epsilon);
+        J = zclamp(J, pmin * den, pmax * den);
+        const f2 dp = scale2(normal, J);
+        s.mx[i1] -= dp.x;
+        s.my[i1] -= dp.y;
+        s.mx[i2] += dp.x;
+        s.my[i2] += dp.y;
+    } else if (type == J_OFFSET) {  // OffsetDistanceJoint.zig:44-105
+        const float epsilon = CONSTRAINT_GRADIENT_DIVISION_LIMIT;
+        const f2 r1 = {__ldg(prm + 3), __ldg(prm + 4)}, r2 = {__ldg(prm + 5), __ldg(prm + 6)};
+        const float target = __ldg(prm + 7);
+        const bool st1 = s.kind[i1] & K_STATIC, st2 = s.kind[i2] & K_STATIC;
+        const f2 rr1 = rot(r1, s.cs[i1], s.sn[i1]);
+        const f2 rr2 = rot(r2, s.cs[i2], s.sn[i2]);
+        const f2 a1 = add2(rr1, f2{s.px[i1], s.py[i1]});
+        const f2 a2 = add2(rr2, f2{s.px[i2], s.py[i2]});
+        const f2 normal = normalize2(sub2(a2, a1));
+        const float inv_m1 = st1 ? 0.f : 1.0f / s.mass[i1];
+        const float inv_m2 = st2 ? 0.f : 1.0f / s.mass[i2];
+        const float inv_i1 = st1 ? 0.f : 1.0f / s.inertia[i1];
+        const float inv_i2 = st2 ? 0.f : 1.0f / s.inertia[i2];
+        const f2 vl1 = scale2(f2{s.mx[i1], s.my[i1]}, inv_m1);
+        const float om1 = s.L[i1] * inv_i1;
+        const f2 vl2 = scale2(f2{s.mx[i2], s.my[i2]}, inv_m2);
+        const float om2 = s.L[i2] * inv_i2;
+        const f2 v1 = add2(vl1, f2{-rr1.y * om1, rr1.x * om1});
+        const f2 v2 = add2(vl2, f2{-rr2.y * om2, rr2.x * om2});
+        const f2 dv = sub2(v2, v1);
+        const float dist_error = length2(sub2(a2, a1)) - target;
+        const float pc = beta * dist_error / zmax(target, epsilon);
+        const float num = dot2(normal, dv) + pc;
+        const float r1xn = cross2(rr1, normal);
+        const float r2xn = cross2(rr2, normal);
+        const float den = inv_m1 + inv_m2 + r1xn * r1xn * inv_i1 + r2xn * r2xn * inv_i2;
+        float J = -num / den;
+        const float ndv = dot2(normal, dv);
+        const float den2 = 1.0f / zmax(fabsf(ndv), epsilon);
+        J = zclamp(J, pmin * den2, pmax * den2);
+        const f2 dp = scale2(normal, J);
+        s.mx[i1] -= dp.x;
+        s.my[i1] -= dp.y;
+        s.L[i1] -= J * r1xn;
+        s.mx[i2] += dp.x;
+        s.my[i2] += dp.y;
+        s.L[i2] += J * r2xn;
+    } else if (type == J_FIXED) {  // FixedPositionJoint.zig:38-72
+        if (s.kind[i1] & K_STATIC) return;
+        const float epsilon = ALLOWED_CONSTRAINT_VALUE;
+        const f2 target = {__ldg(prm + 3), __ldg(prm + 4)};
+        const float w = 1.0f / s.mass[i1];
+        const f2 v = scale2(f2{s.mx[i1], s.my[i1]}, w);
+        const f2 delta = sub2(target, f2{s.px[i1], s.py[i1]});
+        const float dist = length2(delta);
+        if (dist < ALLOWED_CONSTRAINT_VALUE) return;
+        const f2 normal = scale2(delta, 1.0f / dist);
+        const float bias = beta * dist;
+        const float relv = dot2(v, normal);
+        float J = -(relv - bias) / w;
+        const float den = 1.0f / zmax(fabsf(relv), epsilon);
+        J = zclamp(J, pmin * den, pmax * den);
+        const f2 dp = scale2(normal, J);
+        s.mx[i1] += dp.x;
+        s.my[i1] += dp.y;
+    } else {  // MotorJoint.zig:38-64
+        if (s.kind[i1] & K_STATIC) return;
+        const float epsilon = ALLOWED_CONSTRAINT_VALUE;
+        const float target = __ldg(prm + 3);
+        const float I = s.inertia[i1];
+        const float omega = s.L[i1] / I;
+        const float C = omega - target;
+        if (fabsf(C) < ALLOWED_CONSTRAINT_VALUE) return;
+        const float bias = beta * C;
+        const float torque = s.tq[i1];
+        float J = torque - bias;
+        const float relv = torque / I;
+        const float den = 1.0f / zmax(fabsf(relv), epsilon);
+        J = zclamp(J, pmin * den, pmax * den);
+        s.L[i1] += J * h;
+    }
+}
+
+__device__ __forceinline__ bool joint_two_bodies(uint8_t type) {
+    return type == J_DISTANCE || type == J_OFFSET;
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, const Caps C, const Layout Lo) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    __shared__ uint32_t s_wsum[32];
+    __shared__ uint32_t s_ccnt[256];
+    __shared__ int s_err;
+    __shared__ uint32_t s_cnt[4];  // pairs, manifolds, points
+
+    const int tid = threadIdx.x;
+    if (blockIdx.x >= P.nlist) return;
+    const uint32_t w = P.world_list[blockIdx.x];
+    const WorldDesc wd = P.worlds[w];
+    const uint32_t n = wd.n, base = wd.body_off, NB = P.nbodies;
+    const uint32_t T = P.table_mult * n;
+    if (n > C.nb || wd.nj > C.nj || T > C.nt || n > 65535u) {
+        if (tid == 0) {
+            P.world_status[w] = DS_CAPACITY;
+            atomicAdd(P.error_count, 1);
+        }
+        return;
+    }
+    if (tid == 0) {
+        s_err = 0;
+        s_cnt[0] = s_cnt[1] = s_cnt[2] = s_cnt[3] = 0;
+    }
+    int err = 0;
+
+#define SMF(off) reinterpret_cast<float*>(sm + (off))
+#define SMU32(off) reinterpret_cast<uint32_t*>(sm + (off))
+#define SMU16(off) reinterpret_cast<uint16_t*>(sm + (off))
+#define SMU8(off) reinterpret_cast<uint8_t*>(sm + (off))
+#define SMI32(off) reinterpret_cast<int32_t*>(sm + (off))
+
+    SW s;
+    s.px = SMF(Lo.px); s.py = SMF(Lo.py); s.ang = SMF(Lo.ang);
+    s.mx = SMF(Lo.mx); s.my = SMF(Lo.my); s.L = SMF(Lo.L);
+    s.mass = SMF(Lo.mass); s.inertia = SMF(Lo.inertia); s.inv_m = SMF(Lo.inv_m); s.inv_i = SMF(Lo.inv_i);
+    s.cs = SMF(Lo.cs); s.sn = SMF(Lo.sn); s.ang_prev = SMF(Lo.ang_prev); s.tq = SMF(Lo.tq);
+    s.kind = SMU8(Lo.kind);
+    s.ma = SMU16(Lo.ma); s.mb = SMU16(Lo.mb); s.mp0 = SMU16(Lo.mp0);
+    s.mnp = SMU8(Lo.mnp); s.mcol = SMU8(Lo.mcol);
+    s.nx = SMF(Lo.nx); s.ny = SMF(Lo.ny); s.fric = SMF(Lo.fric);
+    s.r1x = SMF(Lo.r1x); s.r1y = SMF(Lo.r1y); s.r2x = SMF(Lo.r2x); s.r2y = SMF(Lo.r2y);
+    s.depth = SMF(Lo.depth); s.odepth = SMF(Lo.odepth); s.mn = SMF(Lo.mn); s.mt = SMF(Lo.mt);
+    s.apn = SMF(Lo.apn); s.apt = SMF(Lo.apt);
+
+    float *ax = SMF(Lo.ax), *ay = SMF(Lo.ay), *ahw = SMF(Lo.ahw), *ahh = SMF(Lo.ahh);
+    int32_t *rx0 = SMI32(Lo.rx0), *ry0 = SMI32(Lo.ry0), *rx1 = SMI32(Lo.rx1), *ry1 = SMI32(Lo.ry1);
+    uint32_t* bcnt = SMU32(Lo.bcnt);
+    uint32_t* ebucket = SMU32(Lo.ebucket);
+    uint16_t *ebody = SMU16(Lo.ebody), *eslot = SMU16(Lo.eslot), *sbody = SMU16(Lo.sbody);
+    uint32_t* table = SMU32(Lo.table);
+    uint32_t* hset = SMU32(Lo.hset);
+    uint32_t* adj = SMU32(Lo.adj);
+    uint16_t* adjl = SMU16(Lo.adjl);
+    unsigned long long* prio = reinterpret_cast<unsigned long long*>(sm + Lo.prio);
+    uint16_t *corder = SMU16(Lo.corder), *coff = SMU16(Lo.coff);
+    uint16_t *jorder = SMU16(Lo.jorder), *joff = SMU16(Lo.joff);
+    uint8_t* jcol = SMU8(Lo.jcol);
+    uint32_t* pairs = SMU32(Lo.pairs);
+
+    const bool disc_rot = (wd.flags & W_DISC_ROTATION) != 0;
+    const float* __restrict__ st = P.state;
+    const float* __restrict__ pr = P.props;
+
+    // ---------------- load the world ----------------
+    for (uint32_t i = tid; i < n; i += NT) {
+        const uint32_t g = base + i;
+        const uint8_t k = __ldg(P.kind + g);
+        const float a = st[(size_t)S_ANGLE * NB + g];
+        s.px[i] = st[(size_t)S_POS_X * NB + g];
+        s.py[i] = st[(size_t)S_POS_Y * NB + g];
+        s.ang[i] = a;
+        s.mx[i] = st[(size_t)S_MOM_X * NB + g];
+        s.my[i] = st[(size_t)S_MOM_Y * NB + g];
+        s.L[i] = st[(size_t)S_ANG_MOM * NB + g];
+        const float m = __ldg(pr + (size_t)P_MASS * NB + g);
+        const float I = __ldg(pr + (size_t)P_INERTIA * NB + g);
+        s.mass[i] = m;
+        s.inertia[i] = I;
+        s.inv_m[i] = (k & K_STATIC) ? 0.f : 1.0f / m;
+        s.inv_i[i] = (k & K_STATIC) ? 0.f : 1.0f / I;
+        s.kind[i] = k;
+        float c = 1.f, sn = 0.f;
+        if ((k & K_RECT) || disc_rot) r2d_sincosf(a, &sn, &c);
+        s.cs[i] = c;
+        s.sn[i] = sn;
+        s.ang_prev[i] = a;
+        s.tq[i] = 0.f;
+        ax[i] = st[(size_t)S_AABB_X * NB + g];
+        ay[i] = st[(size_t)S_AABB_Y * NB + g];
+        ahw[i] = st[(size_t)S_AABB_HW * NB + g];
+        ahh[i] = st[(size_t)S_AABB_HH * NB + g];
+    }
+    for (uint32_t b = tid; b < T + 1; b += NT) table[b] = 0u;
+    for (uint32_t b = tid; b < C.hs; b += NT) hset[b] = 0xFFFFFFFFu;
+    __syncthreads();
+
+    // ---------------- broadphase (SpatialHash.zig:19-137, lib.zig:264-282) ----------------
+    for (uint32_t i = tid; i < n; i += NT) {
+        int32_t x0 = 0, y0 = 0, x1 = -1, y1 = -1;
+        uint32_t cnt = 0;
+        const bool ok = cell_index(ax[i] - ahw[i], P.cell, &x0) && cell_index(ay[i] - ahh[i], P.cell, &y0) &&
+                        cell_index(ax[i] + ahw[i], P.cell, &x1) && cell_index(ay[i] + ahh[i], P.cell, &y1);
+        if (!ok) {
+            err = DS_NONFINITE;
+            x1 = x0 - 1;
+        } else if (x1 >= x0 && y1 >= y0) {
+            const int64_t c64 = ((int64_t)x1 - (int64_t)x0 + 1) * ((int64_t)y1 - (int64_t)y0 + 1);
+            if (c64 > (int64_t)C.ne) err = DS_CAPACITY;
+            else cnt = (uint32_t)c64;
+        }
+        rx0[i] = x0; ry0[i] = y0; rx1[i] = x1; ry1[i] = y1;
+        bcnt[i] = cnt;
+    }
+    if (err) set_err(&s_err, err);
+    if (__syncthreads_or(err != 0)) goto fail;
+    {
+        const uint32_t E = block_scan_excl<NT>(bcnt, n, s_wsum);
+        if (E > C.ne) {
+            if (tid == 0) s_err = DS_CAPACITY;
+            __syncthreads();
+            goto fail;
+        }
+        for (uint32_t i = tid; i < n; i += NT) {
+            uint32_t k = bcnt[i];
+            for (int32_t yi = ry0[i]; yi <= ry1[i]; ++yi)
+                for (int32_t xi = rx0[i]; xi <= rx1[i]; ++xi) {
+                    const uint32_t bk = cell_bucket(xi, yi, T);
+                    ebucket[k] = bk;
+                    ebody[k] = (uint16_t)i;
+                    atomicAdd(&table[bk], 1u);
+                    ++k;
+                }
+        }
+        __syncthreads();
+        block_scan_excl<NT>(table, T, s_wsum);  // table[b] = first slot of bucket b
+        for (uint32_t e = tid; e < E; e += NT) {
+            const uint32_t slot = atomicAdd(&table[ebucket[e]], 1u);
+            sbody[slot] = ebody[e];
+            eslot[e] = (uint16_t)slot;
+        }
+        __syncthreads();  // table[b] = one past the last slot of bucket b
+
+        // Candidates: every two entries of one bucket (the reference's query
+        // returns all bodies of the buckets a body covers), filtered as
+        // lib.zig:273-282, deduplicated like its "manifold already exists"
+        // test (lib.zig:278-281).
+        for (uint32_t e = tid; e < E; e += NT) {
+            const uint32_t i = ebody[e];
+            const uint32_t end = table[ebucket[e]];
+            for (uint32_t q = (uint32_t)eslot[e] + 1u; q < end; ++q) {
+                const uint32_t j = sbody[q];
+                if (j == i) continue;
+                const uint32_t lo = min(i, j), hi = max(i, j);
+                if (s.kind[lo] & s.kind[hi] & K_STATIC) continue;
+                if (!aabb_intersects(f2{ax[lo], ay[lo]}, ahw[lo], ahh[lo], f2{ax[hi], ay[hi]}, ahw[hi], ahh[hi]))
+                    continue;
+                const uint32_t key = (lo << 16) | hi;
+                if (wd.nexcl && excluded(P.excl + wd.excl_off, wd.nexcl, key)) continue;
+                if (hs_insert(hset, C.hs - 1u, key, &err)) {
+                    const uint32_t idx = atomicAdd(&s_cnt[0], 1u);
+                    if (idx < C.np) pairs[idx] = key;
+                    else err = DS_CAPACITY;
+                }
+            }
+        }
+    }
+    if (err) set_err(&s_err, err);
+    if (__syncthreads_or(err != 0)) goto fail;
+
+    // ---------------- narrowphase (collision.zig:299-320, lib.zig:284-294) ----------------
+    {
+        const uint32_t npairs = s_cnt[0];
+        for (uint32_t pi = tid; pi < npairs; pi += NT) {
+            const uint32_t key = pairs[pi];
+            const uint32_t lo = key >> 16, hi = key & 0xFFFFu;
+            const uint32_t o1 = __ldg(P.ids + base + lo) < __ldg(P.ids + base + hi) ? lo : hi;
+            const uint32_t o2 = o1 == lo ? hi : lo;
+            Geo g1, g2;
+            geo_make(g1, f2{s.px[o1], s.py[o1]}, s.kind[o1] & K_RECT, __ldg(pr + (size_t)P_DIM0 * NB + base + o1),
+                     __ldg(pr + (size_t)P_DIM1 * NB + base + o1), s.cs[o1], s.sn[o1]);
+            geo_make(g2, f2{s.px[o2], s.py[o2]}, s.kind[o2] & K_RECT, __ldg(pr + (size_t)P_DIM0 * NB + base + o2),
+                     __ldg(pr + (size_t)P_DIM1 * NB + base + o2), s.cs[o2], s.sn[o2]);
+            SatState sat;
+            if (!perform_narrow_sat(g1, g2, sat)) continue;
+            const uint32_t ref = sat.ref_is_first ? o1 : o2, inc = sat.ref_is_first ? o2 : o1;
+            NewPoint pts[2];
+            const int npt = sat.ref_is_first ? identify_points(g1, g2, sat.refid, pts)
+                                             : identify_points(g2, g1, sat.refid, pts);
+            const uint32_t m = atomicAdd(&s_cnt[1], 1u);
+            if (m >= C.nm) {
+                err = DS_CAPACITY;
+                continue;
+            }
+            const uint32_t p0 = atomicAdd(&s_cnt[2], (uint32_t)npt);
+            if (p0 + npt > C.npt) {
+                err = DS_CAPACITY;
+                continue;
+            }
+            s.ma[m] = (uint16_t)ref;
+            s.mb[m] = (uint16_t)inc;
+            s.mp0[m] = (uint16_t)p0;
+            s.mnp[m] = (uint8_t)npt;
+            s.nx[m] = sat.normal.x;
+            s.ny[m] = sat.normal.y;
+            for (int k = 0; k < npt; ++k) {
+                s.r1x[p0 + k] = pts[k].ref_r.x;
+                s.r1y[p0 + k] = pts[k].ref_r.y;
+                s.r2x[p0 + k] = pts[k].inc_r.x;
+                s.r2y[p0 + k] = pts[k].inc_r.y;
+                s.depth[p0 + k] = pts[k].depth;
+                s.odepth[p0 + k] = pts[k].depth;
+                s.apn[p0 + k] = 0.f;
+                s.apt[p0 + k] = 0.f;
+            }
+        }
+    }
+    if (err) set_err(&s_err, err);
+    if (__syncthreads_or(err != 0)) goto fail;
+
+    {
+        const uint32_t M = min(s_cnt[1], C.nm);
+        const uint32_t NJ = wd.nj;
+        uint32_t ncol = 0, njcol = 0;
+
+        // ---------------- contact colouring (r2d_colour.h) ----------------
+        for (uint32_t i = tid; i <= n; i += NT) adj[i] = 0u;
+        __syncthreads();
+        for (uint32_t m = tid; m < M; m += NT) {
+            const uint32_t a = s.ma[m], b = s.mb[m];
+            if (!(s.kind[a] & K_STATIC)) atomicAdd(&adj[a], 1u);
+            if (!(s.kind[b] & K_STATIC)) atomicAdd(&adj[b], 1u);
+        }
+        __syncthreads();
+        block_scan_excl<NT>(adj, n, s_wsum);
+        for (uint32_t m = tid; m < M; m += NT) {
+            const uint32_t a = s.ma[m], b = s.mb[m];
+            if (!(s.kind[a] & K_STATIC)) adjl[atomicAdd(&adj[a], 1u)] = (uint16_t)m;
+            if (!(s.kind[b] & K_STATIC)) adjl[atomicAdd(&adj[b], 1u)] = (uint16_t)m;
+            const uint32_t lo = min(a, b), hi = max(a, b);
+            prio[m] = ((unsigned long long)r2d_colour_mix(lo, hi) << 32) | ((lo << 16) | hi);
+            s.mcol[m] = 0xFFu;
+        }
+        __syncthreads();  // adj[i] = one past body i's last adjacency slot
+        for (uint32_t round = 0; round <= M + 1; ++round) {
+            int pending = 0;
+            for (uint32_t m = tid; m < M; m += NT) {
+                if (((volatile uint8_t*)s.mcol)[m] != 0xFFu) continue;
+                uint32_t bits[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+                bool ready = true;
+                const unsigned long long pm = prio[m];
+                const uint32_t ends[2] = {s.ma[m], s.mb[m]};
+                for (int e2 = 0; e2 < 2 && ready; ++e2) {
+                    const uint32_t x = ends[e2];
+                    if (s.kind[x] & K_STATIC) continue;
+                    const uint32_t q0 = x ? adj[x - 1] : 0u, q1 = adj[x];
+                    for (uint32_t q = q0; q < q1; ++q) {
+                        const uint32_t o = adjl[q];
+                        if (o == m || prio[o] > pm) continue;
+                        const uint8_t c = ((volatile uint8_t*)s.mcol)[o];
+                        if (c == 0xFFu) {
+                            ready = false;
+                            break;
+                        }
+                        bits[c >> 5] |= 1u << (c & 31);
+                    }
+                }
+                if (ready) {
+                    const uint32_t c = first_free(bits);
+                    if (c == 255u) err = DS_CAPACITY;
+                    ((volatile uint8_t*)s.mcol)[m] = (uint8_t)c;
+                } else {
+                    pending = 1;
+                }
+            }
+            if (!__syncthreads_or(pending)) break;
+        }
+        if (err) set_err(&s_err, err);
+        if (__syncthreads_or(err != 0)) goto fail;
+        // colour-major order
+        for (uint32_t c = tid; c < 256; c += NT) s_ccnt[c] = 0u;
+        __syncthreads();
+        for (uint32_t m = tid; m < M; m += NT) atomicAdd(&s_ccnt[s.mcol[m]], 1u);
+        __syncthreads();
+        for (uint32_t c = 0; c < (uint32_t)MAX_COLOURS; ++c)
+            if (s_ccnt[c]) ncol = c + 1;
+        block_scan_excl<NT>(s_ccnt, 256, s_wsum);
+        for (uint32_t c = tid; c <= ncol; c += NT) coff[c] = (uint16_t)(c < ncol ? s_ccnt[c] : M);
+        __syncthreads();
+        for (uint32_t m = tid; m < M; m += NT) corder[atomicAdd(&s_ccnt[s.mcol[m]], 1u)] = (uint16_t)m;
+
+        // ---------------- joint colouring ----------------
+        if (NJ) {
+            const uint32_t j0 = wd.joint_off;
+            __syncthreads();
+            for (uint32_t i = tid; i <= n; i += NT) adj[i] = 0u;
+            __syncthreads();
+            for (uint32_t j = tid; j < NJ; j += NT) {
+                const uint8_t ty = __ldg(P.jtype + j0 + j);
+                const uint32_t b1 = __ldg(P.jb1 + j0 + j), b2 = __ldg(P.jb2 + j0 + j);
+                atomicAdd(&adj[b1], 1u);
+                if (joint_two_bodies(ty) && b2 != b1) atomicAdd(&adj[b2], 1u);
+            }
+            __syncthreads();
+            block_scan_excl<NT>(adj, n, s_wsum);
+            for (uint32_t j = tid; j < NJ; j += NT) {
+                const uint8_t ty = __ldg(P.jtype + j0 + j);
+                const uint32_t b1 = __ldg(P.jb1 + j0 + j), b2 = __ldg(P.jb2 + j0 + j);
+                adjl[atomicAdd(&adj[b1], 1u)] = (uint16_t)j;
+                if (joint_two_bodies(ty) && b2 != b1) adjl[atomicAdd(&adj[b2], 1u)] = (uint16_t)j;
+                prio[j] = ((unsigned long long)r2d_colour_mix(j, R2D_COLOUR_JOINT_SALT) << 32) | j;
+                jcol[j] = 0xFFu;
+            }
+            __syncthreads();
+            for (uint32_t round = 0; round <= NJ + 1; ++round) {
+                int pending = 0;
+                for (uint32_t j = tid; j < NJ; j += NT) {
+                    if (((volatile uint8_t*)jcol)[j] != 0xFFu) continue;
+                    uint32_t bits[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+                    bool ready = true;
+                    const unsigned long long pj = prio[j];
+                    const uint8_t ty = __ldg(P.jtype + j0 + j);
+                    const uint32_t b1 = __ldg(P.jb1 + j0 + j), b2 = __ldg(P.jb2 + j0 + j);
+                    const int nends = (joint_two_bodies(ty) && b2 != b1) ? 2 : 1;
+                    const uint32_t ends[2] = {b1, b2};
+                    for (int e2 = 0; e2 < nends && ready; ++e2) {
+                        const uint32_t x = ends[e2];
+                        const uint32_t q0 = x ? adj[x - 1] : 0u, q1 = adj[x];
+                        for (uint32_t q = q0; q < q1; ++q) {
+                            const uint32_t o = adjl[q];
+                            if (o == j || prio[o] > pj) continue;
+                            const uint8_t c = ((volatile uint8_t*)jcol)[o];
+                            if (c == 0xFFu) {
+                                ready = false;
+                                break;
+                            }
+                            bits[c >> 5] |= 1u << (c & 31);
+                        }
+                    }
+                    if (ready) {
+                        const uint32_t c = first_free(bits);
+                        if (c == 255u) err = DS_CAPACITY;
+                        ((volatile uint8_t*)jcol)[j] = (uint8_t)c;
+                    } else {
+                        pending = 1;
+                    }
+                }
+                if (!__syncthreads_or(pending)) break;
+            }
+            if (err) set_err(&s_err, err);
+            if (__syncthreads_or(err != 0)) goto fail;
+            for (uint32_t c = tid; c < 256; c += NT) s_ccnt[c] = 0u;
+            __syncthreads();
+            for (uint32_t j = tid; j < NJ; j += NT) atomicAdd(&s_ccnt[jcol[j]], 1u);
+            __syncthreads();
+            for (uint32_t c = 0; c < (uint32_t)MAX_COLOURS; ++c)
+                if (s_ccnt[c]) njcol = c + 1;
+            block_scan_excl<NT>(s_ccnt, 256, s_wsum);
+            for (uint32_t c = tid; c <= njcol; c += NT) joff[c] = (uint16_t)(c < njcol ? s_ccnt[c] : NJ);
+            __syncthreads();
+            for (uint32_t j = tid; j < NJ; j += NT) jorder[atomicAdd(&s_ccnt[jcol[j]], 1u)] = (uint16_t)j;
+        }
+        __syncthreads();
+
+        // ---------------- substeps (lib.zig:199-250) ----------------
+        const uint32_t S = P.sub_steps;
+        const float h = P.dt / (float)S;
+        for (uint32_t sub = 0; sub < S; ++sub) {
+            const bool last = sub + 1 == S;
+            // forces (DownwardsGravity.zig:35-39), AABB, velocities (lib.zig:200-216)
+            for (uint32_t i = tid; i < n; i += NT) {
+                const uint32_t g = base + i;
+                const uint8_t k = s.kind[i];
+                float fx = 0.f, fy = 0.f, tq = 0.f;
+                if (sub == 0) {  // user-set force / torque (RigidBody.Props, RigidBody.zig:73,78)
+                    fx = st[(size_t)S_FORCE_X * NB + g];
+                    fy = st[(size_t)S_FORCE_Y * NB + g];
+                    tq = st[(size_t)S_TORQUE * NB + g];
+                    // a dynamic body's force / torque is cleared after integration (lib.zig:247-248)
+                    if (!(k & K_STATIC) && (fx != 0.f || fy != 0.f || tq != 0.f)) s.kind[i] = k | K_FORCED;
+                }
+                if (!(k & K_STATIC)) {
+                    for (uint32_t gg = 0; gg < wd.ngrav; ++gg) {
+                        fx += 0.0f * s.mass[i];
+                        fy += (-wd.g[gg]) * s.mass[i];
+                    }
+                }
+                if (last) {
+                    float hw, hh;
+                    if (k & K_RECT) {
+                        rect_half_extents(__ldg(pr + (size_t)P_DIM0 * NB + g), __ldg(pr + (size_t)P_DIM1 * NB + g),
+                                          s.cs[i], s.sn[i], &hw, &hh);
+                    } else {
+                        hw = hh = __ldg(pr + (size_t)P_DIM0 * NB + g);
+                    }
+                    P.state[(size_t)S_AABB_X * NB + g] = s.px[i];
+                    P.state[(size_t)S_AABB_Y * NB + g] = s.py[i];
+                    P.state[(size_t)S_AABB_HW * NB + g] = hw;
+                    P.state[(size_t)S_AABB_HH * NB + g] = hh;
+                }
+                if (k & K_STATIC) continue;
+                s.mx[i] += fx * h;
+                s.my[i] += fy * h;
+                s.L[i] += tq * h;
+                s.tq[i] = tq;
+            }
+            __syncthreads();
+            // updateTGSDepth + preStep (collision.zig:73-133)
+            for (uint32_t m = tid; m < M; m += NT) {
+                const uint32_t a = s.ma[m], b = s.mb[m];
+                const f2 n2 = {s.nx[m], s.ny[m]};
+                const uint32_t p0 = s.mp0[m], np = s.mnp[m];
+                for (uint32_t k = 0; k < np; ++k) {
+                    const uint32_t p = p0 + k;
+                    if (approx_eql(s.depth[p], s.odepth[p], 1e-4f)) continue;
+                    float sa_, ca_, sb_, cb_;
+                    r2d_sincosf(s.ang[a] - s.ang_prev[a], &sa_, &ca_);
+                    r2d_sincosf(s.ang[b] - s.ang_prev[b], &sb_, &cb_);
+                    const f2 rr1 = rot(f2{s.r1x[p], s.r1y[p]}, ca_, sa_);
+                    const f2 rr2 = rot(f2{s.r2x[p], s.r2y[p]}, cb_, sb_);
+                    const f2 a1 = add2(rr1, f2{s.px[a], s.py[a]});
+                    const f2 a2 = add2(rr2, f2{s.px[b], s.py[b]});
+                    const float d = dot2(n2, sub2(a2, a1));
+                    s.depth[p] = d + s.odepth[p];
+                    s.r1x[p] = rr1.x;
+                    s.r1y[p] = rr1.y;
+                    s.r2x[p] = rr2.x;
+                    s.r2y[p] = rr2.y;
+                }
+                const float inv_m1 = s.inv_m[a], inv_m2 = s.inv_m[b];
+                const float inv_mass = inv_m1 + inv_m2;
+                const float inv_i1 = s.inv_i[a], inv_i2 = s.inv_i[b];
+                const f2 t2 = cw90(n2);
+                s.fric[m] = sqrtf(__ldg(pr + (size_t)P_MU * NB + base + a) * __ldg(pr + (size_t)P_MU * NB + base + b));
+                for (uint32_t k = 0; k < np; ++k) {
+                    const uint32_t p = p0 + k;
+                    const f2 r1 = {s.r1x[p], s.r1y[p]}, r2 = {s.r2x[p], s.r2y[p]};
+                    const float r1n = cross2(r1, n2), r2n = cross2(r2, n2);
+                    const float kn = inv_mass + inv_i1 * (r1n * r1n) + inv_i2 * (r2n * r2n);
+                    const float r1t = cross2(r1, t2), r2t = cross2(r2, t2);
+                    const float kt = inv_mass + inv_i1 * (r1t * r1t) + inv_i2 * (r2t * r2t);
+                    s.mn[p] = kn > 0.0f ? 1.0f / kn : 0.0f;
+                    s.mt[p] = kt > 0.0f ? 1.0f / kt : 0.0f;
+                }
+            }
+            __syncthreads();
+            // impulse iterations (lib.zig:226-236): joints, then contacts
+            for (uint32_t it = 0; it < P.iters; ++it) {
+                for (uint32_t c = 0; c < njcol; ++c) {
+                    const uint32_t k0 = joff[c], k1 = joff[c + 1];
+                    for (uint32_t k = k0 + tid; k < k1; k += NT) {
+                        const uint32_t j = jorder[k];
+                        const uint32_t gj = wd.joint_off + j;
+                        solve_joint(s, __ldg(P.jtype + gj), __ldg(P.jb1 + gj), __ldg(P.jb2 + gj),
+                                    P.jprm + (size_t)gj * JOINT_PARAMS, h);
+                    }
+                    __syncthreads();
+                }
+                for (uint32_t c = 0; c < ncol; ++c) {
+                    const uint32_t k0 = coff[c], k1 = coff[c + 1];
+                    for (uint32_t k = k0 + tid; k < k1; k += NT) solve_contact(s, corder[k], h);
+                    __syncthreads();
+                }
+            }
+            // integration (lib.zig:238-249)
+            for (uint32_t i = tid; i < n; i += NT) {
+                s.ang_prev[i] = s.ang[i];
+                const uint8_t k = s.kind[i];
+                if (k & K_STATIC) continue;
+                const float sm_ = h / s.mass[i];
+                s.px[i] += s.mx[i] * sm_;
+                s.py[i] += s.my[i] * sm_;
+                s.ang[i] += s.L[i] * h / s.inertia[i];
+                s.tq[i] = 0.f;
+                if (!last && ((k & K_RECT) || disc_rot)) {
+                    float c, sn;
+                    r2d_sincosf(s.ang[i], &sn, &c);
+                    s.cs[i] = c;
+                    s.sn[i] = sn;
+                }
+            }
+            __syncthreads();
+        }
+
+        // ---------------- write back ----------------
+        for (uint32_t i = tid; i < n; i += NT) {
+            const uint32_t g = base + i;
+            P.state[(size_t)S_POS_X * NB + g] = s.px[i];
+            P.state[(size_t)S_POS_Y * NB + g] = s.py[i];
+            P.state[(size_t)S_ANGLE * NB + g] = s.ang[i];
+            P.state[(size_t)S_MOM_X * NB + g] = s.mx[i];
+            P.state[(size_t)S_MOM_Y * NB + g] = s.my[i];
+            P.state[(size_t)S_ANG_MOM * NB + g] = s.L[i];
+            if (s.kind[i] & K_FORCED) {
+                P.state[(size_t)S_FORCE_X * NB + g] = 0.f;
+                P.state[(size_t)S_FORCE_Y * NB + g] = 0.f;
+                P.state[(size_t)S_TORQUE * NB + g] = 0.f;
+            }
+        }
+        if (P.dbg.cap) {
+            const uint32_t cap = P.dbg.cap;
+            if (tid == 0) P.dbg.nman[w] = M;
+            for (uint32_t m = tid; m < M && m < cap; m += NT) {
+                const size_t o = (size_t)w * cap + m;
+                P.dbg.keys[2 * o] = s.ma[m];
+                P.dbg.keys[2 * o + 1] = s.mb[m];
+                P.dbg.colour[o] = s.mcol[m];
+                float* d = P.dbg.data + o * DEBUG_MF;
+                const f2 nn = {s.nx[m], s.ny[m]};
+                const f2 tt = cw90(nn);
+                const uint32_t np = s.mnp[m], p0 = s.mp0[m];
+                d[0] = nn.x; d[1] = nn.y; d[2] = tt.x; d[3] = tt.y; d[4] = s.fric[m];
+                d[5] = np > 0 ? 1.f : 0.f;
+                d[6] = np > 1 ? 1.f : 0.f;
+                d[7] = s.ang_prev[s.ma[m]];
+                d[8] = s.ang_prev[s.mb[m]];
+                for (uint32_t k = 0; k < 2; ++k) {
+                    float* q = d + 9 + 12 * k;
+                    const bool has = k < np;
+                    const uint32_t p = p0 + k;
+                    q[0] = __int_as_float(0x7fc00000);
+                    q[1] = __int_as_float(0x7fc00000);
+                    q[2] = has ? s.r1x[p] : 0.f;
+                    q[3] = has ? s.r1y[p] : 0.f;
+                    q[4] = has ? s.r2x[p] : 0.f;
+                    q[5] = has ? s.r2y[p] : 0.f;
+                    q[6] = has ? s.depth[p] : 0.f;
+                    q[7] = has ? s.odepth[p] : 0.f;
+                    q[8] = has ? s.mn[p] : 0.f;
+                    q[9] = has ? s.mt[p] : 0.f;
+                    q[10] = has ? s.apn[p] : 0.f;
+                    q[11] = has ? s.apt[p] : 0.f;
+                }
+            }
+            if (P.dbg.jcap) {
+                for (uint32_t j = tid; j < NJ && j < P.dbg.jcap; j += NT)
+                    P.dbg.jcolour[(size_t)w * P.dbg.jcap + j] = jcol[j];
+            }
+        }
+        if (tid == 0) P.world_status[w] = DS_OK;
+        return;
+    }
+
+fail:
+    if (tid == 0) {
+        P.world_status[w] = s_err ? s_err : DS_CAPACITY;
+        atomicAdd(P.error_count, 1);
+    }
+#undef SMF
+#undef SMU32
+#undef SMU16
+#undef SMU8
+#undef SMI32
+}
+
+// ---------------------------------------------------------------------------
+// host-side launch helpers
+// ---------------------------------------------------------------------------
+template <int NT>
+cudaError_t launch_world_step_nt(const StepParams& P, const Caps& C, cudaStream_t stream) {
+    const Layout L = make_layout(C);
+    cudaError_t e = cudaFuncSetAttribute(world_step_kernel<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)L.total);
+    if (e != cudaSuccess) return e;
+    if (P.nlist == 0) return cudaSuccess;
+    world_step_kernel<NT><<<P.nlist, NT, L.total, stream>>>(P, C, L);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_world_step(const StepParams& P, const Caps& C, int threads, cudaStream_t stream) {
+    switch (threads) {
+    case 32: return launch_world_step_nt<32>(P, C, stream);
+    case 64: return launch_world_step_nt<64>(P, C, stream);
+    case 128: return launch_world_step_nt<128>(P, C, stream);
+    case 256: return launch_world_step_nt<256>(P, C, stream);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+template <int NT>
+cudaError_t occupancy_nt(const Caps& C, int* blocks_per_sm) {
+    const Layout L = make_layout(C);
+    cudaError_t e = cudaFuncSetAttribute(world_step_kernel<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)L.total);
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, world_step_kernel<NT>, NT, L.total);
+}
+
+cudaError_t world_step_occupancy(const Caps& C, int threads, int* blocks_per_sm) {
+    switch (threads) {
+    case 32: return occupancy_nt<32>(C, blocks_per_sm);
+    case 64: return occupancy_nt<64>(C, blocks_per_sm);
+    case 128: return occupancy_nt<128>(C, blocks_per_sm);
+    case 256: return occupancy_nt<256>(C, blocks_per_sm);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace r2d

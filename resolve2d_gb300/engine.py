@@ -1,0 +1,185 @@
+"""Thin Python handles over the C ABI: one world (``World``, the drop-in for
+the reference's Solver) and many independent worlds (``Batch``).  Both own
+device memory through the library; numpy arrays cross the boundary."""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+from .scenes import NSTATE, Scene, derive_props_state
+
+
+def _config(cell: float, mult: int, debug: bool, stream) -> N.Config:
+    cfg = N.Config()
+    cfg.spatialhash_cell_width = float(cell)
+    cfg.spatialhash_table_size_mult = int(mult)
+    cfg.flags = N.FLAG_DEBUG_TAPS if debug else 0
+    cfg.stream = int(stream) if stream else None
+    return cfg
+
+
+class World:
+    """One world stepped by the fused kernel (r2d_solver_* entry points)."""
+
+    def __init__(self, cell: float = 0.0, mult: int = 0, debug: bool = False, stream=None):
+        self._lib = N.load()
+        self._h = C.c_void_p()
+        cfg = _config(cell, mult, debug, stream)
+        N.check(self._lib.r2d_solver_create(C.byref(cfg), C.byref(self._h)), "r2d_solver_create")
+        self.n = 0
+
+    def close(self):
+        if self._h:
+            self._lib.r2d_solver_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_bodies(self, ids, kind, props, state, init_aabb: bool):
+        ids, kind, props, state = N.u32(ids), N.u8(kind), N.f32(props), N.f32(state)
+        self.n = int(ids.shape[0])
+        N.check(self._lib.r2d_solver_set_bodies(self._h, self.n, N.ptr(ids, C.c_uint32), N.ptr(kind, C.c_uint8),
+                                                N.ptr(props, C.c_float), N.ptr(state, C.c_float), int(init_aabb)),
+                "r2d_solver_set_bodies")
+
+    def set_gravity(self, g):
+        g = N.f32(np.atleast_1d(g))
+        N.check(self._lib.r2d_solver_set_gravity(self._h, int(g.shape[0]), N.ptr(g, C.c_float)), "r2d_solver_set_gravity")
+
+    def set_joints(self, jtype, id1, id2, prm):
+        jtype, id1, id2, prm = N.u8(jtype), N.u32(id1), N.u32(id2), N.f32(prm)
+        N.check(self._lib.r2d_solver_set_joints(self._h, int(jtype.shape[0]), N.ptr(jtype, C.c_uint8),
+                                                N.ptr(id1, C.c_uint32), N.ptr(id2, C.c_uint32),
+                                                N.ptr(prm, C.c_float)), "r2d_solver_set_joints")
+
+    def set_exclusions(self, pairs):
+        pairs = N.u32(np.asarray(pairs).reshape(-1, 2))
+        N.check(self._lib.r2d_solver_set_exclusions(self._h, int(pairs.shape[0]), N.ptr(pairs, C.c_uint32)),
+                "r2d_solver_set_exclusions")
+
+    @classmethod
+    def from_scene(cls, sc: Scene, debug: bool = False, stream=None, **kw) -> "World":
+        assert sc.nworlds == 1
+        w = cls(debug=debug, stream=stream, **kw)
+        props, state = derive_props_state(sc.kind, sc.opt)
+        w.set_gravity(sc.gravity[sc.gravity != 0] if sc.gravity.size else np.zeros(0, np.float32))
+        w.set_bodies(sc.ids, sc.kind & 3, props, state, init_aabb=True)
+        if sc.jtype.size:
+            w.set_joints(sc.jtype, sc.jid1, sc.jid2, sc.jprm)
+        if sc.xpairs.size:
+            w.set_exclusions(sc.xpairs)
+        return w
+
+    def write_state(self, state):
+        state = N.f32(state)
+        N.check(self._lib.r2d_solver_write_state(self._h, N.ptr(state, C.c_float)), "r2d_solver_write_state")
+
+    def read_state(self) -> np.ndarray:
+        out = np.empty((NSTATE, self.n), np.float32)
+        N.check(self._lib.r2d_solver_read_state(self._h, N.ptr(out, C.c_float)), "r2d_solver_read_state")
+        return out
+
+    def process(self, dt: float, sub_steps: int = 1, iters: int = 8):
+        N.check(self._lib.r2d_solver_process(self._h, float(dt), int(sub_steps), int(iters)), "r2d_solver_process")
+
+    def sync(self):
+        N.check(self._lib.r2d_solver_sync(self._h), "r2d_solver_sync")
+
+    def manifolds(self):
+        m = C.c_uint32()
+        N.check(self._lib.r2d_solver_num_manifolds(self._h, C.byref(m)), "r2d_solver_num_manifolds")
+        k = np.zeros((m.value, 2), np.uint32)
+        d = np.zeros((m.value, N.MANIFOLD_FLOATS), np.float32)
+        c = np.zeros(m.value, np.uint32)
+        N.check(self._lib.r2d_solver_get_manifolds(self._h, m.value, N.ptr(k, C.c_uint32), N.ptr(d, C.c_float),
+                                                   N.ptr(c, C.c_uint32)), "r2d_solver_get_manifolds")
+        return k, d, c
+
+    def joint_colours(self, nj: int):
+        c = np.zeros(nj, np.uint32)
+        N.check(self._lib.r2d_solver_get_joint_colours(self._h, nj, N.ptr(c, C.c_uint32)), "r2d_solver_get_joint_colours")
+        return c
+
+
+class Batch:
+    """Many independent worlds stepped together (r2d_batch_* entry points)."""
+
+    def __init__(self, cell: float = 0.0, mult: int = 0, debug: bool = False, stream=None):
+        self._lib = N.load()
+        self._h = C.c_void_p()
+        cfg = _config(cell, mult, debug, stream)
+        N.check(self._lib.r2d_batch_create(C.byref(cfg), C.byref(self._h)), "r2d_batch_create")
+        self.n = 0
+        self.nworlds = 0
+
+    def close(self):
+        if self._h:
+            self._lib.r2d_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_worlds(self, body_off, ids, kind, props, state, gravity, init_aabb: bool):
+        body_off, ids, kind = N.u32(body_off), N.u32(ids), N.u8(kind)
+        props, state, gravity = N.f32(props), N.f32(state), N.f32(gravity)
+        self.nworlds = int(body_off.shape[0] - 1)
+        self.n = int(body_off[-1])
+        N.check(self._lib.r2d_batch_set_worlds(self._h, self.nworlds, N.ptr(body_off, C.c_uint32),
+                                               N.ptr(ids, C.c_uint32), N.ptr(kind, C.c_uint8),
+                                               N.ptr(props, C.c_float), N.ptr(state, C.c_float),
+                                               N.ptr(gravity, C.c_float), int(init_aabb)), "r2d_batch_set_worlds")
+
+    @classmethod
+    def from_scene(cls, sc: Scene, debug: bool = False, stream=None, **kw) -> "Batch":
+        assert sc.jtype.size == 0 and sc.xpairs.size == 0, "the batch entry points take worlds without joints"
+        b = cls(debug=debug, stream=stream, **kw)
+        props, state = derive_props_state(sc.kind, sc.opt)
+        b.set_worlds(sc.body_off, sc.ids, sc.kind & 3, props, state, sc.gravity, init_aabb=True)
+        return b
+
+    def write_state(self, state):
+        state = N.f32(state)
+        N.check(self._lib.r2d_batch_write_state(self._h, N.ptr(state, C.c_float)), "r2d_batch_write_state")
+
+    def read_state(self, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty((NSTATE, self.n), np.float32)
+        N.check(self._lib.r2d_batch_read_state(self._h, N.ptr(out, C.c_float)), "r2d_batch_read_state")
+        return out
+
+    def process(self, dt: float, sub_steps: int = 1, iters: int = 8):
+        N.check(self._lib.r2d_batch_process(self._h, float(dt), int(sub_steps), int(iters)), "r2d_batch_process")
+
+    def sync(self):
+        N.check(self._lib.r2d_batch_sync(self._h), "r2d_batch_sync")
+
+    def launches_per_step(self) -> int:
+        out = C.c_uint32()
+        N.check(self._lib.r2d_batch_launches_per_step(self._h, C.byref(out)), "r2d_batch_launches_per_step")
+        return int(out.value)
+
+    def world_status(self) -> np.ndarray:
+        out = np.zeros(self.nworlds, np.int32)
+        N.check(self._lib.r2d_batch_world_status(self._h, N.ptr(out, C.c_int)), "r2d_batch_world_status")
+        return out
+
+    def manifolds(self, w: int):
+        m = C.c_uint32()
+        N.check(self._lib.r2d_batch_num_manifolds(self._h, w, C.byref(m)), "r2d_batch_num_manifolds")
+        k = np.zeros((m.value, 2), np.uint32)
+        d = np.zeros((m.value, N.MANIFOLD_FLOATS), np.float32)
+        c = np.zeros(m.value, np.uint32)
+        N.check(self._lib.r2d_batch_get_manifolds(self._h, w, m.value, N.ptr(k, C.c_uint32), N.ptr(d, C.c_float),
+                                                  N.ptr(c, C.c_uint32)), "r2d_batch_get_manifolds")
+        return k, d, c

@@ -1,0 +1,62 @@
+"""Helpers shared by the parity tests: run a scene on the GPU path and on the
+oracle, and compare results bit for bit.
+
+Float comparison is by value with NaN == NaN: the GPU path skips the +0 the
+reference adds to a static body (collision.zig:208-212), which can only turn
+a -0.0 into +0.0, so signed zeros are not distinguished.  Everything else must
+be identical.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+FIELDS = ["pos_x", "pos_y", "angle", "mom_x", "mom_y", "ang_mom", "force_x", "force_y", "torque",
+          "aabb_x", "aabb_y", "aabb_hw", "aabb_hh"]
+
+
+def mismatch(got: np.ndarray, want: np.ndarray) -> np.ndarray:
+    got = np.asarray(got)
+    want = np.asarray(want)
+    same = (got == want) | (np.isnan(got) & np.isnan(want))
+    return ~same
+
+
+def assert_state_equal(got: np.ndarray, want: np.ndarray, what: str = "state"):
+    assert got.shape == want.shape, (got.shape, want.shape)
+    bad = mismatch(got, want)
+    if bad.any():
+        idx = np.argwhere(bad)
+        lines = []
+        for f, i in idx[:8]:
+            lines.append(f"  {FIELDS[f] if got.shape[0] == 13 else f}[{i}]: gpu {got[f, i]!r} oracle {want[f, i]!r}")
+        raise AssertionError(f"{what}: {len(idx)} entries differ\n" + "\n".join(lines))
+
+
+def manifold_table(keys: np.ndarray, data: np.ndarray, colours: np.ndarray | None):
+    """Manifolds keyed by (reference, incident), dropping the point positions
+    (the GPU keeps ref_r / inc_r, not the contact position)."""
+    out = {}
+    for m in range(keys.shape[0]):
+        d = data[m].copy()
+        d[9:11] = 0.0   # point 0 pos
+        d[21:23] = 0.0  # point 1 pos
+        npts = int(d[5]) + int(d[6])
+        if npts < 2:
+            d[21:33] = 0.0
+        if npts < 1:
+            d[9:21] = 0.0
+        out[(int(keys[m, 0]), int(keys[m, 1]))] = (d, None if colours is None else int(colours[m]))
+    return out
+
+
+def assert_manifolds_equal(gk, gd, gc, ok, od, oc):
+    g = manifold_table(gk, gd, gc)
+    o = manifold_table(ok, od, oc)
+    assert set(g) == set(o), f"pair sets differ: gpu-only {sorted(set(g) - set(o))[:5]} oracle-only {sorted(set(o) - set(g))[:5]}"
+    for k in o:
+        dg, cg = g[k]
+        do, co = o[k]
+        bad = mismatch(dg, do)
+        assert not bad.any(), f"manifold {k}: fields {np.flatnonzero(bad).tolist()} gpu {dg[bad]} oracle {do[bad]}"
+        assert cg == co, f"manifold {k}: colour gpu {cg} oracle {co}"

@@ -1,0 +1,183 @@
+"""GPU step vs the CPU oracle, through the C ABI.
+
+The oracle replays the reference's per-constraint arithmetic in the GPU's
+colour-major order (ORDER_COLOUR); the bar is bit-identical state, pair sets,
+manifolds and colourings (see parity.py for the signed-zero note).
+"""
+
+import numpy as np
+import pytest
+
+from oracle import ORDER_COLOUR, Oracle
+from parity import assert_manifolds_equal, assert_state_equal
+from resolve2d_gb300 import _native as N
+from resolve2d_gb300 import scenes
+from resolve2d_gb300.engine import Batch, World
+
+pytestmark = pytest.mark.gpu
+
+
+def run_pair(sc, steps, check_every=1, debug=True, sub_steps=None, iters=None):
+    S = sc.sub_steps if sub_steps is None else sub_steps
+    I = sc.iters if iters is None else iters
+    w = World.from_scene(sc, debug=debug)
+    o = Oracle.from_scene(sc)
+    assert_state_equal(w.read_state(), o.state(), "initial state")
+    for s in range(steps):
+        w.process(sc.dt, S, I)
+        w.sync()
+        assert o.process(sc.dt, S, I, ORDER_COLOUR) == 0
+        if (s + 1) % check_every == 0 or s + 1 == steps:
+            assert_state_equal(w.read_state(), o.state(), f"{sc.name} step {s + 1}")
+            if debug:
+                gk, gd, gc = w.manifolds()
+                ok, od = o.manifolds()
+                oc, _ = o.colours()
+                assert_manifolds_equal(gk, gd, gc, ok, od, oc)
+    return w, o
+
+
+def test_config0_first_steps_bit_exact():
+    run_pair(scenes.config0(), steps=5)
+
+
+def test_config0_full_run_bit_exact():
+    sc = scenes.config0()
+    run_pair(sc, steps=sc.steps, check_every=50)
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_random_scenes_with_joints(seed):
+    sc = scenes.random_scene(seed, n=40, joints=True)
+    w, o = run_pair(sc, steps=40, check_every=5)
+    if sc.jtype.size:
+        _, oj = o.colours()
+        np.testing.assert_array_equal(w.joint_colours(len(sc.jtype)), oj)
+
+
+@pytest.mark.parametrize("seed", [11, 12])
+def test_substeps_and_iterations(seed):
+    # the reference demos step with sub_steps = 4, iterations = 4 (demos/native/src/main.zig:16-20)
+    sc = scenes.random_scene(seed, n=30, joints=True)
+    run_pair(sc, steps=20, check_every=4, sub_steps=4, iters=4)
+
+
+def test_batch_matches_oracle_per_world():
+    sc = scenes.batched_worlds("batch-small", seed=3, nworlds=24, steps=40, lo=16, hi=512)
+    b = Batch.from_scene(sc, debug=True)
+    oracles = [Oracle.from_scene(sc.world(w)) for w in range(sc.nworlds)]
+    for s in range(sc.steps):
+        b.process(sc.dt, sc.sub_steps, sc.iters)
+        b.sync()
+        for o in oracles:
+            assert o.process(sc.dt, sc.sub_steps, sc.iters, ORDER_COLOUR) == 0
+    st = b.read_state()
+    for w, o in enumerate(oracles):
+        b0, b1 = sc.body_off[w], sc.body_off[w + 1]
+        assert_state_equal(st[:, b0:b1], o.state(), f"world {w}")
+        gk, gd, gc = b.manifolds(w)
+        ok, od = o.manifolds()
+        oc, _ = o.colours()
+        assert_manifolds_equal(gk, gd, gc, ok, od, oc)
+
+
+def test_batch_equals_single_world_path():
+    sc = scenes.batched_worlds("batch-eq", seed=5, nworlds=6, steps=10)
+    b = Batch.from_scene(sc)
+    ws = [World.from_scene(sc.world(w)) for w in range(sc.nworlds)]
+    for _ in range(sc.steps):
+        b.process(sc.dt, 1, sc.iters)
+        for w in ws:
+            w.process(sc.dt, 1, sc.iters)
+    b.sync()
+    st = b.read_state()
+    for k, w in enumerate(ws):
+        w.sync()
+        np.testing.assert_array_equal(st[:, sc.body_off[k]:sc.body_off[k + 1]], w.read_state())
+
+
+def test_determinism_run_twice():
+    sc = scenes.batched_worlds("det", seed=9, nworlds=32, steps=30)
+    out = []
+    for _ in range(2):
+        b = Batch.from_scene(sc)
+        for _ in range(sc.steps):
+            b.process(sc.dt, 1, sc.iters)
+        b.sync()
+        out.append(b.read_state())
+    assert np.array_equal(out[0].view(np.uint32), out[1].view(np.uint32))
+
+
+def test_external_forces_and_torques():
+    sc = scenes.random_scene(21, n=25, joints=True)
+    w = World.from_scene(sc, debug=True)
+    o = Oracle.from_scene(sc)
+    st = o.state()
+    rng = np.random.default_rng(0)
+    st[6] = rng.normal(size=st.shape[1]).astype(np.float32) * 5
+    st[7] = rng.normal(size=st.shape[1]).astype(np.float32) * 5
+    st[8] = rng.normal(size=st.shape[1]).astype(np.float32)
+    o.set_state(st)
+    w.write_state(st)
+    for s in range(6):
+        w.process(sc.dt, 2, 6)
+        w.sync()
+        assert o.process(sc.dt, 2, 6, ORDER_COLOUR) == 0
+        assert_state_equal(w.read_state(), o.state(), f"forces step {s}")
+
+
+def test_exclusions_and_cell_boundaries():
+    # bodies centred on multiples of the 4.0 cell and at negative coordinates,
+    # touching pairs excluded by id (EntityFactory.excludeCollisionPair, lib.zig:124-129)
+    b = scenes._Builder()
+    b.rect(0.0, -0.5, 60.0, 1.0, 0.5, static=True)
+    for i in range(-6, 7):
+        b.disc(4.0 * i, 0.5, 0.5, 0.5)
+        b.rect(4.0 * i + 0.95, 0.5, 1.0, 1.0, 0.5)
+        b.disc(4.0 * i - 0.001, 4.0, 0.6, 0.5)
+    ids, kind, opt = b.arrays()
+    sc = scenes._concat("cells", [(ids, kind, opt)], [9.81], 1 / 60, 1, 8, 30,
+                        excl=(np.zeros(3, np.uint32), np.array([[1, 2], [4, 5], [7, 8]], np.uint32)))
+    run_pair(sc, steps=30, check_every=3)
+
+
+def test_empty_single_and_static_worlds():
+    for bodies in ([], [("disc", False)], [("rect", True), ("rect", True)]):
+        b = scenes._Builder()
+        for i, (t, st) in enumerate(bodies):
+            if t == "disc":
+                b.disc(0.0, 2.0 * i, 0.5, 0.5, static=st)
+            else:
+                b.rect(0.0, 2.0 * i, 1.0, 1.0, 0.5, static=st)
+        if bodies:
+            ids, kind, opt = b.arrays()
+        else:
+            ids, kind, opt = np.zeros(0, np.uint32), np.zeros(0, np.uint8), np.zeros((10, 0), np.float32)
+        sc = scenes._concat("tiny", [(ids, kind, opt)], [9.81], 1 / 60, 1, 8, 5)
+        if not bodies:
+            w = World()
+            w.process(sc.dt, 1, 8)
+            w.sync()
+            continue
+        run_pair(sc, steps=5)
+
+
+def test_world_over_capacity_reports_error():
+    sc = scenes.batched_worlds("big", seed=1, nworlds=1, steps=1, lo=1500, hi=1500)
+    w = World.from_scene(sc)
+    with pytest.raises(N.R2DError) as e:
+        w.process(sc.dt, 1, 8)
+        w.sync()
+    assert e.value.code == -5
+
+
+def test_unknown_joint_body_id_is_an_error():
+    sc = scenes.random_scene(3, n=10)
+    w = World.from_scene(sc)
+    w.set_joints(np.array([0], np.uint8), np.array([1], np.uint32), np.array([999], np.uint32),
+                 np.array([[np.inf, -np.inf, 10, 1, 0, 0, 0, 0]], np.float32))
+    before = w.read_state()
+    with pytest.raises(N.R2DError) as e:
+        w.process(sc.dt, 1, 8)
+    assert e.value.code == -2
+    np.testing.assert_array_equal(w.read_state(), before)
