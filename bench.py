@@ -207,7 +207,11 @@ def main():
 
     B.build_library()
     sc = scenes.config3(seed=3 + rank)
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: the library launches on it and the CUDA events below
+    # are recorded on it (the legacy default stream has handle 0, which the
+    # library would replace with a stream of its own)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     batch = Batch.from_scene(sc, stream=stream.cuda_stream)
     # settle (untimed): bring the worlds to their loaded state
     for _ in range(SETTLE_STEPS):

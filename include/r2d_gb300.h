@@ -103,6 +103,10 @@ typedef struct r2d_config {
     uint32_t spatialhash_table_size_mult;
     uint32_t flags;
     void* stream;
+    /* Scales the per-world buffer sizes of the fused kernel (0 = 1.0).  A
+     * world that outgrows a buffer is replayed with doubled sizes, so this
+     * trades shared memory against replays; it never changes results. */
+    float capacity_scale;
 } r2d_config;
 
 /* ---------------------------------------------------------------------------

@@ -40,7 +40,7 @@ _SIG = {
     "r2o_update_manifolds": ([_P, C.c_int], C.c_int),
     "r2o_num_manifolds": ([_P], C.c_uint32),
     "r2o_get_manifolds": ([_P, _u32p, _f32p], None),
-    "r2o_get_colours": ([_P, _u32p, _u32p], None),
+    "r2o_get_colours": ([_P, C.c_uint32, _u32p, C.c_uint32, _u32p], C.c_uint32),
     "r2o_nmath_kat": ([_f32p, _f32p, _f32p], None),
     "r2o_aabb_intersects": ([C.c_float] * 8, C.c_int),
     "r2o_sincosf": ([C.c_uint32, _f32p, _f32p, _f32p], None),
@@ -151,10 +151,10 @@ class Oracle:
 
     def colours(self):
         m = int(self.lib.r2o_num_manifolds(self.h))
-        c = np.zeros(m, np.uint32)
+        c = np.zeros(max(m, 1), np.uint32)
         j = np.zeros(max(self.nj, 1), np.uint32)
-        self.lib.r2o_get_colours(self.h, _p(c, C.c_uint32), _p(j, C.c_uint32))
-        return c, j[: self.nj]
+        got = self.lib.r2o_get_colours(self.h, m, _p(c, C.c_uint32), self.nj, _p(j, C.c_uint32))
+        return c[: min(m, got)], j[: self.nj]
 
 
 def batch_run(sc, steps: int, nthreads: int, precision: int = 32, order: int = ORDER_COLOUR, state_in=None):

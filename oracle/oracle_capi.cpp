@@ -249,10 +249,14 @@ void r2o_get_props(void* hp, float* out) {
 int r2o_process(void* hp, float dt, uint32_t sub_steps, uint32_t iters, int order) {
     Handle* h = (Handle*)hp;
     int st = 0;
-    if (h->precision == 64)
-        st = h->d->process(double(dt), sub_steps, iters, order);
-    else
-        st = h->f->process(dt, sub_steps, iters, order);
+    try {
+        if (h->precision == 64)
+            st = h->d->process(double(dt), sub_steps, iters, order);
+        else
+            st = h->f->process(dt, sub_steps, iters, order);
+    } catch (...) {
+        st = ERR_INTERNAL;
+    }
     return st;
 }
 
@@ -261,7 +265,11 @@ int r2o_process(void* hp, float dt, uint32_t sub_steps, uint32_t iters, int orde
 int r2o_update_manifolds(void* hp, int order) {
     Handle* h = (Handle*)hp;
     int st = 0;
-    DISPATCH(h, (st = S.update_manifolds(), st = (st == 0 && order == ORDER_COLOUR) ? S.compute_colouring() : st));
+    try {
+        DISPATCH(h, (st = S.update_manifolds(), st = (st == 0 && order == ORDER_COLOUR) ? S.compute_colouring() : st));
+    } catch (...) {
+        st = ERR_INTERNAL;
+    }
     return st;
 }
 
@@ -278,11 +286,15 @@ void r2o_get_manifolds(void* hp, uint32_t* keys, float* data) {
 }
 
 /* Colours of the manifolds (discovery order) and joints (insertion order)
- * from the last colouring. */
-void r2o_get_colours(void* hp, uint32_t* contact, uint32_t* joint) {
+ * from the last colouring; at most ncap / jcap entries are written.
+ * Returns the number of manifold colours available. */
+uint32_t r2o_get_colours(void* hp, uint32_t ncap, uint32_t* contact, uint32_t jcap, uint32_t* joint) {
     Handle* h = (Handle*)hp;
-    DISPATCH(h, (std::copy(S.contact_colour.begin(), S.contact_colour.end(), contact),
-                 std::copy(S.joint_colour.begin(), S.joint_colour.end(), joint)));
+    uint32_t n = 0;
+    DISPATCH(h, (n = (uint32_t)S.contact_colour.size(),
+                 std::copy_n(S.contact_colour.begin(), std::min<size_t>(ncap, S.contact_colour.size()), contact),
+                 std::copy_n(S.joint_colour.begin(), std::min<size_t>(jcap, S.joint_colour.size()), joint)));
+    return n;
 }
 
 /* Many independent worlds stepped on host threads (one world per task,

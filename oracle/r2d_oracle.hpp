@@ -60,7 +60,13 @@ enum Status : int {
     OK = 0,
     ERR_INVALID_BODY_ID = -2,  // error.InvalidRigidBodyId (DistanceJoint.zig:44-47)
     ERR_NONFINITE_AABB = -7,   // @intFromFloat of NaN/inf is undefined in the reference
+    ERR_CAPACITY = -5,         // a body covers more spatial-hash cells than the oracle will allocate
+    ERR_INTERNAL = -4,         // an exception escaped (allocation failure)
 };
+
+// More cells than any sane scene covers (the reference would allocate them;
+// the oracle reports the blow-up instead of exhausting host memory).
+constexpr int64_t MAX_CELLS = 64ll << 20;
 
 enum Order : int { ORDER_REFERENCE = 0, ORDER_COLOUR = 1 };
 
@@ -668,15 +674,24 @@ public:
         const size_t table_size = table_mult * n;
         manifolds.clear();
         manifold_keys.clear();
+        contact_colour.clear();
+        contact_order.clear();
         if (n == 0) return OK;
 
         // SpatialHash.init (SpatialHash.zig:19-71)
         std::vector<size_t> table(table_size + 1, 0);
         std::vector<std::array<int64_t, 4>> ranges(n);
+        int64_t total_cells = 0;
         for (size_t b = 0; b < n; ++b) {
             int64_t r[4];
             if (!cell_range(bodies[b].aabb, r)) return ERR_NONFINITE_AABB;
             std::copy(r, r + 4, ranges[b].begin());
+            if (r[2] >= r[0] && r[3] >= r[1]) {
+                const double c = (double(r[2]) - double(r[0]) + 1.0) * (double(r[3]) - double(r[1]) + 1.0);
+                if (c > double(MAX_CELLS)) return ERR_CAPACITY;
+                total_cells += (int64_t)c;
+                if (total_cells > MAX_CELLS) return ERR_CAPACITY;
+            }
             for (int64_t yi = r[1]; yi <= r[3]; ++yi)
                 for (int64_t xi = r[0]; xi <= r[2]; ++xi) table[hash_cell(table_size, xi, yi)] += 1;
         }

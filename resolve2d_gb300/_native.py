@@ -42,6 +42,7 @@ class Config(C.Structure):
         ("spatialhash_table_size_mult", C.c_uint32),
         ("flags", C.c_uint32),
         ("stream", C.c_void_p),
+        ("capacity_scale", C.c_float),
     ]
 
 

@@ -11,8 +11,11 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <exception>
+#include <new>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <unordered_map>
@@ -102,6 +105,12 @@ struct Engine {
     r2d_config cfg{};
     cudaStream_t stream = nullptr;
     bool own_stream = false;
+    // Size classes run concurrently on auxiliary streams forked from and
+    // joined back into `stream`, so one class's tail overlaps the others.
+    static constexpr int NAUX = 4;
+    cudaStream_t aux[NAUX] = {};
+    cudaEvent_t ev_fork = nullptr, ev_join[NAUX] = {};
+    bool verbose = false;
     float cell = 4.0f;
     uint32_t table_mult = 2;
 
@@ -143,6 +152,22 @@ struct Engine {
     std::vector<int> status_h;
     bool pending = false;
 
+    // Calls enqueued since the last sync; a world that outgrows its class is
+    // frozen on the device and replayed from its failing call at sync.
+    struct CallRec {
+        float dt;
+        uint32_t sub_steps, iters;
+    };
+    std::vector<CallRec> calls;
+    uint32_t* d_fail_call = nullptr;
+    uint32_t* d_one = nullptr;          // single-world list for replays
+    uint32_t* d_capbits = nullptr;      // [nworlds] which buffers overflowed
+    unsigned long long* d_timers = nullptr;  // phase timers (R2D_PHASE_TIMERS builds)
+    // Doublings of each per-world buffer a world has needed (manifolds,
+    // points, cell entries, candidate pairs), packed one byte each.
+    std::vector<uint32_t> world_boost;
+    static uint32_t boost_of(uint32_t b, int i) { return (b >> (8 * i)) & 0xFFu; }
+
     ~Engine() {
         dfree(d_state); dfree(d_props); dfree(d_kind); dfree(d_ids); dfree(d_worlds);
         dfree(d_status); dfree(d_err);
@@ -150,6 +175,12 @@ struct Engine {
         dfree(d_jtype); dfree(d_jb1); dfree(d_jb2); dfree(d_jprm); dfree(d_excl);
         for (auto& c : classes) dfree(c.d_list);
         dfree(d_dbg_nman); dfree(d_dbg_keys); dfree(d_dbg_data); dfree(d_dbg_col); dfree(d_dbg_jcol);
+        dfree(d_fail_call); dfree(d_one); dfree(d_capbits); dfree(d_timers);
+        for (int a = 0; a < NAUX; ++a) {
+            if (aux[a]) cudaStreamDestroy(aux[a]);
+            if (ev_join[a]) cudaEventDestroy(ev_join[a]);
+        }
+        if (ev_fork) cudaEventDestroy(ev_fork);
         if (own_stream && stream) cudaStreamDestroy(stream);
     }
 
@@ -167,6 +198,13 @@ struct Engine {
         }
         CUDA_TRY(cudaMallocHost((void**)&h_err, sizeof(int)));
         CUDA_TRY(dalloc(d_err, 1));
+        for (int a = 0; a < NAUX; ++a) {
+            CUDA_TRY(cudaStreamCreateWithFlags(&aux[a], cudaStreamNonBlocking));
+            CUDA_TRY(cudaEventCreateWithFlags(&ev_join[a], cudaEventDisableTiming));
+        }
+        CUDA_TRY(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+        const char* v = getenv("R2D_VERBOSE");
+        verbose = v && v[0] && v[0] != '0';
         return R2D_OK;
     }
 
@@ -207,6 +245,16 @@ struct Engine {
         CUDA_TRY(dalloc(d_kind, n));
         CUDA_TRY(dalloc(d_ids, n));
         CUDA_TRY(dalloc(d_status, nw));
+        CUDA_TRY(dalloc(d_fail_call, nw));
+        CUDA_TRY(dalloc(d_capbits, nw));
+#ifdef R2D_PHASE_TIMERS
+        CUDA_TRY(dalloc(d_timers, (size_t)nw * PHASE_SLOTS));
+        CUDA_TRY(cudaMemsetAsync(d_timers, 0, sizeof(unsigned long long) * nw * PHASE_SLOTS, stream));
+#endif
+        CUDA_TRY(cudaMemsetAsync(d_fail_call, 0xFF, sizeof(uint32_t) * nw, stream));
+        world_boost.assign(nw, 0);
+        calls.clear();
+        pending = false;
         CUDA_TRY(cudaMemcpyAsync(d_state, state_h.data(), sizeof(float) * S_NFIELDS * n, cudaMemcpyHostToDevice, stream));
         CUDA_TRY(cudaMemcpyAsync(d_props, props_h.data(), sizeof(float) * P_NFIELDS * n, cudaMemcpyHostToDevice, stream));
         CUDA_TRY(cudaMemcpyAsync(d_kind, kind_h.data(), n, cudaMemcpyHostToDevice, stream));
@@ -292,14 +340,23 @@ struct Engine {
         return R2D_OK;
     }
 
-    // Capacity of a world class sized from the worlds it holds.
-    Caps caps_for(uint32_t nb, uint32_t max_nj, float rect_frac, uint32_t max_cells) const {
+    // Capacity of a world class sized from the worlds it holds.  Settled
+    // piles of the benchmark worlds peak near 2.8 manifolds and 3.1 contact
+    // points per body; a world that still outgrows a buffer is replayed with
+    // every capacity doubled (see sync), so these are sizes, not limits.
+    Caps caps_for(uint32_t nb, uint32_t max_nj, float rect_frac, uint32_t max_cells, uint32_t boost) const {
+        const double base = cfg.capacity_scale > 0.f ? cfg.capacity_scale : 1.0;
+        auto sz = [&](double v, int which) {
+            const double k = base * (double)(1u << boost_of(boost, which));
+            return (uint32_t)std::min(65535.0, std::max(4.0, std::ceil(v * k)));
+        };
         Caps c{};
         c.nb = nb;
-        c.nm = std::min<uint32_t>(65535u, 3u * nb + 32u);
-        c.npt = std::min<uint32_t>(65535u, (uint32_t)std::ceil(c.nm * (1.0f + std::min(1.0f, rect_frac + 0.15f))) + 16u);
-        c.ne = std::min<uint32_t>(65535u, std::max<uint32_t>(4u * nb + 64u, max_cells * 3u / 2u + 64u));
-        c.np = std::min<uint32_t>(65535u, 4u * nb + 32u);
+        c.nm = sz((11.0 * nb) / 4.0 + 16.0, 0);
+        const double ppm = 1.15 + (double)rect_frac * rect_frac;
+        c.npt = sz(((11.0 * nb) / 4.0 + 16.0) * ppm + 16.0, 1);
+        c.ne = sz(std::max(4.0 * nb + 64.0, max_cells * 1.5 + 64.0), 2);
+        c.np = sz(4.0 * nb + 32.0, 3);
         c.hs = next_pow2(2u * c.np);
         c.nj = max_nj;
         c.nt = table_mult * nb;
@@ -323,13 +380,31 @@ struct Engine {
         return c > 65535.0 ? 65535u : (uint32_t)c;
     }
 
+    int smem_limit() const {
+        int dev = 0, v = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        return v;
+    }
+
+    KClass* class_of(uint32_t w) {
+        for (auto& c : classes)
+            if (std::find(c.worlds.begin(), c.worlds.end(), w) != c.worlds.end()) return &c;
+        return nullptr;
+    }
+
     int plan() {
         for (auto& c : classes) dfree(c.d_list);
         classes.clear();
         // size classes by body count: bounds in bodies
-        static const uint32_t bounds[] = {32, 64, 96, 128, 160, 192, 256, 320, 384, 448, 512, 640, 768, 1024};
+        static const uint32_t bounds[] = {32, 64, 96, 128, 160, 192, 256, 320, 384, 448, 520};
         const int nbnd = sizeof(bounds) / sizeof(bounds[0]);
-        std::vector<std::vector<uint32_t>> groups(nbnd);
+        std::vector<uint32_t> boosts;  // distinct boost patterns in use
+        for (uint32_t w = 0; w < nworlds; ++w)
+            if (std::find(boosts.begin(), boosts.end(), world_boost[w]) == boosts.end()) boosts.push_back(world_boost[w]);
+        std::sort(boosts.begin(), boosts.end());
+        const int NBOOST = (int)boosts.size();
+        std::vector<std::vector<uint32_t>> groups(nbnd * NBOOST);
         for (uint32_t w = 0; w < nworlds; ++w) {
             const uint32_t n = worlds_h[w].n;
             int k = 0;
@@ -338,18 +413,18 @@ struct Engine {
                 return fail(R2D_ERR_CAPACITY, "world " + std::to_string(w) + " has " + std::to_string(n) +
                                                   " bodies; the fused kernel holds at most " +
                                                   std::to_string(bounds[nbnd - 1]));
-            groups[k].push_back(w);
+            const int bi = (int)(std::find(boosts.begin(), boosts.end(), world_boost[w]) - boosts.begin());
+            groups[k * NBOOST + bi].push_back(w);
         }
-        int dev = 0;
-        cudaGetDevice(&dev);
-        int smem_optin = 0;
-        cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        for (int k = 0; k < nbnd; ++k) {
-            if (groups[k].empty()) continue;
+        const int smem_optin = smem_limit();
+        for (int gk = 0; gk < nbnd * NBOOST; ++gk) {
+            const int k = gk / NBOOST;
+            const uint32_t boost = boosts[gk % NBOOST];
+            if (groups[gk].empty()) continue;
             KClass kc;
             uint32_t max_nj = 0, max_cells = 0;
             float rect_frac = 0.f;
-            for (uint32_t w : groups[k]) {
+            for (uint32_t w : groups[gk]) {
                 const WorldDesc& d = worlds_h[w];
                 max_nj = std::max(max_nj, d.nj);
                 uint32_t rects = 0, cells = 0;
@@ -360,20 +435,22 @@ struct Engine {
                 max_cells = std::max(max_cells, cells);
                 if (d.n) rect_frac = std::max(rect_frac, (float)rects / (float)d.n);
             }
-            kc.caps = caps_for(bounds[k], max_nj, rect_frac, max_cells);
+            kc.caps = caps_for(bounds[k], max_nj, rect_frac, max_cells, boost);
             kc.threads = bounds[k] <= 64 ? 64 : (bounds[k] <= 256 ? 128 : 256);
             kc.smem = make_layout(kc.caps).total;
             if ((int)kc.smem > smem_optin)
                 return fail(R2D_ERR_CAPACITY, "world class of " + std::to_string(bounds[k]) + " bodies needs " +
                                                   std::to_string(kc.smem) + " B of shared memory");
             // largest worlds first: the longest tasks start earliest
-            std::stable_sort(groups[k].begin(), groups[k].end(),
+            std::stable_sort(groups[gk].begin(), groups[gk].end(),
                              [&](uint32_t a, uint32_t b) { return worlds_h[a].n > worlds_h[b].n; });
-            kc.worlds = groups[k];
+            kc.worlds = groups[gk];
             CUDA_TRY(dalloc(kc.d_list, kc.worlds.size()));
             CUDA_TRY(cudaMemcpyAsync(kc.d_list, kc.worlds.data(), 4 * kc.worlds.size(), cudaMemcpyHostToDevice, stream));
             classes.push_back(std::move(kc));
         }
+        std::stable_sort(classes.begin(), classes.end(),
+                         [](const KClass& a, const KClass& b) { return a.caps.nb > b.caps.nb; });
         CUDA_TRY(dalloc(d_worlds, nworlds));
         CUDA_TRY(cudaMemcpyAsync(d_worlds, worlds_h.data(), sizeof(WorldDesc) * nworlds, cudaMemcpyHostToDevice, stream));
         // debug taps
@@ -411,6 +488,34 @@ struct Engine {
             if (st) return st;
         }
         if (!pending) CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), stream));
+        StepParams P = params(dt, sub_steps, iters, (uint32_t)calls.size());
+        calls.push_back(CallRec{dt, sub_steps, iters});
+        const int nused = (int)std::min<size_t>(classes.size(), (size_t)NAUX);
+        if (classes.size() == 1) {
+            P.world_list = classes[0].d_list;
+            P.nlist = (uint32_t)classes[0].worlds.size();
+            cudaError_t e = launch_world_step(P, classes[0].caps, classes[0].threads, stream);
+            if (e != cudaSuccess) return fail(R2D_ERR_CUDA, std::string("world step launch: ") + cudaGetErrorString(e));
+        } else if (nused > 1) {
+            CUDA_TRY(cudaEventRecord(ev_fork, stream));
+            for (int a = 0; a < nused; ++a) CUDA_TRY(cudaStreamWaitEvent(aux[a], ev_fork, 0));
+            for (size_t i = 0; i < classes.size(); ++i) {
+                const KClass& c = classes[i];
+                P.world_list = c.d_list;
+                P.nlist = (uint32_t)c.worlds.size();
+                cudaError_t e = launch_world_step(P, c.caps, c.threads, aux[i % NAUX]);
+                if (e != cudaSuccess) return fail(R2D_ERR_CUDA, std::string("world step launch: ") + cudaGetErrorString(e));
+            }
+            for (int a = 0; a < nused; ++a) {
+                CUDA_TRY(cudaEventRecord(ev_join[a], aux[a]));
+                CUDA_TRY(cudaStreamWaitEvent(stream, ev_join[a], 0));
+            }
+        }
+        pending = true;
+        return R2D_OK;
+    }
+
+    StepParams params(float dt, uint32_t sub_steps, uint32_t iters, uint32_t call_index) const {
         StepParams P{};
         P.worlds = d_worlds;
         P.state = d_state;
@@ -431,29 +536,128 @@ struct Engine {
         P.cell = cell;
         P.table_mult = table_mult;
         P.dbg = dbg;
-        for (auto& c : classes) {
-            P.world_list = c.d_list;
-            P.nlist = (uint32_t)c.worlds.size();
-            cudaError_t e = launch_world_step(P, c.caps, c.threads, stream);
-            if (e != cudaSuccess) return fail(R2D_ERR_CUDA, std::string("world step launch: ") + cudaGetErrorString(e));
-        }
-        pending = true;
-        return R2D_OK;
+        P.world_fail_call = d_fail_call;
+        P.world_capbits = d_capbits;
+        P.call_index = call_index;
+        P.timers = d_timers;
+        return P;
     }
 
     int sync() {
         CUDA_TRY(cudaStreamSynchronize(stream));
+#ifdef R2D_PHASE_TIMERS
+        dump_timers();
+#endif
         if (!pending) return R2D_OK;
         pending = false;
         CUDA_TRY(cudaMemcpy(h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost));
-        if (*h_err == 0) return R2D_OK;
+        if (*h_err == 0) {
+            calls.clear();
+            return R2D_OK;
+        }
+        std::vector<uint32_t> fail_call(nworlds);
         status_h.resize(nworlds);
         CUDA_TRY(cudaMemcpy(status_h.data(), d_status, sizeof(int) * nworlds, cudaMemcpyDeviceToHost));
-        for (uint32_t w = 0; w < nworlds; ++w)
-            if (status_h[w] != 0)
-                return fail(status_h[w], "world " + std::to_string(w) + " failed with status " +
-                                             std::to_string(status_h[w]));
-        return fail(R2D_ERR_CUDA, "device reported an error without a world status");
+        CUDA_TRY(cudaMemcpy(fail_call.data(), d_fail_call, sizeof(uint32_t) * nworlds, cudaMemcpyDeviceToHost));
+        int first_err = R2D_OK;
+        std::string first_msg;
+        for (uint32_t w = 0; w < nworlds && first_err == R2D_OK; ++w) {
+            if (fail_call[w] == 0xFFFFFFFFu) continue;
+            if (status_h[w] != DS_CAPACITY) {
+                first_err = status_h[w];
+                first_msg = "world " + std::to_string(w) + " failed with status " + std::to_string(status_h[w]);
+                break;
+            }
+            int st = replay_escalated(w, fail_call[w]);
+            if (st != R2D_OK) {
+                first_err = st;
+                first_msg = g_last_error;
+            }
+        }
+        calls.clear();
+        if (first_err != R2D_OK) return fail(first_err, first_msg);
+        plan_dirty = true;  // boosted worlds move to larger classes from the next call
+        return R2D_OK;
+    }
+
+#ifdef R2D_PHASE_TIMERS
+    // Per size class: mean cycles per world-step of each phase, and counts.
+    void dump_timers() {
+        std::vector<unsigned long long> t((size_t)nworlds * PHASE_SLOTS);
+        if (cudaMemcpy(t.data(), d_timers, 8 * t.size(), cudaMemcpyDeviceToHost) != cudaSuccess) return;
+        for (auto& c : classes) {
+            double acc[PHASE_SLOTS] = {0};
+            for (uint32_t w : c.worlds)
+                for (int k = 0; k < PHASE_SLOTS; ++k) acc[k] += (double)t[(size_t)w * PHASE_SLOTS + k];
+            const double steps = acc[11] > 0 ? acc[11] : 1;
+            fprintf(stderr, "r2d timers nb=%u thr=%d worlds=%zu smem=%u | load %.0f bp %.0f np %.0f col %.0f jcol %.0f "
+                            "solve %.0f wb %.0f cycles | pairs %.1f man %.1f colours %.1f rounds %.1f\n",
+                    c.caps.nb, c.threads, c.worlds.size(), c.smem, acc[0] / steps, acc[1] / steps, acc[2] / steps,
+                    acc[3] / steps, acc[4] / steps, acc[5] / steps, acc[6] / steps, acc[7] / steps, acc[8] / steps,
+                    acc[9] / steps, acc[10] / steps);
+        }
+        cudaMemset(d_timers, 0, 8 * t.size());
+    }
+#endif
+
+    // Re-run world w from call `from` to the last logged call with every
+    // capacity doubled, up to three times.  The world's state is exactly the
+    // state before its failing call (a failing world writes nothing back).
+    int replay_escalated(uint32_t w, uint32_t from) {
+        KClass* kc = class_of(w);
+        if (!kc) return fail(R2D_ERR_CAPACITY, "world " + std::to_string(w) + " has no class");
+        if (!d_one) CUDA_TRY(dalloc(d_one, 1));
+        CUDA_TRY(cudaMemcpyAsync(d_one, &w, sizeof(uint32_t), cudaMemcpyHostToDevice, stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        const WorldDesc& d = worlds_h[w];
+        uint32_t rects = 0, cells = 0;
+        for (uint32_t i = d.body_off; i < d.body_off + d.n; ++i) {
+            rects += (kind_h[i] & K_RECT) ? 1u : 0u;
+            cells += cells_of(i);
+        }
+        const float rf = d.n ? (float)rects / (float)d.n : 0.f;
+        uint32_t capbits = 0;
+        CUDA_TRY(cudaMemcpy(&capbits, d_capbits + w, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        uint32_t boost = world_boost[w];
+        for (int attempt = 0; attempt < 8; ++attempt) {
+            if (capbits & (CAP_BODIES | CAP_JOINTS | CAP_COLOURS)) break;  // not a buffer size
+            const int which[4] = {CAP_MANIFOLDS, CAP_POINTS, CAP_ENTRIES, CAP_PAIRS};
+            for (int i = 0; i < 4; ++i)
+                if ((capbits & which[i]) || (which[i] == CAP_MANIFOLDS && (capbits & CAP_POINTS)))
+                    boost += 1u << (8 * i);
+            Caps c = caps_for(kc->caps.nb, kc->caps.nj, rf, cells, boost);
+            if (verbose)
+                fprintf(stderr, "r2d: world %u (%u bodies) outgrew buffers 0x%x at call %u; replaying with "
+                                "manifolds %u points %u entries %u pairs %u (%u B shared)\n",
+                        w, d.n, capbits, from, c.nm, c.npt, c.ne, c.np, make_layout(c).total);
+            if ((int)make_layout(c).total > smem_limit()) break;
+            CUDA_TRY(cudaMemsetAsync(d_fail_call + w, 0xFF, sizeof(uint32_t), stream));
+            CUDA_TRY(cudaMemsetAsync(d_capbits + w, 0, sizeof(uint32_t), stream));
+            CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), stream));
+            for (uint32_t k = from; k < calls.size(); ++k) {
+                StepParams P = params(calls[k].dt, calls[k].sub_steps, calls[k].iters, k);
+                P.world_list = d_one;
+                P.nlist = 1;
+                cudaError_t e = launch_world_step(P, c, kc->threads, stream);
+                if (e != cudaSuccess) return fail(R2D_ERR_CUDA, std::string("replay launch: ") + cudaGetErrorString(e));
+            }
+            CUDA_TRY(cudaStreamSynchronize(stream));
+            CUDA_TRY(cudaMemcpy(h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost));
+            if (*h_err == 0) {
+                world_boost[w] = boost;
+                return R2D_OK;
+            }
+            int st = 0;
+            uint32_t fc = 0;
+            CUDA_TRY(cudaMemcpy(&st, d_status + w, sizeof(int), cudaMemcpyDeviceToHost));
+            CUDA_TRY(cudaMemcpy(&fc, d_fail_call + w, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+            CUDA_TRY(cudaMemcpy(&capbits, d_capbits + w, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+            if (st != DS_CAPACITY)
+                return fail(st, "world " + std::to_string(w) + " failed with status " + std::to_string(st));
+            from = fc;
+        }
+        return fail(R2D_ERR_CAPACITY, "world " + std::to_string(w) +
+                                          " outgrew the largest shared-memory budget of the fused kernel");
     }
 
     int world_status(int* out) {
@@ -493,6 +697,20 @@ struct Engine {
         return R2D_OK;
     }
 };
+
+// No C++ exception may cross the C ABI: allocation failures become statuses.
+template <class F>
+int guarded(F f) {
+    try {
+        return f();
+    } catch (const std::bad_alloc&) {
+        return fail(R2D_ERR_OUT_OF_MEMORY, "host allocation failed");
+    } catch (const std::exception& e) {
+        return fail(R2D_ERR_INVALID_ARGUMENT, e.what());
+    } catch (...) {
+        return fail(R2D_ERR_INVALID_ARGUMENT, "unexpected exception");
+    }
+}
 
 }  // namespace
 
@@ -546,7 +764,7 @@ R2D_API int r2d_solver_set_bodies(r2d_solver* s, uint32_t n, const uint32_t* ids
     if (n > 65535u) return fail(R2D_ERR_CAPACITY, "a world holds at most 65535 bodies");
     const uint32_t off[2] = {0, n};
     const float* g = s->gravity.empty() ? nullptr : s->gravity.data();
-    int st = s->eng.set_bodies(1, off, ids, kind, props, state, g, (uint32_t)s->gravity.size(), init_aabb);
+    int st = guarded([&] { return s->eng.set_bodies(1, off, ids, kind, props, state, g, (uint32_t)s->gravity.size(), init_aabb); });
     if (st) return st;
     s->constraints_dirty = true;
     return R2D_OK;
@@ -554,12 +772,12 @@ R2D_API int r2d_solver_set_bodies(r2d_solver* s, uint32_t n, const uint32_t* ids
 
 R2D_API int r2d_solver_write_state(r2d_solver* s, const float* state) {
     if (!s || !state) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
-    return s->eng.write_state(state);
+    return guarded([&] { return s->eng.write_state(state); });
 }
 
 R2D_API int r2d_solver_read_state(r2d_solver* s, float* state) {
     if (!s || !state) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
-    return s->eng.read_state(state);
+    return guarded([&] { return s->eng.read_state(state); });
 }
 
 R2D_API int r2d_solver_set_gravity(r2d_solver* s, uint32_t n, const float* g) {
@@ -632,31 +850,31 @@ R2D_API int r2d_solver_process(r2d_solver* s, float dt, uint32_t sub_steps, uint
     if (!s) return fail(R2D_ERR_INVALID_ARGUMENT, "solver is NULL");
     if (s->eng.nworlds == 0) return R2D_OK;  // no bodies: nothing to step
     if (s->constraints_dirty) {
-        int st = solver_resolve(s);
+        int st = guarded([&] { return solver_resolve(s); });
         if (st) return st;
         s->constraints_dirty = false;
     }
-    return s->eng.process(dt, sub_steps, collision_iters);
+    return guarded([&] { return s->eng.process(dt, sub_steps, collision_iters); });
 }
 
 R2D_API int r2d_solver_sync(r2d_solver* s) {
     if (!s) return fail(R2D_ERR_INVALID_ARGUMENT, "solver is NULL");
-    return s->eng.sync();
+    return guarded([&] { return s->eng.sync(); });
 }
 
 R2D_API int r2d_solver_num_manifolds(r2d_solver* s, uint32_t* out) {
     if (!s || !out) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
-    return s->eng.num_manifolds(0, out);
+    return guarded([&] { return s->eng.num_manifolds(0, out); });
 }
 
 R2D_API int r2d_solver_get_manifolds(r2d_solver* s, uint32_t cap, uint32_t* keys, float* data, uint32_t* colours) {
     if (!s) return fail(R2D_ERR_INVALID_ARGUMENT, "solver is NULL");
-    return s->eng.get_manifolds(0, cap, keys, data, colours);
+    return guarded([&] { return s->eng.get_manifolds(0, cap, keys, data, colours); });
 }
 
 R2D_API int r2d_solver_get_joint_colours(r2d_solver* s, uint32_t cap, uint32_t* colours) {
     if (!s || !colours) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
-    return s->eng.get_joint_colours(0, cap, colours);
+    return guarded([&] { return s->eng.get_joint_colours(0, cap, colours); });
 }
 
 // ---------------------------------------------------------------------------
@@ -689,7 +907,7 @@ R2D_API int r2d_batch_set_worlds(r2d_batch* b, uint32_t nworlds, const uint32_t*
     if (!b || !body_off || (nworlds && (!gravity))) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
     const uint32_t n = body_off[nworlds];
     if (n && (!ids || !kind || !props || !state)) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
-    int st = b->eng.set_bodies(nworlds, body_off, ids, kind, props, state, gravity, 1, init_aabb);
+    int st = guarded([&] { return b->eng.set_bodies(nworlds, body_off, ids, kind, props, state, gravity, 1, init_aabb); });
     if (st) return st;
     for (auto& d : b->eng.worlds_h) {  // gravity 0 means no generator
         if (d.g[0] == 0.f) d.ngrav = 0;
@@ -698,28 +916,28 @@ R2D_API int r2d_batch_set_worlds(r2d_batch* b, uint32_t nworlds, const uint32_t*
     std::vector<uint8_t> e8;
     std::vector<uint16_t> e16;
     std::vector<float> ef;
-    return b->eng.set_constraints(e32, e8, e16, e16, ef, e32, e32);
+    return guarded([&] { return b->eng.set_constraints(e32, e8, e16, e16, ef, e32, e32); });
 }
 
 R2D_API int r2d_batch_write_state(r2d_batch* b, const float* state) {
     if (!b || !state) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
-    return b->eng.write_state(state);
+    return guarded([&] { return b->eng.write_state(state); });
 }
 
 R2D_API int r2d_batch_read_state(r2d_batch* b, float* state) {
     if (!b || !state) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
-    return b->eng.read_state(state);
+    return guarded([&] { return b->eng.read_state(state); });
 }
 
 R2D_API int r2d_batch_process(r2d_batch* b, float dt, uint32_t sub_steps, uint32_t collision_iters) {
     if (!b) return fail(R2D_ERR_INVALID_ARGUMENT, "batch is NULL");
     if (b->eng.nworlds == 0) return R2D_OK;
-    return b->eng.process(dt, sub_steps, collision_iters);
+    return guarded([&] { return b->eng.process(dt, sub_steps, collision_iters); });
 }
 
 R2D_API int r2d_batch_sync(r2d_batch* b) {
     if (!b) return fail(R2D_ERR_INVALID_ARGUMENT, "batch is NULL");
-    return b->eng.sync();
+    return guarded([&] { return b->eng.sync(); });
 }
 
 R2D_API int r2d_batch_launches_per_step(r2d_batch* b, uint32_t* out) {
@@ -734,18 +952,18 @@ R2D_API int r2d_batch_launches_per_step(r2d_batch* b, uint32_t* out) {
 
 R2D_API int r2d_batch_world_status(r2d_batch* b, int* status) {
     if (!b || !status) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
-    return b->eng.world_status(status);
+    return guarded([&] { return b->eng.world_status(status); });
 }
 
 R2D_API int r2d_batch_num_manifolds(r2d_batch* b, uint32_t w, uint32_t* out) {
     if (!b || !out) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
-    return b->eng.num_manifolds(w, out);
+    return guarded([&] { return b->eng.num_manifolds(w, out); });
 }
 
 R2D_API int r2d_batch_get_manifolds(r2d_batch* b, uint32_t w, uint32_t cap, uint32_t* keys, float* data,
                                     uint32_t* colours) {
     if (!b) return fail(R2D_ERR_INVALID_ARGUMENT, "batch is NULL");
-    return b->eng.get_manifolds(w, cap, keys, data, colours);
+    return guarded([&] { return b->eng.get_manifolds(w, cap, keys, data, colours); });
 }
 
 }  // extern "C"

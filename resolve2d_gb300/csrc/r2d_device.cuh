@@ -112,6 +112,15 @@ R2D_DF void rect_half_extents(float width, float height, float c, float s, float
     *hh = eh;
 }
 
+// a[i] for a runtime i without dynamic indexing (keeps a[] in registers)
+R2D_DF f2 sel4(const f2 a[4], uint32_t i) {
+    f2 r = a[0];
+    r = i == 1u ? a[1] : r;
+    r = i == 2u ? a[2] : r;
+    r = i == 3u ? a[3] : r;
+    return r;
+}
+
 // ---- narrowphase geometry ----
 // One body as the SAT sees it.  For a rectangle the world vertices
 // (Rectangle.zig:88-98) and edge normals (Rectangle.zig:132-151) are
@@ -188,7 +197,9 @@ R2D_DF bool overlap_sat(SatState& ret, const Geo& R, const Geo& I, bool r_is_o1)
     const int nn = R.rect ? 4 : 1;
     f2 disc_axis = {0.f, 0.f};
     if (!R.rect) disc_axis = normalize2(sub2(closest_point(I, R.pos), R.pos));  // Disc.zig:86-90
-    for (int it = 0; it < nn; ++it) {
+#pragma unroll
+    for (int it = 0; it < 4; ++it) {
+        if (it >= nn) break;
         f2 normal = R.rect ? R.en[it] : disc_axis;
         bool flipped = false;
         if (dot2(normal, sub2(I.pos, R.pos)) < 0.0f) {  // normalShouldFlipSAT (:221-226)
@@ -293,23 +304,24 @@ R2D_DF void clip_line_to_line(f2 aa, f2 ab, f2 ba, f2 bb, f2* p1o, f2* p2o) {
 R2D_DF int identify_points(const Geo& ref, const Geo& inc, uint32_t refid, NewPoint out[2]) {
     if (!ref.rect) {
         f2 pos = closest_point(inc, ref.pos);
-        f2 normal = normalize2(sub2(closest_point(inc, ref.pos), ref.pos));
+        f2 normal = normalize2(sub2(pos, ref.pos));  // Disc.getNormal recomputes the same point
         if (dot2(normal, sub2(inc.pos, ref.pos)) < 0.0f) normal = neg_by_mul(normal);
         float dot = dot2(normal, sub2(pos, ref.pos));
         float depth = dot - ref.radius;
         out[0] = make_point(pos, depth, ref.pos, inc.pos, normal);
         return 1;
     }
-    const f2 ea = ref.wv[refid];
-    const f2 eb = ref.wv[(refid + 1) & 3];
-    const f2 ndir = ref.en[refid];
+    const f2 ea = sel4(ref.wv, refid);
+    const f2 eb = sel4(ref.wv, (refid + 1) & 3);
+    const f2 ndir = sel4(ref.en, refid);
     if (!inc.rect) {
         f2 pos = addmult2(inc.pos, ndir, -inc.radius);
         float dot = dot2(sub2(pos, ea), ndir);
         out[0] = make_point(pos, dot, ref.pos, inc.pos, ndir);
         return 1;
     }
-    int best = -1;
+    uint32_t best = 0;
+    bool found = false;
     float best_dot = __int_as_float(0x7f800000);
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
@@ -317,17 +329,50 @@ R2D_DF int identify_points(const Geo& ref, const Geo& inc, uint32_t refid, NewPo
         if (d < best_dot) {
             best_dot = d;
             best = i;
+            found = true;
         }
     }
-    if (best < 0) best = 0;  // every dot NaN: the reference reads an undefined edge
+    if (!found) best = 0;  // every dot NaN: the reference reads an undefined edge
     f2 pa, pb;
-    clip_line_to_line(ea, eb, inc.wv[best], inc.wv[(best + 1) & 3], &pa, &pb);
-    int n = 0;
-    float dot = dot2(sub2(pa, ea), ndir);
-    if (dot < COLLISION_MARGIN) out[n++] = make_point(pa, dot, ref.pos, inc.pos, ndir);
-    dot = dot2(sub2(pb, eb), ndir);
-    if (dot < COLLISION_MARGIN) out[n++] = make_point(pb, dot, ref.pos, inc.pos, ndir);
-    return n;
+    clip_line_to_line(ea, eb, sel4(inc.wv, best), sel4(inc.wv, (best + 1) & 3), &pa, &pb);
+    const float dot_a = dot2(sub2(pa, ea), ndir);
+    const float dot_b = dot2(sub2(pb, eb), ndir);
+    const bool ha = dot_a < COLLISION_MARGIN, hb = dot_b < COLLISION_MARGIN;
+    if (ha) {
+        out[0] = make_point(pa, dot_a, ref.pos, inc.pos, ndir);
+        if (hb) out[1] = make_point(pb, dot_b, ref.pos, inc.pos, ndir);
+    } else if (hb) {
+        out[0] = make_point(pb, dot_b, ref.pos, inc.pos, ndir);
+    }
+    return (ha ? 1 : 0) + (hb ? 1 : 0);
 }
+
+// A set of colours 0..255 held in eight registers.
+struct ColourSet {
+    uint32_t w0 = 0u, w1 = 0u, w2 = 0u, w3 = 0u, w4 = 0u, w5 = 0u, w6 = 0u, w7 = 0u;
+    R2D_DF void add(uint32_t c) {
+        const uint32_t bit = 1u << (c & 31u), wd = c >> 5;
+        w0 |= wd == 0u ? bit : 0u;
+        w1 |= wd == 1u ? bit : 0u;
+        w2 |= wd == 2u ? bit : 0u;
+        w3 |= wd == 3u ? bit : 0u;
+        w4 |= wd == 4u ? bit : 0u;
+        w5 |= wd == 5u ? bit : 0u;
+        w6 |= wd == 6u ? bit : 0u;
+        w7 |= wd == 7u ? bit : 0u;
+    }
+    // lowest colour not in the set; >= limit means none is free below limit
+    R2D_DF uint32_t first_free() const {
+        if (w0 != 0xFFFFFFFFu) return (uint32_t)__ffs(~w0) - 1u;
+        if (w1 != 0xFFFFFFFFu) return 32u + (uint32_t)__ffs(~w1) - 1u;
+        if (w2 != 0xFFFFFFFFu) return 64u + (uint32_t)__ffs(~w2) - 1u;
+        if (w3 != 0xFFFFFFFFu) return 96u + (uint32_t)__ffs(~w3) - 1u;
+        if (w4 != 0xFFFFFFFFu) return 128u + (uint32_t)__ffs(~w4) - 1u;
+        if (w5 != 0xFFFFFFFFu) return 160u + (uint32_t)__ffs(~w5) - 1u;
+        if (w6 != 0xFFFFFFFFu) return 192u + (uint32_t)__ffs(~w6) - 1u;
+        if (w7 != 0xFFFFFFFFu) return 224u + (uint32_t)__ffs(~w7) - 1u;
+        return 256u;
+    }
+};
 
 }  // namespace r2d

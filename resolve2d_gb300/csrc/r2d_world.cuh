@@ -51,7 +51,7 @@ struct Layout {
     uint32_t px, py, ang, mx, my, L, mass, inertia, inv_m, inv_i, cs, sn, ang_prev, tq, kind;
     // manifolds + points (narrowphase .. end) -- aliased by the broadphase scratch
     uint32_t ma, mb, mp0, mnp, mcol, nx, ny, fric;
-    uint32_t r1x, r1y, r2x, r2y, depth, odepth, mn, mt, apn, apt;
+    uint32_t r1x, r1y, r2x, r2y, depth, odepth, mn, mt, apn, apt, bias;
     // broadphase scratch (inside the manifold region)
     uint32_t ax, ay, ahw, ahh, rx0, ry0, rx1, ry1, bcnt, ebucket, ebody, eslot, sbody, table, hset;
     // colouring scratch
@@ -88,7 +88,7 @@ __host__ __device__ inline Layout make_layout(const Caps& c) {
     L.nx = take(nm4); L.ny = take(nm4); L.fric = take(nm4);
     L.r1x = take(np4); L.r1y = take(np4); L.r2x = take(np4); L.r2y = take(np4);
     L.depth = take(np4); L.odepth = take(np4); L.mn = take(np4); L.mt = take(np4);
-    L.apn = take(np4); L.apt = take(np4);
+    L.apn = take(np4); L.apt = take(np4); L.bias = take(np4);
     const uint32_t xend_m = o;
     o = xbase;
     L.ax = take(nb4); L.ay = take(nb4); L.ahw = take(nb4); L.ahh = take(nb4);
@@ -101,19 +101,22 @@ __host__ __device__ inline Layout make_layout(const Caps& c) {
     const uint32_t xend_bp = o;
     o = xend_m > xend_bp ? xend_m : xend_bp;
 
-    // colouring scratch
-    const uint32_t ncon = c.nm > c.nj ? c.nm : c.nj;
-    L.adj = take(4 * (c.nb + 1));
-    L.adjl = take(2 * 2 * ncon);
-    L.prio = take(8 * ncon);
     // orders
     L.corder = take(2 * c.nm);
     L.coff = take(2 * (MAX_COLOURS + 2));
     L.jorder = take(2 * (c.nj ? c.nj : 1));
     L.joff = take(2 * (MAX_COLOURS + 2));
     L.jcol = take(c.nj ? c.nj : 1);
-    // pairs
+    // candidate pairs (broadphase -> narrowphase), then the colouring scratch
+    const uint32_t ybase = o;
     L.pairs = take(4 * c.np);
+    const uint32_t yend_pairs = o;
+    o = ybase;
+    const uint32_t ncon = c.nm > c.nj ? c.nm : c.nj;
+    L.adj = take(4 * (c.nb + 1));
+    L.adjl = take(2 * 2 * ncon);
+    L.prio = take(4 * ncon);
+    o = o > yend_pairs ? o : yend_pairs;
     L.total = o;
     return L;
 }
@@ -143,12 +146,27 @@ struct StepParams {
     const float* jprm;           // [njoints][JOINT_PARAMS]
     const uint32_t* excl;        // sorted (lo << 16 | hi) per world
     int* world_status;           // [nworlds]
+    uint32_t* world_fail_call;   // [nworlds] first call a world failed in; ~0u = healthy
+    uint32_t* world_capbits;     // [nworlds] CAP_* bits of the buffers that overflowed
     int* error_count;
+    uint32_t call_index;         // position of this launch in the calls since the last sync
+    unsigned long long* timers;  // [nworlds][PHASE_SLOTS] when built with R2D_PHASE_TIMERS
     float dt;
     uint32_t sub_steps, iters;
     float cell;
     uint32_t table_mult;
     DebugOut dbg;
+};
+
+// Phase timer slots (cycles, R2D_PHASE_TIMERS builds only): load,
+// broadphase, narrowphase, contact colouring, joint colouring, solve,
+// write-back, then counts: pairs, manifolds, colours, colouring rounds.
+constexpr int PHASE_SLOTS = 12;
+
+// Which per-world buffer overflowed (reported with DS_CAPACITY).
+enum CapBits : uint32_t {
+    CAP_BODIES = 1u, CAP_MANIFOLDS = 2u, CAP_POINTS = 4u, CAP_ENTRIES = 8u,
+    CAP_PAIRS = 16u, CAP_COLOURS = 32u, CAP_JOINTS = 64u
 };
 
 enum DeviceStatus : int {

@@ -86,17 +86,9 @@ __device__ __forceinline__ bool excluded(const uint32_t* ex, uint32_t n, uint32_
 }
 
 __device__ __forceinline__ void set_err(int* s_err, int code) { atomicCAS(s_err, 0, code); }
-
-// First colour not marked in the 256-bit set; 255 when all of 0..253 are taken.
-__device__ __forceinline__ uint32_t first_free(const uint32_t bits[8]) {
-#pragma unroll
-    for (int wd = 0; wd < 8; ++wd) {
-        if (bits[wd] != 0xFFFFFFFFu) {
-            uint32_t c = wd * 32 + __ffs(~bits[wd]) - 1;
-            return c < (uint32_t)MAX_COLOURS ? c : 255u;
-        }
-    }
-    return 255u;
+__device__ __forceinline__ void cap_fail(int* err, uint32_t* s_capbits, uint32_t bit) {
+    *err = DS_CAPACITY;
+    atomicOr(s_capbits, bit);
 }
 
 // Shared-memory views of one world.
@@ -106,11 +98,11 @@ struct SW {
     uint16_t *ma, *mb, *mp0;
     uint8_t *mnp, *mcol;
     float *nx, *ny, *fric;
-    float *r1x, *r1y, *r2x, *r2y, *depth, *odepth, *mn, *mt, *apn, *apt;
+    float *r1x, *r1y, *r2x, *r2y, *depth, *odepth, *mn, *mt, *apn, *apt, *bias;
 };
 
 // CollisionManifold.calculateImpulses (collision.zig:135-218)
-__device__ __forceinline__ void solve_contact(const SW& s, uint32_t m, float h) {
+__device__ __forceinline__ void solve_contact(const SW& s, uint32_t m) {
     const uint32_t a = s.ma[m], b = s.mb[m];
     const bool sa = s.kind[a] & K_STATIC, sb = s.kind[b] & K_STATIC;
     const float inv_m1 = s.inv_m[a], inv_m2 = s.inv_m[b];
@@ -137,8 +129,7 @@ __device__ __forceinline__ void solve_contact(const SW& s, uint32_t m, float h) 
         const f2 v1 = add2(vlinear_1, f2{-r1.y * omega1, r1.x * omega1});
         const f2 v2 = add2(vlinear_2, f2{-r2.y * omega2, r2.x * omega2});
         const f2 dv = sub2(v1, v2);
-        const float bias = BAUMGARTE * zmax(0.0f, (-d) - BAUMGARTE_SLOP) / h;
-        float num = dot2(dv, n) + bias;
+        float num = dot2(dv, n) + s.bias[p];  // BAUMGARTE*max(0,-depth-SLOP)/h, set in the prestep
         const float pn = num * s.mn[p];
         if (pn < MIN_MANIFOLD_IMPULSE) continue;
         num = dot2(dv, t);
@@ -285,6 +276,7 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
     __shared__ uint32_t s_wsum[32];
     __shared__ uint32_t s_ccnt[256];
     __shared__ int s_err;
+    __shared__ uint32_t s_capbits;
     __shared__ uint32_t s_cnt[4];  // pairs, manifolds, points
 
     const int tid = threadIdx.x;
@@ -293,18 +285,41 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
     const WorldDesc wd = P.worlds[w];
     const uint32_t n = wd.n, base = wd.body_off, NB = P.nbodies;
     const uint32_t T = P.table_mult * n;
+    // A world that failed earlier in this batch of calls stays frozen (its
+    // state untouched) until the host replays it with larger capacities.
+    if (P.world_fail_call[w] != 0xFFFFFFFFu) return;
     if (n > C.nb || wd.nj > C.nj || T > C.nt || n > 65535u) {
         if (tid == 0) {
             P.world_status[w] = DS_CAPACITY;
+            P.world_capbits[w] = (n > C.nb || T > C.nt || n > 65535u ? CAP_BODIES : 0u) | (wd.nj > C.nj ? CAP_JOINTS : 0u);
+            P.world_fail_call[w] = P.call_index;
             atomicAdd(P.error_count, 1);
         }
         return;
     }
     if (tid == 0) {
         s_err = 0;
+        s_capbits = 0u;
         s_cnt[0] = s_cnt[1] = s_cnt[2] = s_cnt[3] = 0;
     }
     int err = 0;
+#ifdef R2D_PHASE_TIMERS
+    long long t_mark = clock64();
+    uint32_t jp_rounds = 0;
+#define PHASE(k)                                                              \
+    do {                                                                      \
+        __syncthreads();                                                      \
+        if (tid == 0 && P.timers) {                                           \
+            const long long t_now = clock64();                                \
+            P.timers[(size_t)w * PHASE_SLOTS + (k)] += (unsigned long long)(t_now - t_mark); \
+            t_mark = t_now;                                                   \
+        }                                                                     \
+    } while (0)
+#else
+#define PHASE(k) \
+    do {         \
+    } while (0)
+#endif
 
 #define SMF(off) reinterpret_cast<float*>(sm + (off))
 #define SMU32(off) reinterpret_cast<uint32_t*>(sm + (off))
@@ -323,7 +338,7 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
     s.nx = SMF(Lo.nx); s.ny = SMF(Lo.ny); s.fric = SMF(Lo.fric);
     s.r1x = SMF(Lo.r1x); s.r1y = SMF(Lo.r1y); s.r2x = SMF(Lo.r2x); s.r2y = SMF(Lo.r2y);
     s.depth = SMF(Lo.depth); s.odepth = SMF(Lo.odepth); s.mn = SMF(Lo.mn); s.mt = SMF(Lo.mt);
-    s.apn = SMF(Lo.apn); s.apt = SMF(Lo.apt);
+    s.apn = SMF(Lo.apn); s.apt = SMF(Lo.apt); s.bias = SMF(Lo.bias);
 
     float *ax = SMF(Lo.ax), *ay = SMF(Lo.ay), *ahw = SMF(Lo.ahw), *ahh = SMF(Lo.ahh);
     int32_t *rx0 = SMI32(Lo.rx0), *ry0 = SMI32(Lo.ry0), *rx1 = SMI32(Lo.rx1), *ry1 = SMI32(Lo.ry1);
@@ -334,7 +349,7 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
     uint32_t* hset = SMU32(Lo.hset);
     uint32_t* adj = SMU32(Lo.adj);
     uint16_t* adjl = SMU16(Lo.adjl);
-    unsigned long long* prio = reinterpret_cast<unsigned long long*>(sm + Lo.prio);
+    uint32_t* prio = SMU32(Lo.prio);
     uint16_t *corder = SMU16(Lo.corder), *coff = SMU16(Lo.coff);
     uint16_t *jorder = SMU16(Lo.jorder), *joff = SMU16(Lo.joff);
     uint8_t* jcol = SMU8(Lo.jcol);
@@ -376,6 +391,7 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
     for (uint32_t b = tid; b < T + 1; b += NT) table[b] = 0u;
     for (uint32_t b = tid; b < C.hs; b += NT) hset[b] = 0xFFFFFFFFu;
     __syncthreads();
+    PHASE(0);
 
     // ---------------- broadphase (SpatialHash.zig:19-137, lib.zig:264-282) ----------------
     for (uint32_t i = tid; i < n; i += NT) {
@@ -388,7 +404,7 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
             x1 = x0 - 1;
         } else if (x1 >= x0 && y1 >= y0) {
             const int64_t c64 = ((int64_t)x1 - (int64_t)x0 + 1) * ((int64_t)y1 - (int64_t)y0 + 1);
-            if (c64 > (int64_t)C.ne) err = DS_CAPACITY;
+            if (c64 > (int64_t)C.ne) cap_fail(&err, &s_capbits, CAP_ENTRIES);
             else cnt = (uint32_t)c64;
         }
         rx0[i] = x0; ry0[i] = y0; rx1[i] = x1; ry1[i] = y1;
@@ -399,7 +415,10 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
     {
         const uint32_t E = block_scan_excl<NT>(bcnt, n, s_wsum);
         if (E > C.ne) {
-            if (tid == 0) s_err = DS_CAPACITY;
+            if (tid == 0) {
+                s_err = DS_CAPACITY;
+                s_capbits |= CAP_ENTRIES;
+            }
             __syncthreads();
             goto fail;
         }
@@ -442,7 +461,9 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
                 if (hs_insert(hset, C.hs - 1u, key, &err)) {
                     const uint32_t idx = atomicAdd(&s_cnt[0], 1u);
                     if (idx < C.np) pairs[idx] = key;
-                    else err = DS_CAPACITY;
+                    else cap_fail(&err, &s_capbits, CAP_PAIRS);
+                } else if (err) {
+                    atomicOr(&s_capbits, (uint32_t)CAP_PAIRS);
                 }
             }
         }
@@ -450,6 +471,7 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
     if (err) set_err(&s_err, err);
     if (__syncthreads_or(err != 0)) goto fail;
 
+    PHASE(1);
     // ---------------- narrowphase (collision.zig:299-320, lib.zig:284-294) ----------------
     {
         const uint32_t npairs = s_cnt[0];
@@ -471,12 +493,12 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
                                              : identify_points(g2, g1, sat.refid, pts);
             const uint32_t m = atomicAdd(&s_cnt[1], 1u);
             if (m >= C.nm) {
-                err = DS_CAPACITY;
+                cap_fail(&err, &s_capbits, CAP_MANIFOLDS);
                 continue;
             }
             const uint32_t p0 = atomicAdd(&s_cnt[2], (uint32_t)npt);
             if (p0 + npt > C.npt) {
-                err = DS_CAPACITY;
+                cap_fail(&err, &s_capbits, CAP_POINTS);
                 continue;
             }
             s.ma[m] = (uint16_t)ref;
@@ -485,7 +507,9 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
             s.mnp[m] = (uint8_t)npt;
             s.nx[m] = sat.normal.x;
             s.ny[m] = sat.normal.y;
-            for (int k = 0; k < npt; ++k) {
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                if (k >= npt) break;
                 s.r1x[p0 + k] = pts[k].ref_r.x;
                 s.r1y[p0 + k] = pts[k].ref_r.y;
                 s.r2x[p0 + k] = pts[k].inc_r.x;
@@ -500,6 +524,7 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
     if (err) set_err(&s_err, err);
     if (__syncthreads_or(err != 0)) goto fail;
 
+    PHASE(2);
     {
         const uint32_t M = min(s_cnt[1], C.nm);
         const uint32_t NJ = wd.nj;
@@ -519,8 +544,7 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
             const uint32_t a = s.ma[m], b = s.mb[m];
             if (!(s.kind[a] & K_STATIC)) adjl[atomicAdd(&adj[a], 1u)] = (uint16_t)m;
             if (!(s.kind[b] & K_STATIC)) adjl[atomicAdd(&adj[b], 1u)] = (uint16_t)m;
-            const uint32_t lo = min(a, b), hi = max(a, b);
-            prio[m] = ((unsigned long long)r2d_colour_mix(lo, hi) << 32) | ((lo << 16) | hi);
+            prio[m] = r2d_colour_mix(min(a, b), max(a, b));
             s.mcol[m] = 0xFFu;
         }
         __syncthreads();  // adj[i] = one past body i's last adjacency slot
@@ -528,33 +552,47 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
             int pending = 0;
             for (uint32_t m = tid; m < M; m += NT) {
                 if (((volatile uint8_t*)s.mcol)[m] != 0xFFu) continue;
-                uint32_t bits[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+                ColourSet used;
                 bool ready = true;
-                const unsigned long long pm = prio[m];
-                const uint32_t ends[2] = {s.ma[m], s.mb[m]};
-                for (int e2 = 0; e2 < 2 && ready; ++e2) {
-                    const uint32_t x = ends[e2];
-                    if (s.kind[x] & K_STATIC) continue;
+                const uint32_t pm = prio[m];
+                const uint32_t ea = s.ma[m], eb = s.mb[m];
+                const uint32_t km = (min(ea, eb) << 16) | max(ea, eb);
+#pragma unroll
+                for (int e2 = 0; e2 < 2; ++e2) {
+                    const uint32_t x = e2 ? eb : ea;
+                    if (!ready || (s.kind[x] & K_STATIC)) continue;
                     const uint32_t q0 = x ? adj[x - 1] : 0u, q1 = adj[x];
                     for (uint32_t q = q0; q < q1; ++q) {
                         const uint32_t o = adjl[q];
-                        if (o == m || prio[o] > pm) continue;
+                        if (o == m) continue;
+                        const uint32_t po = prio[o];
+                        if (po > pm) continue;
+                        if (po == pm) {  // equal hashes: the smaller (lo, hi) key goes first
+                            const uint32_t oa = s.ma[o], ob = s.mb[o];
+                            if (((min(oa, ob) << 16) | max(oa, ob)) > km) continue;
+                        }
                         const uint8_t c = ((volatile uint8_t*)s.mcol)[o];
                         if (c == 0xFFu) {
                             ready = false;
                             break;
                         }
-                        bits[c >> 5] |= 1u << (c & 31);
+                        used.add(c);
                     }
                 }
                 if (ready) {
-                    const uint32_t c = first_free(bits);
-                    if (c == 255u) err = DS_CAPACITY;
+                    uint32_t c = used.first_free();
+                    if (c >= (uint32_t)MAX_COLOURS) {
+                        cap_fail(&err, &s_capbits, CAP_COLOURS);
+                        c = 0;
+                    }
                     ((volatile uint8_t*)s.mcol)[m] = (uint8_t)c;
                 } else {
                     pending = 1;
                 }
             }
+#ifdef R2D_PHASE_TIMERS
+            ++jp_rounds;
+#endif
             if (!__syncthreads_or(pending)) break;
         }
         if (err) set_err(&s_err, err);
@@ -571,6 +609,7 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
         __syncthreads();
         for (uint32_t m = tid; m < M; m += NT) corder[atomicAdd(&s_ccnt[s.mcol[m]], 1u)] = (uint16_t)m;
 
+        PHASE(3);
         // ---------------- joint colouring ----------------
         if (NJ) {
             const uint32_t j0 = wd.joint_off;
@@ -590,7 +629,7 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
                 const uint32_t b1 = __ldg(P.jb1 + j0 + j), b2 = __ldg(P.jb2 + j0 + j);
                 adjl[atomicAdd(&adj[b1], 1u)] = (uint16_t)j;
                 if (joint_two_bodies(ty) && b2 != b1) adjl[atomicAdd(&adj[b2], 1u)] = (uint16_t)j;
-                prio[j] = ((unsigned long long)r2d_colour_mix(j, R2D_COLOUR_JOINT_SALT) << 32) | j;
+                prio[j] = r2d_colour_mix(j, R2D_COLOUR_JOINT_SALT);
                 jcol[j] = 0xFFu;
             }
             __syncthreads();
@@ -598,30 +637,35 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
                 int pending = 0;
                 for (uint32_t j = tid; j < NJ; j += NT) {
                     if (((volatile uint8_t*)jcol)[j] != 0xFFu) continue;
-                    uint32_t bits[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+                    ColourSet used;
                     bool ready = true;
-                    const unsigned long long pj = prio[j];
+                    const uint32_t pj = prio[j];
                     const uint8_t ty = __ldg(P.jtype + j0 + j);
                     const uint32_t b1 = __ldg(P.jb1 + j0 + j), b2 = __ldg(P.jb2 + j0 + j);
                     const int nends = (joint_two_bodies(ty) && b2 != b1) ? 2 : 1;
-                    const uint32_t ends[2] = {b1, b2};
-                    for (int e2 = 0; e2 < nends && ready; ++e2) {
-                        const uint32_t x = ends[e2];
+#pragma unroll
+                    for (int e2 = 0; e2 < 2; ++e2) {
+                        if (e2 >= nends || !ready) continue;
+                        const uint32_t x = e2 ? b2 : b1;
                         const uint32_t q0 = x ? adj[x - 1] : 0u, q1 = adj[x];
                         for (uint32_t q = q0; q < q1; ++q) {
                             const uint32_t o = adjl[q];
-                            if (o == j || prio[o] > pj) continue;
+                            if (o == j) continue;
+                            if (prio[o] > pj || (prio[o] == pj && o > j)) continue;
                             const uint8_t c = ((volatile uint8_t*)jcol)[o];
                             if (c == 0xFFu) {
                                 ready = false;
                                 break;
                             }
-                            bits[c >> 5] |= 1u << (c & 31);
+                            used.add(c);
                         }
                     }
                     if (ready) {
-                        const uint32_t c = first_free(bits);
-                        if (c == 255u) err = DS_CAPACITY;
+                        uint32_t c = used.first_free();
+                        if (c >= (uint32_t)MAX_COLOURS) {
+                            cap_fail(&err, &s_capbits, CAP_COLOURS);
+                            c = 0;
+                        }
                         ((volatile uint8_t*)jcol)[j] = (uint8_t)c;
                     } else {
                         pending = 1;
@@ -644,6 +688,7 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
         }
         __syncthreads();
 
+        PHASE(4);
         // ---------------- substeps (lib.zig:199-250) ----------------
         const uint32_t S = P.sub_steps;
         const float h = P.dt / (float)S;
@@ -723,6 +768,8 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
                     const float kt = inv_mass + inv_i1 * (r1t * r1t) + inv_i2 * (r2t * r2t);
                     s.mn[p] = kn > 0.0f ? 1.0f / kn : 0.0f;
                     s.mt[p] = kt > 0.0f ? 1.0f / kt : 0.0f;
+                    // bias of calculateImpulses (collision.zig:172): depth is fixed within a substep
+                    s.bias[p] = BAUMGARTE * zmax(0.0f, (-s.depth[p]) - BAUMGARTE_SLOP) / h;
                 }
             }
             __syncthreads();
@@ -740,7 +787,7 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
                 }
                 for (uint32_t c = 0; c < ncol; ++c) {
                     const uint32_t k0 = coff[c], k1 = coff[c + 1];
-                    for (uint32_t k = k0 + tid; k < k1; k += NT) solve_contact(s, corder[k], h);
+                    for (uint32_t k = k0 + tid; k < k1; k += NT) solve_contact(s, corder[k]);
                     __syncthreads();
                 }
             }
@@ -764,6 +811,7 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
             __syncthreads();
         }
 
+        PHASE(5);
         // ---------------- write back ----------------
         for (uint32_t i = tid; i < n; i += NT) {
             const uint32_t g = base + i;
@@ -819,6 +867,17 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
                     P.dbg.jcolour[(size_t)w * P.dbg.jcap + j] = jcol[j];
             }
         }
+        PHASE(6);
+#ifdef R2D_PHASE_TIMERS
+        if (tid == 0 && P.timers) {
+            unsigned long long* t = P.timers + (size_t)w * PHASE_SLOTS;
+            t[7] += s_cnt[0];
+            t[8] += M;
+            t[9] += ncol;
+            t[10] += jp_rounds;
+            t[11] += 1;
+        }
+#endif
         if (tid == 0) P.world_status[w] = DS_OK;
         return;
     }
@@ -826,6 +885,8 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
 fail:
     if (tid == 0) {
         P.world_status[w] = s_err ? s_err : DS_CAPACITY;
+        P.world_capbits[w] = s_capbits;
+        P.world_fail_call[w] = P.call_index;
         atomicAdd(P.error_count, 1);
     }
 #undef SMF

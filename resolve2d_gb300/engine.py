@@ -12,8 +12,9 @@ from . import _native as N
 from .scenes import NSTATE, Scene, derive_props_state
 
 
-def _config(cell: float, mult: int, debug: bool, stream) -> N.Config:
+def _config(cell: float, mult: int, debug: bool, stream, capacity_scale: float = 0.0) -> N.Config:
     cfg = N.Config()
+    cfg.capacity_scale = float(capacity_scale)
     cfg.spatialhash_cell_width = float(cell)
     cfg.spatialhash_table_size_mult = int(mult)
     cfg.flags = N.FLAG_DEBUG_TAPS if debug else 0
@@ -24,10 +25,10 @@ def _config(cell: float, mult: int, debug: bool, stream) -> N.Config:
 class World:
     """One world stepped by the fused kernel (r2d_solver_* entry points)."""
 
-    def __init__(self, cell: float = 0.0, mult: int = 0, debug: bool = False, stream=None):
+    def __init__(self, cell: float = 0.0, mult: int = 0, debug: bool = False, stream=None, capacity_scale: float = 0.0):
         self._lib = N.load()
         self._h = C.c_void_p()
-        cfg = _config(cell, mult, debug, stream)
+        cfg = _config(cell, mult, debug, stream, capacity_scale)
         N.check(self._lib.r2d_solver_create(C.byref(cfg), C.byref(self._h)), "r2d_solver_create")
         self.n = 0
 
@@ -111,10 +112,10 @@ class World:
 class Batch:
     """Many independent worlds stepped together (r2d_batch_* entry points)."""
 
-    def __init__(self, cell: float = 0.0, mult: int = 0, debug: bool = False, stream=None):
+    def __init__(self, cell: float = 0.0, mult: int = 0, debug: bool = False, stream=None, capacity_scale: float = 0.0):
         self._lib = N.load()
         self._h = C.c_void_p()
-        cfg = _config(cell, mult, debug, stream)
+        cfg = _config(cell, mult, debug, stream, capacity_scale)
         N.check(self._lib.r2d_batch_create(C.byref(cfg), C.byref(self._h)), "r2d_batch_create")
         self.n = 0
         self.nworlds = 0

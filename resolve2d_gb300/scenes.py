@@ -335,10 +335,10 @@ def random_scene(seed: int, n: int = 40, rect_p: float = 0.5, box: float = 8.0, 
             b.disc(x, y, rng.uniform(0.2, 1.0), mu, vx=vx, vy=vy, angle=ang, omega=om, static=st)
     js = None
     if joints:
-        nb = len(b.rows)
+        dyn = np.array([i for i, r in enumerate(b.rows) if not (r[0] & KIND_STATIC)])
         jt, j1, j2, jp = [], [], [], []
         for _ in range(max(1, n // 4)):
-            a, c = rng.choice(np.arange(1, nb), 2, replace=False)
+            a, c = rng.choice(dyn, 2, replace=False)
             t = int(rng.integers(0, 4))
             pmax = float(rng.choice([np.inf, rng.uniform(1, 50)]))
             prm = [pmax, -pmax, float(rng.uniform(1, 20)), 0, 0, 0, 0, 0]
