@@ -26,8 +26,7 @@
 #include "r2d_world.cuh"
 
 namespace r2d {
-cudaError_t launch_world_step(const StepParams& P, const Caps& C, int threads, cudaStream_t stream);
-cudaError_t world_step_occupancy(const Caps& C, int threads, int* blocks_per_sm);
+cudaError_t launch_world_step(const StepParams& P, const Caps& C, int threads, bool lean, cudaStream_t stream);
 }  // namespace r2d
 
 using namespace r2d;
@@ -96,6 +95,7 @@ void init_aabb(uint8_t kind, float x, float y, float angle, float d0, float d1, 
 struct KClass {
     Caps caps{};
     int threads = 128;
+    bool lean = true;
     std::vector<uint32_t> worlds;
     uint32_t* d_list = nullptr;
     uint32_t smem = 0;
@@ -166,7 +166,8 @@ struct Engine {
     // Doublings of each per-world buffer a world has needed (manifolds,
     // points, cell entries, candidate pairs), packed one byte each.
     std::vector<uint32_t> world_boost;
-    static uint32_t boost_of(uint32_t b, int i) { return (b >> (8 * i)) & 0xFFu; }
+    static uint32_t boost_of(uint32_t b, int i) { return (b >> (8 * i)) & 0x7Fu; }
+    static constexpr uint32_t BOOST_FULL = 0x80000000u;  // world needs the full point layout
 
     ~Engine() {
         dfree(d_state); dfree(d_props); dfree(d_kind); dfree(d_ids); dfree(d_worlds);
@@ -352,12 +353,12 @@ struct Engine {
         };
         Caps c{};
         c.nb = nb;
-        c.nm = sz((11.0 * nb) / 4.0 + 16.0, 0);
-        const double ppm = 1.15 + (double)rect_frac * rect_frac;
-        c.npt = sz(((11.0 * nb) / 4.0 + 16.0) * ppm + 16.0, 1);
-        c.ne = sz(std::max(4.0 * nb + 64.0, max_cells * 1.5 + 64.0), 2);
-        c.np = sz(4.0 * nb + 32.0, 3);
-        c.hs = next_pow2(2u * c.np);
+        c.nm = sz(2.25 * nb + 16.0, 0);
+        const double ppm = 1.08 + 0.92 * (double)rect_frac * rect_frac;
+        c.npt = sz((2.25 * nb + 16.0) * ppm + 16.0, 1);
+        c.ne = sz(std::max(2.5 * nb + 64.0, max_cells * 1.25 + 64.0), 2);
+        c.np = sz(3.5 * nb + 32.0, 3);
+        c.hs = next_pow2((3u * c.np + 1u) / 2u);
         c.nj = max_nj;
         c.nt = table_mult * nb;
         return c;
@@ -436,8 +437,11 @@ struct Engine {
                 if (d.n) rect_frac = std::max(rect_frac, (float)rects / (float)d.n);
             }
             kc.caps = caps_for(bounds[k], max_nj, rect_frac, max_cells, boost);
-            kc.threads = bounds[k] <= 64 ? 64 : (bounds[k] <= 256 ? 128 : 256);
-            kc.smem = make_layout(kc.caps).total;
+            kc.lean = !(boost & BOOST_FULL);
+            // Worlds whose shared memory allows one CTA per SM get more threads:
+            // every phase is latency-bound and the per-thread share shrinks.
+            kc.threads = bounds[k] <= 64 ? 64 : (bounds[k] <= 256 ? 128 : (bounds[k] <= 320 ? 256 : 512));
+            kc.smem = make_layout(kc.caps, kc.lean).total;
             if ((int)kc.smem > smem_optin)
                 return fail(R2D_ERR_CAPACITY, "world class of " + std::to_string(bounds[k]) + " bodies needs " +
                                                   std::to_string(kc.smem) + " B of shared memory");
@@ -494,7 +498,7 @@ struct Engine {
         if (classes.size() == 1) {
             P.world_list = classes[0].d_list;
             P.nlist = (uint32_t)classes[0].worlds.size();
-            cudaError_t e = launch_world_step(P, classes[0].caps, classes[0].threads, stream);
+            cudaError_t e = launch_world_step(P, classes[0].caps, classes[0].threads, classes[0].lean, stream);
             if (e != cudaSuccess) return fail(R2D_ERR_CUDA, std::string("world step launch: ") + cudaGetErrorString(e));
         } else if (nused > 1) {
             CUDA_TRY(cudaEventRecord(ev_fork, stream));
@@ -503,7 +507,7 @@ struct Engine {
                 const KClass& c = classes[i];
                 P.world_list = c.d_list;
                 P.nlist = (uint32_t)c.worlds.size();
-                cudaError_t e = launch_world_step(P, c.caps, c.threads, aux[i % NAUX]);
+                cudaError_t e = launch_world_step(P, c.caps, c.threads, c.lean, aux[i % NAUX]);
                 if (e != cudaSuccess) return fail(R2D_ERR_CUDA, std::string("world step launch: ") + cudaGetErrorString(e));
             }
             for (int a = 0; a < nused; ++a) {
@@ -621,16 +625,22 @@ struct Engine {
         uint32_t boost = world_boost[w];
         for (int attempt = 0; attempt < 8; ++attempt) {
             if (capbits & (CAP_BODIES | CAP_JOINTS | CAP_COLOURS)) break;  // not a buffer size
+            if (capbits & CAP_TGS) boost |= BOOST_FULL;
             const int which[4] = {CAP_MANIFOLDS, CAP_POINTS, CAP_ENTRIES, CAP_PAIRS};
             for (int i = 0; i < 4; ++i)
-                if ((capbits & which[i]) || (which[i] == CAP_MANIFOLDS && (capbits & CAP_POINTS)))
+                // manifolds and points grow together (the colouring's sort
+                // scratch lives in the point arrays)
+                if ((capbits & which[i]) || (which[i] == CAP_MANIFOLDS && (capbits & CAP_POINTS)) ||
+                    (which[i] == CAP_POINTS && (capbits & CAP_MANIFOLDS)))
                     boost += 1u << (8 * i);
             Caps c = caps_for(kc->caps.nb, kc->caps.nj, rf, cells, boost);
+            const bool lean = !(boost & BOOST_FULL);
             if (verbose)
                 fprintf(stderr, "r2d: world %u (%u bodies) outgrew buffers 0x%x at call %u; replaying with "
-                                "manifolds %u points %u entries %u pairs %u (%u B shared)\n",
-                        w, d.n, capbits, from, c.nm, c.npt, c.ne, c.np, make_layout(c).total);
-            if ((int)make_layout(c).total > smem_limit()) break;
+                                "manifolds %u points %u entries %u pairs %u, %s layout (%u B shared)\n",
+                        w, d.n, capbits, from, c.nm, c.npt, c.ne, c.np, lean ? "lean" : "full",
+                        make_layout(c, lean).total);
+            if ((int)make_layout(c, lean).total > smem_limit()) break;
             CUDA_TRY(cudaMemsetAsync(d_fail_call + w, 0xFF, sizeof(uint32_t), stream));
             CUDA_TRY(cudaMemsetAsync(d_capbits + w, 0, sizeof(uint32_t), stream));
             CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), stream));
@@ -638,7 +648,7 @@ struct Engine {
                 StepParams P = params(calls[k].dt, calls[k].sub_steps, calls[k].iters, k);
                 P.world_list = d_one;
                 P.nlist = 1;
-                cudaError_t e = launch_world_step(P, c, kc->threads, stream);
+                cudaError_t e = launch_world_step(P, c, kc->threads, lean, stream);
                 if (e != cudaSuccess) return fail(R2D_ERR_CUDA, std::string("replay launch: ") + cudaGetErrorString(e));
             }
             CUDA_TRY(cudaStreamSynchronize(stream));

@@ -60,15 +60,17 @@ R2D_DF f2 cw90(f2 a) { return {a.y, -a.x}; }
 R2D_DF f2 ccw90(f2 a) { return {-a.y, a.x}; }
 
 // Zig @max / @min on floats: the non-NaN operand wins.
+// Written as selects (no branches); same results as: a NaN -> b,
+// else b NaN -> a, else the larger (smaller) with b on ties.
 R2D_DF float zmax(float a, float b) {
-    if (a != a) return b;
-    if (b != b) return a;
-    return a > b ? a : b;
+    float r = a > b ? a : b;
+    r = (b != b) ? a : r;
+    return (a != a) ? b : r;
 }
 R2D_DF float zmin(float a, float b) {
-    if (a != a) return b;
-    if (b != b) return a;
-    return a < b ? a : b;
+    float r = a < b ? a : b;
+    r = (b != b) ? a : r;
+    return (a != a) ? b : r;
 }
 R2D_DF float zclamp(float v, float lo, float hi) { return zmax(lo, zmin(v, hi)); }
 
@@ -256,7 +258,7 @@ R2D_DF bool perform_narrow_sat(const Geo& o1, const Geo& o2, SatState& ret) {
 }
 
 struct NewPoint {
-    f2 ref_r, inc_r;
+    f2 ref_r, inc_r, mid;
     float depth;
 };
 
@@ -264,6 +266,7 @@ struct NewPoint {
 R2D_DF NewPoint make_point(f2 pos, float depth, f2 ref_pos, f2 inc_pos, f2 normal) {
     f2 middle = sub2(pos, scale2(normal, depth / 2.0f));
     NewPoint p;
+    p.mid = middle;
     p.ref_r = sub2(middle, ref_pos);
     p.inc_r = sub2(middle, inc_pos);
     p.depth = depth;

@@ -22,7 +22,7 @@ enum WorldFlags : uint32_t { W_DISC_ROTATION = 2u };
 constexpr int MAX_GRAVITY = 4;
 constexpr int JOINT_PARAMS = 8;
 constexpr int DEBUG_MF = 33;     // floats per manifold in the debug dump (oracle layout)
-constexpr int MAX_COLOURS = 254; // colour 255 marks "not coloured yet"
+constexpr int MAX_COLOURS = 128; // per-body colour masks hold 128 colours
 
 struct WorldDesc {
     uint32_t body_off, n;
@@ -48,14 +48,14 @@ struct Caps {
 // Byte offsets into the dynamic shared memory of one CTA.
 struct Layout {
     // bodies (whole step)
-    uint32_t px, py, ang, mx, my, L, mass, inertia, inv_m, inv_i, cs, sn, ang_prev, tq, kind;
+    uint32_t px, py, ang, mx, my, L, inv_m, inv_i, cs, sn, ang_prev, tq, px0, py0, kind;
     // manifolds + points (narrowphase .. end) -- aliased by the broadphase scratch
     uint32_t ma, mb, mp0, mnp, mcol, nx, ny, fric;
     uint32_t r1x, r1y, r2x, r2y, depth, odepth, mn, mt, apn, apt, bias;
     // broadphase scratch (inside the manifold region)
     uint32_t ax, ay, ahw, ahh, rx0, ry0, rx1, ry1, bcnt, ebucket, ebody, eslot, sbody, table, hset;
-    // colouring scratch
-    uint32_t adj, adjl, prio;
+    // colouring scratch: sort keys/indices, per-body colour masks
+    uint32_t skey, sidx, cmask;
     // orders
     uint32_t corder, coff, jorder, joff, jcol;
     // pairs
@@ -65,7 +65,11 @@ struct Layout {
 
 __host__ __device__ inline uint32_t r2d_align(uint32_t x, uint32_t a) { return (x + a - 1) / a * a; }
 
-__host__ __device__ inline Layout make_layout(const Caps& c) {
+// lean: contact points keep their midpoint (8 B) instead of both lever arms
+// and the original depth (12 B); the lever arms are recomputed from the
+// frame-start positions px0/py0.  Worlds with a TGS-live point (see the
+// kernel) use the full layout.
+__host__ __device__ inline Layout make_layout(const Caps& c, bool lean) {
     Layout L{};
     uint32_t o = 0;
     auto take = [&](uint32_t bytes) {
@@ -76,8 +80,12 @@ __host__ __device__ inline Layout make_layout(const Caps& c) {
     const uint32_t nb4 = 4 * c.nb;
     L.px = take(nb4); L.py = take(nb4); L.ang = take(nb4);
     L.mx = take(nb4); L.my = take(nb4); L.L = take(nb4);
-    L.mass = take(nb4); L.inertia = take(nb4); L.inv_m = take(nb4); L.inv_i = take(nb4);
+    L.inv_m = take(nb4); L.inv_i = take(nb4);
     L.cs = take(nb4); L.sn = take(nb4); L.ang_prev = take(nb4); L.tq = take(nb4);
+    if (lean) {
+        L.px0 = take(nb4);
+        L.py0 = take(nb4);
+    }
     L.kind = take(c.nb);
 
     // region X: manifolds + points, aliased by the broadphase scratch
@@ -86,8 +94,14 @@ __host__ __device__ inline Layout make_layout(const Caps& c) {
     L.ma = take(2 * c.nm); L.mb = take(2 * c.nm); L.mp0 = take(2 * c.nm);
     L.mnp = take(c.nm); L.mcol = take(c.nm);
     L.nx = take(nm4); L.ny = take(nm4); L.fric = take(nm4);
-    L.r1x = take(np4); L.r1y = take(np4); L.r2x = take(np4); L.r2y = take(np4);
-    L.depth = take(np4); L.odepth = take(np4); L.mn = take(np4); L.mt = take(np4);
+    L.r1x = take(np4); L.r1y = take(np4);  // lean: the contact midpoint
+    if (!lean) {
+        L.r2x = take(np4);
+        L.r2y = take(np4);
+    }
+    L.depth = take(np4);
+    if (!lean) L.odepth = take(np4);
+    L.mn = take(np4); L.mt = take(np4);
     L.apn = take(np4); L.apt = take(np4); L.bias = take(np4);
     const uint32_t xend_m = o;
     o = xbase;
@@ -107,16 +121,23 @@ __host__ __device__ inline Layout make_layout(const Caps& c) {
     L.jorder = take(2 * (c.nj ? c.nj : 1));
     L.joff = take(2 * (MAX_COLOURS + 2));
     L.jcol = take(c.nj ? c.nj : 1);
-    // candidate pairs (broadphase -> narrowphase), then the colouring scratch
-    const uint32_t ybase = o;
+    // candidate pairs (broadphase -> narrowphase); after the narrowphase the
+    // per-body colour masks reuse them
     L.pairs = take(4 * c.np);
-    const uint32_t yend_pairs = o;
-    o = ybase;
+    L.cmask = (16 * c.nb <= 4 * c.np) ? L.pairs : take(16 * c.nb);
+    // sort scratch of the colouring: the solver's per-point arrays (mn .. bias,
+    // contiguous) are not live until the prestep that follows the colouring
     const uint32_t ncon = c.nm > c.nj ? c.nm : c.nj;
-    L.adj = take(4 * (c.nb + 1));
-    L.adjl = take(2 * 2 * ncon);
-    L.prio = take(4 * ncon);
-    o = o > yend_pairs ? o : yend_pairs;
+    uint32_t n2 = 1;
+    while (n2 < ncon) n2 <<= 1;
+    const uint32_t sort_bytes = 8 * n2 + 2 * n2;
+    if (sort_bytes <= 5 * np4) {
+        L.skey = L.mn;
+        L.sidx = L.mn + 8 * n2;
+    } else {
+        L.skey = take(8 * n2);
+        L.sidx = take(2 * n2);
+    }
     L.total = o;
     return L;
 }
@@ -166,7 +187,8 @@ constexpr int PHASE_SLOTS = 12;
 // Which per-world buffer overflowed (reported with DS_CAPACITY).
 enum CapBits : uint32_t {
     CAP_BODIES = 1u, CAP_MANIFOLDS = 2u, CAP_POINTS = 4u, CAP_ENTRIES = 8u,
-    CAP_PAIRS = 16u, CAP_COLOURS = 32u, CAP_JOINTS = 64u
+    CAP_PAIRS = 16u, CAP_COLOURS = 32u, CAP_JOINTS = 64u,
+    CAP_TGS = 128u  // a TGS-live contact point: the world needs the full layout
 };
 
 enum DeviceStatus : int {

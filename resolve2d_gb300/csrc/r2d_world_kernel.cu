@@ -91,17 +91,129 @@ __device__ __forceinline__ void cap_fail(int* err, uint32_t* s_capbits, uint32_t
     atomicOr(s_capbits, bit);
 }
 
+// Colours `count` constraints by first-fit greedy in ascending key order
+// (key = mix << 32 | tie-break, unique per constraint; r2d_colour.h).  A
+// bitonic sort orders the keys; then one warp walks the sorted list 32 at a
+// time.  A lane takes the lowest colour absent from its nodes' colour masks
+// once every earlier lane of its chunk that shares a node is coloured, so the
+// result is exactly the sequential greedy colouring, computed with warp
+// shuffles instead of block-wide rounds.  ends(i, &a, &b) names constraint
+// i's conflict nodes (values >= 0x10000 mean "no node").  Returns true on
+// every thread when some constraint would need more than MAX_COLOURS colours.
+template <int NT, class Ends, class Key>
+__device__ bool colour_greedy_sorted(uint32_t count, uint32_t n, Ends ends, Key key, uint8_t* colour,
+                                     unsigned long long* skey, uint16_t* sidx, uint32_t* cmask) {
+    const int tid = threadIdx.x, lane = tid & 31;
+    uint32_t N2 = 1;
+    while (N2 < count) N2 <<= 1;
+    for (uint32_t i = tid; i < N2; i += NT) {
+        if (i < count) {
+            skey[i] = key(i);
+            sidx[i] = (uint16_t)i;
+        } else {
+            skey[i] = ~0ull;
+            sidx[i] = 0xFFFFu;
+        }
+    }
+    for (uint32_t i = tid; i < 4 * n; i += NT) cmask[i] = 0u;
+    __syncthreads();
+    for (uint32_t k = 2; k <= N2; k <<= 1) {
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            for (uint32_t i = tid; i < N2; i += NT) {
+                const uint32_t ixj = i ^ j;
+                if (ixj > i) {
+                    const unsigned long long a = skey[i], b = skey[ixj];
+                    if ((a > b) == ((i & k) == 0)) {
+                        skey[i] = b;
+                        skey[ixj] = a;
+                        const uint16_t t = sidx[i];
+                        sidx[i] = sidx[ixj];
+                        sidx[ixj] = t;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    int overflow = 0;
+    if (tid < 32) {
+        for (uint32_t base = 0; base < count; base += 32) {
+            const uint32_t i = base + lane;
+            const bool valid = i < count;
+            const uint32_t ci = valid ? (uint32_t)sidx[i] : 0u;
+            uint32_t a = 0x10000u + 2u * lane, b = 0x10001u + 2u * lane;
+            if (valid) ends(ci, &a, &b);
+            uint32_t earlier = 0u;  // earlier lanes of this chunk sharing a node
+#pragma unroll 8
+            for (int j = 0; j < 32; ++j) {
+                const uint32_t aj = __shfl_sync(0xffffffffu, a, j), bj = __shfl_sync(0xffffffffu, b, j);
+                if (j < lane && (aj == a || aj == b || bj == a || bj == b)) earlier |= 1u << j;
+            }
+            bool done = !valid;
+            for (int round = 0; round < 32; ++round) {
+                const uint32_t pending = __ballot_sync(0xffffffffu, !done);
+                if (!pending) break;
+                if (!done && !(earlier & pending)) {
+                    const bool na = a < 0x10000u, nb2 = b < 0x10000u;
+                    uint32_t w0 = 0u, w1 = 0u, w2 = 0u, w3 = 0u;
+                    if (na) {
+                        w0 |= cmask[a]; w1 |= cmask[n + a]; w2 |= cmask[2 * n + a]; w3 |= cmask[3 * n + a];
+                    }
+                    if (nb2) {
+                        w0 |= cmask[b]; w1 |= cmask[n + b]; w2 |= cmask[2 * n + b]; w3 |= cmask[3 * n + b];
+                    }
+                    uint32_t c = 128u;
+                    if (w0 != 0xFFFFFFFFu) c = (uint32_t)__ffs(~w0) - 1u;
+                    else if (w1 != 0xFFFFFFFFu) c = 32u + (uint32_t)__ffs(~w1) - 1u;
+                    else if (w2 != 0xFFFFFFFFu) c = 64u + (uint32_t)__ffs(~w2) - 1u;
+                    else if (w3 != 0xFFFFFFFFu) c = 96u + (uint32_t)__ffs(~w3) - 1u;
+                    if (c >= (uint32_t)MAX_COLOURS) {
+                        overflow = 1;
+                        c = 0u;
+                    }
+                    colour[ci] = (uint8_t)c;
+                    if (na) cmask[(c >> 5) * n + a] |= 1u << (c & 31u);
+                    if (nb2) cmask[(c >> 5) * n + b] |= 1u << (c & 31u);
+                    done = true;
+                }
+                __syncwarp();
+            }
+        }
+    }
+    return __syncthreads_or(overflow) != 0;
+}
+
 // Shared-memory views of one world.
 struct SW {
-    float *px, *py, *ang, *mx, *my, *L, *mass, *inertia, *inv_m, *inv_i, *cs, *sn, *ang_prev, *tq;
+    float *px, *py, *ang, *mx, *my, *L, *inv_m, *inv_i, *cs, *sn, *ang_prev, *tq, *px0, *py0;
+    const float* __restrict__ gmass;     // this world's masses (global, read-only)
+    const float* __restrict__ ginertia;  // this world's inertias
     uint8_t* kind;
     uint16_t *ma, *mb, *mp0;
     uint8_t *mnp, *mcol;
     float *nx, *ny, *fric;
     float *r1x, *r1y, *r2x, *r2y, *depth, *odepth, *mn, *mt, *apn, *apt, *bias;
+
+    __device__ __forceinline__ float mass(uint32_t i) const { return __ldg(gmass + i); }
+    __device__ __forceinline__ float inertia(uint32_t i) const { return __ldg(ginertia + i); }
+    // Lever arms of point p between bodies a (reference) and b (incident).
+    // Lean: middle - frame-start position, the subtraction CollisionPoint.init
+    // performs (collision.zig:43-44), so the bits are those it stored.
+    template <bool LEAN>
+    __device__ __forceinline__ void arms(uint32_t p, uint32_t a, uint32_t b, f2* r1, f2* r2) const {
+        if (LEAN) {
+            const f2 mid = {r1x[p], r1y[p]};
+            *r1 = sub2(mid, f2{px0[a], py0[a]});
+            *r2 = sub2(mid, f2{px0[b], py0[b]});
+        } else {
+            *r1 = f2{r1x[p], r1y[p]};
+            *r2 = f2{r2x[p], r2y[p]};
+        }
+    }
 };
 
 // CollisionManifold.calculateImpulses (collision.zig:135-218)
+template <bool LEAN>
 __device__ __forceinline__ void solve_contact(const SW& s, uint32_t m) {
     const uint32_t a = s.ma[m], b = s.mb[m];
     const bool sa = s.kind[a] & K_STATIC, sb = s.kind[b] & K_STATIC;
@@ -125,7 +237,8 @@ __device__ __forceinline__ void solve_contact(const SW& s, uint32_t m) {
             s.apt[p] = 0.f;
             continue;
         }
-        const f2 r1 = {s.r1x[p], s.r1y[p]}, r2 = {s.r2x[p], s.r2y[p]};
+        f2 r1, r2;
+        s.arms<LEAN>(p, a, b, &r1, &r2);
         const f2 v1 = add2(vlinear_1, f2{-r1.y * omega1, r1.x * omega1});
         const f2 v2 = add2(vlinear_2, f2{-r2.y * omega2, r2.x * omega2});
         const f2 dv = sub2(v1, v2);
@@ -174,8 +287,8 @@ __device__ __forceinline__ void solve_joint(const SW& s, uint8_t type, uint32_t 
         const float epsilon = CONSTRAINT_GRADIENT_DIVISION_LIMIT;
         const float target = __ldg(prm + 3);
         const bool st1 = s.kind[i1] & K_STATIC, st2 = s.kind[i2] & K_STATIC;
-        const float w1 = st1 ? 0.f : 1.0f / s.mass[i1];
-        const float w2 = st2 ? 0.f : 1.0f / s.mass[i2];
+        const float w1 = st1 ? 0.f : 1.0f / s.mass(i1);
+        const float w2 = st2 ? 0.f : 1.0f / s.mass(i2);
         const f2 v1 = scale2(f2{s.mx[i1], s.my[i1]}, w1);
         const f2 v2 = scale2(f2{s.mx[i2], s.my[i2]}, w2);
         const f2 rel = sub2(v2, v1);
@@ -202,10 +315,10 @@ __device__ __forceinline__ void solve_joint(const SW& s, uint8_t type, uint32_t 
         const f2 a1 = add2(rr1, f2{s.px[i1], s.py[i1]});
         const f2 a2 = add2(rr2, f2{s.px[i2], s.py[i2]});
         const f2 normal = normalize2(sub2(a2, a1));
-        const float inv_m1 = st1 ? 0.f : 1.0f / s.mass[i1];
-        const float inv_m2 = st2 ? 0.f : 1.0f / s.mass[i2];
-        const float inv_i1 = st1 ? 0.f : 1.0f / s.inertia[i1];
-        const float inv_i2 = st2 ? 0.f : 1.0f / s.inertia[i2];
+        const float inv_m1 = st1 ? 0.f : 1.0f / s.mass(i1);
+        const float inv_m2 = st2 ? 0.f : 1.0f / s.mass(i2);
+        const float inv_i1 = st1 ? 0.f : 1.0f / s.inertia(i1);
+        const float inv_i2 = st2 ? 0.f : 1.0f / s.inertia(i2);
         const f2 vl1 = scale2(f2{s.mx[i1], s.my[i1]}, inv_m1);
         const float om1 = s.L[i1] * inv_i1;
         const f2 vl2 = scale2(f2{s.mx[i2], s.my[i2]}, inv_m2);
@@ -234,7 +347,7 @@ __device__ __forceinline__ void solve_joint(const SW& s, uint8_t type, uint32_t 
         if (s.kind[i1] & K_STATIC) return;
         const float epsilon = ALLOWED_CONSTRAINT_VALUE;
         const f2 target = {__ldg(prm + 3), __ldg(prm + 4)};
-        const float w = 1.0f / s.mass[i1];
+        const float w = 1.0f / s.mass(i1);
         const f2 v = scale2(f2{s.mx[i1], s.my[i1]}, w);
         const f2 delta = sub2(target, f2{s.px[i1], s.py[i1]});
         const float dist = length2(delta);
@@ -252,7 +365,7 @@ __device__ __forceinline__ void solve_joint(const SW& s, uint8_t type, uint32_t 
         if (s.kind[i1] & K_STATIC) return;
         const float epsilon = ALLOWED_CONSTRAINT_VALUE;
         const float target = __ldg(prm + 3);
-        const float I = s.inertia[i1];
+        const float I = s.inertia(i1);
         const float omega = s.L[i1] / I;
         const float C = omega - target;
         if (fabsf(C) < ALLOWED_CONSTRAINT_VALUE) return;
@@ -270,7 +383,7 @@ __device__ __forceinline__ bool joint_two_bodies(uint8_t type) {
     return type == J_DISTANCE || type == J_OFFSET;
 }
 
-template <int NT>
+template <int NT, bool LEAN>
 __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, const Caps C, const Layout Lo) {
     extern __shared__ __align__(16) unsigned char sm[];
     __shared__ uint32_t s_wsum[32];
@@ -305,7 +418,7 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
     int err = 0;
 #ifdef R2D_PHASE_TIMERS
     long long t_mark = clock64();
-    uint32_t jp_rounds = 0;
+    const uint32_t jp_rounds = 0;
 #define PHASE(k)                                                              \
     do {                                                                      \
         __syncthreads();                                                      \
@@ -330,8 +443,11 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
     SW s;
     s.px = SMF(Lo.px); s.py = SMF(Lo.py); s.ang = SMF(Lo.ang);
     s.mx = SMF(Lo.mx); s.my = SMF(Lo.my); s.L = SMF(Lo.L);
-    s.mass = SMF(Lo.mass); s.inertia = SMF(Lo.inertia); s.inv_m = SMF(Lo.inv_m); s.inv_i = SMF(Lo.inv_i);
+    s.inv_m = SMF(Lo.inv_m); s.inv_i = SMF(Lo.inv_i);
     s.cs = SMF(Lo.cs); s.sn = SMF(Lo.sn); s.ang_prev = SMF(Lo.ang_prev); s.tq = SMF(Lo.tq);
+    s.px0 = SMF(Lo.px0); s.py0 = SMF(Lo.py0);
+    s.gmass = P.props + (size_t)P_MASS * NB + base;
+    s.ginertia = P.props + (size_t)P_INERTIA * NB + base;
     s.kind = SMU8(Lo.kind);
     s.ma = SMU16(Lo.ma); s.mb = SMU16(Lo.mb); s.mp0 = SMU16(Lo.mp0);
     s.mnp = SMU8(Lo.mnp); s.mcol = SMU8(Lo.mcol);
@@ -347,9 +463,9 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
     uint16_t *ebody = SMU16(Lo.ebody), *eslot = SMU16(Lo.eslot), *sbody = SMU16(Lo.sbody);
     uint32_t* table = SMU32(Lo.table);
     uint32_t* hset = SMU32(Lo.hset);
-    uint32_t* adj = SMU32(Lo.adj);
-    uint16_t* adjl = SMU16(Lo.adjl);
-    uint32_t* prio = SMU32(Lo.prio);
+    unsigned long long* skey = reinterpret_cast<unsigned long long*>(sm + Lo.skey);
+    uint16_t* sidx = SMU16(Lo.sidx);
+    uint32_t* cmask = SMU32(Lo.cmask);
     uint16_t *corder = SMU16(Lo.corder), *coff = SMU16(Lo.coff);
     uint16_t *jorder = SMU16(Lo.jorder), *joff = SMU16(Lo.joff);
     uint8_t* jcol = SMU8(Lo.jcol);
@@ -372,8 +488,10 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
         s.L[i] = st[(size_t)S_ANG_MOM * NB + g];
         const float m = __ldg(pr + (size_t)P_MASS * NB + g);
         const float I = __ldg(pr + (size_t)P_INERTIA * NB + g);
-        s.mass[i] = m;
-        s.inertia[i] = I;
+        if (LEAN) {
+            s.px0[i] = s.px[i];
+            s.py0[i] = s.py[i];
+        }
         s.inv_m[i] = (k & K_STATIC) ? 0.f : 1.0f / m;
         s.inv_i[i] = (k & K_STATIC) ? 0.f : 1.0f / I;
         s.kind[i] = k;
@@ -510,14 +628,21 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
 #pragma unroll
             for (int k = 0; k < 2; ++k) {
                 if (k >= npt) break;
-                s.r1x[p0 + k] = pts[k].ref_r.x;
-                s.r1y[p0 + k] = pts[k].ref_r.y;
-                s.r2x[p0 + k] = pts[k].inc_r.x;
-                s.r2y[p0 + k] = pts[k].inc_r.y;
+                if (LEAN) {
+                    s.r1x[p0 + k] = pts[k].mid.x;
+                    s.r1y[p0 + k] = pts[k].mid.y;
+                    // a depth for which approxEql(depth, depth, 1e-4) fails
+                    // (|depth| >= 2048 or NaN) makes updateTGSDepth rotate the
+                    // lever arms (collision.zig:80-95): full layout needed
+                    if (!approx_eql(pts[k].depth, pts[k].depth, 1e-4f)) cap_fail(&err, &s_capbits, CAP_TGS);
+                } else {
+                    s.r1x[p0 + k] = pts[k].ref_r.x;
+                    s.r1y[p0 + k] = pts[k].ref_r.y;
+                    s.r2x[p0 + k] = pts[k].inc_r.x;
+                    s.r2y[p0 + k] = pts[k].inc_r.y;
+                    s.odepth[p0 + k] = pts[k].depth;
+                }
                 s.depth[p0 + k] = pts[k].depth;
-                s.odepth[p0 + k] = pts[k].depth;
-                s.apn[p0 + k] = 0.f;
-                s.apt[p0 + k] = 0.f;
             }
         }
     }
@@ -531,72 +656,25 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
         uint32_t ncol = 0, njcol = 0;
 
         // ---------------- contact colouring (r2d_colour.h) ----------------
-        for (uint32_t i = tid; i <= n; i += NT) adj[i] = 0u;
-        __syncthreads();
-        for (uint32_t m = tid; m < M; m += NT) {
-            const uint32_t a = s.ma[m], b = s.mb[m];
-            if (!(s.kind[a] & K_STATIC)) atomicAdd(&adj[a], 1u);
-            if (!(s.kind[b] & K_STATIC)) atomicAdd(&adj[b], 1u);
-        }
-        __syncthreads();
-        block_scan_excl<NT>(adj, n, s_wsum);
-        for (uint32_t m = tid; m < M; m += NT) {
-            const uint32_t a = s.ma[m], b = s.mb[m];
-            if (!(s.kind[a] & K_STATIC)) adjl[atomicAdd(&adj[a], 1u)] = (uint16_t)m;
-            if (!(s.kind[b] & K_STATIC)) adjl[atomicAdd(&adj[b], 1u)] = (uint16_t)m;
-            prio[m] = r2d_colour_mix(min(a, b), max(a, b));
-            s.mcol[m] = 0xFFu;
-        }
-        __syncthreads();  // adj[i] = one past body i's last adjacency slot
-        for (uint32_t round = 0; round <= M + 1; ++round) {
-            int pending = 0;
-            for (uint32_t m = tid; m < M; m += NT) {
-                if (((volatile uint8_t*)s.mcol)[m] != 0xFFu) continue;
-                ColourSet used;
-                bool ready = true;
-                const uint32_t pm = prio[m];
-                const uint32_t ea = s.ma[m], eb = s.mb[m];
-                const uint32_t km = (min(ea, eb) << 16) | max(ea, eb);
-#pragma unroll
-                for (int e2 = 0; e2 < 2; ++e2) {
-                    const uint32_t x = e2 ? eb : ea;
-                    if (!ready || (s.kind[x] & K_STATIC)) continue;
-                    const uint32_t q0 = x ? adj[x - 1] : 0u, q1 = adj[x];
-                    for (uint32_t q = q0; q < q1; ++q) {
-                        const uint32_t o = adjl[q];
-                        if (o == m) continue;
-                        const uint32_t po = prio[o];
-                        if (po > pm) continue;
-                        if (po == pm) {  // equal hashes: the smaller (lo, hi) key goes first
-                            const uint32_t oa = s.ma[o], ob = s.mb[o];
-                            if (((min(oa, ob) << 16) | max(oa, ob)) > km) continue;
-                        }
-                        const uint8_t c = ((volatile uint8_t*)s.mcol)[o];
-                        if (c == 0xFFu) {
-                            ready = false;
-                            break;
-                        }
-                        used.add(c);
-                    }
-                }
-                if (ready) {
-                    uint32_t c = used.first_free();
-                    if (c >= (uint32_t)MAX_COLOURS) {
-                        cap_fail(&err, &s_capbits, CAP_COLOURS);
-                        c = 0;
-                    }
-                    ((volatile uint8_t*)s.mcol)[m] = (uint8_t)c;
-                } else {
-                    pending = 1;
-                }
+        // Conflict nodes of a contact: its non-static bodies.
+        auto contact_ends = [&](uint32_t m, uint32_t* a, uint32_t* b) {
+            const uint32_t x = s.ma[m], y = s.mb[m];
+            if (!(s.kind[x] & K_STATIC)) *a = x;
+            if (!(s.kind[y] & K_STATIC)) *b = y;
+        };
+        auto contact_key = [&](uint32_t m) {
+            const uint32_t x = s.ma[m], y = s.mb[m];
+            const uint32_t lo = min(x, y), hi = max(x, y);
+            return ((unsigned long long)r2d_colour_mix(lo, hi) << 32) | ((lo << 16) | hi);
+        };
+        if (colour_greedy_sorted<NT>(M, n, contact_ends, contact_key, s.mcol, skey, sidx, cmask)) {
+            if (tid == 0) {
+                s_err = DS_CAPACITY;
+                s_capbits |= CAP_COLOURS;
             }
-#ifdef R2D_PHASE_TIMERS
-            ++jp_rounds;
-#endif
-            if (!__syncthreads_or(pending)) break;
+            __syncthreads();
+            goto fail;
         }
-        if (err) set_err(&s_err, err);
-        if (__syncthreads_or(err != 0)) goto fail;
         // colour-major order
         for (uint32_t c = tid; c < 256; c += NT) s_ccnt[c] = 0u;
         __syncthreads();
@@ -614,67 +692,24 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
         if (NJ) {
             const uint32_t j0 = wd.joint_off;
             __syncthreads();
-            for (uint32_t i = tid; i <= n; i += NT) adj[i] = 0u;
-            __syncthreads();
-            for (uint32_t j = tid; j < NJ; j += NT) {
+            // every body a joint names is a conflict node, static or not
+            auto joint_ends = [&](uint32_t j, uint32_t* a, uint32_t* b) {
                 const uint8_t ty = __ldg(P.jtype + j0 + j);
                 const uint32_t b1 = __ldg(P.jb1 + j0 + j), b2 = __ldg(P.jb2 + j0 + j);
-                atomicAdd(&adj[b1], 1u);
-                if (joint_two_bodies(ty) && b2 != b1) atomicAdd(&adj[b2], 1u);
-            }
-            __syncthreads();
-            block_scan_excl<NT>(adj, n, s_wsum);
-            for (uint32_t j = tid; j < NJ; j += NT) {
-                const uint8_t ty = __ldg(P.jtype + j0 + j);
-                const uint32_t b1 = __ldg(P.jb1 + j0 + j), b2 = __ldg(P.jb2 + j0 + j);
-                adjl[atomicAdd(&adj[b1], 1u)] = (uint16_t)j;
-                if (joint_two_bodies(ty) && b2 != b1) adjl[atomicAdd(&adj[b2], 1u)] = (uint16_t)j;
-                prio[j] = r2d_colour_mix(j, R2D_COLOUR_JOINT_SALT);
-                jcol[j] = 0xFFu;
-            }
-            __syncthreads();
-            for (uint32_t round = 0; round <= NJ + 1; ++round) {
-                int pending = 0;
-                for (uint32_t j = tid; j < NJ; j += NT) {
-                    if (((volatile uint8_t*)jcol)[j] != 0xFFu) continue;
-                    ColourSet used;
-                    bool ready = true;
-                    const uint32_t pj = prio[j];
-                    const uint8_t ty = __ldg(P.jtype + j0 + j);
-                    const uint32_t b1 = __ldg(P.jb1 + j0 + j), b2 = __ldg(P.jb2 + j0 + j);
-                    const int nends = (joint_two_bodies(ty) && b2 != b1) ? 2 : 1;
-#pragma unroll
-                    for (int e2 = 0; e2 < 2; ++e2) {
-                        if (e2 >= nends || !ready) continue;
-                        const uint32_t x = e2 ? b2 : b1;
-                        const uint32_t q0 = x ? adj[x - 1] : 0u, q1 = adj[x];
-                        for (uint32_t q = q0; q < q1; ++q) {
-                            const uint32_t o = adjl[q];
-                            if (o == j) continue;
-                            if (prio[o] > pj || (prio[o] == pj && o > j)) continue;
-                            const uint8_t c = ((volatile uint8_t*)jcol)[o];
-                            if (c == 0xFFu) {
-                                ready = false;
-                                break;
-                            }
-                            used.add(c);
-                        }
-                    }
-                    if (ready) {
-                        uint32_t c = used.first_free();
-                        if (c >= (uint32_t)MAX_COLOURS) {
-                            cap_fail(&err, &s_capbits, CAP_COLOURS);
-                            c = 0;
-                        }
-                        ((volatile uint8_t*)jcol)[j] = (uint8_t)c;
-                    } else {
-                        pending = 1;
-                    }
+                *a = b1;
+                if (joint_two_bodies(ty) && b2 != b1) *b = b2;
+            };
+            auto joint_key = [&](uint32_t j) {
+                return ((unsigned long long)r2d_colour_mix(j, R2D_COLOUR_JOINT_SALT) << 32) | j;
+            };
+            if (colour_greedy_sorted<NT>(NJ, n, joint_ends, joint_key, jcol, skey, sidx, cmask)) {
+                if (tid == 0) {
+                    s_err = DS_CAPACITY;
+                    s_capbits |= CAP_COLOURS;
                 }
-                if (!__syncthreads_or(pending)) break;
+                __syncthreads();
+                goto fail;
             }
-            if (err) set_err(&s_err, err);
-            if (__syncthreads_or(err != 0)) goto fail;
             for (uint32_t c = tid; c < 256; c += NT) s_ccnt[c] = 0u;
             __syncthreads();
             for (uint32_t j = tid; j < NJ; j += NT) atomicAdd(&s_ccnt[jcol[j]], 1u);
@@ -685,6 +720,12 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
             for (uint32_t c = tid; c <= njcol; c += NT) joff[c] = (uint16_t)(c < njcol ? s_ccnt[c] : NJ);
             __syncthreads();
             for (uint32_t j = tid; j < NJ; j += NT) jorder[atomicAdd(&s_ccnt[jcol[j]], 1u)] = (uint16_t)j;
+        }
+        __syncthreads();
+        // the sort scratch overlapped the accumulators: they start at zero
+        for (uint32_t p = tid; p < s_cnt[2] && p < C.npt; p += NT) {
+            s.apn[p] = 0.f;
+            s.apt[p] = 0.f;
         }
         __syncthreads();
 
@@ -708,8 +749,8 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
                 }
                 if (!(k & K_STATIC)) {
                     for (uint32_t gg = 0; gg < wd.ngrav; ++gg) {
-                        fx += 0.0f * s.mass[i];
-                        fy += (-wd.g[gg]) * s.mass[i];
+                        fx += 0.0f * s.mass(i);
+                        fy += (-wd.g[gg]) * s.mass(i);
                     }
                 }
                 if (last) {
@@ -737,7 +778,7 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
                 const uint32_t a = s.ma[m], b = s.mb[m];
                 const f2 n2 = {s.nx[m], s.ny[m]};
                 const uint32_t p0 = s.mp0[m], np = s.mnp[m];
-                for (uint32_t k = 0; k < np; ++k) {
+                for (uint32_t k = 0; k < np && !LEAN; ++k) {
                     const uint32_t p = p0 + k;
                     if (approx_eql(s.depth[p], s.odepth[p], 1e-4f)) continue;
                     float sa_, ca_, sb_, cb_;
@@ -761,7 +802,8 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
                 s.fric[m] = sqrtf(__ldg(pr + (size_t)P_MU * NB + base + a) * __ldg(pr + (size_t)P_MU * NB + base + b));
                 for (uint32_t k = 0; k < np; ++k) {
                     const uint32_t p = p0 + k;
-                    const f2 r1 = {s.r1x[p], s.r1y[p]}, r2 = {s.r2x[p], s.r2y[p]};
+                    f2 r1, r2;
+                    s.arms<LEAN>(p, a, b, &r1, &r2);
                     const float r1n = cross2(r1, n2), r2n = cross2(r2, n2);
                     const float kn = inv_mass + inv_i1 * (r1n * r1n) + inv_i2 * (r2n * r2n);
                     const float r1t = cross2(r1, t2), r2t = cross2(r2, t2);
@@ -787,7 +829,7 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
                 }
                 for (uint32_t c = 0; c < ncol; ++c) {
                     const uint32_t k0 = coff[c], k1 = coff[c + 1];
-                    for (uint32_t k = k0 + tid; k < k1; k += NT) solve_contact(s, corder[k]);
+                    for (uint32_t k = k0 + tid; k < k1; k += NT) solve_contact<LEAN>(s, corder[k]);
                     __syncthreads();
                 }
             }
@@ -796,10 +838,10 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
                 s.ang_prev[i] = s.ang[i];
                 const uint8_t k = s.kind[i];
                 if (k & K_STATIC) continue;
-                const float sm_ = h / s.mass[i];
+                const float sm_ = h / s.mass(i);
                 s.px[i] += s.mx[i] * sm_;
                 s.py[i] += s.my[i] * sm_;
-                s.ang[i] += s.L[i] * h / s.inertia[i];
+                s.ang[i] += s.L[i] * h / s.inertia(i);
                 s.tq[i] = 0.f;
                 if (!last && ((k & K_RECT) || disc_rot)) {
                     float c, sn;
@@ -850,12 +892,14 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
                     const uint32_t p = p0 + k;
                     q[0] = __int_as_float(0x7fc00000);
                     q[1] = __int_as_float(0x7fc00000);
-                    q[2] = has ? s.r1x[p] : 0.f;
-                    q[3] = has ? s.r1y[p] : 0.f;
-                    q[4] = has ? s.r2x[p] : 0.f;
-                    q[5] = has ? s.r2y[p] : 0.f;
+                    f2 r1 = {0.f, 0.f}, r2 = {0.f, 0.f};
+                    if (has) s.arms<LEAN>(p, s.ma[m], s.mb[m], &r1, &r2);
+                    q[2] = r1.x;
+                    q[3] = r1.y;
+                    q[4] = r2.x;
+                    q[5] = r2.y;
                     q[6] = has ? s.depth[p] : 0.f;
-                    q[7] = has ? s.odepth[p] : 0.f;
+                    q[7] = has ? (LEAN ? s.depth[p] : s.odepth[p]) : 0.f;
                     q[8] = has ? s.mn[p] : 0.f;
                     q[9] = has ? s.mt[p] : 0.f;
                     q[10] = has ? s.apn[p] : 0.f;
@@ -899,44 +943,29 @@ fail:
 // ---------------------------------------------------------------------------
 // host-side launch helpers
 // ---------------------------------------------------------------------------
-template <int NT>
+template <int NT, bool LEAN>
 cudaError_t launch_world_step_nt(const StepParams& P, const Caps& C, cudaStream_t stream) {
-    const Layout L = make_layout(C);
-    cudaError_t e = cudaFuncSetAttribute(world_step_kernel<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    const Layout L = make_layout(C, LEAN);
+    cudaError_t e = cudaFuncSetAttribute(world_step_kernel<NT, LEAN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)L.total);
     if (e != cudaSuccess) return e;
     if (P.nlist == 0) return cudaSuccess;
-    world_step_kernel<NT><<<P.nlist, NT, L.total, stream>>>(P, C, L);
+    world_step_kernel<NT, LEAN><<<P.nlist, NT, L.total, stream>>>(P, C, L);
     return cudaGetLastError();
 }
 
-cudaError_t launch_world_step(const StepParams& P, const Caps& C, int threads, cudaStream_t stream) {
+cudaError_t launch_world_step(const StepParams& P, const Caps& C, int threads, bool lean, cudaStream_t stream) {
+#define R2D_LAUNCH(NT) \
+    return lean ? launch_world_step_nt<NT, true>(P, C, stream) : launch_world_step_nt<NT, false>(P, C, stream)
     switch (threads) {
-    case 32: return launch_world_step_nt<32>(P, C, stream);
-    case 64: return launch_world_step_nt<64>(P, C, stream);
-    case 128: return launch_world_step_nt<128>(P, C, stream);
-    case 256: return launch_world_step_nt<256>(P, C, stream);
+    case 32: R2D_LAUNCH(32);
+    case 64: R2D_LAUNCH(64);
+    case 128: R2D_LAUNCH(128);
+    case 256: R2D_LAUNCH(256);
+    case 512: R2D_LAUNCH(512);
     default: return cudaErrorInvalidValue;
     }
-}
-
-template <int NT>
-cudaError_t occupancy_nt(const Caps& C, int* blocks_per_sm) {
-    const Layout L = make_layout(C);
-    cudaError_t e = cudaFuncSetAttribute(world_step_kernel<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)L.total);
-    if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, world_step_kernel<NT>, NT, L.total);
-}
-
-cudaError_t world_step_occupancy(const Caps& C, int threads, int* blocks_per_sm) {
-    switch (threads) {
-    case 32: return occupancy_nt<32>(C, blocks_per_sm);
-    case 64: return occupancy_nt<64>(C, blocks_per_sm);
-    case 128: return occupancy_nt<128>(C, blocks_per_sm);
-    case 256: return occupancy_nt<256>(C, blocks_per_sm);
-    default: return cudaErrorInvalidValue;
-    }
+#undef R2D_LAUNCH
 }
 
 }  // namespace r2d

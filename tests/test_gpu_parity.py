@@ -208,3 +208,31 @@ def test_unknown_joint_body_id_is_an_error():
         w.process(sc.dt, 1, 8)
     assert e.value.code == -2
     np.testing.assert_array_equal(w.read_state(), before)
+
+
+def test_tgs_live_depth_uses_full_layout():
+    # Two discs of radius 3000 whose centres are 10 apart: the lower-id disc is
+    # the reference, its contact depth is -5990, and approxEql(depth, depth,
+    # 1e-4) fails at that magnitude, so updateTGSDepth rotates the lever arms
+    # every substep (collision.zig:73-100).  The lean kernel hands such a world
+    # to the full layout; the result must stay bit-identical.  A 1000-unit
+    # cell keeps the spatial hash small (Solver.init's cell width argument).
+    b = scenes._Builder()
+    b.disc(0.0, 0.0, 3000.0, 0.5, vx=0.5)
+    b.disc(10.0, 0.0, 3000.0, 0.5, vx=-0.5, omega=0.3)
+    b.rect(0.0, 4000.0, 2.0, 1.0, 0.5)
+    ids, kind, opt = b.arrays()
+    sc = scenes._concat("tgs", [(ids, kind, opt)], [0.0], 1 / 60, 1, 8, 6)
+    w = World.from_scene(sc, debug=True, cell=1000.0)
+    o = Oracle.from_scene(sc)
+    o.set_hash(1000.0, 2)
+    for s in range(6):
+        w.process(sc.dt, 2, 4)
+        w.sync()
+        assert o.process(sc.dt, 2, 4, ORDER_COLOUR) == 0
+        assert_state_equal(w.read_state(), o.state(), f"tgs step {s}")
+        gk, gd, gc = w.manifolds()
+        ok, od = o.manifolds()
+        oc, _ = o.colours()
+        assert_manifolds_equal(gk, gd, gc, ok, od, oc)
+    assert abs(od[0, 9 + 6]) > 2048
