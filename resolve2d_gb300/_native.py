@@ -8,11 +8,15 @@ says so.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from pathlib import Path
 
 import numpy as np
 
 LIB_PATH = Path(__file__).resolve().parent / "_build" / "libr2d_gb300.so"
+# A different build of the same library (for A/B timing); the default is the in-tree one.
+if os.environ.get("R2D_LIB_PATH"):
+    LIB_PATH = Path(os.environ["R2D_LIB_PATH"])
 
 R2D_OK = 0
 STATUS_NAMES = {

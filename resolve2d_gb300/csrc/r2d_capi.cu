@@ -26,7 +26,8 @@
 #include "r2d_world.cuh"
 
 namespace r2d {
-cudaError_t launch_world_step(const StepParams& P, const Caps& C, int threads, bool lean, cudaStream_t stream);
+cudaError_t launch_world_step(const StepParams& P, const Caps& C, int threads, const LayoutOpts& opts,
+                              cudaStream_t stream);
 }  // namespace r2d
 
 using namespace r2d;
@@ -95,7 +96,7 @@ void init_aabb(uint8_t kind, float x, float y, float angle, float d0, float d1, 
 struct KClass {
     Caps caps{};
     int threads = 128;
-    bool lean = true;
+    LayoutOpts opts{true, false, false, false};
     std::vector<uint32_t> worlds;
     uint32_t* d_list = nullptr;
     uint32_t smem = 0;
@@ -107,7 +108,7 @@ struct Engine {
     bool own_stream = false;
     // Size classes run concurrently on auxiliary streams forked from and
     // joined back into `stream`, so one class's tail overlaps the others.
-    static constexpr int NAUX = 4;
+    static constexpr int NAUX = 16;
     cudaStream_t aux[NAUX] = {};
     cudaEvent_t ev_fork = nullptr, ev_join[NAUX] = {};
     bool verbose = false;
@@ -140,6 +141,7 @@ struct Engine {
 
     std::vector<KClass> classes;
     bool plan_dirty = true;
+    bool plan_multi_substep = false;  // layouts keep frame-start positions
 
     // debug taps
     DebugOut dbg{};
@@ -348,7 +350,7 @@ struct Engine {
     Caps caps_for(uint32_t nb, uint32_t max_nj, float rect_frac, uint32_t max_cells, uint32_t boost) const {
         const double base = cfg.capacity_scale > 0.f ? cfg.capacity_scale : 1.0;
         auto sz = [&](double v, int which) {
-            const double k = base * (double)(1u << boost_of(boost, which));
+            const double k = base * std::pow(1.25, (double)boost_of(boost, which));
             return (uint32_t)std::min(65535.0, std::max(4.0, std::ceil(v * k)));
         };
         Caps c{};
@@ -357,7 +359,7 @@ struct Engine {
         const double ppm = 1.08 + 0.92 * (double)rect_frac * rect_frac;
         c.npt = sz((2.25 * nb + 16.0) * ppm + 16.0, 1);
         c.ne = sz(std::max(2.5 * nb + 64.0, max_cells * 1.25 + 64.0), 2);
-        c.np = sz(3.5 * nb + 32.0, 3);
+        c.np = sz(3.25 * nb + 32.0, 3);
         c.hs = next_pow2((3u * c.np + 1u) / 2u);
         c.nj = max_nj;
         c.nt = table_mult * nb;
@@ -379,6 +381,12 @@ struct Engine {
         const double span = std::floor(2.0 * r / cell) + 2.0;
         const double c = span * span;
         return c > 65535.0 ? 65535u : (uint32_t)c;
+    }
+
+    LayoutOpts layout_opts(bool lean, bool multi_substep) const {
+        const bool debug = (cfg.flags & R2D_FLAG_DEBUG_TAPS) != 0;
+        // debug taps report lever arms after integration: keep frame-start positions
+        return LayoutOpts{lean, debug, multi_substep || debug, debug};
     }
 
     int smem_limit() const {
@@ -437,11 +445,11 @@ struct Engine {
                 if (d.n) rect_frac = std::max(rect_frac, (float)rects / (float)d.n);
             }
             kc.caps = caps_for(bounds[k], max_nj, rect_frac, max_cells, boost);
-            kc.lean = !(boost & BOOST_FULL);
-            // Worlds whose shared memory allows one CTA per SM get more threads:
-            // every phase is latency-bound and the per-thread share shrinks.
-            kc.threads = bounds[k] <= 64 ? 64 : (bounds[k] <= 256 ? 128 : (bounds[k] <= 320 ? 256 : 512));
-            kc.smem = make_layout(kc.caps, kc.lean).total;
+            kc.opts = layout_opts(!(boost & BOOST_FULL), plan_multi_substep);
+            // A world's phases rarely have more parallel items than this many
+            // threads; smaller CTAs let more worlds share an SM.
+            kc.threads = bounds[k] <= 64 ? 64 : (bounds[k] <= 256 ? 128 : 256);
+            kc.smem = make_layout(kc.caps, kc.opts).total;
             if ((int)kc.smem > smem_optin)
                 return fail(R2D_ERR_CAPACITY, "world class of " + std::to_string(bounds[k]) + " bodies needs " +
                                                   std::to_string(kc.smem) + " B of shared memory");
@@ -487,6 +495,10 @@ struct Engine {
     int process(float dt, uint32_t sub_steps, uint32_t iters) {
         if (sub_steps == 0) return fail(R2D_ERR_INVALID_ARGUMENT, "sub_steps must be >= 1");
         if (!d_state) return fail(R2D_ERR_INVALID_ARGUMENT, "no bodies");
+        if ((sub_steps > 1) != plan_multi_substep) {
+            plan_multi_substep = sub_steps > 1;
+            plan_dirty = true;
+        }
         if (plan_dirty) {
             int st = plan();
             if (st) return st;
@@ -498,16 +510,17 @@ struct Engine {
         if (classes.size() == 1) {
             P.world_list = classes[0].d_list;
             P.nlist = (uint32_t)classes[0].worlds.size();
-            cudaError_t e = launch_world_step(P, classes[0].caps, classes[0].threads, classes[0].lean, stream);
+            cudaError_t e = launch_world_step(P, classes[0].caps, classes[0].threads, classes[0].opts, stream);
             if (e != cudaSuccess) return fail(R2D_ERR_CUDA, std::string("world step launch: ") + cudaGetErrorString(e));
         } else if (nused > 1) {
             CUDA_TRY(cudaEventRecord(ev_fork, stream));
             for (int a = 0; a < nused; ++a) CUDA_TRY(cudaStreamWaitEvent(aux[a], ev_fork, 0));
+            // one stream per class (classes beyond NAUX share): all run at once
             for (size_t i = 0; i < classes.size(); ++i) {
                 const KClass& c = classes[i];
                 P.world_list = c.d_list;
                 P.nlist = (uint32_t)c.worlds.size();
-                cudaError_t e = launch_world_step(P, c.caps, c.threads, c.lean, aux[i % NAUX]);
+                cudaError_t e = launch_world_step(P, c.caps, c.threads, c.opts, aux[i % NAUX]);
                 if (e != cudaSuccess) return fail(R2D_ERR_CUDA, std::string("world step launch: ") + cudaGetErrorString(e));
             }
             for (int a = 0; a < nused; ++a) {
@@ -623,7 +636,7 @@ struct Engine {
         uint32_t capbits = 0;
         CUDA_TRY(cudaMemcpy(&capbits, d_capbits + w, sizeof(uint32_t), cudaMemcpyDeviceToHost));
         uint32_t boost = world_boost[w];
-        for (int attempt = 0; attempt < 8; ++attempt) {
+        for (int attempt = 0; attempt < 24; ++attempt) {
             if (capbits & (CAP_BODIES | CAP_JOINTS | CAP_COLOURS)) break;  // not a buffer size
             if (capbits & CAP_TGS) boost |= BOOST_FULL;
             const int which[4] = {CAP_MANIFOLDS, CAP_POINTS, CAP_ENTRIES, CAP_PAIRS};
@@ -634,13 +647,13 @@ struct Engine {
                     (which[i] == CAP_POINTS && (capbits & CAP_MANIFOLDS)))
                     boost += 1u << (8 * i);
             Caps c = caps_for(kc->caps.nb, kc->caps.nj, rf, cells, boost);
-            const bool lean = !(boost & BOOST_FULL);
+            const LayoutOpts opts = layout_opts(!(boost & BOOST_FULL), kc->opts.pos0);
             if (verbose)
                 fprintf(stderr, "r2d: world %u (%u bodies) outgrew buffers 0x%x at call %u; replaying with "
                                 "manifolds %u points %u entries %u pairs %u, %s layout (%u B shared)\n",
-                        w, d.n, capbits, from, c.nm, c.npt, c.ne, c.np, lean ? "lean" : "full",
-                        make_layout(c, lean).total);
-            if ((int)make_layout(c, lean).total > smem_limit()) break;
+                        w, d.n, capbits, from, c.nm, c.npt, c.ne, c.np, opts.lean ? "lean" : "full",
+                        make_layout(c, opts).total);
+            if ((int)make_layout(c, opts).total > smem_limit()) break;
             CUDA_TRY(cudaMemsetAsync(d_fail_call + w, 0xFF, sizeof(uint32_t), stream));
             CUDA_TRY(cudaMemsetAsync(d_capbits + w, 0, sizeof(uint32_t), stream));
             CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), stream));
@@ -648,7 +661,7 @@ struct Engine {
                 StepParams P = params(calls[k].dt, calls[k].sub_steps, calls[k].iters, k);
                 P.world_list = d_one;
                 P.nlist = 1;
-                cudaError_t e = launch_world_step(P, c, kc->threads, lean, stream);
+                cudaError_t e = launch_world_step(P, c, kc->threads, opts, stream);
                 if (e != cudaSuccess) return fail(R2D_ERR_CUDA, std::string("replay launch: ") + cudaGetErrorString(e));
             }
             CUDA_TRY(cudaStreamSynchronize(stream));

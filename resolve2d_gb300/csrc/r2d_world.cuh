@@ -54,8 +54,10 @@ struct Layout {
     uint32_t r1x, r1y, r2x, r2y, depth, odepth, mn, mt, apn, apt, bias;
     // broadphase scratch (inside the manifold region)
     uint32_t ax, ay, ahw, ahh, rx0, ry0, rx1, ry1, bcnt, ebucket, ebody, eslot, sbody, table, hset;
-    // colouring scratch: sort keys/indices, per-body colour masks
-    uint32_t skey, sidx, cmask;
+    // colouring scratch: sort keys, per-body colour masks
+    uint32_t skey, cmask;
+    // optional arrays (offset 0 = absent)
+    bool has_depth, has_pos0, has_prev;
     // orders
     uint32_t corder, coff, jorder, joff, jcol;
     // pairs
@@ -65,11 +67,20 @@ struct Layout {
 
 __host__ __device__ inline uint32_t r2d_align(uint32_t x, uint32_t a) { return (x + a - 1) / a * a; }
 
-// lean: contact points keep their midpoint (8 B) instead of both lever arms
-// and the original depth (12 B); the lever arms are recomputed from the
-// frame-start positions px0/py0.  Worlds with a TGS-live point (see the
-// kernel) use the full layout.
-__host__ __device__ inline Layout make_layout(const Caps& c, bool lean) {
+// Shared-memory layout of one world.
+//   lean:  contact points keep their midpoint (8 B) instead of both lever arms
+//          and the original depth; the lever arms are recomputed from the
+//          frame-start positions.  Worlds with a TGS-live point use the full
+//          layout (the kernel detects them).
+//   depth: keep each point's depth (full layout, or debug taps)
+//   pos0:  keep frame-start positions (lean with more than one substep;
+//          with one substep the positions do not move before integration)
+//   prev:  keep each body's previous-substep angle (full layout, debug taps)
+struct LayoutOpts {
+    bool lean, depth, pos0, prev;
+};
+
+__host__ __device__ inline Layout make_layout(const Caps& c, const LayoutOpts& f) {
     Layout L{};
     uint32_t o = 0;
     auto take = [&](uint32_t bytes) {
@@ -78,11 +89,15 @@ __host__ __device__ inline Layout make_layout(const Caps& c, bool lean) {
         return at;
     };
     const uint32_t nb4 = 4 * c.nb;
+    L.has_depth = f.depth || !f.lean;
+    L.has_pos0 = f.lean && f.pos0;
+    L.has_prev = f.prev || !f.lean;
     L.px = take(nb4); L.py = take(nb4); L.ang = take(nb4);
     L.mx = take(nb4); L.my = take(nb4); L.L = take(nb4);
     L.inv_m = take(nb4); L.inv_i = take(nb4);
-    L.cs = take(nb4); L.sn = take(nb4); L.ang_prev = take(nb4); L.tq = take(nb4);
-    if (lean) {
+    L.cs = take(nb4); L.sn = take(nb4); L.tq = take(nb4);
+    if (L.has_prev) L.ang_prev = take(nb4);
+    if (L.has_pos0) {
         L.px0 = take(nb4);
         L.py0 = take(nb4);
     }
@@ -95,14 +110,16 @@ __host__ __device__ inline Layout make_layout(const Caps& c, bool lean) {
     L.mnp = take(c.nm); L.mcol = take(c.nm);
     L.nx = take(nm4); L.ny = take(nm4); L.fric = take(nm4);
     L.r1x = take(np4); L.r1y = take(np4);  // lean: the contact midpoint
-    if (!lean) {
+    if (!f.lean) {
         L.r2x = take(np4);
         L.r2y = take(np4);
+        L.odepth = take(np4);
     }
-    L.depth = take(np4);
-    if (!lean) L.odepth = take(np4);
+    if (L.has_depth) L.depth = take(np4);
+    L.bias = take(np4);
+    // mn .. apt are contiguous: the colouring sorts its keys there
     L.mn = take(np4); L.mt = take(np4);
-    L.apn = take(np4); L.apt = take(np4); L.bias = take(np4);
+    L.apn = take(np4); L.apt = take(np4);
     const uint32_t xend_m = o;
     o = xbase;
     L.ax = take(nb4); L.ay = take(nb4); L.ahw = take(nb4); L.ahh = take(nb4);
@@ -125,19 +142,12 @@ __host__ __device__ inline Layout make_layout(const Caps& c, bool lean) {
     // per-body colour masks reuse them
     L.pairs = take(4 * c.np);
     L.cmask = (16 * c.nb <= 4 * c.np) ? L.pairs : take(16 * c.nb);
-    // sort scratch of the colouring: the solver's per-point arrays (mn .. bias,
-    // contiguous) are not live until the prestep that follows the colouring
+    // sort keys of the colouring (8 B each, a power-of-two count): the
+    // point arrays mn .. apt are not live until after the colouring
     const uint32_t ncon = c.nm > c.nj ? c.nm : c.nj;
     uint32_t n2 = 1;
     while (n2 < ncon) n2 <<= 1;
-    const uint32_t sort_bytes = 8 * n2 + 2 * n2;
-    if (sort_bytes <= 5 * np4) {
-        L.skey = L.mn;
-        L.sidx = L.mn + 8 * n2;
-    } else {
-        L.skey = take(8 * n2);
-        L.sidx = take(2 * n2);
-    }
+    L.skey = (8 * n2 <= 4 * np4) ? L.mn : take(8 * n2);
     L.total = o;
     return L;
 }

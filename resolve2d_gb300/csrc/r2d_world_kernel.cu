@@ -91,30 +91,23 @@ __device__ __forceinline__ void cap_fail(int* err, uint32_t* s_capbits, uint32_t
     atomicOr(s_capbits, bit);
 }
 
-// Colours `count` constraints by first-fit greedy in ascending key order
-// (key = mix << 32 | tie-break, unique per constraint; r2d_colour.h).  A
-// bitonic sort orders the keys; then one warp walks the sorted list 32 at a
-// time.  A lane takes the lowest colour absent from its nodes' colour masks
+// Colours `count` constraints by first-fit greedy in ascending priority
+// order (mix(i), then tie(i); unique per constraint; r2d_colour.h).  A
+// bitonic sort orders the constraints; then one warp walks the sorted list 32
+// at a time.  A lane takes the lowest colour absent from its nodes' colour masks
 // once every earlier lane of its chunk that shares a node is coloured, so the
 // result is exactly the sequential greedy colouring, computed with warp
 // shuffles instead of block-wide rounds.  ends(i, &a, &b) names constraint
 // i's conflict nodes (values >= 0x10000 mean "no node").  Returns true on
 // every thread when some constraint would need more than MAX_COLOURS colours.
-template <int NT, class Ends, class Key>
-__device__ bool colour_greedy_sorted(uint32_t count, uint32_t n, Ends ends, Key key, uint8_t* colour,
-                                     unsigned long long* skey, uint16_t* sidx, uint32_t* cmask) {
+template <int NT, class Ends, class Mix, class Tie>
+__device__ bool colour_greedy_sorted(uint32_t count, uint32_t n, Ends ends, Mix mix, Tie tie, uint8_t* colour,
+                                     unsigned long long* skey, uint32_t* cmask) {
     const int tid = threadIdx.x, lane = tid & 31;
     uint32_t N2 = 1;
     while (N2 < count) N2 <<= 1;
-    for (uint32_t i = tid; i < N2; i += NT) {
-        if (i < count) {
-            skey[i] = key(i);
-            sidx[i] = (uint16_t)i;
-        } else {
-            skey[i] = ~0ull;
-            sidx[i] = 0xFFFFu;
-        }
-    }
+    // key = mix << 32 | index; equal mixes are reordered by their tie key below
+    for (uint32_t i = tid; i < N2; i += NT) skey[i] = i < count ? ((unsigned long long)mix(i) << 32) | i : ~0ull;
     for (uint32_t i = tid; i < 4 * n; i += NT) cmask[i] = 0u;
     __syncthreads();
     for (uint32_t k = 2; k <= N2; k <<= 1) {
@@ -126,21 +119,37 @@ __device__ bool colour_greedy_sorted(uint32_t count, uint32_t n, Ends ends, Key 
                     if ((a > b) == ((i & k) == 0)) {
                         skey[i] = b;
                         skey[ixj] = a;
-                        const uint16_t t = sidx[i];
-                        sidx[i] = sidx[ixj];
-                        sidx[ixj] = t;
                     }
                 }
             }
             __syncthreads();
         }
     }
+    // runs of equal mix (rare): order them by the tie key, first thread of a run
+    for (uint32_t i = tid; i + 1 < count; i += NT) {
+        const uint32_t h = (uint32_t)(skey[i] >> 32);
+        if ((i == 0 || (uint32_t)(skey[i - 1] >> 32) != h) && (uint32_t)(skey[i + 1] >> 32) == h) {
+            uint32_t e = i + 1;
+            while (e < count && (uint32_t)(skey[e] >> 32) == h) ++e;
+            for (uint32_t x = i + 1; x < e; ++x) {  // insertion sort by tie key
+                const unsigned long long v = skey[x];
+                const uint32_t tv = tie((uint32_t)v);
+                uint32_t y = x;
+                while (y > i && tie((uint32_t)skey[y - 1]) > tv) {
+                    skey[y] = skey[y - 1];
+                    --y;
+                }
+                skey[y] = v;
+            }
+        }
+    }
+    __syncthreads();
     int overflow = 0;
     if (tid < 32) {
         for (uint32_t base = 0; base < count; base += 32) {
             const uint32_t i = base + lane;
             const bool valid = i < count;
-            const uint32_t ci = valid ? (uint32_t)sidx[i] : 0u;
+            const uint32_t ci = valid ? (uint32_t)skey[i] : 0u;
             uint32_t a = 0x10000u + 2u * lane, b = 0x10001u + 2u * lane;
             if (valid) ends(ci, &a, &b);
             uint32_t earlier = 0u;  // earlier lanes of this chunk sharing a node
@@ -186,6 +195,7 @@ __device__ bool colour_greedy_sorted(uint32_t count, uint32_t n, Ends ends, Key 
 // Shared-memory views of one world.
 struct SW {
     float *px, *py, *ang, *mx, *my, *L, *inv_m, *inv_i, *cs, *sn, *ang_prev, *tq, *px0, *py0;
+    bool pos0;                           // px0/py0 hold frame-start positions
     const float* __restrict__ gmass;     // this world's masses (global, read-only)
     const float* __restrict__ ginertia;  // this world's inertias
     uint8_t* kind;
@@ -203,8 +213,10 @@ struct SW {
     __device__ __forceinline__ void arms(uint32_t p, uint32_t a, uint32_t b, f2* r1, f2* r2) const {
         if (LEAN) {
             const f2 mid = {r1x[p], r1y[p]};
-            *r1 = sub2(mid, f2{px0[a], py0[a]});
-            *r2 = sub2(mid, f2{px0[b], py0[b]});
+            const float* bx = pos0 ? px0 : px;  // one substep: positions do not move before integration
+            const float* by = pos0 ? py0 : py;
+            *r1 = sub2(mid, f2{bx[a], by[a]});
+            *r2 = sub2(mid, f2{bx[b], by[b]});
         } else {
             *r1 = f2{r1x[p], r1y[p]};
             *r2 = f2{r2x[p], r2y[p]};
@@ -231,18 +243,14 @@ __device__ __forceinline__ void solve_contact(const SW& s, uint32_t m) {
     const uint32_t p0 = s.mp0[m], np = s.mnp[m];
     for (uint32_t k = 0; k < np; ++k) {
         const uint32_t p = p0 + k;
-        const float d = s.depth[p];
-        if (d >= 0.0f) {
-            s.apn[p] = 0.f;
-            s.apt[p] = 0.f;
-            continue;
-        }
+        const float bias = s.bias[p];
+        if (bias < 0.0f) continue;  // depth >= 0: accumulators stay 0 (collision.zig:154-158)
         f2 r1, r2;
         s.arms<LEAN>(p, a, b, &r1, &r2);
         const f2 v1 = add2(vlinear_1, f2{-r1.y * omega1, r1.x * omega1});
         const f2 v2 = add2(vlinear_2, f2{-r2.y * omega2, r2.x * omega2});
         const f2 dv = sub2(v1, v2);
-        float num = dot2(dv, n) + s.bias[p];  // BAUMGARTE*max(0,-depth-SLOP)/h, set in the prestep
+        float num = dot2(dv, n) + bias;  // BAUMGARTE*max(0,-depth-SLOP)/h (collision.zig:172)
         const float pn = num * s.mn[p];
         if (pn < MIN_MANIFOLD_IMPULSE) continue;
         num = dot2(dv, t);
@@ -383,8 +391,18 @@ __device__ __forceinline__ bool joint_two_bodies(uint8_t type) {
     return type == J_DISTANCE || type == J_OFFSET;
 }
 
+// Register budget per thread: low enough that several worlds share an SM
+// (the kernel is latency-bound; concurrency hides it).
+#ifndef R2D_REG_TARGET
+#define R2D_REG_TARGET 96
+#endif
+constexpr int min_blocks_for(int nt) {
+    return 65536 / (nt * R2D_REG_TARGET) > 0 ? 65536 / (nt * R2D_REG_TARGET) : 1;
+}
+
 template <int NT, bool LEAN>
-__global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, const Caps C, const Layout Lo) {
+__global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(const StepParams P, const Caps C,
+                                                                               const Layout Lo) {
     extern __shared__ __align__(16) unsigned char sm[];
     __shared__ uint32_t s_wsum[32];
     __shared__ uint32_t s_ccnt[256];
@@ -446,6 +464,7 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
     s.inv_m = SMF(Lo.inv_m); s.inv_i = SMF(Lo.inv_i);
     s.cs = SMF(Lo.cs); s.sn = SMF(Lo.sn); s.ang_prev = SMF(Lo.ang_prev); s.tq = SMF(Lo.tq);
     s.px0 = SMF(Lo.px0); s.py0 = SMF(Lo.py0);
+    s.pos0 = Lo.has_pos0;
     s.gmass = P.props + (size_t)P_MASS * NB + base;
     s.ginertia = P.props + (size_t)P_INERTIA * NB + base;
     s.kind = SMU8(Lo.kind);
@@ -464,7 +483,6 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
     uint32_t* table = SMU32(Lo.table);
     uint32_t* hset = SMU32(Lo.hset);
     unsigned long long* skey = reinterpret_cast<unsigned long long*>(sm + Lo.skey);
-    uint16_t* sidx = SMU16(Lo.sidx);
     uint32_t* cmask = SMU32(Lo.cmask);
     uint16_t *corder = SMU16(Lo.corder), *coff = SMU16(Lo.coff);
     uint16_t *jorder = SMU16(Lo.jorder), *joff = SMU16(Lo.joff);
@@ -488,7 +506,7 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
         s.L[i] = st[(size_t)S_ANG_MOM * NB + g];
         const float m = __ldg(pr + (size_t)P_MASS * NB + g);
         const float I = __ldg(pr + (size_t)P_INERTIA * NB + g);
-        if (LEAN) {
+        if (Lo.has_pos0) {
             s.px0[i] = s.px[i];
             s.py0[i] = s.py[i];
         }
@@ -499,7 +517,7 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
         if ((k & K_RECT) || disc_rot) r2d_sincosf(a, &sn, &c);
         s.cs[i] = c;
         s.sn[i] = sn;
-        s.ang_prev[i] = a;
+        if (Lo.has_prev) s.ang_prev[i] = a;
         s.tq[i] = 0.f;
         ax[i] = st[(size_t)S_AABB_X * NB + g];
         ay[i] = st[(size_t)S_AABB_Y * NB + g];
@@ -592,6 +610,7 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
     PHASE(1);
     // ---------------- narrowphase (collision.zig:299-320, lib.zig:284-294) ----------------
     {
+        const float h = P.dt / (float)P.sub_steps;
         const uint32_t npairs = s_cnt[0];
         for (uint32_t pi = tid; pi < npairs; pi += NT) {
             const uint32_t key = pairs[pi];
@@ -628,21 +647,26 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
 #pragma unroll
             for (int k = 0; k < 2; ++k) {
                 if (k >= npt) break;
+                const float d = pts[k].depth;
                 if (LEAN) {
                     s.r1x[p0 + k] = pts[k].mid.x;
                     s.r1y[p0 + k] = pts[k].mid.y;
                     // a depth for which approxEql(depth, depth, 1e-4) fails
                     // (|depth| >= 2048 or NaN) makes updateTGSDepth rotate the
                     // lever arms (collision.zig:80-95): full layout needed
-                    if (!approx_eql(pts[k].depth, pts[k].depth, 1e-4f)) cap_fail(&err, &s_capbits, CAP_TGS);
+                    if (!approx_eql(d, d, 1e-4f)) cap_fail(&err, &s_capbits, CAP_TGS);
+                    // otherwise the depth is fixed for the frame, and so is the
+                    // bias of calculateImpulses (collision.zig:154-172); a
+                    // negative bias marks a point with depth >= 0
+                    s.bias[p0 + k] = d >= 0.0f ? -1.0f : BAUMGARTE * zmax(0.0f, (-d) - BAUMGARTE_SLOP) / h;
                 } else {
                     s.r1x[p0 + k] = pts[k].ref_r.x;
                     s.r1y[p0 + k] = pts[k].ref_r.y;
                     s.r2x[p0 + k] = pts[k].inc_r.x;
                     s.r2y[p0 + k] = pts[k].inc_r.y;
-                    s.odepth[p0 + k] = pts[k].depth;
+                    s.odepth[p0 + k] = d;
                 }
-                s.depth[p0 + k] = pts[k].depth;
+                if (Lo.has_depth) s.depth[p0 + k] = d;
             }
         }
     }
@@ -662,12 +686,15 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
             if (!(s.kind[x] & K_STATIC)) *a = x;
             if (!(s.kind[y] & K_STATIC)) *b = y;
         };
-        auto contact_key = [&](uint32_t m) {
+        auto contact_mix = [&](uint32_t m) {
             const uint32_t x = s.ma[m], y = s.mb[m];
-            const uint32_t lo = min(x, y), hi = max(x, y);
-            return ((unsigned long long)r2d_colour_mix(lo, hi) << 32) | ((lo << 16) | hi);
+            return r2d_colour_mix(min(x, y), max(x, y));
         };
-        if (colour_greedy_sorted<NT>(M, n, contact_ends, contact_key, s.mcol, skey, sidx, cmask)) {
+        auto contact_tie = [&](uint32_t m) {
+            const uint32_t x = s.ma[m], y = s.mb[m];
+            return (min(x, y) << 16) | max(x, y);
+        };
+        if (colour_greedy_sorted<NT>(M, n, contact_ends, contact_mix, contact_tie, s.mcol, skey, cmask)) {
             if (tid == 0) {
                 s_err = DS_CAPACITY;
                 s_capbits |= CAP_COLOURS;
@@ -699,10 +726,9 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
                 *a = b1;
                 if (joint_two_bodies(ty) && b2 != b1) *b = b2;
             };
-            auto joint_key = [&](uint32_t j) {
-                return ((unsigned long long)r2d_colour_mix(j, R2D_COLOUR_JOINT_SALT) << 32) | j;
-            };
-            if (colour_greedy_sorted<NT>(NJ, n, joint_ends, joint_key, jcol, skey, sidx, cmask)) {
+            auto joint_mix = [&](uint32_t j) { return r2d_colour_mix(j, R2D_COLOUR_JOINT_SALT); };
+            auto joint_tie = [&](uint32_t j) { return j; };
+            if (colour_greedy_sorted<NT>(NJ, n, joint_ends, joint_mix, joint_tie, jcol, skey, cmask)) {
                 if (tid == 0) {
                     s_err = DS_CAPACITY;
                     s_capbits |= CAP_COLOURS;
@@ -810,8 +836,10 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
                     const float kt = inv_mass + inv_i1 * (r1t * r1t) + inv_i2 * (r2t * r2t);
                     s.mn[p] = kn > 0.0f ? 1.0f / kn : 0.0f;
                     s.mt[p] = kt > 0.0f ? 1.0f / kt : 0.0f;
-                    // bias of calculateImpulses (collision.zig:172): depth is fixed within a substep
-                    s.bias[p] = BAUMGARTE * zmax(0.0f, (-s.depth[p]) - BAUMGARTE_SLOP) / h;
+                    if (!LEAN) {  // bias of calculateImpulses (collision.zig:154-172); depth fixed in a substep
+                        const float d = s.depth[p];
+                        s.bias[p] = d >= 0.0f ? -1.0f : BAUMGARTE * zmax(0.0f, (-d) - BAUMGARTE_SLOP) / h;
+                    }
                 }
             }
             __syncthreads();
@@ -835,7 +863,7 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
             }
             // integration (lib.zig:238-249)
             for (uint32_t i = tid; i < n; i += NT) {
-                s.ang_prev[i] = s.ang[i];
+                if (Lo.has_prev) s.ang_prev[i] = s.ang[i];
                 const uint8_t k = s.kind[i];
                 if (k & K_STATIC) continue;
                 const float sm_ = h / s.mass(i);
@@ -884,8 +912,8 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
                 d[0] = nn.x; d[1] = nn.y; d[2] = tt.x; d[3] = tt.y; d[4] = s.fric[m];
                 d[5] = np > 0 ? 1.f : 0.f;
                 d[6] = np > 1 ? 1.f : 0.f;
-                d[7] = s.ang_prev[s.ma[m]];
-                d[8] = s.ang_prev[s.mb[m]];
+                d[7] = Lo.has_prev ? s.ang_prev[s.ma[m]] : __int_as_float(0x7fc00000);
+                d[8] = Lo.has_prev ? s.ang_prev[s.mb[m]] : __int_as_float(0x7fc00000);
                 for (uint32_t k = 0; k < 2; ++k) {
                     float* q = d + 9 + 12 * k;
                     const bool has = k < np;
@@ -898,8 +926,9 @@ __global__ void __launch_bounds__(NT) world_step_kernel(const StepParams P, cons
                     q[3] = r1.y;
                     q[4] = r2.x;
                     q[5] = r2.y;
-                    q[6] = has ? s.depth[p] : 0.f;
-                    q[7] = has ? (LEAN ? s.depth[p] : s.odepth[p]) : 0.f;
+                    const float dd = Lo.has_depth ? s.depth[p] : __int_as_float(0x7fc00000);
+                    q[6] = has ? dd : 0.f;
+                    q[7] = has ? (LEAN ? dd : s.odepth[p]) : 0.f;
                     q[8] = has ? s.mn[p] : 0.f;
                     q[9] = has ? s.mt[p] : 0.f;
                     q[10] = has ? s.apn[p] : 0.f;
@@ -944,8 +973,8 @@ fail:
 // host-side launch helpers
 // ---------------------------------------------------------------------------
 template <int NT, bool LEAN>
-cudaError_t launch_world_step_nt(const StepParams& P, const Caps& C, cudaStream_t stream) {
-    const Layout L = make_layout(C, LEAN);
+cudaError_t launch_world_step_nt(const StepParams& P, const Caps& C, const LayoutOpts& opts, cudaStream_t stream) {
+    const Layout L = make_layout(C, opts);
     cudaError_t e = cudaFuncSetAttribute(world_step_kernel<NT, LEAN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)L.total);
     if (e != cudaSuccess) return e;
@@ -954,9 +983,11 @@ cudaError_t launch_world_step_nt(const StepParams& P, const Caps& C, cudaStream_
     return cudaGetLastError();
 }
 
-cudaError_t launch_world_step(const StepParams& P, const Caps& C, int threads, bool lean, cudaStream_t stream) {
-#define R2D_LAUNCH(NT) \
-    return lean ? launch_world_step_nt<NT, true>(P, C, stream) : launch_world_step_nt<NT, false>(P, C, stream)
+cudaError_t launch_world_step(const StepParams& P, const Caps& C, int threads, const LayoutOpts& opts,
+                              cudaStream_t stream) {
+#define R2D_LAUNCH(NT)                                                        \
+    return opts.lean ? launch_world_step_nt<NT, true>(P, C, opts, stream) \
+                     : launch_world_step_nt<NT, false>(P, C, opts, stream)
     switch (threads) {
     case 32: R2D_LAUNCH(32);
     case 64: R2D_LAUNCH(64);
