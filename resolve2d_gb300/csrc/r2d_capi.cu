@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "../../include/r2d_gb300.h"
+#include "r2d_device.cuh"
 #include "r2d_sincos.h"
 #include "r2d_world.cuh"
 
@@ -463,6 +464,7 @@ struct Engine {
         }
         std::stable_sort(classes.begin(), classes.end(),
                          [](const KClass& a, const KClass& b) { return a.caps.nb > b.caps.nb; });
+        for (auto& d : worlds_h) d.bucket_recip = bucket_recip(table_mult * d.n);
         CUDA_TRY(dalloc(d_worlds, nworlds));
         CUDA_TRY(cudaMemcpyAsync(d_worlds, worlds_h.data(), sizeof(WorldDesc) * nworlds, cudaMemcpyHostToDevice, stream));
         // debug taps
@@ -607,11 +609,12 @@ struct Engine {
             for (uint32_t w : c.worlds)
                 for (int k = 0; k < PHASE_SLOTS; ++k) acc[k] += (double)t[(size_t)w * PHASE_SLOTS + k];
             const double steps = acc[11] > 0 ? acc[11] : 1;
-            fprintf(stderr, "r2d timers nb=%u thr=%d worlds=%zu smem=%u | load %.0f bp %.0f np %.0f col %.0f jcol %.0f "
-                            "solve %.0f wb %.0f cycles | pairs %.1f man %.1f colours %.1f rounds %.1f\n",
-                    c.caps.nb, c.threads, c.worlds.size(), c.smem, acc[0] / steps, acc[1] / steps, acc[2] / steps,
-                    acc[3] / steps, acc[4] / steps, acc[5] / steps, acc[6] / steps, acc[7] / steps, acc[8] / steps,
-                    acc[9] / steps, acc[10] / steps);
+            fprintf(stderr, "r2d timers nb=%u thr=%d worlds=%zu smem=%u | load %.0f bp %.0f [cells %.0f sort %.0f] "
+                            "np %.0f col %.0f [sort %.0f walk %.0f] jcol %.0f solve %.0f wb %.0f | pairs %.1f man %.1f "
+                            "colours %.1f\n",
+                    c.caps.nb, c.threads, c.worlds.size(), c.smem, acc[0] / steps, acc[1] / steps, acc[12] / steps,
+                    acc[13] / steps, acc[2] / steps, acc[3] / steps, acc[15] / steps, acc[16] / steps, acc[4] / steps,
+                    acc[5] / steps, acc[6] / steps, acc[7] / steps, acc[8] / steps, acc[9] / steps);
         }
         cudaMemset(d_timers, 0, 8 * t.size());
     }

@@ -75,9 +75,23 @@ R2D_DF float zmin(float a, float b) {
 R2D_DF float zclamp(float v, float lo, float hi) { return zmax(lo, zmin(v, hi)); }
 
 // ---- spatial hash (src/core/SpatialHash.zig:78-81) ----
-R2D_DF uint32_t cell_bucket(int64_t xi, int64_t yi, uint32_t table_size) {
-    uint64_t h = ((uint64_t)xi * 92837111ull) ^ ((uint64_t)yi * 689287499ull);
-    return (uint32_t)(h % (uint64_t)table_size);
+// u64 % table_size without a 64-bit division: Barrett reduction with
+// recip = floor((2^64 - 1) / table_size), then at most two corrections.
+// Exact for every 64-bit hash and every table size >= 1.
+struct BucketMod {
+    uint64_t recip;
+    uint32_t size;
+};
+__host__ __device__ __forceinline__ uint64_t bucket_recip(uint32_t table_size) {
+    return table_size ? 0xFFFFFFFFFFFFFFFFull / (uint64_t)table_size : 0ull;
+}
+R2D_DF uint32_t cell_bucket(int64_t xi, int64_t yi, const BucketMod& m) {
+    const uint64_t h = ((uint64_t)xi * 92837111ull) ^ ((uint64_t)yi * 689287499ull);
+    const uint64_t q = __umul64hi(h, m.recip);
+    uint64_t r = h - q * (uint64_t)m.size;
+    if (r >= m.size) r -= m.size;
+    if (r >= m.size) r -= m.size;
+    return (uint32_t)r;
 }
 
 // floor(c / cell) as the reference's @intFromFloat(@floor(..)) (SpatialHash.zig:93-96);

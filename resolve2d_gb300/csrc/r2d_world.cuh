@@ -30,6 +30,9 @@ struct WorldDesc {
     uint32_t excl_off, nexcl;
     uint32_t ngrav, flags;
     float g[MAX_GRAVITY];
+    // floor((2^64 - 1) / (table_mult * n)): Barrett reciprocal of the
+    // spatial-hash table size, so the kernel needs no 64-bit division
+    unsigned long long bucket_recip;
 };
 
 // Per-world capacities of one kernel class; every buffer below is sized
@@ -141,7 +144,7 @@ __host__ __device__ inline Layout make_layout(const Caps& c, const LayoutOpts& f
     // candidate pairs (broadphase -> narrowphase); after the narrowphase the
     // per-body colour masks reuse them
     L.pairs = take(4 * c.np);
-    L.cmask = (16 * c.nb <= 4 * c.np) ? L.pairs : take(16 * c.nb);
+    L.cmask = (20 * c.nb <= 4 * c.np) ? L.pairs : take(20 * c.nb);  // 4 colour words + lane bits
     // sort keys of the colouring (8 B each, a power-of-two count): the
     // point arrays mn .. apt are not live until after the colouring
     const uint32_t ncon = c.nm > c.nj ? c.nm : c.nj;
@@ -192,7 +195,7 @@ struct StepParams {
 // Phase timer slots (cycles, R2D_PHASE_TIMERS builds only): load,
 // broadphase, narrowphase, contact colouring, joint colouring, solve,
 // write-back, then counts: pairs, manifolds, colours, colouring rounds.
-constexpr int PHASE_SLOTS = 12;
+constexpr int PHASE_SLOTS = 20;  // 12..: sub-phases (cells, bucket sort, colour sort, colour walk)
 
 // Which per-world buffer overflowed (reported with DS_CAPACITY).
 enum CapBits : uint32_t {

@@ -100,15 +100,15 @@ __device__ __forceinline__ void cap_fail(int* err, uint32_t* s_capbits, uint32_t
 // shuffles instead of block-wide rounds.  ends(i, &a, &b) names constraint
 // i's conflict nodes (values >= 0x10000 mean "no node").  Returns true on
 // every thread when some constraint would need more than MAX_COLOURS colours.
-template <int NT, class Ends, class Mix, class Tie>
+template <int NT, class Ends, class Mix, class Tie, class Hook>
 __device__ bool colour_greedy_sorted(uint32_t count, uint32_t n, Ends ends, Mix mix, Tie tie, uint8_t* colour,
-                                     unsigned long long* skey, uint32_t* cmask) {
+                                     unsigned long long* skey, uint32_t* cmask, Hook SUBPHASE_HOOK) {
     const int tid = threadIdx.x, lane = tid & 31;
     uint32_t N2 = 1;
     while (N2 < count) N2 <<= 1;
     // key = mix << 32 | index; equal mixes are reordered by their tie key below
     for (uint32_t i = tid; i < N2; i += NT) skey[i] = i < count ? ((unsigned long long)mix(i) << 32) | i : ~0ull;
-    for (uint32_t i = tid; i < 4 * n; i += NT) cmask[i] = 0u;
+    for (uint32_t i = tid; i < 5 * n; i += NT) cmask[i] = 0u;
     __syncthreads();
     for (uint32_t k = 2; k <= N2; k <<= 1) {
         for (uint32_t j = k >> 1; j > 0; j >>= 1) {
@@ -144,26 +144,39 @@ __device__ bool colour_greedy_sorted(uint32_t count, uint32_t n, Ends ends, Mix 
         }
     }
     __syncthreads();
+    SUBPHASE_HOOK();
     int overflow = 0;
     if (tid < 32) {
-        for (uint32_t base = 0; base < count; base += 32) {
+        uint32_t* lanebits = cmask + 4 * n;  // per node: lanes of this chunk that name it
+        auto fetch = [&](uint32_t base, uint32_t* ci, uint32_t* a, uint32_t* b, bool* valid) {
             const uint32_t i = base + lane;
-            const bool valid = i < count;
-            const uint32_t ci = valid ? (uint32_t)skey[i] : 0u;
-            uint32_t a = 0x10000u + 2u * lane, b = 0x10001u + 2u * lane;
-            if (valid) ends(ci, &a, &b);
-            uint32_t earlier = 0u;  // earlier lanes of this chunk sharing a node
-#pragma unroll 8
-            for (int j = 0; j < 32; ++j) {
-                const uint32_t aj = __shfl_sync(0xffffffffu, a, j), bj = __shfl_sync(0xffffffffu, b, j);
-                if (j < lane && (aj == a || aj == b || bj == a || bj == b)) earlier |= 1u << j;
-            }
+            *valid = i < count;
+            *ci = *valid ? (uint32_t)skey[i] : 0u;
+            *a = 0x10000u + 2u * lane;
+            *b = 0x10001u + 2u * lane;
+            if (*valid) ends(*ci, a, b);
+        };
+        uint32_t ci, a, b;
+        bool valid;
+        fetch(0, &ci, &a, &b, &valid);
+        for (uint32_t base = 0; base < count; base += 32) {
+            const bool na = a < 0x10000u, nb2 = b < 0x10000u;
+            if (na) atomicOr(&lanebits[a], 1u << lane);
+            if (nb2) atomicOr(&lanebits[b], 1u << lane);
+            __syncwarp();
+            // earlier lanes of this chunk sharing a node
+            const uint32_t earlier = ((na ? lanebits[a] : 0u) | (nb2 ? lanebits[b] : 0u)) & ((1u << lane) - 1u);
+            __syncwarp();
+            if (na) lanebits[a] = 0u;
+            if (nb2) lanebits[b] = 0u;
+            uint32_t nci, nxa, nxb;  // the next chunk, fetched while this one resolves
+            bool nvalid;
+            fetch(base + 32, &nci, &nxa, &nxb, &nvalid);
             bool done = !valid;
             for (int round = 0; round < 32; ++round) {
                 const uint32_t pending = __ballot_sync(0xffffffffu, !done);
                 if (!pending) break;
                 if (!done && !(earlier & pending)) {
-                    const bool na = a < 0x10000u, nb2 = b < 0x10000u;
                     uint32_t w0 = 0u, w1 = 0u, w2 = 0u, w3 = 0u;
                     if (na) {
                         w0 |= cmask[a]; w1 |= cmask[n + a]; w2 |= cmask[2 * n + a]; w3 |= cmask[3 * n + a];
@@ -187,6 +200,10 @@ __device__ bool colour_greedy_sorted(uint32_t count, uint32_t n, Ends ends, Mix 
                 }
                 __syncwarp();
             }
+            ci = nci;
+            a = nxa;
+            b = nxb;
+            valid = nvalid;
         }
     }
     return __syncthreads_or(overflow) != 0;
@@ -437,6 +454,7 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
 #ifdef R2D_PHASE_TIMERS
     long long t_mark = clock64();
     const uint32_t jp_rounds = 0;
+    long long t_sub = t_mark;
 #define PHASE(k)                                                              \
     do {                                                                      \
         __syncthreads();                                                      \
@@ -444,11 +462,24 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
             const long long t_now = clock64();                                \
             P.timers[(size_t)w * PHASE_SLOTS + (k)] += (unsigned long long)(t_now - t_mark); \
             t_mark = t_now;                                                   \
+            t_sub = t_now;                                                    \
+        }                                                                     \
+    } while (0)
+#define SUBPHASE(k)                                                           \
+    do {                                                                      \
+        __syncthreads();                                                      \
+        if (tid == 0 && P.timers) {                                           \
+            const long long t_now = clock64();                                \
+            P.timers[(size_t)w * PHASE_SLOTS + (k)] += (unsigned long long)(t_now - t_sub); \
+            t_sub = t_now;                                                    \
         }                                                                     \
     } while (0)
 #else
 #define PHASE(k) \
     do {         \
+    } while (0)
+#define SUBPHASE(k) \
+    do {            \
     } while (0)
 #endif
 
@@ -549,6 +580,7 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
     if (err) set_err(&s_err, err);
     if (__syncthreads_or(err != 0)) goto fail;
     {
+        SUBPHASE(12);
         const uint32_t E = block_scan_excl<NT>(bcnt, n, s_wsum);
         if (E > C.ne) {
             if (tid == 0) {
@@ -558,11 +590,12 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
             __syncthreads();
             goto fail;
         }
+        const BucketMod bmod = {wd.bucket_recip, T};
         for (uint32_t i = tid; i < n; i += NT) {
             uint32_t k = bcnt[i];
             for (int32_t yi = ry0[i]; yi <= ry1[i]; ++yi)
                 for (int32_t xi = rx0[i]; xi <= rx1[i]; ++xi) {
-                    const uint32_t bk = cell_bucket(xi, yi, T);
+                    const uint32_t bk = cell_bucket(xi, yi, bmod);
                     ebucket[k] = bk;
                     ebody[k] = (uint16_t)i;
                     atomicAdd(&table[bk], 1u);
@@ -577,6 +610,7 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
             eslot[e] = (uint16_t)slot;
         }
         __syncthreads();  // table[b] = one past the last slot of bucket b
+        SUBPHASE(13);
 
         // Candidates: every two entries of one bucket (the reference's query
         // returns all bodies of the buckets a body covers), filtered as
@@ -585,13 +619,16 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
         for (uint32_t e = tid; e < E; e += NT) {
             const uint32_t i = ebody[e];
             const uint32_t end = table[ebucket[e]];
+            const f2 pi = {ax[i], ay[i]};
+            const float hwi = ahw[i], hhi = ahh[i];
+            const bool sti = (s.kind[i] & K_STATIC) != 0;
             for (uint32_t q = (uint32_t)eslot[e] + 1u; q < end; ++q) {
                 const uint32_t j = sbody[q];
                 if (j == i) continue;
+                if (sti && (s.kind[j] & K_STATIC)) continue;
+                // symmetric in the two bodies: |dx|, |dy| and the sums commute
+                if (!aabb_intersects(pi, hwi, hhi, f2{ax[j], ay[j]}, ahw[j], ahh[j])) continue;
                 const uint32_t lo = min(i, j), hi = max(i, j);
-                if (s.kind[lo] & s.kind[hi] & K_STATIC) continue;
-                if (!aabb_intersects(f2{ax[lo], ay[lo]}, ahw[lo], ahh[lo], f2{ax[hi], ay[hi]}, ahw[hi], ahh[hi]))
-                    continue;
                 const uint32_t key = (lo << 16) | hi;
                 if (wd.nexcl && excluded(P.excl + wd.excl_off, wd.nexcl, key)) continue;
                 if (hs_insert(hset, C.hs - 1u, key, &err)) {
@@ -694,7 +731,8 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
             const uint32_t x = s.ma[m], y = s.mb[m];
             return (min(x, y) << 16) | max(x, y);
         };
-        if (colour_greedy_sorted<NT>(M, n, contact_ends, contact_mix, contact_tie, s.mcol, skey, cmask)) {
+        if (colour_greedy_sorted<NT>(M, n, contact_ends, contact_mix, contact_tie, s.mcol, skey, cmask,
+                                     [&]() { SUBPHASE(15); })) {
             if (tid == 0) {
                 s_err = DS_CAPACITY;
                 s_capbits |= CAP_COLOURS;
@@ -702,6 +740,7 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
             __syncthreads();
             goto fail;
         }
+        SUBPHASE(16);
         // colour-major order
         for (uint32_t c = tid; c < 256; c += NT) s_ccnt[c] = 0u;
         __syncthreads();
@@ -728,7 +767,7 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
             };
             auto joint_mix = [&](uint32_t j) { return r2d_colour_mix(j, R2D_COLOUR_JOINT_SALT); };
             auto joint_tie = [&](uint32_t j) { return j; };
-            if (colour_greedy_sorted<NT>(NJ, n, joint_ends, joint_mix, joint_tie, jcol, skey, cmask)) {
+            if (colour_greedy_sorted<NT>(NJ, n, joint_ends, joint_mix, joint_tie, jcol, skey, cmask, [&]() {})) {
                 if (tid == 0) {
                     s_err = DS_CAPACITY;
                     s_capbits |= CAP_COLOURS;
