@@ -42,7 +42,7 @@ typedef enum r2d_status {
     R2D_ERR_INVALID_BODY_ID = -2, /* error.InvalidRigidBodyId (src/core/Constraints/DistanceJoint.zig:44-47) */
     R2D_ERR_OUT_OF_MEMORY = -3,   /* error.OutOfMemory */
     R2D_ERR_CUDA = -4,            /* a CUDA runtime call failed (see r2d_last_error_string) */
-    R2D_ERR_CAPACITY = -5,        /* a world outgrew the per-world capacity of its kernel class */
+    R2D_ERR_CAPACITY = -5,        /* a hard limit: more than 128 colours, or more than 64Mi spatial-hash cells */
     R2D_ERR_TIMEOUT = -6,         /* a bounded device-side wait gave up */
     R2D_ERR_NONFINITE = -7,       /* an AABB coordinate is not a representable spatial-hash cell */
     R2D_ERR_NO_DEVICE = -8        /* no CUDA device is visible */
@@ -92,7 +92,11 @@ enum { R2D_JOINT_PARAMS = 8 };
 enum { R2D_MANIFOLD_FLOATS = 33 };
 
 enum {
-    R2D_FLAG_DEBUG_TAPS = 1u /* keep manifolds and colours for r2d_*_get_manifolds */
+    R2D_FLAG_DEBUG_TAPS = 1u, /* keep manifolds and colours for r2d_*_get_manifolds */
+    /* Step every world through the grid-wide pipeline that worlds above 520
+     * bodies always use (global scratch, one kernel per phase and colour)
+     * instead of the fused one-CTA-per-world kernel.  Same results. */
+    R2D_FLAG_GRID_PIPELINE = 2u
 };
 
 typedef struct r2d_config {

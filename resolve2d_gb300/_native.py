@@ -31,6 +31,7 @@ STATUS_NAMES = {
     -8: "R2D_ERR_NO_DEVICE",
 }
 FLAG_DEBUG_TAPS = 1
+FLAG_GRID_PIPELINE = 2
 MANIFOLD_FLOATS = 33
 
 

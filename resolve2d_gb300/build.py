@@ -22,7 +22,7 @@ BUILD = PKG / "_build"
 LIB = BUILD / "libr2d_gb300.so"
 INCLUDE = REPO / "include"
 
-SOURCES = ["r2d_world_kernel.cu", "r2d_capi.cu"]
+SOURCES = ["r2d_world_kernel.cu", "r2d_large.cu", "r2d_capi.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
     "-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-prec-div=true", "-prec-sqrt=true",

@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <exception>
+#include <memory>
 #include <new>
 #include <cmath>
 #include <cstdio>
@@ -23,6 +24,7 @@
 
 #include "../../include/r2d_gb300.h"
 #include "r2d_device.cuh"
+#include "r2d_large.h"
 #include "r2d_sincos.h"
 #include "r2d_world.cuh"
 
@@ -135,10 +137,10 @@ struct Engine {
     // joints / exclusions (resolved to world-local indices)
     uint32_t njoints = 0, nexcl = 0;
     uint8_t* d_jtype = nullptr;
-    uint16_t* d_jb1 = nullptr;
-    uint16_t* d_jb2 = nullptr;
+    uint32_t* d_jb1 = nullptr;
+    uint32_t* d_jb2 = nullptr;
     float* d_jprm = nullptr;
-    uint32_t* d_excl = nullptr;
+    unsigned long long* d_excl = nullptr;
 
     std::vector<KClass> classes;
     bool plan_dirty = true;
@@ -172,7 +174,21 @@ struct Engine {
     static uint32_t boost_of(uint32_t b, int i) { return (b >> (8 * i)) & 0x7Fu; }
     static constexpr uint32_t BOOST_FULL = 0x80000000u;  // world needs the full point layout
 
+    // Worlds above the largest fused class, or that outgrew its shared
+    // memory, step through the grid-wide pipeline of r2d_large.cu on their
+    // own stream while the fused classes run.
+    static constexpr uint32_t FUSED_MAX_BODIES = 520;
+    std::vector<uint8_t> world_large;                 // [nworlds] routed to the large path
+    std::vector<uint32_t> large_list;                 // those worlds, in index order
+    std::vector<std::unique_ptr<LargeWorld>> large;   // [nworlds] scratch of each large world
+    std::vector<int> large_status;                    // [nworlds] status of its last step
+    std::vector<uint8_t> large_frozen;                // failed since the last sync
+    std::string large_msg;
+    cudaStream_t lstream = nullptr;
+    cudaEvent_t ev_ljoin = nullptr;
+
     ~Engine() {
+        large.clear();
         dfree(d_state); dfree(d_props); dfree(d_kind); dfree(d_ids); dfree(d_worlds);
         dfree(d_status); dfree(d_err);
         if (h_err) cudaFreeHost(h_err);
@@ -185,6 +201,8 @@ struct Engine {
             if (ev_join[a]) cudaEventDestroy(ev_join[a]);
         }
         if (ev_fork) cudaEventDestroy(ev_fork);
+        if (lstream) cudaStreamDestroy(lstream);
+        if (ev_ljoin) cudaEventDestroy(ev_ljoin);
         if (own_stream && stream) cudaStreamDestroy(stream);
     }
 
@@ -207,6 +225,8 @@ struct Engine {
             CUDA_TRY(cudaEventCreateWithFlags(&ev_join[a], cudaEventDisableTiming));
         }
         CUDA_TRY(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+        CUDA_TRY(cudaStreamCreateWithFlags(&lstream, cudaStreamNonBlocking));
+        CUDA_TRY(cudaEventCreateWithFlags(&ev_ljoin, cudaEventDisableTiming));
         const char* v = getenv("R2D_VERBOSE");
         verbose = v && v[0] && v[0] != '0';
         return R2D_OK;
@@ -256,7 +276,15 @@ struct Engine {
         CUDA_TRY(cudaMemsetAsync(d_timers, 0, sizeof(unsigned long long) * nw * PHASE_SLOTS, stream));
 #endif
         CUDA_TRY(cudaMemsetAsync(d_fail_call, 0xFF, sizeof(uint32_t) * nw, stream));
+        CUDA_TRY(cudaMemsetAsync(d_status, 0, sizeof(int) * nw, stream));
         world_boost.assign(nw, 0);
+        world_large.assign(nw, 0);
+        const bool grid_all = (cfg.flags & R2D_FLAG_GRID_PIPELINE) != 0;
+        for (uint32_t w = 0; w < nw; ++w) world_large[w] = grid_all || worlds_h[w].n > FUSED_MAX_BODIES;
+        large.clear();
+        large.resize(nw);
+        large_status.assign(nw, 0);
+        large_frozen.assign(nw, 0);
         calls.clear();
         pending = false;
         CUDA_TRY(cudaMemcpyAsync(d_state, state_h.data(), sizeof(float) * S_NFIELDS * n, cudaMemcpyHostToDevice, stream));
@@ -283,16 +311,16 @@ struct Engine {
 
     // Joints / exclusions already resolved to world-local indices.
     int set_constraints(const std::vector<uint32_t>& jworld, const std::vector<uint8_t>& jtype,
-                        const std::vector<uint16_t>& jb1, const std::vector<uint16_t>& jb2,
+                        const std::vector<uint32_t>& jb1, const std::vector<uint32_t>& jb2,
                         const std::vector<float>& jprm, const std::vector<uint32_t>& xworld,
-                        const std::vector<uint32_t>& xkey) {
+                        const std::vector<unsigned long long>& xkey) {
         // joints are grouped per world in the order given (insertion order inside a world)
         njoints = (uint32_t)jtype.size();
         std::vector<uint32_t> order(njoints);
         for (uint32_t j = 0; j < njoints; ++j) order[j] = j;
         std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return jworld[a] < jworld[b]; });
         std::vector<uint8_t> t(njoints);
-        std::vector<uint16_t> b1(njoints), b2(njoints);
+        std::vector<uint32_t> b1(njoints), b2(njoints);
         std::vector<float> p((size_t)njoints * JOINT_PARAMS);
         for (auto& d : worlds_h) {
             d.joint_off = 0;
@@ -314,15 +342,15 @@ struct Engine {
             if (jtype[j] == J_OFFSET) d.flags |= W_DISC_ROTATION;
         }
         nexcl = (uint32_t)xkey.size();
-        std::vector<uint64_t> xs(nexcl);
-        for (uint32_t k = 0; k < nexcl; ++k) xs[k] = ((uint64_t)xworld[k] << 32) | xkey[k];
+        std::vector<std::pair<uint32_t, unsigned long long>> xs(nexcl);
+        for (uint32_t k = 0; k < nexcl; ++k) xs[k] = {xworld[k], xkey[k]};
         std::sort(xs.begin(), xs.end());
         xs.erase(std::unique(xs.begin(), xs.end()), xs.end());
         nexcl = (uint32_t)xs.size();
-        std::vector<uint32_t> xk(nexcl);
+        std::vector<unsigned long long> xk(nexcl);
         for (uint32_t k = 0; k < nexcl; ++k) {
-            const uint32_t w = (uint32_t)(xs[k] >> 32);
-            xk[k] = (uint32_t)xs[k];
+            const uint32_t w = xs[k].first;
+            xk[k] = xs[k].second;
             WorldDesc& d = worlds_h[w];
             if (d.nexcl == 0) d.excl_off = k;
             d.nexcl++;
@@ -334,11 +362,11 @@ struct Engine {
         CUDA_TRY(dalloc(d_excl, nexcl));
         if (njoints) {
             CUDA_TRY(cudaMemcpyAsync(d_jtype, t.data(), njoints, cudaMemcpyHostToDevice, stream));
-            CUDA_TRY(cudaMemcpyAsync(d_jb1, b1.data(), 2 * njoints, cudaMemcpyHostToDevice, stream));
-            CUDA_TRY(cudaMemcpyAsync(d_jb2, b2.data(), 2 * njoints, cudaMemcpyHostToDevice, stream));
+            CUDA_TRY(cudaMemcpyAsync(d_jb1, b1.data(), 4 * njoints, cudaMemcpyHostToDevice, stream));
+            CUDA_TRY(cudaMemcpyAsync(d_jb2, b2.data(), 4 * njoints, cudaMemcpyHostToDevice, stream));
             CUDA_TRY(cudaMemcpyAsync(d_jprm, p.data(), sizeof(float) * p.size(), cudaMemcpyHostToDevice, stream));
         }
-        if (nexcl) CUDA_TRY(cudaMemcpyAsync(d_excl, xk.data(), 4 * nexcl, cudaMemcpyHostToDevice, stream));
+        if (nexcl) CUDA_TRY(cudaMemcpyAsync(d_excl, xk.data(), 8 * nexcl, cudaMemcpyHostToDevice, stream));
         CUDA_TRY(cudaStreamSynchronize(stream));
         plan_dirty = true;
         return R2D_OK;
@@ -407,26 +435,44 @@ struct Engine {
         for (auto& c : classes) dfree(c.d_list);
         classes.clear();
         // size classes by body count: bounds in bodies
-        static const uint32_t bounds[] = {32, 64, 96, 128, 160, 192, 256, 320, 384, 448, 520};
-        const int nbnd = sizeof(bounds) / sizeof(bounds[0]);
+        static constexpr uint32_t bounds[] = {32, 64, 96, 128, 160, 192, 256, 320, 384, 448, 520};
+        constexpr int nbnd = sizeof(bounds) / sizeof(bounds[0]);
+        static_assert(bounds[nbnd - 1] == FUSED_MAX_BODIES, "largest fused class");
+        auto bound_of = [&](uint32_t n) {
+            int k = 0;
+            while (k < nbnd - 1 && n > bounds[k]) ++k;
+            return k;
+        };
+        const int smem_optin = smem_limit();
+        // A world whose own buffers do not fit one CTA's shared memory (many
+        // spatial-hash cells, say) takes the grid-wide pipeline.
+        for (uint32_t w = 0; w < nworlds; ++w) {
+            if (world_large[w]) continue;
+            const WorldDesc& d = worlds_h[w];
+            uint32_t rects = 0, cells = 0;
+            for (uint32_t i = d.body_off; i < d.body_off + d.n; ++i) {
+                rects += (kind_h[i] & K_RECT) ? 1u : 0u;
+                cells += cells_of(i);
+            }
+            const float rf = d.n ? (float)rects / (float)d.n : 0.f;
+            const Caps c = caps_for(bounds[bound_of(d.n)], d.nj, rf, cells, world_boost[w]);
+            if ((int)make_layout(c, layout_opts(!(world_boost[w] & BOOST_FULL), plan_multi_substep)).total > smem_optin)
+                world_large[w] = 1;
+        }
         std::vector<uint32_t> boosts;  // distinct boost patterns in use
-        for (uint32_t w = 0; w < nworlds; ++w)
+        for (uint32_t w = 0; w < nworlds; ++w) {
+            if (world_large[w]) continue;
             if (std::find(boosts.begin(), boosts.end(), world_boost[w]) == boosts.end()) boosts.push_back(world_boost[w]);
+        }
         std::sort(boosts.begin(), boosts.end());
         const int NBOOST = (int)boosts.size();
         std::vector<std::vector<uint32_t>> groups(nbnd * NBOOST);
         for (uint32_t w = 0; w < nworlds; ++w) {
-            const uint32_t n = worlds_h[w].n;
-            int k = 0;
-            while (k < nbnd - 1 && n > bounds[k]) ++k;
-            if (n > bounds[nbnd - 1])
-                return fail(R2D_ERR_CAPACITY, "world " + std::to_string(w) + " has " + std::to_string(n) +
-                                                  " bodies; the fused kernel holds at most " +
-                                                  std::to_string(bounds[nbnd - 1]));
+            if (world_large[w]) continue;
+            const int k = bound_of(worlds_h[w].n);
             const int bi = (int)(std::find(boosts.begin(), boosts.end(), world_boost[w]) - boosts.begin());
             groups[k * NBOOST + bi].push_back(w);
         }
-        const int smem_optin = smem_limit();
         for (int gk = 0; gk < nbnd * NBOOST; ++gk) {
             const int k = gk / NBOOST;
             const uint32_t boost = boosts[gk % NBOOST];
@@ -451,9 +497,11 @@ struct Engine {
             // threads; smaller CTAs let more worlds share an SM.
             kc.threads = bounds[k] <= 64 ? 64 : (bounds[k] <= 256 ? 128 : 256);
             kc.smem = make_layout(kc.caps, kc.opts).total;
-            if ((int)kc.smem > smem_optin)
-                return fail(R2D_ERR_CAPACITY, "world class of " + std::to_string(bounds[k]) + " bodies needs " +
-                                                  std::to_string(kc.smem) + " B of shared memory");
+            if ((int)kc.smem > smem_optin) {
+                // each world fits alone, their maxima together do not
+                for (uint32_t w : groups[gk]) world_large[w] = 1;
+                continue;
+            }
             // largest worlds first: the longest tasks start earliest
             std::stable_sort(groups[gk].begin(), groups[gk].end(),
                              [&](uint32_t a, uint32_t b) { return worlds_h[a].n > worlds_h[b].n; });
@@ -464,6 +512,12 @@ struct Engine {
         }
         std::stable_sort(classes.begin(), classes.end(),
                          [](const KClass& a, const KClass& b) { return a.caps.nb > b.caps.nb; });
+        large_list.clear();
+        for (uint32_t w = 0; w < nworlds; ++w) {
+            if (!world_large[w]) continue;
+            large_list.push_back(w);
+            if (!large[w]) large[w].reset(new LargeWorld());
+        }
         for (auto& d : worlds_h) d.bucket_recip = bucket_recip(table_mult * d.n);
         CUDA_TRY(dalloc(d_worlds, nworlds));
         CUDA_TRY(cudaMemcpyAsync(d_worlds, worlds_h.data(), sizeof(WorldDesc) * nworlds, cudaMemcpyHostToDevice, stream));
@@ -509,13 +563,13 @@ struct Engine {
         StepParams P = params(dt, sub_steps, iters, (uint32_t)calls.size());
         calls.push_back(CallRec{dt, sub_steps, iters});
         const int nused = (int)std::min<size_t>(classes.size(), (size_t)NAUX);
+        if (nused > 1 || !large_list.empty()) CUDA_TRY(cudaEventRecord(ev_fork, stream));
         if (classes.size() == 1) {
             P.world_list = classes[0].d_list;
             P.nlist = (uint32_t)classes[0].worlds.size();
             cudaError_t e = launch_world_step(P, classes[0].caps, classes[0].threads, classes[0].opts, stream);
             if (e != cudaSuccess) return fail(R2D_ERR_CUDA, std::string("world step launch: ") + cudaGetErrorString(e));
         } else if (nused > 1) {
-            CUDA_TRY(cudaEventRecord(ev_fork, stream));
             for (int a = 0; a < nused; ++a) CUDA_TRY(cudaStreamWaitEvent(aux[a], ev_fork, 0));
             // one stream per class (classes beyond NAUX share): all run at once
             for (size_t i = 0; i < classes.size(); ++i) {
@@ -531,7 +585,72 @@ struct Engine {
             }
         }
         pending = true;
+        if (!large_list.empty()) {
+            // the fused launches above are queued: the large worlds' host-driven
+            // pipelines run while they execute
+            CUDA_TRY(cudaStreamWaitEvent(lstream, ev_fork, 0));
+            for (uint32_t w : large_list) {
+                int st = step_large(w, dt, sub_steps, iters, lstream);
+                if (st) return st;
+            }
+            CUDA_TRY(cudaEventRecord(ev_ljoin, lstream));
+            CUDA_TRY(cudaStreamWaitEvent(stream, ev_ljoin, 0));
+        }
         return R2D_OK;
+    }
+
+    LargeInputs large_inputs(uint32_t w) const {
+        const WorldDesc& d = worlds_h[w];
+        LargeInputs in{};
+        in.state = d_state;
+        in.props = d_props;
+        in.kind = d_kind;
+        in.ids = d_ids;
+        in.NB = nbodies;
+        in.base = d.body_off;
+        in.n = d.n;
+        in.jtype = d_jtype + d.joint_off;
+        in.jb1 = d_jb1 + d.joint_off;
+        in.jb2 = d_jb2 + d.joint_off;
+        in.jprm = d_jprm + (size_t)d.joint_off * JOINT_PARAMS;
+        in.nj = d.nj;
+        in.excl = d_excl + d.excl_off;
+        in.nexcl = d.nexcl;
+        in.ngrav = d.ngrav;
+        for (int k = 0; k < MAX_GRAVITY; ++k) in.g[k] = d.g[k];
+        in.cell = cell;
+        in.table_mult = table_mult;
+        in.disc_rot = (d.flags & W_DISC_ROTATION) != 0;
+        return in;
+    }
+
+    // One call of a large world.  A world whose step fails (a non-finite
+    // AABB, more than MAX_COLOURS colours) keeps the state before that call
+    // and stays frozen until sync reports it, as a fused world does; CUDA
+    // errors are returned at once.
+    int step_large(uint32_t w, float dt, uint32_t sub_steps, uint32_t iters, cudaStream_t st) {
+        if (large_frozen[w]) return R2D_OK;
+        std::string msg;
+        const int r = large[w]->step(large_inputs(w), dt, sub_steps, iters, st, &msg);
+        large_status[w] = r;
+        if (r == R2D_ERR_CUDA || r == R2D_ERR_OUT_OF_MEMORY) return fail(r, "world " + std::to_string(w) + ": " + msg);
+        if (r != R2D_OK) {
+            large_frozen[w] = 1;
+            if (large_msg.empty()) large_msg = "world " + std::to_string(w) + ": " + msg;
+        }
+        return R2D_OK;
+    }
+
+    // First error of a large world since the last sync (0 if none); unfreezes them.
+    int take_large_error(std::string* msg) {
+        int first = R2D_OK;
+        for (uint32_t w : large_list) {
+            if (large_frozen[w] && first == R2D_OK) first = large_status[w];
+            large_frozen[w] = 0;
+        }
+        *msg = large_msg;
+        large_msg.clear();
+        return first;
     }
 
     StepParams params(float dt, uint32_t sub_steps, uint32_t iters, uint32_t call_index) const {
@@ -569,9 +688,12 @@ struct Engine {
 #endif
         if (!pending) return R2D_OK;
         pending = false;
+        std::string lmsg;
+        const int lerr = take_large_error(&lmsg);
         CUDA_TRY(cudaMemcpy(h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost));
         if (*h_err == 0) {
             calls.clear();
+            if (lerr != R2D_OK) return fail(lerr, lmsg);
             return R2D_OK;
         }
         std::vector<uint32_t> fail_call(nworlds);
@@ -594,8 +716,9 @@ struct Engine {
             }
         }
         calls.clear();
-        if (first_err != R2D_OK) return fail(first_err, first_msg);
         plan_dirty = true;  // boosted worlds move to larger classes from the next call
+        if (first_err != R2D_OK) return fail(first_err, first_msg);
+        if (lerr != R2D_OK) return fail(lerr, lmsg);
         return R2D_OK;
     }
 
@@ -682,8 +805,24 @@ struct Engine {
                 return fail(st, "world " + std::to_string(w) + " failed with status " + std::to_string(st));
             from = fc;
         }
-        return fail(R2D_ERR_CAPACITY, "world " + std::to_string(w) +
-                                          " outgrew the largest shared-memory budget of the fused kernel");
+        if (capbits & CAP_COLOURS)
+            return fail(R2D_ERR_CAPACITY, "world " + std::to_string(w) + " needs more than " +
+                                              std::to_string(MAX_COLOURS) + " colours");
+        // Outgrew the largest shared-memory budget: from now on the world
+        // steps through the large-world pipeline, starting with the calls
+        // it has not done yet.
+        if (verbose)
+            fprintf(stderr, "r2d: world %u (%u bodies) moves to the large-world path at call %u\n", w, d.n, from);
+        world_large[w] = 1;
+        large[w].reset(new LargeWorld());
+        for (uint32_t k = from; k < calls.size(); ++k) {
+            std::string msg;
+            const int r = large[w]->step(large_inputs(w), calls[k].dt, calls[k].sub_steps, calls[k].iters, stream, &msg);
+            large_status[w] = r;
+            if (r != R2D_OK) return fail(r, "world " + std::to_string(w) + ": " + msg);
+        }
+        CUDA_TRY(cudaMemsetAsync(d_status + w, 0, sizeof(int), stream));
+        return R2D_OK;
     }
 
     int world_status(int* out) {
@@ -691,14 +830,22 @@ struct Engine {
         (void)st;
         status_h.assign(nworlds, 0);
         if (nworlds) CUDA_TRY(cudaMemcpy(status_h.data(), d_status, sizeof(int) * nworlds, cudaMemcpyDeviceToHost));
+        for (uint32_t w = 0; w < nworlds; ++w)
+            if (world_large[w]) status_h[w] = large_status[w];
         std::copy(status_h.begin(), status_h.end(), out);
         return R2D_OK;
     }
 
+    bool debug_taps() const { return (cfg.flags & R2D_FLAG_DEBUG_TAPS) != 0; }
+
     int num_manifolds(uint32_t w, uint32_t* out) {
-        if (!dbg.cap) return fail(R2D_ERR_INVALID_ARGUMENT, "debug taps are off (R2D_FLAG_DEBUG_TAPS)");
+        if (!debug_taps()) return fail(R2D_ERR_INVALID_ARGUMENT, "debug taps are off (R2D_FLAG_DEBUG_TAPS)");
         if (w >= nworlds) return fail(R2D_ERR_INVALID_ARGUMENT, "world index out of range");
         CUDA_TRY(cudaStreamSynchronize(stream));
+        if (world_large[w]) {
+            *out = large[w] ? large[w]->num_manifolds() : 0u;
+            return R2D_OK;
+        }
         CUDA_TRY(cudaMemcpy(out, d_dbg_nman + w, 4, cudaMemcpyDeviceToHost));
         return R2D_OK;
     }
@@ -707,6 +854,12 @@ struct Engine {
         uint32_t m = 0;
         int st = num_manifolds(w, &m);
         if (st) return st;
+        if (world_large[w]) {
+            if (!large[w]) return R2D_OK;
+            std::string msg;
+            const int r = large[w]->dump(cap, keys, data, colours, stream, &msg);
+            return r ? fail(r, msg) : R2D_OK;
+        }
         m = std::min(m, std::min(cap, dbg.cap));
         const size_t o = (size_t)w * dbg.cap;
         if (keys) CUDA_TRY(cudaMemcpy(keys, d_dbg_keys + 2 * o, 8 * (size_t)m, cudaMemcpyDeviceToHost));
@@ -716,8 +869,15 @@ struct Engine {
     }
 
     int get_joint_colours(uint32_t w, uint32_t cap, uint32_t* colours) {
-        if (!dbg.cap) return fail(R2D_ERR_INVALID_ARGUMENT, "debug taps are off (R2D_FLAG_DEBUG_TAPS)");
+        if (!debug_taps()) return fail(R2D_ERR_INVALID_ARGUMENT, "debug taps are off (R2D_FLAG_DEBUG_TAPS)");
+        if (w >= nworlds) return fail(R2D_ERR_INVALID_ARGUMENT, "world index out of range");
         CUDA_TRY(cudaStreamSynchronize(stream));
+        if (world_large[w]) {
+            if (!large[w]) return R2D_OK;
+            std::string msg;
+            const int r = large[w]->joint_colours(cap, colours, stream, &msg);
+            return r ? fail(r, msg) : R2D_OK;
+        }
         const uint32_t m = std::min(std::min(cap, dbg.jcap), worlds_h[w].nj);
         if (m) CUDA_TRY(cudaMemcpy(colours, d_dbg_jcol + (size_t)w * dbg.jcap, 4 * (size_t)m, cudaMemcpyDeviceToHost));
         return R2D_OK;
@@ -787,7 +947,6 @@ R2D_API int r2d_solver_destroy(r2d_solver* s) {
 R2D_API int r2d_solver_set_bodies(r2d_solver* s, uint32_t n, const uint32_t* ids, const uint8_t* kind,
                                   const float* props, const float* state, int init_aabb) {
     if (!s || (n && (!ids || !kind || !props || !state))) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
-    if (n > 65535u) return fail(R2D_ERR_CAPACITY, "a world holds at most 65535 bodies");
     const uint32_t off[2] = {0, n};
     const float* g = s->gravity.empty() ? nullptr : s->gravity.data();
     int st = guarded([&] { return s->eng.set_bodies(1, off, ids, kind, props, state, g, (uint32_t)s->gravity.size(), init_aabb); });
@@ -846,28 +1005,29 @@ static int solver_resolve(r2d_solver* s) {
     for (uint32_t i = 0; i < e.nbodies; ++i) idx[e.ids_h[i]] = i;
     const uint32_t nj = (uint32_t)s->jtype.size();
     std::vector<uint32_t> jw(nj, 0);
-    std::vector<uint16_t> b1(nj), b2(nj);
+    std::vector<uint32_t> b1(nj), b2(nj);
     for (uint32_t j = 0; j < nj; ++j) {
         auto a = idx.find(s->jid1[j]);
         if (a == idx.end()) return fail(R2D_ERR_INVALID_BODY_ID, "joint " + std::to_string(j) + " names an unknown body id");
-        b1[j] = (uint16_t)a->second;
+        b1[j] = a->second;
         b2[j] = b1[j];
         if (s->jtype[j] == J_DISTANCE || s->jtype[j] == J_OFFSET) {
             auto b = idx.find(s->jid2[j]);
             if (b == idx.end())
                 return fail(R2D_ERR_INVALID_BODY_ID, "joint " + std::to_string(j) + " names an unknown body id");
-            b2[j] = (uint16_t)b->second;
+            b2[j] = b->second;
         }
     }
     const uint32_t nx = (uint32_t)(s->xpairs.size() / 2);
-    std::vector<uint32_t> xw, xk;
+    std::vector<uint32_t> xw;
+    std::vector<unsigned long long> xk;
     for (uint32_t k = 0; k < nx; ++k) {
         auto a = idx.find(s->xpairs[2 * k]), b = idx.find(s->xpairs[2 * k + 1]);
         if (a == idx.end() || b == idx.end()) continue;  // an exclusion of a missing body excludes nothing
         const uint32_t lo = std::min(a->second, b->second), hi = std::max(a->second, b->second);
         if (lo == hi) continue;
         xw.push_back(0);
-        xk.push_back((lo << 16) | hi);
+        xk.push_back(((unsigned long long)lo << 32) | hi);
     }
     return e.set_constraints(jw, s->jtype, b1, b2, s->jprm, xw, xk);
 }
@@ -940,9 +1100,9 @@ R2D_API int r2d_batch_set_worlds(r2d_batch* b, uint32_t nworlds, const uint32_t*
     }
     std::vector<uint32_t> e32;
     std::vector<uint8_t> e8;
-    std::vector<uint16_t> e16;
     std::vector<float> ef;
-    return guarded([&] { return b->eng.set_constraints(e32, e8, e16, e16, ef, e32, e32); });
+    std::vector<unsigned long long> e64;
+    return guarded([&] { return b->eng.set_constraints(e32, e8, e32, e32, ef, e32, e64); });
 }
 
 R2D_API int r2d_batch_write_state(r2d_batch* b, const float* state) {
@@ -972,7 +1132,10 @@ R2D_API int r2d_batch_launches_per_step(r2d_batch* b, uint32_t* out) {
         int st = b->eng.plan();
         if (st) return st;
     }
-    *out = (uint32_t)b->eng.classes.size();
+    uint32_t n = (uint32_t)b->eng.classes.size();
+    for (uint32_t w : b->eng.large_list)
+        if (b->eng.large[w]) n += b->eng.large[w]->launches();
+    *out = n;
     return R2D_OK;
 }
 

@@ -1,0 +1,931 @@
+/*
+ * r2d_large.cu -- the step of one world too large for a single CTA's shared
+ * memory (a 12,001-body pyramid, a 200,004-body box with chains and motors).
+ *
+ * The stages of the fused per-world kernel run as grid-wide kernels over
+ * global scratch buffers, and every per-item computation is the fused
+ * kernel's own device function (r2d_device.cuh, r2d_solve.cuh), so both
+ * paths produce the same bits for the same world:
+ *
+ *   cells, entries, bucket sort    SpatialHash.zig:19-137 (a counting sort)
+ *   candidate pairs                lib.zig:264-282 (bucket sharing, filters,
+ *                                  "manifold already exists" as a hash set)
+ *   narrowphase + manifolds        collision.zig:299-363, Bodies/*.zig
+ *   colouring                      Jones-Plassmann rounds: a constraint takes
+ *                                  its colour once every neighbour that comes
+ *                                  before it in priority order has one, which
+ *                                  is exactly the sequential first-fit
+ *                                  colouring of r2d_colour.h
+ *   substeps                       lib.zig:199-250, one kernel per phase and
+ *                                  one per colour of each iteration
+ *
+ * Buffer sizes are exact where they can be (cell entries are counted before
+ * they are written; a manifold needs a candidate pair; a manifold has at most
+ * two points).  Only the candidate-pair set is guessed; when it overflows,
+ * the pair search reruns with a larger set, which is exact because nothing
+ * writes the world's state before the substeps.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <initializer_list>
+#include <string>
+#include <vector>
+
+#include "r2d_device.cuh"
+#include "r2d_large.h"
+#include "r2d_solve.cuh"
+#include "r2d_world.cuh"
+
+namespace r2d {
+
+namespace {
+
+constexpr int LT = 256;                                       // threads per block
+constexpr unsigned long long MAX_CELL_ENTRIES = 64ull << 20;  // spatial-hash entries of one step
+
+enum LargeCounter : int {
+    LC_PAIRS = 0,      // candidate pairs found
+    LC_MANIFOLDS,      // manifolds built
+    LC_POINTS,         // contact points built
+    LC_PENDING,        // constraints still uncoloured after a colouring round
+    LC_PAIR_OVERFLOW,  // the pair set or list was full
+    LC_NONFINITE,      // a body's AABB has no cell index
+    LC_COLOURS,        // a constraint needed more than MAX_COLOURS colours
+    LC_BIG,            // one body covers more than MAX_CELL_ENTRIES cells
+    LC_N
+};
+
+inline uint32_t blocks(uint64_t n) { return (uint32_t)std::max<uint64_t>(1, (n + LT - 1) / LT); }
+
+// In-place exclusive scan of a[0..n) by one block of 1024 threads; a[n]
+// receives the total.
+__global__ void __launch_bounds__(1024) lk_scan(uint32_t* a, uint32_t n) {
+    __shared__ uint32_t wsum[32];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t per = (n + 1023) / 1024;
+    const uint32_t beg = min(n, (uint32_t)tid * per), end = min(n, beg + per);
+    uint32_t s = 0;
+    for (uint32_t i = beg; i < end; ++i) s += a[i];
+    uint32_t x = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t v = wsum[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v += y;
+        }
+        wsum[lane] = v;
+    }
+    __syncthreads();
+    uint32_t run = (warp ? wsum[warp - 1] : 0u) + x - s;
+    for (uint32_t i = beg; i < end; ++i) {
+        const uint32_t v = a[i];
+        a[i] = run;
+        run += v;
+    }
+    if (tid == 1023) a[n] = wsum[31];
+}
+
+// ---------------------------------------------------------------------------
+// broadphase + narrowphase
+// ---------------------------------------------------------------------------
+struct Phase1 {
+    SWT<uint32_t> s;
+    const float* state;  // field-major, stride NB
+    const float* props;
+    const uint8_t* kind_in;
+    const uint32_t* ids;
+    uint32_t NB, base, n;
+    float cell;
+    BucketMod bmod;
+    bool disc_rot;
+    int32_t *rx0, *ry0, *rx1, *ry1;
+    uint32_t *bcnt, *ebucket, *ebody, *eslot, *sbody, *table;
+    unsigned long long* hset;  // pair set, ~0 = empty
+    unsigned long long* pairs;
+    uint32_t np, hs, nm, npt;
+    const unsigned long long* excl;
+    uint32_t nexcl;
+    uint32_t* cnt;
+    unsigned long long* entries;  // total cell entries (64-bit)
+
+    __device__ float st(int f, uint32_t i) const { return state[(size_t)f * NB + base + i]; }
+    __device__ float pr(int f, uint32_t i) const { return __ldg(props + (size_t)f * NB + base + i); }
+};
+
+// per body: derived quantities, and the cells its stored AABB covers
+__global__ void lk_load(Phase1 A) {
+    const uint32_t i = blockIdx.x * LT + threadIdx.x;
+    if (i >= A.n) return;
+    const uint8_t k = __ldg(A.kind_in + A.base + i);
+    const float a = A.st(S_ANGLE, i);
+    A.s.kind[i] = k;
+    A.s.inv_m[i] = (k & K_STATIC) ? 0.f : 1.0f / A.pr(P_MASS, i);
+    A.s.inv_i[i] = (k & K_STATIC) ? 0.f : 1.0f / A.pr(P_INERTIA, i);
+    float c = 1.f, sn = 0.f;
+    if ((k & K_RECT) || A.disc_rot) r2d_sincosf(a, &sn, &c);
+    A.s.cs[i] = c;
+    A.s.sn[i] = sn;
+    A.s.ang_prev[i] = a;
+    A.s.tq[i] = 0.f;
+    const float ax = A.st(S_AABB_X, i), ay = A.st(S_AABB_Y, i);
+    const float hw = A.st(S_AABB_HW, i), hh = A.st(S_AABB_HH, i);
+    int32_t x0 = 0, y0 = 0, x1 = -1, y1 = -1;
+    uint32_t count = 0;
+    const bool ok = cell_index(ax - hw, A.cell, &x0) && cell_index(ay - hh, A.cell, &y0) &&
+                    cell_index(ax + hw, A.cell, &x1) && cell_index(ay + hh, A.cell, &y1);
+    if (!ok) {
+        atomicExch(&A.cnt[LC_NONFINITE], 1u);
+        x1 = x0 - 1;
+    } else if (x1 >= x0 && y1 >= y0) {
+        const unsigned long long c64 =
+            (unsigned long long)((int64_t)x1 - (int64_t)x0 + 1) * (unsigned long long)((int64_t)y1 - (int64_t)y0 + 1);
+        if (c64 > MAX_CELL_ENTRIES) {
+            atomicExch(&A.cnt[LC_BIG], 1u);
+            x1 = x0 - 1;
+        } else {
+            count = (uint32_t)c64;
+            atomicAdd(A.entries, c64);
+        }
+    }
+    A.rx0[i] = x0; A.ry0[i] = y0; A.rx1[i] = x1; A.ry1[i] = y1;
+    A.bcnt[i] = count;
+}
+
+__global__ void lk_emit(Phase1 A) {
+    const uint32_t i = blockIdx.x * LT + threadIdx.x;
+    if (i >= A.n) return;
+    uint32_t k = A.bcnt[i];
+    for (int32_t yi = A.ry0[i]; yi <= A.ry1[i]; ++yi)
+        for (int32_t xi = A.rx0[i]; xi <= A.rx1[i]; ++xi) {
+            const uint32_t bk = cell_bucket(xi, yi, A.bmod);
+            A.ebucket[k] = bk;
+            A.ebody[k] = i;
+            atomicAdd(&A.table[bk], 1u);
+            ++k;
+        }
+}
+
+// after the scan: table[b] = first slot of bucket b; afterwards one past its last
+__global__ void lk_scatter(Phase1 A, uint32_t E) {
+    const uint32_t e = blockIdx.x * LT + threadIdx.x;
+    if (e >= E) return;
+    const uint32_t slot = atomicAdd(&A.table[A.ebucket[e]], 1u);
+    A.sbody[slot] = A.ebody[e];
+    A.eslot[e] = slot;
+}
+
+__device__ __forceinline__ bool lk_excluded(const unsigned long long* ex, uint32_t n, unsigned long long key) {
+    uint32_t lo = 0, hi = n;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        const unsigned long long v = __ldg(ex + mid);
+        if (v == key) return true;
+        if (v < key) lo = mid + 1;
+        else hi = mid;
+    }
+    return false;
+}
+
+// Candidates: every two entries of one bucket, filtered as lib.zig:273-282,
+// deduplicated like its "manifold already exists" test (lib.zig:278-281).
+__global__ void lk_pairs(Phase1 A, uint32_t E) {
+    const uint32_t e = blockIdx.x * LT + threadIdx.x;
+    if (e >= E) return;
+    const uint32_t i = A.ebody[e];
+    const uint32_t end = A.table[A.ebucket[e]];
+    const f2 pi = {A.st(S_AABB_X, i), A.st(S_AABB_Y, i)};
+    const float hwi = A.st(S_AABB_HW, i), hhi = A.st(S_AABB_HH, i);
+    const bool sti = (A.s.kind[i] & K_STATIC) != 0;
+    const unsigned long long mask = (unsigned long long)A.hs - 1ull;
+    for (uint32_t q = A.eslot[e] + 1u; q < end; ++q) {
+        const uint32_t j = A.sbody[q];
+        if (j == i) continue;
+        if (sti && (A.s.kind[j] & K_STATIC)) continue;
+        if (!aabb_intersects(pi, hwi, hhi, f2{A.st(S_AABB_X, j), A.st(S_AABB_Y, j)}, A.st(S_AABB_HW, j),
+                             A.st(S_AABB_HH, j)))
+            continue;
+        const uint32_t lo = min(i, j), hi = max(i, j);
+        const unsigned long long key = ((unsigned long long)lo << 32) | hi;
+        if (A.nexcl && lk_excluded(A.excl, A.nexcl, key)) continue;
+        unsigned long long h = key * 0x9E3779B97F4A7C15ull;
+        h ^= h >> 31;
+        bool fresh = false, placed = false;
+        for (unsigned long long probe = 0; probe <= mask; ++probe) {
+            const unsigned long long slot = (h + probe) & mask;
+            const unsigned long long prev = atomicCAS(&A.hset[slot], ~0ull, key);
+            if (prev == ~0ull || prev == key) {
+                fresh = prev == ~0ull;
+                placed = true;
+                break;
+            }
+        }
+        if (!placed) {
+            atomicExch(&A.cnt[LC_PAIR_OVERFLOW], 1u);
+            return;
+        }
+        if (fresh) {
+            const uint32_t idx = atomicAdd(&A.cnt[LC_PAIRS], 1u);
+            if (idx < A.np) A.pairs[idx] = key;
+            else atomicExch(&A.cnt[LC_PAIR_OVERFLOW], 1u);
+        }
+    }
+}
+
+// performNarrowSAT + manifold build (collision.zig:299-320, lib.zig:284-294)
+__global__ void lk_narrow(Phase1 A, uint32_t npairs) {
+    const uint32_t pi = blockIdx.x * LT + threadIdx.x;
+    if (pi >= npairs) return;
+    const SWT<uint32_t>& s = A.s;
+    const unsigned long long key = A.pairs[pi];
+    const uint32_t lo = (uint32_t)(key >> 32), hi = (uint32_t)key;
+    const uint32_t o1 = __ldg(A.ids + A.base + lo) < __ldg(A.ids + A.base + hi) ? lo : hi;
+    const uint32_t o2 = o1 == lo ? hi : lo;
+    Geo g1, g2;
+    geo_make(g1, f2{s.px[o1], s.py[o1]}, s.kind[o1] & K_RECT, A.pr(P_DIM0, o1), A.pr(P_DIM1, o1), s.cs[o1], s.sn[o1]);
+    geo_make(g2, f2{s.px[o2], s.py[o2]}, s.kind[o2] & K_RECT, A.pr(P_DIM0, o2), A.pr(P_DIM1, o2), s.cs[o2], s.sn[o2]);
+    SatState sat;
+    if (!perform_narrow_sat(g1, g2, sat)) return;
+    const uint32_t ref = sat.ref_is_first ? o1 : o2, inc = sat.ref_is_first ? o2 : o1;
+    NewPoint pts[2];
+    const int npt = sat.ref_is_first ? identify_points(g1, g2, sat.refid, pts) : identify_points(g2, g1, sat.refid, pts);
+    const uint32_t m = atomicAdd(&A.cnt[LC_MANIFOLDS], 1u);
+    const uint32_t p0 = atomicAdd(&A.cnt[LC_POINTS], (uint32_t)npt);
+    if (m >= A.nm || p0 + npt > A.npt) return;  // cannot happen: sized from the pair count
+    s.ma[m] = ref;
+    s.mb[m] = inc;
+    s.mp0[m] = p0;
+    s.mnp[m] = (uint8_t)npt;
+    s.nx[m] = sat.normal.x;
+    s.ny[m] = sat.normal.y;
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        if (k >= npt) break;
+        const uint32_t p = p0 + k;
+        s.r1x[p] = pts[k].ref_r.x;
+        s.r1y[p] = pts[k].ref_r.y;
+        s.r2x[p] = pts[k].inc_r.x;
+        s.r2y[p] = pts[k].inc_r.y;
+        s.depth[p] = pts[k].depth;
+        s.odepth[p] = pts[k].depth;
+        s.apn[p] = 0.f;
+        s.apt[p] = 0.f;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// colouring (r2d_colour.h) by Jones-Plassmann rounds
+// ---------------------------------------------------------------------------
+constexpr uint32_t NO_NODE = 0xFFFFFFFFu;
+
+struct Colouring {
+    uint32_t count;
+    bool joints;  // joints: every named body is a node; contacts: non-static bodies
+    const uint8_t* jtype;
+    const uint32_t* jb1;
+    const uint32_t* jb2;
+    const uint32_t* ma;
+    const uint32_t* mb;
+    const uint8_t* kind;
+    uint8_t* colour;  // 0xFF = not yet coloured
+    uint32_t *adj, *adjl, *prio, *cursor;
+    uint32_t* cnt;
+
+    __device__ void ends(uint32_t i, uint32_t* a, uint32_t* b) const {
+        *a = NO_NODE;
+        *b = NO_NODE;
+        if (joints) {
+            const uint32_t b1 = __ldg(jb1 + i), b2 = __ldg(jb2 + i);
+            *a = b1;
+            if (joint_two_bodies(__ldg(jtype + i)) && b2 != b1) *b = b2;
+        } else {
+            const uint32_t x = ma[i], y = mb[i];
+            if (!(kind[x] & K_STATIC)) *a = x;
+            if (!(kind[y] & K_STATIC)) *b = y;
+        }
+    }
+    // the order among equal mixes: the joint index, or the contact's (lo, hi)
+    __device__ unsigned long long tie(uint32_t i) const {
+        if (joints) return i;
+        const uint32_t x = ma[i], y = mb[i];
+        return ((unsigned long long)min(x, y) << 32) | max(x, y);
+    }
+};
+
+__global__ void lk_col_count(Colouring C) {
+    const uint32_t i = blockIdx.x * LT + threadIdx.x;
+    if (i >= C.count) return;
+    uint32_t a, b;
+    C.ends(i, &a, &b);
+    if (a != NO_NODE) atomicAdd(&C.adj[a], 1u);
+    if (b != NO_NODE) atomicAdd(&C.adj[b], 1u);
+}
+
+__global__ void lk_col_fill(Colouring C) {
+    const uint32_t i = blockIdx.x * LT + threadIdx.x;
+    if (i >= C.count) return;
+    uint32_t a, b;
+    C.ends(i, &a, &b);
+    if (a != NO_NODE) C.adjl[atomicAdd(&C.cursor[a], 1u)] = i;
+    if (b != NO_NODE) C.adjl[atomicAdd(&C.cursor[b], 1u)] = i;
+    if (C.joints) {
+        C.prio[i] = r2d_colour_mix(i, R2D_COLOUR_JOINT_SALT);
+    } else {
+        const uint32_t x = C.ma[i], y = C.mb[i];
+        C.prio[i] = r2d_colour_mix(min(x, y), max(x, y));
+    }
+    C.colour[i] = 0xFFu;
+}
+
+// One round: an uncoloured constraint whose earlier neighbours (in priority
+// order) are all coloured takes the lowest colour none of them holds.  A
+// colour, once written, is final, so reading one written in this same round
+// is as good as reading it next round.
+__global__ void lk_col_round(Colouring C) {
+    const uint32_t i = blockIdx.x * LT + threadIdx.x;
+    if (i >= C.count) return;
+    volatile uint8_t* col = C.colour;
+    if (col[i] != 0xFFu) return;
+    uint32_t ends[2];
+    C.ends(i, &ends[0], &ends[1]);
+    const uint32_t pi = C.prio[i];
+    const unsigned long long ti = C.tie(i);
+    ColourSet used;
+    bool ready = true;
+    for (int e2 = 0; e2 < 2 && ready; ++e2) {
+        const uint32_t x = ends[e2];
+        if (x == NO_NODE) continue;
+        const uint32_t q1 = C.adj[x + 1];
+        for (uint32_t q = C.adj[x]; q < q1; ++q) {
+            const uint32_t o = C.adjl[q];
+            if (o == i) continue;
+            const uint32_t po = C.prio[o];
+            if (po > pi || (po == pi && C.tie(o) > ti)) continue;  // comes later
+            const uint8_t c = col[o];
+            if (c == 0xFFu) {
+                ready = false;
+                break;
+            }
+            used.add(c);
+        }
+    }
+    if (!ready) {
+        atomicAdd(&C.cnt[LC_PENDING], 1u);
+        return;
+    }
+    uint32_t c = used.first_free();
+    if (c >= (uint32_t)MAX_COLOURS) {
+        atomicExch(&C.cnt[LC_COLOURS], 1u);
+        c = 0u;
+    }
+    col[i] = (uint8_t)c;
+}
+
+__global__ void lk_col_hist(Colouring C, uint32_t* hist) {
+    const uint32_t i = blockIdx.x * LT + threadIdx.x;
+    if (i >= C.count) return;
+    atomicAdd(&hist[C.colour[i]], 1u);
+}
+
+// colour-major order; inside a colour the order is free (body-disjoint)
+__global__ void lk_col_order(Colouring C, uint32_t* cursor, uint32_t* order) {
+    const uint32_t i = blockIdx.x * LT + threadIdx.x;
+    if (i >= C.count) return;
+    order[atomicAdd(&cursor[C.colour[i]], 1u)] = i;
+}
+
+// ---------------------------------------------------------------------------
+// substeps (lib.zig:199-250)
+// ---------------------------------------------------------------------------
+struct Phase2 {
+    SWT<uint32_t> s;
+    float* state;
+    const float* props;
+    uint32_t NB, base, n, nman;
+    float h;
+    bool first, last, disc_rot;
+    uint32_t ngrav;
+    float g[MAX_GRAVITY];
+    const uint8_t* jtype;
+    const uint32_t* jb1;
+    const uint32_t* jb2;
+    const float* jprm;
+    const uint32_t* order;  // constraints of the colour [k0, k1)
+    uint32_t k0, k1;
+
+    __device__ float& st(int f, uint32_t i) const { return state[(size_t)f * NB + base + i]; }
+    __device__ float pr(int f, uint32_t i) const { return __ldg(props + (size_t)f * NB + base + i); }
+};
+
+// forces (DownwardsGravity.zig:35-39), AABB (last substep), velocities (lib.zig:200-216)
+__global__ void lk_forces(Phase2 A) {
+    const uint32_t i = blockIdx.x * LT + threadIdx.x;
+    if (i >= A.n) return;
+    const SWT<uint32_t>& s = A.s;
+    const uint8_t k = s.kind[i];
+    float fx = 0.f, fy = 0.f, tq = 0.f;
+    if (A.first) {  // user-set force / torque (RigidBody.zig:73,78)
+        fx = A.st(S_FORCE_X, i);
+        fy = A.st(S_FORCE_Y, i);
+        tq = A.st(S_TORQUE, i);
+        // a dynamic body's force / torque is cleared after integration (lib.zig:247-248)
+        if (!(k & K_STATIC) && (fx != 0.f || fy != 0.f || tq != 0.f)) s.kind[i] = k | K_FORCED;
+    }
+    if (!(k & K_STATIC)) {
+        for (uint32_t gg = 0; gg < A.ngrav; ++gg) {
+            fx += 0.0f * s.mass(i);
+            fy += (-A.g[gg]) * s.mass(i);
+        }
+    }
+    if (A.last) {
+        float hw, hh;
+        if (k & K_RECT) {
+            rect_half_extents(A.pr(P_DIM0, i), A.pr(P_DIM1, i), s.cs[i], s.sn[i], &hw, &hh);
+        } else {
+            hw = hh = A.pr(P_DIM0, i);
+        }
+        A.st(S_AABB_X, i) = s.px[i];
+        A.st(S_AABB_Y, i) = s.py[i];
+        A.st(S_AABB_HW, i) = hw;
+        A.st(S_AABB_HH, i) = hh;
+    }
+    if (k & K_STATIC) return;
+    s.mx[i] += fx * A.h;
+    s.my[i] += fy * A.h;
+    s.L[i] += tq * A.h;
+    s.tq[i] = tq;
+}
+
+// updateTGSDepth + preStep (collision.zig:73-133)
+__global__ void lk_prestep(Phase2 A) {
+    const uint32_t m = blockIdx.x * LT + threadIdx.x;
+    if (m >= A.nman) return;
+    const SWT<uint32_t>& s = A.s;
+    const uint32_t a = s.ma[m], b = s.mb[m];
+    const f2 n2 = {s.nx[m], s.ny[m]};
+    const uint32_t p0 = s.mp0[m], np = s.mnp[m];
+    for (uint32_t k = 0; k < np; ++k) {
+        const uint32_t p = p0 + k;
+        if (approx_eql(s.depth[p], s.odepth[p], 1e-4f)) continue;
+        float sa_, ca_, sb_, cb_;
+        r2d_sincosf(s.ang[a] - s.ang_prev[a], &sa_, &ca_);
+        r2d_sincosf(s.ang[b] - s.ang_prev[b], &sb_, &cb_);
+        const f2 rr1 = rot(f2{s.r1x[p], s.r1y[p]}, ca_, sa_);
+        const f2 rr2 = rot(f2{s.r2x[p], s.r2y[p]}, cb_, sb_);
+        const f2 a1 = add2(rr1, f2{s.px[a], s.py[a]});
+        const f2 a2 = add2(rr2, f2{s.px[b], s.py[b]});
+        const float d = dot2(n2, sub2(a2, a1));
+        s.depth[p] = d + s.odepth[p];
+        s.r1x[p] = rr1.x;
+        s.r1y[p] = rr1.y;
+        s.r2x[p] = rr2.x;
+        s.r2y[p] = rr2.y;
+    }
+    const float inv_m1 = s.inv_m[a], inv_m2 = s.inv_m[b];
+    const float inv_mass = inv_m1 + inv_m2;
+    const float inv_i1 = s.inv_i[a], inv_i2 = s.inv_i[b];
+    const f2 t2 = cw90(n2);
+    s.fric[m] = sqrtf(A.pr(P_MU, a) * A.pr(P_MU, b));
+    for (uint32_t k = 0; k < np; ++k) {
+        const uint32_t p = p0 + k;
+        const f2 r1 = {s.r1x[p], s.r1y[p]}, r2 = {s.r2x[p], s.r2y[p]};
+        const float r1n = cross2(r1, n2), r2n = cross2(r2, n2);
+        const float kn = inv_mass + inv_i1 * (r1n * r1n) + inv_i2 * (r2n * r2n);
+        const float r1t = cross2(r1, t2), r2t = cross2(r2, t2);
+        const float kt = inv_mass + inv_i1 * (r1t * r1t) + inv_i2 * (r2t * r2t);
+        s.mn[p] = kn > 0.0f ? 1.0f / kn : 0.0f;
+        s.mt[p] = kt > 0.0f ? 1.0f / kt : 0.0f;
+        // bias of calculateImpulses (collision.zig:154-172); the depth is fixed within a substep
+        const float d = s.depth[p];
+        s.bias[p] = d >= 0.0f ? -1.0f : BAUMGARTE * zmax(0.0f, (-d) - BAUMGARTE_SLOP) / A.h;
+    }
+}
+
+__global__ void lk_contacts(Phase2 A) {
+    const uint32_t k = A.k0 + blockIdx.x * LT + threadIdx.x;
+    if (k >= A.k1) return;
+    solve_contact<false>(A.s, A.order[k]);
+}
+
+__global__ void lk_joints(Phase2 A) {
+    const uint32_t k = A.k0 + blockIdx.x * LT + threadIdx.x;
+    if (k >= A.k1) return;
+    const uint32_t j = A.order[k];
+    solve_joint(A.s, __ldg(A.jtype + j), __ldg(A.jb1 + j), __ldg(A.jb2 + j), A.jprm + (size_t)j * JOINT_PARAMS, A.h);
+}
+
+// integration (lib.zig:238-249); the last substep clears consumed forces
+__global__ void lk_integrate(Phase2 A) {
+    const uint32_t i = blockIdx.x * LT + threadIdx.x;
+    if (i >= A.n) return;
+    const SWT<uint32_t>& s = A.s;
+    s.ang_prev[i] = s.ang[i];
+    const uint8_t k = s.kind[i];
+    if (k & K_STATIC) return;
+    const float sm_ = A.h / s.mass(i);
+    s.px[i] += s.mx[i] * sm_;
+    s.py[i] += s.my[i] * sm_;
+    s.ang[i] += s.L[i] * A.h / s.inertia(i);
+    s.tq[i] = 0.f;
+    if (!A.last && ((k & K_RECT) || A.disc_rot)) {
+        float c, sn;
+        r2d_sincosf(s.ang[i], &sn, &c);
+        s.cs[i] = c;
+        s.sn[i] = sn;
+    }
+    if (A.last && (k & K_FORCED)) {
+        A.st(S_FORCE_X, i) = 0.f;
+        A.st(S_FORCE_Y, i) = 0.f;
+        A.st(S_TORQUE, i) = 0.f;
+    }
+}
+
+// debug taps in the oracle's manifold layout (DebugOut)
+__global__ void lk_dump(SWT<uint32_t> s, uint32_t m_count, uint32_t* keys, float* data, uint32_t* colours) {
+    const uint32_t m = blockIdx.x * LT + threadIdx.x;
+    if (m >= m_count) return;
+    keys[2 * m] = s.ma[m];
+    keys[2 * m + 1] = s.mb[m];
+    colours[m] = s.mcol[m];
+    float* d = data + (size_t)m * DEBUG_MF;
+    const f2 nn = {s.nx[m], s.ny[m]};
+    const f2 tt = cw90(nn);
+    const uint32_t np = s.mnp[m], p0 = s.mp0[m];
+    d[0] = nn.x; d[1] = nn.y; d[2] = tt.x; d[3] = tt.y; d[4] = s.fric[m];
+    d[5] = np > 0 ? 1.f : 0.f;
+    d[6] = np > 1 ? 1.f : 0.f;
+    d[7] = s.ang_prev[s.ma[m]];
+    d[8] = s.ang_prev[s.mb[m]];
+    for (uint32_t k = 0; k < 2; ++k) {
+        float* q = d + 9 + 12 * k;
+        const bool has = k < np;
+        const uint32_t p = p0 + k;
+        q[0] = __int_as_float(0x7fc00000);
+        q[1] = __int_as_float(0x7fc00000);
+        q[2] = has ? s.r1x[p] : 0.f;
+        q[3] = has ? s.r1y[p] : 0.f;
+        q[4] = has ? s.r2x[p] : 0.f;
+        q[5] = has ? s.r2y[p] : 0.f;
+        q[6] = has ? s.depth[p] : 0.f;
+        q[7] = has ? s.odepth[p] : 0.f;
+        q[8] = has ? s.mn[p] : 0.f;
+        q[9] = has ? s.mt[p] : 0.f;
+        q[10] = has ? s.apn[p] : 0.f;
+        q[11] = has ? s.apt[p] : 0.f;
+    }
+}
+
+__global__ void lk_widen(const uint8_t* in, uint32_t n, uint32_t* out) {
+    const uint32_t i = blockIdx.x * LT + threadIdx.x;
+    if (i < n) out[i] = in[i];
+}
+
+// A group of device arrays that share one element capacity.
+struct Buf {
+    void** p;
+    size_t elem;
+};
+#define LB(x) Buf{(void**)&(x), sizeof(*(x))}
+
+cudaError_t regrow(size_t& cap, size_t need, std::initializer_list<Buf> bufs) {
+    if (need <= cap) return cudaSuccess;
+    const size_t c = need + need / 4 + 64;
+    for (const Buf& b : bufs) {
+        if (*b.p) cudaFree(*b.p);
+        *b.p = nullptr;
+    }
+    cap = 0;
+    for (const Buf& b : bufs) {
+        cudaError_t e = cudaMalloc(b.p, c * b.elem);
+        if (e != cudaSuccess) return e;
+    }
+    cap = c;
+    return cudaSuccess;
+}
+
+}  // namespace
+
+struct LargeWorld::Impl {
+    size_t cap_n = 0, cap_t = 0, cap_e = 0, cap_hs = 0, cap_p = 0, cap_m = 0, cap_pt = 0, cap_c = 0, cap_j = 0,
+           cap_d = 0, cap_dd = 0;
+    // bodies
+    float *inv_m = nullptr, *inv_i = nullptr, *cs = nullptr, *sn = nullptr, *tq = nullptr, *ang_prev = nullptr;
+    uint8_t* kind = nullptr;
+    int32_t *rx0 = nullptr, *ry0 = nullptr, *rx1 = nullptr, *ry1 = nullptr;
+    uint32_t *bcnt = nullptr, *adj = nullptr, *cursor = nullptr;
+    // spatial hash
+    uint32_t* table = nullptr;
+    uint32_t *ebucket = nullptr, *ebody = nullptr, *eslot = nullptr, *sbody = nullptr;
+    unsigned long long *hset = nullptr, *pairs = nullptr;
+    // manifolds and points
+    uint32_t *ma = nullptr, *mb = nullptr, *mp0 = nullptr, *corder = nullptr;
+    uint8_t *mnp = nullptr, *mcol = nullptr;
+    float *nx = nullptr, *ny = nullptr, *fric = nullptr;
+    float *r1x = nullptr, *r1y = nullptr, *r2x = nullptr, *r2y = nullptr, *depth = nullptr, *odepth = nullptr;
+    float *mn = nullptr, *mt = nullptr, *apn = nullptr, *apt = nullptr, *bias = nullptr;
+    // colouring
+    uint32_t *adjl = nullptr, *prio = nullptr;
+    uint8_t* jcol = nullptr;
+    uint32_t* jorder = nullptr;
+    uint32_t* cnt = nullptr;                // LargeCounter
+    unsigned long long* entries = nullptr;  // total cell entries
+    uint32_t* hist = nullptr;               // [MAX_COLOURS + 1]
+    uint32_t* h_cnt = nullptr;              // pinned: counters, then the entry total
+    // debug taps
+    uint32_t *dk = nullptr, *dc = nullptr;
+    float* dd = nullptr;
+
+    double pair_scale = 1.0;  // grows when the candidate-pair set overflows
+    uint32_t nman = 0, nj = 0, nlaunch = 0;
+    std::vector<uint32_t> coff, joff;
+
+    ~Impl() {
+        void* ps[] = {inv_m, inv_i, cs, sn, tq, ang_prev, kind, rx0, ry0, rx1, ry1, bcnt, adj, cursor,
+                      table, ebucket, ebody, eslot, sbody, hset, pairs, ma, mb, mp0, corder, mnp, mcol,
+                      nx, ny, fric, r1x, r1y, r2x, r2y, depth, odepth, mn, mt, apn, apt, bias, adjl, prio,
+                      jcol, jorder, cnt, entries, hist, dk, dc, dd};
+        for (void* p : ps)
+            if (p) cudaFree(p);
+        if (h_cnt) cudaFreeHost(h_cnt);
+    }
+
+    SWT<uint32_t> views(const LargeInputs& in) const {
+        SWT<uint32_t> s{};
+        float* S = in.state;
+        const size_t NB = in.NB;
+        s.px = S + (size_t)S_POS_X * NB + in.base;
+        s.py = S + (size_t)S_POS_Y * NB + in.base;
+        s.ang = S + (size_t)S_ANGLE * NB + in.base;
+        s.mx = S + (size_t)S_MOM_X * NB + in.base;
+        s.my = S + (size_t)S_MOM_Y * NB + in.base;
+        s.L = S + (size_t)S_ANG_MOM * NB + in.base;
+        s.inv_m = inv_m; s.inv_i = inv_i; s.cs = cs; s.sn = sn; s.ang_prev = ang_prev; s.tq = tq;
+        s.px0 = nullptr; s.py0 = nullptr; s.pos0 = false;
+        s.gmass = in.props + (size_t)P_MASS * NB + in.base;
+        s.ginertia = in.props + (size_t)P_INERTIA * NB + in.base;
+        s.kind = kind;
+        s.ma = ma; s.mb = mb; s.mp0 = mp0; s.mnp = mnp; s.mcol = mcol;
+        s.nx = nx; s.ny = ny; s.fric = fric;
+        s.r1x = r1x; s.r1y = r1y; s.r2x = r2x; s.r2y = r2y;
+        s.depth = depth; s.odepth = odepth; s.mn = mn; s.mt = mt; s.apn = apn; s.apt = apt; s.bias = bias;
+        return s;
+    }
+};
+
+LargeWorld::LargeWorld() : impl(new Impl()) {}
+LargeWorld::~LargeWorld() { delete impl; }
+
+#define LTRY(expr)                                                     \
+    do {                                                               \
+        cudaError_t e_ = (expr);                                       \
+        if (e_ != cudaSuccess) {                                       \
+            *msg = std::string(#expr) + ": " + cudaGetErrorString(e_); \
+            return e_ == cudaErrorMemoryAllocation ? -3 : -4;          \
+        }                                                              \
+    } while (0)
+#define LAUNCH(kernel, grid, ...)                   \
+    do {                                            \
+        kernel<<<(grid), LT, 0, st>>>(__VA_ARGS__); \
+        ++I.nlaunch;                                \
+    } while (0)
+
+int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32_t iters, cudaStream_t st,
+                     std::string* msg) {
+    Impl& I = *impl;
+    const uint32_t n = in.n;
+    I.nman = 0;
+    I.nj = 0;
+    I.nlaunch = 0;
+    I.coff.assign(1, 0u);
+    I.joff.assign(1, 0u);
+    if (n == 0) return 0;
+    const uint32_t T = in.table_mult * n;
+    if (!I.h_cnt) LTRY(cudaMallocHost((void**)&I.h_cnt, sizeof(uint32_t) * (LC_N + 2)));
+    if (!I.cnt) {
+        LTRY(cudaMalloc((void**)&I.cnt, sizeof(uint32_t) * LC_N));
+        LTRY(cudaMalloc((void**)&I.entries, sizeof(unsigned long long)));
+        LTRY(cudaMalloc((void**)&I.hist, sizeof(uint32_t) * (MAX_COLOURS + 1)));
+    }
+    LTRY(regrow(I.cap_n, (size_t)n + 1,
+                {LB(I.inv_m), LB(I.inv_i), LB(I.cs), LB(I.sn), LB(I.tq), LB(I.ang_prev), LB(I.kind), LB(I.rx0),
+                 LB(I.ry0), LB(I.rx1), LB(I.ry1), LB(I.bcnt), LB(I.adj), LB(I.cursor)}));
+    LTRY(regrow(I.cap_t, (size_t)T + 1, {LB(I.table)}));
+
+    Phase1 A{};
+    A.s = I.views(in);
+    A.state = in.state; A.props = in.props; A.kind_in = in.kind; A.ids = in.ids;
+    A.NB = in.NB; A.base = in.base; A.n = n; A.cell = in.cell;
+    A.bmod = BucketMod{bucket_recip(T), T};
+    A.disc_rot = in.disc_rot;
+    A.rx0 = I.rx0; A.ry0 = I.ry0; A.rx1 = I.rx1; A.ry1 = I.ry1; A.bcnt = I.bcnt; A.table = I.table;
+    A.excl = in.excl; A.nexcl = in.nexcl;
+    A.cnt = I.cnt; A.entries = I.entries;
+
+    // ---- cells: count them, then size the entry arrays exactly ----
+    LTRY(cudaMemsetAsync(I.cnt, 0, sizeof(uint32_t) * LC_N, st));
+    LTRY(cudaMemsetAsync(I.entries, 0, sizeof(unsigned long long), st));
+    LTRY(cudaMemsetAsync(I.table, 0, sizeof(uint32_t) * ((size_t)T + 1), st));
+    LAUNCH(lk_load, blocks(n), A);
+    LTRY(cudaMemcpyAsync(I.h_cnt, I.cnt, sizeof(uint32_t) * LC_N, cudaMemcpyDeviceToHost, st));
+    LTRY(cudaMemcpyAsync(I.h_cnt + LC_N, I.entries, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    LTRY(cudaStreamSynchronize(st));
+    if (I.h_cnt[LC_NONFINITE]) {
+        *msg = "a body's AABB is not finite (it has no spatial-hash cell)";
+        return DS_NONFINITE;
+    }
+    unsigned long long E64 = 0;
+    memcpy(&E64, I.h_cnt + LC_N, sizeof(E64));
+    if (I.h_cnt[LC_BIG] || E64 > MAX_CELL_ENTRIES) {
+        *msg = "the bodies cover more than 64Mi spatial-hash cells";
+        return DS_CAPACITY;
+    }
+    const uint32_t E = (uint32_t)E64;
+    LTRY(regrow(I.cap_e, (size_t)E + 1, {LB(I.ebucket), LB(I.ebody), LB(I.eslot), LB(I.sbody)}));
+    A.ebucket = I.ebucket; A.ebody = I.ebody; A.eslot = I.eslot; A.sbody = I.sbody;
+    LAUNCH(lk_scan, 1, I.bcnt, n);
+    LAUNCH(lk_emit, blocks(n), A);
+    LAUNCH(lk_scan, 1, I.table, T);
+    LAUNCH(lk_scatter, blocks(E), A, E);
+
+    // ---- candidate pairs (the set grows until it holds them all) ----
+    uint32_t npairs = 0;
+    for (;;) {
+        const double want = (3.25 * n + 64.0) * I.pair_scale;
+        if (want > 1.0e9) {
+            *msg = "more than 1e9 candidate pairs";
+            return DS_CAPACITY;
+        }
+        const uint32_t np = (uint32_t)want;
+        uint32_t hs = 1;
+        while (hs < np + np / 2) hs <<= 1;
+        LTRY(regrow(I.cap_p, np, {LB(I.pairs)}));
+        LTRY(regrow(I.cap_hs, hs, {LB(I.hset)}));
+        A.pairs = I.pairs; A.hset = I.hset; A.np = np; A.hs = hs;
+        LTRY(cudaMemsetAsync(I.hset, 0xFF, sizeof(unsigned long long) * hs, st));
+        LTRY(cudaMemsetAsync(I.cnt, 0, sizeof(uint32_t) * LC_N, st));
+        LAUNCH(lk_pairs, blocks(E), A, E);
+        LTRY(cudaMemcpyAsync(I.h_cnt, I.cnt, sizeof(uint32_t) * LC_N, cudaMemcpyDeviceToHost, st));
+        LTRY(cudaStreamSynchronize(st));
+        if (!I.h_cnt[LC_PAIR_OVERFLOW]) {
+            npairs = I.h_cnt[LC_PAIRS];
+            break;
+        }
+        I.pair_scale *= std::max(1.5, 1.25 * (double)I.h_cnt[LC_PAIRS] / (double)np);
+    }
+
+    // ---- narrowphase: at most one manifold per pair, two points per manifold ----
+    LTRY(regrow(I.cap_m, (size_t)npairs + 1,
+                {LB(I.ma), LB(I.mb), LB(I.mp0), LB(I.corder), LB(I.mnp), LB(I.mcol), LB(I.nx), LB(I.ny),
+                 LB(I.fric)}));
+    LTRY(regrow(I.cap_pt, 2 * (size_t)npairs + 1,
+                {LB(I.r1x), LB(I.r1y), LB(I.r2x), LB(I.r2y), LB(I.depth), LB(I.odepth), LB(I.mn), LB(I.mt),
+                 LB(I.apn), LB(I.apt), LB(I.bias)}));
+    A.s = I.views(in);
+    A.nm = npairs;
+    A.npt = 2 * npairs;
+    LTRY(cudaMemsetAsync(I.cnt, 0, sizeof(uint32_t) * LC_N, st));
+    LAUNCH(lk_narrow, blocks(npairs), A, npairs);
+    LTRY(cudaMemcpyAsync(I.h_cnt, I.cnt, sizeof(uint32_t) * LC_N, cudaMemcpyDeviceToHost, st));
+    LTRY(cudaStreamSynchronize(st));
+    const uint32_t M = I.h_cnt[LC_MANIFOLDS];
+
+    // ---- colouring: contacts, then joints ----
+    LTRY(regrow(I.cap_c, 2 * (size_t)std::max(M, in.nj) + 2, {LB(I.adjl), LB(I.prio)}));
+    LTRY(regrow(I.cap_j, (size_t)in.nj + 1, {LB(I.jcol), LB(I.jorder)}));
+    auto colour = [&](bool joints, uint32_t count, uint8_t* col, uint32_t* order, std::vector<uint32_t>& off) -> int {
+        off.assign(1, 0u);
+        if (count == 0) return 0;
+        Colouring C{};
+        C.count = count;
+        C.joints = joints;
+        C.jtype = in.jtype; C.jb1 = in.jb1; C.jb2 = in.jb2;
+        C.ma = I.ma; C.mb = I.mb; C.kind = I.kind; C.colour = col;
+        C.adj = I.adj; C.adjl = I.adjl; C.prio = I.prio; C.cursor = I.cursor; C.cnt = I.cnt;
+        LTRY(cudaMemsetAsync(I.adj, 0, sizeof(uint32_t) * ((size_t)n + 1), st));
+        LTRY(cudaMemsetAsync(I.cnt, 0, sizeof(uint32_t) * LC_N, st));
+        LAUNCH(lk_col_count, blocks(count), C);
+        LAUNCH(lk_scan, 1, I.adj, n);
+        LTRY(cudaMemcpyAsync(I.cursor, I.adj, sizeof(uint32_t) * ((size_t)n + 1), cudaMemcpyDeviceToDevice, st));
+        LAUNCH(lk_col_fill, blocks(count), C);
+        // Each round colours at least the highest-priority uncoloured
+        // constraint, so `count` rounds always finish; random priorities
+        // need a few dozen.
+        for (uint32_t rounds = 0;;) {
+            for (int r = 0; r < 4; ++r) {
+                LTRY(cudaMemsetAsync(I.cnt + LC_PENDING, 0, sizeof(uint32_t), st));
+                LAUNCH(lk_col_round, blocks(count), C);
+            }
+            rounds += 4;
+            LTRY(cudaMemcpyAsync(I.h_cnt, I.cnt, sizeof(uint32_t) * LC_N, cudaMemcpyDeviceToHost, st));
+            LTRY(cudaStreamSynchronize(st));
+            if (I.h_cnt[LC_COLOURS]) {
+                *msg = "a constraint needs more than " + std::to_string(MAX_COLOURS) + " colours";
+                return DS_CAPACITY;
+            }
+            if (I.h_cnt[LC_PENDING] == 0) break;
+            if (rounds > count + 4) {
+                *msg = "the colouring did not finish";
+                return -4;
+            }
+        }
+        std::vector<uint32_t> hist(MAX_COLOURS + 1, 0u);
+        LTRY(cudaMemsetAsync(I.hist, 0, sizeof(uint32_t) * (MAX_COLOURS + 1), st));
+        LAUNCH(lk_col_hist, blocks(count), C, I.hist);
+        LTRY(cudaMemcpyAsync(hist.data(), I.hist, sizeof(uint32_t) * (MAX_COLOURS + 1), cudaMemcpyDeviceToHost, st));
+        LTRY(cudaStreamSynchronize(st));
+        uint32_t ncol = 0;
+        for (uint32_t c = 0; c < (uint32_t)MAX_COLOURS; ++c)
+            if (hist[c]) ncol = c + 1;
+        off.assign(ncol + 1, 0u);
+        for (uint32_t c = 0; c < ncol; ++c) off[c + 1] = off[c] + hist[c];
+        LTRY(cudaMemcpyAsync(I.hist, off.data(), sizeof(uint32_t) * (ncol + 1), cudaMemcpyHostToDevice, st));
+        LAUNCH(lk_col_order, blocks(count), C, I.hist, order);
+        // `off` is the source of the copy above: wait before it can change
+        LTRY(cudaStreamSynchronize(st));
+        return 0;
+    };
+    int cst = colour(false, M, I.mcol, I.corder, I.coff);
+    if (cst) return cst;
+    cst = colour(true, in.nj, I.jcol, I.jorder, I.joff);
+    if (cst) return cst;
+    I.nman = M;
+    I.nj = in.nj;
+
+    // ---- substeps: the world's state changes from here on ----
+    Phase2 S{};
+    S.s = I.views(in);
+    S.state = in.state; S.props = in.props; S.NB = in.NB; S.base = in.base; S.n = n; S.nman = M;
+    S.h = dt / (float)sub_steps;
+    S.disc_rot = in.disc_rot;
+    S.ngrav = in.ngrav;
+    for (int k = 0; k < MAX_GRAVITY; ++k) S.g[k] = in.g[k];
+    S.jtype = in.jtype; S.jb1 = in.jb1; S.jb2 = in.jb2; S.jprm = in.jprm;
+    for (uint32_t sub = 0; sub < sub_steps; ++sub) {
+        S.first = sub == 0;
+        S.last = sub + 1 == sub_steps;
+        LAUNCH(lk_forces, blocks(n), S);
+        if (M) LAUNCH(lk_prestep, blocks(M), S);
+        for (uint32_t it = 0; it < iters; ++it) {
+            S.order = I.jorder;
+            for (size_t c = 0; c + 1 < I.joff.size(); ++c) {
+                S.k0 = I.joff[c];
+                S.k1 = I.joff[c + 1];
+                LAUNCH(lk_joints, blocks(S.k1 - S.k0), S);
+            }
+            S.order = I.corder;
+            for (size_t c = 0; c + 1 < I.coff.size(); ++c) {
+                S.k0 = I.coff[c];
+                S.k1 = I.coff[c + 1];
+                LAUNCH(lk_contacts, blocks(S.k1 - S.k0), S);
+            }
+        }
+        LAUNCH(lk_integrate, blocks(n), S);
+    }
+    LTRY(cudaGetLastError());
+    return 0;
+}
+
+uint32_t LargeWorld::num_manifolds() const { return impl->nman; }
+uint32_t LargeWorld::launches() const { return impl->nlaunch; }
+
+int LargeWorld::dump(uint32_t cap, uint32_t* keys, float* data, uint32_t* colours, cudaStream_t st,
+                     std::string* msg) {
+    Impl& I = *impl;
+    const uint32_t m = std::min(cap, I.nman);
+    if (m == 0) return 0;
+    LTRY(regrow(I.cap_d, 2 * (size_t)m, {LB(I.dk), LB(I.dc)}));
+    LTRY(regrow(I.cap_dd, (size_t)DEBUG_MF * m, {LB(I.dd)}));
+    SWT<uint32_t> s{};
+    s.ma = I.ma; s.mb = I.mb; s.mp0 = I.mp0; s.mnp = I.mnp; s.mcol = I.mcol;
+    s.nx = I.nx; s.ny = I.ny; s.fric = I.fric; s.ang_prev = I.ang_prev;
+    s.r1x = I.r1x; s.r1y = I.r1y; s.r2x = I.r2x; s.r2y = I.r2y;
+    s.depth = I.depth; s.odepth = I.odepth; s.mn = I.mn; s.mt = I.mt; s.apn = I.apn; s.apt = I.apt;
+    lk_dump<<<blocks(m), LT, 0, st>>>(s, m, I.dk, I.dd, I.dc);
+    LTRY(cudaStreamSynchronize(st));
+    if (keys) LTRY(cudaMemcpy(keys, I.dk, 8ull * m, cudaMemcpyDeviceToHost));
+    if (data) LTRY(cudaMemcpy(data, I.dd, sizeof(float) * DEBUG_MF * (size_t)m, cudaMemcpyDeviceToHost));
+    if (colours) LTRY(cudaMemcpy(colours, I.dc, 4ull * m, cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+int LargeWorld::joint_colours(uint32_t cap, uint32_t* colours, cudaStream_t st, std::string* msg) {
+    Impl& I = *impl;
+    const uint32_t m = std::min(cap, I.nj);
+    if (m == 0) return 0;
+    LTRY(regrow(I.cap_d, m, {LB(I.dk), LB(I.dc)}));
+    lk_widen<<<blocks(m), LT, 0, st>>>(I.jcol, m, I.dc);
+    LTRY(cudaStreamSynchronize(st));
+    LTRY(cudaMemcpy(colours, I.dc, 4ull * m, cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+}  // namespace r2d

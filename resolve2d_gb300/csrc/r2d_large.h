@@ -1,0 +1,62 @@
+/*
+ * r2d_large.h -- host interface of the large-world step (r2d_large.cu): one
+ * world whose bodies do not fit one CTA's shared memory, stepped by a
+ * pipeline of grid-wide kernels over global scratch buffers.
+ */
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "r2d_world.cuh"
+
+namespace r2d {
+
+// Device views of one world inside an engine's field-major arrays.
+struct LargeInputs {
+    float* state;          // [S_NFIELDS][NB]
+    const float* props;    // [P_NFIELDS][NB]
+    const uint8_t* kind;   // [NB]
+    const uint32_t* ids;   // [NB]
+    uint32_t NB;           // bodies of the whole engine (field stride)
+    uint32_t base, n;      // this world's first body and body count
+    const uint8_t* jtype;  // this world's joints (world-local body indices)
+    const uint32_t* jb1;
+    const uint32_t* jb2;
+    const float* jprm;     // [nj][JOINT_PARAMS]
+    uint32_t nj;
+    const unsigned long long* excl;  // sorted (lo << 32 | hi) keys of this world
+    uint32_t nexcl;
+    uint32_t ngrav;
+    float g[MAX_GRAVITY];
+    float cell;
+    uint32_t table_mult;
+    bool disc_rot;         // some joint reads disc orientations
+};
+
+class LargeWorld {
+public:
+    LargeWorld();
+    ~LargeWorld();
+    LargeWorld(const LargeWorld&) = delete;
+    LargeWorld& operator=(const LargeWorld&) = delete;
+
+    // One Solver.process call.  Returns 0 or a negative r2d status (with
+    // *msg set); on an error the world's state is that before the call.
+    int step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32_t iters, cudaStream_t st, std::string* msg);
+    // Manifolds and colourings of the last step (debug taps, oracle layout).
+    uint32_t num_manifolds() const;
+    int dump(uint32_t cap, uint32_t* keys, float* data, uint32_t* colours, cudaStream_t st, std::string* msg);
+    int joint_colours(uint32_t cap, uint32_t* colours, cudaStream_t st, std::string* msg);
+    // Kernel launches of the last step.
+    uint32_t launches() const;
+
+    struct Impl;
+
+private:
+    Impl* impl;
+};
+
+}  // namespace r2d

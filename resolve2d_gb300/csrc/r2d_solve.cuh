@@ -1,0 +1,218 @@
+/*
+ * r2d_solve.cuh -- per-constraint solve functions shared by the fused
+ * per-world kernel and the large-world kernels.  Each function works on one
+ * contact manifold or one joint through array views (SWT) that may point into
+ * shared or global memory.
+ */
+#pragma once
+
+#include <stdint.h>
+
+#include "r2d_device.cuh"
+#include "r2d_world.cuh"
+
+namespace r2d {
+
+// Views of one world's arrays: shared memory in the fused kernel (16-bit
+// manifold indices), global memory in the large-world path (32-bit).
+template <class IDX>
+struct SWT {
+    float *px, *py, *ang, *mx, *my, *L, *inv_m, *inv_i, *cs, *sn, *ang_prev, *tq, *px0, *py0;
+    bool pos0;                           // px0/py0 hold frame-start positions
+    const float* __restrict__ gmass;     // this world's masses (global, read-only)
+    const float* __restrict__ ginertia;  // this world's inertias
+    uint8_t* kind;
+    IDX *ma, *mb, *mp0;
+    uint8_t *mnp, *mcol;
+    float *nx, *ny, *fric;
+    float *r1x, *r1y, *r2x, *r2y, *depth, *odepth, *mn, *mt, *apn, *apt, *bias;
+
+    __device__ __forceinline__ float mass(uint32_t i) const { return __ldg(gmass + i); }
+    __device__ __forceinline__ float inertia(uint32_t i) const { return __ldg(ginertia + i); }
+    // Lever arms of point p between bodies a (reference) and b (incident).
+    // Lean: middle - frame-start position, the subtraction CollisionPoint.init
+    // performs (collision.zig:43-44), so the bits are those it stored.
+    template <bool LEAN>
+    __device__ __forceinline__ void arms(uint32_t p, uint32_t a, uint32_t b, f2* r1, f2* r2) const {
+        if (LEAN) {
+            const f2 mid = {r1x[p], r1y[p]};
+            const float* bx = pos0 ? px0 : px;  // one substep: positions do not move before integration
+            const float* by = pos0 ? py0 : py;
+            *r1 = sub2(mid, f2{bx[a], by[a]});
+            *r2 = sub2(mid, f2{bx[b], by[b]});
+        } else {
+            *r1 = f2{r1x[p], r1y[p]};
+            *r2 = f2{r2x[p], r2y[p]};
+        }
+    }
+};
+
+// CollisionManifold.calculateImpulses (collision.zig:135-218)
+template <bool LEAN, class IDX>
+__device__ __forceinline__ void solve_contact(const SWT<IDX>& s, uint32_t m) {
+    const uint32_t a = s.ma[m], b = s.mb[m];
+    const bool sa = s.kind[a] & K_STATIC, sb = s.kind[b] & K_STATIC;
+    const float inv_m1 = s.inv_m[a], inv_m2 = s.inv_m[b];
+    const float inv_i1 = s.inv_i[a], inv_i2 = s.inv_i[b];
+    const f2 vlinear_1 = scale2(f2{s.mx[a], s.my[a]}, inv_m1);
+    const float omega1 = s.L[a] * inv_i1;
+    const f2 vlinear_2 = scale2(f2{s.mx[b], s.my[b]}, inv_m2);
+    const float omega2 = s.L[b] * inv_i2;
+    const f2 n = {s.nx[m], s.ny[m]};
+    const f2 t = cw90(n);
+    const float fr = s.fric[m];
+    f2 alp1 = {0.f, 0.f}, alp2 = {0.f, 0.f};
+    float arp1 = 0.f, arp2 = 0.f;
+    const uint32_t p0 = s.mp0[m], np = s.mnp[m];
+    for (uint32_t k = 0; k < np; ++k) {
+        const uint32_t p = p0 + k;
+        const float bias = s.bias[p];
+        if (bias < 0.0f) continue;  // depth >= 0: accumulators stay 0 (collision.zig:154-158)
+        f2 r1, r2;
+        s.arms<LEAN>(p, a, b, &r1, &r2);
+        const f2 v1 = add2(vlinear_1, f2{-r1.y * omega1, r1.x * omega1});
+        const f2 v2 = add2(vlinear_2, f2{-r2.y * omega2, r2.x * omega2});
+        const f2 dv = sub2(v1, v2);
+        float num = dot2(dv, n) + bias;  // BAUMGARTE*max(0,-depth-SLOP)/h (collision.zig:172)
+        const float pn = num * s.mn[p];
+        if (pn < MIN_MANIFOLD_IMPULSE) continue;
+        num = dot2(dv, t);
+        const float pt = num * s.mt[p];
+        const float acc = s.apn[p];
+        const float nacc = zmax(0.0f, acc + pn);
+        const float applied_pn = nacc - acc;
+        s.apn[p] = nacc;
+        const float max_pt = fr * fabsf(nacc);
+        const float acct = s.apt[p];
+        const float nacct = zclamp(acct + pt, -max_pt, max_pt);
+        const float applied_pt = nacct - acct;
+        s.apt[p] = nacct;
+        const f2 dp = add2(scale2(n, applied_pn), scale2(t, applied_pt));
+        if (!sa) {
+            alp1 = sub2(alp1, dp);
+            arp1 -= cross2(r1, dp);
+        }
+        if (!sb) {
+            alp2 = add2(alp2, dp);
+            arp2 += cross2(r2, dp);
+        }
+    }
+    // A static body receives exactly +0 in the reference; its state is left alone.
+    if (!sa) {
+        s.mx[a] += alp1.x;
+        s.my[a] += alp1.y;
+        s.L[a] += arp1;
+    }
+    if (!sb) {
+        s.mx[b] += alp2.x;
+        s.my[b] += alp2.y;
+        s.L[b] += arp2;
+    }
+}
+
+// Constraint solve functions (src/core/Constraints/*.zig).
+template <class IDX>
+__device__ __forceinline__ void solve_joint(const SWT<IDX>& s, uint8_t type, uint32_t i1, uint32_t i2,
+                                            const float* __restrict__ prm, float h) {
+    const float pmax = __ldg(prm + 0), pmin = __ldg(prm + 1), beta = __ldg(prm + 2);
+    if (type == J_DISTANCE) {  // DistanceJoint.zig:40-75
+        const float epsilon = CONSTRAINT_GRADIENT_DIVISION_LIMIT;
+        const float target = __ldg(prm + 3);
+        const bool st1 = s.kind[i1] & K_STATIC, st2 = s.kind[i2] & K_STATIC;
+        const float w1 = st1 ? 0.f : 1.0f / s.mass(i1);
+        const float w2 = st2 ? 0.f : 1.0f / s.mass(i2);
+        const f2 v1 = scale2(f2{s.mx[i1], s.my[i1]}, w1);
+        const f2 v2 = scale2(f2{s.mx[i2], s.my[i2]}, w2);
+        const f2 rel = sub2(v2, v1);
+        const f2 d = sub2(f2{s.px[i2], s.py[i2]}, f2{s.px[i1], s.py[i1]});
+        const f2 normal = normalize2(d);
+        const float dist_error = length2(d) - target;
+        const float pc = beta * dist_error / zmax(target, 0.001f);
+        float J = -(dot2(rel, normal) + pc) / (w1 + w2);
+        const float ndv = dot2(normal, rel);
+        const float den = 1.0f / zmax(fabsf(ndv), epsilon);
+        J = zclamp(J, pmin * den, pmax * den);
+        const f2 dp = scale2(normal, J);
+        s.mx[i1] -= dp.x;
+        s.my[i1] -= dp.y;
+        s.mx[i2] += dp.x;
+        s.my[i2] += dp.y;
+    } else if (type == J_OFFSET) {  // OffsetDistanceJoint.zig:44-105
+        const float epsilon = CONSTRAINT_GRADIENT_DIVISION_LIMIT;
+        const f2 r1 = {__ldg(prm + 3), __ldg(prm + 4)}, r2 = {__ldg(prm + 5), __ldg(prm + 6)};
+        const float target = __ldg(prm + 7);
+        const bool st1 = s.kind[i1] & K_STATIC, st2 = s.kind[i2] & K_STATIC;
+        const f2 rr1 = rot(r1, s.cs[i1], s.sn[i1]);
+        const f2 rr2 = rot(r2, s.cs[i2], s.sn[i2]);
+        const f2 a1 = add2(rr1, f2{s.px[i1], s.py[i1]});
+        const f2 a2 = add2(rr2, f2{s.px[i2], s.py[i2]});
+        const f2 normal = normalize2(sub2(a2, a1));
+        const float inv_m1 = st1 ? 0.f : 1.0f / s.mass(i1);
+        const float inv_m2 = st2 ? 0.f : 1.0f / s.mass(i2);
+        const float inv_i1 = st1 ? 0.f : 1.0f / s.inertia(i1);
+        const float inv_i2 = st2 ? 0.f : 1.0f / s.inertia(i2);
+        const f2 vl1 = scale2(f2{s.mx[i1], s.my[i1]}, inv_m1);
+        const float om1 = s.L[i1] * inv_i1;
+        const f2 vl2 = scale2(f2{s.mx[i2], s.my[i2]}, inv_m2);
+        const float om2 = s.L[i2] * inv_i2;
+        const f2 v1 = add2(vl1, f2{-rr1.y * om1, rr1.x * om1});
+        const f2 v2 = add2(vl2, f2{-rr2.y * om2, rr2.x * om2});
+        const f2 dv = sub2(v2, v1);
+        const float dist_error = length2(sub2(a2, a1)) - target;
+        const float pc = beta * dist_error / zmax(target, epsilon);
+        const float num = dot2(normal, dv) + pc;
+        const float r1xn = cross2(rr1, normal);
+        const float r2xn = cross2(rr2, normal);
+        const float den = inv_m1 + inv_m2 + r1xn * r1xn * inv_i1 + r2xn * r2xn * inv_i2;
+        float J = -num / den;
+        const float ndv = dot2(normal, dv);
+        const float den2 = 1.0f / zmax(fabsf(ndv), epsilon);
+        J = zclamp(J, pmin * den2, pmax * den2);
+        const f2 dp = scale2(normal, J);
+        s.mx[i1] -= dp.x;
+        s.my[i1] -= dp.y;
+        s.L[i1] -= J * r1xn;
+        s.mx[i2] += dp.x;
+        s.my[i2] += dp.y;
+        s.L[i2] += J * r2xn;
+    } else if (type == J_FIXED) {  // FixedPositionJoint.zig:38-72
+        if (s.kind[i1] & K_STATIC) return;
+        const float epsilon = ALLOWED_CONSTRAINT_VALUE;
+        const f2 target = {__ldg(prm + 3), __ldg(prm + 4)};
+        const float w = 1.0f / s.mass(i1);
+        const f2 v = scale2(f2{s.mx[i1], s.my[i1]}, w);
+        const f2 delta = sub2(target, f2{s.px[i1], s.py[i1]});
+        const float dist = length2(delta);
+        if (dist < ALLOWED_CONSTRAINT_VALUE) return;
+        const f2 normal = scale2(delta, 1.0f / dist);
+        const float bias = beta * dist;
+        const float relv = dot2(v, normal);
+        float J = -(relv - bias) / w;
+        const float den = 1.0f / zmax(fabsf(relv), epsilon);
+        J = zclamp(J, pmin * den, pmax * den);
+        const f2 dp = scale2(normal, J);
+        s.mx[i1] += dp.x;
+        s.my[i1] += dp.y;
+    } else {  // MotorJoint.zig:38-64
+        if (s.kind[i1] & K_STATIC) return;
+        const float epsilon = ALLOWED_CONSTRAINT_VALUE;
+        const float target = __ldg(prm + 3);
+        const float I = s.inertia(i1);
+        const float omega = s.L[i1] / I;
+        const float C = omega - target;
+        if (fabsf(C) < ALLOWED_CONSTRAINT_VALUE) return;
+        const float bias = beta * C;
+        const float torque = s.tq[i1];
+        float J = torque - bias;
+        const float relv = torque / I;
+        const float den = 1.0f / zmax(fabsf(relv), epsilon);
+        J = zclamp(J, pmin * den, pmax * den);
+        s.L[i1] += J * h;
+    }
+}
+
+__device__ __forceinline__ bool joint_two_bodies(uint8_t type) {
+    return type == J_DISTANCE || type == J_OFFSET;
+}
+
+}  // namespace r2d

@@ -175,10 +175,10 @@ struct StepParams {
     const uint32_t* ids;         // [nbodies]
     uint32_t nbodies;
     const uint8_t* jtype;        // [njoints]
-    const uint16_t* jb1;         // world-local body index
-    const uint16_t* jb2;
+    const uint32_t* jb1;         // world-local body index
+    const uint32_t* jb2;
     const float* jprm;           // [njoints][JOINT_PARAMS]
-    const uint32_t* excl;        // sorted (lo << 16 | hi) per world
+    const unsigned long long* excl;  // sorted ((u64)lo << 32 | hi) per world
     int* world_status;           // [nworlds]
     uint32_t* world_fail_call;   // [nworlds] first call a world failed in; ~0u = healthy
     uint32_t* world_capbits;     // [nworlds] CAP_* bits of the buffers that overflowed

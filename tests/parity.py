@@ -10,6 +10,7 @@ be identical.
 from __future__ import annotations
 
 import numpy as np
+import pytest
 
 FIELDS = ["pos_x", "pos_y", "angle", "mom_x", "mom_y", "ang_mom", "force_x", "force_y", "torque",
           "aabb_x", "aabb_y", "aabb_hw", "aabb_hh"]
@@ -60,3 +61,40 @@ def assert_manifolds_equal(gk, gd, gc, ok, od, oc):
         bad = mismatch(dg, do)
         assert not bad.any(), f"manifold {k}: fields {np.flatnonzero(bad).tolist()} gpu {dg[bad]} oracle {do[bad]}"
         assert cg == co, f"manifold {k}: colour gpu {cg} oracle {co}"
+
+
+def run_pair(sc, steps, check_every=1, debug=True, sub_steps=None, iters=None, **world_kw):
+    """Step scene `sc` on the GPU (one world through the C ABI) and on the
+    oracle in colour-major order; compare state, manifolds and colours every
+    `check_every` steps.  Returns (world, oracle), or (None, None) when the
+    step fails on both with the same status."""
+    from oracle import ORDER_COLOUR, Oracle
+    from resolve2d_gb300 import _native as N
+    from resolve2d_gb300.engine import World
+
+    S = sc.sub_steps if sub_steps is None else sub_steps
+    I = sc.iters if iters is None else iters
+    w = World.from_scene(sc, debug=debug, **world_kw)
+    o = Oracle.from_scene(sc)
+    assert_state_equal(w.read_state(), o.state(), "initial state")
+    for s in range(steps):
+        want = o.process(sc.dt, S, I, ORDER_COLOUR)
+        if want != 0:
+            # the reference's step fails here too (e.g. a non-finite AABB,
+            # whose @intFromFloat is undefined); the GPU must report the same
+            # error and leave the state of the last good step
+            with pytest.raises(N.R2DError) as e:
+                w.process(sc.dt, S, I)
+                w.sync()
+            assert e.value.code == want, (e.value.code, want)
+            return None, None
+        w.process(sc.dt, S, I)
+        w.sync()
+        if (s + 1) % check_every == 0 or s + 1 == steps:
+            assert_state_equal(w.read_state(), o.state(), f"{sc.name} step {s + 1}")
+            if debug:
+                gk, gd, gc = w.manifolds()
+                ok, od = o.manifolds()
+                oc, _ = o.colours()
+                assert_manifolds_equal(gk, gd, gc, ok, od, oc)
+    return w, o

@@ -9,41 +9,12 @@ import numpy as np
 import pytest
 
 from oracle import ORDER_COLOUR, Oracle
-from parity import assert_manifolds_equal, assert_state_equal
+from parity import assert_manifolds_equal, assert_state_equal, run_pair
 from resolve2d_gb300 import _native as N
 from resolve2d_gb300 import scenes
 from resolve2d_gb300.engine import Batch, World
 
 pytestmark = pytest.mark.gpu
-
-
-def run_pair(sc, steps, check_every=1, debug=True, sub_steps=None, iters=None):
-    S = sc.sub_steps if sub_steps is None else sub_steps
-    I = sc.iters if iters is None else iters
-    w = World.from_scene(sc, debug=debug)
-    o = Oracle.from_scene(sc)
-    assert_state_equal(w.read_state(), o.state(), "initial state")
-    for s in range(steps):
-        want = o.process(sc.dt, S, I, ORDER_COLOUR)
-        if want != 0:
-            # the reference's step fails here too (e.g. a non-finite AABB,
-            # whose @intFromFloat is undefined); the GPU must report the same
-            # error and leave the state of the last good step
-            with pytest.raises(N.R2DError) as e:
-                w.process(sc.dt, S, I)
-                w.sync()
-            assert e.value.code == want, (e.value.code, want)
-            return None, None
-        w.process(sc.dt, S, I)
-        w.sync()
-        if (s + 1) % check_every == 0 or s + 1 == steps:
-            assert_state_equal(w.read_state(), o.state(), f"{sc.name} step {s + 1}")
-            if debug:
-                gk, gd, gc = w.manifolds()
-                ok, od = o.manifolds()
-                oc, _ = o.colours()
-                assert_manifolds_equal(gk, gd, gc, ok, od, oc)
-    return w, o
 
 
 def test_config0_first_steps_bit_exact():
@@ -189,13 +160,11 @@ def test_empty_single_and_static_worlds():
         run_pair(sc, steps=5)
 
 
-def test_world_over_capacity_reports_error():
-    sc = scenes.batched_worlds("big", seed=1, nworlds=1, steps=1, lo=1500, hi=1500)
-    w = World.from_scene(sc)
-    with pytest.raises(N.R2DError) as e:
-        w.process(sc.dt, 1, 8)
-        w.sync()
-    assert e.value.code == -5
+def test_world_above_fused_limit_takes_grid_pipeline():
+    # 1,500 bodies exceed the largest fused class (520): the world steps
+    # through the grid-wide pipeline and still matches the oracle bit for bit
+    sc = scenes.batched_worlds("big", seed=1, nworlds=1, steps=6, lo=1500, hi=1500)
+    run_pair(sc, steps=6, check_every=2)
 
 
 def test_unknown_joint_body_id_is_an_error():
