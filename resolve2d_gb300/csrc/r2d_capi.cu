@@ -743,6 +743,34 @@ struct Engine {
     }
 #endif
 
+    // Debug taps hold `dbg.cap` manifolds per world; a world replayed with
+    // larger buffers needs more.  Re-pitch every world's slots to the new cap.
+    int grow_debug(uint32_t cap) {
+        if (!dbg.cap || cap <= dbg.cap) return R2D_OK;
+        uint32_t *keys = nullptr, *col = nullptr;
+        float* data = nullptr;
+        CUDA_TRY(dalloc(keys, (size_t)nworlds * cap * 2));
+        CUDA_TRY(dalloc(data, (size_t)nworlds * cap * DEBUG_MF));
+        CUDA_TRY(dalloc(col, (size_t)nworlds * cap));
+        const size_t o = dbg.cap, h = nworlds;
+        CUDA_TRY(cudaMemcpy2DAsync(keys, 8 * (size_t)cap, d_dbg_keys, 8 * o, 8 * o, h, cudaMemcpyDeviceToDevice, stream));
+        CUDA_TRY(cudaMemcpy2DAsync(data, 4 * DEBUG_MF * (size_t)cap, d_dbg_data, 4 * DEBUG_MF * o, 4 * DEBUG_MF * o, h,
+                                   cudaMemcpyDeviceToDevice, stream));
+        CUDA_TRY(cudaMemcpy2DAsync(col, 4 * (size_t)cap, d_dbg_col, 4 * o, 4 * o, h, cudaMemcpyDeviceToDevice, stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        dfree(d_dbg_keys);
+        dfree(d_dbg_data);
+        dfree(d_dbg_col);
+        d_dbg_keys = keys;
+        d_dbg_data = data;
+        d_dbg_col = col;
+        dbg.cap = cap;
+        dbg.keys = keys;
+        dbg.data = data;
+        dbg.colour = col;
+        return R2D_OK;
+    }
+
     // Re-run world w from call `from` to the last logged call with every
     // capacity doubled, up to three times.  The world's state is exactly the
     // state before its failing call (a failing world writes nothing back).
@@ -780,6 +808,7 @@ struct Engine {
                         w, d.n, capbits, from, c.nm, c.npt, c.ne, c.np, opts.lean ? "lean" : "full",
                         make_layout(c, opts).total);
             if ((int)make_layout(c, opts).total > smem_limit()) break;
+            if (int st = grow_debug(c.nm)) return st;
             CUDA_TRY(cudaMemsetAsync(d_fail_call + w, 0xFF, sizeof(uint32_t), stream));
             CUDA_TRY(cudaMemsetAsync(d_capbits + w, 0, sizeof(uint32_t), stream));
             CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), stream));

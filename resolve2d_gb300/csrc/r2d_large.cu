@@ -59,12 +59,13 @@ enum LargeCounter : int {
 
 inline uint32_t blocks(uint64_t n) { return (uint32_t)std::max<uint64_t>(1, (n + LT - 1) / LT); }
 
-// In-place exclusive scan of a[0..n) by one block of 1024 threads; a[n]
-// receives the total.
-__global__ void __launch_bounds__(1024) lk_scan(uint32_t* a, uint32_t n) {
+// In-place exclusive scan of a[0..n) by one block of SCAN_THREADS threads;
+// a[n] receives the total.
+constexpr int SCAN_THREADS = 1024;
+__global__ void __launch_bounds__(SCAN_THREADS) lk_scan(uint32_t* a, uint32_t n) {
     __shared__ uint32_t wsum[32];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const uint32_t per = (n + 1023) / 1024;
+    const uint32_t per = (n + SCAN_THREADS - 1) / SCAN_THREADS;
     const uint32_t beg = min(n, (uint32_t)tid * per), end = min(n, beg + per);
     uint32_t s = 0;
     for (uint32_t i = beg; i < end; ++i) s += a[i];
@@ -92,7 +93,7 @@ __global__ void __launch_bounds__(1024) lk_scan(uint32_t* a, uint32_t n) {
         a[i] = run;
         run += v;
     }
-    if (tid == 1023) a[n] = wsum[31];
+    if (tid == SCAN_THREADS - 1) a[n] = wsum[31];
 }
 
 // ---------------------------------------------------------------------------
@@ -697,6 +698,12 @@ LargeWorld::~LargeWorld() { delete impl; }
         kernel<<<(grid), LT, 0, st>>>(__VA_ARGS__); \
         ++I.nlaunch;                                \
     } while (0)
+// the scan is one block of exactly SCAN_THREADS threads
+#define SCAN(a, n)                                      \
+    do {                                                \
+        lk_scan<<<1, SCAN_THREADS, 0, st>>>((a), (n));  \
+        ++I.nlaunch;                                    \
+    } while (0)
 
 int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32_t iters, cudaStream_t st,
                      std::string* msg) {
@@ -751,9 +758,9 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
     const uint32_t E = (uint32_t)E64;
     LTRY(regrow(I.cap_e, (size_t)E + 1, {LB(I.ebucket), LB(I.ebody), LB(I.eslot), LB(I.sbody)}));
     A.ebucket = I.ebucket; A.ebody = I.ebody; A.eslot = I.eslot; A.sbody = I.sbody;
-    LAUNCH(lk_scan, 1, I.bcnt, n);
+    SCAN(I.bcnt, n);
     LAUNCH(lk_emit, blocks(n), A);
-    LAUNCH(lk_scan, 1, I.table, T);
+    SCAN(I.table, T);
     LAUNCH(lk_scatter, blocks(E), A, E);
 
     // ---- candidate pairs (the set grows until it holds them all) ----
@@ -813,7 +820,7 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
         LTRY(cudaMemsetAsync(I.adj, 0, sizeof(uint32_t) * ((size_t)n + 1), st));
         LTRY(cudaMemsetAsync(I.cnt, 0, sizeof(uint32_t) * LC_N, st));
         LAUNCH(lk_col_count, blocks(count), C);
-        LAUNCH(lk_scan, 1, I.adj, n);
+        SCAN(I.adj, n);
         LTRY(cudaMemcpyAsync(I.cursor, I.adj, sizeof(uint32_t) * ((size_t)n + 1), cudaMemcpyDeviceToDevice, st));
         LAUNCH(lk_col_fill, blocks(count), C);
         // Each round colours at least the highest-priority uncoloured
