@@ -15,10 +15,15 @@ e2e        the same metric through the C ABI with host buffers: every step
            back (r2d_batch_write_state / process / read_state).
 roofline   algorithmic HBM bytes of the world-step kernel per step
            (117 B per body-step: 77 B read, 40 B written) over its measured
-           time, against the measured copy bandwidth.
+           time, against the measured copy bandwidth.  The unit is one step's
+           world-step launches (one per size class, run concurrently on their
+           own streams), timed by the events around the step.
+pos_error_vs_fp64  the first 32 worlds stepped 600 steps from their initial
+           state on the GPU (f32) and on the FP64 oracle: position error in
+           body radii (disc radius; half the shorter side of a rectangle).
 cpu_baseline  the CPU oracle (the C++ restatement of the reference's step,
            replaying the same constraint order) on this host's cores, from
-           the same settled state.
+           the same settled state, for about ten seconds.
 
 --impl reference times that CPU step alone (the reference is Zig and cannot
 be built here) and prints its own line.
@@ -148,6 +153,29 @@ def oracle_time(sc, state, steps, threads):
     return secs
 
 
+def pos_error_vs_fp64(sc, nworlds: int, steps: int, stream):
+    """Position error of the f32 GPU step against the FP64 oracle after
+    `steps` steps of the first `nworlds` worlds, in body radii."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+    from resolve2d_gb300.engine import Batch
+
+    sub = sc.worlds(0, nworlds)
+    b = Batch.from_scene(sub, stream=stream)
+    for _ in range(steps):
+        b.process(sub.dt, sub.sub_steps, sub.iters)
+    b.sync()
+    got = b.read_state().astype(np.float64)
+    b.close()
+    _, want, st = O.batch_run(sub, steps, cpu_threads(), precision=64)
+    assert st == 0, st
+    dyn = (sub.kind & 2) == 0
+    err = np.hypot(got[0] - want[0], got[1] - want[1])[dyn] / sub.body_radius()[dyn]
+    return {"worlds": nworlds, "steps": steps, "bodies": int(dyn.sum()), "unit": "body radii",
+            "max": float(err.max()), "p99": float(np.percentile(err, 99)), "median": float(np.median(err)),
+            "frac_below_1e-3": float((err < 1e-3).mean()), "integration": "f32 (reference mode)"}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -187,6 +215,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-precision", action="store_true", help="skip the f32 vs FP64 position-error sample")
     ap.add_argument("--plain-worlds", type=int, default=64,
                     help="worlds stepped one per launch for the plain-path comparison")
     args = ap.parse_args()
@@ -309,19 +338,23 @@ def main():
         "e2e": {"value": e2e_v, "unit": "body-steps/s", "h2d_bytes_per_step": 52 * nb, "d2h_bytes_per_step": 52 * nb},
         "plain_one_world_per_launch": {"value": plain, "unit": "body-steps/s", "worlds": args.plain_worlds,
                                        "batched_over_plain": (value / world) / plain if plain else None},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "roofline": {"bound": "hbm", "kernel": "world_step_kernel (the size-class launches of one step)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_src,
                      "traffic": None if traffic is None else traffic * nb,
                      "bytes_per_body_step": BYTES_READ + BYTES_WRITE},
         "clocks": clk,
     }
+    if rank == 0 and not args.no_precision:
+        line["pos_error_vs_fp64"] = pos_error_vs_fp64(sc, 32, 600, stream.cuda_stream)
     if rank == 0 and not args.no_cpu_baseline:
         threads = cpu_threads()
-        sub_steps = 2
-        secs = oracle_time(sc, settled, sub_steps, threads)
-        line["cpu_baseline"] = {"value": nb * sub_steps / secs, "unit": "body-steps/s", "cores": threads,
-                                "kind": "port",
-                                "sample": f"all {sc.nworlds} worlds x {sub_steps} steps from the settled state "
+        one = oracle_time(sc, settled, 1, threads)
+        cpu_steps = max(2, min(200, int(10.0 / max(one, 1e-3))))
+        secs = oracle_time(sc, settled, cpu_steps, threads)
+        line["cpu_baseline"] = {"value": nb * cpu_steps / secs, "unit": "body-steps/s", "cores": threads,
+                                "kind": "port", "seconds": secs,
+                                "sample": f"all {sc.nworlds} worlds x {cpu_steps} steps from the settled state "
                                           "(C++ restatement of Solver.process; Zig toolchain absent)"}
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -69,7 +69,7 @@ __device__ __forceinline__ void solve_contact(const SWT<IDX>& s, uint32_t m) {
         const float bias = s.bias[p];
         if (bias < 0.0f) continue;  // depth >= 0: accumulators stay 0 (collision.zig:154-158)
         f2 r1, r2;
-        s.arms<LEAN>(p, a, b, &r1, &r2);
+        s.template arms<LEAN>(p, a, b, &r1, &r2);
         const f2 v1 = add2(vlinear_1, f2{-r1.y * omega1, r1.x * omega1});
         const f2 v2 = add2(vlinear_2, f2{-r2.y * omega2, r2.x * omega2});
         const f2 dv = sub2(v1, v2);

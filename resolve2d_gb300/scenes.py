@@ -84,6 +84,26 @@ class Scene:
             xworld=np.zeros(int(xm.sum()), np.uint32), xpairs=self.xpairs[xm],
         )
 
+    def worlds(self, w0: int, w1: int) -> "Scene":
+        """Worlds ``w0 .. w1-1`` as their own (joint-free) scene."""
+        assert self.jtype.size == 0 and self.xpairs.size == 0, "joint-free scenes only"
+        b0, b1 = int(self.body_off[w0]), int(self.body_off[w1])
+        return Scene(
+            name=f"{self.name}[{w0}:{w1}]",
+            ids=self.ids[b0:b1].copy(),
+            kind=self.kind[b0:b1].copy(),
+            opt=self.opt[:, b0:b1].copy(),
+            body_off=(self.body_off[w0 : w1 + 1] - self.body_off[w0]).astype(np.uint32),
+            gravity=self.gravity[w0:w1].copy(),
+            dt=self.dt, sub_steps=self.sub_steps, iters=self.iters, steps=self.steps,
+        )
+
+    def body_radius(self) -> np.ndarray:
+        """Size of each body for error figures: a disc's radius, half the
+        shorter side of a rectangle."""
+        rect = (self.kind & KIND_RECT) != 0
+        return np.where(rect, 0.5 * np.minimum(self.opt[DIM0], self.opt[DIM1]), self.opt[DIM0]).astype(np.float64)
+
 
 def derive_props_state(kind: np.ndarray, opt: np.ndarray):
     """Mass, inertia and initial momenta of new bodies, in float32.
