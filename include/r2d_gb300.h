@@ -3,9 +3,9 @@
  *
  * It replaces the CPU step of nilsblix/resolve2d, Solver.process
  * (src/core/lib.zig:189-251), behind plain pointers and sizes so that the
- * reference's own host language can bind it (Zig `extern fn`; the binding a
- * maintainer would add is shown in INTEGRATION.md).  Reference paths below
- * are relative to the reference project.
+ * reference's own host language can bind it directly (one Zig `extern fn`
+ * per entry point).  Reference paths below are relative to the reference
+ * project.
  *
  * Conventions
  *   - Every entry point returns an r2d_status (0 = success, negative = error).
@@ -108,7 +108,7 @@ typedef struct r2d_config {
     uint32_t flags;
     void* stream;
     /* Scales the per-world buffer sizes of the fused kernel (0 = 1.0).  A
-     * world that outgrows a buffer is replayed with doubled sizes, so this
+     * world that outgrows a buffer is replayed with larger sizes, so this
      * trades shared memory against replays; it never changes results. */
     float capacity_scale;
 } r2d_config;
