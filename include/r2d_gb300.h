@@ -184,6 +184,39 @@ R2D_API int r2d_batch_num_manifolds(r2d_batch* b, uint32_t w, uint32_t* out);
 R2D_API int r2d_batch_get_manifolds(r2d_batch* b, uint32_t w, uint32_t cap, uint32_t* keys, float* data,
                                     uint32_t* colours);
 
+/* ---------------------------------------------------------------------------
+ * One world stepped with no allocation.  No counterpart in the reference.
+ *
+ * For callers that must not allocate device memory once they run: a fixed-step
+ * physics tick inside a game or robotics frame loop with a hard frame budget
+ * (cudaMalloc and cudaFree can synchronise the whole device and stall the
+ * frame), or an embedder that owns all device memory through its own pool and
+ * forbids driver allocations after start-up.  The caller passes the world in
+ * its own DEVICE buffers (state [13][n] and props [5][n] field-major as
+ * above, kind [n], ids [n]; AABB fields initialised, e.g. from
+ * r2d_solver_read_state); `state` is stepped in place, as one
+ * r2d_solver_process call would step it, bit for bit.  `gravity` is a host
+ * array of ngrav <= 4 magnitudes; cell_width 0 and table_mult 0 select 4.0
+ * and 2.
+ *
+ * Scratch lives in one static device array of 3,899,392 bytes (3.72 MiB),
+ * which every GPU that loads this library holds until the process exits.
+ * Limits: 4,096 bodies, 65,536 spatial-hash cell entries, 16,384 candidate
+ * pairs, no joints or exclusions; a world beyond them returns
+ * R2D_ERR_CAPACITY with the state untouched.  The call allocates nothing
+ * (no cudaMalloc, cudaFree or pinned host memory) and synchronises `stream`
+ * a few times to read counters back.
+ *
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  Every call on a device shares the one array and
+ * overwrites it: calls that overlap on the GPU (two streams, two host threads)
+ * race, so serialise them.
+ * ------------------------------------------------------------------------- */
+R2D_API int r2d_world_step_static(float* state, const float* props, const uint8_t* kind, const uint32_t* ids,
+                                  uint32_t n, const float* gravity, uint32_t ngrav, float dt, uint32_t sub_steps,
+                                  uint32_t collision_iters, float cell_width, uint32_t table_mult, void* stream);
+
 /* Library information. */
 R2D_API const char* r2d_last_error_string(void);
 R2D_API int r2d_version(void);

@@ -1184,4 +1184,31 @@ R2D_API int r2d_batch_get_manifolds(r2d_batch* b, uint32_t w, uint32_t cap, uint
     return guarded([&] { return b->eng.get_manifolds(w, cap, keys, data, colours); });
 }
 
+// The allocation-free world step: validation here, the pipeline over the
+// static scratch array in r2d_large.cu.
+R2D_API int r2d_world_step_static(float* state, const float* props, const uint8_t* kind, const uint32_t* ids,
+                                  uint32_t n, const float* gravity, uint32_t ngrav, float dt, uint32_t sub_steps,
+                                  uint32_t collision_iters, float cell_width, uint32_t table_mult, void* stream) {
+    if (n && (!state || !props || !kind || !ids)) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL device buffer");
+    if (ngrav > (uint32_t)MAX_GRAVITY || (ngrav && !gravity))
+        return fail(R2D_ERR_INVALID_ARGUMENT, "at most 4 gravity generators, passed by a host array");
+    if (sub_steps == 0) return fail(R2D_ERR_INVALID_ARGUMENT, "sub_steps must be >= 1");
+    StaticStepArgs a{};
+    a.state = state;
+    a.props = props;
+    a.kind = kind;
+    a.ids = ids;
+    a.n = n;
+    a.ngrav = ngrav;
+    for (uint32_t k = 0; k < ngrav; ++k) a.g[k] = gravity[k];
+    a.dt = dt;
+    a.sub_steps = sub_steps;
+    a.iters = collision_iters;
+    a.cell = cell_width > 0.f ? cell_width : 4.0f;
+    a.table_mult = table_mult ? table_mult : 2u;
+    std::string msg;
+    const int r = static_world_step(a, (cudaStream_t)stream, &msg);
+    return r ? fail(r, msg) : R2D_OK;
+}
+
 }  // extern "C"

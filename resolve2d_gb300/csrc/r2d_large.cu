@@ -28,6 +28,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <initializer_list>
 #include <string>
@@ -932,6 +933,278 @@ int LargeWorld::joint_colours(uint32_t cap, uint32_t* colours, cudaStream_t st, 
     lk_widen<<<blocks(m), LT, 0, st>>>(I.jcol, m, I.dc);
     LTRY(cudaStreamSynchronize(st));
     LTRY(cudaMemcpy(colours, I.dc, 4ull * m, cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+
+// ---------------------------------------------------------------------------
+// The world step with no allocation (r2d_world_step_static).  Some callers
+// cannot allocate device memory once they are running: a fixed-step physics
+// tick inside a frame loop with a hard budget (cudaMalloc and cudaFree can
+// synchronise the whole device and stall the frame), or an embedder whose
+// own pool owns all device memory.  For them the same kernels run with their
+// scratch carved from one file-scope device array instead of cudaMalloc'd
+// buffers, and the host side keeps its counters on the stack.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct StaticCarve {
+    size_t off = 0;
+    template <class T>
+    constexpr size_t take(size_t count) {
+        const size_t at = off;
+        off = (off + count * sizeof(T) + 255) / 256 * 256;
+        return at;
+    }
+};
+
+// Byte offsets of every scratch buffer for the static maxima; the same
+// function sizes the array (at compile time) and hands out the pointers.
+struct StaticLayout {
+    size_t inv_m, inv_i, cs, sn, tq, ang_prev, kind, rx0, ry0, rx1, ry1, bcnt, adj, cursor;
+    size_t table, ebucket, ebody, eslot, sbody, hset, pairs;
+    size_t ma, mb, mp0, corder, mnp, mcol, nx, ny, fric;
+    size_t r1x, r1y, r2x, r2y, depth, odepth, mn, mt, apn, apt, bias;
+    size_t adjl, prio, jcol, jorder, cnt, entries, hist;
+    size_t total;
+};
+
+constexpr uint32_t SX_BODIES = R2D_STATIC_MAX_BODIES;
+constexpr uint32_t SX_BUCKETS = 2 * R2D_STATIC_MAX_BODIES;
+constexpr uint32_t SX_ENTRIES = R2D_STATIC_MAX_CELL_ENTRIES;
+constexpr uint32_t SX_PAIRS = R2D_STATIC_MAX_PAIRS;
+constexpr uint32_t SX_HASH = 2 * R2D_STATIC_MAX_PAIRS;  // power of two, >= 1.5x the pairs
+
+constexpr StaticLayout static_layout() {
+    StaticLayout L{};
+    StaticCarve c;
+    const size_t nb = SX_BODIES + 1, np = SX_PAIRS + 1, npt = 2 * (size_t)SX_PAIRS + 1;
+    L.inv_m = c.take<float>(nb); L.inv_i = c.take<float>(nb); L.cs = c.take<float>(nb); L.sn = c.take<float>(nb);
+    L.tq = c.take<float>(nb); L.ang_prev = c.take<float>(nb); L.kind = c.take<uint8_t>(nb);
+    L.rx0 = c.take<int32_t>(nb); L.ry0 = c.take<int32_t>(nb); L.rx1 = c.take<int32_t>(nb); L.ry1 = c.take<int32_t>(nb);
+    L.bcnt = c.take<uint32_t>(nb); L.adj = c.take<uint32_t>(nb); L.cursor = c.take<uint32_t>(nb);
+    L.table = c.take<uint32_t>(SX_BUCKETS + 1);
+    L.ebucket = c.take<uint32_t>(SX_ENTRIES + 1); L.ebody = c.take<uint32_t>(SX_ENTRIES + 1);
+    L.eslot = c.take<uint32_t>(SX_ENTRIES + 1); L.sbody = c.take<uint32_t>(SX_ENTRIES + 1);
+    L.hset = c.take<unsigned long long>(SX_HASH); L.pairs = c.take<unsigned long long>(SX_PAIRS);
+    L.ma = c.take<uint32_t>(np); L.mb = c.take<uint32_t>(np); L.mp0 = c.take<uint32_t>(np);
+    L.corder = c.take<uint32_t>(np); L.mnp = c.take<uint8_t>(np); L.mcol = c.take<uint8_t>(np);
+    L.nx = c.take<float>(np); L.ny = c.take<float>(np); L.fric = c.take<float>(np);
+    L.r1x = c.take<float>(npt); L.r1y = c.take<float>(npt); L.r2x = c.take<float>(npt); L.r2y = c.take<float>(npt);
+    L.depth = c.take<float>(npt); L.odepth = c.take<float>(npt); L.mn = c.take<float>(npt); L.mt = c.take<float>(npt);
+    L.apn = c.take<float>(npt); L.apt = c.take<float>(npt); L.bias = c.take<float>(npt);
+    L.adjl = c.take<uint32_t>(2 * (size_t)SX_PAIRS + 2); L.prio = c.take<uint32_t>(2 * (size_t)SX_PAIRS + 2);
+    L.jcol = c.take<uint8_t>(1); L.jorder = c.take<uint32_t>(1);
+    L.cnt = c.take<uint32_t>(LC_N); L.entries = c.take<unsigned long long>(1);
+    L.hist = c.take<uint32_t>(MAX_COLOURS + 1);
+    L.total = c.off;
+    return L;
+}
+
+constexpr StaticLayout SL = static_layout();
+static_assert(SL.total == R2D_STATIC_SCRATCH_BYTES, "R2D_STATIC_SCRATCH_BYTES must equal the carved layout");
+
+// The scratch of every allocation-free call on this device.  Each GPU that
+// loads the library holds these R2D_STATIC_SCRATCH_BYTES until the process
+// exits.  In host code the name stands for the symbol, not an address: the
+// address comes from cudaGetSymbolAddress, once per device.
+static __device__ __align__(256) unsigned char g_static_scratch[R2D_STATIC_SCRATCH_BYTES];
+
+constexpr int STATIC_MAX_DEVICES = 64;
+std::atomic<unsigned char*> g_static_ptr[STATIC_MAX_DEVICES];
+
+}  // namespace
+
+int static_scratch_address(unsigned char** out, std::string* msg) {
+    int dev = 0;
+    LTRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= STATIC_MAX_DEVICES) {
+        *msg = "device index beyond " + std::to_string(STATIC_MAX_DEVICES);
+        return -1;
+    }
+    unsigned char* p = g_static_ptr[dev].load();
+    if (!p) {
+        // set-up, once per device, with that device current
+        void* sym = nullptr;
+        LTRY(cudaGetSymbolAddress(&sym, g_static_scratch));
+        p = static_cast<unsigned char*>(sym);
+        g_static_ptr[dev].store(p);
+    }
+    *out = p;
+    return 0;
+}
+
+#undef LAUNCH
+#undef SCAN
+#define LAUNCH(kernel, grid, ...) kernel<<<(grid), LT, 0, st>>>(__VA_ARGS__)
+#define SCAN(a, n) lk_scan<<<1, SCAN_THREADS, 0, st>>>((a), (n))
+
+int static_world_step(const StaticStepArgs& in, cudaStream_t st, std::string* msg) {
+    const uint32_t n = in.n;
+    if (n == 0) return 0;
+    if (n > SX_BODIES) {
+        *msg = std::to_string(n) + " bodies exceed the static-scratch maximum of " + std::to_string(SX_BODIES);
+        return DS_CAPACITY;
+    }
+    const uint32_t T = in.table_mult * n;
+    if (in.table_mult == 0 || T > SX_BUCKETS) {
+        *msg = "spatial-hash table of " + std::to_string(T) + " buckets exceeds the static-scratch maximum of " +
+               std::to_string(SX_BUCKETS);
+        return DS_CAPACITY;
+    }
+    unsigned char* base = nullptr;
+    if (int r = static_scratch_address(&base, msg)) return r;
+#define SP(T_, field) reinterpret_cast<T_*>(base + SL.field)
+    uint32_t* cnt = SP(uint32_t, cnt);
+    unsigned long long* entries = SP(unsigned long long, entries);
+    uint32_t* hist = SP(uint32_t, hist);
+    uint32_t h[LC_N + 2];  // counters read back to the host (host stack, no allocation)
+
+    SWT<uint32_t> s{};
+    float* S = in.state;
+    s.px = S + (size_t)S_POS_X * n; s.py = S + (size_t)S_POS_Y * n; s.ang = S + (size_t)S_ANGLE * n;
+    s.mx = S + (size_t)S_MOM_X * n; s.my = S + (size_t)S_MOM_Y * n; s.L = S + (size_t)S_ANG_MOM * n;
+    s.inv_m = SP(float, inv_m); s.inv_i = SP(float, inv_i); s.cs = SP(float, cs); s.sn = SP(float, sn);
+    s.ang_prev = SP(float, ang_prev); s.tq = SP(float, tq);
+    s.px0 = nullptr; s.py0 = nullptr; s.pos0 = false;
+    s.gmass = in.props + (size_t)P_MASS * n;
+    s.ginertia = in.props + (size_t)P_INERTIA * n;
+    s.kind = SP(uint8_t, kind);
+    s.ma = SP(uint32_t, ma); s.mb = SP(uint32_t, mb); s.mp0 = SP(uint32_t, mp0);
+    s.mnp = SP(uint8_t, mnp); s.mcol = SP(uint8_t, mcol);
+    s.nx = SP(float, nx); s.ny = SP(float, ny); s.fric = SP(float, fric);
+    s.r1x = SP(float, r1x); s.r1y = SP(float, r1y); s.r2x = SP(float, r2x); s.r2y = SP(float, r2y);
+    s.depth = SP(float, depth); s.odepth = SP(float, odepth); s.mn = SP(float, mn); s.mt = SP(float, mt);
+    s.apn = SP(float, apn); s.apt = SP(float, apt); s.bias = SP(float, bias);
+
+    Phase1 A{};
+    A.s = s;
+    A.state = in.state; A.props = in.props; A.kind_in = in.kind; A.ids = in.ids;
+    A.NB = n; A.base = 0; A.n = n; A.cell = in.cell;
+    A.bmod = BucketMod{bucket_recip(T), T};
+    A.disc_rot = false;
+    A.rx0 = SP(int32_t, rx0); A.ry0 = SP(int32_t, ry0); A.rx1 = SP(int32_t, rx1); A.ry1 = SP(int32_t, ry1);
+    A.bcnt = SP(uint32_t, bcnt); A.table = SP(uint32_t, table);
+    A.ebucket = SP(uint32_t, ebucket); A.ebody = SP(uint32_t, ebody); A.eslot = SP(uint32_t, eslot);
+    A.sbody = SP(uint32_t, sbody);
+    A.hset = SP(unsigned long long, hset); A.pairs = SP(unsigned long long, pairs);
+    A.np = SX_PAIRS; A.hs = SX_HASH;
+    A.excl = nullptr; A.nexcl = 0;
+    A.cnt = cnt; A.entries = entries;
+
+    // The array keeps the previous call's contents: clear what starts at zero.
+    LTRY(cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * LC_N, st));
+    LTRY(cudaMemsetAsync(entries, 0, sizeof(unsigned long long), st));
+    LTRY(cudaMemsetAsync(A.table, 0, sizeof(uint32_t) * ((size_t)T + 1), st));
+    LTRY(cudaMemsetAsync(A.hset, 0xFF, sizeof(unsigned long long) * SX_HASH, st));
+    LAUNCH(lk_load, blocks(n), A);
+    LTRY(cudaMemcpyAsync(h, cnt, sizeof(uint32_t) * LC_N, cudaMemcpyDeviceToHost, st));
+    LTRY(cudaMemcpyAsync(h + LC_N, entries, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    LTRY(cudaStreamSynchronize(st));
+    if (h[LC_NONFINITE]) {
+        *msg = "a body's AABB is not finite (it has no spatial-hash cell)";
+        return DS_NONFINITE;
+    }
+    unsigned long long E64 = 0;
+    memcpy(&E64, h + LC_N, sizeof(E64));
+    if (h[LC_BIG] || E64 > SX_ENTRIES) {
+        *msg = "the bodies cover more than the static-scratch maximum of " + std::to_string(SX_ENTRIES) +
+               " spatial-hash cell entries";
+        return DS_CAPACITY;
+    }
+    const uint32_t E = (uint32_t)E64;
+    SCAN(A.bcnt, n);
+    LAUNCH(lk_emit, blocks(n), A);
+    SCAN(A.table, T);
+    LAUNCH(lk_scatter, blocks(E), A, E);
+    LAUNCH(lk_pairs, blocks(E), A, E);
+    LTRY(cudaMemcpyAsync(h, cnt, sizeof(uint32_t) * LC_N, cudaMemcpyDeviceToHost, st));
+    LTRY(cudaStreamSynchronize(st));
+    if (h[LC_PAIR_OVERFLOW]) {
+        *msg = "more candidate pairs than the static-scratch maximum of " + std::to_string(SX_PAIRS);
+        return DS_CAPACITY;
+    }
+    const uint32_t npairs = h[LC_PAIRS];
+    A.nm = npairs;
+    A.npt = 2 * npairs;
+    LTRY(cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * LC_N, st));
+    LAUNCH(lk_narrow, blocks(npairs), A, npairs);
+    LTRY(cudaMemcpyAsync(h, cnt, sizeof(uint32_t) * LC_N, cudaMemcpyDeviceToHost, st));
+    LTRY(cudaStreamSynchronize(st));
+    const uint32_t M = h[LC_MANIFOLDS];
+
+    // contact colouring (Jones-Plassmann rounds), colour-major order
+    uint32_t coff[MAX_COLOURS + 1];
+    uint32_t ncol = 0;
+    coff[0] = 0;
+    if (M) {
+        Colouring C{};
+        C.count = M;
+        C.joints = false;
+        C.ma = s.ma; C.mb = s.mb; C.kind = s.kind; C.colour = s.mcol;
+        C.adj = SP(uint32_t, adj); C.adjl = SP(uint32_t, adjl); C.prio = SP(uint32_t, prio);
+        C.cursor = SP(uint32_t, cursor); C.cnt = cnt;
+        LTRY(cudaMemsetAsync(C.adj, 0, sizeof(uint32_t) * ((size_t)n + 1), st));
+        LTRY(cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * LC_N, st));
+        LAUNCH(lk_col_count, blocks(M), C);
+        SCAN(C.adj, n);
+        LTRY(cudaMemcpyAsync(C.cursor, C.adj, sizeof(uint32_t) * ((size_t)n + 1), cudaMemcpyDeviceToDevice, st));
+        LAUNCH(lk_col_fill, blocks(M), C);
+        for (uint32_t rounds = 0;;) {
+            for (int r = 0; r < 4; ++r) {
+                LTRY(cudaMemsetAsync(cnt + LC_PENDING, 0, sizeof(uint32_t), st));
+                LAUNCH(lk_col_round, blocks(M), C);
+            }
+            rounds += 4;
+            LTRY(cudaMemcpyAsync(h, cnt, sizeof(uint32_t) * LC_N, cudaMemcpyDeviceToHost, st));
+            LTRY(cudaStreamSynchronize(st));
+            if (h[LC_COLOURS]) {
+                *msg = "a contact needs more than " + std::to_string(MAX_COLOURS) + " colours";
+                return DS_CAPACITY;
+            }
+            if (h[LC_PENDING] == 0) break;
+            if (rounds > M + 4) {
+                *msg = "the colouring did not finish";
+                return -4;
+            }
+        }
+        uint32_t hh[MAX_COLOURS + 1];
+        LTRY(cudaMemsetAsync(hist, 0, sizeof(uint32_t) * (MAX_COLOURS + 1), st));
+        LAUNCH(lk_col_hist, blocks(M), C, hist);
+        LTRY(cudaMemcpyAsync(hh, hist, sizeof(uint32_t) * (MAX_COLOURS + 1), cudaMemcpyDeviceToHost, st));
+        LTRY(cudaStreamSynchronize(st));
+        for (uint32_t c = 0; c < (uint32_t)MAX_COLOURS; ++c)
+            if (hh[c]) ncol = c + 1;
+        for (uint32_t c = 0; c < ncol; ++c) coff[c + 1] = coff[c] + hh[c];
+        LTRY(cudaMemcpyAsync(hist, coff, sizeof(uint32_t) * (ncol + 1), cudaMemcpyHostToDevice, st));
+        LAUNCH(lk_col_order, blocks(M), C, hist, SP(uint32_t, corder));
+        LTRY(cudaStreamSynchronize(st));  // coff is the source of the copy above
+    }
+
+    // substeps: the caller's state changes from here on
+    Phase2 P{};
+    P.s = s;
+    P.state = in.state; P.props = in.props; P.NB = n; P.base = 0; P.n = n; P.nman = M;
+    P.h = in.dt / (float)in.sub_steps;
+    P.disc_rot = false;
+    P.ngrav = in.ngrav;
+    for (int k = 0; k < MAX_GRAVITY; ++k) P.g[k] = in.g[k];
+    P.order = SP(uint32_t, corder);
+    for (uint32_t sub = 0; sub < in.sub_steps; ++sub) {
+        P.first = sub == 0;
+        P.last = sub + 1 == in.sub_steps;
+        LAUNCH(lk_forces, blocks(n), P);
+        if (M) LAUNCH(lk_prestep, blocks(M), P);
+        for (uint32_t it = 0; it < in.iters; ++it)
+            for (uint32_t c = 0; c < ncol; ++c) {
+                P.k0 = coff[c];
+                P.k1 = coff[c + 1];
+                LAUNCH(lk_contacts, blocks(P.k1 - P.k0), P);
+            }
+        LAUNCH(lk_integrate, blocks(n), P);
+    }
+#undef SP
+    LTRY(cudaGetLastError());
     return 0;
 }
 

@@ -59,4 +59,27 @@ private:
     Impl* impl;
 };
 
+// Allocation-free world step (r2d_world_step_static): maxima of the static
+// scratch array and the inputs of one call.
+#define R2D_STATIC_MAX_BODIES 4096u
+#define R2D_STATIC_MAX_CELL_ENTRIES 65536u
+#define R2D_STATIC_MAX_PAIRS 16384u
+#define R2D_STATIC_SCRATCH_BYTES 3899392ull  // 3.72 MiB
+
+struct StaticStepArgs {
+    float* state;          // [S_NFIELDS][n], device
+    const float* props;    // [P_NFIELDS][n], device
+    const uint8_t* kind;   // [n], device
+    const uint32_t* ids;   // [n], device
+    uint32_t n;
+    uint32_t ngrav;
+    float g[MAX_GRAVITY];
+    float dt;
+    uint32_t sub_steps, iters;
+    float cell;
+    uint32_t table_mult;
+};
+
+int static_world_step(const StaticStepArgs& in, cudaStream_t st, std::string* msg);
+
 }  // namespace r2d
