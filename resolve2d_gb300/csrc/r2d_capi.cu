@@ -66,12 +66,6 @@ cudaError_t dalloc(T*& p, size_t count) {
     return cudaMalloc((void**)&p, count * sizeof(T));
 }
 
-uint32_t next_pow2(uint32_t v) {
-    uint32_t p = 1;
-    while (p < v) p <<= 1;
-    return p;
-}
-
 // AABB of a freshly created body (Disc.zig:63-66, Rectangle.zig:71-86).
 void init_aabb(uint8_t kind, float x, float y, float angle, float d0, float d1, float out[4]) {
     out[0] = x;
@@ -389,27 +383,47 @@ struct Engine {
         c.npt = sz((2.25 * nb + 16.0) * ppm + 16.0, 1);
         c.ne = sz(std::max(2.5 * nb + 64.0, max_cells * 1.25 + 64.0), 2);
         c.np = sz(3.25 * nb + 32.0, 3);
-        c.hs = next_pow2((3u * c.np + 1u) / 2u);
+        c.hs = c.np;
         c.nj = max_nj;
         c.nt = table_mult * nb;
         return c;
     }
 
-    uint32_t cells_of(uint32_t i) const {
+    // Cell width of a world's binning grid (WorldDesc::fine_cell): the
+    // largest dynamic body's diameter plus twice the binning margin, so that
+    // such a body covers at most 2 x 2 cells; between 1/16 of the spatial
+    // hash's cell and that cell.
+    float fine_cell_of(uint32_t w) const {
+        const WorldDesc& d = worlds_h[w];
         const uint32_t n = nbodies;
-        const float x = state_h[(size_t)S_AABB_X * n + i], y = state_h[(size_t)S_AABB_Y * n + i];
-        const float hw = state_h[(size_t)S_AABB_HW * n + i], hh = state_h[(size_t)S_AABB_HH * n + i];
-        // rotation can grow a rectangle's extents up to its half-diagonal
-        float r = hw > hh ? hw : hh;
-        if (kind_h[i] & K_RECT) {
+        float dmax = 0.f;
+        for (uint32_t i = d.body_off; i < d.body_off + d.n; ++i) {
+            if (kind_h[i] & K_STATIC) continue;
             const float d0 = props_h[(size_t)P_DIM0 * n + i], d1 = props_h[(size_t)P_DIM1 * n + i];
-            r = 0.5f * std::sqrt(d0 * d0 + d1 * d1);
+            const float dia = (kind_h[i] & K_RECT) ? std::sqrt(d0 * d0 + d1 * d1) : 2.0f * d0;
+            if (dia > dmax) dmax = dia;
         }
-        (void)x;
-        (void)y;
-        const double span = std::floor(2.0 * r / cell) + 2.0;
-        const double c = span * span;
-        return c > 65535.0 ? 65535u : (uint32_t)c;
+        if (!(dmax > 0.f)) return cell;
+        return std::min(cell, std::max(cell / 16.0f, dmax + 0.05f));
+    }
+
+    // Expected binning-grid cells of world w: a dynamic body covers 1-4
+    // cells (2.25 on average is planned for; more replays), a static body
+    // its AABB's span.
+    uint32_t fine_cells_of_world(uint32_t w) const {
+        const WorldDesc& d = worlds_h[w];
+        const uint32_t n = nbodies;
+        const float g = d.fine_cell > 0.f ? d.fine_cell : fine_cell_of(w);
+        double total = 0.0;
+        for (uint32_t i = d.body_off; i < d.body_off + d.n; ++i) {
+            if (!(kind_h[i] & K_STATIC)) {
+                total += 2.25;
+                continue;
+            }
+            const double hw = state_h[(size_t)S_AABB_HW * n + i], hh = state_h[(size_t)S_AABB_HH * n + i];
+            total += (std::floor(2.0 * hw / g) + 2.0) * (std::floor(2.0 * hh / g) + 2.0);
+        }
+        return total > 65535.0 ? 65535u : (uint32_t)std::ceil(total);
     }
 
     LayoutOpts layout_opts(bool lean, bool multi_substep) const {
@@ -444,16 +458,15 @@ struct Engine {
             return k;
         };
         const int smem_optin = smem_limit();
+        for (uint32_t w = 0; w < nworlds; ++w) worlds_h[w].fine_cell = fine_cell_of(w);
         // A world whose own buffers do not fit one CTA's shared memory (many
         // spatial-hash cells, say) takes the grid-wide pipeline.
         for (uint32_t w = 0; w < nworlds; ++w) {
             if (world_large[w]) continue;
             const WorldDesc& d = worlds_h[w];
-            uint32_t rects = 0, cells = 0;
-            for (uint32_t i = d.body_off; i < d.body_off + d.n; ++i) {
-                rects += (kind_h[i] & K_RECT) ? 1u : 0u;
-                cells += cells_of(i);
-            }
+            uint32_t rects = 0;
+            for (uint32_t i = d.body_off; i < d.body_off + d.n; ++i) rects += (kind_h[i] & K_RECT) ? 1u : 0u;
+            const uint32_t cells = fine_cells_of_world(w);
             const float rf = d.n ? (float)rects / (float)d.n : 0.f;
             const Caps c = caps_for(bounds[bound_of(d.n)], d.nj, rf, cells, world_boost[w]);
             if ((int)make_layout(c, layout_opts(!(world_boost[w] & BOOST_FULL), plan_multi_substep)).total > smem_optin)
@@ -483,11 +496,9 @@ struct Engine {
             for (uint32_t w : groups[gk]) {
                 const WorldDesc& d = worlds_h[w];
                 max_nj = std::max(max_nj, d.nj);
-                uint32_t rects = 0, cells = 0;
-                for (uint32_t i = d.body_off; i < d.body_off + d.n; ++i) {
-                    rects += (kind_h[i] & K_RECT) ? 1u : 0u;
-                    cells += cells_of(i);
-                }
+                uint32_t rects = 0;
+                for (uint32_t i = d.body_off; i < d.body_off + d.n; ++i) rects += (kind_h[i] & K_RECT) ? 1u : 0u;
+                const uint32_t cells = fine_cells_of_world(w);
                 max_cells = std::max(max_cells, cells);
                 if (d.n) rect_frac = std::max(rect_frac, (float)rects / (float)d.n);
             }
@@ -732,12 +743,13 @@ struct Engine {
             for (uint32_t w : c.worlds)
                 for (int k = 0; k < PHASE_SLOTS; ++k) acc[k] += (double)t[(size_t)w * PHASE_SLOTS + k];
             const double steps = acc[11] > 0 ? acc[11] : 1;
-            fprintf(stderr, "r2d timers nb=%u thr=%d worlds=%zu smem=%u | load %.0f bp %.0f [cells %.0f sort %.0f] "
-                            "np %.0f col %.0f [sort %.0f walk %.0f] jcol %.0f solve %.0f wb %.0f | pairs %.1f man %.1f "
-                            "colours %.1f\n",
+            fprintf(stderr, "r2d timers nb=%u thr=%d worlds=%zu smem=%u | load %.0f bp %.0f [cells %.0f sort %.0f "
+                            "cand %.0f compact %.0f] np %.0f col %.0f [sort %.0f walk %.0f] jcol %.0f solve %.0f "
+                            "wb %.0f | entries %.1f candidates %.1f pairs %.1f man %.1f colours %.1f\n",
                     c.caps.nb, c.threads, c.worlds.size(), c.smem, acc[0] / steps, acc[1] / steps, acc[12] / steps,
-                    acc[13] / steps, acc[2] / steps, acc[3] / steps, acc[15] / steps, acc[16] / steps, acc[4] / steps,
-                    acc[5] / steps, acc[6] / steps, acc[7] / steps, acc[8] / steps, acc[9] / steps);
+                    acc[13] / steps, acc[14] / steps, acc[17] / steps, acc[2] / steps, acc[3] / steps,
+                    acc[15] / steps, acc[16] / steps, acc[4] / steps, acc[5] / steps, acc[6] / steps,
+                    acc[19] / steps, acc[18] / steps, acc[7] / steps, acc[8] / steps, acc[9] / steps);
         }
         cudaMemset(d_timers, 0, 8 * t.size());
     }
@@ -781,11 +793,9 @@ struct Engine {
         CUDA_TRY(cudaMemcpyAsync(d_one, &w, sizeof(uint32_t), cudaMemcpyHostToDevice, stream));
         CUDA_TRY(cudaStreamSynchronize(stream));
         const WorldDesc& d = worlds_h[w];
-        uint32_t rects = 0, cells = 0;
-        for (uint32_t i = d.body_off; i < d.body_off + d.n; ++i) {
-            rects += (kind_h[i] & K_RECT) ? 1u : 0u;
-            cells += cells_of(i);
-        }
+        uint32_t rects = 0;
+        for (uint32_t i = d.body_off; i < d.body_off + d.n; ++i) rects += (kind_h[i] & K_RECT) ? 1u : 0u;
+        const uint32_t cells = fine_cells_of_world(w);
         const float rf = d.n ? (float)rects / (float)d.n : 0.f;
         uint32_t capbits = 0;
         CUDA_TRY(cudaMemcpy(&capbits, d_capbits + w, sizeof(uint32_t), cudaMemcpyDeviceToHost));

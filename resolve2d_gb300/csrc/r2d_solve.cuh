@@ -110,6 +110,106 @@ __device__ __forceinline__ void solve_contact(const SWT<IDX>& s, uint32_t m) {
     }
 }
 
+// calculateImpulses with two lanes per manifold: lane 2q + h of a warp takes
+// contact point h.  Both points start from the velocities read once per
+// manifold (collision.zig:145-149), so they are independent until their
+// impulses reach the bodies; the even lane adds them in the reference's
+// order, point 0 then point 1, which keeps every sum bit-identical to
+// solve_contact.  Every lane of the warp must call this (it shuffles);
+// `valid` says whether the lane pair holds a manifold.
+template <bool LEAN, class IDX>
+__device__ __forceinline__ void solve_contact_lanes(const SWT<IDX>& s, uint32_t m, bool valid, uint32_t lane) {
+    const uint32_t half = lane & 1u;
+    uint32_t a = 0, b = 0;
+    bool sa = true, sb = true, hit = false;
+    f2 dp = {0.f, 0.f};
+    float c1 = 0.f, c2 = 0.f;
+    if (valid) {
+        a = s.ma[m];
+        b = s.mb[m];
+        sa = s.kind[a] & K_STATIC;
+        sb = s.kind[b] & K_STATIC;
+        if (half < (uint32_t)s.mnp[m]) {
+            const uint32_t p = s.mp0[m] + half;
+            const float bias = s.bias[p];
+            if (!(bias < 0.0f)) {  // bias < 0: depth >= 0, accumulators stay 0 (collision.zig:154-158)
+                const float inv_m1 = s.inv_m[a], inv_m2 = s.inv_m[b];
+                const float inv_i1 = s.inv_i[a], inv_i2 = s.inv_i[b];
+                const f2 vlinear_1 = scale2(f2{s.mx[a], s.my[a]}, inv_m1);
+                const float omega1 = s.L[a] * inv_i1;
+                const f2 vlinear_2 = scale2(f2{s.mx[b], s.my[b]}, inv_m2);
+                const float omega2 = s.L[b] * inv_i2;
+                const f2 n = {s.nx[m], s.ny[m]};
+                const f2 t = cw90(n);
+                f2 r1, r2;
+                s.template arms<LEAN>(p, a, b, &r1, &r2);
+                const f2 v1 = add2(vlinear_1, f2{-r1.y * omega1, r1.x * omega1});
+                const f2 v2 = add2(vlinear_2, f2{-r2.y * omega2, r2.x * omega2});
+                const f2 dv = sub2(v1, v2);
+                float num = dot2(dv, n) + bias;
+                const float pn = num * s.mn[p];
+                if (!(pn < MIN_MANIFOLD_IMPULSE)) {  // as solve_contact's skip, NaN included
+                    num = dot2(dv, t);
+                    const float pt = num * s.mt[p];
+                    const float acc = s.apn[p];
+                    const float nacc = zmax(0.0f, acc + pn);
+                    const float applied_pn = nacc - acc;
+                    s.apn[p] = nacc;
+                    const float max_pt = s.fric[m] * fabsf(nacc);
+                    const float acct = s.apt[p];
+                    const float nacct = zclamp(acct + pt, -max_pt, max_pt);
+                    const float applied_pt = nacct - acct;
+                    s.apt[p] = nacct;
+                    dp = add2(scale2(n, applied_pn), scale2(t, applied_pt));
+                    c1 = cross2(r1, dp);
+                    c2 = cross2(r2, dp);
+                    hit = true;
+                }
+            }
+        }
+    }
+    const float dqx = __shfl_down_sync(0xffffffffu, dp.x, 1);
+    const float dqy = __shfl_down_sync(0xffffffffu, dp.y, 1);
+    const float q1 = __shfl_down_sync(0xffffffffu, c1, 1);
+    const float q2 = __shfl_down_sync(0xffffffffu, c2, 1);
+    const bool hit1 = __shfl_down_sync(0xffffffffu, hit ? 1 : 0, 1) != 0;
+    if (!valid || half) return;
+    f2 alp1 = {0.f, 0.f}, alp2 = {0.f, 0.f};
+    float arp1 = 0.f, arp2 = 0.f;
+    if (hit) {
+        if (!sa) {
+            alp1 = sub2(alp1, dp);
+            arp1 -= c1;
+        }
+        if (!sb) {
+            alp2 = add2(alp2, dp);
+            arp2 += c2;
+        }
+    }
+    if (hit1) {
+        const f2 d1 = {dqx, dqy};
+        if (!sa) {
+            alp1 = sub2(alp1, d1);
+            arp1 -= q1;
+        }
+        if (!sb) {
+            alp2 = add2(alp2, d1);
+            arp2 += q2;
+        }
+    }
+    // A static body receives exactly +0 in the reference; its state is left alone.
+    if (!sa) {
+        s.mx[a] += alp1.x;
+        s.my[a] += alp1.y;
+        s.L[a] += arp1;
+    }
+    if (!sb) {
+        s.mx[b] += alp2.x;
+        s.my[b] += alp2.y;
+        s.L[b] += arp2;
+    }
+}
+
 // Constraint solve functions (src/core/Constraints/*.zig).
 template <class IDX>
 __device__ __forceinline__ void solve_joint(const SWT<IDX>& s, uint8_t type, uint32_t i1, uint32_t i2,

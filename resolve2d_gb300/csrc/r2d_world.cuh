@@ -33,6 +33,11 @@ struct WorldDesc {
     // floor((2^64 - 1) / (table_mult * n)): Barrett reciprocal of the
     // spatial-hash table size, so the kernel needs no 64-bit division
     unsigned long long bucket_recip;
+    // Cell width of the binning grid that finds candidate pairs: about one
+    // body diameter, so a bucket holds a few bodies (the spatial hash's own
+    // cells still decide which pairs are candidates).
+    float fine_cell;
+    uint32_t pad_;
 };
 
 // Per-world capacities of one kernel class; every buffer below is sized
@@ -43,7 +48,7 @@ struct Caps {
     uint32_t npt;  // contact points
     uint32_t ne;   // (cell, body) entries of the spatial hash
     uint32_t np;   // candidate pairs that passed the AABB test
-    uint32_t hs;   // pair hash-set slots (power of two)
+    uint32_t hs;   // candidate-pair list slots before the pairs are grouped (= np)
     uint32_t nj;   // joints
     uint32_t nt;   // spatial-hash buckets (table_mult * bodies)
 };
@@ -56,7 +61,7 @@ struct Layout {
     uint32_t ma, mb, mp0, mnp, mcol, nx, ny, fric;
     uint32_t r1x, r1y, r2x, r2y, depth, odepth, mn, mt, apn, apt, bias;
     // broadphase scratch (inside the manifold region)
-    uint32_t ax, ay, ahw, ahh, rx0, ry0, rx1, ry1, bcnt, ebucket, ebody, eslot, sbody, table, hset;
+    uint32_t ax, ay, ahw, ahh, rx0, ry0, rx1, ry1, fx0, fy0, fx1, fy1, bcnt, ebucket, ebody, eslot, sbody, table, hset;
     // colouring scratch: sort keys, per-body colour masks
     uint32_t skey, cmask;
     // optional arrays (offset 0 = absent)
@@ -127,6 +132,7 @@ __host__ __device__ inline Layout make_layout(const Caps& c, const LayoutOpts& f
     o = xbase;
     L.ax = take(nb4); L.ay = take(nb4); L.ahw = take(nb4); L.ahh = take(nb4);
     L.rx0 = take(nb4); L.ry0 = take(nb4); L.rx1 = take(nb4); L.ry1 = take(nb4);
+    L.fx0 = take(nb4); L.fy0 = take(nb4); L.fx1 = take(nb4); L.fy1 = take(nb4);
     L.bcnt = take(4 * (c.nb + 1));
     L.ebucket = take(4 * c.ne); L.ebody = take(2 * c.ne); L.eslot = take(2 * c.ne);
     L.sbody = take(2 * c.ne);

@@ -16,6 +16,7 @@
  * equals the reference's per-constraint arithmetic replayed colour by colour.
  * No floating-point atomics are used anywhere: every run is bit-reproducible.
  */
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -24,6 +25,8 @@
 #include "r2d_world.cuh"
 
 namespace r2d {
+
+namespace cg = cooperative_groups;
 
 template <int NT>
 __device__ uint32_t block_scan_excl(uint32_t* a, uint32_t n, uint32_t* wsum) {
@@ -62,15 +65,67 @@ __device__ uint32_t block_scan_excl(uint32_t* a, uint32_t n, uint32_t* wsum) {
     return total;
 }
 
-__device__ __forceinline__ bool hs_insert(uint32_t* hs, uint32_t mask, uint32_t key, int* err) {
-    uint32_t h = (key * 0x9E3779B1u) ^ (key >> 15);
-    for (uint32_t probe = 0; probe <= mask; ++probe) {
-        uint32_t slot = (h + probe) & mask;
-        uint32_t prev = atomicCAS(&hs[slot], 0xFFFFFFFFu, key);
-        if (prev == 0xFFFFFFFFu) return true;
-        if (prev == key) return false;
+// Exclusive scan of one u64 value per thread across the block; *total gets
+// the block's sum.  Shared scratch: 32 words.
+template <int NT>
+__device__ unsigned long long block_scan_value_u64(unsigned long long v, unsigned long long* wsum,
+                                                   unsigned long long* total) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int NW = NT / 32;
+    unsigned long long x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
     }
-    *err = DS_CAPACITY;
+    if (lane == 31) wsum[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned long long w = lane < NW ? wsum[lane] : 0ull;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < NW) wsum[lane] = w;
+    }
+    __syncthreads();
+    const unsigned long long before = (warp ? wsum[warp - 1] : 0ull) + x - v;
+    *total = wsum[NW - 1];
+    __syncthreads();
+    return before;
+}
+
+// Cell of entry e of body i: entries are emitted row by row over the body's
+// cell range, starting at its prefix offset `start`.
+__device__ __forceinline__ void entry_cell(uint32_t e, uint32_t start, int32_t x0, int32_t x1, int32_t y0,
+                                           int32_t* x, int32_t* y) {
+    const uint32_t t = e - start, wx = (uint32_t)(x1 - x0) + 1u;
+    if (wx == 1u) {
+        *x = x0;
+        *y = y0 + (int32_t)t;
+    } else if (wx == 2u) {
+        *x = x0 + (int32_t)(t & 1u);
+        *y = y0 + (int32_t)(t >> 1);
+    } else {
+        *x = x0 + (int32_t)(t % wx);
+        *y = y0 + (int32_t)(t / wx);
+    }
+}
+
+// Whether bodies i and j share a bucket of the reference's spatial hash,
+// given their cell ranges (SpatialHash.zig:78-137): a common cell, or two
+// cells whose buckets collide.
+__device__ __forceinline__ bool shares_bucket(uint32_t i, uint32_t j, const int32_t* rx0, const int32_t* ry0,
+                                              const int32_t* rx1, const int32_t* ry1, const BucketMod& bmod) {
+    if (max(rx0[i], rx0[j]) <= min(rx1[i], rx1[j]) && max(ry0[i], ry0[j]) <= min(ry1[i], ry1[j])) return true;
+    for (int32_t yi = ry0[i]; yi <= ry1[i]; ++yi)
+        for (int32_t xi = rx0[i]; xi <= rx1[i]; ++xi) {
+            const uint32_t bi = cell_bucket(xi, yi, bmod);
+            for (int32_t yj = ry0[j]; yj <= ry1[j]; ++yj)
+                for (int32_t xj = rx0[j]; xj <= rx1[j]; ++xj)
+                    if (cell_bucket(xj, yj, bmod) == bi) return true;
+        }
     return false;
 }
 
@@ -92,59 +147,60 @@ __device__ __forceinline__ void cap_fail(int* err, uint32_t* s_capbits, uint32_t
     atomicOr(s_capbits, bit);
 }
 
+// Orders constraints 0..count-1 into skey[0..count) by (mix, tie): a
+// counting sort on the top 8 bits of the mix (mixes are uniform hashes, so
+// each of the 256 buckets holds a few constraints), then an insertion sort of
+// each bucket by the full (mix, tie) key.  skey[k] = mix << 32 | index.
+template <int NT, class Mix, class Tie>
+__device__ void priority_order(uint32_t count, Mix mix, Tie tie, unsigned long long* skey, uint32_t* bucket,
+                               uint32_t* wsum) {
+    const int tid = threadIdx.x;
+    for (uint32_t b = tid; b < 256; b += NT) bucket[b] = 0u;
+    __syncthreads();
+    for (uint32_t i = tid; i < count; i += NT) atomicAdd(&bucket[mix(i) >> 24], 1u);
+    __syncthreads();
+    block_scan_excl<NT>(bucket, 256, wsum);  // bucket[b] = first slot of bucket b
+    for (uint32_t i = tid; i < count; i += NT) {
+        const uint32_t h = mix(i);
+        skey[atomicAdd(&bucket[h >> 24], 1u)] = ((unsigned long long)h << 32) | i;
+    }
+    __syncthreads();  // bucket[b] = one past the last slot of bucket b
+    for (uint32_t b = tid; b < 256; b += NT) {
+        const uint32_t lo = b ? bucket[b - 1] : 0u, hi = bucket[b];
+        for (uint32_t x = lo + 1; x < hi; ++x) {
+            const unsigned long long v = skey[x];
+            const uint32_t hv = (uint32_t)(v >> 32), tv = tie((uint32_t)v);
+            uint32_t y = x;
+            while (y > lo) {
+                const unsigned long long u = skey[y - 1];
+                const uint32_t hu = (uint32_t)(u >> 32);
+                if (hu < hv || (hu == hv && tie((uint32_t)u) < tv)) break;
+                skey[y] = u;
+                --y;
+            }
+            skey[y] = v;
+        }
+    }
+    __syncthreads();
+}
+
 // Colours `count` constraints by first-fit greedy in ascending priority
-// order (mix(i), then tie(i); unique per constraint; r2d_colour.h).  A
-// bitonic sort orders the constraints; then one warp walks the sorted list 32
-// at a time.  A lane takes the lowest colour absent from its nodes' colour masks
-// once every earlier lane of its chunk that shares a node is coloured, so the
-// result is exactly the sequential greedy colouring, computed with warp
-// shuffles instead of block-wide rounds.  ends(i, &a, &b) names constraint
-// i's conflict nodes (values >= 0x10000 mean "no node").  Returns true on
-// every thread when some constraint would need more than MAX_COLOURS colours.
+// order (mix(i), then tie(i); unique per constraint; r2d_colour.h).  The
+// constraints are put in priority order (priority_order); then one warp walks
+// the sorted list 32 at a time.  A lane takes the lowest colour absent from
+// its nodes' colour masks once every earlier lane of its chunk that shares a
+// node is coloured, so the result is exactly the sequential greedy colouring,
+// computed with warp shuffles instead of block-wide rounds.  ends(i, &a, &b)
+// names constraint i's conflict nodes (values >= 0x10000 mean "no node").
+// Returns true on every thread when some constraint would need more than
+// MAX_COLOURS colours.  bucket: 256 words of shared scratch.
 template <int NT, class Ends, class Mix, class Tie, class Hook>
 __device__ bool colour_greedy_sorted(uint32_t count, uint32_t n, Ends ends, Mix mix, Tie tie, uint8_t* colour,
-                                     unsigned long long* skey, uint32_t* cmask, Hook SUBPHASE_HOOK) {
+                                     unsigned long long* skey, uint32_t* cmask, uint32_t* bucket, uint32_t* wsum,
+                                     Hook SUBPHASE_HOOK) {
     const int tid = threadIdx.x, lane = tid & 31;
-    uint32_t N2 = 1;
-    while (N2 < count) N2 <<= 1;
-    // key = mix << 32 | index; equal mixes are reordered by their tie key below
-    for (uint32_t i = tid; i < N2; i += NT) skey[i] = i < count ? ((unsigned long long)mix(i) << 32) | i : ~0ull;
     for (uint32_t i = tid; i < 5 * n; i += NT) cmask[i] = 0u;
-    __syncthreads();
-    for (uint32_t k = 2; k <= N2; k <<= 1) {
-        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-            for (uint32_t i = tid; i < N2; i += NT) {
-                const uint32_t ixj = i ^ j;
-                if (ixj > i) {
-                    const unsigned long long a = skey[i], b = skey[ixj];
-                    if ((a > b) == ((i & k) == 0)) {
-                        skey[i] = b;
-                        skey[ixj] = a;
-                    }
-                }
-            }
-            __syncthreads();
-        }
-    }
-    // runs of equal mix (rare): order them by the tie key, first thread of a run
-    for (uint32_t i = tid; i + 1 < count; i += NT) {
-        const uint32_t h = (uint32_t)(skey[i] >> 32);
-        if ((i == 0 || (uint32_t)(skey[i - 1] >> 32) != h) && (uint32_t)(skey[i + 1] >> 32) == h) {
-            uint32_t e = i + 1;
-            while (e < count && (uint32_t)(skey[e] >> 32) == h) ++e;
-            for (uint32_t x = i + 1; x < e; ++x) {  // insertion sort by tie key
-                const unsigned long long v = skey[x];
-                const uint32_t tv = tie((uint32_t)v);
-                uint32_t y = x;
-                while (y > i && tie((uint32_t)skey[y - 1]) > tv) {
-                    skey[y] = skey[y - 1];
-                    --y;
-                }
-                skey[y] = v;
-            }
-        }
-    }
-    __syncthreads();
+    priority_order<NT>(count, mix, tie, skey, bucket, wsum);
     SUBPHASE_HOOK();
     int overflow = 0;
     if (tid < 32) {
@@ -230,6 +286,7 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
     __shared__ int s_err;
     __shared__ uint32_t s_capbits;
     __shared__ uint32_t s_cnt[4];  // pairs, manifolds, points
+    __shared__ unsigned long long s_wsum64[32];
 
     const int tid = threadIdx.x;
     if (blockIdx.x >= P.nlist) return;
@@ -312,11 +369,12 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
 
     float *ax = SMF(Lo.ax), *ay = SMF(Lo.ay), *ahw = SMF(Lo.ahw), *ahh = SMF(Lo.ahh);
     int32_t *rx0 = SMI32(Lo.rx0), *ry0 = SMI32(Lo.ry0), *rx1 = SMI32(Lo.rx1), *ry1 = SMI32(Lo.ry1);
+    int32_t *fx0 = SMI32(Lo.fx0), *fy0 = SMI32(Lo.fy0), *fx1 = SMI32(Lo.fx1), *fy1 = SMI32(Lo.fy1);
     uint32_t* bcnt = SMU32(Lo.bcnt);
     uint32_t* ebucket = SMU32(Lo.ebucket);
     uint16_t *ebody = SMU16(Lo.ebody), *eslot = SMU16(Lo.eslot), *sbody = SMU16(Lo.sbody);
     uint32_t* table = SMU32(Lo.table);
-    uint32_t* hset = SMU32(Lo.hset);
+    uint32_t* cand = SMU32(Lo.hset);  // candidate pairs before they are grouped by shape type
     unsigned long long* skey = reinterpret_cast<unsigned long long*>(sm + Lo.skey);
     uint32_t* cmask = SMU32(Lo.cmask);
     uint16_t *corder = SMU16(Lo.corder), *coff = SMU16(Lo.coff);
@@ -360,25 +418,46 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
         ahh[i] = st[(size_t)S_AABB_HH * NB + g];
     }
     for (uint32_t b = tid; b < T + 1; b += NT) table[b] = 0u;
-    for (uint32_t b = tid; b < C.hs; b += NT) hset[b] = 0xFFFFFFFFu;
     __syncthreads();
     PHASE(0);
 
     // ---------------- broadphase (SpatialHash.zig:19-137, lib.zig:264-282) ----------------
+    // The reference pairs every two bodies that share a bucket of its spatial
+    // hash (cells 4.0 wide: dense piles put ~30 bodies in one bucket) and
+    // keeps those whose AABBs intersect.  An intersecting pair shares a
+    // bucket exactly when its cell ranges overlap or two of its cells hash
+    // alike, so the kernel finds the intersecting pairs on a finer grid
+    // (boxes grown past the 0.01 overlap margin) and applies that test: the
+    // same pair set from a few candidates per body.
+    const float gfine = wd.fine_cell;
     for (uint32_t i = tid; i < n; i += NT) {
         int32_t x0 = 0, y0 = 0, x1 = -1, y1 = -1;
         uint32_t cnt = 0;
         const bool ok = cell_index(ax[i] - ahw[i], P.cell, &x0) && cell_index(ay[i] - ahh[i], P.cell, &y0) &&
                         cell_index(ax[i] + ahw[i], P.cell, &x1) && cell_index(ay[i] + ahh[i], P.cell, &y1);
+        int32_t u0 = 0, v0 = 0, u1 = -1, v1 = -1;
         if (!ok) {
             err = DS_NONFINITE;
             x1 = x0 - 1;
-        } else if (x1 >= x0 && y1 >= y0) {
-            const int64_t c64 = ((int64_t)x1 - (int64_t)x0 + 1) * ((int64_t)y1 - (int64_t)y0 + 1);
-            if (c64 > (int64_t)C.ne) cap_fail(&err, &s_capbits, CAP_ENTRIES);
-            else cnt = (uint32_t)c64;
+        } else {
+            // margin: the overlap epsilon, plus slack for the rounding of
+            // the intersection test at this magnitude
+            const float m = AABB_EPS_OVERLAP + 1e-6f * (fabsf(ax[i]) + fabsf(ay[i]) + ahw[i] + ahh[i]);
+            const bool okf = cell_index((ax[i] - ahw[i]) - m, gfine, &u0) &&
+                             cell_index((ay[i] - ahh[i]) - m, gfine, &v0) &&
+                             cell_index((ax[i] + ahw[i]) + m, gfine, &u1) &&
+                             cell_index((ay[i] + ahh[i]) + m, gfine, &v1);
+            if (!okf) {
+                cap_fail(&err, &s_capbits, CAP_ENTRIES);  // the grid pipeline bins on the coarse cells
+                u1 = u0 - 1;
+            } else if (u1 >= u0 && v1 >= v0) {
+                const int64_t c64 = ((int64_t)u1 - (int64_t)u0 + 1) * ((int64_t)v1 - (int64_t)v0 + 1);
+                if (c64 > (int64_t)C.ne) cap_fail(&err, &s_capbits, CAP_ENTRIES);
+                else cnt = (uint32_t)c64;
+            }
         }
         rx0[i] = x0; ry0[i] = y0; rx1[i] = x1; ry1[i] = y1;
+        fx0[i] = u0; fy0[i] = v0; fx1[i] = u1; fy1[i] = v1;
         bcnt[i] = cnt;
     }
     if (err) set_err(&s_err, err);
@@ -397,8 +476,8 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
         const BucketMod bmod = {wd.bucket_recip, T};
         for (uint32_t i = tid; i < n; i += NT) {
             uint32_t k = bcnt[i];
-            for (int32_t yi = ry0[i]; yi <= ry1[i]; ++yi)
-                for (int32_t xi = rx0[i]; xi <= rx1[i]; ++xi) {
+            for (int32_t yi = fy0[i]; yi <= fy1[i]; ++yi)
+                for (int32_t xi = fx0[i]; xi <= fx1[i]; ++xi) {
                     const uint32_t bk = cell_bucket(xi, yi, bmod);
                     ebucket[k] = bk;
                     ebody[k] = (uint16_t)i;
@@ -410,71 +489,177 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
         block_scan_excl<NT>(table, T, s_wsum);  // table[b] = first slot of bucket b
         for (uint32_t e = tid; e < E; e += NT) {
             const uint32_t slot = atomicAdd(&table[ebucket[e]], 1u);
-            sbody[slot] = ebody[e];
+            sbody[slot] = (uint16_t)e;  // the entry: body and cell
             eslot[e] = (uint16_t)slot;
         }
         __syncthreads();  // table[b] = one past the last slot of bucket b
         SUBPHASE(13);
 
-        // Candidates: every two entries of one bucket (the reference's query
-        // returns all bodies of the buckets a body covers), filtered as
-        // lib.zig:273-282, deduplicated like its "manifold already exists"
-        // test (lib.zig:278-281).
-        for (uint32_t e = tid; e < E; e += NT) {
-            const uint32_t i = ebody[e];
-            const uint32_t end = table[ebucket[e]];
-            const f2 pi = {ax[i], ay[i]};
-            const float hwi = ahw[i], hhi = ahh[i];
-            const bool sti = (s.kind[i] & K_STATIC) != 0;
-            for (uint32_t q = (uint32_t)eslot[e] + 1u; q < end; ++q) {
-                const uint32_t j = sbody[q];
-                if (j == i) continue;
+        // Candidates: every two entries of one fine bucket.  Entries of other
+        // cells that hash to the same bucket are skipped, and a pair is
+        // reported only from the first cell the two cover in common, so each
+        // pair comes out once (the reference's "manifold already exists"
+        // test, lib.zig:278-281, without a set).  Then the filters of
+        // lib.zig:273-282 and the shared-bucket test.  Entry e pairs with the
+        // entries after it in its bucket; a prefix sum over those counts deals
+        // the candidates out to the threads in equal contiguous ranges.
+        for (uint32_t e = tid; e < E; e += NT) ebucket[e] = table[ebucket[e]] - (uint32_t)eslot[e] - 1u;
+        __syncthreads();
+        const uint32_t W = block_scan_excl<NT>(ebucket, E, s_wsum);  // ebucket[e] = first candidate of e
+        const uint32_t k0 = (uint32_t)(((unsigned long long)W * (uint32_t)tid) / NT);
+        const uint32_t k1 = (uint32_t)(((unsigned long long)W * (uint32_t)(tid + 1)) / NT);
+        if (k0 < k1) {
+            uint32_t lo = 0, hi = E;  // the entry holding candidate k0: ebucket[lo] <= k0 < ebucket[hi]
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (ebucket[mid] <= k0) lo = mid;
+                else hi = mid;
+            }
+            uint32_t e = lo, first = ebucket[e], next = e + 1 < E ? ebucket[e + 1] : W;
+            uint32_t i = ebody[e];
+            int32_t fx0i = fx0[i], fy0i = fy0[i], cxe, cye;
+            entry_cell(e, bcnt[i], fx0i, fx1[i], fy0i, &cxe, &cye);
+            f2 pi = {ax[i], ay[i]};
+            float hwi = ahw[i], hhi = ahh[i];
+            bool sti = (s.kind[i] & K_STATIC) != 0;
+            for (uint32_t k = k0; k < k1; ++k) {
+                if (k >= next) {
+                    do {
+                        ++e;
+                        first = next;
+                        next = e + 1 < E ? ebucket[e + 1] : W;
+                    } while (k >= next);
+                    i = ebody[e];
+                    fx0i = fx0[i];
+                    fy0i = fy0[i];
+                    entry_cell(e, bcnt[i], fx0i, fx1[i], fy0i, &cxe, &cye);
+                    pi = f2{ax[i], ay[i]};
+                    hwi = ahw[i];
+                    hhi = ahh[i];
+                    sti = (s.kind[i] & K_STATIC) != 0;
+                }
+                const uint32_t e2 = sbody[(uint32_t)eslot[e] + 1u + (k - first)];
+                const uint32_t j = ebody[e2];
+                const int32_t fx0j = fx0[j], fy0j = fy0[j];
+                // a pair is reported from the first cell the two cover in common
+                if (max(fx0i, fx0j) != cxe || max(fy0i, fy0j) != cye) continue;
+                int32_t cx2, cy2;
+                entry_cell(e2, bcnt[j], fx0j, fx1[j], fy0j, &cx2, &cy2);
+                if (cx2 != cxe || cy2 != cye) continue;  // another cell hashed to this bucket
                 if (sti && (s.kind[j] & K_STATIC)) continue;
                 // symmetric in the two bodies: |dx|, |dy| and the sums commute
                 if (!aabb_intersects(pi, hwi, hhi, f2{ax[j], ay[j]}, ahw[j], ahh[j])) continue;
-                const uint32_t lo = min(i, j), hi = max(i, j);
-                const uint32_t key = (lo << 16) | hi;
-                if (wd.nexcl && excluded(P.excl + wd.excl_off, wd.nexcl, ((unsigned long long)lo << 32) | hi)) continue;
-                if (hs_insert(hset, C.hs - 1u, key, &err)) {
-                    const uint32_t idx = atomicAdd(&s_cnt[0], 1u);
-                    if (idx < C.np) pairs[idx] = key;
-                    else cap_fail(&err, &s_capbits, CAP_PAIRS);
-                } else if (err) {
-                    atomicOr(&s_capbits, (uint32_t)CAP_PAIRS);
-                }
+                if (!shares_bucket(i, j, rx0, ry0, rx1, ry1, bmod)) continue;
+                const uint32_t plo = min(i, j), phi = max(i, j);
+                if (wd.nexcl && excluded(P.excl + wd.excl_off, wd.nexcl, ((unsigned long long)plo << 32) | phi)) continue;
+                const cg::coalesced_group g = cg::coalesced_threads();
+                uint32_t at = 0;
+                if (g.thread_rank() == 0) at = atomicAdd(&s_cnt[0], g.size());
+                const uint32_t slot = g.shfl(at, 0) + g.thread_rank();
+                if (slot < C.hs) cand[slot] = (plo << 16) | phi;
             }
         }
+        __syncthreads();
+        SUBPHASE(14);
+#ifdef R2D_PHASE_TIMERS
+        if (tid == 0 && P.timers) {
+            P.timers[(size_t)w * PHASE_SLOTS + 18] += W;
+            P.timers[(size_t)w * PHASE_SLOTS + 19] += E;
+        }
+#endif
+        // The pair list, grouped by shape type (disc-disc, disc-rectangle,
+        // rectangle-rectangle) so that the narrowphase's warps mostly follow
+        // one code path.
+        {
+            const uint32_t found = s_cnt[0];
+            if (found > C.np) {
+                if (tid == 0) {
+                    s_err = DS_CAPACITY;
+                    s_capbits |= CAP_PAIRS;
+                }
+                __syncthreads();
+                goto fail;
+            }
+            const uint32_t per = (found + NT - 1) / NT;
+            const uint32_t s0 = min(found, (uint32_t)tid * per), s1 = min(found, s0 + per);
+            unsigned long long mine = 0;
+            for (uint32_t q = s0; q < s1; ++q) {
+                const uint32_t key = cand[q];
+                mine += 1ull << (21u * ((s.kind[key >> 16] & K_RECT) + (s.kind[key & 0xFFFFu] & K_RECT)));
+            }
+            unsigned long long total = 0;
+            const unsigned long long before = block_scan_value_u64<NT>(mine, s_wsum64, &total);
+            constexpr unsigned long long F = (1ull << 21) - 1ull;
+            const uint32_t t0 = (uint32_t)(total & F), t1 = (uint32_t)((total >> 21) & F);
+            uint32_t at[3] = {(uint32_t)(before & F), t0 + (uint32_t)((before >> 21) & F),
+                              t0 + t1 + (uint32_t)(before >> 42)};
+            for (uint32_t q = s0; q < s1; ++q) {
+                const uint32_t key = cand[q];
+                const uint32_t t = (s.kind[key >> 16] & K_RECT) + (s.kind[key & 0xFFFFu] & K_RECT);
+                const uint32_t slot = t == 0 ? at[0]++ : (t == 1 ? at[1]++ : at[2]++);
+                pairs[slot] = key;
+            }
+        }
+        SUBPHASE(17);
     }
-    if (err) set_err(&s_err, err);
-    if (__syncthreads_or(err != 0)) goto fail;
+    __syncthreads();
 
     PHASE(1);
     // ---------------- narrowphase (collision.zig:299-320, lib.zig:284-294) ----------------
     {
         const float h = P.dt / (float)P.sub_steps;
         const uint32_t npairs = s_cnt[0];
-        for (uint32_t pi = tid; pi < npairs; pi += NT) {
-            const uint32_t key = pairs[pi];
-            const uint32_t lo = key >> 16, hi = key & 0xFFFFu;
-            const uint32_t o1 = __ldg(P.ids + base + lo) < __ldg(P.ids + base + hi) ? lo : hi;
-            const uint32_t o2 = o1 == lo ? hi : lo;
-            Geo g1, g2;
-            geo_make(g1, f2{s.px[o1], s.py[o1]}, s.kind[o1] & K_RECT, __ldg(pr + (size_t)P_DIM0 * NB + base + o1),
-                     __ldg(pr + (size_t)P_DIM1 * NB + base + o1), s.cs[o1], s.sn[o1]);
-            geo_make(g2, f2{s.px[o2], s.py[o2]}, s.kind[o2] & K_RECT, __ldg(pr + (size_t)P_DIM0 * NB + base + o2),
-                     __ldg(pr + (size_t)P_DIM1 * NB + base + o2), s.cs[o2], s.sn[o2]);
+        const uint32_t lane = tid & 31u;
+        // every thread runs the same number of rounds, so whole warps claim
+        // manifold and point slots together (one atomic per warp and round)
+        for (uint32_t b0 = 0; b0 < npairs; b0 += NT) {
+            const uint32_t pi = b0 + tid;
+            bool hit = false;
+            int npt = 0;
+            uint32_t ref = 0, inc = 0;
             SatState sat;
-            if (!perform_narrow_sat(g1, g2, sat)) continue;
-            const uint32_t ref = sat.ref_is_first ? o1 : o2, inc = sat.ref_is_first ? o2 : o1;
             NewPoint pts[2];
-            const int npt = sat.ref_is_first ? identify_points(g1, g2, sat.refid, pts)
-                                             : identify_points(g2, g1, sat.refid, pts);
-            const uint32_t m = atomicAdd(&s_cnt[1], 1u);
+            if (pi < npairs) {
+                const uint32_t key = pairs[pi];
+                const uint32_t lo = key >> 16, hi = key & 0xFFFFu;
+                const uint32_t o1 = __ldg(P.ids + base + lo) < __ldg(P.ids + base + hi) ? lo : hi;
+                const uint32_t o2 = o1 == lo ? hi : lo;
+                Geo g1, g2;
+                geo_make(g1, f2{s.px[o1], s.py[o1]}, s.kind[o1] & K_RECT, __ldg(pr + (size_t)P_DIM0 * NB + base + o1),
+                         __ldg(pr + (size_t)P_DIM1 * NB + base + o1), s.cs[o1], s.sn[o1]);
+                geo_make(g2, f2{s.px[o2], s.py[o2]}, s.kind[o2] & K_RECT, __ldg(pr + (size_t)P_DIM0 * NB + base + o2),
+                         __ldg(pr + (size_t)P_DIM1 * NB + base + o2), s.cs[o2], s.sn[o2]);
+                hit = perform_narrow_sat(g1, g2, sat);
+                if (hit) {
+                    ref = sat.ref_is_first ? o1 : o2;
+                    inc = sat.ref_is_first ? o2 : o1;
+                    npt = sat.ref_is_first ? identify_points(g1, g2, sat.refid, pts)
+                                           : identify_points(g2, g1, sat.refid, pts);
+                }
+            }
+            // inclusive warp scan of (manifolds, points) packed 16:16
+            const uint32_t mine = (hit ? 1u : 0u) | ((uint32_t)npt << 16);
+            uint32_t incl = mine;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= (uint32_t)o) incl += y;
+            }
+            uint32_t mbase = 0, pbase = 0;
+            if (lane == 31u && incl) {
+                mbase = atomicAdd(&s_cnt[1], incl & 0xFFFFu);
+                pbase = atomicAdd(&s_cnt[2], incl >> 16);
+            }
+            mbase = __shfl_sync(0xffffffffu, mbase, 31);
+            pbase = __shfl_sync(0xffffffffu, pbase, 31);
+            if (!hit) continue;
+            const uint32_t before = incl - mine;
+            const uint32_t m = mbase + (before & 0xFFFFu);
+            const uint32_t p0 = pbase + (before >> 16);
             if (m >= C.nm) {
                 cap_fail(&err, &s_capbits, CAP_MANIFOLDS);
                 continue;
             }
-            const uint32_t p0 = atomicAdd(&s_cnt[2], (uint32_t)npt);
             if (p0 + npt > C.npt) {
                 cap_fail(&err, &s_capbits, CAP_POINTS);
                 continue;
@@ -535,8 +720,8 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
             const uint32_t x = s.ma[m], y = s.mb[m];
             return (min(x, y) << 16) | max(x, y);
         };
-        if (colour_greedy_sorted<NT>(M, n, contact_ends, contact_mix, contact_tie, s.mcol, skey, cmask,
-                                     [&]() { SUBPHASE(15); })) {
+        if (colour_greedy_sorted<NT>(M, n, contact_ends, contact_mix, contact_tie, s.mcol, skey, cmask, s_ccnt,
+                                     s_wsum, [&]() { SUBPHASE(15); })) {
             if (tid == 0) {
                 s_err = DS_CAPACITY;
                 s_capbits |= CAP_COLOURS;
@@ -571,7 +756,8 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
             };
             auto joint_mix = [&](uint32_t j) { return r2d_colour_mix(j, R2D_COLOUR_JOINT_SALT); };
             auto joint_tie = [&](uint32_t j) { return j; };
-            if (colour_greedy_sorted<NT>(NJ, n, joint_ends, joint_mix, joint_tie, jcol, skey, cmask, [&]() {})) {
+            if (colour_greedy_sorted<NT>(NJ, n, joint_ends, joint_mix, joint_tie, jcol, skey, cmask, s_ccnt, s_wsum,
+                                         [&]() {})) {
                 if (tid == 0) {
                     s_err = DS_CAPACITY;
                     s_capbits |= CAP_COLOURS;
@@ -698,9 +884,16 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
                     }
                     __syncthreads();
                 }
+                // A colour that fits the block twice over takes two lanes per
+                // manifold (one per contact point); a larger one, one lane.
                 for (uint32_t c = 0; c < ncol; ++c) {
                     const uint32_t k0 = coff[c], k1 = coff[c + 1];
-                    for (uint32_t k = k0 + tid; k < k1; k += NT) solve_contact<LEAN>(s, corder[k]);
+                    if (k1 - k0 <= (uint32_t)(NT / 2)) {
+                        const uint32_t k = k0 + ((uint32_t)tid >> 1);
+                        solve_contact_lanes<LEAN>(s, k < k1 ? (uint32_t)corder[k] : 0u, k < k1, (uint32_t)tid & 31u);
+                    } else {
+                        for (uint32_t k = k0 + tid; k < k1; k += NT) solve_contact<LEAN>(s, corder[k]);
+                    }
                     __syncthreads();
                 }
             }

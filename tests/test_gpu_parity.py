@@ -205,3 +205,54 @@ def test_tgs_live_depth_uses_full_layout():
         oc, _ = o.colours()
         assert_manifolds_equal(gk, gd, gc, ok, od, oc)
     assert abs(od[0, 9 + 6]) > 2048
+
+
+def _bucket(x, y, table):
+    """The reference's bucket of cell (x, y) (SpatialHash.zig:78-81): i64
+    wrapping products, xor, as u64, modulo the table size."""
+    m = (1 << 64) - 1
+    return (((x * 92837111) & m) ^ ((y * 689287499) & m)) % table
+
+
+@pytest.mark.parametrize("grid", [False, True])
+def test_pairs_across_cell_boundaries_with_and_without_bucket_collisions(grid):
+    # Disc pairs whose AABBs are 0.005 apart across a 4.0 cell boundary: the
+    # AABB test (margin 0.01) and SAT (margin 0.01) accept them, so the
+    # reference makes a manifold exactly when the two cells' buckets
+    # collide.  Half the pairs sit on rows where they do.  (With an even
+    # table, side-by-side cells never collide -- both hash multipliers are
+    # odd -- so this world uses table_mult 3 and an odd body count.)
+    n_pairs, filler, mult = 10, 5, 3
+    n = 2 * n_pairs + filler
+    table = mult * n
+    r, gap = 0.4, 0.005
+    rows_hit, rows_miss = [], []
+    for yc in range(-300, 300):
+        for k in (1, 2, 3):
+            same = _bucket(k - 1, yc, table) == _bucket(k, yc, table)
+            (rows_hit if same else rows_miss).append((k, yc))
+    picks = rows_hit[:n_pairs // 2] + rows_miss[:n_pairs - n_pairs // 2]
+    assert len(picks) == n_pairs
+    b = scenes._Builder()
+    for k, yc in picks:
+        y = 4.0 * yc + 2.0
+        b.disc(4.0 * k - r - gap / 2, y, r, 0.5)
+        b.disc(4.0 * k + r + gap / 2, y, r, 0.5)
+    for f in range(filler):
+        b.disc(5000.0 + 10.0 * f, 5000.0, r, 0.5)
+    ids, kind, opt = b.arrays()
+    assert len(ids) == n
+    sc = scenes._concat("boundary", [(ids, kind, opt)], [0.0], 1 / 60, 1, 8, 2)
+    w = World.from_scene(sc, debug=True, mult=mult, grid=grid)
+    o = Oracle.from_scene(sc)
+    o.set_hash(4.0, mult)
+    for s in range(2):
+        assert o.process(sc.dt, 1, 8, ORDER_COLOUR) == 0
+        w.process(sc.dt, 1, 8)
+        w.sync()
+        assert_state_equal(w.read_state(), o.state(), f"boundary step {s + 1}")
+        gk, gd, gc = w.manifolds()
+        ok, od = o.manifolds()
+        oc, _ = o.colours()
+        assert_manifolds_equal(gk, gd, gc, ok, od, oc)
+    assert len(ok) == n_pairs // 2  # only the colliding rows pair up
