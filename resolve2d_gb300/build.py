@@ -48,19 +48,27 @@ def _stale(target: Path, deps: list[Path]) -> bool:
     return any(d.stat().st_mtime > t for d in deps)
 
 
-def build_library(force: bool = False, verbose: bool = False) -> Path:
-    """Compile the translation units in parallel and link libr2d_gb300.so."""
+TIMERS_LIB = BUILD / "libr2d_timers.so"
+
+
+def build_library(force: bool = False, verbose: bool = False, timers: bool = False) -> Path:
+    """Compile the translation units in parallel and link libr2d_gb300.so.
+    timers=True builds libr2d_timers.so instead: the same library with the
+    fused kernel's per-phase cycle counters (R2D_PHASE_TIMERS), for
+    resolve2d_gb300.phase_timers."""
     BUILD.mkdir(exist_ok=True)
     deps = _deps()
-    if not force and not _stale(LIB, deps):
-        return LIB
+    lib = TIMERS_LIB if timers else LIB
+    if not force and not _stale(lib, deps):
+        return lib
     cc = nvcc()
     procs = []
     objs = []
+    extra = ["-DR2D_PHASE_TIMERS"] if timers else []
     for src in SOURCES:
-        obj = BUILD / (Path(src).stem + ".o")
+        obj = BUILD / (Path(src).stem + ("_timers.o" if timers else ".o"))
         objs.append(obj)
-        cmd = [cc, *ARCH, *NVCC_FLAGS, "-I", str(INCLUDE), "-c", str(CSRC / src), "-o", str(obj)]
+        cmd = [cc, *ARCH, *NVCC_FLAGS, *extra, "-I", str(INCLUDE), "-c", str(CSRC / src), "-o", str(obj)]
         if verbose:
             print(" ".join(cmd))
         procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))
@@ -68,13 +76,13 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
         out, _ = p.communicate()
         if p.returncode != 0:
             raise RuntimeError(f"nvcc failed ({' '.join(cmd)}):\n{out}")
-    tmp = BUILD / (LIB.name + ".tmp")
+    tmp = BUILD / (lib.name + ".tmp")
     cmd = [cc, *ARCH, "-shared", "-o", str(tmp), *[str(o) for o in objs], "-lcudart"]
     out = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     if out.returncode != 0:
         raise RuntimeError(f"link failed ({' '.join(cmd)}):\n{out.stdout}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 def build_oracle(force: bool = False) -> Path:
