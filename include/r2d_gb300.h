@@ -96,7 +96,13 @@ enum {
     /* Step every world through the grid-wide pipeline that worlds above 520
      * bodies always use (global scratch, one kernel per phase and colour)
      * instead of the fused one-CTA-per-world kernel.  Same results. */
-    R2D_FLAG_GRID_PIPELINE = 2u
+    R2D_FLAG_GRID_PIPELINE = 2u,
+    /* Keep each body's x, y and angle in f64 as well and integrate them in
+     * f64 (x += p * (h / m), angle += L * h / I); the f32 pose the step uses
+     * is that pose rounded.  Momenta, contacts and joints stay f32.  No
+     * counterpart in the reference, which is f32 throughout; it reduces
+     * drift over long horizons (r2d_*_read_positions_f64 reads the pose). */
+    R2D_FLAG_FP64_POSITIONS = 4u
 };
 
 typedef struct r2d_config {
@@ -148,6 +154,10 @@ R2D_API int r2d_solver_set_exclusions(r2d_solver* s, uint32_t n, const uint32_t*
 /* Solver.process (lib.zig:189-251) / solverProcess (wasm_root.zig:39-43). */
 R2D_API int r2d_solver_process(r2d_solver* s, float dt, uint32_t sub_steps, uint32_t collision_iters);
 R2D_API int r2d_solver_sync(r2d_solver* s);
+/* The f64 pose [3][n] (x, y, angle) kept under R2D_FLAG_FP64_POSITIONS;
+ * writing the f32 state restarts it from that state.  No counterpart in the
+ * reference. */
+R2D_API int r2d_solver_read_positions_f64(r2d_solver* s, double* pose);
 /* Debug taps (need R2D_FLAG_DEBUG_TAPS): the last frame's manifolds
  * (Solver.manifolds, lib.zig:137) with their contact colours.  keys [cap][2]
  * are (reference, incident) body indices; data [cap][R2D_MANIFOLD_FLOATS]. */
@@ -177,6 +187,9 @@ R2D_API int r2d_batch_process(r2d_batch* b, float dt, uint32_t sub_steps, uint32
 R2D_API int r2d_batch_sync(r2d_batch* b);
 /* Kernel launches one r2d_batch_process enqueues (one per occupied size class). */
 R2D_API int r2d_batch_launches_per_step(r2d_batch* b, uint32_t* out);
+/* The f64 pose [3][total bodies] under R2D_FLAG_FP64_POSITIONS (see the
+ * solver's). */
+R2D_API int r2d_batch_read_positions_f64(r2d_batch* b, double* pose);
 /* Per-world status of the last synced step (0 or an r2d_status). */
 R2D_API int r2d_batch_world_status(r2d_batch* b, int* status);
 /* Debug taps for world w (need R2D_FLAG_DEBUG_TAPS). */

@@ -120,6 +120,7 @@ struct Engine {
     std::vector<float> state_h;  // last uploaded (for capacity planning)
 
     float* d_state = nullptr;
+    double* d_pos64 = nullptr;  // [3][nbodies] f64 x, y, angle (R2D_FLAG_FP64_POSITIONS)
     float* d_props = nullptr;
     uint8_t* d_kind = nullptr;
     uint32_t* d_ids = nullptr;
@@ -183,7 +184,7 @@ struct Engine {
 
     ~Engine() {
         large.clear();
-        dfree(d_state); dfree(d_props); dfree(d_kind); dfree(d_ids); dfree(d_worlds);
+        dfree(d_state); dfree(d_pos64); dfree(d_props); dfree(d_kind); dfree(d_ids); dfree(d_worlds);
         dfree(d_status); dfree(d_err);
         if (h_err) cudaFreeHost(h_err);
         dfree(d_jtype); dfree(d_jb1); dfree(d_jb2); dfree(d_jprm); dfree(d_excl);
@@ -282,6 +283,10 @@ struct Engine {
         calls.clear();
         pending = false;
         CUDA_TRY(cudaMemcpyAsync(d_state, state_h.data(), sizeof(float) * S_NFIELDS * n, cudaMemcpyHostToDevice, stream));
+        if (fp64_positions()) {
+            CUDA_TRY(dalloc(d_pos64, (size_t)3 * n));
+            CUDA_TRY(upload_pose64(state_h.data()));
+        }
         CUDA_TRY(cudaMemcpyAsync(d_props, props_h.data(), sizeof(float) * P_NFIELDS * n, cudaMemcpyHostToDevice, stream));
         CUDA_TRY(cudaMemcpyAsync(d_kind, kind_h.data(), n, cudaMemcpyHostToDevice, stream));
         CUDA_TRY(cudaMemcpyAsync(d_ids, ids_h.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice, stream));
@@ -293,6 +298,26 @@ struct Engine {
     int write_state(const float* state) {
         if (!d_state) return fail(R2D_ERR_INVALID_ARGUMENT, "no bodies");
         CUDA_TRY(cudaMemcpyAsync(d_state, state, sizeof(float) * S_NFIELDS * nbodies, cudaMemcpyHostToDevice, stream));
+        if (d_pos64) CUDA_TRY(upload_pose64(state));  // the f64 pose restarts from the written f32 one
+        return R2D_OK;
+    }
+
+    bool fp64_positions() const { return (cfg.flags & R2D_FLAG_FP64_POSITIONS) != 0; }
+
+    // d_pos64 = the pose fields of a host f32 state, widened.
+    cudaError_t upload_pose64(const float* state) {
+        std::vector<double> p((size_t)3 * nbodies);
+        for (size_t f = 0; f < 3; ++f)
+            for (size_t i = 0; i < nbodies; ++i) p[f * nbodies + i] = (double)state[f * nbodies + i];
+        cudaError_t e = cudaMemcpyAsync(d_pos64, p.data(), sizeof(double) * p.size(), cudaMemcpyHostToDevice, stream);
+        if (e != cudaSuccess) return e;
+        return cudaStreamSynchronize(stream);  // p is released on return
+    }
+
+    int read_pose64(double* out) {
+        if (!d_pos64) return fail(R2D_ERR_INVALID_ARGUMENT, "FP64 positions are off (R2D_FLAG_FP64_POSITIONS)");
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        CUDA_TRY(cudaMemcpy(out, d_pos64, sizeof(double) * 3 * nbodies, cudaMemcpyDeviceToHost));
         return R2D_OK;
     }
 
@@ -632,6 +657,7 @@ struct Engine {
         in.cell = cell;
         in.table_mult = table_mult;
         in.disc_rot = (d.flags & W_DISC_ROTATION) != 0;
+        in.pos64 = d_pos64;
         return in;
     }
 
@@ -689,6 +715,7 @@ struct Engine {
         P.world_capbits = d_capbits;
         P.call_index = call_index;
         P.timers = d_timers;
+        P.pos64 = d_pos64;
         return P;
     }
 
@@ -1097,6 +1124,11 @@ R2D_API int r2d_solver_get_manifolds(r2d_solver* s, uint32_t cap, uint32_t* keys
     return guarded([&] { return s->eng.get_manifolds(0, cap, keys, data, colours); });
 }
 
+R2D_API int r2d_solver_read_positions_f64(r2d_solver* s, double* pose) {
+    if (!s || !pose) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
+    return guarded([&] { return s->eng.read_pose64(pose); });
+}
+
 R2D_API int r2d_solver_get_joint_colours(r2d_solver* s, uint32_t cap, uint32_t* colours) {
     if (!s || !colours) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
     return guarded([&] { return s->eng.get_joint_colours(0, cap, colours); });
@@ -1152,6 +1184,11 @@ R2D_API int r2d_batch_write_state(r2d_batch* b, const float* state) {
 R2D_API int r2d_batch_read_state(r2d_batch* b, float* state) {
     if (!b || !state) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
     return guarded([&] { return b->eng.read_state(state); });
+}
+
+R2D_API int r2d_batch_read_positions_f64(r2d_batch* b, double* pose) {
+    if (!b || !pose) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
+    return guarded([&] { return b->eng.read_pose64(pose); });
 }
 
 R2D_API int r2d_batch_process(r2d_batch* b, float dt, uint32_t sub_steps, uint32_t collision_iters) {

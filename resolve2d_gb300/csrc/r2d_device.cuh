@@ -365,6 +365,25 @@ R2D_DF int identify_points(const Geo& ref, const Geo& inc, uint32_t refid, NewPo
 }
 
 // A set of colours 0..255 held in eight registers.
+// Integration of a dynamic body's pose in the FP64-positions mode: the
+// f32 step's arithmetic (lib.zig:238-243: pos += momentum * (h / mass),
+// angle += ang_momentum * h / inertia) in double on a double pose kept in
+// HBM (pos64[f * NB + g], f = x, y, angle); the f32 pose becomes its
+// rounding.  Momenta and everything else stay f32.
+R2D_DF void integrate_pose64(double* __restrict__ pos64, size_t NB, uint32_t g, float mx, float my, float L,
+                             float h, float mass, float inertia, float* px, float* py, float* ang) {
+    const double sm = (double)h / (double)mass;
+    const double x = pos64[g] + (double)mx * sm;
+    const double y = pos64[NB + g] + (double)my * sm;
+    const double a = pos64[2 * NB + g] + (double)L * (double)h / (double)inertia;
+    pos64[g] = x;
+    pos64[NB + g] = y;
+    pos64[2 * NB + g] = a;
+    *px = (float)x;
+    *py = (float)y;
+    *ang = (float)a;
+}
+
 struct ColourSet {
     uint32_t w0 = 0u, w1 = 0u, w2 = 0u, w3 = 0u, w4 = 0u, w5 = 0u, w6 = 0u, w7 = 0u;
     R2D_DF void add(uint32_t c) {

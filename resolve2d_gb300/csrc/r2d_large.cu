@@ -423,6 +423,7 @@ struct Phase2 {
     const float* jprm;
     const uint32_t* order;  // constraints of the colour [k0, k1)
     uint32_t k0, k1;
+    double* pos64;          // f64 pose (FP64-positions mode), else null
 
     __device__ float& st(int f, uint32_t i) const { return state[(size_t)f * NB + base + i]; }
     __device__ float pr(int f, uint32_t i) const { return __ldg(props + (size_t)f * NB + base + i); }
@@ -533,10 +534,15 @@ __global__ void lk_integrate(Phase2 A) {
     s.ang_prev[i] = s.ang[i];
     const uint8_t k = s.kind[i];
     if (k & K_STATIC) return;
-    const float sm_ = A.h / s.mass(i);
-    s.px[i] += s.mx[i] * sm_;
-    s.py[i] += s.my[i] * sm_;
-    s.ang[i] += s.L[i] * A.h / s.inertia(i);
+    if (A.pos64) {
+        integrate_pose64(A.pos64, A.NB, A.base + i, s.mx[i], s.my[i], s.L[i], A.h, s.mass(i), s.inertia(i), &s.px[i],
+                         &s.py[i], &s.ang[i]);
+    } else {
+        const float sm_ = A.h / s.mass(i);
+        s.px[i] += s.mx[i] * sm_;
+        s.py[i] += s.my[i] * sm_;
+        s.ang[i] += s.L[i] * A.h / s.inertia(i);
+    }
     s.tq[i] = 0.f;
     if (!A.last && ((k & K_RECT) || A.disc_rot)) {
         float c, sn;
@@ -877,6 +883,7 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
     S.ngrav = in.ngrav;
     for (int k = 0; k < MAX_GRAVITY; ++k) S.g[k] = in.g[k];
     S.jtype = in.jtype; S.jb1 = in.jb1; S.jb2 = in.jb2; S.jprm = in.jprm;
+    S.pos64 = in.pos64;
     for (uint32_t sub = 0; sub < sub_steps; ++sub) {
         S.first = sub == 0;
         S.last = sub + 1 == sub_steps;

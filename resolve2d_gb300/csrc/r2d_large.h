@@ -34,6 +34,7 @@ struct LargeInputs {
     float cell;
     uint32_t table_mult;
     bool disc_rot;         // some joint reads disc orientations
+    double* pos64;         // [3][NB] f64 pose (FP64-positions mode), else null
 };
 
 class LargeWorld {

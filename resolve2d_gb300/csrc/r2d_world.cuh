@@ -191,6 +191,7 @@ struct StepParams {
     int* error_count;
     uint32_t call_index;         // position of this launch in the calls since the last sync
     unsigned long long* timers;  // [nworlds][PHASE_SLOTS] when built with R2D_PHASE_TIMERS
+    double* pos64;               // [3][nbodies] x, y, angle in f64 (FP64-positions mode), else null
     float dt;
     uint32_t sub_steps, iters;
     float cell;

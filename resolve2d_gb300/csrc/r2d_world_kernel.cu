@@ -902,10 +902,15 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
                 if (Lo.has_prev) s.ang_prev[i] = s.ang[i];
                 const uint8_t k = s.kind[i];
                 if (k & K_STATIC) continue;
-                const float sm_ = h / s.mass(i);
-                s.px[i] += s.mx[i] * sm_;
-                s.py[i] += s.my[i] * sm_;
-                s.ang[i] += s.L[i] * h / s.inertia(i);
+                if (P.pos64) {
+                    integrate_pose64(P.pos64, NB, base + i, s.mx[i], s.my[i], s.L[i], h, s.mass(i), s.inertia(i),
+                                     &s.px[i], &s.py[i], &s.ang[i]);
+                } else {
+                    const float sm_ = h / s.mass(i);
+                    s.px[i] += s.mx[i] * sm_;
+                    s.py[i] += s.my[i] * sm_;
+                    s.ang[i] += s.L[i] * h / s.inertia(i);
+                }
                 s.tq[i] = 0.f;
                 if (!last && ((k & K_RECT) || disc_rot)) {
                     float c, sn;

@@ -13,12 +13,13 @@ from .scenes import NSTATE, Scene, derive_props_state
 
 
 def _config(cell: float, mult: int, debug: bool, stream, capacity_scale: float = 0.0,
-            grid: bool = False) -> N.Config:
+            grid: bool = False, fp64_positions: bool = False) -> N.Config:
     cfg = N.Config()
     cfg.capacity_scale = float(capacity_scale)
     cfg.spatialhash_cell_width = float(cell)
     cfg.spatialhash_table_size_mult = int(mult)
-    cfg.flags = (N.FLAG_DEBUG_TAPS if debug else 0) | (N.FLAG_GRID_PIPELINE if grid else 0)
+    cfg.flags = ((N.FLAG_DEBUG_TAPS if debug else 0) | (N.FLAG_GRID_PIPELINE if grid else 0)
+                 | (N.FLAG_FP64_POSITIONS if fp64_positions else 0))
     cfg.stream = int(stream) if stream else None
     return cfg
 
@@ -28,10 +29,10 @@ class World:
     520 bodies, the grid-wide pipeline above that (or always, ``grid=True``)."""
 
     def __init__(self, cell: float = 0.0, mult: int = 0, debug: bool = False, stream=None, capacity_scale: float = 0.0,
-                 grid: bool = False):
+                 grid: bool = False, fp64_positions: bool = False):
         self._lib = N.load()
         self._h = C.c_void_p()
-        cfg = _config(cell, mult, debug, stream, capacity_scale, grid)
+        cfg = _config(cell, mult, debug, stream, capacity_scale, grid, fp64_positions)
         N.check(self._lib.r2d_solver_create(C.byref(cfg), C.byref(self._h)), "r2d_solver_create")
         self.n = 0
 
@@ -106,6 +107,12 @@ class World:
                                                    N.ptr(c, C.c_uint32)), "r2d_solver_get_manifolds")
         return k, d, c
 
+    def read_positions_f64(self) -> np.ndarray:
+        out = np.empty((3, self.n), np.float64)
+        N.check(self._lib.r2d_solver_read_positions_f64(self._h, out.ctypes.data_as(C.POINTER(C.c_double))),
+                "r2d_solver_read_positions_f64")
+        return out
+
     def joint_colours(self, nj: int):
         c = np.zeros(nj, np.uint32)
         N.check(self._lib.r2d_solver_get_joint_colours(self._h, nj, N.ptr(c, C.c_uint32)), "r2d_solver_get_joint_colours")
@@ -116,10 +123,10 @@ class Batch:
     """Many independent worlds stepped together (r2d_batch_* entry points)."""
 
     def __init__(self, cell: float = 0.0, mult: int = 0, debug: bool = False, stream=None, capacity_scale: float = 0.0,
-                 grid: bool = False):
+                 grid: bool = False, fp64_positions: bool = False):
         self._lib = N.load()
         self._h = C.c_void_p()
-        cfg = _config(cell, mult, debug, stream, capacity_scale, grid)
+        cfg = _config(cell, mult, debug, stream, capacity_scale, grid, fp64_positions)
         N.check(self._lib.r2d_batch_create(C.byref(cfg), C.byref(self._h)), "r2d_batch_create")
         self.n = 0
         self.nworlds = 0
@@ -168,6 +175,12 @@ class Batch:
 
     def sync(self):
         N.check(self._lib.r2d_batch_sync(self._h), "r2d_batch_sync")
+
+    def read_positions_f64(self) -> np.ndarray:
+        out = np.empty((3, self.n), np.float64)
+        N.check(self._lib.r2d_batch_read_positions_f64(self._h, out.ctypes.data_as(C.POINTER(C.c_double))),
+                "r2d_batch_read_positions_f64")
+        return out
 
     def launches_per_step(self) -> int:
         out = C.c_uint32()

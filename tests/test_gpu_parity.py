@@ -256,3 +256,43 @@ def test_pairs_across_cell_boundaries_with_and_without_bucket_collisions(grid):
         oc, _ = o.colours()
         assert_manifolds_equal(gk, gd, gc, ok, od, oc)
     assert len(ok) == n_pairs // 2  # only the colliding rows pair up
+
+
+@pytest.mark.parametrize("grid", [False, True])
+def test_fp64_positions_integrate_in_double(grid):
+    # Bodies in free flight (far apart, no contacts), under gravity, with
+    # spin: momenta evolve in f32 exactly as in the f32 step; the pose is
+    # integrated in double, x += p * (h / m), angle += L * h / I
+    # (R2D_FLAG_FP64_POSITIONS).  Restated here in numpy float64.
+    b = scenes._Builder()
+    for k in range(6):
+        b.disc(50.0 * k, 10.0 + k, 0.3 + 0.05 * k, 0.5, vx=0.37 * k, vy=1.3, omega=0.7 * k)
+        b.rect(50.0 * k + 20.0, -5.0, 0.5 + 0.1 * k, 0.4, 0.5, vx=-0.21, omega=-1.1 + 0.3 * k)
+    ids, kind, opt = b.arrays()
+    g, dt, steps = 9.81, 1 / 60, 40
+    sc = scenes._concat("flight", [(ids, kind, opt)], [g], dt, 1, 8, steps)
+    w = World.from_scene(sc, fp64_positions=True, grid=grid)
+    st0 = w.read_state()
+    pose0 = w.read_positions_f64()
+    np.testing.assert_array_equal(pose0, st0[:3].astype(np.float64))
+    props, _ = scenes.derive_props_state(sc.kind, sc.opt)
+    m, inertia = props[0].astype(np.float32), props[1].astype(np.float32)
+    f32 = np.float32
+    h = f32(f32(dt) / f32(1))
+    my = st0[4].copy()
+    mx, L = st0[3].copy(), st0[5].copy()
+    x, y, a = pose0[0].copy(), pose0[1].copy(), pose0[2].copy()
+    for _ in range(steps):
+        fy = f32(0.0) + (f32(-g) * m)  # DownwardsGravity.apply on a zero force
+        my = (my + fy * h).astype(np.float32)
+        sm = np.float64(h) / m.astype(np.float64)
+        x = x + mx.astype(np.float64) * sm
+        y = y + my.astype(np.float64) * sm
+        a = a + L.astype(np.float64) * np.float64(h) / inertia.astype(np.float64)
+        w.process(dt, 1, 8)
+    w.sync()
+    pose = w.read_positions_f64()
+    np.testing.assert_array_equal(pose, np.stack([x, y, a]))
+    st = w.read_state()
+    np.testing.assert_array_equal(st[:3], pose.astype(np.float32))
+    np.testing.assert_array_equal(st[4], my)
