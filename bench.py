@@ -10,9 +10,10 @@ Solver.process-equivalent pass over all 4,096 worlds.
 value      body-steps/s with the state resident in HBM, CUDA events around
            each step on the library's stream, L2 flushed (256 MiB write)
            between steps outside the timed events.
-e2e        the same metric through the C ABI with host buffers: every step
-           writes the full state from pinned host memory, steps, and reads it
-           back (r2d_batch_write_state / process / read_state).
+e2e        the same metric through the C ABI with pinned host buffers: every
+           step writes its inputs (force and torque rows), steps, and reads
+           its result (pose and momenta rows); the full-state round trip is
+           reported beside it.
 roofline   algorithmic HBM bytes of the world-step kernel per step
            (117 B per body-step: 77 B read, 40 B written) over its measured
            time, against the measured copy bandwidth.  The unit is one step's
@@ -279,22 +280,40 @@ def main():
     value = nb * args.steps * world / dev_s
     launches = batch.launches_per_step() * args.steps
 
-    # end to end through the C ABI with pinned host buffers
-    host = torch.empty((13, nb), dtype=torch.float32).pin_memory()
-    host_np = host.numpy()
-    host_np[...] = settled
-    batch.write_state(host_np)
-    batch.sync()
+    # End to end through the C ABI with pinned host buffers.  Each step
+    # writes its inputs, the force and torque rows (12 B/body), and reads its
+    # result, the pose and momenta rows (24 B/body), as a frame loop does with
+    # r2d_batch_write_state_fields / process / read_state_fields; the whole
+    # state both ways (52 B/body each) is timed beside it.
     e2e_steps = max(3, min(args.steps, 10))
-    torch.cuda.synchronize()
-    t1 = time.perf_counter()
-    for _ in range(e2e_steps):
-        batch.write_state(host_np)
+
+    def timed_e2e(step_fn):
+        batch.write_state(settled)
+        batch.sync()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        for _ in range(e2e_steps):
+            step_fn()
+        batch.sync()
+        return nb * e2e_steps / (time.perf_counter() - t1)
+
+    forces_in = torch.zeros((3, nb), dtype=torch.float32).pin_memory().numpy()
+    pose_out = torch.empty((6, nb), dtype=torch.float32).pin_memory().numpy()
+    state_io = torch.empty((13, nb), dtype=torch.float32).pin_memory().numpy()
+    state_io[...] = settled
+
+    def fields_step():
+        batch.write_fields(6, forces_in)
         batch.process(sc.dt, sc.sub_steps, sc.iters)
-        batch.read_state(host_np)
-    batch.sync()
-    e2e_s = time.perf_counter() - t1
-    e2e_v = nb * e2e_steps / e2e_s
+        batch.read_fields(0, 6, pose_out)
+
+    def full_step():
+        batch.write_state(state_io)
+        batch.process(sc.dt, sc.sub_steps, sc.iters)
+        batch.read_state(state_io)
+
+    e2e_v = timed_e2e(fields_step)
+    e2e_full = timed_e2e(full_step)
 
     # plain path: the same worlds, one world per launch
     plain = None
@@ -332,7 +351,9 @@ def main():
                    "parallelism": f"replicas x{world}"},
         "gpu_launches": launches,
         "wall_s_timed_loop": wall,
-        "e2e": {"value": e2e_v, "unit": "body-steps/s", "h2d_bytes_per_step": 52 * nb, "d2h_bytes_per_step": 52 * nb},
+        "e2e": {"value": e2e_v, "unit": "body-steps/s", "h2d_bytes_per_step": 12 * nb, "d2h_bytes_per_step": 24 * nb,
+                "inputs": "force and torque rows (pinned)", "results": "pose and momenta rows (pinned)",
+                "full_state": {"value": e2e_full, "h2d_bytes_per_step": 52 * nb, "d2h_bytes_per_step": 52 * nb}},
         "plain_one_world_per_launch": {"value": plain, "unit": "body-steps/s", "worlds": args.plain_worlds,
                                        "batched_over_plain": (value / world) / plain if plain else None},
         "roofline": {"bound": "hbm", "kernel": "world_step_kernel (the size-class launches of one step)",

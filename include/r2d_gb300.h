@@ -154,6 +154,14 @@ R2D_API int r2d_solver_set_exclusions(r2d_solver* s, uint32_t n, const uint32_t*
 /* Solver.process (lib.zig:189-251) / solverProcess (wasm_root.zig:39-43). */
 R2D_API int r2d_solver_process(r2d_solver* s, float dt, uint32_t sub_steps, uint32_t collision_iters);
 R2D_API int r2d_solver_sync(r2d_solver* s);
+/* Bulk get/set of part of the state: rows [first, first + count) of the
+ * field-major state (each row n floats), one contiguous copy.  The batched
+ * form of the WASM exports' per-field body getters and setters
+ * (src/wasm_root.zig:88-251), e.g. forces (R2D_S_FORCE_X, 3) in before a
+ * step and pose and momenta (R2D_S_POS_X, 6) out after it.  Reading waits for
+ * the step. */
+R2D_API int r2d_solver_write_state_fields(r2d_solver* s, uint32_t first, uint32_t count, const float* rows);
+R2D_API int r2d_solver_read_state_fields(r2d_solver* s, uint32_t first, uint32_t count, float* rows);
 /* The f64 pose [3][n] (x, y, angle) kept under R2D_FLAG_FP64_POSITIONS;
  * writing the f32 state restarts it from that state.  No counterpart in the
  * reference. */
@@ -187,6 +195,10 @@ R2D_API int r2d_batch_process(r2d_batch* b, float dt, uint32_t sub_steps, uint32
 R2D_API int r2d_batch_sync(r2d_batch* b);
 /* Kernel launches one r2d_batch_process enqueues (one per occupied size class). */
 R2D_API int r2d_batch_launches_per_step(r2d_batch* b, uint32_t* out);
+/* Rows [first, first + count) of the state over all bodies (see the
+ * solver's). */
+R2D_API int r2d_batch_write_state_fields(r2d_batch* b, uint32_t first, uint32_t count, const float* rows);
+R2D_API int r2d_batch_read_state_fields(r2d_batch* b, uint32_t first, uint32_t count, float* rows);
 /* The f64 pose [3][total bodies] under R2D_FLAG_FP64_POSITIONS (see the
  * solver's). */
 R2D_API int r2d_batch_read_positions_f64(r2d_batch* b, double* pose);

@@ -85,6 +85,10 @@ SIGNATURES = {
     "r2d_batch_world_status": ([_P, _i32p], C.c_int),
     "r2d_batch_num_manifolds": ([_P, C.c_uint32, _u32p], C.c_int),
     "r2d_batch_get_manifolds": ([_P, C.c_uint32, C.c_uint32, _u32p, _f32p, _u32p], C.c_int),
+    "r2d_solver_write_state_fields": ([_P, C.c_uint32, C.c_uint32, _f32p], C.c_int),
+    "r2d_solver_read_state_fields": ([_P, C.c_uint32, C.c_uint32, _f32p], C.c_int),
+    "r2d_batch_write_state_fields": ([_P, C.c_uint32, C.c_uint32, _f32p], C.c_int),
+    "r2d_batch_read_state_fields": ([_P, C.c_uint32, C.c_uint32, _f32p], C.c_int),
     "r2d_solver_read_positions_f64": ([_P, C.POINTER(C.c_double)], C.c_int),
     "r2d_batch_read_positions_f64": ([_P, C.POINTER(C.c_double)], C.c_int),
     "r2d_world_step_static": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, _f32p, C.c_uint32,

@@ -31,6 +31,8 @@
 namespace r2d {
 cudaError_t launch_world_step(const StepParams& P, const Caps& C, int threads, const LayoutOpts& opts,
                               cudaStream_t stream);
+cudaError_t allow_world_step_smem(int bytes);
+cudaError_t launch_count_call(uint32_t* counter, cudaStream_t stream);
 }  // namespace r2d
 
 using namespace r2d;
@@ -182,8 +184,20 @@ struct Engine {
     cudaStream_t lstream = nullptr;
     cudaEvent_t ev_ljoin = nullptr;
 
+    // The fused step of one call, captured once as a CUDA graph and replayed
+    // while the plan and (dt, sub_steps, iters) stay the same.  Calls count
+    // themselves on the device (d_call), so the graph needs no per-call
+    // parameters.
+    uint32_t* d_call = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    float g_dt = 0.f;
+    uint32_t g_sub = 0, g_iters = 0;
+    bool use_graph = true;
+
     ~Engine() {
         large.clear();
+        if (gexec) cudaGraphExecDestroy(gexec);
+        dfree(d_call);
         dfree(d_state); dfree(d_pos64); dfree(d_props); dfree(d_kind); dfree(d_ids); dfree(d_worlds);
         dfree(d_status); dfree(d_err);
         if (h_err) cudaFreeHost(h_err);
@@ -224,6 +238,11 @@ struct Engine {
         CUDA_TRY(cudaEventCreateWithFlags(&ev_ljoin, cudaEventDisableTiming));
         const char* v = getenv("R2D_VERBOSE");
         verbose = v && v[0] && v[0] != '0';
+        const char* ng = getenv("R2D_NO_GRAPH");
+        use_graph = !(ng && ng[0] && ng[0] != '0');
+        CUDA_TRY(dalloc(d_call, 1));
+        CUDA_TRY(cudaMemsetAsync(d_call, 0, sizeof(uint32_t), stream));
+        CUDA_TRY(allow_world_step_smem(smem_optin()));
         return R2D_OK;
     }
 
@@ -299,6 +318,37 @@ struct Engine {
         if (!d_state) return fail(R2D_ERR_INVALID_ARGUMENT, "no bodies");
         CUDA_TRY(cudaMemcpyAsync(d_state, state, sizeof(float) * S_NFIELDS * nbodies, cudaMemcpyHostToDevice, stream));
         if (d_pos64) CUDA_TRY(upload_pose64(state));  // the f64 pose restarts from the written f32 one
+        return R2D_OK;
+    }
+
+    // Rows [first, first + count) of the field-major state: one contiguous
+    // copy each way.
+    int write_fields(uint32_t first, uint32_t count, const float* rows) {
+        if (!d_state) return fail(R2D_ERR_INVALID_ARGUMENT, "no bodies");
+        if (first > (uint32_t)S_NFIELDS || count > (uint32_t)S_NFIELDS - first)
+            return fail(R2D_ERR_INVALID_ARGUMENT, "field range beyond the 13 state fields");
+        if (!count || !nbodies) return R2D_OK;
+        CUDA_TRY(cudaMemcpyAsync(d_state + (size_t)first * nbodies, rows, sizeof(float) * count * nbodies,
+                                 cudaMemcpyHostToDevice, stream));
+        if (d_pos64 && first < 3) {  // the f64 pose restarts from the written f32 pose rows
+            const uint32_t end = std::min(3u, first + count);
+            std::vector<double> p((size_t)(end - first) * nbodies);
+            for (size_t k = 0; k < p.size(); ++k) p[k] = (double)rows[k];
+            CUDA_TRY(cudaMemcpyAsync(d_pos64 + (size_t)first * nbodies, p.data(), sizeof(double) * p.size(),
+                                     cudaMemcpyHostToDevice, stream));
+            CUDA_TRY(cudaStreamSynchronize(stream));
+        }
+        return R2D_OK;
+    }
+
+    int read_fields(uint32_t first, uint32_t count, float* rows) {
+        if (!d_state) return fail(R2D_ERR_INVALID_ARGUMENT, "no bodies");
+        if (first > (uint32_t)S_NFIELDS || count > (uint32_t)S_NFIELDS - first)
+            return fail(R2D_ERR_INVALID_ARGUMENT, "field range beyond the 13 state fields");
+        if (!count || !nbodies) return R2D_OK;
+        CUDA_TRY(cudaMemcpyAsync(rows, d_state + (size_t)first * nbodies, sizeof(float) * count * nbodies,
+                                 cudaMemcpyDeviceToHost, stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
         return R2D_OK;
     }
 
@@ -457,12 +507,16 @@ struct Engine {
         return LayoutOpts{lean, debug, multi_substep || debug, debug};
     }
 
-    int smem_limit() const {
+    // Shared memory a CTA may have (opt-in maximum) ...
+    int smem_optin() const {
         int dev = 0, v = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
         return v;
     }
+    // ... and the part a class's layout may take: the fused kernel's own
+    // static shared memory (under 2 KB) comes off the top.
+    int smem_limit() const { return smem_optin() - 2048; }
 
     KClass* class_of(uint32_t w) {
         for (auto& c : classes)
@@ -470,7 +524,13 @@ struct Engine {
         return nullptr;
     }
 
+    void drop_graph() {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        gexec = nullptr;
+    }
+
     int plan() {
+        drop_graph();
         for (auto& c : classes) dfree(c.d_list);
         classes.clear();
         // size classes by body count: bounds in bodies
@@ -596,10 +656,55 @@ struct Engine {
             if (st) return st;
         }
         if (!pending) CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), stream));
-        StepParams P = params(dt, sub_steps, iters, (uint32_t)calls.size());
         calls.push_back(CallRec{dt, sub_steps, iters});
+        pending = true;
+        if (large_list.empty() && use_graph) {
+            // the fused step alone: replay (or first capture) the graph
+            if (!gexec || g_dt != dt || g_sub != sub_steps || g_iters != iters) {
+                drop_graph();
+                cudaGraph_t graph = nullptr;
+                CUDA_TRY(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+                const int st = enqueue_fused(dt, sub_steps, iters);
+                const cudaError_t ec = cudaStreamEndCapture(stream, &graph);
+                if (st) {
+                    if (graph) cudaGraphDestroy(graph);
+                    return st;
+                }
+                CUDA_TRY(ec);
+                const cudaError_t ei = cudaGraphInstantiate(&gexec, graph, 0);
+                cudaGraphDestroy(graph);
+                CUDA_TRY(ei);
+                g_dt = dt;
+                g_sub = sub_steps;
+                g_iters = iters;
+            }
+            CUDA_TRY(cudaGraphLaunch(gexec, stream));
+            return R2D_OK;
+        }
+        if (int st = enqueue_fused(dt, sub_steps, iters)) return st;
+        if (!large_list.empty()) {
+            // the fused launches above are queued: the large worlds' host-driven
+            // pipelines run while they execute
+            CUDA_TRY(cudaStreamWaitEvent(lstream, ev_fork, 0));
+            for (uint32_t w : large_list) {
+                int st = step_large(w, dt, sub_steps, iters, lstream);
+                if (st) return st;
+            }
+            CUDA_TRY(cudaEventRecord(ev_ljoin, lstream));
+            CUDA_TRY(cudaStreamWaitEvent(stream, ev_ljoin, 0));
+        }
+        return R2D_OK;
+    }
+
+    // One call of the fused kernel classes, forked from `stream` onto the
+    // auxiliary streams and joined back; ev_fork also marks the point the
+    // grid pipeline's stream waits for.
+    int enqueue_fused(float dt, uint32_t sub_steps, uint32_t iters) {
+        StepParams P = params(dt, sub_steps, iters, 0u);
+        P.call_counter = d_call;
+        CUDA_TRY(launch_count_call(d_call, stream));
         const int nused = (int)std::min<size_t>(classes.size(), (size_t)NAUX);
-        if (nused > 1 || !large_list.empty()) CUDA_TRY(cudaEventRecord(ev_fork, stream));
+        CUDA_TRY(cudaEventRecord(ev_fork, stream));
         if (classes.size() == 1) {
             P.world_list = classes[0].d_list;
             P.nlist = (uint32_t)classes[0].worlds.size();
@@ -619,18 +724,6 @@ struct Engine {
                 CUDA_TRY(cudaEventRecord(ev_join[a], aux[a]));
                 CUDA_TRY(cudaStreamWaitEvent(stream, ev_join[a], 0));
             }
-        }
-        pending = true;
-        if (!large_list.empty()) {
-            // the fused launches above are queued: the large worlds' host-driven
-            // pipelines run while they execute
-            CUDA_TRY(cudaStreamWaitEvent(lstream, ev_fork, 0));
-            for (uint32_t w : large_list) {
-                int st = step_large(w, dt, sub_steps, iters, lstream);
-                if (st) return st;
-            }
-            CUDA_TRY(cudaEventRecord(ev_ljoin, lstream));
-            CUDA_TRY(cudaStreamWaitEvent(stream, ev_ljoin, 0));
         }
         return R2D_OK;
     }
@@ -731,6 +824,7 @@ struct Engine {
         CUDA_TRY(cudaMemcpy(h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost));
         if (*h_err == 0) {
             calls.clear();
+            CUDA_TRY(cudaMemsetAsync(d_call, 0, sizeof(uint32_t), stream));
             if (lerr != R2D_OK) return fail(lerr, lmsg);
             return R2D_OK;
         }
@@ -754,6 +848,7 @@ struct Engine {
             }
         }
         calls.clear();
+        CUDA_TRY(cudaMemsetAsync(d_call, 0, sizeof(uint32_t), stream));
         plan_dirty = true;  // boosted worlds move to larger classes from the next call
         if (first_err != R2D_OK) return fail(first_err, first_msg);
         if (lerr != R2D_OK) return fail(lerr, lmsg);
@@ -1124,6 +1219,16 @@ R2D_API int r2d_solver_get_manifolds(r2d_solver* s, uint32_t cap, uint32_t* keys
     return guarded([&] { return s->eng.get_manifolds(0, cap, keys, data, colours); });
 }
 
+R2D_API int r2d_solver_write_state_fields(r2d_solver* s, uint32_t first, uint32_t count, const float* rows) {
+    if (!s || (count && !rows)) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
+    return guarded([&] { return s->eng.write_fields(first, count, rows); });
+}
+
+R2D_API int r2d_solver_read_state_fields(r2d_solver* s, uint32_t first, uint32_t count, float* rows) {
+    if (!s || (count && !rows)) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
+    return guarded([&] { return s->eng.read_fields(first, count, rows); });
+}
+
 R2D_API int r2d_solver_read_positions_f64(r2d_solver* s, double* pose) {
     if (!s || !pose) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
     return guarded([&] { return s->eng.read_pose64(pose); });
@@ -1184,6 +1289,16 @@ R2D_API int r2d_batch_write_state(r2d_batch* b, const float* state) {
 R2D_API int r2d_batch_read_state(r2d_batch* b, float* state) {
     if (!b || !state) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
     return guarded([&] { return b->eng.read_state(state); });
+}
+
+R2D_API int r2d_batch_write_state_fields(r2d_batch* b, uint32_t first, uint32_t count, const float* rows) {
+    if (!b || (count && !rows)) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
+    return guarded([&] { return b->eng.write_fields(first, count, rows); });
+}
+
+R2D_API int r2d_batch_read_state_fields(r2d_batch* b, uint32_t first, uint32_t count, float* rows) {
+    if (!b || (count && !rows)) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
+    return guarded([&] { return b->eng.read_fields(first, count, rows); });
 }
 
 R2D_API int r2d_batch_read_positions_f64(r2d_batch* b, double* pose) {

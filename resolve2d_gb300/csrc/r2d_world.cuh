@@ -189,7 +189,8 @@ struct StepParams {
     uint32_t* world_fail_call;   // [nworlds] first call a world failed in; ~0u = healthy
     uint32_t* world_capbits;     // [nworlds] CAP_* bits of the buffers that overflowed
     int* error_count;
-    uint32_t call_index;         // position of this launch in the calls since the last sync
+    uint32_t call_index;         // position of this launch in the calls since the last sync ...
+    const uint32_t* call_counter;  // ... or, when set, *call_counter - 1 (bumped on the device per call)
     unsigned long long* timers;  // [nworlds][PHASE_SLOTS] when built with R2D_PHASE_TIMERS
     double* pos64;               // [3][nbodies] x, y, angle in f64 (FP64-positions mode), else null
     float dt;

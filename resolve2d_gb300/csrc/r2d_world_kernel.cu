@@ -301,7 +301,7 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
         if (tid == 0) {
             P.world_status[w] = DS_CAPACITY;
             P.world_capbits[w] = (n > C.nb || T > C.nt || n > 65535u ? CAP_BODIES : 0u) | (wd.nj > C.nj ? CAP_JOINTS : 0u);
-            P.world_fail_call[w] = P.call_index;
+            P.world_fail_call[w] = P.call_counter ? *P.call_counter - 1u : P.call_index;
             atomicAdd(P.error_count, 1);
         }
         return;
@@ -1000,7 +1000,7 @@ fail:
     if (tid == 0) {
         P.world_status[w] = s_err ? s_err : DS_CAPACITY;
         P.world_capbits[w] = s_capbits;
-        P.world_fail_call[w] = P.call_index;
+        P.world_fail_call[w] = P.call_counter ? *P.call_counter - 1u : P.call_index;
         atomicAdd(P.error_count, 1);
     }
 #undef SMF
@@ -1010,17 +1010,45 @@ fail:
 #undef SMI32
 }
 
+// One call of the step begins by counting itself (StepParams::call_counter).
+__global__ void count_call_kernel(uint32_t* counter) { *counter += 1u; }
+
 // ---------------------------------------------------------------------------
 // host-side launch helpers
 // ---------------------------------------------------------------------------
 template <int NT, bool LEAN>
 cudaError_t launch_world_step_nt(const StepParams& P, const Caps& C, const LayoutOpts& opts, cudaStream_t stream) {
     const Layout L = make_layout(C, opts);
-    cudaError_t e = cudaFuncSetAttribute(world_step_kernel<NT, LEAN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)L.total);
-    if (e != cudaSuccess) return e;
     if (P.nlist == 0) return cudaSuccess;
     world_step_kernel<NT, LEAN><<<P.nlist, NT, L.total, stream>>>(P, C, L);
+    return cudaGetLastError();
+}
+
+template <int NT, bool LEAN>
+cudaError_t allow_smem_nt(int bytes) {
+    cudaFuncAttributes fa;
+    const cudaError_t e = cudaFuncGetAttributes(&fa, world_step_kernel<NT, LEAN>);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(world_step_kernel<NT, LEAN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                bytes - (int)fa.sharedSizeBytes);
+}
+
+// Lets every instantiation use all the shared memory a CTA may have (`bytes`,
+// static included) as dynamic shared memory; set once, before any launch,
+// so that launches (and graph capture) set nothing.
+cudaError_t allow_world_step_smem(int bytes) {
+    const cudaError_t es[] = {allow_smem_nt<32, true>(bytes),  allow_smem_nt<32, false>(bytes),
+                              allow_smem_nt<64, true>(bytes),  allow_smem_nt<64, false>(bytes),
+                              allow_smem_nt<128, true>(bytes), allow_smem_nt<128, false>(bytes),
+                              allow_smem_nt<256, true>(bytes), allow_smem_nt<256, false>(bytes),
+                              allow_smem_nt<512, true>(bytes), allow_smem_nt<512, false>(bytes)};
+    for (cudaError_t e : es)
+        if (e != cudaSuccess) return e;
+    return cudaSuccess;
+}
+
+cudaError_t launch_count_call(uint32_t* counter, cudaStream_t stream) {
+    count_call_kernel<<<1, 1, 0, stream>>>(counter);
     return cudaGetLastError();
 }
 

@@ -107,6 +107,19 @@ class World:
                                                    N.ptr(c, C.c_uint32)), "r2d_solver_get_manifolds")
         return k, d, c
 
+    def write_fields(self, first: int, rows):
+        """State rows [first, first + len(rows)) (field-major)."""
+        rows = N.f32(rows)
+        N.check(self._lib.r2d_solver_write_state_fields(self._h, first, rows.shape[0], N.ptr(rows, C.c_float)),
+                "r2d_solver_write_state_fields")
+
+    def read_fields(self, first: int, count: int, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty((count, self.n), np.float32)
+        N.check(self._lib.r2d_solver_read_state_fields(self._h, first, count, N.ptr(out, C.c_float)),
+                "r2d_solver_read_state_fields")
+        return out
+
     def read_positions_f64(self) -> np.ndarray:
         out = np.empty((3, self.n), np.float64)
         N.check(self._lib.r2d_solver_read_positions_f64(self._h, out.ctypes.data_as(C.POINTER(C.c_double))),
@@ -175,6 +188,19 @@ class Batch:
 
     def sync(self):
         N.check(self._lib.r2d_batch_sync(self._h), "r2d_batch_sync")
+
+    def write_fields(self, first: int, rows):
+        """State rows [first, first + len(rows)) over all bodies (field-major)."""
+        rows = N.f32(rows)
+        N.check(self._lib.r2d_batch_write_state_fields(self._h, first, rows.shape[0], N.ptr(rows, C.c_float)),
+                "r2d_batch_write_state_fields")
+
+    def read_fields(self, first: int, count: int, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty((count, self.n), np.float32)
+        N.check(self._lib.r2d_batch_read_state_fields(self._h, first, count, N.ptr(out, C.c_float)),
+                "r2d_batch_read_state_fields")
+        return out
 
     def read_positions_f64(self) -> np.ndarray:
         out = np.empty((3, self.n), np.float64)

@@ -296,3 +296,26 @@ def test_fp64_positions_integrate_in_double(grid):
     st = w.read_state()
     np.testing.assert_array_equal(st[:3], pose.astype(np.float32))
     np.testing.assert_array_equal(st[4], my)
+
+
+def test_state_field_ranges_read_and_write():
+    sc = scenes.random_scene(5, n=30)
+    w = World.from_scene(sc)
+    o = Oracle.from_scene(sc)
+    full = w.read_state()
+    np.testing.assert_array_equal(w.read_fields(0, 13), full)
+    np.testing.assert_array_equal(w.read_fields(9, 4), full[9:13])
+    # push the bodies: forces and torques in through the field-range entry point
+    rng = np.random.default_rng(1)
+    forces = (rng.normal(size=(3, full.shape[1])) * 4).astype(np.float32)
+    w.write_fields(6, forces)
+    st = o.state()
+    st[6:9] = forces
+    o.set_state(st)
+    for _ in range(3):
+        w.process(sc.dt, 1, sc.iters)
+        w.sync()
+        assert o.process(sc.dt, 1, sc.iters, ORDER_COLOUR) == 0
+    assert_state_equal(w.read_fields(0, 13), o.state(), "after forces")
+    with pytest.raises(N.R2DError):
+        w.read_fields(10, 4)
