@@ -209,6 +209,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default threads per size class")
     ap.add_argument("--no-precision", action="store_true", help="accepted for older command lines; no effect")
     ap.add_argument("--plain-worlds", type=int, default=64,
                     help="worlds stepped one per launch for the plain-path comparison")
@@ -241,6 +242,10 @@ def main():
         batch.process(sc.dt, sc.sub_steps, sc.iters)
     batch.sync()
     settled = batch.read_state()
+    # pick each size class's threads per CTA on the settled worlds (untimed;
+    # the state is restored)
+    if not args.no_autotune:
+        batch.autotune(sc.dt, sc.sub_steps, sc.iters, trial_steps=8)
     nb = sc.nbodies
 
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -348,6 +353,8 @@ def main():
         "config": {"workload": "config3: 4096 worlds, counts log-uniform [16,512], dt 1/60, 8 iterations, "
                                "settled 300 steps", "bodies": nb, "worlds": sc.nworlds,
                    "l2": "flushed between timed steps (256 MiB write outside the events)",
+                   "tiles": "threads per CTA of each size class autotuned on the settled worlds"
+                   if not args.no_autotune else "default threads per size class",
                    "parallelism": f"replicas x{world}"},
         "gpu_launches": launches,
         "wall_s_timed_loop": wall,

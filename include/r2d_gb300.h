@@ -199,6 +199,12 @@ R2D_API int r2d_batch_launches_per_step(r2d_batch* b, uint32_t* out);
  * solver's). */
 R2D_API int r2d_batch_write_state_fields(r2d_batch* b, uint32_t first, uint32_t count, const float* rows);
 R2D_API int r2d_batch_read_state_fields(r2d_batch* b, uint32_t first, uint32_t count, float* rows);
+/* Autotuning (no counterpart in the reference): picks the threads per CTA of
+ * each size class by timing `trial_steps` whole steps per candidate from the
+ * current state, which is restored afterwards.  Results never depend on the
+ * choice; it persists for later calls.  Takes a few hundred steps' time. */
+R2D_API int r2d_batch_autotune(r2d_batch* b, float dt, uint32_t sub_steps, uint32_t collision_iters,
+                               uint32_t trial_steps);
 /* The f64 pose [3][total bodies] under R2D_FLAG_FP64_POSITIONS (see the
  * solver's). */
 R2D_API int r2d_batch_read_positions_f64(r2d_batch* b, double* pose);

@@ -82,6 +82,7 @@ SIGNATURES = {
     "r2d_batch_process": ([_P, C.c_float, C.c_uint32, C.c_uint32], C.c_int),
     "r2d_batch_sync": ([_P], C.c_int),
     "r2d_batch_launches_per_step": ([_P, _u32p], C.c_int),
+    "r2d_batch_autotune": ([_P, C.c_float, C.c_uint32, C.c_uint32, C.c_uint32], C.c_int),
     "r2d_batch_world_status": ([_P, _i32p], C.c_int),
     "r2d_batch_num_manifolds": ([_P, C.c_uint32, _u32p], C.c_int),
     "r2d_batch_get_manifolds": ([_P, C.c_uint32, C.c_uint32, _u32p, _f32p, _u32p], C.c_int),

@@ -190,6 +190,9 @@ struct Engine {
     // parameters.
     uint32_t* d_call = nullptr;
     cudaGraphExec_t gexec = nullptr;
+    // threads per CTA chosen by autotune() for each size class (0 = the
+    // default policy), by index into the class bounds
+    int thread_override[16] = {};
     float g_dt = 0.f;
     uint32_t g_sub = 0, g_iters = 0;
     bool use_graph = true;
@@ -524,6 +527,102 @@ struct Engine {
         return nullptr;
     }
 
+    // Threads per CTA for a class of `nb` bodies: a world's phases rarely
+    // have more parallel items than this, and smaller CTAs let more worlds
+    // share an SM.
+    static int default_threads(uint32_t nb) { return nb <= 64 ? 64 : (nb <= 256 ? 128 : 256); }
+
+    // Picks each size class's threads per CTA by timing whole steps (all
+    // classes running together, as in use) from the current state, which is
+    // restored after every trial and at the end: one coordinate-descent pass
+    // over the classes, candidates 32..256 threads, a candidate replacing the
+    // standing choice only when 1.5 % faster.  Results do not depend on the
+    // choice (the colouring, scans and solve order do not), only speed.
+    int autotune(float dt, uint32_t sub_steps, uint32_t iters, uint32_t trial_steps) {
+        if (!d_state) return fail(R2D_ERR_INVALID_ARGUMENT, "no bodies");
+        if (sub_steps == 0 || trial_steps == 0) return fail(R2D_ERR_INVALID_ARGUMENT, "sub_steps and trial steps >= 1");
+        if (int st = sync()) return st;
+        if (plan_dirty)
+            if (int st = plan()) return st;
+        float* saved = nullptr;
+        double* saved64 = nullptr;
+        CUDA_TRY(dalloc(saved, (size_t)S_NFIELDS * nbodies));
+        if (d_pos64) CUDA_TRY(dalloc(saved64, (size_t)3 * nbodies));
+        CUDA_TRY(cudaMemcpyAsync(saved, d_state, sizeof(float) * S_NFIELDS * nbodies, cudaMemcpyDeviceToDevice, stream));
+        if (d_pos64)
+            CUDA_TRY(cudaMemcpyAsync(saved64, d_pos64, sizeof(double) * 3 * nbodies, cudaMemcpyDeviceToDevice, stream));
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        int status = R2D_OK;
+        auto restore = [&]() -> cudaError_t {
+            cudaError_t e = cudaMemcpyAsync(d_state, saved, sizeof(float) * S_NFIELDS * nbodies,
+                                            cudaMemcpyDeviceToDevice, stream);
+            if (e == cudaSuccess && d_pos64)
+                e = cudaMemcpyAsync(d_pos64, saved64, sizeof(double) * 3 * nbodies, cudaMemcpyDeviceToDevice, stream);
+            return e;
+        };
+        // seconds per step of the current plan (best of three runs), or < 0 on error
+        auto time_steps = [&]() -> float {
+            float best = -1.f;
+            for (int run = 0; run < 4; ++run) {
+                if (restore() != cudaSuccess) return -1.f;
+                if (run == 0) {  // plan, graph capture, capacity replays: untimed
+                    if (process(dt, sub_steps, iters) || sync()) return -1.f;
+                    continue;
+                }
+                if (cudaEventRecord(e0, stream) != cudaSuccess) return -1.f;
+                for (uint32_t k = 0; k < trial_steps; ++k)
+                    if (process(dt, sub_steps, iters)) return -1.f;
+                if (cudaEventRecord(e1, stream) != cudaSuccess || sync()) return -1.f;
+                float ms = 0.f;
+                if (cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) return -1.f;
+                const float per = ms / 1e3f / (float)trial_steps;
+                if (best < 0.f || per < best) best = per;
+            }
+            return best;
+        };
+        if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+            status = fail(R2D_ERR_CUDA, "autotune events");
+        } else {
+            static constexpr uint32_t bnd[] = {32, 64, 96, 128, 160, 192, 256, 320, 384, 448, 520};
+            static constexpr int cand[] = {32, 64, 128, 256};
+            std::vector<int> used(11, 0);
+            for (const auto& c : classes)
+                for (int k = 0; k < 11; ++k)
+                    if (c.caps.nb == bnd[k]) used[k] = 1;
+            for (int k = 0; k < 11 && status == R2D_OK; ++k) {
+                if (!used[k]) continue;
+                const int start = thread_override[k] ? thread_override[k] : default_threads(bnd[k]);
+                thread_override[k] = start;
+                plan_dirty = true;
+                float best_t = time_steps();
+                int best = start;
+                for (int nt : cand) {
+                    if (nt == start || (bnd[k] > 192 && nt < 64) || (bnd[k] <= 64 && nt > 128)) continue;
+                    thread_override[k] = nt;
+                    plan_dirty = true;
+                    const float t = time_steps();
+                    // a change must beat the standing choice by more than the timing noise
+                    if (t > 0.f && (best_t < 0.f || t < 0.985f * best_t)) {
+                        best_t = t;
+                        best = nt;
+                    }
+                }
+                thread_override[k] = best;
+                if (verbose) fprintf(stderr, "r2d: autotune class %u bodies -> %d threads (%.1f us/step)\n", bnd[k], best, best_t * 1e6f);
+            }
+            plan_dirty = true;
+        }
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        const cudaError_t er = restore();
+        const cudaError_t es = cudaStreamSynchronize(stream);
+        dfree(saved);
+        dfree(saved64);
+        if (status) return status;
+        if (er != cudaSuccess || es != cudaSuccess) return fail(R2D_ERR_CUDA, "autotune: restoring the state");
+        return R2D_OK;
+    }
+
     void drop_graph() {
         if (gexec) cudaGraphExecDestroy(gexec);
         gexec = nullptr;
@@ -591,7 +690,7 @@ struct Engine {
             kc.opts = layout_opts(!(boost & BOOST_FULL), plan_multi_substep);
             // A world's phases rarely have more parallel items than this many
             // threads; smaller CTAs let more worlds share an SM.
-            kc.threads = bounds[k] <= 64 ? 64 : (bounds[k] <= 256 ? 128 : 256);
+            kc.threads = thread_override[k] ? thread_override[k] : default_threads(bounds[k]);
             kc.smem = make_layout(kc.caps, kc.opts).total;
             if ((int)kc.smem > smem_optin) {
                 // each world fits alone, their maxima together do not
@@ -1315,6 +1414,13 @@ R2D_API int r2d_batch_process(r2d_batch* b, float dt, uint32_t sub_steps, uint32
 R2D_API int r2d_batch_sync(r2d_batch* b) {
     if (!b) return fail(R2D_ERR_INVALID_ARGUMENT, "batch is NULL");
     return guarded([&] { return b->eng.sync(); });
+}
+
+R2D_API int r2d_batch_autotune(r2d_batch* b, float dt, uint32_t sub_steps, uint32_t collision_iters,
+                               uint32_t trial_steps) {
+    if (!b) return fail(R2D_ERR_INVALID_ARGUMENT, "batch is NULL");
+    if (b->eng.nworlds == 0) return R2D_OK;
+    return guarded([&] { return b->eng.autotune(dt, sub_steps, collision_iters, trial_steps); });
 }
 
 R2D_API int r2d_batch_launches_per_step(r2d_batch* b, uint32_t* out) {

@@ -208,6 +208,11 @@ class Batch:
                 "r2d_batch_read_positions_f64")
         return out
 
+    def autotune(self, dt: float, sub_steps: int = 1, iters: int = 8, trial_steps: int = 3):
+        """Pick each size class's threads per CTA by timing (state restored)."""
+        N.check(self._lib.r2d_batch_autotune(self._h, float(dt), int(sub_steps), int(iters), int(trial_steps)),
+                "r2d_batch_autotune")
+
     def launches_per_step(self) -> int:
         out = C.c_uint32()
         N.check(self._lib.r2d_batch_launches_per_step(self._h, C.byref(out)), "r2d_batch_launches_per_step")

@@ -319,3 +319,27 @@ def test_state_field_ranges_read_and_write():
     assert_state_equal(w.read_fields(0, 13), o.state(), "after forces")
     with pytest.raises(N.R2DError):
         w.read_fields(10, 4)
+
+
+def test_autotune_restores_state_and_keeps_results():
+    # the autotuner times trial steps with other thread counts and restores
+    # the state; the steps after it must still match the oracle bit for bit
+    sc = scenes.batched_worlds("tune", seed=12, nworlds=40, steps=6, lo=16, hi=512)
+    b = Batch.from_scene(sc)
+    oracles = [Oracle.from_scene(sc.world(w)) for w in range(sc.nworlds)]
+
+    def step(k):
+        for _ in range(k):
+            b.process(sc.dt, sc.sub_steps, sc.iters)
+            for o in oracles:
+                assert o.process(sc.dt, sc.sub_steps, sc.iters, ORDER_COLOUR) == 0
+        b.sync()
+
+    step(2)
+    before = b.read_state()
+    b.autotune(sc.dt, sc.sub_steps, sc.iters, trial_steps=2)
+    np.testing.assert_array_equal(b.read_state().view(np.uint32), before.view(np.uint32))
+    step(4)
+    st = b.read_state()
+    for w, o in enumerate(oracles):
+        assert_state_equal(st[:, sc.body_off[w]:sc.body_off[w + 1]], o.state(), f"world {w}")
