@@ -102,7 +102,15 @@ enum {
      * is that pose rounded.  Momenta, contacts and joints stay f32.  No
      * counterpart in the reference, which is f32 throughout; it reduces
      * drift over long horizons (r2d_*_read_positions_f64 reads the pose). */
-    R2D_FLAG_FP64_POSITIONS = 4u
+    R2D_FLAG_FP64_POSITIONS = 4u,
+    /* Warm starting (no counterpart in the reference, whose manifolds are
+     * cleared every frame, src/core/lib.zig:261): a manifold whose
+     * (reference, incident) pair had one last frame starts from last frame's
+     * accumulated impulses, applied to the bodies after the first substep's
+     * preStep; and since such a sum must be able to shrink, impulses below
+     * the reference's 1e-4 skip threshold are applied (clamped at zero)
+     * instead of skipped. */
+    R2D_FLAG_WARM_START = 8u
 };
 
 typedef struct r2d_config {

@@ -32,6 +32,7 @@ _SIG = {
     "r2o_exclude_pair": ([_P, C.c_uint32, C.c_uint32], None),
     "r2o_add_joints": ([_P, C.c_uint32, _u8p, _u32p, _u32p, _f32p], None),
     "r2o_set_hash_config": ([_P, C.c_float, C.c_uint32], None),
+    "r2o_set_warm_start": ([_P, C.c_int], None),
     "r2o_get_state": ([_P, _f32p], None),
     "r2o_get_state_f64": ([_P, _f64p], None),
     "r2o_set_state": ([_P, _f32p], None),
@@ -116,6 +117,11 @@ class Oracle:
 
     def set_hash(self, cell: float, mult: int):
         self.lib.r2o_set_hash_config(self.h, cell, mult)
+
+    def set_warm_start(self, on: bool = True):
+        """Warm starting (off in reference mode): manifolds found again start
+        from last frame's accumulated impulses."""
+        self.lib.r2o_set_warm_start(self.h, int(bool(on)))
 
     def state(self) -> np.ndarray:
         out = np.empty((NSTATE, self.n), np.float32)

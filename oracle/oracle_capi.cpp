@@ -220,6 +220,11 @@ void r2o_set_hash_config(void* hp, float cell_size, uint32_t table_mult) {
     DISPATCH(h, (S.cell_size = cell_size, S.table_mult = table_mult));
 }
 
+void r2o_set_warm_start(void* hp, int on) {
+    Handle* h = (Handle*)hp;
+    DISPATCH(h, (S.warm_start = on != 0, S.warm_prev.clear()));
+}
+
 void r2o_get_state(void* hp, float* out) {
     Handle* h = (Handle*)hp;
     if (h->precision == 64)

@@ -512,6 +512,13 @@ public:
         size_t ref, inc;
     };
 
+    // Warm starting (an extension, off in reference mode): a manifold found
+    // again the next frame with the same (reference, incident) pair starts
+    // from last frame's accumulated impulses, which are applied to the
+    // bodies once, after the first substep's preStep.
+    bool warm_start = false;
+    std::unordered_map<uint64_t, std::array<R, 4>> warm_prev;  // (ref << 32 | inc) -> pn0, pt0, pn1, pt1
+
     std::vector<Body<R>> bodies;  // insertion order
     std::unordered_map<uint32_t, size_t> index_of_id;
     std::vector<R> gravity;       // one DownwardsGravity per entry (ForceGen list)
@@ -822,7 +829,10 @@ public:
                      zmax(R(0), (-point.depth) - C<R>::BAUMGARTE_SLOP) / dt;
             R num = dot2(dv, m.normal) + bias;
             R pn = num * point.mass_n;
-            if (pn < C<R>::MIN_MANIFOLD_IMPULSE) continue;
+            // The reference skips small or negative impulses, so an
+            // accumulated impulse never decreases; a warm-started one must be
+            // able to, so warm starting clamps the sum instead (below).
+            if (!warm_start && pn < C<R>::MIN_MANIFOLD_IMPULSE) continue;
             num = dot2(dv, m.tangent);
             R pt = num * point.mass_t;
             R new_accumulated_pn = zmax(R(0), point.accumulated_pn + pn);
@@ -852,6 +862,67 @@ public:
         m.applied_rot_p_1 = 0;
         m.applied_linear_p2 = V2<R>{};
         m.applied_rot_p_2 = 0;
+    }
+
+    // ---- warm starting ----
+    void warm_load() {
+        for (auto& km : manifolds) {
+            auto it = warm_prev.find(((uint64_t)km.first.ref << 32) | (uint64_t)km.first.inc);
+            if (it == warm_prev.end()) continue;
+            for (int i = 0; i < 2; ++i) {
+                if (!km.second.has_point[i]) continue;
+                km.second.points[i].accumulated_pn = it->second[2 * i];
+                km.second.points[i].accumulated_pt = it->second[2 * i + 1];
+            }
+        }
+    }
+
+    // Applies a manifold's accumulated impulses, summed like calculateImpulses
+    // sums its applied ones; a point with depth >= 0 starts from zero.
+    void warm_apply(Manifold<R>& m, const Key& k) {
+        Body<R>& b1 = bodies[k.ref];
+        Body<R>& b2 = bodies[k.inc];
+        V2<R> alp1{}, alp2{};
+        R arp1 = 0, arp2 = 0;
+        for (int i = 0; i < 2; ++i) {
+            if (!m.has_point[i]) continue;
+            CollisionPoint<R>& point = m.points[i];
+            if (point.depth >= R(0)) {
+                point.accumulated_pn = 0;
+                point.accumulated_pt = 0;
+                continue;
+            }
+            V2<R> dp = add2(scale2(m.normal, point.accumulated_pn), scale2(m.tangent, point.accumulated_pt));
+            if (!b1.is_static) {
+                alp1 = sub2(alp1, dp);
+                arp1 -= cross2(point.ref_r, dp);
+            }
+            if (!b2.is_static) {
+                alp2 = add2(alp2, dp);
+                arp2 += cross2(point.inc_r, dp);
+            }
+        }
+        if (!b1.is_static) {
+            b1.props.momentum = add2(b1.props.momentum, alp1);
+            b1.props.ang_momentum += arp1;
+        }
+        if (!b2.is_static) {
+            b2.props.momentum = add2(b2.props.momentum, alp2);
+            b2.props.ang_momentum += arp2;
+        }
+    }
+
+    void warm_store() {
+        warm_prev.clear();
+        for (auto& km : manifolds) {
+            std::array<R, 4> a{R(0), R(0), R(0), R(0)};
+            for (int i = 0; i < 2; ++i) {
+                if (!km.second.has_point[i]) continue;
+                a[2 * i] = km.second.points[i].accumulated_pn;
+                a[2 * i + 1] = km.second.points[i].accumulated_pt;
+            }
+            warm_prev[((uint64_t)km.first.ref << 32) | (uint64_t)km.first.inc] = a;
+        }
     }
 
     // ---- joint solves ----
@@ -1077,6 +1148,7 @@ public:
             st = compute_colouring();
             if (st != OK) return st;
         }
+        if (warm_start) warm_load();
 
         for (size_t s = 0; s < sub_steps; ++s) {
             for (R g : gravity) {  // DownwardsGravity.apply (DownwardsGravity.zig:35-39)
@@ -1097,6 +1169,13 @@ public:
             for (auto& km : manifolds) {  // lib.zig:218-224
                 update_tgs_depth(km.second, km.first);
                 pre_step(km.second, km.first);
+            }
+            if (warm_start && s == 0) {
+                if (order == ORDER_COLOUR) {
+                    for (size_t m : contact_order) warm_apply(manifolds[m].second, manifolds[m].first);
+                } else {
+                    for (auto& km : manifolds) warm_apply(km.second, km.first);
+                }
             }
             for (size_t it = 0; it < collision_iters; ++it) {  // lib.zig:226-236
                 if (order == ORDER_COLOUR) {
@@ -1124,6 +1203,7 @@ public:
                 b.props.torque = 0;
             }
         }
+        if (warm_start) warm_store();
         return OK;
     }
 };

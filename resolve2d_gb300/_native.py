@@ -33,6 +33,7 @@ STATUS_NAMES = {
 FLAG_DEBUG_TAPS = 1
 FLAG_GRID_PIPELINE = 2
 FLAG_FP64_POSITIONS = 4
+FLAG_WARM_START = 8
 MANIFOLD_FLOATS = 33
 
 

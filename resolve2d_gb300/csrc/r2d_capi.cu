@@ -33,6 +33,10 @@ cudaError_t launch_world_step(const StepParams& P, const Caps& C, int threads, c
                               cudaStream_t stream);
 cudaError_t allow_world_step_smem(int bytes);
 cudaError_t launch_count_call(uint32_t* counter, cudaStream_t stream);
+cudaError_t launch_migrate_warm(uint32_t nworlds, const uint32_t* old_keys, const float4* old_vals,
+                                const uint32_t* old_off, const uint32_t* old_hs, const uint32_t* old_cur,
+                                uint32_t* new_keys, float4* new_vals, const uint32_t* new_off, const uint32_t* new_hs,
+                                cudaStream_t stream);
 }  // namespace r2d
 
 using namespace r2d;
@@ -193,6 +197,16 @@ struct Engine {
     // threads per CTA chosen by autotune() for each size class (0 = the
     // default policy), by index into the class bounds
     int thread_override[16] = {};
+
+    // Warm starting (R2D_FLAG_WARM_START): each fused world's two tables of
+    // warm_hs slots (WorldDesc::warm_off), sized from its class's manifold
+    // capacity; d_warm_cur[w] names the table holding last frame.
+    uint32_t* d_warm_keys = nullptr;
+    float4* d_warm_vals = nullptr;
+    uint32_t* d_warm_cur = nullptr;
+    uint32_t* d_warm_off = nullptr;  // [nworlds] copies of WorldDesc::warm_off / warm_hs for migration
+    uint32_t* d_warm_hs = nullptr;
+    std::vector<uint32_t> warm_hs_h, warm_off_h;
     float g_dt = 0.f;
     uint32_t g_sub = 0, g_iters = 0;
     bool use_graph = true;
@@ -201,6 +215,7 @@ struct Engine {
         large.clear();
         if (gexec) cudaGraphExecDestroy(gexec);
         dfree(d_call);
+        dfree(d_warm_keys); dfree(d_warm_vals); dfree(d_warm_cur); dfree(d_warm_off); dfree(d_warm_hs);
         dfree(d_state); dfree(d_pos64); dfree(d_props); dfree(d_kind); dfree(d_ids); dfree(d_worlds);
         dfree(d_status); dfree(d_err);
         if (h_err) cudaFreeHost(h_err);
@@ -302,6 +317,13 @@ struct Engine {
         large.resize(nw);
         large_status.assign(nw, 0);
         large_frozen.assign(nw, 0);
+        dfree(d_warm_keys); dfree(d_warm_vals); dfree(d_warm_cur); dfree(d_warm_off); dfree(d_warm_hs);
+        warm_hs_h.assign(nw, 0);
+        warm_off_h.assign(nw, 0);
+        if (warm_start()) {
+            CUDA_TRY(dalloc(d_warm_cur, nw));
+            CUDA_TRY(cudaMemsetAsync(d_warm_cur, 0, sizeof(uint32_t) * nw, stream));
+        }
         calls.clear();
         pending = false;
         CUDA_TRY(cudaMemcpyAsync(d_state, state_h.data(), sizeof(float) * S_NFIELDS * n, cudaMemcpyHostToDevice, stream));
@@ -356,6 +378,51 @@ struct Engine {
     }
 
     bool fp64_positions() const { return (cfg.flags & R2D_FLAG_FP64_POSITIONS) != 0; }
+    bool warm_start() const { return (cfg.flags & R2D_FLAG_WARM_START) != 0; }
+
+    static uint32_t pow2_at_least(uint32_t v) {
+        uint32_t p = 1;
+        while (p < v) p <<= 1;
+        return p;
+    }
+
+    // (Re)lays out the fused worlds' warm tables for the capacities `nm`
+    // of their classes (0 for grid-pipeline worlds), carrying last frame's
+    // entries over; a no-op when nothing changed.
+    int layout_warm(const std::vector<uint32_t>& nm) {
+        std::vector<uint32_t> hs(nworlds, 0), off(nworlds, 0);
+        size_t total = 0;
+        for (uint32_t w = 0; w < nworlds; ++w) {
+            hs[w] = nm[w] ? pow2_at_least(2u * nm[w] + 2u) : 0u;
+            off[w] = (uint32_t)total;
+            total += 2ull * hs[w];
+        }
+        if (hs == warm_hs_h && d_warm_keys) return R2D_OK;
+        uint32_t *keys = nullptr, *doff = nullptr, *dhs = nullptr;
+        float4* vals = nullptr;
+        CUDA_TRY(dalloc(keys, std::max<size_t>(total, 1)));
+        CUDA_TRY(dalloc(vals, std::max<size_t>(total, 1)));
+        CUDA_TRY(dalloc(doff, nworlds));
+        CUDA_TRY(dalloc(dhs, nworlds));
+        CUDA_TRY(cudaMemcpyAsync(doff, off.data(), 4 * nworlds, cudaMemcpyHostToDevice, stream));
+        CUDA_TRY(cudaMemcpyAsync(dhs, hs.data(), 4 * nworlds, cudaMemcpyHostToDevice, stream));
+        CUDA_TRY(launch_migrate_warm(nworlds, d_warm_keys, d_warm_vals, d_warm_off, d_warm_keys ? d_warm_hs : nullptr,
+                                     d_warm_cur, keys, vals, doff, dhs, stream));
+        CUDA_TRY(cudaMemsetAsync(d_warm_cur, 0, sizeof(uint32_t) * nworlds, stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        dfree(d_warm_keys); dfree(d_warm_vals); dfree(d_warm_off); dfree(d_warm_hs);
+        d_warm_keys = keys;
+        d_warm_vals = vals;
+        d_warm_off = doff;
+        d_warm_hs = dhs;
+        warm_hs_h = hs;
+        warm_off_h = off;
+        for (uint32_t w = 0; w < nworlds; ++w) {
+            worlds_h[w].warm_hs = hs[w];
+            worlds_h[w].warm_off = off[w];
+        }
+        return R2D_OK;
+    }
 
     // d_pos64 = the pose fields of a host f32 state, widened.
     cudaError_t upload_pose64(const float* state) {
@@ -713,6 +780,12 @@ struct Engine {
             large_list.push_back(w);
             if (!large[w]) large[w].reset(new LargeWorld());
         }
+        if (warm_start()) {
+            std::vector<uint32_t> nm(nworlds, 0);
+            for (const auto& c : classes)
+                for (uint32_t w : c.worlds) nm[w] = c.caps.nm;
+            if (int st = layout_warm(nm)) return st;
+        }
         for (auto& d : worlds_h) d.bucket_recip = bucket_recip(table_mult * d.n);
         CUDA_TRY(dalloc(d_worlds, nworlds));
         CUDA_TRY(cudaMemcpyAsync(d_worlds, worlds_h.data(), sizeof(WorldDesc) * nworlds, cudaMemcpyHostToDevice, stream));
@@ -850,6 +923,7 @@ struct Engine {
         in.table_mult = table_mult;
         in.disc_rot = (d.flags & W_DISC_ROTATION) != 0;
         in.pos64 = d_pos64;
+        in.warm = warm_start();
         return in;
     }
 
@@ -908,6 +982,11 @@ struct Engine {
         P.call_index = call_index;
         P.timers = d_timers;
         P.pos64 = d_pos64;
+        if (warm_start()) {
+            P.warm_keys = d_warm_keys;
+            P.warm_vals = d_warm_vals;
+            P.warm_cur = d_warm_cur;
+        }
         return P;
     }
 
@@ -1040,6 +1119,16 @@ struct Engine {
                         make_layout(c, opts).total);
             if ((int)make_layout(c, opts).total > smem_limit()) break;
             if (int st = grow_debug(c.nm)) return st;
+            if (warm_start() && warm_hs_h[w] < pow2_at_least(2u * c.nm + 2u)) {
+                // the world's warm table must hold the larger manifold capacity
+                std::vector<uint32_t> nm(nworlds, 0);
+                for (const auto& kc2 : classes)
+                    for (uint32_t w2 : kc2.worlds) nm[w2] = kc2.caps.nm;
+                nm[w] = std::max(nm[w], c.nm);
+                if (int st = layout_warm(nm)) return st;
+                CUDA_TRY(cudaMemcpyAsync(d_worlds, worlds_h.data(), sizeof(WorldDesc) * nworlds,
+                                         cudaMemcpyHostToDevice, stream));
+            }
             CUDA_TRY(cudaMemsetAsync(d_fail_call + w, 0xFF, sizeof(uint32_t), stream));
             CUDA_TRY(cudaMemsetAsync(d_capbits + w, 0, sizeof(uint32_t), stream));
             CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), stream));
@@ -1075,6 +1164,15 @@ struct Engine {
             fprintf(stderr, "r2d: world %u (%u bodies) moves to the large-world path at call %u\n", w, d.n, from);
         world_large[w] = 1;
         large[w].reset(new LargeWorld());
+        if (warm_start() && d_warm_keys && warm_hs_h[w]) {
+            // last frame's impulses go with the world
+            uint32_t cur = 0;
+            CUDA_TRY(cudaMemcpy(&cur, d_warm_cur + w, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+            const size_t at = (size_t)warm_off_h[w] + (size_t)cur * warm_hs_h[w];
+            std::string msg;
+            const int r = large[w]->seed_warm(d_warm_keys + at, d_warm_vals + at, warm_hs_h[w], stream, &msg);
+            if (r) return fail(r, msg);
+        }
         for (uint32_t k = from; k < calls.size(); ++k) {
             std::string msg;
             const int r = large[w]->step(large_inputs(w), calls[k].dt, calls[k].sub_steps, calls[k].iters, stream, &msg);

@@ -424,6 +424,7 @@ struct Phase2 {
     const uint32_t* order;  // constraints of the colour [k0, k1)
     uint32_t k0, k1;
     double* pos64;          // f64 pose (FP64-positions mode), else null
+    bool warm;              // warm starting
 
     __device__ float& st(int f, uint32_t i) const { return state[(size_t)f * NB + base + i]; }
     __device__ float pr(int f, uint32_t i) const { return __ldg(props + (size_t)f * NB + base + i); }
@@ -516,7 +517,59 @@ __global__ void lk_prestep(Phase2 A) {
 __global__ void lk_contacts(Phase2 A) {
     const uint32_t k = A.k0 + blockIdx.x * LT + threadIdx.x;
     if (k >= A.k1) return;
-    solve_contact<false>(A.s, A.order[k]);
+    solve_contact<false>(A.s, A.order[k], A.warm);
+}
+
+// ---- warm starting: the world's tables of last frame's impulses ----
+__device__ __forceinline__ unsigned long long warm_key64(uint32_t ref, uint32_t inc) {
+    return ((unsigned long long)ref << 32) | inc;
+}
+
+__global__ void lk_warm_load(SWT<uint32_t> s, uint32_t M, const unsigned long long* keys, const float4* vals,
+                             uint32_t hs) {
+    const uint32_t m = blockIdx.x * LT + threadIdx.x;
+    if (m >= M) return;
+    const int slot = warm_find(keys, hs, warm_key64(s.ma[m], s.mb[m]));
+    if (slot < 0) return;
+    const float4 v = vals[slot];
+    const uint32_t p0 = s.mp0[m], np = s.mnp[m];
+    if (np > 0) {
+        s.apn[p0] = v.x;
+        s.apt[p0] = v.y;
+    }
+    if (np > 1) {
+        s.apn[p0 + 1] = v.z;
+        s.apt[p0 + 1] = v.w;
+    }
+}
+
+__global__ void lk_warm_apply(Phase2 A) {
+    const uint32_t k = A.k0 + blockIdx.x * LT + threadIdx.x;
+    if (k >= A.k1) return;
+    warm_apply_contact<false>(A.s, A.order[k]);
+}
+
+__global__ void lk_warm_clear(unsigned long long* keys, uint32_t hs) {
+    const uint32_t q = blockIdx.x * LT + threadIdx.x;
+    if (q < hs) keys[q] = ~0ull;
+}
+
+__global__ void lk_warm_store(SWT<uint32_t> s, uint32_t M, unsigned long long* keys, float4* vals, uint32_t hs) {
+    const uint32_t m = blockIdx.x * LT + threadIdx.x;
+    if (m >= M) return;
+    const uint32_t p0 = s.mp0[m], np = s.mnp[m];
+    const float4 v = make_float4(np > 0 ? s.apn[p0] : 0.f, np > 0 ? s.apt[p0] : 0.f, np > 1 ? s.apn[p0 + 1] : 0.f,
+                                 np > 1 ? s.apt[p0 + 1] : 0.f);
+    warm_insert(keys, vals, hs, warm_key64(s.ma[m], s.mb[m]), v);
+}
+
+// a fused-kernel table (16-bit reference << 16 | incident keys) into this path's
+__global__ void lk_warm_copy(const uint32_t* keys, const float4* vals, uint32_t hs, unsigned long long* nkeys,
+                             float4* nvals, uint32_t nhs) {
+    const uint32_t q = blockIdx.x * LT + threadIdx.x;
+    if (q >= hs) return;
+    const uint32_t key = keys[q];
+    if (key != 0xFFFFFFFFu) warm_insert(nkeys, nvals, nhs, warm_key64(key >> 16, key & 0xFFFFu), vals[q]);
 }
 
 __global__ void lk_joints(Phase2 A) {
@@ -652,6 +705,13 @@ struct LargeWorld::Impl {
     uint32_t *dk = nullptr, *dc = nullptr;
     float* dd = nullptr;
 
+    // warm starting: two tables (last frame's = wcur), sizes in slots
+    unsigned long long* wkeys[2] = {nullptr, nullptr};
+    float4* wvals[2] = {nullptr, nullptr};
+    size_t wcap[2] = {0, 0};
+    uint32_t whs[2] = {0, 0};
+    int wcur = 0;
+
     double pair_scale = 1.0;  // grows when the candidate-pair set overflows
     uint32_t nman = 0, nj = 0, nlaunch = 0;
     std::vector<uint32_t> coff, joff;
@@ -663,6 +723,10 @@ struct LargeWorld::Impl {
                       jcol, jorder, cnt, entries, hist, dk, dc, dd};
         for (void* p : ps)
             if (p) cudaFree(p);
+        for (int b = 0; b < 2; ++b) {
+            if (wkeys[b]) cudaFree(wkeys[b]);
+            if (wvals[b]) cudaFree(wvals[b]);
+        }
         if (h_cnt) cudaFreeHost(h_cnt);
     }
 
@@ -874,6 +938,17 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
     I.nman = M;
     I.nj = in.nj;
 
+    if (in.warm && M && I.whs[I.wcur]) {
+        LAUNCH(lk_warm_load, blocks(M), I.views(in), M, I.wkeys[I.wcur], I.wvals[I.wcur], I.whs[I.wcur]);
+    }
+    // the table this call writes, sized for its manifolds (at most half full)
+    const int wnext = 1 - I.wcur;
+    uint32_t whs_next = 1;
+    while (whs_next < 2u * M + 2u) whs_next <<= 1;
+    if (in.warm) {
+        LTRY(regrow(I.wcap[wnext], whs_next, {LB(I.wkeys[wnext]), LB(I.wvals[wnext])}));
+    }
+
     // ---- substeps: the world's state changes from here on ----
     Phase2 S{};
     S.s = I.views(in);
@@ -884,11 +959,20 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
     for (int k = 0; k < MAX_GRAVITY; ++k) S.g[k] = in.g[k];
     S.jtype = in.jtype; S.jb1 = in.jb1; S.jb2 = in.jb2; S.jprm = in.jprm;
     S.pos64 = in.pos64;
+    S.warm = in.warm;
     for (uint32_t sub = 0; sub < sub_steps; ++sub) {
         S.first = sub == 0;
         S.last = sub + 1 == sub_steps;
         LAUNCH(lk_forces, blocks(n), S);
         if (M) LAUNCH(lk_prestep, blocks(M), S);
+        if (in.warm && sub == 0) {  // the warm-started impulses, colour by colour
+            S.order = I.corder;
+            for (size_t c = 0; c + 1 < I.coff.size(); ++c) {
+                S.k0 = I.coff[c];
+                S.k1 = I.coff[c + 1];
+                LAUNCH(lk_warm_apply, blocks(S.k1 - S.k0), S);
+            }
+        }
         for (uint32_t it = 0; it < iters; ++it) {
             S.order = I.jorder;
             for (size_t c = 0; c + 1 < I.joff.size(); ++c) {
@@ -905,7 +989,25 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
         }
         LAUNCH(lk_integrate, blocks(n), S);
     }
+    if (in.warm) {  // this call's impulses become the next call's start
+        LAUNCH(lk_warm_clear, blocks(whs_next), I.wkeys[wnext], whs_next);
+        if (M) LAUNCH(lk_warm_store, blocks(M), S.s, M, I.wkeys[wnext], I.wvals[wnext], whs_next);
+        I.whs[wnext] = whs_next;
+        I.wcur = wnext;
+    }
     LTRY(cudaGetLastError());
+    return 0;
+}
+
+int LargeWorld::seed_warm(const uint32_t* keys, const float4* vals, uint32_t hs, cudaStream_t st, std::string* msg) {
+    Impl& I = *impl;
+    LTRY(regrow(I.wcap[0], hs, {LB(I.wkeys[0]), LB(I.wvals[0])}));
+    lk_warm_clear<<<blocks(hs), LT, 0, st>>>(I.wkeys[0], hs);
+    lk_warm_copy<<<blocks(hs), LT, 0, st>>>(keys, vals, hs, I.wkeys[0], I.wvals[0], hs);
+    LTRY(cudaStreamSynchronize(st));
+    I.whs[0] = hs;
+    I.whs[1] = 0;
+    I.wcur = 0;
     return 0;
 }
 

@@ -35,6 +35,7 @@ struct LargeInputs {
     uint32_t table_mult;
     bool disc_rot;         // some joint reads disc orientations
     double* pos64;         // [3][NB] f64 pose (FP64-positions mode), else null
+    bool warm;             // warm starting (the world keeps its impulses across calls)
 };
 
 class LargeWorld {
@@ -53,6 +54,10 @@ public:
     int joint_colours(uint32_t cap, uint32_t* colours, cudaStream_t st, std::string* msg);
     // Kernel launches of the last step.
     uint32_t launches() const;
+    // Warm starting: take over another table of last frame's impulses
+    // (keys / values of `hs` slots in device memory, the fused kernel's
+    // layout) when a world moves to this path.
+    int seed_warm(const uint32_t* keys, const float4* vals, uint32_t hs, cudaStream_t st, std::string* msg);
 
     struct Impl;
 

@@ -47,9 +47,13 @@ struct SWT {
     }
 };
 
-// CollisionManifold.calculateImpulses (collision.zig:135-218)
+// CollisionManifold.calculateImpulses (collision.zig:135-218).  `warm`:
+// warm-starting mode, where an increment below MIN_MANIFOLD_IMPULSE is not
+// skipped (the reference's skip keeps an accumulated impulse from ever
+// decreasing, which a warm-started one must be able to); the sum is clamped
+// at zero as written.
 template <bool LEAN, class IDX>
-__device__ __forceinline__ void solve_contact(const SWT<IDX>& s, uint32_t m) {
+__device__ __forceinline__ void solve_contact(const SWT<IDX>& s, uint32_t m, bool warm = false) {
     const uint32_t a = s.ma[m], b = s.mb[m];
     const bool sa = s.kind[a] & K_STATIC, sb = s.kind[b] & K_STATIC;
     const float inv_m1 = s.inv_m[a], inv_m2 = s.inv_m[b];
@@ -75,7 +79,7 @@ __device__ __forceinline__ void solve_contact(const SWT<IDX>& s, uint32_t m) {
         const f2 dv = sub2(v1, v2);
         float num = dot2(dv, n) + bias;  // BAUMGARTE*max(0,-depth-SLOP)/h (collision.zig:172)
         const float pn = num * s.mn[p];
-        if (pn < MIN_MANIFOLD_IMPULSE) continue;
+        if (!warm && pn < MIN_MANIFOLD_IMPULSE) continue;
         num = dot2(dv, t);
         const float pt = num * s.mt[p];
         const float acc = s.apn[p];
@@ -118,7 +122,8 @@ __device__ __forceinline__ void solve_contact(const SWT<IDX>& s, uint32_t m) {
 // solve_contact.  Every lane of the warp must call this (it shuffles);
 // `valid` says whether the lane pair holds a manifold.
 template <bool LEAN, class IDX>
-__device__ __forceinline__ void solve_contact_lanes(const SWT<IDX>& s, uint32_t m, bool valid, uint32_t lane) {
+__device__ __forceinline__ void solve_contact_lanes(const SWT<IDX>& s, uint32_t m, bool valid, uint32_t lane,
+                                                    bool warm = false) {
     const uint32_t half = lane & 1u;
     uint32_t a = 0, b = 0;
     bool sa = true, sb = true, hit = false;
@@ -148,7 +153,7 @@ __device__ __forceinline__ void solve_contact_lanes(const SWT<IDX>& s, uint32_t 
                 const f2 dv = sub2(v1, v2);
                 float num = dot2(dv, n) + bias;
                 const float pn = num * s.mn[p];
-                if (!(pn < MIN_MANIFOLD_IMPULSE)) {  // as solve_contact's skip, NaN included
+                if (warm || !(pn < MIN_MANIFOLD_IMPULSE)) {  // as solve_contact's skip, NaN included
                     num = dot2(dv, t);
                     const float pt = num * s.mt[p];
                     const float acc = s.apn[p];
@@ -198,6 +203,94 @@ __device__ __forceinline__ void solve_contact_lanes(const SWT<IDX>& s, uint32_t 
         }
     }
     // A static body receives exactly +0 in the reference; its state is left alone.
+    if (!sa) {
+        s.mx[a] += alp1.x;
+        s.my[a] += alp1.y;
+        s.L[a] += arp1;
+    }
+    if (!sb) {
+        s.mx[b] += alp2.x;
+        s.my[b] += alp2.y;
+        s.L[b] += arp2;
+    }
+}
+
+// ---- warm starting (an extension; off in reference mode) ----
+// Each world keeps last frame's accumulated impulses in an open-addressing
+// table in HBM: key (reference << 16 | incident), value (pn0, pt0, pn1, pt1).
+__device__ __forceinline__ uint32_t warm_hash(uint32_t k) {
+    k ^= k >> 16;
+    k *= 0x7FEB352Du;
+    k ^= k >> 15;
+    k *= 0x846CA68Bu;
+    k ^= k >> 16;
+    return k;
+}
+
+// 64-bit keys (the grid pipeline: reference << 32 | incident)
+__device__ __forceinline__ uint32_t warm_hash(unsigned long long k) {
+    return warm_hash((uint32_t)k ^ (warm_hash((uint32_t)(k >> 32)) * 0x9E3779B1u));
+}
+
+// Slot of `key` in a table of `hs` slots (a power of two), or -1; all-ones
+// keys mark empty slots.
+template <class K>
+__device__ __forceinline__ int warm_find(const K* __restrict__ keys, uint32_t hs, K key) {
+    const uint32_t mask = hs - 1u, h = warm_hash(key);
+    for (uint32_t probe = 0; probe < hs; ++probe) {
+        const uint32_t slot = (h + probe) & mask;
+        const K k = keys[slot];
+        if (k == key) return (int)slot;
+        if (k == ~K(0)) return -1;
+    }
+    return -1;
+}
+
+// Inserts a key that is not in the table yet (keys are unique per frame);
+// the table holds at most half its slots, so a free slot is always found.
+template <class K>
+__device__ __forceinline__ void warm_insert(K* keys, float4* vals, uint32_t hs, K key, float4 v) {
+    const uint32_t mask = hs - 1u, h = warm_hash(key);
+    for (uint32_t probe = 0; probe < hs; ++probe) {
+        const uint32_t slot = (h + probe) & mask;
+        if (atomicCAS(&keys[slot], ~K(0), key) == ~K(0)) {
+            vals[slot] = v;
+            return;
+        }
+    }
+}
+
+// Applies a manifold's (warm-started) accumulated impulses to its bodies,
+// summed as calculateImpulses sums its applied ones; a point with depth >= 0
+// (bias < 0) starts from zero instead.
+template <bool LEAN, class IDX>
+__device__ __forceinline__ void warm_apply_contact(const SWT<IDX>& s, uint32_t m) {
+    const uint32_t a = s.ma[m], b = s.mb[m];
+    const bool sa = s.kind[a] & K_STATIC, sb = s.kind[b] & K_STATIC;
+    const f2 n = {s.nx[m], s.ny[m]};
+    const f2 t = cw90(n);
+    f2 alp1 = {0.f, 0.f}, alp2 = {0.f, 0.f};
+    float arp1 = 0.f, arp2 = 0.f;
+    const uint32_t p0 = s.mp0[m], np = s.mnp[m];
+    for (uint32_t k = 0; k < np; ++k) {
+        const uint32_t p = p0 + k;
+        if (s.bias[p] < 0.0f) {
+            s.apn[p] = 0.f;
+            s.apt[p] = 0.f;
+            continue;
+        }
+        f2 r1, r2;
+        s.template arms<LEAN>(p, a, b, &r1, &r2);
+        const f2 dp = add2(scale2(n, s.apn[p]), scale2(t, s.apt[p]));
+        if (!sa) {
+            alp1 = sub2(alp1, dp);
+            arp1 -= cross2(r1, dp);
+        }
+        if (!sb) {
+            alp2 = add2(alp2, dp);
+            arp2 += cross2(r2, dp);
+        }
+    }
     if (!sa) {
         s.mx[a] += alp1.x;
         s.my[a] += alp1.y;

@@ -37,6 +37,10 @@ struct WorldDesc {
     // body diameter, so a bucket holds a few bodies (the spatial hash's own
     // cells still decide which pairs are candidates).
     float fine_cell;
+    // warm starting: this world's two tables of warm_hs slots start at
+    // entry warm_off (table b at warm_off + b * warm_hs)
+    uint32_t warm_hs;
+    uint32_t warm_off;
     uint32_t pad_;
 };
 
@@ -193,6 +197,9 @@ struct StepParams {
     const uint32_t* call_counter;  // ... or, when set, *call_counter - 1 (bumped on the device per call)
     unsigned long long* timers;  // [nworlds][PHASE_SLOTS] when built with R2D_PHASE_TIMERS
     double* pos64;               // [3][nbodies] x, y, angle in f64 (FP64-positions mode), else null
+    uint32_t* warm_keys;         // warm-start tables (WorldDesc::warm_off), else null
+    float4* warm_vals;
+    uint32_t* warm_cur;          // [nworlds] which of a world's two tables holds last frame
     float dt;
     uint32_t sub_steps, iters;
     float cell;

@@ -782,6 +782,28 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
             s.apn[p] = 0.f;
             s.apt[p] = 0.f;
         }
+        const bool warm = P.warm_keys != nullptr;
+        const uint32_t wcur = warm ? P.warm_cur[w] : 0u;
+        if (warm) {
+            // a manifold of last frame's pair starts from its impulses
+            __syncthreads();
+            const uint32_t* keys = P.warm_keys + wd.warm_off + wcur * wd.warm_hs;
+            const float4* vals = P.warm_vals + wd.warm_off + wcur * wd.warm_hs;
+            for (uint32_t m = tid; m < M; m += NT) {
+                const int slot = warm_find(keys, wd.warm_hs, ((uint32_t)s.ma[m] << 16) | s.mb[m]);
+                if (slot < 0) continue;
+                const float4 v = vals[slot];
+                const uint32_t p0 = s.mp0[m], np = s.mnp[m];
+                if (np > 0) {
+                    s.apn[p0] = v.x;
+                    s.apt[p0] = v.y;
+                }
+                if (np > 1) {
+                    s.apn[p0 + 1] = v.z;
+                    s.apt[p0 + 1] = v.w;
+                }
+            }
+        }
         __syncthreads();
 
         PHASE(4);
@@ -872,6 +894,12 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
                 }
             }
             __syncthreads();
+            if (warm && sub == 0) {  // the warm-started impulses, colour by colour
+                for (uint32_t c = 0; c < ncol; ++c) {
+                    for (uint32_t k = coff[c] + tid; k < coff[c + 1]; k += NT) warm_apply_contact<LEAN>(s, corder[k]);
+                    __syncthreads();
+                }
+            }
             // impulse iterations (lib.zig:226-236): joints, then contacts
             for (uint32_t it = 0; it < P.iters; ++it) {
                 for (uint32_t c = 0; c < njcol; ++c) {
@@ -890,9 +918,10 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
                     const uint32_t k0 = coff[c], k1 = coff[c + 1];
                     if (k1 - k0 <= (uint32_t)(NT / 2)) {
                         const uint32_t k = k0 + ((uint32_t)tid >> 1);
-                        solve_contact_lanes<LEAN>(s, k < k1 ? (uint32_t)corder[k] : 0u, k < k1, (uint32_t)tid & 31u);
+                        solve_contact_lanes<LEAN>(s, k < k1 ? (uint32_t)corder[k] : 0u, k < k1, (uint32_t)tid & 31u,
+                                                  warm);
                     } else {
-                        for (uint32_t k = k0 + tid; k < k1; k += NT) solve_contact<LEAN>(s, corder[k]);
+                        for (uint32_t k = k0 + tid; k < k1; k += NT) solve_contact<LEAN>(s, corder[k], warm);
                     }
                     __syncthreads();
                 }
@@ -920,6 +949,23 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
                 }
             }
             __syncthreads();
+        }
+
+        if (warm) {
+            // this frame's impulses go to the world's other table, which then
+            // becomes the one the next frame reads
+            uint32_t* keys = P.warm_keys + wd.warm_off + (1u - wcur) * wd.warm_hs;
+            float4* vals = P.warm_vals + wd.warm_off + (1u - wcur) * wd.warm_hs;
+            for (uint32_t q = tid; q < wd.warm_hs; q += NT) keys[q] = 0xFFFFFFFFu;
+            __syncthreads();
+            for (uint32_t m = tid; m < M; m += NT) {
+                const uint32_t p0 = s.mp0[m], np = s.mnp[m];
+                const float4 v = make_float4(np > 0 ? s.apn[p0] : 0.f, np > 0 ? s.apt[p0] : 0.f,
+                                             np > 1 ? s.apn[p0 + 1] : 0.f, np > 1 ? s.apt[p0 + 1] : 0.f);
+                warm_insert(keys, vals, wd.warm_hs, ((uint32_t)s.ma[m] << 16) | s.mb[m], v);
+            }
+            __syncthreads();
+            if (tid == 0) P.warm_cur[w] = 1u - wcur;
         }
 
         PHASE(5);
@@ -1045,6 +1091,36 @@ cudaError_t allow_world_step_smem(int bytes) {
     for (cudaError_t e : es)
         if (e != cudaSuccess) return e;
     return cudaSuccess;
+}
+
+// Moves each world's last-frame warm-start table into a new layout (one CTA
+// per world): entries of the old table `old_cur[w]` are inserted into table 0
+// of the new one.  Old offsets/sizes of 0 slots mean "no table".
+__global__ void migrate_warm_kernel(const uint32_t* old_keys, const float4* old_vals, const uint32_t* old_off,
+                                    const uint32_t* old_hs, const uint32_t* old_cur, uint32_t* new_keys,
+                                    float4* new_vals, const uint32_t* new_off, const uint32_t* new_hs) {
+    const uint32_t w = blockIdx.x;
+    const uint32_t nh = new_hs[w], oh = old_hs ? old_hs[w] : 0u;
+    uint32_t* nk = new_keys + new_off[w];
+    float4* nv = new_vals + new_off[w];
+    for (uint32_t q = threadIdx.x; q < 2u * nh; q += blockDim.x) nk[q] = 0xFFFFFFFFu;
+    __syncthreads();
+    if (!oh || !nh) return;
+    const uint32_t base = old_off[w] + old_cur[w] * oh;
+    for (uint32_t q = threadIdx.x; q < oh; q += blockDim.x) {
+        const uint32_t key = old_keys[base + q];
+        if (key != 0xFFFFFFFFu) warm_insert(nk, nv, nh, key, old_vals[base + q]);
+    }
+}
+
+cudaError_t launch_migrate_warm(uint32_t nworlds, const uint32_t* old_keys, const float4* old_vals,
+                                const uint32_t* old_off, const uint32_t* old_hs, const uint32_t* old_cur,
+                                uint32_t* new_keys, float4* new_vals, const uint32_t* new_off, const uint32_t* new_hs,
+                                cudaStream_t stream) {
+    if (nworlds == 0) return cudaSuccess;
+    migrate_warm_kernel<<<nworlds, 256, 0, stream>>>(old_keys, old_vals, old_off, old_hs, old_cur, new_keys, new_vals,
+                                                     new_off, new_hs);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_count_call(uint32_t* counter, cudaStream_t stream) {

@@ -13,13 +13,13 @@ from .scenes import NSTATE, Scene, derive_props_state
 
 
 def _config(cell: float, mult: int, debug: bool, stream, capacity_scale: float = 0.0,
-            grid: bool = False, fp64_positions: bool = False) -> N.Config:
+            grid: bool = False, fp64_positions: bool = False, warm_start: bool = False) -> N.Config:
     cfg = N.Config()
     cfg.capacity_scale = float(capacity_scale)
     cfg.spatialhash_cell_width = float(cell)
     cfg.spatialhash_table_size_mult = int(mult)
     cfg.flags = ((N.FLAG_DEBUG_TAPS if debug else 0) | (N.FLAG_GRID_PIPELINE if grid else 0)
-                 | (N.FLAG_FP64_POSITIONS if fp64_positions else 0))
+                 | (N.FLAG_FP64_POSITIONS if fp64_positions else 0) | (N.FLAG_WARM_START if warm_start else 0))
     cfg.stream = int(stream) if stream else None
     return cfg
 
@@ -29,10 +29,10 @@ class World:
     520 bodies, the grid-wide pipeline above that (or always, ``grid=True``)."""
 
     def __init__(self, cell: float = 0.0, mult: int = 0, debug: bool = False, stream=None, capacity_scale: float = 0.0,
-                 grid: bool = False, fp64_positions: bool = False):
+                 grid: bool = False, fp64_positions: bool = False, warm_start: bool = False):
         self._lib = N.load()
         self._h = C.c_void_p()
-        cfg = _config(cell, mult, debug, stream, capacity_scale, grid, fp64_positions)
+        cfg = _config(cell, mult, debug, stream, capacity_scale, grid, fp64_positions, warm_start)
         N.check(self._lib.r2d_solver_create(C.byref(cfg), C.byref(self._h)), "r2d_solver_create")
         self.n = 0
 
@@ -136,10 +136,10 @@ class Batch:
     """Many independent worlds stepped together (r2d_batch_* entry points)."""
 
     def __init__(self, cell: float = 0.0, mult: int = 0, debug: bool = False, stream=None, capacity_scale: float = 0.0,
-                 grid: bool = False, fp64_positions: bool = False):
+                 grid: bool = False, fp64_positions: bool = False, warm_start: bool = False):
         self._lib = N.load()
         self._h = C.c_void_p()
-        cfg = _config(cell, mult, debug, stream, capacity_scale, grid, fp64_positions)
+        cfg = _config(cell, mult, debug, stream, capacity_scale, grid, fp64_positions, warm_start)
         N.check(self._lib.r2d_batch_create(C.byref(cfg), C.byref(self._h)), "r2d_batch_create")
         self.n = 0
         self.nworlds = 0

@@ -63,7 +63,7 @@ def assert_manifolds_equal(gk, gd, gc, ok, od, oc):
         assert cg == co, f"manifold {k}: colour gpu {cg} oracle {co}"
 
 
-def run_pair(sc, steps, check_every=1, debug=True, sub_steps=None, iters=None, **world_kw):
+def run_pair(sc, steps, check_every=1, debug=True, sub_steps=None, iters=None, warm=False, **world_kw):
     """Step scene `sc` on the GPU (one world through the C ABI) and on the
     oracle in colour-major order; compare state, manifolds and colours every
     `check_every` steps.  Returns (world, oracle), or (None, None) when the
@@ -74,8 +74,9 @@ def run_pair(sc, steps, check_every=1, debug=True, sub_steps=None, iters=None, *
 
     S = sc.sub_steps if sub_steps is None else sub_steps
     I = sc.iters if iters is None else iters
-    w = World.from_scene(sc, debug=debug, **world_kw)
+    w = World.from_scene(sc, debug=debug, warm_start=warm, **world_kw)
     o = Oracle.from_scene(sc)
+    o.set_warm_start(warm)
     assert_state_equal(w.read_state(), o.state(), "initial state")
     for s in range(steps):
         want = o.process(sc.dt, S, I, ORDER_COLOUR)
