@@ -1527,7 +1527,8 @@ R2D_API int r2d_batch_launches_per_step(r2d_batch* b, uint32_t* out) {
         int st = b->eng.plan();
         if (st) return st;
     }
-    uint32_t n = (uint32_t)b->eng.classes.size();
+    // one kernel per size class, plus the call counter of the step
+    uint32_t n = (uint32_t)b->eng.classes.size() + (b->eng.classes.empty() ? 0u : 1u);
     for (uint32_t w : b->eng.large_list)
         if (b->eng.large[w]) n += b->eng.large[w]->launches();
     *out = n;
