@@ -924,6 +924,7 @@ struct Engine {
         in.disc_rot = (d.flags & W_DISC_ROTATION) != 0;
         in.pos64 = d_pos64;
         in.warm = warm_start();
+        in.verbose = verbose;
         return in;
     }
 

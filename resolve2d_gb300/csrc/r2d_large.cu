@@ -29,6 +29,9 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <initializer_list>
 #include <string>
@@ -55,22 +58,29 @@ enum LargeCounter : int {
     LC_NONFINITE,      // a body's AABB has no cell index
     LC_COLOURS,        // a constraint needed more than MAX_COLOURS colours
     LC_BIG,            // one body covers more than MAX_CELL_ENTRIES cells
+    LC_PEND0,          // three rotating "still uncoloured" counters of the colouring rounds
+    LC_PEND1,
+    LC_PEND2,
+    LC_DONE,           // a colouring round found the previous one had nothing left
+    LC_ROUNDS,         // the rounds that colouring needed
     LC_N
 };
 
+// pinned host words of a grid step: the counters, the 64-bit entry total,
+// then the colourings' counters and result blocks
+constexpr uint32_t H_COLOUR = LC_N + 2;
+
 inline uint32_t blocks(uint64_t n) { return (uint32_t)std::max<uint64_t>(1, (n + LT - 1) / LT); }
 
-// In-place exclusive scan of a[0..n) by one block of SCAN_THREADS threads;
-// a[n] receives the total.
+// Exclusive scan of one value per thread over a block of SCAN_THREADS
+// threads; *total receives the block's sum.
 constexpr int SCAN_THREADS = 1024;
-__global__ void __launch_bounds__(SCAN_THREADS) lk_scan(uint32_t* a, uint32_t n) {
+constexpr uint32_t SCAN_TILE = 4 * SCAN_THREADS;        // elements per block of the multi-block scan
+constexpr uint32_t SCAN_ONE_BLOCK = 4 * SCAN_TILE;      // longer arrays take the multi-block scan
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* total) {
     __shared__ uint32_t wsum[32];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const uint32_t per = (n + SCAN_THREADS - 1) / SCAN_THREADS;
-    const uint32_t beg = min(n, (uint32_t)tid * per), end = min(n, beg + per);
-    uint32_t s = 0;
-    for (uint32_t i = beg; i < end; ++i) s += a[i];
-    uint32_t x = s;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
@@ -79,22 +89,73 @@ __global__ void __launch_bounds__(SCAN_THREADS) lk_scan(uint32_t* a, uint32_t n)
     if (lane == 31) wsum[warp] = x;
     __syncthreads();
     if (warp == 0) {
-        uint32_t v = wsum[lane];
+        uint32_t w = wsum[lane];
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, v, o);
-            if (lane >= o) v += y;
+            const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
         }
-        wsum[lane] = v;
+        wsum[lane] = w;
     }
     __syncthreads();
-    uint32_t run = (warp ? wsum[warp - 1] : 0u) + x - s;
-    for (uint32_t i = beg; i < end; ++i) {
-        const uint32_t v = a[i];
-        a[i] = run;
-        run += v;
+    const uint32_t r = (warp ? wsum[warp - 1] : 0u) + x - v;
+    *total = wsum[31];
+    __syncthreads();  // wsum is reused by the next call
+    return r;
+}
+
+// In-place exclusive scan of a[0..n) by one block, SCAN_THREADS consecutive
+// elements at a time; a[n] receives the total.
+__global__ void __launch_bounds__(SCAN_THREADS) lk_scan(uint32_t* a, uint32_t n) {
+    uint32_t carry = 0;
+    for (uint32_t at = 0; at < n; at += SCAN_THREADS) {
+        const uint32_t i = at + threadIdx.x;
+        const uint32_t v = i < n ? a[i] : 0u;
+        uint32_t tot;
+        const uint32_t ex = block_exclusive_scan(v, &tot);
+        if (i < n) a[i] = carry + ex;
+        carry += tot;
     }
-    if (tid == SCAN_THREADS - 1) a[n] = wsum[31];
+    if (threadIdx.x == 0) a[n] = carry;
+}
+
+// Multi-block scan, first pass: each block scans its SCAN_TILE elements in
+// place and leaves the tile's sum in tsum[tile].
+__global__ void __launch_bounds__(SCAN_THREADS) lk_scan_tiles(uint32_t* a, uint32_t n, uint32_t* tsum) {
+    const uint32_t base = blockIdx.x * SCAN_TILE;
+    uint32_t carry = 0;
+#pragma unroll 1
+    for (uint32_t k = 0; k < SCAN_TILE; k += SCAN_THREADS) {
+        const uint32_t i = base + k + threadIdx.x;
+        const uint32_t v = i < n ? a[i] : 0u;
+        uint32_t tot;
+        const uint32_t ex = block_exclusive_scan(v, &tot);
+        if (i < n) a[i] = carry + ex;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) tsum[blockIdx.x] = carry;
+}
+
+// Last pass, after tsum[0..tiles) has been scanned (its total at tsum[tiles]).
+__global__ void lk_scan_add(uint32_t* a, uint32_t n, const uint32_t* tsum, uint32_t tiles) {
+    const uint32_t i = blockIdx.x * 256 + threadIdx.x;
+    if (i < n) a[i] += tsum[i / SCAN_TILE];
+    if (i == n) a[n] = tsum[tiles];
+}
+
+// ---------------------------------------------------------------------------
+// one-cluster resident kernels
+// ---------------------------------------------------------------------------
+// The colouring rounds and the colour-by-colour solve are chains of short
+// dependent phases.  One thread-block cluster runs a whole chain and the
+// hardware cluster barrier separates the phases: no launch per phase, no host
+// round trip per few colouring rounds.  The barrier's release/acquire makes
+// each phase's global-memory writes visible to the whole cluster.
+constexpr int RT = 512;                     // threads per CTA of the resident kernels
+constexpr uint32_t RESIDENT_MAX_PASSES = 4;  // colour sizes (in cluster threads) the resident solve takes
+
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;\n" ::: "memory");
 }
 
 // ---------------------------------------------------------------------------
@@ -288,6 +349,7 @@ __global__ void lk_narrow(Phase1 A, uint32_t npairs) {
 // colouring (r2d_colour.h) by Jones-Plassmann rounds
 // ---------------------------------------------------------------------------
 constexpr uint32_t NO_NODE = 0xFFFFFFFFu;
+constexpr uint32_t PRED_ROW = 16;  // earlier neighbours kept per constraint
 
 struct Colouring {
     uint32_t count;
@@ -301,6 +363,8 @@ struct Colouring {
     uint8_t* colour;  // 0xFF = not yet coloured
     uint32_t *adj, *adjl, *prio, *cursor;
     uint32_t* cnt;
+    uint32_t* npred;  // earlier neighbours of each constraint (null: rounds walk the adjacency)
+    uint32_t* preds;  // their indices, PRED_ROW a constraint (those with more walk the adjacency)
 
     __device__ void ends(uint32_t i, uint32_t* a, uint32_t* b) const {
         *a = NO_NODE;
@@ -348,22 +412,69 @@ __global__ void lk_col_fill(Colouring C) {
     C.colour[i] = 0xFFu;
 }
 
-// One round: an uncoloured constraint whose earlier neighbours (in priority
-// order) are all coloured takes the lowest colour none of them holds.  A
-// colour, once written, is final, so reading one written in this same round
-// is as good as reading it next round.
-__global__ void lk_col_round(Colouring C) {
+// Constraint i's neighbours that come before it in priority order, into its
+// row of preds (PRED_ROW entries); npred[i] is their number, which may
+// exceed the row (the rounds then walk the adjacency instead).  A neighbour
+// through both ends is listed twice, which changes no colour.
+__global__ void lk_col_preds(Colouring C) {
     const uint32_t i = blockIdx.x * LT + threadIdx.x;
     if (i >= C.count) return;
+    uint32_t ends[2];
+    C.ends(i, &ends[0], &ends[1]);
+    const uint32_t pi = C.prio[i];
+    const unsigned long long ti = C.tie(i);
+    uint32_t* row = C.preds + (size_t)i * PRED_ROW;
+    uint32_t k = 0;
+    for (int e2 = 0; e2 < 2; ++e2) {
+        const uint32_t x = ends[e2];
+        if (x == NO_NODE) continue;
+        const uint32_t q1 = C.adj[x + 1];
+#pragma unroll 4
+        for (uint32_t q = C.adj[x]; q < q1; ++q) {
+            const uint32_t o = C.adjl[q];
+            if (o == i) continue;
+            const uint32_t po = C.prio[o];
+            if (po > pi || (po == pi && C.tie(o) > ti)) continue;  // comes later
+            if (k < PRED_ROW) row[k] = o;
+            ++k;
+        }
+    }
+    C.npred[i] = k;
+}
+
+// One round's test of constraint i: if every earlier neighbour (in priority
+// order) has a colour, i takes the lowest colour none of them holds.  Returns
+// 1 while i stays uncoloured.  A colour, once written, is final, so reading
+// one written in this same round is as good as reading it next round.
+__device__ uint32_t colour_try(const Colouring& C, uint32_t i) {
     volatile uint8_t* col = C.colour;
-    if (col[i] != 0xFFu) return;
+    if (col[i] != 0xFFu) return 0u;
+    const uint32_t np = C.npred ? C.npred[i] : NO_NODE;
+    if (np <= PRED_ROW) {  // the listed earlier neighbours: independent loads, no walk
+        const uint32_t* row = C.preds + (size_t)i * PRED_ROW;
+        ColourSet used;
+        bool ready = true;
+#pragma unroll 4
+        for (uint32_t q = 0; q < np; ++q) {
+            const uint8_t c = col[row[q]];
+            if (c == 0xFFu) ready = false;
+            else used.add(c);
+        }
+        if (!ready) return 1u;
+        uint32_t c = used.first_free();
+        if (c >= (uint32_t)MAX_COLOURS) {
+            atomicExch(&C.cnt[LC_COLOURS], 1u);
+            c = 0u;
+        }
+        col[i] = (uint8_t)c;
+        return 0u;
+    }
     uint32_t ends[2];
     C.ends(i, &ends[0], &ends[1]);
     const uint32_t pi = C.prio[i];
     const unsigned long long ti = C.tie(i);
     ColourSet used;
-    bool ready = true;
-    for (int e2 = 0; e2 < 2 && ready; ++e2) {
+    for (int e2 = 0; e2 < 2; ++e2) {
         const uint32_t x = ends[e2];
         if (x == NO_NODE) continue;
         const uint32_t q1 = C.adj[x + 1];
@@ -373,16 +484,9 @@ __global__ void lk_col_round(Colouring C) {
             const uint32_t po = C.prio[o];
             if (po > pi || (po == pi && C.tie(o) > ti)) continue;  // comes later
             const uint8_t c = col[o];
-            if (c == 0xFFu) {
-                ready = false;
-                break;
-            }
+            if (c == 0xFFu) return 1u;
             used.add(c);
         }
-    }
-    if (!ready) {
-        atomicAdd(&C.cnt[LC_PENDING], 1u);
-        return;
     }
     uint32_t c = used.first_free();
     if (c >= (uint32_t)MAX_COLOURS) {
@@ -390,19 +494,204 @@ __global__ void lk_col_round(Colouring C) {
         c = 0u;
     }
     col[i] = (uint8_t)c;
+    return 0u;
 }
 
-__global__ void lk_col_hist(Colouring C, uint32_t* hist) {
+// One Jones-Plassmann round over every constraint.  Round r counts the
+// constraints it leaves uncoloured in slot r % 3 and clears slot (r + 1) % 3
+// for the next round.  A round that finds the previous round's count at zero
+// marks the colouring done and returns, so rounds can be queued past the end
+// and the host learns the outcome with one round trip.
+__global__ void lk_col_round(Colouring C, uint32_t round) {
+    volatile uint32_t* cnt = C.cnt;
+    if (cnt[LC_DONE]) return;
+    if (round > 0 && cnt[LC_PEND0 + (round - 1) % 3] == 0u) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            cnt[LC_ROUNDS] = round;
+            cnt[LC_DONE] = 1u;
+        }
+        return;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) cnt[LC_PEND0 + (round + 1) % 3] = 0u;
     const uint32_t i = blockIdx.x * LT + threadIdx.x;
-    if (i >= C.count) return;
-    atomicAdd(&hist[C.colour[i]], 1u);
+    uint32_t waiting = i < C.count ? colour_try(C, i) : 0u;
+    waiting = __reduce_add_sync(0xffffffffu, waiting);
+    if ((threadIdx.x & 31u) == 0 && waiting) atomicAdd(C.cnt + LC_PEND0 + round % 3, waiting);
 }
 
-// colour-major order; inside a colour the order is free (body-disjoint)
-__global__ void lk_col_order(Colouring C, uint32_t* cursor, uint32_t* order) {
+// A colouring's result block (words): per-colour counts, cursors, offsets
+// (colour c is order[off[c], off[c+1])) and the number of colours.
+constexpr uint32_t CB_HIST = 0, CB_CURSOR = MAX_COLOURS, CB_OFF = 2 * MAX_COLOURS, CB_NCOL = 3 * MAX_COLOURS + 1,
+                   CB_WORDS = 4 * MAX_COLOURS;
+constexpr uint32_t H_WORDS = H_COLOUR + 2 * LC_N + 2 * CB_WORDS;
+static_assert(MAX_COLOURS == 128, "the offsets warp scans four colours a lane");
+
+// per-colour counts, one global add per block and colour
+__global__ void lk_col_hist(Colouring C, uint32_t* cb) {
+    __shared__ uint32_t h[MAX_COLOURS];
+    for (uint32_t c = threadIdx.x; c < (uint32_t)MAX_COLOURS; c += LT) h[c] = 0u;
+    __syncthreads();
     const uint32_t i = blockIdx.x * LT + threadIdx.x;
-    if (i >= C.count) return;
-    order[atomicAdd(&cursor[C.colour[i]], 1u)] = i;
+    if (i < C.count) {
+        const uint32_t c = C.colour[i];
+        if (c < (uint32_t)MAX_COLOURS) atomicAdd(&h[c], 1u);
+    }
+    __syncthreads();
+    for (uint32_t c = threadIdx.x; c < (uint32_t)MAX_COLOURS; c += LT)
+        if (h[c]) atomicAdd(&cb[CB_HIST + c], h[c]);
+}
+
+// exclusive offsets of the colours (one warp, four colours a lane)
+__global__ void lk_col_offsets(uint32_t* cb) {
+    const uint32_t lane = threadIdx.x;
+    uint32_t h[4], sum = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        h[k] = cb[CB_HIST + 4 * lane + k];
+        sum += h[k];
+    }
+    uint32_t x = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    uint32_t run = x - sum, top = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        cb[CB_OFF + 4 * lane + k] = run;
+        cb[CB_CURSOR + 4 * lane + k] = run;
+        run += h[k];
+        if (h[k]) top = 4 * lane + k + 1;
+    }
+    top = __reduce_max_sync(0xffffffffu, top);
+    if (lane == 31) cb[CB_OFF + MAX_COLOURS] = x;
+    if (lane == 0) cb[CB_NCOL] = top;
+}
+
+// colour-major order; inside a colour the order is free (body-disjoint), so
+// a block reserves one range per colour and fills it in any order
+__global__ void lk_col_order(Colouring C, uint32_t* cb, uint32_t* order) {
+    __shared__ uint32_t h[MAX_COLOURS], base[MAX_COLOURS];
+    for (uint32_t c = threadIdx.x; c < (uint32_t)MAX_COLOURS; c += LT) h[c] = 0u;
+    __syncthreads();
+    const uint32_t i = blockIdx.x * LT + threadIdx.x;
+    uint32_t c = 0xFFu, rank = 0;
+    if (i < C.count) {
+        c = C.colour[i];
+        if (c < (uint32_t)MAX_COLOURS) rank = atomicAdd(&h[c], 1u);
+    }
+    __syncthreads();
+    for (uint32_t q = threadIdx.x; q < (uint32_t)MAX_COLOURS; q += LT)
+        if (h[q]) base[q] = atomicAdd(&cb[CB_CURSOR + q], h[q]);
+    __syncthreads();
+    if (c < (uint32_t)MAX_COLOURS) order[base[c] + rank] = i;
+}
+
+// Manifolds and their points in colour-major order: manifold k of dst is
+// manifold order[k] of src, and its points are 2k and 2k + 1.  Each colour
+// then is one contiguous range, read with coalesced loads and no index
+// indirection.  Fields the pre-step derives (friction, masses, bias) are not
+// copied.
+__global__ void lk_permute(SWT<uint32_t> src, SWT<uint32_t> dst, const uint32_t* order, uint32_t M) {
+    const uint32_t k = blockIdx.x * LT + threadIdx.x;
+    if (k >= M) return;
+    const uint32_t m = order[k];
+    const uint32_t p0 = src.mp0[m], np = src.mnp[m];
+    dst.ma[k] = src.ma[m];
+    dst.mb[k] = src.mb[m];
+    dst.mp0[k] = 2 * k;
+    dst.mnp[k] = (uint8_t)np;
+    dst.mcol[k] = src.mcol[m];
+    dst.nx[k] = src.nx[m];
+    dst.ny[k] = src.ny[m];
+    for (uint32_t j = 0; j < np; ++j) {
+        const uint32_t p = p0 + j, q = 2 * k + j;
+        dst.r1x[q] = src.r1x[p];
+        dst.r1y[q] = src.r1y[p];
+        dst.r2x[q] = src.r2x[p];
+        dst.r2y[q] = src.r2y[p];
+        dst.depth[q] = src.depth[p];
+        dst.odepth[q] = src.odepth[p];
+        dst.apn[q] = src.apn[p];
+        dst.apt[q] = src.apt[p];
+    }
+}
+
+// calculateImpulses (collision.zig:135-218) of colour-major manifold m
+// (points 2m, 2m + 1): solve_contact's arithmetic in the same order, with
+// both points' loads issued before the first store, so one round trip to
+// memory feeds the manifold instead of one per point.
+__device__ __forceinline__ void solve_contact_cm(const SWT<uint32_t>& s, uint32_t m, bool warm) {
+    const uint32_t a = s.ma[m], b = s.mb[m], np = s.mnp[m];
+    const f2 n = {s.nx[m], s.ny[m]};
+    const float fr = s.fric[m];
+    float bias[2], r1x[2], r1y[2], r2x[2], r2y[2], mn[2], mt[2], apn[2], apt[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {  // slot 1 of a one-point manifold is loaded and not used
+        const uint32_t p = 2 * m + k;
+        bias[k] = s.bias[p];
+        r1x[k] = s.r1x[p];
+        r1y[k] = s.r1y[p];
+        r2x[k] = s.r2x[p];
+        r2y[k] = s.r2y[p];
+        mn[k] = s.mn[p];
+        mt[k] = s.mt[p];
+        apn[k] = s.apn[p];
+        apt[k] = s.apt[p];
+    }
+    const bool sa = s.kind[a] & K_STATIC, sb = s.kind[b] & K_STATIC;
+    const float inv_m1 = s.inv_m[a], inv_m2 = s.inv_m[b];
+    const float inv_i1 = s.inv_i[a], inv_i2 = s.inv_i[b];
+    const f2 vlinear_1 = scale2(f2{s.mx[a], s.my[a]}, inv_m1);
+    const float omega1 = s.L[a] * inv_i1;
+    const f2 vlinear_2 = scale2(f2{s.mx[b], s.my[b]}, inv_m2);
+    const float omega2 = s.L[b] * inv_i2;
+    const f2 t = cw90(n);
+    f2 alp1 = {0.f, 0.f}, alp2 = {0.f, 0.f};
+    float arp1 = 0.f, arp2 = 0.f;
+#pragma unroll
+    for (uint32_t k = 0; k < 2; ++k) {
+        if (k >= np) break;
+        if (bias[k] < 0.0f) continue;  // depth >= 0: accumulators stay 0 (collision.zig:154-158)
+        const f2 r1 = {r1x[k], r1y[k]}, r2 = {r2x[k], r2y[k]};
+        const f2 v1 = add2(vlinear_1, f2{-r1.y * omega1, r1.x * omega1});
+        const f2 v2 = add2(vlinear_2, f2{-r2.y * omega2, r2.x * omega2});
+        const f2 dv = sub2(v1, v2);
+        float num = dot2(dv, n) + bias[k];
+        const float pn = num * mn[k];
+        if (!warm && pn < MIN_MANIFOLD_IMPULSE) continue;
+        num = dot2(dv, t);
+        const float pt = num * mt[k];
+        const float acc = apn[k];
+        const float nacc = zmax(0.0f, acc + pn);
+        const float applied_pn = nacc - acc;
+        s.apn[2 * m + k] = nacc;
+        const float max_pt = fr * fabsf(nacc);
+        const float acct = apt[k];
+        const float nacct = zclamp(acct + pt, -max_pt, max_pt);
+        const float applied_pt = nacct - acct;
+        s.apt[2 * m + k] = nacct;
+        const f2 dp = add2(scale2(n, applied_pn), scale2(t, applied_pt));
+        if (!sa) {
+            alp1 = sub2(alp1, dp);
+            arp1 -= cross2(r1, dp);
+        }
+        if (!sb) {
+            alp2 = add2(alp2, dp);
+            arp2 += cross2(r2, dp);
+        }
+    }
+    if (!sa) {
+        s.mx[a] += alp1.x;
+        s.my[a] += alp1.y;
+        s.L[a] += arp1;
+    }
+    if (!sb) {
+        s.mx[b] += alp2.x;
+        s.my[b] += alp2.y;
+        s.L[b] += arp2;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -431,13 +720,11 @@ struct Phase2 {
 };
 
 // forces (DownwardsGravity.zig:35-39), AABB (last substep), velocities (lib.zig:200-216)
-__global__ void lk_forces(Phase2 A) {
-    const uint32_t i = blockIdx.x * LT + threadIdx.x;
-    if (i >= A.n) return;
+__device__ __forceinline__ void forces_one(const Phase2& A, uint32_t i, bool first, bool last) {
     const SWT<uint32_t>& s = A.s;
     const uint8_t k = s.kind[i];
     float fx = 0.f, fy = 0.f, tq = 0.f;
-    if (A.first) {  // user-set force / torque (RigidBody.zig:73,78)
+    if (first) {  // user-set force / torque (RigidBody.zig:73,78)
         fx = A.st(S_FORCE_X, i);
         fy = A.st(S_FORCE_Y, i);
         tq = A.st(S_TORQUE, i);
@@ -450,7 +737,7 @@ __global__ void lk_forces(Phase2 A) {
             fy += (-A.g[gg]) * s.mass(i);
         }
     }
-    if (A.last) {
+    if (last) {
         float hw, hh;
         if (k & K_RECT) {
             rect_half_extents(A.pr(P_DIM0, i), A.pr(P_DIM1, i), s.cs[i], s.sn[i], &hw, &hh);
@@ -469,10 +756,13 @@ __global__ void lk_forces(Phase2 A) {
     s.tq[i] = tq;
 }
 
+__global__ void lk_forces(Phase2 A) {
+    const uint32_t i = blockIdx.x * LT + threadIdx.x;
+    if (i < A.n) forces_one(A, i, A.first, A.last);
+}
+
 // updateTGSDepth + preStep (collision.zig:73-133)
-__global__ void lk_prestep(Phase2 A) {
-    const uint32_t m = blockIdx.x * LT + threadIdx.x;
-    if (m >= A.nman) return;
+__device__ __forceinline__ void prestep_one(const Phase2& A, uint32_t m) {
     const SWT<uint32_t>& s = A.s;
     const uint32_t a = s.ma[m], b = s.mb[m];
     const f2 n2 = {s.nx[m], s.ny[m]};
@@ -514,10 +804,15 @@ __global__ void lk_prestep(Phase2 A) {
     }
 }
 
+__global__ void lk_prestep(Phase2 A) {
+    const uint32_t m = blockIdx.x * LT + threadIdx.x;
+    if (m < A.nman) prestep_one(A, m);
+}
+
 __global__ void lk_contacts(Phase2 A) {
     const uint32_t k = A.k0 + blockIdx.x * LT + threadIdx.x;
     if (k >= A.k1) return;
-    solve_contact<false>(A.s, A.order[k], A.warm);
+    solve_contact_cm(A.s, k, A.warm);
 }
 
 // ---- warm starting: the world's tables of last frame's impulses ----
@@ -546,7 +841,7 @@ __global__ void lk_warm_load(SWT<uint32_t> s, uint32_t M, const unsigned long lo
 __global__ void lk_warm_apply(Phase2 A) {
     const uint32_t k = A.k0 + blockIdx.x * LT + threadIdx.x;
     if (k >= A.k1) return;
-    warm_apply_contact<false>(A.s, A.order[k]);
+    warm_apply_contact<false>(A.s, k);
 }
 
 __global__ void lk_warm_clear(unsigned long long* keys, uint32_t hs) {
@@ -572,17 +867,17 @@ __global__ void lk_warm_copy(const uint32_t* keys, const float4* vals, uint32_t 
     if (key != 0xFFFFFFFFu) warm_insert(nkeys, nvals, nhs, warm_key64(key >> 16, key & 0xFFFFu), vals[q]);
 }
 
-__global__ void lk_joints(Phase2 A) {
-    const uint32_t k = A.k0 + blockIdx.x * LT + threadIdx.x;
-    if (k >= A.k1) return;
-    const uint32_t j = A.order[k];
+__device__ __forceinline__ void joint_one(const Phase2& A, uint32_t j) {
     solve_joint(A.s, __ldg(A.jtype + j), __ldg(A.jb1 + j), __ldg(A.jb2 + j), A.jprm + (size_t)j * JOINT_PARAMS, A.h);
 }
 
+__global__ void lk_joints(Phase2 A) {
+    const uint32_t k = A.k0 + blockIdx.x * LT + threadIdx.x;
+    if (k < A.k1) joint_one(A, A.order[k]);
+}
+
 // integration (lib.zig:238-249); the last substep clears consumed forces
-__global__ void lk_integrate(Phase2 A) {
-    const uint32_t i = blockIdx.x * LT + threadIdx.x;
-    if (i >= A.n) return;
+__device__ __forceinline__ void integrate_one(const Phase2& A, uint32_t i, bool last) {
     const SWT<uint32_t>& s = A.s;
     s.ang_prev[i] = s.ang[i];
     const uint8_t k = s.kind[i];
@@ -597,16 +892,70 @@ __global__ void lk_integrate(Phase2 A) {
         s.ang[i] += s.L[i] * A.h / s.inertia(i);
     }
     s.tq[i] = 0.f;
-    if (!A.last && ((k & K_RECT) || A.disc_rot)) {
+    if (!last && ((k & K_RECT) || A.disc_rot)) {
         float c, sn;
         r2d_sincosf(s.ang[i], &sn, &c);
         s.cs[i] = c;
         s.sn[i] = sn;
     }
-    if (A.last && (k & K_FORCED)) {
+    if (last && (k & K_FORCED)) {
         A.st(S_FORCE_X, i) = 0.f;
         A.st(S_FORCE_Y, i) = 0.f;
         A.st(S_TORQUE, i) = 0.f;
+    }
+}
+
+__global__ void lk_integrate(Phase2 A) {
+    const uint32_t i = blockIdx.x * LT + threadIdx.x;
+    if (i < A.n) integrate_one(A, i, A.last);
+}
+
+// The colour offsets of one step: contact colour c is manifolds [coff[c],
+// coff[c+1]) (colour-major), joint colour c is jorder[joff[c], joff[c+1]).
+struct ResidentPlan {
+    const uint32_t* jorder;
+    const uint32_t* coff;
+    const uint32_t* joff;
+    uint32_t ncol, njcol, sub_steps, iters;
+};
+
+// Every substep of the step in one cluster (lib.zig:199-250): the same
+// per-item functions as the one-launch-per-phase kernels, in the same order.
+// A body's integration and its next substep's forces touch only that body,
+// so they share a phase; so do the forces and the pre-step (the pre-step
+// reads no momentum).
+__global__ void __launch_bounds__(RT, 1) lk_substeps_resident(Phase2 A, ResidentPlan R) {
+    const uint32_t t0 = blockIdx.x * RT + threadIdx.x, nt = gridDim.x * RT;
+    for (uint32_t sub = 0; sub < R.sub_steps; ++sub) {
+        const bool first = sub == 0, last = sub + 1 == R.sub_steps;
+        if (first)
+            for (uint32_t i = t0; i < A.n; i += nt) forces_one(A, i, true, last);
+        for (uint32_t m = t0; m < A.nman; m += nt) prestep_one(A, m);
+        cluster_sync_all();
+        if (A.warm && first) {
+            for (uint32_t c = 0; c < R.ncol; ++c) {
+                const uint32_t k1 = R.coff[c + 1];
+                for (uint32_t k = R.coff[c] + t0; k < k1; k += nt) warm_apply_contact<false>(A.s, k);
+                cluster_sync_all();
+            }
+        }
+        for (uint32_t it = 0; it < R.iters; ++it) {
+            for (uint32_t c = 0; c < R.njcol; ++c) {
+                const uint32_t k1 = R.joff[c + 1];
+                for (uint32_t k = R.joff[c] + t0; k < k1; k += nt) joint_one(A, R.jorder[k]);
+                cluster_sync_all();
+            }
+            for (uint32_t c = 0; c < R.ncol; ++c) {
+                const uint32_t k1 = R.coff[c + 1];
+                for (uint32_t k = R.coff[c] + t0; k < k1; k += nt) solve_contact_cm(A.s, k, A.warm);
+                cluster_sync_all();
+            }
+        }
+        for (uint32_t i = t0; i < A.n; i += nt) {
+            integrate_one(A, i, last);
+            if (!last) forces_one(A, i, false, sub + 2 == R.sub_steps);
+        }
+        if (!last) cluster_sync_all();
     }
 }
 
@@ -673,6 +1022,88 @@ cudaError_t regrow(size_t& cap, size_t need, std::initializer_list<Buf> bufs) {
     return cudaSuccess;
 }
 
+constexpr int MAX_DEVICES = 64;
+std::atomic<int> g_cluster_size[2][MAX_DEVICES];  // [resident kernel][device]; 0 = not known yet
+
+// The cluster size of a resident kernel: 16 CTAs where the device can hold
+// such a cluster with the kernel's resources, else the portable 8.  Found
+// once per device and kernel.
+template <class... P>
+cudaError_t resident_cluster(int which, void (*kernel)(P...), int* out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= MAX_DEVICES) return cudaErrorInvalidDevice;
+    int cl = g_cluster_size[which][dev].load();
+    if (cl == 0) {
+        cl = 8;
+        if (cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
+            cudaLaunchConfig_t cfg{};
+            cfg.gridDim = dim3(16);
+            cfg.blockDim = dim3(RT);
+            cudaLaunchAttribute at{};
+            at.id = cudaLaunchAttributeClusterDimension;
+            at.val.clusterDim.x = 16;
+            at.val.clusterDim.y = 1;
+            at.val.clusterDim.z = 1;
+            cfg.attrs = &at;
+            cfg.numAttrs = 1;
+            int nc = 0;
+            if (cudaOccupancyMaxActiveClusters(&nc, kernel, &cfg) == cudaSuccess && nc > 0) cl = 16;
+        }
+        (void)cudaGetLastError();  // a refused probe leaves no error behind
+        g_cluster_size[which][dev].store(cl);
+    }
+    *out = cl;
+    return cudaSuccess;
+}
+
+// One cluster of `cl` CTAs: the whole grid of a resident kernel.
+template <class... P, class... A>
+cudaError_t launch_resident(void (*kernel)(P...), int cl, cudaStream_t st, A... args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(cl);
+    cfg.blockDim = dim3(RT);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute at{};
+    at.id = cudaLaunchAttributeClusterDimension;
+    at.val.clusterDim.x = cl;
+    at.val.clusterDim.y = 1;
+    at.val.clusterDim.z = 1;
+    cfg.attrs = &at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
+// Exclusive scan of a[0..n) (a[n] = total): one block for short arrays, else
+// tiles, their sums (tsum, ceil(n / SCAN_TILE) + 1 words) and a fix-up.
+cudaError_t scan(uint32_t* a, uint32_t n, uint32_t* tsum, cudaStream_t st, uint32_t* nlaunch) {
+    if (n <= SCAN_ONE_BLOCK || !tsum) {
+        lk_scan<<<1, SCAN_THREADS, 0, st>>>(a, n);
+        *nlaunch += 1;
+    } else {
+        const uint32_t tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+        lk_scan_tiles<<<tiles, SCAN_THREADS, 0, st>>>(a, n, tsum);
+        lk_scan<<<1, SCAN_THREADS, 0, st>>>(tsum, tiles);
+        lk_scan_add<<<(n + 256) / 256, 256, 0, st>>>(a, n, tsum, tiles);
+        *nlaunch += 3;
+    }
+    return cudaGetLastError();
+}
+
+// Whether the substeps run as one resident cluster or as one launch per
+// phase and colour (R2D_RESIDENT=0 / 1 forces either).  The cluster wins
+// while its threads cover a colour in a few passes.
+bool use_resident_substeps(uint32_t largest_colour, int cl) {
+    static const int forced = [] {
+        const char* e = getenv("R2D_RESIDENT");
+        return e && *e ? atoi(e) : -1;
+    }();
+    if (forced >= 0) return forced != 0;
+    return largest_colour <= RESIDENT_MAX_PASSES * (uint32_t)cl * RT;
+}
+
 }  // namespace
 
 struct LargeWorld::Impl {
@@ -693,13 +1124,26 @@ struct LargeWorld::Impl {
     float *nx = nullptr, *ny = nullptr, *fric = nullptr;
     float *r1x = nullptr, *r1y = nullptr, *r2x = nullptr, *r2y = nullptr, *depth = nullptr, *odepth = nullptr;
     float *mn = nullptr, *mt = nullptr, *apn = nullptr, *apt = nullptr, *bias = nullptr;
+    // the permutation's second copy of the fields it moves (swapped with the first after each step's permutation)
+    uint32_t *ma2 = nullptr, *mb2 = nullptr, *mp02 = nullptr;
+    uint8_t *mnp2 = nullptr, *mcol2 = nullptr;
+    float *nx2 = nullptr, *ny2 = nullptr;
+    float *r1x2 = nullptr, *r1y2 = nullptr, *r2x2 = nullptr, *r2y2 = nullptr, *depth2 = nullptr, *odepth2 = nullptr,
+          *apn2 = nullptr, *apt2 = nullptr;
     // colouring
     uint32_t *adjl = nullptr, *prio = nullptr;
+    uint32_t *jadj = nullptr, *jadjl = nullptr, *jprio = nullptr;  // the joints' own adjacency
+    uint32_t *npred = nullptr, *jnpred = nullptr, *preds = nullptr, *jpreds = nullptr;
+    size_t cap_pr = 0, cap_prr = 0;
     uint8_t* jcol = nullptr;
     uint32_t* jorder = nullptr;
-    uint32_t* cnt = nullptr;                // LargeCounter
+    uint32_t* cnt = nullptr;                // LargeCounter; a second block for the joint colouring
     unsigned long long* entries = nullptr;  // total cell entries
-    uint32_t* hist = nullptr;               // [MAX_COLOURS + 1]
+    uint32_t* hist = nullptr;               // two colouring result blocks (contacts, joints)
+    uint32_t* tsum = nullptr;               // tile sums of the multi-block scan
+    size_t cap_ts = 0;
+    int cl_solve = 0;                       // cluster size of the resident substeps
+    uint32_t round_hint[2] = {32, 32};      // colouring rounds to queue (contacts, joints): last step's + 2
     uint32_t* h_cnt = nullptr;              // pinned: counters, then the entry total
     // debug taps
     uint32_t *dk = nullptr, *dc = nullptr;
@@ -720,7 +1164,9 @@ struct LargeWorld::Impl {
         void* ps[] = {inv_m, inv_i, cs, sn, tq, ang_prev, kind, rx0, ry0, rx1, ry1, bcnt, adj, cursor,
                       table, ebucket, ebody, eslot, sbody, hset, pairs, ma, mb, mp0, corder, mnp, mcol,
                       nx, ny, fric, r1x, r1y, r2x, r2y, depth, odepth, mn, mt, apn, apt, bias, adjl, prio,
-                      jcol, jorder, cnt, entries, hist, dk, dc, dd};
+                      jcol, jorder, cnt, entries, hist, tsum, dk, dc, dd, ma2, mb2, mp02, mnp2, mcol2, nx2, ny2,
+                      r1x2, r1y2, r2x2, r2y2, depth2, odepth2, apn2, apt2, jadj, jadjl, jprio, npred, jnpred,
+                      preds, jpreds};
         for (void* p : ps)
             if (p) cudaFree(p);
         for (int b = 0; b < 2; ++b) {
@@ -751,6 +1197,20 @@ struct LargeWorld::Impl {
         s.depth = depth; s.odepth = odepth; s.mn = mn; s.mt = mt; s.apn = apn; s.apt = apt; s.bias = bias;
         return s;
     }
+    // the permutation's destination: views() with the second copies
+    SWT<uint32_t> shadow_views(const LargeInputs& in) const {
+        SWT<uint32_t> s = views(in);
+        s.ma = ma2; s.mb = mb2; s.mp0 = mp02; s.mnp = mnp2; s.mcol = mcol2; s.nx = nx2; s.ny = ny2;
+        s.r1x = r1x2; s.r1y = r1y2; s.r2x = r2x2; s.r2y = r2y2; s.depth = depth2; s.odepth = odepth2;
+        s.apn = apn2; s.apt = apt2;
+        return s;
+    }
+    void swap_shadow() {
+        std::swap(ma, ma2); std::swap(mb, mb2); std::swap(mp0, mp02); std::swap(mnp, mnp2); std::swap(mcol, mcol2);
+        std::swap(nx, nx2); std::swap(ny, ny2); std::swap(r1x, r1x2); std::swap(r1y, r1y2); std::swap(r2x, r2x2);
+        std::swap(r2y, r2y2); std::swap(depth, depth2); std::swap(odepth, odepth2); std::swap(apn, apn2);
+        std::swap(apt, apt2);
+    }
 };
 
 LargeWorld::LargeWorld() : impl(new Impl()) {}
@@ -769,17 +1229,17 @@ LargeWorld::~LargeWorld() { delete impl; }
         kernel<<<(grid), LT, 0, st>>>(__VA_ARGS__); \
         ++I.nlaunch;                                \
     } while (0)
-// the scan is one block of exactly SCAN_THREADS threads
-#define SCAN(a, n)                                      \
-    do {                                                \
-        lk_scan<<<1, SCAN_THREADS, 0, st>>>((a), (n));  \
-        ++I.nlaunch;                                    \
-    } while (0)
+#define SCAN(a, n) LTRY(scan((a), (n), I.tsum, st, &I.nlaunch))
 
 int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32_t iters, cudaStream_t st,
                      std::string* msg) {
     Impl& I = *impl;
     const uint32_t n = in.n;
+    const auto t_start = std::chrono::steady_clock::now();
+    double t_ms[5] = {0, 0, 0, 0, 0};  // cells+entries, pairs, narrowphase, colouring, substeps (verbose)
+    auto mark = [&](int k) {
+        t_ms[k] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+    };
     I.nman = 0;
     I.nj = 0;
     I.nlaunch = 0;
@@ -787,16 +1247,18 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
     I.joff.assign(1, 0u);
     if (n == 0) return 0;
     const uint32_t T = in.table_mult * n;
-    if (!I.h_cnt) LTRY(cudaMallocHost((void**)&I.h_cnt, sizeof(uint32_t) * (LC_N + 2)));
+    if (!I.h_cnt) LTRY(cudaMallocHost((void**)&I.h_cnt, sizeof(uint32_t) * H_WORDS));
     if (!I.cnt) {
-        LTRY(cudaMalloc((void**)&I.cnt, sizeof(uint32_t) * LC_N));
+        LTRY(cudaMalloc((void**)&I.cnt, sizeof(uint32_t) * 2 * LC_N));
         LTRY(cudaMalloc((void**)&I.entries, sizeof(unsigned long long)));
-        LTRY(cudaMalloc((void**)&I.hist, sizeof(uint32_t) * (MAX_COLOURS + 1)));
+        LTRY(cudaMalloc((void**)&I.hist, sizeof(uint32_t) * 2 * CB_WORDS));
+        LTRY(resident_cluster(0, lk_substeps_resident, &I.cl_solve));
     }
     LTRY(regrow(I.cap_n, (size_t)n + 1,
                 {LB(I.inv_m), LB(I.inv_i), LB(I.cs), LB(I.sn), LB(I.tq), LB(I.ang_prev), LB(I.kind), LB(I.rx0),
-                 LB(I.ry0), LB(I.rx1), LB(I.ry1), LB(I.bcnt), LB(I.adj), LB(I.cursor)}));
+                 LB(I.ry0), LB(I.rx1), LB(I.ry1), LB(I.bcnt), LB(I.adj), LB(I.jadj), LB(I.cursor)}));
     LTRY(regrow(I.cap_t, (size_t)T + 1, {LB(I.table)}));
+    LTRY(regrow(I.cap_ts, std::max(n, T) / SCAN_TILE + 2, {LB(I.tsum)}));
 
     Phase1 A{};
     A.s = I.views(in);
@@ -827,6 +1289,7 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
         return DS_CAPACITY;
     }
     const uint32_t E = (uint32_t)E64;
+    mark(0);
     LTRY(regrow(I.cap_e, (size_t)E + 1, {LB(I.ebucket), LB(I.ebody), LB(I.eslot), LB(I.sbody)}));
     A.ebucket = I.ebucket; A.ebody = I.ebody; A.eslot = I.eslot; A.sbody = I.sbody;
     SCAN(I.bcnt, n);
@@ -860,13 +1323,15 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
         I.pair_scale *= std::max(1.5, 1.25 * (double)I.h_cnt[LC_PAIRS] / (double)np);
     }
 
+    mark(1);
     // ---- narrowphase: at most one manifold per pair, two points per manifold ----
     LTRY(regrow(I.cap_m, (size_t)npairs + 1,
                 {LB(I.ma), LB(I.mb), LB(I.mp0), LB(I.corder), LB(I.mnp), LB(I.mcol), LB(I.nx), LB(I.ny),
-                 LB(I.fric)}));
+                 LB(I.fric), LB(I.ma2), LB(I.mb2), LB(I.mp02), LB(I.mnp2), LB(I.mcol2), LB(I.nx2), LB(I.ny2)}));
     LTRY(regrow(I.cap_pt, 2 * (size_t)npairs + 1,
                 {LB(I.r1x), LB(I.r1y), LB(I.r2x), LB(I.r2y), LB(I.depth), LB(I.odepth), LB(I.mn), LB(I.mt),
-                 LB(I.apn), LB(I.apt), LB(I.bias)}));
+                 LB(I.apn), LB(I.apt), LB(I.bias), LB(I.r1x2), LB(I.r1y2), LB(I.r2x2), LB(I.r2y2), LB(I.depth2),
+                 LB(I.odepth2), LB(I.apn2), LB(I.apt2)}));
     A.s = I.views(in);
     A.nm = npairs;
     A.npt = 2 * npairs;
@@ -875,68 +1340,118 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
     LTRY(cudaMemcpyAsync(I.h_cnt, I.cnt, sizeof(uint32_t) * LC_N, cudaMemcpyDeviceToHost, st));
     LTRY(cudaStreamSynchronize(st));
     const uint32_t M = I.h_cnt[LC_MANIFOLDS];
+    mark(2);
 
-    // ---- colouring: contacts, then joints ----
-    LTRY(regrow(I.cap_c, 2 * (size_t)std::max(M, in.nj) + 2, {LB(I.adjl), LB(I.prio)}));
+    // ---- colouring: contacts, then joints (Jones-Plassmann rounds) ----
+    // Each colouring queues the rounds its previous step needed, then its
+    // counts, offsets and order; one round trip then checks both, and only a
+    // colouring that needed more rounds queues more.
+    LTRY(regrow(I.cap_c, 2 * (size_t)std::max(M, in.nj) + 2,
+                {LB(I.adjl), LB(I.prio), LB(I.jadjl), LB(I.jprio)}));
     LTRY(regrow(I.cap_j, (size_t)in.nj + 1, {LB(I.jcol), LB(I.jorder)}));
-    auto colour = [&](bool joints, uint32_t count, uint8_t* col, uint32_t* order, std::vector<uint32_t>& off) -> int {
-        off.assign(1, 0u);
-        if (count == 0) return 0;
-        Colouring C{};
+    LTRY(regrow(I.cap_pr, (size_t)std::max(M, in.nj) + 1, {LB(I.npred), LB(I.jnpred)}));
+    LTRY(regrow(I.cap_prr, ((size_t)std::max(M, in.nj) + 1) * PRED_ROW, {LB(I.preds), LB(I.jpreds)}));
+    LTRY(cudaMemsetAsync(I.cnt, 0, sizeof(uint32_t) * 2 * LC_N, st));
+    struct ColourJob {
+        Colouring C;
+        uint32_t* cb;
+        uint32_t* order;
+        uint32_t rounds;  // rounds queued so far
+        bool active;
+    };
+    uint32_t* cb_c = I.hist;
+    uint32_t* cb_j = I.hist + CB_WORDS;
+    auto finish = [&](ColourJob& J) -> int {  // counts, offsets, order (after any queued rounds)
+        const uint32_t count = J.C.count;
+        LTRY(cudaMemsetAsync(J.cb, 0, sizeof(uint32_t) * CB_WORDS, st));
+        LAUNCH(lk_col_hist, blocks(count), J.C, J.cb);
+        lk_col_offsets<<<1, 32, 0, st>>>(J.cb);
+        ++I.nlaunch;
+        LAUNCH(lk_col_order, blocks(count), J.C, J.cb, J.order);
+        return 0;
+    };
+    auto start = [&](ColourJob& J, bool joints, uint32_t count, uint8_t* col, uint32_t* order, uint32_t* cb,
+                     uint32_t* cnt, uint32_t* adj, uint32_t* adjl, uint32_t* prio, uint32_t* npred, uint32_t* preds,
+                     uint32_t hint) -> int {
+        J.cb = cb;
+        J.order = order;
+        J.rounds = 0;
+        J.active = count > 0;
+        LTRY(cudaMemsetAsync(cb, 0, sizeof(uint32_t) * CB_WORDS, st));
+        if (!J.active) return 0;
+        Colouring& C = J.C;
+        C = Colouring{};
         C.count = count;
         C.joints = joints;
         C.jtype = in.jtype; C.jb1 = in.jb1; C.jb2 = in.jb2;
         C.ma = I.ma; C.mb = I.mb; C.kind = I.kind; C.colour = col;
-        C.adj = I.adj; C.adjl = I.adjl; C.prio = I.prio; C.cursor = I.cursor; C.cnt = I.cnt;
-        LTRY(cudaMemsetAsync(I.adj, 0, sizeof(uint32_t) * ((size_t)n + 1), st));
-        LTRY(cudaMemsetAsync(I.cnt, 0, sizeof(uint32_t) * LC_N, st));
+        C.adj = adj; C.adjl = adjl; C.prio = prio; C.cursor = I.cursor; C.cnt = cnt;
+        C.npred = npred; C.preds = preds;
+        LTRY(cudaMemsetAsync(adj, 0, sizeof(uint32_t) * ((size_t)n + 1), st));
         LAUNCH(lk_col_count, blocks(count), C);
-        SCAN(I.adj, n);
-        LTRY(cudaMemcpyAsync(I.cursor, I.adj, sizeof(uint32_t) * ((size_t)n + 1), cudaMemcpyDeviceToDevice, st));
+        SCAN(adj, n);
+        LTRY(cudaMemcpyAsync(I.cursor, adj, sizeof(uint32_t) * ((size_t)n + 1), cudaMemcpyDeviceToDevice, st));
         LAUNCH(lk_col_fill, blocks(count), C);
-        // Each round colours at least the highest-priority uncoloured
-        // constraint, so `count` rounds always finish; random priorities
-        // need a few dozen.
-        for (uint32_t rounds = 0;;) {
-            for (int r = 0; r < 4; ++r) {
-                LTRY(cudaMemsetAsync(I.cnt + LC_PENDING, 0, sizeof(uint32_t), st));
-                LAUNCH(lk_col_round, blocks(count), C);
-            }
-            rounds += 4;
-            LTRY(cudaMemcpyAsync(I.h_cnt, I.cnt, sizeof(uint32_t) * LC_N, cudaMemcpyDeviceToHost, st));
-            LTRY(cudaStreamSynchronize(st));
-            if (I.h_cnt[LC_COLOURS]) {
+        LAUNCH(lk_col_preds, blocks(count), C);
+        for (uint32_t r = 0; r < hint; ++r) LAUNCH(lk_col_round, blocks(count), C, r);
+        J.rounds = hint;
+        return finish(J);
+    };
+    ColourJob jobs[2];
+    if (int r = start(jobs[0], false, M, I.mcol, I.corder, cb_c, I.cnt, I.adj, I.adjl, I.prio, I.npred, I.preds,
+                      I.round_hint[0]))
+        return r;
+    if (int r = start(jobs[1], true, in.nj, I.jcol, I.jorder, cb_j, I.cnt + LC_N, I.jadj, I.jadjl, I.jprio,
+                      I.jnpred, I.jpreds, I.round_hint[1]))
+        return r;
+    uint32_t* hc = I.h_cnt + H_COLOUR;  // both counter blocks, then both result blocks
+    for (;;) {
+        LTRY(cudaMemcpyAsync(hc, I.cnt, sizeof(uint32_t) * 2 * LC_N, cudaMemcpyDeviceToHost, st));
+        LTRY(cudaMemcpyAsync(hc + 2 * LC_N, I.hist, sizeof(uint32_t) * 2 * CB_WORDS, cudaMemcpyDeviceToHost, st));
+        LTRY(cudaStreamSynchronize(st));
+        bool again = false;
+        for (int j = 0; j < 2; ++j) {
+            ColourJob& J = jobs[j];
+            if (!J.active) continue;
+            const uint32_t* h = hc + j * LC_N;
+            if (h[LC_COLOURS]) {
                 *msg = "a constraint needs more than " + std::to_string(MAX_COLOURS) + " colours";
                 return DS_CAPACITY;
             }
-            if (I.h_cnt[LC_PENDING] == 0) break;
-            if (rounds > count + 4) {
+            if (h[LC_DONE] || h[LC_PEND0 + (J.rounds - 1) % 3] == 0u) {
+                I.round_hint[j] = (h[LC_DONE] ? h[LC_ROUNDS] : J.rounds) + 2;
+                J.active = false;
+                continue;
+            }
+            // each round colours at least the highest-priority uncoloured constraint
+            if (J.rounds > J.C.count + 1) {
                 *msg = "the colouring did not finish";
                 return -4;
             }
+            const uint32_t more = std::max(8u, J.rounds / 2);
+            for (uint32_t r = 0; r < more; ++r) LAUNCH(lk_col_round, blocks(J.C.count), J.C, J.rounds + r);
+            J.rounds += more;
+            if (int r = finish(J)) return r;
+            again = true;
         }
-        std::vector<uint32_t> hist(MAX_COLOURS + 1, 0u);
-        LTRY(cudaMemsetAsync(I.hist, 0, sizeof(uint32_t) * (MAX_COLOURS + 1), st));
-        LAUNCH(lk_col_hist, blocks(count), C, I.hist);
-        LTRY(cudaMemcpyAsync(hist.data(), I.hist, sizeof(uint32_t) * (MAX_COLOURS + 1), cudaMemcpyDeviceToHost, st));
-        LTRY(cudaStreamSynchronize(st));
-        uint32_t ncol = 0;
-        for (uint32_t c = 0; c < (uint32_t)MAX_COLOURS; ++c)
-            if (hist[c]) ncol = c + 1;
-        off.assign(ncol + 1, 0u);
-        for (uint32_t c = 0; c < ncol; ++c) off[c + 1] = off[c] + hist[c];
-        LTRY(cudaMemcpyAsync(I.hist, off.data(), sizeof(uint32_t) * (ncol + 1), cudaMemcpyHostToDevice, st));
-        LAUNCH(lk_col_order, blocks(count), C, I.hist, order);
-        // `off` is the source of the copy above: wait before it can change
-        LTRY(cudaStreamSynchronize(st));
-        return 0;
+        if (!again) break;
+    }
+    uint32_t largest = 0;
+    auto offsets = [&](const uint32_t* cb, std::vector<uint32_t>& off) {
+        const uint32_t ncol = cb[CB_NCOL];
+        off.assign(cb + CB_OFF, cb + CB_OFF + ncol + 1);
+        for (uint32_t c = 0; c < ncol; ++c) largest = std::max(largest, off[c + 1] - off[c]);
     };
-    int cst = colour(false, M, I.mcol, I.corder, I.coff);
-    if (cst) return cst;
-    cst = colour(true, in.nj, I.jcol, I.jorder, I.joff);
-    if (cst) return cst;
+    offsets(hc + 2 * LC_N, I.coff);
+    offsets(hc + 2 * LC_N + CB_WORDS, I.joff);
     I.nman = M;
     I.nj = in.nj;
+    // manifolds in colour-major order: colour c is manifolds [coff[c], coff[c+1])
+    if (M) {
+        LAUNCH(lk_permute, blocks(M), I.views(in), I.shadow_views(in), I.corder, M);
+        I.swap_shadow();
+    }
+    mark(3);
 
     if (in.warm && M && I.whs[I.wcur]) {
         LAUNCH(lk_warm_load, blocks(M), I.views(in), M, I.wkeys[I.wcur], I.wvals[I.wcur], I.whs[I.wcur]);
@@ -960,7 +1475,17 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
     S.jtype = in.jtype; S.jb1 = in.jb1; S.jb2 = in.jb2; S.jprm = in.jprm;
     S.pos64 = in.pos64;
     S.warm = in.warm;
-    for (uint32_t sub = 0; sub < sub_steps; ++sub) {
+    const bool resident = use_resident_substeps(largest, I.cl_solve);
+    if (resident) {
+        ResidentPlan R{};
+        R.jorder = I.jorder;
+        R.coff = cb_c + CB_OFF; R.joff = cb_j + CB_OFF;
+        R.ncol = (uint32_t)I.coff.size() - 1; R.njcol = (uint32_t)I.joff.size() - 1;
+        R.sub_steps = sub_steps; R.iters = iters;
+        LTRY(launch_resident(lk_substeps_resident, I.cl_solve, st, S, R));
+        ++I.nlaunch;
+    }
+    for (uint32_t sub = 0; sub < sub_steps && !resident; ++sub) {
         S.first = sub == 0;
         S.last = sub + 1 == sub_steps;
         LAUNCH(lk_forces, blocks(n), S);
@@ -996,6 +1521,17 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
         I.wcur = wnext;
     }
     LTRY(cudaGetLastError());
+    if (in.verbose) {
+        LTRY(cudaStreamSynchronize(st));
+        mark(4);
+        fprintf(stderr,
+                "r2d grid step: %u bodies, %u entries, %u pairs, %u manifolds, %zu contact colours, %zu joint colours, "
+                "largest colour %u, %s substeps, %u launches | ms: cells %.3f pairs %.3f narrow %.3f colour %.3f "
+                "substeps %.3f\n",
+                n, E, npairs, M, I.coff.size() - 1, I.joff.size() - 1, largest,
+                resident ? "resident" : "per-colour", I.nlaunch, t_ms[0], t_ms[1] - t_ms[0], t_ms[2] - t_ms[1],
+                t_ms[3] - t_ms[2], t_ms[4] - t_ms[3]);
+    }
     return 0;
 }
 
@@ -1075,6 +1611,7 @@ struct StaticLayout {
     size_t ma, mb, mp0, corder, mnp, mcol, nx, ny, fric;
     size_t r1x, r1y, r2x, r2y, depth, odepth, mn, mt, apn, apt, bias;
     size_t adjl, prio, jcol, jorder, cnt, entries, hist;
+    size_t ma2, mb2, mp02, mnp2, mcol2, nx2, ny2, r1x2, r1y2, r2x2, r2y2, depth2, odepth2, apn2, apt2;
     size_t total;
 };
 
@@ -1105,7 +1642,12 @@ constexpr StaticLayout static_layout() {
     L.adjl = c.take<uint32_t>(2 * (size_t)SX_PAIRS + 2); L.prio = c.take<uint32_t>(2 * (size_t)SX_PAIRS + 2);
     L.jcol = c.take<uint8_t>(1); L.jorder = c.take<uint32_t>(1);
     L.cnt = c.take<uint32_t>(LC_N); L.entries = c.take<unsigned long long>(1);
-    L.hist = c.take<uint32_t>(MAX_COLOURS + 1);
+    L.hist = c.take<uint32_t>(CB_WORDS);
+    L.ma2 = c.take<uint32_t>(np); L.mb2 = c.take<uint32_t>(np); L.mp02 = c.take<uint32_t>(np);
+    L.mnp2 = c.take<uint8_t>(np); L.mcol2 = c.take<uint8_t>(np); L.nx2 = c.take<float>(np); L.ny2 = c.take<float>(np);
+    L.r1x2 = c.take<float>(npt); L.r1y2 = c.take<float>(npt); L.r2x2 = c.take<float>(npt);
+    L.r2y2 = c.take<float>(npt); L.depth2 = c.take<float>(npt); L.odepth2 = c.take<float>(npt);
+    L.apn2 = c.take<float>(npt); L.apt2 = c.take<float>(npt);
     L.total = c.off;
     return L;
 }
@@ -1242,10 +1784,13 @@ int static_world_step(const StaticStepArgs& in, cudaStream_t st, std::string* ms
     LTRY(cudaStreamSynchronize(st));
     const uint32_t M = h[LC_MANIFOLDS];
 
-    // contact colouring (Jones-Plassmann rounds), colour-major order
-    uint32_t coff[MAX_COLOURS + 1];
+    // contact colouring (Jones-Plassmann rounds, queued STATIC_ROUNDS at a
+    // time), the colour-major permutation, then the substeps in one resident
+    // cluster
+    constexpr uint32_t STATIC_ROUNDS = 32;
+    int cl_solve = 0;
+    LTRY(resident_cluster(0, lk_substeps_resident, &cl_solve));
     uint32_t ncol = 0;
-    coff[0] = 0;
     if (M) {
         Colouring C{};
         C.count = M;
@@ -1260,34 +1805,35 @@ int static_world_step(const StaticStepArgs& in, cudaStream_t st, std::string* ms
         LTRY(cudaMemcpyAsync(C.cursor, C.adj, sizeof(uint32_t) * ((size_t)n + 1), cudaMemcpyDeviceToDevice, st));
         LAUNCH(lk_col_fill, blocks(M), C);
         for (uint32_t rounds = 0;;) {
-            for (int r = 0; r < 4; ++r) {
-                LTRY(cudaMemsetAsync(cnt + LC_PENDING, 0, sizeof(uint32_t), st));
-                LAUNCH(lk_col_round, blocks(M), C);
-            }
-            rounds += 4;
+            for (uint32_t r = 0; r < STATIC_ROUNDS; ++r) LAUNCH(lk_col_round, blocks(M), C, rounds + r);
+            rounds += STATIC_ROUNDS;
             LTRY(cudaMemcpyAsync(h, cnt, sizeof(uint32_t) * LC_N, cudaMemcpyDeviceToHost, st));
             LTRY(cudaStreamSynchronize(st));
             if (h[LC_COLOURS]) {
                 *msg = "a contact needs more than " + std::to_string(MAX_COLOURS) + " colours";
                 return DS_CAPACITY;
             }
-            if (h[LC_PENDING] == 0) break;
-            if (rounds > M + 4) {
+            if (h[LC_DONE] || h[LC_PEND0 + (rounds - 1) % 3] == 0u) break;
+            if (rounds > M + 1) {
                 *msg = "the colouring did not finish";
                 return -4;
             }
         }
-        uint32_t hh[MAX_COLOURS + 1];
-        LTRY(cudaMemsetAsync(hist, 0, sizeof(uint32_t) * (MAX_COLOURS + 1), st));
+        LTRY(cudaMemsetAsync(hist, 0, sizeof(uint32_t) * CB_WORDS, st));
         LAUNCH(lk_col_hist, blocks(M), C, hist);
-        LTRY(cudaMemcpyAsync(hh, hist, sizeof(uint32_t) * (MAX_COLOURS + 1), cudaMemcpyDeviceToHost, st));
-        LTRY(cudaStreamSynchronize(st));
-        for (uint32_t c = 0; c < (uint32_t)MAX_COLOURS; ++c)
-            if (hh[c]) ncol = c + 1;
-        for (uint32_t c = 0; c < ncol; ++c) coff[c + 1] = coff[c] + hh[c];
-        LTRY(cudaMemcpyAsync(hist, coff, sizeof(uint32_t) * (ncol + 1), cudaMemcpyHostToDevice, st));
+        lk_col_offsets<<<1, 32, 0, st>>>(hist);
         LAUNCH(lk_col_order, blocks(M), C, hist, SP(uint32_t, corder));
-        LTRY(cudaStreamSynchronize(st));  // coff is the source of the copy above
+        LTRY(cudaMemcpyAsync(h + LC_N, hist + CB_NCOL, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        // manifolds in colour-major order (into the second copies, which the substeps then use)
+        SWT<uint32_t> d = s;
+        d.ma = SP(uint32_t, ma2); d.mb = SP(uint32_t, mb2); d.mp0 = SP(uint32_t, mp02); d.mnp = SP(uint8_t, mnp2);
+        d.mcol = SP(uint8_t, mcol2); d.nx = SP(float, nx2); d.ny = SP(float, ny2);
+        d.r1x = SP(float, r1x2); d.r1y = SP(float, r1y2); d.r2x = SP(float, r2x2); d.r2y = SP(float, r2y2);
+        d.depth = SP(float, depth2); d.odepth = SP(float, odepth2); d.apn = SP(float, apn2); d.apt = SP(float, apt2);
+        LAUNCH(lk_permute, blocks(M), s, d, SP(uint32_t, corder), M);
+        s = d;
+        LTRY(cudaStreamSynchronize(st));
+        ncol = h[LC_N];
     }
 
     // substeps: the caller's state changes from here on
@@ -1298,20 +1844,12 @@ int static_world_step(const StaticStepArgs& in, cudaStream_t st, std::string* ms
     P.disc_rot = false;
     P.ngrav = in.ngrav;
     for (int k = 0; k < MAX_GRAVITY; ++k) P.g[k] = in.g[k];
-    P.order = SP(uint32_t, corder);
-    for (uint32_t sub = 0; sub < in.sub_steps; ++sub) {
-        P.first = sub == 0;
-        P.last = sub + 1 == in.sub_steps;
-        LAUNCH(lk_forces, blocks(n), P);
-        if (M) LAUNCH(lk_prestep, blocks(M), P);
-        for (uint32_t it = 0; it < in.iters; ++it)
-            for (uint32_t c = 0; c < ncol; ++c) {
-                P.k0 = coff[c];
-                P.k1 = coff[c + 1];
-                LAUNCH(lk_contacts, blocks(P.k1 - P.k0), P);
-            }
-        LAUNCH(lk_integrate, blocks(n), P);
-    }
+    ResidentPlan R{};
+    R.jorder = nullptr;
+    R.coff = hist + CB_OFF; R.joff = nullptr;
+    R.ncol = ncol; R.njcol = 0;
+    R.sub_steps = in.sub_steps; R.iters = in.iters;
+    LTRY(launch_resident(lk_substeps_resident, cl_solve, st, P, R));
 #undef SP
     LTRY(cudaGetLastError());
     return 0;

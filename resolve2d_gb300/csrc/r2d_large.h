@@ -36,6 +36,7 @@ struct LargeInputs {
     bool disc_rot;         // some joint reads disc orientations
     double* pos64;         // [3][NB] f64 pose (FP64-positions mode), else null
     bool warm;             // warm starting (the world keeps its impulses across calls)
+    bool verbose;          // print each step's phase times and counts to stderr
 };
 
 class LargeWorld {
@@ -70,7 +71,7 @@ private:
 #define R2D_STATIC_MAX_BODIES 4096u
 #define R2D_STATIC_MAX_CELL_ENTRIES 65536u
 #define R2D_STATIC_MAX_PAIRS 16384u
-#define R2D_STATIC_SCRATCH_BYTES 3899392ull  // 3.72 MiB
+#define R2D_STATIC_SCRATCH_BYTES 5313536ull  // 5.07 MiB
 
 struct StaticStepArgs {
     float* state;          // [S_NFIELDS][n], device
