@@ -238,7 +238,7 @@ R2D_API int r2d_batch_get_manifolds(r2d_batch* b, uint32_t w, uint32_t cap, uint
  * array of ngrav <= 4 magnitudes; cell_width 0 and table_mult 0 select 4.0
  * and 2.
  *
- * Scratch lives in one static device array of 5,313,536 bytes (5.07 MiB),
+ * Scratch lives in one static device array of 7,216,128 bytes (6.88 MiB),
  * which every GPU that loads this library holds until the process exits.
  * Limits: 4,096 bodies, 65,536 spatial-hash cell entries, 16,384 candidate
  * pairs, no joints or exclusions; a world beyond them returns

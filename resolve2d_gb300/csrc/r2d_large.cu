@@ -61,8 +61,8 @@ enum LargeCounter : int {
     LC_PEND0,          // three rotating "still uncoloured" counters of the colouring rounds
     LC_PEND1,
     LC_PEND2,
-    LC_DONE,           // a colouring round found the previous one had nothing left
     LC_ROUNDS,         // the rounds that colouring needed
+    LC_STUCK,          // a colouring ran more rounds than it has constraints (cannot happen)
     LC_N
 };
 
@@ -192,8 +192,10 @@ __global__ void lk_load(Phase1 A) {
     const uint8_t k = __ldg(A.kind_in + A.base + i);
     const float a = A.st(S_ANGLE, i);
     A.s.kind[i] = k;
-    A.s.inv_m[i] = (k & K_STATIC) ? 0.f : 1.0f / A.pr(P_MASS, i);
-    A.s.inv_i[i] = (k & K_STATIC) ? 0.f : 1.0f / A.pr(P_INERTIA, i);
+    const float inv_m = (k & K_STATIC) ? 0.f : 1.0f / A.pr(P_MASS, i);
+    const float inv_i = (k & K_STATIC) ? 0.f : 1.0f / A.pr(P_INERTIA, i);
+    A.s.inv_m[i] = inv_m;
+    A.s.inv_i[i] = inv_i;
     float c = 1.f, sn = 0.f;
     if ((k & K_RECT) || A.disc_rot) r2d_sincosf(a, &sn, &c);
     A.s.cs[i] = c;
@@ -261,16 +263,18 @@ __device__ __forceinline__ bool lk_excluded(const unsigned long long* ex, uint32
 
 // Candidates: every two entries of one bucket, filtered as lib.zig:273-282,
 // deduplicated like its "manifold already exists" test (lib.zig:278-281).
+// One warp per entry; its lanes take the bucket's later entries 32 at a time.
 __global__ void lk_pairs(Phase1 A, uint32_t E) {
-    const uint32_t e = blockIdx.x * LT + threadIdx.x;
-    if (e >= E) return;
+    const uint64_t w = ((uint64_t)blockIdx.x * LT + threadIdx.x) >> 5;
+    if (w >= E) return;
+    const uint32_t e = (uint32_t)w, lane = threadIdx.x & 31u;
     const uint32_t i = A.ebody[e];
     const uint32_t end = A.table[A.ebucket[e]];
     const f2 pi = {A.st(S_AABB_X, i), A.st(S_AABB_Y, i)};
     const float hwi = A.st(S_AABB_HW, i), hhi = A.st(S_AABB_HH, i);
     const bool sti = (A.s.kind[i] & K_STATIC) != 0;
     const unsigned long long mask = (unsigned long long)A.hs - 1ull;
-    for (uint32_t q = A.eslot[e] + 1u; q < end; ++q) {
+    for (uint32_t q = A.eslot[e] + 1u + lane; q < end; q += 32u) {
         const uint32_t j = A.sbody[q];
         if (j == i) continue;
         if (sti && (A.s.kind[j] & K_STATIC)) continue;
@@ -349,7 +353,7 @@ __global__ void lk_narrow(Phase1 A, uint32_t npairs) {
 // colouring (r2d_colour.h) by Jones-Plassmann rounds
 // ---------------------------------------------------------------------------
 constexpr uint32_t NO_NODE = 0xFFFFFFFFu;
-constexpr uint32_t PRED_ROW = 16;  // earlier neighbours kept per constraint
+constexpr uint32_t PRED_ROW = 32;  // earlier neighbours kept per constraint (a 14-contact body pair has 23)
 
 struct Colouring {
     uint32_t count;
@@ -365,6 +369,7 @@ struct Colouring {
     uint32_t* cnt;
     uint32_t* npred;  // earlier neighbours of each constraint (null: rounds walk the adjacency)
     uint32_t* preds;  // their indices, PRED_ROW a constraint (those with more walk the adjacency)
+    uint32_t* wl[2];  // worklists of the constraints a round left uncoloured (null: rounds scan all)
 
     __device__ void ends(uint32_t i, uint32_t* a, uint32_t* b) const {
         *a = NO_NODE;
@@ -445,10 +450,14 @@ __global__ void lk_col_preds(Colouring C) {
 // One round's test of constraint i: if every earlier neighbour (in priority
 // order) has a colour, i takes the lowest colour none of them holds.  Returns
 // 1 while i stays uncoloured.  A colour, once written, is final, so reading
-// one written in this same round is as good as reading it next round.
+// one written in this same round is as good as reading it next round, and a
+// stale read only defers i by a round: the colours are read from L2
+// (ld.global.cg), which sees every earlier round's writes.  (A volatile load
+// here would be a system-scope access, several microseconds apiece on a
+// coherent CPU-GPU node.)
 __device__ uint32_t colour_try(const Colouring& C, uint32_t i) {
-    volatile uint8_t* col = C.colour;
-    if (col[i] != 0xFFu) return 0u;
+    const uint8_t* col = C.colour;
+    if (__ldcg(col + i) != 0xFFu) return 0u;
     const uint32_t np = C.npred ? C.npred[i] : NO_NODE;
     if (np <= PRED_ROW) {  // the listed earlier neighbours: independent loads, no walk
         const uint32_t* row = C.preds + (size_t)i * PRED_ROW;
@@ -456,7 +465,7 @@ __device__ uint32_t colour_try(const Colouring& C, uint32_t i) {
         bool ready = true;
 #pragma unroll 4
         for (uint32_t q = 0; q < np; ++q) {
-            const uint8_t c = col[row[q]];
+            const uint8_t c = __ldcg(col + row[q]);
             if (c == 0xFFu) ready = false;
             else used.add(c);
         }
@@ -466,7 +475,7 @@ __device__ uint32_t colour_try(const Colouring& C, uint32_t i) {
             atomicExch(&C.cnt[LC_COLOURS], 1u);
             c = 0u;
         }
-        col[i] = (uint8_t)c;
+        C.colour[i] = (uint8_t)c;
         return 0u;
     }
     uint32_t ends[2];
@@ -483,7 +492,7 @@ __device__ uint32_t colour_try(const Colouring& C, uint32_t i) {
             if (o == i) continue;
             const uint32_t po = C.prio[o];
             if (po > pi || (po == pi && C.tie(o) > ti)) continue;  // comes later
-            const uint8_t c = col[o];
+            const uint8_t c = __ldcg(col + o);
             if (c == 0xFFu) return 1u;
             used.add(c);
         }
@@ -493,30 +502,54 @@ __device__ uint32_t colour_try(const Colouring& C, uint32_t i) {
         atomicExch(&C.cnt[LC_COLOURS], 1u);
         c = 0u;
     }
-    col[i] = (uint8_t)c;
+    C.colour[i] = (uint8_t)c;
     return 0u;
 }
 
-// One Jones-Plassmann round over every constraint.  Round r counts the
-// constraints it leaves uncoloured in slot r % 3 and clears slot (r + 1) % 3
-// for the next round.  A round that finds the previous round's count at zero
-// marks the colouring done and returns, so rounds can be queued past the end
-// and the host learns the outcome with one round trip.
-__global__ void lk_col_round(Colouring C, uint32_t round) {
-    volatile uint32_t* cnt = C.cnt;
-    if (cnt[LC_DONE]) return;
-    if (round > 0 && cnt[LC_PEND0 + (round - 1) % 3] == 0u) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            cnt[LC_ROUNDS] = round;
-            cnt[LC_DONE] = 1u;
+// Every Jones-Plassmann round, in one cluster (lib.zig's constraint order
+// through r2d_colour.h's priorities).  Round r counts the constraints it
+// leaves uncoloured in slot r % 3 and clears slot (r + 1) % 3 for the next
+// round; with worklists it takes round r - 1's list (wl[(r + 1) & 1], as
+// many entries as slot (r - 1) % 3 counts) and appends its own uncoloured
+// constraints to wl[r & 1], so later rounds touch only open constraints.
+// Every thread reads a slot only between the barrier after the round that
+// fills it and the next barrier, and the slot is cleared two rounds later,
+// so all threads see the same count and leave the loop together.  Expects
+// slot 0 zeroed.
+__global__ void __launch_bounds__(RT, 1) lk_colour_cluster(Colouring C) {
+    const uint32_t t0 = blockIdx.x * RT + threadIdx.x, nt = gridDim.x * RT;
+    const uint32_t lane = threadIdx.x & 31u;
+    const bool listed = C.wl[0] != nullptr;
+    uint32_t* cnt = C.cnt;
+    uint32_t open = C.count;
+    for (uint32_t round = 0;; ++round) {
+        if (t0 == 0) cnt[LC_PEND0 + (round + 1) % 3] = 0u;
+        const uint32_t* in = listed && round > 0 ? C.wl[(round + 1) & 1] : nullptr;
+        uint32_t* out = listed ? C.wl[round & 1] : nullptr;
+        const uint32_t span = listed ? open : C.count;
+        for (uint32_t at = 0; at < span; at += nt) {  // uniform trip count: the ballot sees whole warps
+            const uint32_t t = at + t0;
+            const uint32_t i = (in && t < span) ? __ldcg(in + t) : t;
+            const bool waiting = t < span && colour_try(C, i) != 0u;
+            const uint32_t mask = __ballot_sync(0xffffffffu, waiting);
+            if (mask == 0u) continue;
+            uint32_t slot = 0;
+            if (lane == 0) slot = atomicAdd(cnt + LC_PEND0 + round % 3, (uint32_t)__popc(mask));
+            slot = __shfl_sync(0xffffffffu, slot, 0);
+            if (out && waiting) out[slot + __popc(mask & ((1u << lane) - 1u))] = i;
         }
-        return;
+        cluster_sync_all();
+        open = __ldcg(cnt + LC_PEND0 + round % 3);
+        if (open == 0u) {
+            if (t0 == 0) cnt[LC_ROUNDS] = round + 1;
+            break;
+        }
+        // each round colours at least the highest-priority uncoloured constraint
+        if (round >= C.count) {
+            if (t0 == 0) cnt[LC_STUCK] = 1u;
+            break;
+        }
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) cnt[LC_PEND0 + (round + 1) % 3] = 0u;
-    const uint32_t i = blockIdx.x * LT + threadIdx.x;
-    uint32_t waiting = i < C.count ? colour_try(C, i) : 0u;
-    waiting = __reduce_add_sync(0xffffffffu, waiting);
-    if ((threadIdx.x & 31u) == 0 && waiting) atomicAdd(C.cnt + LC_PEND0 + round % 3, waiting);
 }
 
 // A colouring's result block (words): per-colour counts, cursors, offsets
@@ -618,35 +651,53 @@ __global__ void lk_permute(SWT<uint32_t> src, SWT<uint32_t> dst, const uint32_t*
     }
 }
 
-// calculateImpulses (collision.zig:135-218) of colour-major manifold m
-// (points 2m, 2m + 1): solve_contact's arithmetic in the same order, with
-// both points' loads issued before the first store, so one round trip to
-// memory feeds the manifold instead of one per point.
-__device__ __forceinline__ void solve_contact_cm(const SWT<uint32_t>& s, uint32_t m, bool warm) {
-    const uint32_t a = s.ma[m], b = s.mb[m], np = s.mnp[m];
-    const f2 n = {s.nx[m], s.ny[m]};
-    const float fr = s.fric[m];
-    float bias[2], r1x[2], r1y[2], r2x[2], r2y[2], mn[2], mt[2], apn[2], apt[2];
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {  // slot 1 of a one-point manifold is loaded and not used
-        const uint32_t p = 2 * m + k;
-        bias[k] = s.bias[p];
-        r1x[k] = s.r1x[p];
-        r1y[k] = s.r1y[p];
-        r2x[k] = s.r2x[p];
-        r2y[k] = s.r2y[p];
-        mn[k] = s.mn[p];
-        mt[k] = s.mt[p];
-        apn[k] = s.apn[p];
-        apt[k] = s.apt[p];
+// The contact solve's records: per colour-major manifold seven float4 (v0 =
+// bodies and normal, v1 = friction, point count and static flags, biases,
+// v2 / v3 = the lever arms of points 0 / 1, v4 = their effective masses,
+// v5 = their accumulated impulses, live during the step, v6 = both bodies'
+// 1/mass and 1/inertia).  A warp reads each with one coalesced 16-byte load
+// instead of a scalar load per field, and the per-body constants come with
+// the manifold instead of from two scattered bodies.  mom4, when set, holds
+// each body's live momentum {px, py, L, 0} during the step (one scattered
+// load and store per body instead of three); worlds with joints or warm
+// starting keep it in the state rows, which their other solvers use.
+struct Packed {
+    float4 *v0, *v1, *v2, *v3, *v4, *v5, *v6;
+    float4* mom4;
+};
+constexpr uint32_t PK_NP = 0xFFu, PK_STATIC_A = 0x100u, PK_STATIC_B = 0x200u;  // v1.y bits
+
+// calculateImpulses (collision.zig:135-218) of colour-major manifold m from
+// its packed record: solve_contact's arithmetic in the same order.  Seven
+// coalesced record loads are issued together, then the two bodies'
+// momenta; the accumulators go back as one store.
+template <bool MOM4>
+__device__ __forceinline__ void solve_contact_packed(const Packed& pk, float* mx, float* my, float* L, uint32_t m,
+                                                     bool warm) {
+    const float4 v0 = pk.v0[m], v1 = pk.v1[m], v2 = pk.v2[m], v3 = pk.v3[m], v4 = pk.v4[m], v5 = pk.v5[m],
+                 v6 = pk.v6[m];
+    const uint32_t a = __float_as_uint(v0.x), b = __float_as_uint(v0.y), flags = __float_as_uint(v1.y);
+    const uint32_t np = flags & PK_NP;
+    const bool sa = flags & PK_STATIC_A, sb = flags & PK_STATIC_B;
+    const f2 n = {v0.z, v0.w};
+    const float fr = v1.x;
+    const float bias[2] = {v1.z, v1.w};
+    const f2 r1s[2] = {{v2.x, v2.y}, {v3.x, v3.y}}, r2s[2] = {{v2.z, v2.w}, {v3.z, v3.w}};
+    const float mn[2] = {v4.x, v4.z}, mt[2] = {v4.y, v4.w};
+    float apn[2] = {v5.x, v5.z}, apt[2] = {v5.y, v5.w};
+    const float inv_m1 = v6.x, inv_i1 = v6.y, inv_m2 = v6.z, inv_i2 = v6.w;
+    float4 ma4, mb4;
+    if (MOM4) {
+        ma4 = pk.mom4[a];
+        mb4 = pk.mom4[b];
+    } else {
+        ma4 = make_float4(mx[a], my[a], L[a], 0.f);
+        mb4 = make_float4(mx[b], my[b], L[b], 0.f);
     }
-    const bool sa = s.kind[a] & K_STATIC, sb = s.kind[b] & K_STATIC;
-    const float inv_m1 = s.inv_m[a], inv_m2 = s.inv_m[b];
-    const float inv_i1 = s.inv_i[a], inv_i2 = s.inv_i[b];
-    const f2 vlinear_1 = scale2(f2{s.mx[a], s.my[a]}, inv_m1);
-    const float omega1 = s.L[a] * inv_i1;
-    const f2 vlinear_2 = scale2(f2{s.mx[b], s.my[b]}, inv_m2);
-    const float omega2 = s.L[b] * inv_i2;
+    const f2 vlinear_1 = scale2(f2{ma4.x, ma4.y}, inv_m1);
+    const float omega1 = ma4.z * inv_i1;
+    const f2 vlinear_2 = scale2(f2{mb4.x, mb4.y}, inv_m2);
+    const float omega2 = mb4.z * inv_i2;
     const f2 t = cw90(n);
     f2 alp1 = {0.f, 0.f}, alp2 = {0.f, 0.f};
     float arp1 = 0.f, arp2 = 0.f;
@@ -654,7 +705,7 @@ __device__ __forceinline__ void solve_contact_cm(const SWT<uint32_t>& s, uint32_
     for (uint32_t k = 0; k < 2; ++k) {
         if (k >= np) break;
         if (bias[k] < 0.0f) continue;  // depth >= 0: accumulators stay 0 (collision.zig:154-158)
-        const f2 r1 = {r1x[k], r1y[k]}, r2 = {r2x[k], r2y[k]};
+        const f2 r1 = r1s[k], r2 = r2s[k];
         const f2 v1 = add2(vlinear_1, f2{-r1.y * omega1, r1.x * omega1});
         const f2 v2 = add2(vlinear_2, f2{-r2.y * omega2, r2.x * omega2});
         const f2 dv = sub2(v1, v2);
@@ -666,12 +717,12 @@ __device__ __forceinline__ void solve_contact_cm(const SWT<uint32_t>& s, uint32_
         const float acc = apn[k];
         const float nacc = zmax(0.0f, acc + pn);
         const float applied_pn = nacc - acc;
-        s.apn[2 * m + k] = nacc;
+        apn[k] = nacc;
         const float max_pt = fr * fabsf(nacc);
         const float acct = apt[k];
         const float nacct = zclamp(acct + pt, -max_pt, max_pt);
         const float applied_pt = nacct - acct;
-        s.apt[2 * m + k] = nacct;
+        apt[k] = nacct;
         const f2 dp = add2(scale2(n, applied_pn), scale2(t, applied_pt));
         if (!sa) {
             alp1 = sub2(alp1, dp);
@@ -682,16 +733,31 @@ __device__ __forceinline__ void solve_contact_cm(const SWT<uint32_t>& s, uint32_
             arp2 += cross2(r2, dp);
         }
     }
+    pk.v5[m] = make_float4(apn[0], apt[0], apn[1], apt[1]);
     if (!sa) {
-        s.mx[a] += alp1.x;
-        s.my[a] += alp1.y;
-        s.L[a] += arp1;
+        if (MOM4) {
+            pk.mom4[a] = make_float4(ma4.x + alp1.x, ma4.y + alp1.y, ma4.z + arp1, 0.f);
+        } else {
+            mx[a] = ma4.x + alp1.x;
+            my[a] = ma4.y + alp1.y;
+            L[a] = ma4.z + arp1;
+        }
     }
     if (!sb) {
-        s.mx[b] += alp2.x;
-        s.my[b] += alp2.y;
-        s.L[b] += arp2;
+        if (MOM4) {
+            pk.mom4[b] = make_float4(mb4.x + alp2.x, mb4.y + alp2.y, mb4.z + arp2, 0.f);
+        } else {
+            mx[b] = mb4.x + alp2.x;
+            my[b] = mb4.y + alp2.y;
+            L[b] = mb4.z + arp2;
+        }
     }
+}
+
+__device__ __forceinline__ void solve_contact_packed(const Packed& pk, float* mx, float* my, float* L, uint32_t m,
+                                                     bool warm) {
+    if (pk.mom4) solve_contact_packed<true>(pk, mx, my, L, m, warm);
+    else solve_contact_packed<false>(pk, mx, my, L, m, warm);
 }
 
 // ---------------------------------------------------------------------------
@@ -699,6 +765,7 @@ __device__ __forceinline__ void solve_contact_cm(const SWT<uint32_t>& s, uint32_
 // ---------------------------------------------------------------------------
 struct Phase2 {
     SWT<uint32_t> s;
+    Packed pk;
     float* state;
     const float* props;
     uint32_t NB, base, n, nman;
@@ -749,11 +816,13 @@ __device__ __forceinline__ void forces_one(const Phase2& A, uint32_t i, bool fir
         A.st(S_AABB_HW, i) = hw;
         A.st(S_AABB_HH, i) = hh;
     }
-    if (k & K_STATIC) return;
-    s.mx[i] += fx * A.h;
-    s.my[i] += fy * A.h;
-    s.L[i] += tq * A.h;
-    s.tq[i] = tq;
+    if (!(k & K_STATIC)) {
+        s.mx[i] += fx * A.h;
+        s.my[i] += fy * A.h;
+        s.L[i] += tq * A.h;
+        s.tq[i] = tq;
+    }
+    if (A.pk.mom4) A.pk.mom4[i] = make_float4(s.mx[i], s.my[i], s.L[i], 0.f);
 }
 
 __global__ void lk_forces(Phase2 A) {
@@ -804,15 +873,59 @@ __device__ __forceinline__ void prestep_one(const Phase2& A, uint32_t m) {
     }
 }
 
+// The solve's record of colour-major manifold m (points 2m, 2m + 1), from
+// the fields the pre-step just wrote (slot 1 of a one-point manifold carries
+// whatever it holds, unused).  The first substep also starts the live
+// accumulators from the manifold's stored ones, except that a point with
+// depth >= 0 (bias < 0) starts from zero, as the warm start leaves it.
+__device__ __forceinline__ void pack_one(const Phase2& A, uint32_t m, bool first) {
+    const SWT<uint32_t>& s = A.s;
+    const uint32_t p = 2 * m;
+    const float b0 = s.bias[p], b1 = s.bias[p + 1];
+    const uint32_t a = s.ma[m], b = s.mb[m];
+    const uint32_t flags = (uint32_t)s.mnp[m] | ((s.kind[a] & K_STATIC) ? PK_STATIC_A : 0u) |
+                           ((s.kind[b] & K_STATIC) ? PK_STATIC_B : 0u);
+    A.pk.v0[m] = make_float4(__uint_as_float(a), __uint_as_float(b), s.nx[m], s.ny[m]);
+    A.pk.v1[m] = make_float4(s.fric[m], __uint_as_float(flags), b0, b1);
+    A.pk.v6[m] = make_float4(s.inv_m[a], s.inv_i[a], s.inv_m[b], s.inv_i[b]);
+    A.pk.v2[m] = make_float4(s.r1x[p], s.r1y[p], s.r2x[p], s.r2y[p]);
+    A.pk.v3[m] = make_float4(s.r1x[p + 1], s.r1y[p + 1], s.r2x[p + 1], s.r2y[p + 1]);
+    A.pk.v4[m] = make_float4(s.mn[p], s.mt[p], s.mn[p + 1], s.mt[p + 1]);
+    if (first) {
+        const bool z0 = b0 < 0.0f, z1 = b1 < 0.0f;
+        A.pk.v5[m] = make_float4(z0 ? 0.f : s.apn[p], z0 ? 0.f : s.apt[p], z1 ? 0.f : s.apn[p + 1],
+                                 z1 ? 0.f : s.apt[p + 1]);
+    }
+}
+
+// the live accumulators back into the manifold's fields (end of the step)
+__device__ __forceinline__ void unpack_one(const Phase2& A, uint32_t m) {
+    const float4 v = A.pk.v5[m];
+    const uint32_t p = 2 * m, np = A.s.mnp[m];
+    A.s.apn[p] = v.x;
+    A.s.apt[p] = v.y;
+    if (np > 1) {
+        A.s.apn[p + 1] = v.z;
+        A.s.apt[p + 1] = v.w;
+    }
+}
+
 __global__ void lk_prestep(Phase2 A) {
     const uint32_t m = blockIdx.x * LT + threadIdx.x;
-    if (m < A.nman) prestep_one(A, m);
+    if (m >= A.nman) return;
+    prestep_one(A, m);
+    pack_one(A, m, A.first);
+}
+
+__global__ void lk_unpack(Phase2 A) {
+    const uint32_t m = blockIdx.x * LT + threadIdx.x;
+    if (m < A.nman) unpack_one(A, m);
 }
 
 __global__ void lk_contacts(Phase2 A) {
     const uint32_t k = A.k0 + blockIdx.x * LT + threadIdx.x;
     if (k >= A.k1) return;
-    solve_contact_cm(A.s, k, A.warm);
+    solve_contact_packed(A.pk, A.s.mx, A.s.my, A.s.L, k, A.warm);
 }
 
 // ---- warm starting: the world's tables of last frame's impulses ----
@@ -882,6 +995,12 @@ __device__ __forceinline__ void integrate_one(const Phase2& A, uint32_t i, bool 
     s.ang_prev[i] = s.ang[i];
     const uint8_t k = s.kind[i];
     if (k & K_STATIC) return;
+    if (A.pk.mom4) {  // the solve's momentum back into the state rows
+        const float4 q = A.pk.mom4[i];
+        s.mx[i] = q.x;
+        s.my[i] = q.y;
+        s.L[i] = q.z;
+    }
     if (A.pos64) {
         integrate_pose64(A.pos64, A.NB, A.base + i, s.mx[i], s.my[i], s.L[i], A.h, s.mass(i), s.inertia(i), &s.px[i],
                          &s.py[i], &s.ang[i]);
@@ -930,7 +1049,10 @@ __global__ void __launch_bounds__(RT, 1) lk_substeps_resident(Phase2 A, Resident
         const bool first = sub == 0, last = sub + 1 == R.sub_steps;
         if (first)
             for (uint32_t i = t0; i < A.n; i += nt) forces_one(A, i, true, last);
-        for (uint32_t m = t0; m < A.nman; m += nt) prestep_one(A, m);
+        for (uint32_t m = t0; m < A.nman; m += nt) {
+            prestep_one(A, m);
+            pack_one(A, m, first);
+        }
         cluster_sync_all();
         if (A.warm && first) {
             for (uint32_t c = 0; c < R.ncol; ++c) {
@@ -947,7 +1069,8 @@ __global__ void __launch_bounds__(RT, 1) lk_substeps_resident(Phase2 A, Resident
             }
             for (uint32_t c = 0; c < R.ncol; ++c) {
                 const uint32_t k1 = R.coff[c + 1];
-                for (uint32_t k = R.coff[c] + t0; k < k1; k += nt) solve_contact_cm(A.s, k, A.warm);
+                for (uint32_t k = R.coff[c] + t0; k < k1; k += nt)
+                    solve_contact_packed(A.pk, A.s.mx, A.s.my, A.s.L, k, A.warm);
                 cluster_sync_all();
             }
         }
@@ -957,6 +1080,7 @@ __global__ void __launch_bounds__(RT, 1) lk_substeps_resident(Phase2 A, Resident
         }
         if (!last) cluster_sync_all();
     }
+    for (uint32_t m = t0; m < A.nman; m += nt) unpack_one(A, m);
 }
 
 // debug taps in the oracle's manifold layout (DebugOut)
@@ -1124,6 +1248,8 @@ struct LargeWorld::Impl {
     float *nx = nullptr, *ny = nullptr, *fric = nullptr;
     float *r1x = nullptr, *r1y = nullptr, *r2x = nullptr, *r2y = nullptr, *depth = nullptr, *odepth = nullptr;
     float *mn = nullptr, *mt = nullptr, *apn = nullptr, *apt = nullptr, *bias = nullptr;
+    float4* pk[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // Packed records
+    float4* mom4 = nullptr;
     // the permutation's second copy of the fields it moves (swapped with the first after each step's permutation)
     uint32_t *ma2 = nullptr, *mb2 = nullptr, *mp02 = nullptr;
     uint8_t *mnp2 = nullptr, *mcol2 = nullptr;
@@ -1134,6 +1260,7 @@ struct LargeWorld::Impl {
     uint32_t *adjl = nullptr, *prio = nullptr;
     uint32_t *jadj = nullptr, *jadjl = nullptr, *jprio = nullptr;  // the joints' own adjacency
     uint32_t *npred = nullptr, *jnpred = nullptr, *preds = nullptr, *jpreds = nullptr;
+    uint32_t *wl0 = nullptr, *wl1 = nullptr, *jwl0 = nullptr, *jwl1 = nullptr;  // colouring worklists
     size_t cap_pr = 0, cap_prr = 0;
     uint8_t* jcol = nullptr;
     uint32_t* jorder = nullptr;
@@ -1142,8 +1269,7 @@ struct LargeWorld::Impl {
     uint32_t* hist = nullptr;               // two colouring result blocks (contacts, joints)
     uint32_t* tsum = nullptr;               // tile sums of the multi-block scan
     size_t cap_ts = 0;
-    int cl_solve = 0;                       // cluster size of the resident substeps
-    uint32_t round_hint[2] = {32, 32};      // colouring rounds to queue (contacts, joints): last step's + 2
+    int cl_solve = 0, cl_colour = 0;        // cluster sizes of the resident substeps and colouring
     uint32_t* h_cnt = nullptr;              // pinned: counters, then the entry total
     // debug taps
     uint32_t *dk = nullptr, *dc = nullptr;
@@ -1166,7 +1292,7 @@ struct LargeWorld::Impl {
                       nx, ny, fric, r1x, r1y, r2x, r2y, depth, odepth, mn, mt, apn, apt, bias, adjl, prio,
                       jcol, jorder, cnt, entries, hist, tsum, dk, dc, dd, ma2, mb2, mp02, mnp2, mcol2, nx2, ny2,
                       r1x2, r1y2, r2x2, r2y2, depth2, odepth2, apn2, apt2, jadj, jadjl, jprio, npred, jnpred,
-                      preds, jpreds};
+                      preds, jpreds, pk[0], pk[1], pk[2], pk[3], pk[4], pk[5], pk[6], mom4, wl0, wl1, jwl0, jwl1};
         for (void* p : ps)
             if (p) cudaFree(p);
         for (int b = 0; b < 2; ++b) {
@@ -1253,10 +1379,12 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
         LTRY(cudaMalloc((void**)&I.entries, sizeof(unsigned long long)));
         LTRY(cudaMalloc((void**)&I.hist, sizeof(uint32_t) * 2 * CB_WORDS));
         LTRY(resident_cluster(0, lk_substeps_resident, &I.cl_solve));
+        LTRY(resident_cluster(1, lk_colour_cluster, &I.cl_colour));
     }
     LTRY(regrow(I.cap_n, (size_t)n + 1,
                 {LB(I.inv_m), LB(I.inv_i), LB(I.cs), LB(I.sn), LB(I.tq), LB(I.ang_prev), LB(I.kind), LB(I.rx0),
-                 LB(I.ry0), LB(I.rx1), LB(I.ry1), LB(I.bcnt), LB(I.adj), LB(I.jadj), LB(I.cursor)}));
+                 LB(I.ry0), LB(I.rx1), LB(I.ry1), LB(I.bcnt), LB(I.adj), LB(I.jadj), LB(I.cursor),
+                 LB(I.mom4)}));
     LTRY(regrow(I.cap_t, (size_t)T + 1, {LB(I.table)}));
     LTRY(regrow(I.cap_ts, std::max(n, T) / SCAN_TILE + 2, {LB(I.tsum)}));
 
@@ -1313,7 +1441,7 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
         A.pairs = I.pairs; A.hset = I.hset; A.np = np; A.hs = hs;
         LTRY(cudaMemsetAsync(I.hset, 0xFF, sizeof(unsigned long long) * hs, st));
         LTRY(cudaMemsetAsync(I.cnt, 0, sizeof(uint32_t) * LC_N, st));
-        LAUNCH(lk_pairs, blocks(E), A, E);
+        LAUNCH(lk_pairs, blocks(32ull * E), A, E);
         LTRY(cudaMemcpyAsync(I.h_cnt, I.cnt, sizeof(uint32_t) * LC_N, cudaMemcpyDeviceToHost, st));
         LTRY(cudaStreamSynchronize(st));
         if (!I.h_cnt[LC_PAIR_OVERFLOW]) {
@@ -1327,7 +1455,8 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
     // ---- narrowphase: at most one manifold per pair, two points per manifold ----
     LTRY(regrow(I.cap_m, (size_t)npairs + 1,
                 {LB(I.ma), LB(I.mb), LB(I.mp0), LB(I.corder), LB(I.mnp), LB(I.mcol), LB(I.nx), LB(I.ny),
-                 LB(I.fric), LB(I.ma2), LB(I.mb2), LB(I.mp02), LB(I.mnp2), LB(I.mcol2), LB(I.nx2), LB(I.ny2)}));
+                 LB(I.fric), LB(I.ma2), LB(I.mb2), LB(I.mp02), LB(I.mnp2), LB(I.mcol2), LB(I.nx2), LB(I.ny2),
+                 LB(I.pk[0]), LB(I.pk[1]), LB(I.pk[2]), LB(I.pk[3]), LB(I.pk[4]), LB(I.pk[5]), LB(I.pk[6])}));
     LTRY(regrow(I.cap_pt, 2 * (size_t)npairs + 1,
                 {LB(I.r1x), LB(I.r1y), LB(I.r2x), LB(I.r2y), LB(I.depth), LB(I.odepth), LB(I.mn), LB(I.mt),
                  LB(I.apn), LB(I.apt), LB(I.bias), LB(I.r1x2), LB(I.r1y2), LB(I.r2x2), LB(I.r2y2), LB(I.depth2),
@@ -1349,92 +1478,64 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
     LTRY(regrow(I.cap_c, 2 * (size_t)std::max(M, in.nj) + 2,
                 {LB(I.adjl), LB(I.prio), LB(I.jadjl), LB(I.jprio)}));
     LTRY(regrow(I.cap_j, (size_t)in.nj + 1, {LB(I.jcol), LB(I.jorder)}));
-    LTRY(regrow(I.cap_pr, (size_t)std::max(M, in.nj) + 1, {LB(I.npred), LB(I.jnpred)}));
+    LTRY(regrow(I.cap_pr, (size_t)std::max(M, in.nj) + 1,
+                {LB(I.npred), LB(I.jnpred), LB(I.wl0), LB(I.wl1), LB(I.jwl0), LB(I.jwl1)}));
     LTRY(regrow(I.cap_prr, ((size_t)std::max(M, in.nj) + 1) * PRED_ROW, {LB(I.preds), LB(I.jpreds)}));
     LTRY(cudaMemsetAsync(I.cnt, 0, sizeof(uint32_t) * 2 * LC_N, st));
-    struct ColourJob {
-        Colouring C;
-        uint32_t* cb;
-        uint32_t* order;
-        uint32_t rounds;  // rounds queued so far
-        bool active;
-    };
     uint32_t* cb_c = I.hist;
     uint32_t* cb_j = I.hist + CB_WORDS;
-    auto finish = [&](ColourJob& J) -> int {  // counts, offsets, order (after any queued rounds)
-        const uint32_t count = J.C.count;
-        LTRY(cudaMemsetAsync(J.cb, 0, sizeof(uint32_t) * CB_WORDS, st));
-        LAUNCH(lk_col_hist, blocks(count), J.C, J.cb);
-        lk_col_offsets<<<1, 32, 0, st>>>(J.cb);
-        ++I.nlaunch;
-        LAUNCH(lk_col_order, blocks(count), J.C, J.cb, J.order);
-        return 0;
-    };
-    auto start = [&](ColourJob& J, bool joints, uint32_t count, uint8_t* col, uint32_t* order, uint32_t* cb,
-                     uint32_t* cnt, uint32_t* adj, uint32_t* adjl, uint32_t* prio, uint32_t* npred, uint32_t* preds,
-                     uint32_t hint) -> int {
-        J.cb = cb;
-        J.order = order;
-        J.rounds = 0;
-        J.active = count > 0;
+    uint32_t rounds[2] = {0, 0};
+    // adjacency, earlier-neighbour rows, every round (one cluster), then the
+    // colour counts, offsets and colour-major order
+    auto colour = [&](bool joints, uint32_t count, uint8_t* col, uint32_t* order, uint32_t* cb, uint32_t* cnt,
+                      uint32_t* adj, uint32_t* adjl, uint32_t* prio, uint32_t* npred, uint32_t* preds, uint32_t* wl0,
+                      uint32_t* wl1) -> int {
         LTRY(cudaMemsetAsync(cb, 0, sizeof(uint32_t) * CB_WORDS, st));
-        if (!J.active) return 0;
-        Colouring& C = J.C;
-        C = Colouring{};
+        if (count == 0) return 0;
+        Colouring C{};
         C.count = count;
         C.joints = joints;
         C.jtype = in.jtype; C.jb1 = in.jb1; C.jb2 = in.jb2;
         C.ma = I.ma; C.mb = I.mb; C.kind = I.kind; C.colour = col;
         C.adj = adj; C.adjl = adjl; C.prio = prio; C.cursor = I.cursor; C.cnt = cnt;
         C.npred = npred; C.preds = preds;
+        C.wl[0] = wl0; C.wl[1] = wl1;
         LTRY(cudaMemsetAsync(adj, 0, sizeof(uint32_t) * ((size_t)n + 1), st));
         LAUNCH(lk_col_count, blocks(count), C);
         SCAN(adj, n);
         LTRY(cudaMemcpyAsync(I.cursor, adj, sizeof(uint32_t) * ((size_t)n + 1), cudaMemcpyDeviceToDevice, st));
         LAUNCH(lk_col_fill, blocks(count), C);
         LAUNCH(lk_col_preds, blocks(count), C);
-        for (uint32_t r = 0; r < hint; ++r) LAUNCH(lk_col_round, blocks(count), C, r);
-        J.rounds = hint;
-        return finish(J);
+        LTRY(launch_resident(lk_colour_cluster, I.cl_colour, st, C));
+        ++I.nlaunch;
+        LAUNCH(lk_col_hist, blocks(count), C, cb);
+        lk_col_offsets<<<1, 32, 0, st>>>(cb);
+        ++I.nlaunch;
+        LAUNCH(lk_col_order, blocks(count), C, cb, order);
+        return 0;
     };
-    ColourJob jobs[2];
-    if (int r = start(jobs[0], false, M, I.mcol, I.corder, cb_c, I.cnt, I.adj, I.adjl, I.prio, I.npred, I.preds,
-                      I.round_hint[0]))
+    if (int r = colour(false, M, I.mcol, I.corder, cb_c, I.cnt, I.adj, I.adjl, I.prio, I.npred, I.preds, I.wl0,
+                       I.wl1))
         return r;
-    if (int r = start(jobs[1], true, in.nj, I.jcol, I.jorder, cb_j, I.cnt + LC_N, I.jadj, I.jadjl, I.jprio,
-                      I.jnpred, I.jpreds, I.round_hint[1]))
+    if (int r = colour(true, in.nj, I.jcol, I.jorder, cb_j, I.cnt + LC_N, I.jadj, I.jadjl, I.jprio, I.jnpred,
+                       I.jpreds, I.jwl0, I.jwl1))
         return r;
+    // one round trip for both colourings: their flags and colour offsets
     uint32_t* hc = I.h_cnt + H_COLOUR;  // both counter blocks, then both result blocks
-    for (;;) {
-        LTRY(cudaMemcpyAsync(hc, I.cnt, sizeof(uint32_t) * 2 * LC_N, cudaMemcpyDeviceToHost, st));
-        LTRY(cudaMemcpyAsync(hc + 2 * LC_N, I.hist, sizeof(uint32_t) * 2 * CB_WORDS, cudaMemcpyDeviceToHost, st));
-        LTRY(cudaStreamSynchronize(st));
-        bool again = false;
-        for (int j = 0; j < 2; ++j) {
-            ColourJob& J = jobs[j];
-            if (!J.active) continue;
-            const uint32_t* h = hc + j * LC_N;
-            if (h[LC_COLOURS]) {
-                *msg = "a constraint needs more than " + std::to_string(MAX_COLOURS) + " colours";
-                return DS_CAPACITY;
-            }
-            if (h[LC_DONE] || h[LC_PEND0 + (J.rounds - 1) % 3] == 0u) {
-                I.round_hint[j] = (h[LC_DONE] ? h[LC_ROUNDS] : J.rounds) + 2;
-                J.active = false;
-                continue;
-            }
-            // each round colours at least the highest-priority uncoloured constraint
-            if (J.rounds > J.C.count + 1) {
-                *msg = "the colouring did not finish";
-                return -4;
-            }
-            const uint32_t more = std::max(8u, J.rounds / 2);
-            for (uint32_t r = 0; r < more; ++r) LAUNCH(lk_col_round, blocks(J.C.count), J.C, J.rounds + r);
-            J.rounds += more;
-            if (int r = finish(J)) return r;
-            again = true;
+    LTRY(cudaMemcpyAsync(hc, I.cnt, sizeof(uint32_t) * 2 * LC_N, cudaMemcpyDeviceToHost, st));
+    LTRY(cudaMemcpyAsync(hc + 2 * LC_N, I.hist, sizeof(uint32_t) * 2 * CB_WORDS, cudaMemcpyDeviceToHost, st));
+    LTRY(cudaStreamSynchronize(st));
+    for (int j = 0; j < 2; ++j) {
+        const uint32_t* h = hc + j * LC_N;
+        if (h[LC_COLOURS]) {
+            *msg = "a constraint needs more than " + std::to_string(MAX_COLOURS) + " colours";
+            return DS_CAPACITY;
         }
-        if (!again) break;
+        if (h[LC_STUCK]) {
+            *msg = "the colouring did not finish";
+            return -4;
+        }
+        rounds[j] = h[LC_ROUNDS];
     }
     uint32_t largest = 0;
     auto offsets = [&](const uint32_t* cb, std::vector<uint32_t>& off) {
@@ -1475,6 +1576,8 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
     S.jtype = in.jtype; S.jb1 = in.jb1; S.jb2 = in.jb2; S.jprm = in.jprm;
     S.pos64 = in.pos64;
     S.warm = in.warm;
+    S.pk = Packed{I.pk[0], I.pk[1], I.pk[2], I.pk[3], I.pk[4], I.pk[5], I.pk[6],
+                  in.nj == 0 && !in.warm ? I.mom4 : nullptr};
     const bool resident = use_resident_substeps(largest, I.cl_solve);
     if (resident) {
         ResidentPlan R{};
@@ -1514,6 +1617,7 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
         }
         LAUNCH(lk_integrate, blocks(n), S);
     }
+    if (!resident && M) LAUNCH(lk_unpack, blocks(M), S);
     if (in.warm) {  // this call's impulses become the next call's start
         LAUNCH(lk_warm_clear, blocks(whs_next), I.wkeys[wnext], whs_next);
         if (M) LAUNCH(lk_warm_store, blocks(M), S.s, M, I.wkeys[wnext], I.wvals[wnext], whs_next);
@@ -1526,9 +1630,9 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
         mark(4);
         fprintf(stderr,
                 "r2d grid step: %u bodies, %u entries, %u pairs, %u manifolds, %zu contact colours, %zu joint colours, "
-                "largest colour %u, %s substeps, %u launches | ms: cells %.3f pairs %.3f narrow %.3f colour %.3f "
-                "substeps %.3f\n",
-                n, E, npairs, M, I.coff.size() - 1, I.joff.size() - 1, largest,
+                "largest colour %u, colouring rounds %u + %u, %s substeps, %u launches | ms: cells %.3f pairs %.3f "
+                "narrow %.3f colour %.3f substeps %.3f\n",
+                n, E, npairs, M, I.coff.size() - 1, I.joff.size() - 1, largest, rounds[0], rounds[1],
                 resident ? "resident" : "per-colour", I.nlaunch, t_ms[0], t_ms[1] - t_ms[0], t_ms[2] - t_ms[1],
                 t_ms[3] - t_ms[2], t_ms[4] - t_ms[3]);
     }
@@ -1612,6 +1716,7 @@ struct StaticLayout {
     size_t r1x, r1y, r2x, r2y, depth, odepth, mn, mt, apn, apt, bias;
     size_t adjl, prio, jcol, jorder, cnt, entries, hist;
     size_t ma2, mb2, mp02, mnp2, mcol2, nx2, ny2, r1x2, r1y2, r2x2, r2y2, depth2, odepth2, apn2, apt2;
+    size_t pk[7], mom4;
     size_t total;
 };
 
@@ -1648,6 +1753,8 @@ constexpr StaticLayout static_layout() {
     L.r1x2 = c.take<float>(npt); L.r1y2 = c.take<float>(npt); L.r2x2 = c.take<float>(npt);
     L.r2y2 = c.take<float>(npt); L.depth2 = c.take<float>(npt); L.odepth2 = c.take<float>(npt);
     L.apn2 = c.take<float>(npt); L.apt2 = c.take<float>(npt);
+    for (int k = 0; k < 7; ++k) L.pk[k] = c.take<float4>(np);
+    L.mom4 = c.take<float4>(nb);
     L.total = c.off;
     return L;
 }
@@ -1768,7 +1875,7 @@ int static_world_step(const StaticStepArgs& in, cudaStream_t st, std::string* ms
     LAUNCH(lk_emit, blocks(n), A);
     SCAN(A.table, T);
     LAUNCH(lk_scatter, blocks(E), A, E);
-    LAUNCH(lk_pairs, blocks(E), A, E);
+    LAUNCH(lk_pairs, blocks(32ull * E), A, E);
     LTRY(cudaMemcpyAsync(h, cnt, sizeof(uint32_t) * LC_N, cudaMemcpyDeviceToHost, st));
     LTRY(cudaStreamSynchronize(st));
     if (h[LC_PAIR_OVERFLOW]) {
@@ -1787,9 +1894,9 @@ int static_world_step(const StaticStepArgs& in, cudaStream_t st, std::string* ms
     // contact colouring (Jones-Plassmann rounds, queued STATIC_ROUNDS at a
     // time), the colour-major permutation, then the substeps in one resident
     // cluster
-    constexpr uint32_t STATIC_ROUNDS = 32;
-    int cl_solve = 0;
+    int cl_solve = 0, cl_colour = 0;
     LTRY(resident_cluster(0, lk_substeps_resident, &cl_solve));
+    LTRY(resident_cluster(1, lk_colour_cluster, &cl_colour));
     uint32_t ncol = 0;
     if (M) {
         Colouring C{};
@@ -1804,25 +1911,12 @@ int static_world_step(const StaticStepArgs& in, cudaStream_t st, std::string* ms
         SCAN(C.adj, n);
         LTRY(cudaMemcpyAsync(C.cursor, C.adj, sizeof(uint32_t) * ((size_t)n + 1), cudaMemcpyDeviceToDevice, st));
         LAUNCH(lk_col_fill, blocks(M), C);
-        for (uint32_t rounds = 0;;) {
-            for (uint32_t r = 0; r < STATIC_ROUNDS; ++r) LAUNCH(lk_col_round, blocks(M), C, rounds + r);
-            rounds += STATIC_ROUNDS;
-            LTRY(cudaMemcpyAsync(h, cnt, sizeof(uint32_t) * LC_N, cudaMemcpyDeviceToHost, st));
-            LTRY(cudaStreamSynchronize(st));
-            if (h[LC_COLOURS]) {
-                *msg = "a contact needs more than " + std::to_string(MAX_COLOURS) + " colours";
-                return DS_CAPACITY;
-            }
-            if (h[LC_DONE] || h[LC_PEND0 + (rounds - 1) % 3] == 0u) break;
-            if (rounds > M + 1) {
-                *msg = "the colouring did not finish";
-                return -4;
-            }
-        }
+        LTRY(launch_resident(lk_colour_cluster, cl_colour, st, C));
         LTRY(cudaMemsetAsync(hist, 0, sizeof(uint32_t) * CB_WORDS, st));
         LAUNCH(lk_col_hist, blocks(M), C, hist);
         lk_col_offsets<<<1, 32, 0, st>>>(hist);
         LAUNCH(lk_col_order, blocks(M), C, hist, SP(uint32_t, corder));
+        LTRY(cudaMemcpyAsync(h, cnt, sizeof(uint32_t) * LC_N, cudaMemcpyDeviceToHost, st));
         LTRY(cudaMemcpyAsync(h + LC_N, hist + CB_NCOL, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
         // manifolds in colour-major order (into the second copies, which the substeps then use)
         SWT<uint32_t> d = s;
@@ -1833,6 +1927,14 @@ int static_world_step(const StaticStepArgs& in, cudaStream_t st, std::string* ms
         LAUNCH(lk_permute, blocks(M), s, d, SP(uint32_t, corder), M);
         s = d;
         LTRY(cudaStreamSynchronize(st));
+        if (h[LC_COLOURS]) {
+            *msg = "a contact needs more than " + std::to_string(MAX_COLOURS) + " colours";
+            return DS_CAPACITY;
+        }
+        if (h[LC_STUCK]) {
+            *msg = "the colouring did not finish";
+            return -4;
+        }
         ncol = h[LC_N];
     }
 
@@ -1844,6 +1946,10 @@ int static_world_step(const StaticStepArgs& in, cudaStream_t st, std::string* ms
     P.disc_rot = false;
     P.ngrav = in.ngrav;
     for (int k = 0; k < MAX_GRAVITY; ++k) P.g[k] = in.g[k];
+    P.pk = Packed{reinterpret_cast<float4*>(base + SL.pk[0]), reinterpret_cast<float4*>(base + SL.pk[1]),
+                  reinterpret_cast<float4*>(base + SL.pk[2]), reinterpret_cast<float4*>(base + SL.pk[3]),
+                  reinterpret_cast<float4*>(base + SL.pk[4]), reinterpret_cast<float4*>(base + SL.pk[5]),
+                  reinterpret_cast<float4*>(base + SL.pk[6]), SP(float4, mom4)};
     ResidentPlan R{};
     R.jorder = nullptr;
     R.coff = hist + CB_OFF; R.joff = nullptr;

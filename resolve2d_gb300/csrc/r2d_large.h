@@ -71,7 +71,7 @@ private:
 #define R2D_STATIC_MAX_BODIES 4096u
 #define R2D_STATIC_MAX_CELL_ENTRIES 65536u
 #define R2D_STATIC_MAX_PAIRS 16384u
-#define R2D_STATIC_SCRATCH_BYTES 5313536ull  // 5.07 MiB
+#define R2D_STATIC_SCRATCH_BYTES 7216128ull  // 6.88 MiB
 
 struct StaticStepArgs {
     float* state;          // [S_NFIELDS][n], device
