@@ -506,41 +506,92 @@ __device__ uint32_t colour_try(const Colouring& C, uint32_t i) {
     return 0u;
 }
 
-// Every Jones-Plassmann round, in one cluster (lib.zig's constraint order
-// through r2d_colour.h's priorities).  Round r counts the constraints it
-// leaves uncoloured in slot r % 3 and clears slot (r + 1) % 3 for the next
-// round; with worklists it takes round r - 1's list (wl[(r + 1) & 1], as
-// many entries as slot (r - 1) % 3 counts) and appends its own uncoloured
-// constraints to wl[r & 1], so later rounds touch only open constraints.
-// Every thread reads a slot only between the barrier after the round that
-// fills it and the next barrier, and the slot is cleared two rounds later,
-// so all threads see the same count and leave the loop together.  Expects
-// slot 0 zeroed.
-__global__ void __launch_bounds__(RT, 1) lk_colour_cluster(Colouring C) {
-    const uint32_t t0 = blockIdx.x * RT + threadIdx.x, nt = gridDim.x * RT;
-    const uint32_t lane = threadIdx.x & 31u;
-    const bool listed = C.wl[0] != nullptr;
+// colour_try for a constraint known to be open whose earlier neighbours fit
+// its row: the row's used 16-byte pieces and then every listed neighbour's
+// colour are loaded at once, two memory round trips in all.
+__device__ __forceinline__ uint32_t colour_try_row(const Colouring& C, uint32_t i) {
+    const uint32_t np = C.npred[i];
+    if (np > PRED_ROW) return colour_try(C, i);
+    static_assert(PRED_ROW == 32, "the row is eight 16-byte loads");
+    const uint4* row4 = reinterpret_cast<const uint4*>(C.preds + (size_t)i * PRED_ROW);
+    uint32_t o[PRED_ROW];
+#pragma unroll
+    for (uint32_t v = 0; v < 8; ++v) {
+        const uint4 r = 4 * v < np ? __ldcg(row4 + v) : make_uint4(0u, 0u, 0u, 0u);
+        o[4 * v] = r.x;
+        o[4 * v + 1] = r.y;
+        o[4 * v + 2] = r.z;
+        o[4 * v + 3] = r.w;
+    }
+    uint32_t c[PRED_ROW];
+#pragma unroll
+    for (uint32_t q = 0; q < PRED_ROW; ++q) c[q] = q < np ? (uint32_t)__ldcg(C.colour + o[q]) : 0u;
+    // colours below 32 (nearly always): one word of the set, one shift and OR each
+    uint32_t w0 = 0u, any_open = 0u, high = 0u;
+#pragma unroll
+    for (uint32_t q = 0; q < PRED_ROW; ++q) {
+        if (q >= np) break;
+        any_open |= c[q] == 0xFFu;
+        high |= c[q] >> 5;
+        w0 |= 1u << (c[q] & 31u);
+    }
+    if (any_open) return 1u;
+    uint32_t col;
+    if (high == 0u) {
+        col = w0 == 0xFFFFFFFFu ? 32u : (uint32_t)__ffs(~w0) - 1u;
+    } else {
+        ColourSet used;
+#pragma unroll
+        for (uint32_t q = 0; q < PRED_ROW; ++q) {
+            if (q >= np) break;
+            used.add(c[q]);
+        }
+        col = used.first_free();
+    }
+    if (col >= (uint32_t)MAX_COLOURS) {
+        atomicExch(&C.cnt[LC_COLOURS], 1u);
+        col = 0u;
+    }
+    C.colour[i] = (uint8_t)col;
+    return 0u;
+}
+
+// Every Jones-Plassmann round, in one cluster of CT-thread CTAs
+// (r2d_colour.h's order).  With worklists, each thread keeps the constraints
+// it holds that are still open in its own slots of the round's list (slot
+// t + j * nt of wl[r & 1] for its j-th), so rounds need no atomics: round 0
+// holds constraint t + j * nt, round r re-tries what the thread kept from
+// round r - 1.  Without them every round re-scans all constraints.  A thread
+// that leaves one open sets flag slot r % 3; the flag of round r + 1 is
+// cleared in round r, and each thread reads slot r % 3 between the barrier
+// after round r and the next barrier, two rounds before the slot is cleared
+// again, so all threads see the same flag and leave the loop together.
+// Expects flag slot 0 zeroed.
+constexpr int CT = 1024;  // threads per CTA of the colouring cluster
+__global__ void __launch_bounds__(CT, 1) lk_colour_cluster(Colouring C) {
+    const uint32_t t0 = blockIdx.x * CT + threadIdx.x, nt = gridDim.x * CT;
+    const bool listed = C.wl[0] != nullptr && C.npred != nullptr;
     uint32_t* cnt = C.cnt;
-    uint32_t open = C.count;
+    uint32_t held = C.count > t0 ? (C.count - t0 - 1) / nt + 1 : 0u;  // constraints this thread holds
     for (uint32_t round = 0;; ++round) {
         if (t0 == 0) cnt[LC_PEND0 + (round + 1) % 3] = 0u;
-        const uint32_t* in = listed && round > 0 ? C.wl[(round + 1) & 1] : nullptr;
-        uint32_t* out = listed ? C.wl[round & 1] : nullptr;
-        const uint32_t span = listed ? open : C.count;
-        for (uint32_t at = 0; at < span; at += nt) {  // uniform trip count: the ballot sees whole warps
-            const uint32_t t = at + t0;
-            const uint32_t i = (in && t < span) ? __ldcg(in + t) : t;
-            const bool waiting = t < span && colour_try(C, i) != 0u;
-            const uint32_t mask = __ballot_sync(0xffffffffu, waiting);
-            if (mask == 0u) continue;
-            uint32_t slot = 0;
-            if (lane == 0) slot = atomicAdd(cnt + LC_PEND0 + round % 3, (uint32_t)__popc(mask));
-            slot = __shfl_sync(0xffffffffu, slot, 0);
-            if (out && waiting) out[slot + __popc(mask & ((1u << lane) - 1u))] = i;
+        bool open = false;
+        if (listed) {
+            const uint32_t* in = round > 0 ? C.wl[(round + 1) & 1] : nullptr;
+            uint32_t* out = C.wl[round & 1];
+            uint32_t kept = 0;
+            for (uint32_t j = 0; j < held; ++j) {
+                const uint32_t i = in ? __ldcg(in + t0 + j * nt) : t0 + j * nt;
+                if (colour_try_row(C, i)) out[t0 + (kept++) * nt] = i;
+            }
+            held = kept;
+            open = kept > 0;
+        } else {
+            for (uint32_t i = t0; i < C.count; i += nt) open |= colour_try(C, i) != 0u;
         }
+        if (open) cnt[LC_PEND0 + round % 3] = 1u;
         cluster_sync_all();
-        open = __ldcg(cnt + LC_PEND0 + round % 3);
-        if (open == 0u) {
+        if (__ldcg(cnt + LC_PEND0 + round % 3) == 0u) {
             if (t0 == 0) cnt[LC_ROUNDS] = round + 1;
             break;
         }
@@ -1153,7 +1204,7 @@ std::atomic<int> g_cluster_size[2][MAX_DEVICES];  // [resident kernel][device]; 
 // such a cluster with the kernel's resources, else the portable 8.  Found
 // once per device and kernel.
 template <class... P>
-cudaError_t resident_cluster(int which, void (*kernel)(P...), int* out) {
+cudaError_t resident_cluster(int which, void (*kernel)(P...), int threads, int* out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
@@ -1164,7 +1215,7 @@ cudaError_t resident_cluster(int which, void (*kernel)(P...), int* out) {
         if (cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
             cudaLaunchConfig_t cfg{};
             cfg.gridDim = dim3(16);
-            cfg.blockDim = dim3(RT);
+            cfg.blockDim = dim3(threads);
             cudaLaunchAttribute at{};
             at.id = cudaLaunchAttributeClusterDimension;
             at.val.clusterDim.x = 16;
@@ -1184,10 +1235,10 @@ cudaError_t resident_cluster(int which, void (*kernel)(P...), int* out) {
 
 // One cluster of `cl` CTAs: the whole grid of a resident kernel.
 template <class... P, class... A>
-cudaError_t launch_resident(void (*kernel)(P...), int cl, cudaStream_t st, A... args) {
+cudaError_t launch_resident(void (*kernel)(P...), int cl, int threads, cudaStream_t st, A... args) {
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3(cl);
-    cfg.blockDim = dim3(RT);
+    cfg.blockDim = dim3(threads);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = st;
     cudaLaunchAttribute at{};
@@ -1378,8 +1429,8 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
         LTRY(cudaMalloc((void**)&I.cnt, sizeof(uint32_t) * 2 * LC_N));
         LTRY(cudaMalloc((void**)&I.entries, sizeof(unsigned long long)));
         LTRY(cudaMalloc((void**)&I.hist, sizeof(uint32_t) * 2 * CB_WORDS));
-        LTRY(resident_cluster(0, lk_substeps_resident, &I.cl_solve));
-        LTRY(resident_cluster(1, lk_colour_cluster, &I.cl_colour));
+        LTRY(resident_cluster(0, lk_substeps_resident, RT, &I.cl_solve));
+        LTRY(resident_cluster(1, lk_colour_cluster, CT, &I.cl_colour));
     }
     LTRY(regrow(I.cap_n, (size_t)n + 1,
                 {LB(I.inv_m), LB(I.inv_i), LB(I.cs), LB(I.sn), LB(I.tq), LB(I.ang_prev), LB(I.kind), LB(I.rx0),
@@ -1506,7 +1557,7 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
         LTRY(cudaMemcpyAsync(I.cursor, adj, sizeof(uint32_t) * ((size_t)n + 1), cudaMemcpyDeviceToDevice, st));
         LAUNCH(lk_col_fill, blocks(count), C);
         LAUNCH(lk_col_preds, blocks(count), C);
-        LTRY(launch_resident(lk_colour_cluster, I.cl_colour, st, C));
+        LTRY(launch_resident(lk_colour_cluster, I.cl_colour, CT, st, C));
         ++I.nlaunch;
         LAUNCH(lk_col_hist, blocks(count), C, cb);
         lk_col_offsets<<<1, 32, 0, st>>>(cb);
@@ -1585,7 +1636,7 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
         R.coff = cb_c + CB_OFF; R.joff = cb_j + CB_OFF;
         R.ncol = (uint32_t)I.coff.size() - 1; R.njcol = (uint32_t)I.joff.size() - 1;
         R.sub_steps = sub_steps; R.iters = iters;
-        LTRY(launch_resident(lk_substeps_resident, I.cl_solve, st, S, R));
+        LTRY(launch_resident(lk_substeps_resident, I.cl_solve, RT, st, S, R));
         ++I.nlaunch;
     }
     for (uint32_t sub = 0; sub < sub_steps && !resident; ++sub) {
@@ -1895,8 +1946,8 @@ int static_world_step(const StaticStepArgs& in, cudaStream_t st, std::string* ms
     // time), the colour-major permutation, then the substeps in one resident
     // cluster
     int cl_solve = 0, cl_colour = 0;
-    LTRY(resident_cluster(0, lk_substeps_resident, &cl_solve));
-    LTRY(resident_cluster(1, lk_colour_cluster, &cl_colour));
+    LTRY(resident_cluster(0, lk_substeps_resident, RT, &cl_solve));
+    LTRY(resident_cluster(1, lk_colour_cluster, CT, &cl_colour));
     uint32_t ncol = 0;
     if (M) {
         Colouring C{};
@@ -1911,7 +1962,7 @@ int static_world_step(const StaticStepArgs& in, cudaStream_t st, std::string* ms
         SCAN(C.adj, n);
         LTRY(cudaMemcpyAsync(C.cursor, C.adj, sizeof(uint32_t) * ((size_t)n + 1), cudaMemcpyDeviceToDevice, st));
         LAUNCH(lk_col_fill, blocks(M), C);
-        LTRY(launch_resident(lk_colour_cluster, cl_colour, st, C));
+        LTRY(launch_resident(lk_colour_cluster, cl_colour, CT, st, C));
         LTRY(cudaMemsetAsync(hist, 0, sizeof(uint32_t) * CB_WORDS, st));
         LAUNCH(lk_col_hist, blocks(M), C, hist);
         lk_col_offsets<<<1, 32, 0, st>>>(hist);
@@ -1955,7 +2006,7 @@ int static_world_step(const StaticStepArgs& in, cudaStream_t st, std::string* ms
     R.coff = hist + CB_OFF; R.joff = nullptr;
     R.ncol = ncol; R.njcol = 0;
     R.sub_steps = in.sub_steps; R.iters = in.iters;
-    LTRY(launch_resident(lk_substeps_resident, cl_solve, st, P, R));
+    LTRY(launch_resident(lk_substeps_resident, cl_solve, RT, st, P, R));
 #undef SP
     LTRY(cudaGetLastError());
     return 0;
