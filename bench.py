@@ -28,6 +28,12 @@ cpu_baseline  the CPU oracle (the C++ restatement of the reference's step,
 
 --impl reference times that CPU step alone (the reference is Zig and cannot
 be built here) and prints its own line.
+
+--workload config1 | config2 measures one large world instead (the
+12,001-body pyramid with falling discs; the 200,004-body box with chains and
+motors), which the library steps on its grid pipeline: same metric, same
+keys, CUDA events around each step (the pipeline's host round trips are
+inside them), no plain-path comparison (the workload is one world).
 """
 
 from __future__ import annotations
@@ -49,6 +55,14 @@ SETTLE_STEPS = 300
 BYTES_READ = 77   # pos 8, angle 4, momentum 8, ang. momentum 4, force+torque 12, AABB 16, mass/inertia/mu/dims 20, kind 1, id 4
 BYTES_WRITE = 40  # pos 8, angle 4, momentum 8, ang. momentum 4, AABB 16
 METRIC = "body-steps/sec on 1 GB300, batched FP32 vs plain, at stated pos error vs FP64"
+HEADLINE = "config3: 4096 worlds, counts log-uniform [16,512], dt 1/60, 8 iterations, settled 300 steps"
+# single large worlds: (scene name, description, settle steps)
+LARGE = {
+    "config1": ("config1: one world, 10,000-box pyramid + 2,000 discs falling onto it (12,001 bodies), dt 1/60, "
+                "10 iterations, settled 300 steps", 300),
+    "config2": ("config2: one world, 200,004 bodies in a walled 2000x500 box, 5,000 chains of 20 distance joints "
+                "+ 2,000 motors, dt 1/120, 8 iterations, settled 30 steps", 30),
+}
 
 
 def dist_env():
@@ -178,9 +192,14 @@ def run_reference(args):
     from resolve2d_gb300 import scenes
 
     B.build_oracle()
-    sc = scenes.config3(seed=3)
+    if args.workload in LARGE:
+        sc = getattr(scenes, args.workload)()
+        workload, settle = LARGE[args.workload]
+    else:
+        sc = scenes.config3(seed=3)
+        workload, settle = HEADLINE, SETTLE_STEPS
     threads = cpu_threads()
-    state = settle_scene(sc, SETTLE_STEPS)
+    state = settle_scene(sc, settle)
     # each step: one full pass over all 4,096 worlds
     for _ in range(args.warmup):
         oracle_time(sc, state, 1, threads)
@@ -192,13 +211,107 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded)",
-        "config": {"workload": "config3: 4096 worlds, counts log-uniform [16,512], dt 1/60, 8 iterations, settled 300 steps",
-                   "bodies": sc.nbodies, "worlds": sc.nworlds},
+        "config": {"workload": workload, "bodies": sc.nbodies, "worlds": sc.nworlds},
         "cpu_baseline": {"value": v, "unit": "body-steps/s", "cores": threads, "kind": "port",
                          "sample": f"all {sc.nworlds} worlds x {args.steps} steps from the settled state; "
                                    "C++ restatement of Solver.process (Zig toolchain absent)"},
         "e2e": {"value": v, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    print(json.dumps(line), flush=True)
+
+
+def run_large(args):
+    """One large world on the grid pipeline (--workload config1 / config2)."""
+    rank, world, local = dist_env()
+    import torch
+
+    torch.cuda.set_device(local)
+    from resolve2d_gb300 import build as B
+    from resolve2d_gb300 import scenes
+    from resolve2d_gb300.engine import World
+
+    B.build_library()
+    sc = getattr(scenes, args.workload)()
+    workload, settle = LARGE[args.workload]
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    batch = World.from_scene(sc, stream=stream.cuda_stream)
+    for _ in range(settle):
+        batch.process(sc.dt, sc.sub_steps, sc.iters)
+    batch.sync()
+    settled = batch.read_state()
+    nb = sc.nbodies
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        batch.process(sc.dt, sc.sub_steps, sc.iters)
+    batch.sync()
+    batch.write_state(settled)
+    batch.sync()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    torch.cuda.synchronize()
+    clocks.start()
+    torch.cuda.profiler.start()
+    t0 = time.perf_counter()
+    launches = 0
+    for k in range(args.steps):
+        flush.zero_()
+        starts[k].record(stream)
+        batch.process(sc.dt, sc.sub_steps, sc.iters)
+        ends[k].record(stream)
+        launches += batch.launches_per_step()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    torch.cuda.profiler.stop()
+    batch.sync()
+    clk = clocks.stop()
+    dev_s = sum(s_.elapsed_time(e_) for s_, e_ in zip(starts, ends)) / 1e3
+    step_s = dev_s / args.steps
+    value = nb * args.steps / dev_s
+
+    e2e_steps = max(3, min(args.steps, 10))
+    forces_in = torch.zeros((3, nb), dtype=torch.float32).pin_memory().numpy()
+    pose_out = torch.empty((6, nb), dtype=torch.float32).pin_memory().numpy()
+    batch.write_state(settled)
+    batch.sync()
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for _ in range(e2e_steps):
+        batch.write_fields(6, forces_in)
+        batch.process(sc.dt, sc.sub_steps, sc.iters)
+        batch.read_fields(0, 6, pose_out)
+    batch.sync()
+    e2e_v = nb * e2e_steps / (time.perf_counter() - t1)
+
+    peak, peak_src = measured_peaks()
+    achieved = (BYTES_READ + BYTES_WRITE) * nb / step_s / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * step_s, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": workload, "bodies": nb, "worlds": sc.nworlds, "joints": int(len(sc.jtype)),
+                   "l2": "flushed between timed steps (256 MiB write outside the events)",
+                   "path": "grid pipeline (one world larger than a CTA's shared memory)"},
+        "gpu_launches": launches,
+        "wall_s_timed_loop": wall,
+        "e2e": {"value": e2e_v, "unit": "body-steps/s", "h2d_bytes_per_step": 12 * nb, "d2h_bytes_per_step": 24 * nb,
+                "inputs": "force and torque rows (pinned)", "results": "pose and momenta rows (pinned)"},
+        "plain_one_world_per_launch": None,
+        "roofline": {"bound": "hbm", "kernel": "grid pipeline (all launches of one step)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_src, "traffic": None, "bytes_per_body_step": BYTES_READ + BYTES_WRITE},
+        "clocks": clk,
+    }
+    if not args.no_cpu_baseline:
+        threads = cpu_threads()
+        one = oracle_time(sc, settled, 1, threads)
+        cpu_steps = max(2, min(200, int(10.0 / max(one, 1e-3))))
+        secs = oracle_time(sc, settled, cpu_steps, threads)
+        line["cpu_baseline"] = {"value": nb * cpu_steps / secs, "unit": "body-steps/s", "cores": 1,
+                                "kind": "port", "seconds": secs,
+                                "sample": f"the world x {cpu_steps} steps from the settled state on one core (the "
+                                          "oracle threads over worlds; C++ restatement of Solver.process)"}
     print(json.dumps(line), flush=True)
 
 
@@ -213,9 +326,13 @@ def main():
     ap.add_argument("--no-precision", action="store_true", help="accepted for older command lines; no effect")
     ap.add_argument("--plain-worlds", type=int, default=64,
                     help="worlds stepped one per launch for the plain-path comparison")
+    ap.add_argument("--workload", default="config3", choices=["config3", *LARGE],
+                    help="config3 (the headline batch) or one large world on the grid pipeline")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload in LARGE:
+        return run_large(args)
 
     rank, world, local = dist_env()
     import torch
@@ -350,8 +467,7 @@ def main():
         "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * step_s, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-        "config": {"workload": "config3: 4096 worlds, counts log-uniform [16,512], dt 1/60, 8 iterations, "
-                               "settled 300 steps", "bodies": nb, "worlds": sc.nworlds,
+        "config": {"workload": HEADLINE, "bodies": nb, "worlds": sc.nworlds,
                    "l2": "flushed between timed steps (256 MiB write outside the events)",
                    "tiles": "threads per CTA of each size class autotuned on the settled worlds"
                    if not args.no_autotune else "default threads per size class",

@@ -177,6 +177,9 @@ R2D_API int r2d_solver_read_positions_f64(r2d_solver* s, double* pose);
 /* Debug taps (need R2D_FLAG_DEBUG_TAPS): the last frame's manifolds
  * (Solver.manifolds, lib.zig:137) with their contact colours.  keys [cap][2]
  * are (reference, incident) body indices; data [cap][R2D_MANIFOLD_FLOATS]. */
+/* Kernel launches of the solver's latest step (a world on the grid pipeline
+ * launches per phase and per colouring; a fused world launches one kernel). */
+R2D_API int r2d_solver_launches_per_step(r2d_solver* s, uint32_t* out);
 R2D_API int r2d_solver_num_manifolds(r2d_solver* s, uint32_t* out);
 R2D_API int r2d_solver_get_manifolds(r2d_solver* s, uint32_t cap, uint32_t* keys, float* data,
                                      uint32_t* colours);

@@ -73,6 +73,7 @@ SIGNATURES = {
     "r2d_solver_process": ([_P, C.c_float, C.c_uint32, C.c_uint32], C.c_int),
     "r2d_solver_sync": ([_P], C.c_int),
     "r2d_solver_num_manifolds": ([_P, _u32p], C.c_int),
+    "r2d_solver_launches_per_step": ([_P, _u32p], C.c_int),
     "r2d_solver_get_manifolds": ([_P, C.c_uint32, _u32p, _f32p, _u32p], C.c_int),
     "r2d_solver_get_joint_colours": ([_P, C.c_uint32, _u32p], C.c_int),
     "r2d_batch_create": ([C.POINTER(Config), C.POINTER(_P)], C.c_int),

@@ -1522,18 +1522,28 @@ R2D_API int r2d_batch_autotune(r2d_batch* b, float dt, uint32_t sub_steps, uint3
     return guarded([&] { return b->eng.autotune(dt, sub_steps, collision_iters, trial_steps); });
 }
 
-R2D_API int r2d_batch_launches_per_step(r2d_batch* b, uint32_t* out) {
-    if (!b || !out) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
-    if (b->eng.plan_dirty && b->eng.nworlds) {
-        int st = b->eng.plan();
+// One kernel per size class, plus the call counter of the step, plus what
+// each grid-pipeline world launched in its latest step.
+static int launches_of(Engine& eng, uint32_t* out) {
+    if (eng.plan_dirty && eng.nworlds) {
+        int st = eng.plan();
         if (st) return st;
     }
-    // one kernel per size class, plus the call counter of the step
-    uint32_t n = (uint32_t)b->eng.classes.size() + (b->eng.classes.empty() ? 0u : 1u);
-    for (uint32_t w : b->eng.large_list)
-        if (b->eng.large[w]) n += b->eng.large[w]->launches();
+    uint32_t n = (uint32_t)eng.classes.size() + (eng.classes.empty() ? 0u : 1u);
+    for (uint32_t w : eng.large_list)
+        if (eng.large[w]) n += eng.large[w]->launches();
     *out = n;
     return R2D_OK;
+}
+
+R2D_API int r2d_batch_launches_per_step(r2d_batch* b, uint32_t* out) {
+    if (!b || !out) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
+    return launches_of(b->eng, out);
+}
+
+R2D_API int r2d_solver_launches_per_step(r2d_solver* s, uint32_t* out) {
+    if (!s || !out) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
+    return launches_of(s->eng, out);
 }
 
 R2D_API int r2d_batch_world_status(r2d_batch* b, int* status) {

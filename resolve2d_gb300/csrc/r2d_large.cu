@@ -185,10 +185,9 @@ struct Phase1 {
     __device__ float pr(int f, uint32_t i) const { return __ldg(props + (size_t)f * NB + base + i); }
 };
 
-// per body: derived quantities, and the cells its stored AABB covers
-__global__ void lk_load(Phase1 A) {
-    const uint32_t i = blockIdx.x * LT + threadIdx.x;
-    if (i >= A.n) return;
+// per body: derived quantities, and the cells its stored AABB covers;
+// returns its cell count
+__device__ __forceinline__ uint32_t load_body(const Phase1& A, uint32_t i) {
     const uint8_t k = __ldg(A.kind_in + A.base + i);
     const float a = A.st(S_ANGLE, i);
     A.s.kind[i] = k;
@@ -219,25 +218,42 @@ __global__ void lk_load(Phase1 A) {
             x1 = x0 - 1;
         } else {
             count = (uint32_t)c64;
-            atomicAdd(A.entries, c64);
         }
     }
     A.rx0[i] = x0; A.ry0[i] = y0; A.rx1[i] = x1; A.ry1[i] = y1;
     A.bcnt[i] = count;
+    return count;
 }
 
-__global__ void lk_emit(Phase1 A) {
+// The cell-entry total is summed per warp first: one atomic per warp
+// instead of one per body on a single counter.
+__global__ void lk_load(Phase1 A) {
     const uint32_t i = blockIdx.x * LT + threadIdx.x;
-    if (i >= A.n) return;
-    uint32_t k = A.bcnt[i];
-    for (int32_t yi = A.ry0[i]; yi <= A.ry1[i]; ++yi)
-        for (int32_t xi = A.rx0[i]; xi <= A.rx1[i]; ++xi) {
-            const uint32_t bk = cell_bucket(xi, yi, A.bmod);
-            A.ebucket[k] = bk;
-            A.ebody[k] = i;
-            atomicAdd(&A.table[bk], 1u);
-            ++k;
-        }
+    unsigned long long sum = i < A.n ? load_body(A, i) : 0ull;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+    if ((threadIdx.x & 31u) == 0 && sum) atomicAdd(A.entries, sum);
+}
+
+// One thread per cell entry (a wall can cover hundreds of cells): after the
+// scan of the counts, entry e belongs to the last body whose first entry is
+// at most e, and is that body's (e - first)-th cell in row-major order.
+__global__ void lk_emit(Phase1 A, uint32_t E) {
+    const uint32_t e = blockIdx.x * LT + threadIdx.x;
+    if (e >= E) return;
+    uint32_t lo = 0, hi = A.n;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (A.bcnt[mid] <= e) lo = mid;
+        else hi = mid;
+    }
+    const uint32_t i = lo, r = e - A.bcnt[i];
+    const uint32_t w = (uint32_t)(A.rx1[i] - A.rx0[i] + 1);
+    const int32_t xi = A.rx0[i] + (int32_t)(r % w), yi = A.ry0[i] + (int32_t)(r / w);
+    const uint32_t bk = cell_bucket(xi, yi, A.bmod);
+    A.ebucket[e] = bk;
+    A.ebody[e] = i;
+    atomicAdd(&A.table[bk], 1u);
 }
 
 // after the scan: table[b] = first slot of bucket b; afterwards one past its last
@@ -353,7 +369,7 @@ __global__ void lk_narrow(Phase1 A, uint32_t npairs) {
 // colouring (r2d_colour.h) by Jones-Plassmann rounds
 // ---------------------------------------------------------------------------
 constexpr uint32_t NO_NODE = 0xFFFFFFFFu;
-constexpr uint32_t PRED_ROW = 32;  // earlier neighbours kept per constraint (a 14-contact body pair has 23)
+constexpr uint32_t PRED_ROW = 64;  // earlier neighbours kept per constraint (two 21-contact bodies: 36)
 
 struct Colouring {
     uint32_t count;
@@ -507,45 +523,46 @@ __device__ uint32_t colour_try(const Colouring& C, uint32_t i) {
 }
 
 // colour_try for a constraint known to be open whose earlier neighbours fit
-// its row: the row's used 16-byte pieces and then every listed neighbour's
-// colour are loaded at once, two memory round trips in all.
+// its row, read 16 at a time: a chunk's used 16-byte pieces, then all its
+// neighbours' colours, are loaded at once (two memory round trips a chunk;
+// most constraints need one chunk).  It stops at the first chunk that holds
+// an uncoloured neighbour.
 __device__ __forceinline__ uint32_t colour_try_row(const Colouring& C, uint32_t i) {
     const uint32_t np = C.npred[i];
     if (np > PRED_ROW) return colour_try(C, i);
-    static_assert(PRED_ROW == 32, "the row is eight 16-byte loads");
     const uint4* row4 = reinterpret_cast<const uint4*>(C.preds + (size_t)i * PRED_ROW);
-    uint32_t o[PRED_ROW];
-#pragma unroll
-    for (uint32_t v = 0; v < 8; ++v) {
-        const uint4 r = 4 * v < np ? __ldcg(row4 + v) : make_uint4(0u, 0u, 0u, 0u);
-        o[4 * v] = r.x;
-        o[4 * v + 1] = r.y;
-        o[4 * v + 2] = r.z;
-        o[4 * v + 3] = r.w;
-    }
-    uint32_t c[PRED_ROW];
-#pragma unroll
-    for (uint32_t q = 0; q < PRED_ROW; ++q) c[q] = q < np ? (uint32_t)__ldcg(C.colour + o[q]) : 0u;
     // colours below 32 (nearly always): one word of the set, one shift and OR each
-    uint32_t w0 = 0u, any_open = 0u, high = 0u;
+    uint32_t w0 = 0u, high = 0u;
+    for (uint32_t at = 0; at < np; at += 16) {
+        uint32_t o[16];
 #pragma unroll
-    for (uint32_t q = 0; q < PRED_ROW; ++q) {
-        if (q >= np) break;
-        any_open |= c[q] == 0xFFu;
-        high |= c[q] >> 5;
-        w0 |= 1u << (c[q] & 31u);
+        for (uint32_t v = 0; v < 4; ++v) {
+            const uint4 r = at + 4 * v < np ? __ldcg(row4 + at / 4 + v) : make_uint4(0u, 0u, 0u, 0u);
+            o[4 * v] = r.x;
+            o[4 * v + 1] = r.y;
+            o[4 * v + 2] = r.z;
+            o[4 * v + 3] = r.w;
+        }
+        uint32_t c[16];
+#pragma unroll
+        for (uint32_t q = 0; q < 16; ++q) c[q] = at + q < np ? (uint32_t)__ldcg(C.colour + o[q]) : 0u;
+        uint32_t any_open = 0u;
+#pragma unroll
+        for (uint32_t q = 0; q < 16; ++q) {
+            if (at + q >= np) break;
+            any_open |= c[q] == 0xFFu;
+            high |= c[q] >> 5;
+            w0 |= 1u << (c[q] & 31u);
+        }
+        if (any_open) return 1u;
     }
-    if (any_open) return 1u;
     uint32_t col;
     if (high == 0u) {
         col = w0 == 0xFFFFFFFFu ? 32u : (uint32_t)__ffs(~w0) - 1u;
-    } else {
+    } else {  // a colour of 32 or more: the full set, from the row again
         ColourSet used;
-#pragma unroll
-        for (uint32_t q = 0; q < PRED_ROW; ++q) {
-            if (q >= np) break;
-            used.add(c[q]);
-        }
+        const uint32_t* row = C.preds + (size_t)i * PRED_ROW;
+        for (uint32_t q = 0; q < np; ++q) used.add(__ldcg(C.colour + __ldcg(row + q)));
         col = used.first_free();
     }
     if (col >= (uint32_t)MAX_COLOURS) {
@@ -1472,7 +1489,7 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
     LTRY(regrow(I.cap_e, (size_t)E + 1, {LB(I.ebucket), LB(I.ebody), LB(I.eslot), LB(I.sbody)}));
     A.ebucket = I.ebucket; A.ebody = I.ebody; A.eslot = I.eslot; A.sbody = I.sbody;
     SCAN(I.bcnt, n);
-    LAUNCH(lk_emit, blocks(n), A);
+    LAUNCH(lk_emit, blocks(E), A, E);
     SCAN(I.table, T);
     LAUNCH(lk_scatter, blocks(E), A, E);
 
@@ -1923,7 +1940,7 @@ int static_world_step(const StaticStepArgs& in, cudaStream_t st, std::string* ms
     }
     const uint32_t E = (uint32_t)E64;
     SCAN(A.bcnt, n);
-    LAUNCH(lk_emit, blocks(n), A);
+    LAUNCH(lk_emit, blocks(E), A, E);
     SCAN(A.table, T);
     LAUNCH(lk_scatter, blocks(E), A, E);
     LAUNCH(lk_pairs, blocks(32ull * E), A, E);

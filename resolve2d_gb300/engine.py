@@ -97,6 +97,11 @@ class World:
     def sync(self):
         N.check(self._lib.r2d_solver_sync(self._h), "r2d_solver_sync")
 
+    def launches_per_step(self) -> int:
+        out = C.c_uint32()
+        N.check(self._lib.r2d_solver_launches_per_step(self._h, C.byref(out)), "r2d_solver_launches_per_step")
+        return int(out.value)
+
     def manifolds(self):
         m = C.c_uint32()
         N.check(self._lib.r2d_solver_num_manifolds(self._h, C.byref(m)), "r2d_solver_num_manifolds")
