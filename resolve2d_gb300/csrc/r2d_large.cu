@@ -739,11 +739,18 @@ constexpr uint32_t PK_NP = 0xFFu, PK_STATIC_A = 0x100u, PK_STATIC_B = 0x200u;  /
 // its packed record: solve_contact's arithmetic in the same order.  Seven
 // coalesced record loads are issued together, then the two bodies'
 // momenta; the accumulators go back as one store.
+struct MRec {  // one manifold's packed record
+    float4 v0, v1, v2, v3, v4, v5, v6;
+};
+
+__device__ __forceinline__ MRec load_rec(const Packed& pk, uint32_t m) {
+    return MRec{pk.v0[m], pk.v1[m], pk.v2[m], pk.v3[m], pk.v4[m], pk.v5[m], pk.v6[m]};
+}
+
 template <bool MOM4>
-__device__ __forceinline__ void solve_contact_packed(const Packed& pk, float* mx, float* my, float* L, uint32_t m,
-                                                     bool warm) {
-    const float4 v0 = pk.v0[m], v1 = pk.v1[m], v2 = pk.v2[m], v3 = pk.v3[m], v4 = pk.v4[m], v5 = pk.v5[m],
-                 v6 = pk.v6[m];
+__device__ __forceinline__ void solve_contact_rec(const Packed& pk, const MRec& rec, float* mx, float* my, float* L,
+                                                  uint32_t m, bool warm) {
+    const float4 v0 = rec.v0, v1 = rec.v1, v2 = rec.v2, v3 = rec.v3, v4 = rec.v4, v5 = rec.v5, v6 = rec.v6;
     const uint32_t a = __float_as_uint(v0.x), b = __float_as_uint(v0.y), flags = __float_as_uint(v1.y);
     const uint32_t np = flags & PK_NP;
     const bool sa = flags & PK_STATIC_A, sb = flags & PK_STATIC_B;
@@ -822,10 +829,15 @@ __device__ __forceinline__ void solve_contact_packed(const Packed& pk, float* mx
     }
 }
 
+__device__ __forceinline__ void solve_contact_rec(const Packed& pk, const MRec& rec, float* mx, float* my, float* L,
+                                                  uint32_t m, bool warm) {
+    if (pk.mom4) solve_contact_rec<true>(pk, rec, mx, my, L, m, warm);
+    else solve_contact_rec<false>(pk, rec, mx, my, L, m, warm);
+}
+
 __device__ __forceinline__ void solve_contact_packed(const Packed& pk, float* mx, float* my, float* L, uint32_t m,
                                                      bool warm) {
-    if (pk.mom4) solve_contact_packed<true>(pk, mx, my, L, m, warm);
-    else solve_contact_packed<false>(pk, mx, my, L, m, warm);
+    solve_contact_rec(pk, load_rec(pk, m), mx, my, L, m, warm);
 }
 
 // ---------------------------------------------------------------------------
@@ -1129,16 +1141,39 @@ __global__ void __launch_bounds__(RT, 1) lk_substeps_resident(Phase2 A, Resident
                 cluster_sync_all();
             }
         }
+        MRec cur;
         for (uint32_t it = 0; it < R.iters; ++it) {
             for (uint32_t c = 0; c < R.njcol; ++c) {
                 const uint32_t k1 = R.joff[c + 1];
                 for (uint32_t k = R.joff[c] + t0; k < k1; k += nt) joint_one(A, R.jorder[k]);
                 cluster_sync_all();
             }
+            // Software-pipelined: the thread's first manifold of the next
+            // contact colour (the next iteration's first colour after the
+            // last) is loaded before this colour is solved.  Within a
+            // substep a record changes only in its accumulators, which only
+            // the manifold's own thread writes (manifold k of colour c is
+            // always thread (k - coff[c]) mod nt's), so the early load sees
+            // their latest values, unless the next manifold is this one
+            // (a single colour), whose accumulators are then reloaded.
             for (uint32_t c = 0; c < R.ncol; ++c) {
-                const uint32_t k1 = R.coff[c + 1];
-                for (uint32_t k = R.coff[c] + t0; k < k1; k += nt)
+                const uint32_t k0 = R.coff[c] + t0, k1 = R.coff[c + 1];
+                const uint32_t cn = c + 1 < R.ncol ? c + 1 : 0u;
+                const bool more = c + 1 < R.ncol || it + 1 < R.iters;
+                const uint32_t kn = R.coff[cn] + t0;
+                MRec next;
+                if (more && kn < R.coff[cn + 1]) next = load_rec(A.pk, kn);
+                if (k0 < k1) {
+                    if (c > 0 || it > 0) {
+                        if (R.ncol == 1) cur.v5 = A.pk.v5[k0];
+                    } else {
+                        cur = load_rec(A.pk, k0);
+                    }
+                    solve_contact_rec(A.pk, cur, A.s.mx, A.s.my, A.s.L, k0, A.warm);
+                }
+                for (uint32_t k = k0 + nt; k < k1; k += nt)
                     solve_contact_packed(A.pk, A.s.mx, A.s.my, A.s.L, k, A.warm);
+                cur = next;
                 cluster_sync_all();
             }
         }
