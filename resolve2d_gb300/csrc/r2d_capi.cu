@@ -139,6 +139,7 @@ struct Engine {
     uint32_t njoints = 0, nexcl = 0;
     uint8_t* d_jtype = nullptr;
     uint32_t* d_jb1 = nullptr;
+    uint64_t joint_epoch = 0;  // bumped by every upload of the joint arrays
     uint32_t* d_jb2 = nullptr;
     float* d_jprm = nullptr;
     unsigned long long* d_excl = nullptr;
@@ -455,6 +456,7 @@ struct Engine {
                         const std::vector<unsigned long long>& xkey) {
         // joints are grouped per world in the order given (insertion order inside a world)
         njoints = (uint32_t)jtype.size();
+        ++joint_epoch;  // the grid pipeline's cached joint colourings are stale
         std::vector<uint32_t> order(njoints);
         for (uint32_t j = 0; j < njoints; ++j) order[j] = j;
         std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return jworld[a] < jworld[b]; });
@@ -915,6 +917,7 @@ struct Engine {
         in.jb2 = d_jb2 + d.joint_off;
         in.jprm = d_jprm + (size_t)d.joint_off * JOINT_PARAMS;
         in.nj = d.nj;
+        in.joint_epoch = joint_epoch;
         in.excl = d_excl + d.excl_off;
         in.nexcl = d.nexcl;
         in.ngrav = d.ngrav;

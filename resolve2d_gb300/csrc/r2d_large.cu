@@ -279,18 +279,20 @@ __device__ __forceinline__ bool lk_excluded(const unsigned long long* ex, uint32
 
 // Candidates: every two entries of one bucket, filtered as lib.zig:273-282,
 // deduplicated like its "manifold already exists" test (lib.zig:278-281).
-// One warp per entry; its lanes take the bucket's later entries 32 at a time.
+// PAIR_GROUP lanes per entry take the bucket's later entries PAIR_GROUP at a
+// time (a pyramid cell holds ~16 entries, a sparse box's ~3).
+constexpr uint32_t PAIR_GROUP = 8;
 __global__ void lk_pairs(Phase1 A, uint32_t E) {
-    const uint64_t w = ((uint64_t)blockIdx.x * LT + threadIdx.x) >> 5;
+    const uint64_t w = ((uint64_t)blockIdx.x * LT + threadIdx.x) / PAIR_GROUP;
     if (w >= E) return;
-    const uint32_t e = (uint32_t)w, lane = threadIdx.x & 31u;
+    const uint32_t e = (uint32_t)w, lane = threadIdx.x % PAIR_GROUP;
     const uint32_t i = A.ebody[e];
     const uint32_t end = A.table[A.ebucket[e]];
     const f2 pi = {A.st(S_AABB_X, i), A.st(S_AABB_Y, i)};
     const float hwi = A.st(S_AABB_HW, i), hhi = A.st(S_AABB_HH, i);
     const bool sti = (A.s.kind[i] & K_STATIC) != 0;
     const unsigned long long mask = (unsigned long long)A.hs - 1ull;
-    for (uint32_t q = A.eslot[e] + 1u + lane; q < end; q += 32u) {
+    for (uint32_t q = A.eslot[e] + 1u + lane; q < end; q += PAIR_GROUP) {
         const uint32_t j = A.sbody[q];
         if (j == i) continue;
         if (sti && (A.s.kind[j] & K_STATIC)) continue;
@@ -857,6 +859,8 @@ struct Phase2 {
     const uint32_t* jb1;
     const uint32_t* jb2;
     const float* jprm;
+    const uint4* jhead;     // colour-major joints: {type, body 1, body 2, -}
+    const float* jprm_cm;   // and their parameters, [k][JOINT_PARAMS]
     const uint32_t* order;  // constraints of the colour [k0, k1)
     uint32_t k0, k1;
     double* pos64;          // f64 pose (FP64-positions mode), else null
@@ -1060,13 +1064,28 @@ __global__ void lk_warm_copy(const uint32_t* keys, const float4* vals, uint32_t 
     if (key != 0xFFFFFFFFu) warm_insert(nkeys, nvals, nhs, warm_key64(key >> 16, key & 0xFFFFu), vals[q]);
 }
 
-__device__ __forceinline__ void joint_one(const Phase2& A, uint32_t j) {
-    solve_joint(A.s, __ldg(A.jtype + j), __ldg(A.jb1 + j), __ldg(A.jb2 + j), A.jprm + (size_t)j * JOINT_PARAMS, A.h);
+// the joint at colour-major position k (one coalesced head, 32 B of parameters)
+__device__ __forceinline__ void joint_one(const Phase2& A, uint32_t k) {
+    const uint4 h = A.jhead[k];
+    solve_joint(A.s, (uint8_t)h.x, h.y, h.z, A.jprm_cm + (size_t)k * JOINT_PARAMS, A.h);
 }
 
 __global__ void lk_joints(Phase2 A) {
     const uint32_t k = A.k0 + blockIdx.x * LT + threadIdx.x;
-    if (k < A.k1) joint_one(A, A.order[k]);
+    if (k < A.k1) joint_one(A, k);
+}
+
+// joints in colour-major order: position k holds joint order[k]
+__global__ void lk_joint_pack(const uint8_t* jtype, const uint32_t* jb1, const uint32_t* jb2, const float* jprm,
+                              const uint32_t* order, uint32_t nj, uint4* jhead, float* jprm_cm) {
+    const uint32_t k = blockIdx.x * LT + threadIdx.x;
+    if (k >= nj) return;
+    const uint32_t j = order[k];
+    jhead[k] = make_uint4(jtype[j], jb1[j], jb2[j], 0u);
+    const float4* src = reinterpret_cast<const float4*>(jprm + (size_t)j * JOINT_PARAMS);
+    float4* dst = reinterpret_cast<float4*>(jprm_cm + (size_t)k * JOINT_PARAMS);
+    dst[0] = src[0];
+    dst[1] = src[1];
 }
 
 // integration (lib.zig:238-249); the last substep clears consumed forces
@@ -1145,7 +1164,7 @@ __global__ void __launch_bounds__(RT, 1) lk_substeps_resident(Phase2 A, Resident
         for (uint32_t it = 0; it < R.iters; ++it) {
             for (uint32_t c = 0; c < R.njcol; ++c) {
                 const uint32_t k1 = R.joff[c + 1];
-                for (uint32_t k = R.joff[c] + t0; k < k1; k += nt) joint_one(A, R.jorder[k]);
+                for (uint32_t k = R.joff[c] + t0; k < k1; k += nt) joint_one(A, k);
                 cluster_sync_all();
             }
             // Software-pipelined: the thread's first manifold of the next
@@ -1364,6 +1383,12 @@ struct LargeWorld::Impl {
     uint32_t *jadj = nullptr, *jadjl = nullptr, *jprio = nullptr;  // the joints' own adjacency
     uint32_t *npred = nullptr, *jnpred = nullptr, *preds = nullptr, *jpreds = nullptr;
     uint32_t *wl0 = nullptr, *wl1 = nullptr, *jwl0 = nullptr, *jwl1 = nullptr;  // colouring worklists
+    // colour-major joints, and the joint arrays they were coloured from
+    uint4* jhead = nullptr;
+    float* jprm_cm = nullptr;
+    size_t cap_jh = 0, cap_jp = 0;
+    uint64_t joint_epoch = 0;
+    uint32_t joint_nj = 0;
     size_t cap_pr = 0, cap_prr = 0;
     uint8_t* jcol = nullptr;
     uint32_t* jorder = nullptr;
@@ -1395,7 +1420,8 @@ struct LargeWorld::Impl {
                       nx, ny, fric, r1x, r1y, r2x, r2y, depth, odepth, mn, mt, apn, apt, bias, adjl, prio,
                       jcol, jorder, cnt, entries, hist, tsum, dk, dc, dd, ma2, mb2, mp02, mnp2, mcol2, nx2, ny2,
                       r1x2, r1y2, r2x2, r2y2, depth2, odepth2, apn2, apt2, jadj, jadjl, jprio, npred, jnpred,
-                      preds, jpreds, pk[0], pk[1], pk[2], pk[3], pk[4], pk[5], pk[6], mom4, wl0, wl1, jwl0, jwl1};
+                      preds, jpreds, pk[0], pk[1], pk[2], pk[3], pk[4], pk[5], pk[6], mom4, wl0, wl1, jwl0, jwl1,
+                      jhead, jprm_cm};
         for (void* p : ps)
             if (p) cudaFree(p);
         for (int b = 0; b < 2; ++b) {
@@ -1544,7 +1570,7 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
         A.pairs = I.pairs; A.hset = I.hset; A.np = np; A.hs = hs;
         LTRY(cudaMemsetAsync(I.hset, 0xFF, sizeof(unsigned long long) * hs, st));
         LTRY(cudaMemsetAsync(I.cnt, 0, sizeof(uint32_t) * LC_N, st));
-        LAUNCH(lk_pairs, blocks(32ull * E), A, E);
+        LAUNCH(lk_pairs, blocks((uint64_t)PAIR_GROUP * E), A, E);
         LTRY(cudaMemcpyAsync(I.h_cnt, I.cnt, sizeof(uint32_t) * LC_N, cudaMemcpyDeviceToHost, st));
         LTRY(cudaStreamSynchronize(st));
         if (!I.h_cnt[LC_PAIR_OVERFLOW]) {
@@ -1620,9 +1646,21 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
     if (int r = colour(false, M, I.mcol, I.corder, cb_c, I.cnt, I.adj, I.adjl, I.prio, I.npred, I.preds, I.wl0,
                        I.wl1))
         return r;
-    if (int r = colour(true, in.nj, I.jcol, I.jorder, cb_j, I.cnt + LC_N, I.jadj, I.jadjl, I.jprio, I.jnpred,
-                       I.jpreds, I.jwl0, I.jwl1))
-        return r;
+    // The joint colouring depends on the joint arrays alone: it is kept while
+    // their epoch stays the same.
+    const bool joints_kept = in.nj && in.joint_epoch && in.joint_epoch == I.joint_epoch && in.nj == I.joint_nj;
+    if (!joints_kept) {
+        I.joint_epoch = 0;
+        if (int r = colour(true, in.nj, I.jcol, I.jorder, cb_j, I.cnt + LC_N, I.jadj, I.jadjl, I.jprio, I.jnpred,
+                           I.jpreds, I.jwl0, I.jwl1))
+            return r;
+        if (in.nj) {
+            LTRY(regrow(I.cap_jh, in.nj, {LB(I.jhead)}));
+            LTRY(regrow(I.cap_jp, (size_t)in.nj * JOINT_PARAMS, {LB(I.jprm_cm)}));
+            LAUNCH(lk_joint_pack, blocks(in.nj), in.jtype, in.jb1, in.jb2, in.jprm, I.jorder, in.nj, I.jhead,
+                   I.jprm_cm);
+        }
+    }
     // one round trip for both colourings: their flags and colour offsets
     uint32_t* hc = I.h_cnt + H_COLOUR;  // both counter blocks, then both result blocks
     LTRY(cudaMemcpyAsync(hc, I.cnt, sizeof(uint32_t) * 2 * LC_N, cudaMemcpyDeviceToHost, st));
@@ -1639,6 +1677,10 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
             return -4;
         }
         rounds[j] = h[LC_ROUNDS];
+    }
+    if (in.nj && !joints_kept) {
+        I.joint_epoch = in.joint_epoch;
+        I.joint_nj = in.nj;
     }
     uint32_t largest = 0;
     auto offsets = [&](const uint32_t* cb, std::vector<uint32_t>& off) {
@@ -1677,6 +1719,7 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
     S.ngrav = in.ngrav;
     for (int k = 0; k < MAX_GRAVITY; ++k) S.g[k] = in.g[k];
     S.jtype = in.jtype; S.jb1 = in.jb1; S.jb2 = in.jb2; S.jprm = in.jprm;
+    S.jhead = I.jhead; S.jprm_cm = I.jprm_cm;
     S.pos64 = in.pos64;
     S.warm = in.warm;
     S.pk = Packed{I.pk[0], I.pk[1], I.pk[2], I.pk[3], I.pk[4], I.pk[5], I.pk[6],
@@ -1978,7 +2021,7 @@ int static_world_step(const StaticStepArgs& in, cudaStream_t st, std::string* ms
     LAUNCH(lk_emit, blocks(E), A, E);
     SCAN(A.table, T);
     LAUNCH(lk_scatter, blocks(E), A, E);
-    LAUNCH(lk_pairs, blocks(32ull * E), A, E);
+    LAUNCH(lk_pairs, blocks((uint64_t)PAIR_GROUP * E), A, E);
     LTRY(cudaMemcpyAsync(h, cnt, sizeof(uint32_t) * LC_N, cudaMemcpyDeviceToHost, st));
     LTRY(cudaStreamSynchronize(st));
     if (h[LC_PAIR_OVERFLOW]) {

@@ -27,6 +27,7 @@ struct LargeInputs {
     const uint32_t* jb2;
     const float* jprm;     // [nj][JOINT_PARAMS]
     uint32_t nj;
+    uint64_t joint_epoch;  // changes whenever the joint arrays change; 0 = unknown (recolour every step)
     const unsigned long long* excl;  // sorted (lo << 32 | hi) keys of this world
     uint32_t nexcl;
     uint32_t ngrav;
