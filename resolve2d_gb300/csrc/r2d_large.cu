@@ -15,9 +15,12 @@
  *                                  its colour once every neighbour that comes
  *                                  before it in priority order has one, which
  *                                  is exactly the sequential first-fit
- *                                  colouring of r2d_colour.h
- *   substeps                       lib.zig:199-250, one kernel per phase and
- *                                  one per colour of each iteration
+ *                                  colouring of r2d_colour.h; all rounds in
+ *                                  one thread-block cluster
+ *   substeps                       lib.zig:199-250 on colour-major packed
+ *                                  records: every substep in one resident
+ *                                  cluster, or one kernel per phase and per
+ *                                  colour of each iteration
  *
  * Buffer sizes are exact where they can be (cell entries are counted before
  * they are written; a manifold needs a candidate pair; a manifold has at most
