@@ -1,8 +1,9 @@
 """The grid-wide pipeline against the oracle, through the C ABI.
 
 Worlds above 520 bodies, worlds whose buffers do not fit one CTA's shared
-memory, and every world under R2D_FLAG_GRID_PIPELINE step through one kernel
-per phase and per colour over global scratch (r2d_large.cu).  It shares the
+memory, and every world under R2D_FLAG_GRID_PIPELINE step through the grid
+pipeline over global scratch (r2d_large.cu): cluster-wide colouring, then
+every substep in one resident cluster or one kernel per phase and colour.  It shares the
 fused kernel's per-item device functions and its colouring, so the bar is the
 same: bit-identical state, pair sets, manifolds and colourings.
 """
@@ -180,3 +181,61 @@ def test_config2_chains_and_motors_first_steps():
     w, o = run_pair(sc, steps=6, check_every=3)
     _, oj = o.colours()
     np.testing.assert_array_equal(w.joint_colours(len(sc.jtype)), oj)
+
+
+def test_new_joints_midrun_are_recoloured():
+    """A grid-pipeline world keeps its joint colouring from step to step; new
+    joints (here the same joints in reverse insertion order, which changes their
+    priorities) must be coloured and packed afresh: stepping on after
+    set_joints equals a world that had those joints from the same state."""
+    sc = scenes.random_scene(21, n=40, joints=True)
+    rev = slice(None, None, -1)
+    jt, j1, j2, jp = (np.ascontiguousarray(a[rev]) for a in (sc.jtype, sc.jid1, sc.jid2, sc.jprm))
+    w1 = World.from_scene(sc, debug=True, grid=True)
+    kept = World.from_scene(sc, grid=True)
+    for _ in range(10):
+        w1.process(sc.dt, sc.sub_steps, sc.iters)
+        kept.process(sc.dt, sc.sub_steps, sc.iters)
+    w1.sync()
+    kept.sync()
+    mid = w1.read_state()
+    w1.set_joints(jt, j1, j2, jp)
+    fresh = World.from_scene(sc, debug=True, grid=True)
+    fresh.set_joints(jt, j1, j2, jp)
+    fresh.write_state(mid)
+    for _ in range(10):
+        for w in (w1, fresh, kept):
+            w.process(sc.dt, sc.sub_steps, sc.iters)
+    for w in (w1, fresh, kept):
+        w.sync()
+    assert_state_equal(w1.read_state(), fresh.read_state(), "set_joints mid-run")
+    np.testing.assert_array_equal(w1.joint_colours(len(jt)), fresh.joint_colours(len(jt)))
+    # the order matters, so a stale colouring would have shown
+    assert not np.array_equal(kept.read_state(), w1.read_state())
+
+
+def test_per_colour_launch_path():
+    """Small worlds take the resident cluster; R2D_RESIDENT=0 (read once per
+    process, hence a child process) forces the one-launch-per-phase-and-colour
+    path that large colours take, against the oracle, with joints, substeps and
+    warm starting."""
+    import os
+    import subprocess
+    import sys
+
+    here = os.path.dirname(os.path.abspath(__file__))
+    code = (
+        "import sys; sys.path[:0] = [%r, %r, %r]\n"
+        "from parity import run_pair\n"
+        "from resolve2d_gb300 import scenes\n"
+        "for seed in (31, 32):\n"
+        "    run_pair(scenes.random_scene(seed, n=40, joints=True), steps=20, check_every=5, grid=True)\n"
+        "run_pair(scenes.random_scene(33, n=30, joints=True), steps=12, check_every=4, sub_steps=3, iters=4, grid=True)\n"
+        "run_pair(scenes.random_scene(34, n=40, joints=True), steps=20, check_every=5, warm=True, grid=True)\n"
+        "run_pair(scenes.config0(), steps=10, check_every=5, grid=True)\n"
+        "print('per-colour path ok')\n" % (here, os.path.dirname(here), os.path.join(os.path.dirname(here), "oracle"))
+    )
+    env = dict(os.environ, R2D_RESIDENT="0")
+    r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-3000:]
+    assert "per-colour path ok" in r.stdout
