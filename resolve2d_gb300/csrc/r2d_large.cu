@@ -1208,6 +1208,18 @@ __global__ void __launch_bounds__(RT, 1) lk_substeps_resident(Phase2 A, Resident
     for (uint32_t m = t0; m < A.nman; m += nt) unpack_one(A, m);
 }
 
+// One iteration's contact colours in one cluster, a cluster barrier between
+// colours: for worlds whose joint colours are too large for the resident
+// kernel but whose contact colours are not.
+__global__ void __launch_bounds__(RT, 1) lk_contacts_cluster(Phase2 A, const uint32_t* coff, uint32_t ncol) {
+    const uint32_t t0 = blockIdx.x * RT + threadIdx.x, nt = gridDim.x * RT;
+    for (uint32_t c = 0; c < ncol; ++c) {
+        const uint32_t k1 = coff[c + 1];
+        for (uint32_t k = coff[c] + t0; k < k1; k += nt) solve_contact_packed(A.pk, A.s.mx, A.s.my, A.s.L, k, A.warm);
+        if (c + 1 < ncol) cluster_sync_all();
+    }
+}
+
 // debug taps in the oracle's manifold layout (DebugOut)
 __global__ void lk_dump(SWT<uint32_t> s, uint32_t m_count, uint32_t* keys, float* data, uint32_t* colours) {
     const uint32_t m = blockIdx.x * LT + threadIdx.x;
@@ -1272,7 +1284,7 @@ cudaError_t regrow(size_t& cap, size_t need, std::initializer_list<Buf> bufs) {
 }
 
 constexpr int MAX_DEVICES = 64;
-std::atomic<int> g_cluster_size[2][MAX_DEVICES];  // [resident kernel][device]; 0 = not known yet
+std::atomic<int> g_cluster_size[3][MAX_DEVICES];  // [resident kernel][device]; 0 = not known yet
 
 // The cluster size of a resident kernel: 16 CTAs where the device can hold
 // such a cluster with the kernel's resources, else the portable 8.  Found
@@ -1341,16 +1353,29 @@ cudaError_t scan(uint32_t* a, uint32_t n, uint32_t* tsum, cudaStream_t st, uint3
     return cudaGetLastError();
 }
 
-// Whether the substeps run as one resident cluster or as one launch per
-// phase and colour (R2D_RESIDENT=0 / 1 forces either).  The cluster wins
-// while its threads cover a colour in a few passes.
-bool use_resident_substeps(uint32_t largest_colour, int cl) {
+// Whether the substeps run as one resident cluster, or as one launch per
+// phase and colour, with an iteration's contact colours then in one cluster
+// launch when they fit.  The cluster wins while its threads cover a colour in
+// a few passes.  R2D_RESIDENT forces a choice: 1 the resident cluster, 0 one
+// launch per colour throughout, 2 per-colour joints with clustered contacts.
+int resident_override() {
     static const int forced = [] {
         const char* e = getenv("R2D_RESIDENT");
         return e && *e ? atoi(e) : -1;
     }();
-    if (forced >= 0) return forced != 0;
+    return forced;
+}
+
+bool use_resident_substeps(uint32_t largest_colour, int cl) {
+    const int o = resident_override();
+    if (o >= 0) return o == 1;
     return largest_colour <= RESIDENT_MAX_PASSES * (uint32_t)cl * RT;
+}
+
+bool use_contacts_cluster(uint32_t largest_contact_colour, int cl) {
+    const int o = resident_override();
+    if (o >= 0) return o == 2;
+    return largest_contact_colour <= RESIDENT_MAX_PASSES * (uint32_t)cl * RT;
 }
 
 }  // namespace
@@ -1400,7 +1425,7 @@ struct LargeWorld::Impl {
     uint32_t* hist = nullptr;               // two colouring result blocks (contacts, joints)
     uint32_t* tsum = nullptr;               // tile sums of the multi-block scan
     size_t cap_ts = 0;
-    int cl_solve = 0, cl_colour = 0;        // cluster sizes of the resident substeps and colouring
+    int cl_solve = 0, cl_colour = 0, cl_contacts = 0;  // cluster sizes of the resident kernels
     uint32_t* h_cnt = nullptr;              // pinned: counters, then the entry total
     // debug taps
     uint32_t *dk = nullptr, *dc = nullptr;
@@ -1512,6 +1537,7 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
         LTRY(cudaMalloc((void**)&I.hist, sizeof(uint32_t) * 2 * CB_WORDS));
         LTRY(resident_cluster(0, lk_substeps_resident, RT, &I.cl_solve));
         LTRY(resident_cluster(1, lk_colour_cluster, CT, &I.cl_colour));
+        LTRY(resident_cluster(2, lk_contacts_cluster, RT, &I.cl_contacts));
     }
     LTRY(regrow(I.cap_n, (size_t)n + 1,
                 {LB(I.inv_m), LB(I.inv_i), LB(I.cs), LB(I.sn), LB(I.tq), LB(I.ang_prev), LB(I.kind), LB(I.rx0),
@@ -1685,14 +1711,15 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
         I.joint_epoch = in.joint_epoch;
         I.joint_nj = in.nj;
     }
-    uint32_t largest = 0;
     auto offsets = [&](const uint32_t* cb, std::vector<uint32_t>& off) {
         const uint32_t ncol = cb[CB_NCOL];
         off.assign(cb + CB_OFF, cb + CB_OFF + ncol + 1);
-        for (uint32_t c = 0; c < ncol; ++c) largest = std::max(largest, off[c + 1] - off[c]);
+        uint32_t big = 0;
+        for (uint32_t c = 0; c < ncol; ++c) big = std::max(big, off[c + 1] - off[c]);
+        return big;
     };
-    offsets(hc + 2 * LC_N, I.coff);
-    offsets(hc + 2 * LC_N + CB_WORDS, I.joff);
+    const uint32_t largest_contacts = offsets(hc + 2 * LC_N, I.coff);
+    const uint32_t largest = std::max(largest_contacts, offsets(hc + 2 * LC_N + CB_WORDS, I.joff));
     I.nman = M;
     I.nj = in.nj;
     // manifolds in colour-major order: colour c is manifolds [coff[c], coff[c+1])
@@ -1728,6 +1755,9 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
     S.pk = Packed{I.pk[0], I.pk[1], I.pk[2], I.pk[3], I.pk[4], I.pk[5], I.pk[6],
                   in.nj == 0 && !in.warm ? I.mom4 : nullptr};
     const bool resident = use_resident_substeps(largest, I.cl_solve);
+    // on the per-colour path, an iteration's contact colours may still share one cluster launch
+    const bool contacts_clustered = !resident && M && I.coff.size() > 2 &&
+                                    use_contacts_cluster(largest_contacts, I.cl_contacts);
     if (resident) {
         ResidentPlan R{};
         R.jorder = I.jorder;
@@ -1756,6 +1786,12 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
                 S.k0 = I.joff[c];
                 S.k1 = I.joff[c + 1];
                 LAUNCH(lk_joints, blocks(S.k1 - S.k0), S);
+            }
+            if (contacts_clustered) {
+                LTRY(launch_resident(lk_contacts_cluster, I.cl_contacts, RT, st, S, cb_c + CB_OFF,
+                                     (uint32_t)I.coff.size() - 1));
+                ++I.nlaunch;
+                continue;
             }
             S.order = I.corder;
             for (size_t c = 0; c + 1 < I.coff.size(); ++c) {

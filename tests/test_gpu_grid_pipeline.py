@@ -214,11 +214,13 @@ def test_new_joints_midrun_are_recoloured():
     assert not np.array_equal(kept.read_state(), w1.read_state())
 
 
-def test_per_colour_launch_path():
-    """Small worlds take the resident cluster; R2D_RESIDENT=0 (read once per
-    process, hence a child process) forces the one-launch-per-phase-and-colour
-    path that large colours take, against the oracle, with joints, substeps and
-    warm starting."""
+@pytest.mark.parametrize("mode", ["0", "2"])
+def test_per_colour_launch_path(mode):
+    """Small worlds take the resident cluster; R2D_RESIDENT (read once per
+    process, hence a child process) forces the paths that large colours take:
+    0 one launch per phase and colour, 2 per-colour joints with each
+    iteration's contact colours in one cluster launch.  Against the oracle,
+    with joints, substeps and warm starting."""
     import os
     import subprocess
     import sys
@@ -235,7 +237,7 @@ def test_per_colour_launch_path():
         "run_pair(scenes.config0(), steps=10, check_every=5, grid=True)\n"
         "print('per-colour path ok')\n" % (here, os.path.dirname(here), os.path.join(os.path.dirname(here), "oracle"))
     )
-    env = dict(os.environ, R2D_RESIDENT="0")
+    env = dict(os.environ, R2D_RESIDENT=mode)
     r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-3000:]
     assert "per-colour path ok" in r.stdout
