@@ -234,18 +234,20 @@ __device__ bool colour_greedy_sorted(uint32_t count, uint32_t n, Ends ends, Mix 
                 const uint32_t pending = __ballot_sync(0xffffffffu, !done);
                 if (!pending) break;
                 if (!done && !(earlier & pending)) {
-                    uint32_t w0 = 0u, w1 = 0u, w2 = 0u, w3 = 0u;
-                    if (na) {
-                        w0 |= cmask[a]; w1 |= cmask[n + a]; w2 |= cmask[2 * n + a]; w3 |= cmask[3 * n + a];
-                    }
-                    if (nb2) {
-                        w0 |= cmask[b]; w1 |= cmask[n + b]; w2 |= cmask[2 * n + b]; w3 |= cmask[3 * n + b];
-                    }
+                    // the lowest free colour, reading a mask word only when
+                    // every colour below it is taken (colours are nearly
+                    // always below 32)
+                    auto word = [&](uint32_t q) {
+                        return (na ? cmask[q * n + a] : 0u) | (nb2 ? cmask[q * n + b] : 0u);
+                    };
                     uint32_t c = 128u;
-                    if (w0 != 0xFFFFFFFFu) c = (uint32_t)__ffs(~w0) - 1u;
-                    else if (w1 != 0xFFFFFFFFu) c = 32u + (uint32_t)__ffs(~w1) - 1u;
-                    else if (w2 != 0xFFFFFFFFu) c = 64u + (uint32_t)__ffs(~w2) - 1u;
-                    else if (w3 != 0xFFFFFFFFu) c = 96u + (uint32_t)__ffs(~w3) - 1u;
+                    for (uint32_t q = 0; q < 4; ++q) {
+                        const uint32_t wq = word(q);
+                        if (wq != 0xFFFFFFFFu) {
+                            c = 32u * q + (uint32_t)__ffs(~wq) - 1u;
+                            break;
+                        }
+                    }
                     if (c >= (uint32_t)MAX_COLOURS) {
                         overflow = 1;
                         c = 0u;
