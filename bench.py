@@ -496,6 +496,17 @@ def main():
                                 "kind": "port", "seconds": secs,
                                 "sample": f"all {sc.nworlds} worlds x {cpu_steps} steps from the settled state "
                                           "(C++ restatement of Solver.process; Zig toolchain absent)"}
+        # the same step on one core (the reference itself is single-threaded), on a bounded
+        # sample: the first worlds holding about a tenth of the bodies, for about five seconds
+        sub_w = int(np.searchsorted(sc.body_off, nb // 10)) + 1
+        sub = sc.worlds(0, min(sub_w, sc.nworlds))
+        sub_state = np.ascontiguousarray(settled[:, : sub.nbodies])
+        one1 = oracle_time(sub, sub_state, 1, 1)
+        steps1 = max(1, min(50, int(5.0 / max(one1, 1e-3))))
+        secs1 = oracle_time(sub, sub_state, steps1, 1)
+        line["cpu_baseline"]["one_core"] = {
+            "value": sub.nbodies * steps1 / secs1, "unit": "body-steps/s", "seconds": secs1,
+            "sample": f"worlds 0..{sub.nworlds - 1} ({sub.nbodies} bodies) x {steps1} steps on one thread"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -858,14 +858,9 @@ struct Phase2 {
     bool first, last, disc_rot;
     uint32_t ngrav;
     float g[MAX_GRAVITY];
-    const uint8_t* jtype;
-    const uint32_t* jb1;
-    const uint32_t* jb2;
-    const float* jprm;
     const uint4* jhead;     // colour-major joints: {type, body 1, body 2, -}
     const float* jprm_cm;   // and their parameters, [k][JOINT_PARAMS]
-    const uint32_t* order;  // constraints of the colour [k0, k1)
-    uint32_t k0, k1;
+    uint32_t k0, k1;        // the colour-major constraints one per-colour launch solves
     double* pos64;          // f64 pose (FP64-positions mode), else null
     bool warm;              // warm starting
 
@@ -1132,9 +1127,9 @@ __global__ void lk_integrate(Phase2 A) {
 }
 
 // The colour offsets of one step: contact colour c is manifolds [coff[c],
-// coff[c+1]) (colour-major), joint colour c is jorder[joff[c], joff[c+1]).
+// coff[c+1]), joint colour c is packed joints [joff[c], joff[c+1]) (both
+// colour-major).
 struct ResidentPlan {
-    const uint32_t* jorder;
     const uint32_t* coff;
     const uint32_t* joff;
     uint32_t ncol, njcol, sub_steps, iters;
@@ -1748,7 +1743,6 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
     S.disc_rot = in.disc_rot;
     S.ngrav = in.ngrav;
     for (int k = 0; k < MAX_GRAVITY; ++k) S.g[k] = in.g[k];
-    S.jtype = in.jtype; S.jb1 = in.jb1; S.jb2 = in.jb2; S.jprm = in.jprm;
     S.jhead = I.jhead; S.jprm_cm = I.jprm_cm;
     S.pos64 = in.pos64;
     S.warm = in.warm;
@@ -1760,7 +1754,6 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
                                     use_contacts_cluster(largest_contacts, I.cl_contacts);
     if (resident) {
         ResidentPlan R{};
-        R.jorder = I.jorder;
         R.coff = cb_c + CB_OFF; R.joff = cb_j + CB_OFF;
         R.ncol = (uint32_t)I.coff.size() - 1; R.njcol = (uint32_t)I.joff.size() - 1;
         R.sub_steps = sub_steps; R.iters = iters;
@@ -1773,7 +1766,6 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
         LAUNCH(lk_forces, blocks(n), S);
         if (M) LAUNCH(lk_prestep, blocks(M), S);
         if (in.warm && sub == 0) {  // the warm-started impulses, colour by colour
-            S.order = I.corder;
             for (size_t c = 0; c + 1 < I.coff.size(); ++c) {
                 S.k0 = I.coff[c];
                 S.k1 = I.coff[c + 1];
@@ -1781,7 +1773,6 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
             }
         }
         for (uint32_t it = 0; it < iters; ++it) {
-            S.order = I.jorder;
             for (size_t c = 0; c + 1 < I.joff.size(); ++c) {
                 S.k0 = I.joff[c];
                 S.k1 = I.joff[c + 1];
@@ -1793,7 +1784,6 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
                 ++I.nlaunch;
                 continue;
             }
-            S.order = I.corder;
             for (size_t c = 0; c + 1 < I.coff.size(); ++c) {
                 S.k0 = I.coff[c];
                 S.k1 = I.coff[c + 1];
@@ -2136,7 +2126,6 @@ int static_world_step(const StaticStepArgs& in, cudaStream_t st, std::string* ms
                   reinterpret_cast<float4*>(base + SL.pk[4]), reinterpret_cast<float4*>(base + SL.pk[5]),
                   reinterpret_cast<float4*>(base + SL.pk[6]), SP(float4, mom4)};
     ResidentPlan R{};
-    R.jorder = nullptr;
     R.coff = hist + CB_OFF; R.joff = nullptr;
     R.ncol = ncol; R.njcol = 0;
     R.sub_steps = in.sub_steps; R.iters = in.iters;
