@@ -2,7 +2,8 @@
 batched distribution, seed 4, 3,600 steps at dt 1/60).
 
     python tests/precision_study.py [--worlds 16384] [--steps 3600]
-        [--oracle-worlds 256] [--out profiles/precision_config4.json]
+        [--checkpoints 1,10,60,120,300,600] [--oracle-worlds 256]
+        [--out profiles/precision_config4.json]
 
 Two GPU modes step every world from the same start: f32 throughout (the
 reference's arithmetic, bit-identical to the f32 oracle) and f32 with the
@@ -90,7 +91,8 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--worlds", type=int, default=16384)
     ap.add_argument("--steps", type=int, default=3600)
-    ap.add_argument("--checkpoint", type=int, default=600)
+    ap.add_argument("--checkpoints", default="1,10,60,120,300,600",
+                    help="steps (besides the last) at which the errors are measured")
     ap.add_argument("--oracle-worlds", type=int, default=256)
     ap.add_argument("--threads", type=int, default=len(os.sched_getaffinity(0)))
     ap.add_argument("--out")
@@ -101,7 +103,7 @@ def main():
     sub = sc.worlds(0, a.oracle_worlds)
     props, _ = derive_props_state(sc.kind, sc.opt)
     sprops, _ = derive_props_state(sub.kind, sub.opt)
-    checks = sorted({min(a.checkpoint, a.steps), a.steps})
+    checks = sorted({min(int(c), a.steps) for c in a.checkpoints.split(",") if c.strip()} | {a.steps})
     res = {"workload": f"config4: {sc.nworlds} worlds, {sc.nbodies} bodies, seed 4, dt 1/60, {a.steps} steps",
            "oracle_worlds": a.oracle_worlds, "oracle_bodies": sub.nbodies, "checkpoints": {}}
 
