@@ -2,10 +2,11 @@
  * r2d_large.cu -- the step of one world too large for a single CTA's shared
  * memory (a 12,001-body pyramid, a 200,004-body box with chains and motors).
  *
- * The stages of the fused per-world kernel run as grid-wide kernels over
- * global scratch buffers, and every per-item computation is the fused
- * kernel's own device function (r2d_device.cuh, r2d_solve.cuh), so both
- * paths produce the same bits for the same world:
+ * The stages of the fused per-world kernel run as grid-wide and
+ * cluster-resident kernels over global scratch buffers.  Every per-item
+ * computation is the fused kernel's own device function (r2d_device.cuh,
+ * r2d_solve.cuh) or, for the contact solve on packed records, its arithmetic
+ * in the same order, so both paths produce the same bits for the same world:
  *
  *   cells, entries, bucket sort    SpatialHash.zig:19-137 (a counting sort)
  *   candidate pairs                lib.zig:264-282 (bucket sharing, filters,
@@ -56,7 +57,6 @@ enum LargeCounter : int {
     LC_PAIRS = 0,      // candidate pairs found
     LC_MANIFOLDS,      // manifolds built
     LC_POINTS,         // contact points built
-    LC_PENDING,        // constraints still uncoloured after a colouring round
     LC_PAIR_OVERFLOW,  // the pair set or list was full
     LC_NONFINITE,      // a body's AABB has no cell index
     LC_COLOURS,        // a constraint needed more than MAX_COLOURS colours
