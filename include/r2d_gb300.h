@@ -110,7 +110,14 @@ enum {
      * preStep; and since such a sum must be able to shrink, impulses below
      * the reference's 1e-4 skip threshold are applied (clamped at zero)
      * instead of skipped. */
-    R2D_FLAG_WARM_START = 8u
+    R2D_FLAG_WARM_START = 8u,
+    /* Sleeping (no counterpart in the reference; its roadmap lists it,
+     * README.md:64-67): a world whose every non-static body ends 60
+     * consecutive steps slower than 0.01 units/s and 0.01 rad/s is not
+     * stepped again until the host writes to the engine (state, fields,
+     * bodies, gravity, joints or exclusions), which wakes every world.
+     * r2d_*_sleep_frames reads the per-world counters. */
+    R2D_FLAG_SLEEP = 16u
 };
 
 typedef struct r2d_config {
@@ -177,6 +184,9 @@ R2D_API int r2d_solver_read_positions_f64(r2d_solver* s, double* pose);
 /* Debug taps (need R2D_FLAG_DEBUG_TAPS): the last frame's manifolds
  * (Solver.manifolds, lib.zig:137) with their contact colours.  keys [cap][2]
  * are (reference, incident) body indices; data [cap][R2D_MANIFOLD_FLOATS]. */
+/* Consecutive still steps of the solver's world (R2D_FLAG_SLEEP); from 60 on
+ * the world sleeps.  0 when sleeping is off. */
+R2D_API int r2d_solver_sleep_frames(r2d_solver* s, uint32_t* frames);
 /* Kernel launches of the solver's latest step (a world on the grid pipeline
  * launches per phase and per colouring; a fused world launches one kernel). */
 R2D_API int r2d_solver_launches_per_step(r2d_solver* s, uint32_t* out);
@@ -206,6 +216,9 @@ R2D_API int r2d_batch_process(r2d_batch* b, float dt, uint32_t sub_steps, uint32
 R2D_API int r2d_batch_sync(r2d_batch* b);
 /* Kernel launches one r2d_batch_process enqueues (one per occupied size class). */
 R2D_API int r2d_batch_launches_per_step(r2d_batch* b, uint32_t* out);
+/* Consecutive still steps of every world [nworlds] (R2D_FLAG_SLEEP; a world
+ * sleeps from 60 on); zeros when sleeping is off. */
+R2D_API int r2d_batch_sleep_frames(r2d_batch* b, uint32_t* frames);
 /* Rows [first, first + count) of the state over all bodies (see the
  * solver's). */
 R2D_API int r2d_batch_write_state_fields(r2d_batch* b, uint32_t first, uint32_t count, const float* rows);

@@ -33,6 +33,8 @@ _SIG = {
     "r2o_add_joints": ([_P, C.c_uint32, _u8p, _u32p, _u32p, _f32p], None),
     "r2o_set_hash_config": ([_P, C.c_float, C.c_uint32], None),
     "r2o_set_warm_start": ([_P, C.c_int], None),
+    "r2o_set_sleep": ([_P, C.c_int], None),
+    "r2o_sleep_frames": ([_P], C.c_uint32),
     "r2o_get_state": ([_P, _f32p], None),
     "r2o_get_state_f64": ([_P, _f64p], None),
     "r2o_set_state": ([_P, _f32p], None),
@@ -122,6 +124,14 @@ class Oracle:
         """Warm starting (off in reference mode): manifolds found again start
         from last frame's accumulated impulses."""
         self.lib.r2o_set_warm_start(self.h, int(bool(on)))
+
+    def set_sleep(self, on: bool = True):
+        """Sleeping (r2d_sleep.h): a world still for R2D_SLEEP_FRAMES
+        consecutive steps is not stepped until its state is written."""
+        self.lib.r2o_set_sleep(self.h, int(bool(on)))
+
+    def sleep_frames(self) -> int:
+        return int(self.lib.r2o_sleep_frames(self.h))
 
     def state(self) -> np.ndarray:
         out = np.empty((NSTATE, self.n), np.float32)

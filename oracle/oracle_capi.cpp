@@ -243,7 +243,17 @@ void r2o_get_state_f64(void* hp, double* out) {
 
 void r2o_set_state(void* hp, const float* in) {
     Handle* h = (Handle*)hp;
-    DISPATCH(h, set_state(S, in));
+    DISPATCH(h, (set_state(S, in), S.sleep_frames = 0u));  // a write wakes the world
+}
+
+void r2o_set_sleep(void* hp, int on) {
+    Handle* h = (Handle*)hp;
+    DISPATCH(h, (S.sleep_enabled = on != 0, S.sleep_frames = 0u));
+}
+
+uint32_t r2o_sleep_frames(void* hp) {
+    Handle* h = (Handle*)hp;
+    return h->precision == 64 ? h->d->sleep_frames : h->f->sleep_frames;
 }
 
 void r2o_get_props(void* hp, float* out) {

@@ -53,6 +53,7 @@
 
 #include "../resolve2d_gb300/csrc/r2d_colour.h"
 #include "../resolve2d_gb300/csrc/r2d_sincos.h"
+#include "../resolve2d_gb300/csrc/r2d_sleep.h"
 
 namespace r2o {
 
@@ -518,6 +519,12 @@ public:
     // bodies once, after the first substep's preStep.
     bool warm_start = false;
     std::unordered_map<uint64_t, std::array<R, 4>> warm_prev;  // (ref << 32 | inc) -> pn0, pt0, pn1, pt1
+
+    // Sleeping (an extension, off in reference mode; r2d_sleep.h): after
+    // R2D_SLEEP_FRAMES consecutive still frames the world is not stepped
+    // until its state is written again.
+    bool sleep_enabled = false;
+    uint32_t sleep_frames = 0;
 
     std::vector<Body<R>> bodies;  // insertion order
     std::unordered_map<uint32_t, size_t> index_of_id;
@@ -1130,6 +1137,22 @@ public:
 
     // ---- Solver.process (lib.zig:189-251) ----
     int process(R dt, size_t sub_steps, size_t collision_iters, int order = ORDER_REFERENCE) {
+        if (sleep_enabled && sleep_frames >= R2D_SLEEP_FRAMES) return OK;  // asleep: nothing moves
+        const int st = step(dt, sub_steps, collision_iters, order);
+        if (st == OK && sleep_enabled) {
+            bool still = true;
+            for (const Body<R>& b : bodies) {
+                if (b.is_static) continue;
+                const float inv_m = 1.0f / float(b.props.mass), inv_i = 1.0f / float(b.props.inertia);
+                still = still && r2d_body_still(float(b.props.momentum.x), float(b.props.momentum.y),
+                                                float(b.props.ang_momentum), inv_m, inv_i);
+            }
+            sleep_frames = r2d_sleep_next(sleep_frames, still);
+        }
+        return st;
+    }
+
+    int step(R dt, size_t sub_steps, size_t collision_iters, int order) {
         const R f32_sub = R(sub_steps);
         const R sub_dt = dt / f32_sub;
 

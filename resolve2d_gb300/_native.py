@@ -34,6 +34,7 @@ FLAG_DEBUG_TAPS = 1
 FLAG_GRID_PIPELINE = 2
 FLAG_FP64_POSITIONS = 4
 FLAG_WARM_START = 8
+FLAG_SLEEP = 16
 MANIFOLD_FLOATS = 33
 
 
@@ -74,6 +75,8 @@ SIGNATURES = {
     "r2d_solver_sync": ([_P], C.c_int),
     "r2d_solver_num_manifolds": ([_P, _u32p], C.c_int),
     "r2d_solver_launches_per_step": ([_P, _u32p], C.c_int),
+    "r2d_solver_sleep_frames": ([_P, _u32p], C.c_int),
+    "r2d_batch_sleep_frames": ([_P, _u32p], C.c_int),
     "r2d_solver_get_manifolds": ([_P, C.c_uint32, _u32p, _f32p, _u32p], C.c_int),
     "r2d_solver_get_joint_colours": ([_P, C.c_uint32, _u32p], C.c_int),
     "r2d_batch_create": ([C.POINTER(Config), C.POINTER(_P)], C.c_int),

@@ -205,6 +205,7 @@ struct Engine {
     uint32_t* d_warm_keys = nullptr;
     float4* d_warm_vals = nullptr;
     uint32_t* d_warm_cur = nullptr;
+    uint32_t* d_sleep = nullptr;  // [nworlds] consecutive still frames (R2D_FLAG_SLEEP)
     uint32_t* d_warm_off = nullptr;  // [nworlds] copies of WorldDesc::warm_off / warm_hs for migration
     uint32_t* d_warm_hs = nullptr;
     std::vector<uint32_t> warm_hs_h, warm_off_h;
@@ -217,6 +218,7 @@ struct Engine {
         if (gexec) cudaGraphExecDestroy(gexec);
         dfree(d_call);
         dfree(d_warm_keys); dfree(d_warm_vals); dfree(d_warm_cur); dfree(d_warm_off); dfree(d_warm_hs);
+        dfree(d_sleep);
         dfree(d_state); dfree(d_pos64); dfree(d_props); dfree(d_kind); dfree(d_ids); dfree(d_worlds);
         dfree(d_status); dfree(d_err);
         if (h_err) cudaFreeHost(h_err);
@@ -325,6 +327,11 @@ struct Engine {
             CUDA_TRY(dalloc(d_warm_cur, nw));
             CUDA_TRY(cudaMemsetAsync(d_warm_cur, 0, sizeof(uint32_t) * nw, stream));
         }
+        dfree(d_sleep);
+        if (sleeping()) {
+            CUDA_TRY(dalloc(d_sleep, nw));
+            CUDA_TRY(cudaMemsetAsync(d_sleep, 0, sizeof(uint32_t) * nw, stream));
+        }
         calls.clear();
         pending = false;
         CUDA_TRY(cudaMemcpyAsync(d_state, state_h.data(), sizeof(float) * S_NFIELDS * n, cudaMemcpyHostToDevice, stream));
@@ -340,8 +347,24 @@ struct Engine {
         return R2D_OK;
     }
 
+    // Any host write wakes every sleeping world (R2D_FLAG_SLEEP).
+    cudaError_t wake() {
+        return d_sleep ? cudaMemsetAsync(d_sleep, 0, sizeof(uint32_t) * nworlds, stream) : cudaSuccess;
+    }
+
+    int sleep_frames(uint32_t* out) {
+        if (!d_sleep) {
+            std::fill(out, out + nworlds, 0u);
+            return R2D_OK;
+        }
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        CUDA_TRY(cudaMemcpy(out, d_sleep, sizeof(uint32_t) * nworlds, cudaMemcpyDeviceToHost));
+        return R2D_OK;
+    }
+
     int write_state(const float* state) {
         if (!d_state) return fail(R2D_ERR_INVALID_ARGUMENT, "no bodies");
+        CUDA_TRY(wake());
         CUDA_TRY(cudaMemcpyAsync(d_state, state, sizeof(float) * S_NFIELDS * nbodies, cudaMemcpyHostToDevice, stream));
         if (d_pos64) CUDA_TRY(upload_pose64(state));  // the f64 pose restarts from the written f32 one
         return R2D_OK;
@@ -354,6 +377,7 @@ struct Engine {
         if (first > (uint32_t)S_NFIELDS || count > (uint32_t)S_NFIELDS - first)
             return fail(R2D_ERR_INVALID_ARGUMENT, "field range beyond the 13 state fields");
         if (!count || !nbodies) return R2D_OK;
+        CUDA_TRY(wake());
         CUDA_TRY(cudaMemcpyAsync(d_state + (size_t)first * nbodies, rows, sizeof(float) * count * nbodies,
                                  cudaMemcpyHostToDevice, stream));
         if (d_pos64 && first < 3) {  // the f64 pose restarts from the written f32 pose rows
@@ -380,6 +404,7 @@ struct Engine {
 
     bool fp64_positions() const { return (cfg.flags & R2D_FLAG_FP64_POSITIONS) != 0; }
     bool warm_start() const { return (cfg.flags & R2D_FLAG_WARM_START) != 0; }
+    bool sleeping() const { return (cfg.flags & R2D_FLAG_SLEEP) != 0; }
 
     static uint32_t pow2_at_least(uint32_t v) {
         uint32_t p = 1;
@@ -457,6 +482,7 @@ struct Engine {
         // joints are grouped per world in the order given (insertion order inside a world)
         njoints = (uint32_t)jtype.size();
         ++joint_epoch;  // the grid pipeline's cached joint colourings are stale
+        CUDA_TRY(wake());
         std::vector<uint32_t> order(njoints);
         for (uint32_t j = 0; j < njoints; ++j) order[j] = j;
         std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return jworld[a] < jworld[b]; });
@@ -928,6 +954,7 @@ struct Engine {
         in.pos64 = d_pos64;
         in.warm = warm_start();
         in.verbose = verbose;
+        in.sleep = d_sleep ? d_sleep + w : nullptr;
         return in;
     }
 
@@ -986,6 +1013,7 @@ struct Engine {
         P.call_index = call_index;
         P.timers = d_timers;
         P.pos64 = d_pos64;
+        P.sleep = d_sleep;
         if (warm_start()) {
             P.warm_keys = d_warm_keys;
             P.warm_vals = d_warm_vals;
@@ -1336,6 +1364,7 @@ R2D_API int r2d_solver_set_gravity(r2d_solver* s, uint32_t n, const float* g) {
         d.ngrav = n;
         for (uint32_t k = 0; k < n; ++k) d.g[k] = g[k];
         s->eng.plan_dirty = true;
+        if (s->eng.wake() != cudaSuccess) return fail(R2D_ERR_CUDA, "waking the world failed");
     }
     return R2D_OK;
 }
@@ -1547,6 +1576,20 @@ R2D_API int r2d_batch_launches_per_step(r2d_batch* b, uint32_t* out) {
 R2D_API int r2d_solver_launches_per_step(r2d_solver* s, uint32_t* out) {
     if (!s || !out) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
     return launches_of(s->eng, out);
+}
+
+R2D_API int r2d_solver_sleep_frames(r2d_solver* s, uint32_t* frames) {
+    if (!s || !frames) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (s->eng.nworlds == 0) {
+        *frames = 0;
+        return R2D_OK;
+    }
+    return guarded([&] { return s->eng.sleep_frames(frames); });
+}
+
+R2D_API int r2d_batch_sleep_frames(r2d_batch* b, uint32_t* frames) {
+    if (!b || (!frames && b->eng.nworlds)) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
+    return guarded([&] { return b->eng.sleep_frames(frames); });
 }
 
 R2D_API int r2d_batch_world_status(r2d_batch* b, int* status) {

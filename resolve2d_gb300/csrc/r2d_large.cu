@@ -43,6 +43,7 @@
 
 #include "r2d_device.cuh"
 #include "r2d_large.h"
+#include "r2d_sleep.h"
 #include "r2d_solve.cuh"
 #include "r2d_world.cuh"
 
@@ -65,6 +66,7 @@ enum LargeCounter : int {
     LC_PEND1,
     LC_PEND2,
     LC_ROUNDS,         // the rounds that colouring needed
+    LC_MOVING,         // some non-static body ended the step moving (sleeping mode)
     LC_STUCK,          // a colouring ran more rounds than it has constraints (cannot happen)
     LC_N
 };
@@ -1215,6 +1217,18 @@ __global__ void __launch_bounds__(RT, 1) lk_contacts_cluster(Phase2 A, const uin
     }
 }
 
+// sleeping mode (r2d_sleep.h): is any non-static body still moving?
+__global__ void lk_still(SWT<uint32_t> s, uint32_t n, uint32_t* moving) {
+    const uint32_t i = blockIdx.x * LT + threadIdx.x;
+    bool m = false;
+    if (i < n && !(s.kind[i] & K_STATIC)) m = !r2d_body_still(s.mx[i], s.my[i], s.L[i], s.inv_m[i], s.inv_i[i]);
+    if (__any_sync(0xffffffffu, m) && (threadIdx.x & 31u) == 0) atomicOr(moving, 1u);
+}
+
+__global__ void lk_sleep_update(const uint32_t* moving, uint32_t* frames) {
+    *frames = r2d_sleep_next(*frames, *moving == 0u);
+}
+
 // debug taps in the oracle's manifold layout (DebugOut)
 __global__ void lk_dump(SWT<uint32_t> s, uint32_t m_count, uint32_t* keys, float* data, uint32_t* colours) {
     const uint32_t m = blockIdx.x * LT + threadIdx.x;
@@ -1518,6 +1532,15 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
     auto mark = [&](int k) {
         t_ms[k] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
     };
+    if (!I.h_cnt) LTRY(cudaMallocHost((void**)&I.h_cnt, sizeof(uint32_t) * H_WORDS));
+    if (in.sleep && n) {  // a sleeping world is not stepped; its last frame's manifolds stay (r2d_sleep.h)
+        LTRY(cudaMemcpyAsync(I.h_cnt, in.sleep, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        LTRY(cudaStreamSynchronize(st));
+        if (I.h_cnt[0] >= R2D_SLEEP_FRAMES) {
+            I.nlaunch = 0;
+            return 0;
+        }
+    }
     I.nman = 0;
     I.nj = 0;
     I.nlaunch = 0;
@@ -1525,7 +1548,6 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
     I.joff.assign(1, 0u);
     if (n == 0) return 0;
     const uint32_t T = in.table_mult * n;
-    if (!I.h_cnt) LTRY(cudaMallocHost((void**)&I.h_cnt, sizeof(uint32_t) * H_WORDS));
     if (!I.cnt) {
         LTRY(cudaMalloc((void**)&I.cnt, sizeof(uint32_t) * 2 * LC_N));
         LTRY(cudaMalloc((void**)&I.entries, sizeof(unsigned long long)));
@@ -1798,6 +1820,12 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
         if (M) LAUNCH(lk_warm_store, blocks(M), S.s, M, I.wkeys[wnext], I.wvals[wnext], whs_next);
         I.whs[wnext] = whs_next;
         I.wcur = wnext;
+    }
+    if (in.sleep) {
+        LTRY(cudaMemsetAsync(I.cnt + LC_MOVING, 0, sizeof(uint32_t), st));
+        LAUNCH(lk_still, blocks(n), I.views(in), n, I.cnt + LC_MOVING);
+        lk_sleep_update<<<1, 1, 0, st>>>(I.cnt + LC_MOVING, in.sleep);
+        ++I.nlaunch;
     }
     LTRY(cudaGetLastError());
     if (in.verbose) {

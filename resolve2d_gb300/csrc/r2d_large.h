@@ -38,6 +38,7 @@ struct LargeInputs {
     double* pos64;         // [3][NB] f64 pose (FP64-positions mode), else null
     bool warm;             // warm starting (the world keeps its impulses across calls)
     bool verbose;          // print each step's phase times and counts to stderr
+    uint32_t* sleep;       // this world's still-frame counter (sleeping mode, r2d_sleep.h), else null
 };
 
 class LargeWorld {

@@ -200,6 +200,7 @@ struct StepParams {
     uint32_t* warm_keys;         // warm-start tables (WorldDesc::warm_off), else null
     float4* warm_vals;
     uint32_t* warm_cur;          // [nworlds] which of a world's two tables holds last frame
+    uint32_t* sleep;             // [nworlds] consecutive still frames (sleeping mode, r2d_sleep.h), else null
     float dt;
     uint32_t sub_steps, iters;
     float cell;

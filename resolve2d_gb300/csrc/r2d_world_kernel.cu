@@ -21,6 +21,7 @@
 #include <stdint.h>
 
 #include "r2d_device.cuh"
+#include "r2d_sleep.h"
 #include "r2d_solve.cuh"
 #include "r2d_world.cuh"
 
@@ -299,6 +300,11 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
     // A world that failed earlier in this batch of calls stays frozen (its
     // state untouched) until the host replays it with larger capacities.
     if (P.world_fail_call[w] != 0xFFFFFFFFu) return;
+    // a sleeping world is not stepped (r2d_sleep.h)
+    if (P.sleep && P.sleep[w] >= R2D_SLEEP_FRAMES) {
+        if (tid == 0) P.world_status[w] = DS_OK;
+        return;
+    }
     if (n > C.nb || wd.nj > C.nj || T > C.nt || n > 65535u) {
         if (tid == 0) {
             P.world_status[w] = DS_CAPACITY;
@@ -972,6 +978,7 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
 
         PHASE(5);
         // ---------------- write back ----------------
+        bool moving = false;
         for (uint32_t i = tid; i < n; i += NT) {
             const uint32_t g = base + i;
             P.state[(size_t)S_POS_X * NB + g] = s.px[i];
@@ -985,6 +992,12 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
                 P.state[(size_t)S_FORCE_Y * NB + g] = 0.f;
                 P.state[(size_t)S_TORQUE * NB + g] = 0.f;
             }
+            if (P.sleep && !(s.kind[i] & K_STATIC))
+                moving = moving || !r2d_body_still(s.mx[i], s.my[i], s.L[i], s.inv_m[i], s.inv_i[i]);
+        }
+        if (P.sleep) {
+            const bool any_moving = __syncthreads_or(moving) != 0;
+            if (tid == 0) P.sleep[w] = r2d_sleep_next(P.sleep[w], !any_moving);
         }
         if (P.dbg.cap) {
             const uint32_t cap = P.dbg.cap;

@@ -13,13 +13,15 @@ from .scenes import NSTATE, Scene, derive_props_state
 
 
 def _config(cell: float, mult: int, debug: bool, stream, capacity_scale: float = 0.0,
-            grid: bool = False, fp64_positions: bool = False, warm_start: bool = False) -> N.Config:
+            grid: bool = False, fp64_positions: bool = False, warm_start: bool = False,
+            sleep: bool = False) -> N.Config:
     cfg = N.Config()
     cfg.capacity_scale = float(capacity_scale)
     cfg.spatialhash_cell_width = float(cell)
     cfg.spatialhash_table_size_mult = int(mult)
     cfg.flags = ((N.FLAG_DEBUG_TAPS if debug else 0) | (N.FLAG_GRID_PIPELINE if grid else 0)
-                 | (N.FLAG_FP64_POSITIONS if fp64_positions else 0) | (N.FLAG_WARM_START if warm_start else 0))
+                 | (N.FLAG_FP64_POSITIONS if fp64_positions else 0) | (N.FLAG_WARM_START if warm_start else 0)
+                 | (N.FLAG_SLEEP if sleep else 0))
     cfg.stream = int(stream) if stream else None
     return cfg
 
@@ -29,10 +31,11 @@ class World:
     520 bodies, the grid-wide pipeline above that (or always, ``grid=True``)."""
 
     def __init__(self, cell: float = 0.0, mult: int = 0, debug: bool = False, stream=None, capacity_scale: float = 0.0,
-                 grid: bool = False, fp64_positions: bool = False, warm_start: bool = False):
+                 grid: bool = False, fp64_positions: bool = False, warm_start: bool = False,
+                 sleep: bool = False):
         self._lib = N.load()
         self._h = C.c_void_p()
-        cfg = _config(cell, mult, debug, stream, capacity_scale, grid, fp64_positions, warm_start)
+        cfg = _config(cell, mult, debug, stream, capacity_scale, grid, fp64_positions, warm_start, sleep)
         N.check(self._lib.r2d_solver_create(C.byref(cfg), C.byref(self._h)), "r2d_solver_create")
         self.n = 0
 
@@ -102,6 +105,12 @@ class World:
         N.check(self._lib.r2d_solver_launches_per_step(self._h, C.byref(out)), "r2d_solver_launches_per_step")
         return int(out.value)
 
+    def sleep_frames(self) -> int:
+        """Consecutive still steps of the world (sleeping mode; it sleeps from 60)."""
+        out = C.c_uint32()
+        N.check(self._lib.r2d_solver_sleep_frames(self._h, C.byref(out)), "r2d_solver_sleep_frames")
+        return int(out.value)
+
     def manifolds(self):
         m = C.c_uint32()
         N.check(self._lib.r2d_solver_num_manifolds(self._h, C.byref(m)), "r2d_solver_num_manifolds")
@@ -141,10 +150,11 @@ class Batch:
     """Many independent worlds stepped together (r2d_batch_* entry points)."""
 
     def __init__(self, cell: float = 0.0, mult: int = 0, debug: bool = False, stream=None, capacity_scale: float = 0.0,
-                 grid: bool = False, fp64_positions: bool = False, warm_start: bool = False):
+                 grid: bool = False, fp64_positions: bool = False, warm_start: bool = False,
+                 sleep: bool = False):
         self._lib = N.load()
         self._h = C.c_void_p()
-        cfg = _config(cell, mult, debug, stream, capacity_scale, grid, fp64_positions, warm_start)
+        cfg = _config(cell, mult, debug, stream, capacity_scale, grid, fp64_positions, warm_start, sleep)
         N.check(self._lib.r2d_batch_create(C.byref(cfg), C.byref(self._h)), "r2d_batch_create")
         self.n = 0
         self.nworlds = 0
@@ -222,6 +232,12 @@ class Batch:
         out = C.c_uint32()
         N.check(self._lib.r2d_batch_launches_per_step(self._h, C.byref(out)), "r2d_batch_launches_per_step")
         return int(out.value)
+
+    def sleep_frames(self) -> np.ndarray:
+        """Consecutive still steps of every world (sleeping mode; a world sleeps from 60)."""
+        out = np.zeros(self.nworlds, np.uint32)
+        N.check(self._lib.r2d_batch_sleep_frames(self._h, N.ptr(out, C.c_uint32)), "r2d_batch_sleep_frames")
+        return out
 
     def world_status(self) -> np.ndarray:
         out = np.zeros(self.nworlds, np.int32)
