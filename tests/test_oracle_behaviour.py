@@ -153,3 +153,46 @@ def test_fp64_oracle_tracks_fp32_over_short_horizon():
         a.process(sc.dt, 1, 8)
         b.process(sc.dt, 1, 8)
     assert np.abs(a.state()[:2] - b.state64()[:2]).max() < 1e-2
+
+
+def _resting(shift=0.0):
+    b = scenes._Builder()
+    b.rect(0.0, -0.5, 40.0, 1.0, 0.5, static=True)
+    for i in range(8):
+        b.rect(-8.0 + 2.0 * i + shift, 0.5, 1.0, 1.0, 0.5)
+        b.disc(-8.0 + 2.0 * i + shift, 1.5, 0.5, 0.5)
+    return scenes._concat("resting", [b.arrays()], [9.81], 1 / 60, 1, 8, 100)
+
+
+def test_sleeping_rule():
+    """The sleeping extension (r2d_sleep.h): a world whose bodies stay still
+    for 60 steps stops changing; writing its state wakes it; a moving world
+    never sleeps; with sleeping off nothing is skipped."""
+    sc = _resting()
+    o = Oracle.from_scene(sc)
+    o.set_sleep(True)
+    frames = []
+    for _ in range(80):
+        assert o.process(sc.dt, sc.sub_steps, sc.iters, ORDER_COLOUR) == 0
+        frames.append(o.sleep_frames())
+    assert max(frames) == 60 and frames[-1] == 60
+    first = frames.index(60)
+    assert frames[first - 59 : first + 1] == list(range(1, 61))  # 60 consecutive still frames
+    asleep = o.state()
+    assert o.process(sc.dt, sc.sub_steps, sc.iters, ORDER_COLOUR) == 0
+    np.testing.assert_array_equal(o.state(), asleep)
+    asleep[scenes.S_MOM_X, 1] = 5.0  # a kick wakes it
+    o.set_state(asleep)
+    assert o.sleep_frames() == 0
+    assert o.process(sc.dt, sc.sub_steps, sc.iters, ORDER_COLOUR) == 0
+    assert o.sleep_frames() == 0 and not np.array_equal(o.state(), asleep)
+    # sleeping off: the same steps are all taken
+    off = Oracle.from_scene(sc)
+    for _ in range(80):
+        assert off.process(sc.dt, sc.sub_steps, sc.iters, ORDER_COLOUR) == 0
+    assert off.sleep_frames() == 0
+    moving = Oracle.from_scene(scenes.config0())
+    moving.set_sleep(True)
+    for _ in range(80):
+        assert moving.process(1 / 60, 1, 8, ORDER_COLOUR) == 0
+    assert moving.sleep_frames() < 60
