@@ -11,8 +11,11 @@ value      body-steps/s with the state resident in HBM, CUDA events around
            each step on the library's stream, L2 flushed (256 MiB write)
            between steps outside the timed events.
 e2e        the same metric through the C ABI with pinned host buffers: every
-           step writes its inputs (force and torque rows), steps, and reads
-           its result (pose and momenta rows); the full-state round trip is
+           step takes its inputs (force and torque rows) from the host and
+           returns its result (pose and momenta rows) to the host, in one
+           r2d_batch_process_io call whose kernels read and write the pinned
+           rows over the CPU-GPU link; the same frame as three calls
+           (write rows, step, read rows) and the full-state round trip are
            reported beside it.
 roofline   algorithmic HBM bytes of the world-step kernel per step
            (117 B per body-step: 77 B read, 40 B written) over its measured
@@ -278,9 +281,7 @@ def run_large(args):
     torch.cuda.synchronize()
     t1 = time.perf_counter()
     for _ in range(e2e_steps):
-        batch.write_fields(6, forces_in)
-        batch.process(sc.dt, sc.sub_steps, sc.iters)
-        batch.read_fields(0, 6, pose_out)
+        batch.process_io(sc.dt, sc.sub_steps, sc.iters, forces_in, pose_out)
     batch.sync()
     e2e_v = nb * e2e_steps / (time.perf_counter() - t1)
 
@@ -296,7 +297,8 @@ def run_large(args):
         "gpu_launches": launches,
         "wall_s_timed_loop": wall,
         "e2e": {"value": e2e_v, "unit": "body-steps/s", "h2d_bytes_per_step": 12 * nb, "d2h_bytes_per_step": 24 * nb,
-                "inputs": "force and torque rows (pinned)", "results": "pose and momenta rows (pinned)"},
+                "inputs": "force and torque rows (pinned)", "results": "pose and momenta rows (pinned)",
+                "call": "r2d_solver_process_io (grid-pipeline worlds copy the rows around the step)"},
         "plain_one_world_per_launch": None,
         "roofline": {"bound": "hbm", "kernel": "grid pipeline (all launches of one step)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -424,6 +426,9 @@ def main():
     state_io = torch.empty((13, nb), dtype=torch.float32).pin_memory().numpy()
     state_io[...] = settled
 
+    def frame_step():  # one call: the step reads the pinned force rows and writes the result rows itself
+        batch.process_io(sc.dt, sc.sub_steps, sc.iters, forces_in, pose_out)
+
     def fields_step():
         batch.write_fields(6, forces_in)
         batch.process(sc.dt, sc.sub_steps, sc.iters)
@@ -434,7 +439,8 @@ def main():
         batch.process(sc.dt, sc.sub_steps, sc.iters)
         batch.read_state(state_io)
 
-    e2e_v = timed_e2e(fields_step)
+    e2e_v = timed_e2e(frame_step)
+    e2e_three = timed_e2e(fields_step)
     e2e_full = timed_e2e(full_step)
 
     # plain path: the same worlds, one world per launch
@@ -476,6 +482,8 @@ def main():
         "wall_s_timed_loop": wall,
         "e2e": {"value": e2e_v, "unit": "body-steps/s", "h2d_bytes_per_step": 12 * nb, "d2h_bytes_per_step": 24 * nb,
                 "inputs": "force and torque rows (pinned)", "results": "pose and momenta rows (pinned)",
+                "call": "r2d_batch_process_io (the step reads and writes the pinned rows over the CPU-GPU link)",
+                "three_calls": {"value": e2e_three, "call": "write_state_fields, process, read_state_fields"},
                 "full_state": {"value": e2e_full, "h2d_bytes_per_step": 52 * nb, "d2h_bytes_per_step": 52 * nb}},
         "plain_one_world_per_launch": {"value": plain, "unit": "body-steps/s", "worlds": args.plain_worlds,
                                        "batched_over_plain": (value / world) / plain if plain else None},

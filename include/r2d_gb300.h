@@ -169,6 +169,17 @@ R2D_API int r2d_solver_set_exclusions(r2d_solver* s, uint32_t n, const uint32_t*
 /* Solver.process (lib.zig:189-251) / solverProcess (wasm_root.zig:39-43). */
 R2D_API int r2d_solver_process(r2d_solver* s, float dt, uint32_t sub_steps, uint32_t collision_iters);
 R2D_API int r2d_solver_sync(r2d_solver* s);
+/* One frame of a host loop in one call: the force and torque rows
+ * `force_rows` [3][n] (state fields 6..8) are this frame's forces, the frame
+ * is stepped, and the pose and momentum rows (fields 0..5) are written to
+ * `out_rows` [6][n]; returns once they are there (with the status of
+ * r2d_solver_sync).  Either pointer may be NULL.  Pinned (page-locked) or
+ * managed buffers are read and written by the step itself over the coherent
+ * CPU-GPU link; pageable ones are copied.  The bulk counterpart of the WASM
+ * exports' per-field setters, solverProcess and getters
+ * (src/wasm_root.zig:39-43,88-251). */
+R2D_API int r2d_solver_process_io(r2d_solver* s, float dt, uint32_t sub_steps, uint32_t collision_iters,
+                                  const float* force_rows, float* out_rows);
 /* Bulk get/set of part of the state: rows [first, first + count) of the
  * field-major state (each row n floats), one contiguous copy.  The batched
  * form of the WASM exports' per-field body getters and setters
@@ -214,6 +225,9 @@ R2D_API int r2d_batch_write_state(r2d_batch* b, const float* state);
 R2D_API int r2d_batch_read_state(r2d_batch* b, float* state);
 R2D_API int r2d_batch_process(r2d_batch* b, float dt, uint32_t sub_steps, uint32_t collision_iters);
 R2D_API int r2d_batch_sync(r2d_batch* b);
+/* r2d_solver_process_io over all worlds' bodies (rows of total-bodies length). */
+R2D_API int r2d_batch_process_io(r2d_batch* b, float dt, uint32_t sub_steps, uint32_t collision_iters,
+                                 const float* force_rows, float* out_rows);
 /* Kernel launches one r2d_batch_process enqueues (one per occupied size class). */
 R2D_API int r2d_batch_launches_per_step(r2d_batch* b, uint32_t* out);
 /* Consecutive still steps of every world [nworlds] (R2D_FLAG_SLEEP; a world

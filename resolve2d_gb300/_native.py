@@ -76,6 +76,8 @@ SIGNATURES = {
     "r2d_solver_num_manifolds": ([_P, _u32p], C.c_int),
     "r2d_solver_launches_per_step": ([_P, _u32p], C.c_int),
     "r2d_solver_sleep_frames": ([_P, _u32p], C.c_int),
+    "r2d_solver_process_io": ([_P, C.c_float, C.c_uint32, C.c_uint32, _f32p, _f32p], C.c_int),
+    "r2d_batch_process_io": ([_P, C.c_float, C.c_uint32, C.c_uint32, _f32p, _f32p], C.c_int),
     "r2d_batch_sleep_frames": ([_P, _u32p], C.c_int),
     "r2d_solver_get_manifolds": ([_P, C.c_uint32, _u32p, _f32p, _u32p], C.c_int),
     "r2d_solver_get_joint_colours": ([_P, C.c_uint32, _u32p], C.c_int),

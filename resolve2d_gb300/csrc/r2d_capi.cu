@@ -206,6 +206,11 @@ struct Engine {
     float4* d_warm_vals = nullptr;
     uint32_t* d_warm_cur = nullptr;
     uint32_t* d_sleep = nullptr;  // [nworlds] consecutive still frames (R2D_FLAG_SLEEP)
+    // A frame call's host rows (process_io): the device copy the kernels read
+    // (StepParams::ext) and the value last copied there.
+    ExtIO* d_ext = nullptr;
+    ExtIO ext_cur{};
+    ExtIO ext_src{};  // pageable source of the copy: free to change once the copy call returns
     uint32_t* d_warm_off = nullptr;  // [nworlds] copies of WorldDesc::warm_off / warm_hs for migration
     uint32_t* d_warm_hs = nullptr;
     std::vector<uint32_t> warm_hs_h, warm_off_h;
@@ -217,6 +222,7 @@ struct Engine {
         large.clear();
         if (gexec) cudaGraphExecDestroy(gexec);
         dfree(d_call);
+        dfree(d_ext);
         dfree(d_warm_keys); dfree(d_warm_vals); dfree(d_warm_cur); dfree(d_warm_off); dfree(d_warm_hs);
         dfree(d_sleep);
         dfree(d_state); dfree(d_pos64); dfree(d_props); dfree(d_kind); dfree(d_ids); dfree(d_worlds);
@@ -262,6 +268,8 @@ struct Engine {
         const char* ng = getenv("R2D_NO_GRAPH");
         use_graph = !(ng && ng[0] && ng[0] != '0');
         CUDA_TRY(dalloc(d_call, 1));
+        CUDA_TRY(dalloc(d_ext, 1));
+        CUDA_TRY(cudaMemsetAsync(d_ext, 0, sizeof(ExtIO), stream));
         CUDA_TRY(cudaMemsetAsync(d_call, 0, sizeof(uint32_t), stream));
         CUDA_TRY(allow_world_step_smem(smem_optin()));
         return R2D_OK;
@@ -844,7 +852,60 @@ struct Engine {
         return R2D_OK;
     }
 
+    // The host rows the next steps read and write (null: none).  The device
+    // copy changes between calls on `stream`, so a replayed graph reads it.
+    cudaError_t set_ext(const float* force, float* out) {
+        if (ext_cur.force == force && ext_cur.out == out) return cudaSuccess;
+        ext_src.force = force;
+        ext_src.out = out;
+        const cudaError_t e = cudaMemcpyAsync(d_ext, &ext_src, sizeof(ExtIO), cudaMemcpyHostToDevice, stream);
+        if (e == cudaSuccess) ext_cur = ext_src;
+        return e;
+    }
+
+    // The address kernels use for a host buffer they may read or write
+    // directly (pinned or managed), else null.
+    static void* device_view(const void* p) {
+        if (!p) return nullptr;
+        cudaPointerAttributes a{};
+        if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+            (void)cudaGetLastError();
+            return nullptr;
+        }
+        if (a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeManaged || a.type == cudaMemoryTypeDevice)
+            return a.devicePointer;
+        return nullptr;
+    }
+
+    // One frame (r2d_*_process_io): the force/torque rows in, a step, the pose
+    // and momentum rows out, synchronised.  Fused worlds read and write pinned
+    // host rows directly over the CPU-GPU link; otherwise (pageable buffers,
+    // grid-pipeline worlds, sleeping) the rows are copied around the step.
+    int process_io(float dt, uint32_t sub_steps, uint32_t iters, const float* force, float* out) {
+        if (!d_state) return fail(R2D_ERR_INVALID_ARGUMENT, "no bodies");
+        const float* dforce = static_cast<const float*>(device_view(force));
+        float* dout = static_cast<float*>(device_view(out));
+        const bool direct = (!force || dforce) && (!out || dout) && !sleeping() &&
+                            std::none_of(world_large.begin(), world_large.end(), [](uint8_t v) { return v != 0; });
+        if (!direct) {
+            if (force) {
+                if (int st = write_fields(S_FORCE_X, 3, force)) return st;
+            }
+            if (int st = process(dt, sub_steps, iters)) return st;
+            if (int st = sync()) return st;
+            return out ? read_fields(0, 6, out) : R2D_OK;
+        }
+        CUDA_TRY(set_ext(dforce, dout));
+        if (int st = process_step(dt, sub_steps, iters)) return st;
+        return sync();
+    }
+
     int process(float dt, uint32_t sub_steps, uint32_t iters) {
+        CUDA_TRY(set_ext(nullptr, nullptr));
+        return process_step(dt, sub_steps, iters);
+    }
+
+    int process_step(float dt, uint32_t sub_steps, uint32_t iters) {
         if (sub_steps == 0) return fail(R2D_ERR_INVALID_ARGUMENT, "sub_steps must be >= 1");
         if (!d_state) return fail(R2D_ERR_INVALID_ARGUMENT, "no bodies");
         if ((sub_steps > 1) != plan_multi_substep) {
@@ -1014,6 +1075,7 @@ struct Engine {
         P.timers = d_timers;
         P.pos64 = d_pos64;
         P.sleep = d_sleep;
+        P.ext = d_ext;
         if (warm_start()) {
             P.warm_keys = d_warm_keys;
             P.warm_vals = d_warm_vals;
@@ -1434,6 +1496,18 @@ R2D_API int r2d_solver_process(r2d_solver* s, float dt, uint32_t sub_steps, uint
     return guarded([&] { return s->eng.process(dt, sub_steps, collision_iters); });
 }
 
+R2D_API int r2d_solver_process_io(r2d_solver* s, float dt, uint32_t sub_steps, uint32_t collision_iters,
+                                  const float* force_rows, float* out_rows) {
+    if (!s) return fail(R2D_ERR_INVALID_ARGUMENT, "solver is NULL");
+    if (s->eng.nworlds == 0) return R2D_OK;
+    if (s->constraints_dirty) {
+        int st = guarded([&] { return solver_resolve(s); });
+        if (st) return st;
+        s->constraints_dirty = false;
+    }
+    return guarded([&] { return s->eng.process_io(dt, sub_steps, collision_iters, force_rows, out_rows); });
+}
+
 R2D_API int r2d_solver_sync(r2d_solver* s) {
     if (!s) return fail(R2D_ERR_INVALID_ARGUMENT, "solver is NULL");
     return guarded([&] { return s->eng.sync(); });
@@ -1540,6 +1614,13 @@ R2D_API int r2d_batch_process(r2d_batch* b, float dt, uint32_t sub_steps, uint32
     if (!b) return fail(R2D_ERR_INVALID_ARGUMENT, "batch is NULL");
     if (b->eng.nworlds == 0) return R2D_OK;
     return guarded([&] { return b->eng.process(dt, sub_steps, collision_iters); });
+}
+
+R2D_API int r2d_batch_process_io(r2d_batch* b, float dt, uint32_t sub_steps, uint32_t collision_iters,
+                                 const float* force_rows, float* out_rows) {
+    if (!b) return fail(R2D_ERR_INVALID_ARGUMENT, "batch is NULL");
+    if (b->eng.nworlds == 0) return R2D_OK;
+    return guarded([&] { return b->eng.process_io(dt, sub_steps, collision_iters, force_rows, out_rows); });
 }
 
 R2D_API int r2d_batch_sync(r2d_batch* b) {

@@ -175,6 +175,15 @@ struct DebugOut {
     uint32_t jcap;
 };
 
+// Host rows a frame call reads and writes directly over the coherent
+// CPU-GPU link (r2d_*_process_io): the frame's force and torque [3][nbodies]
+// and the pose and momenta it returns [6][nbodies], field-major like the
+// state.  Null pointers: the state rows are the only inputs and outputs.
+struct ExtIO {
+    const float* force;
+    float* out;
+};
+
 struct StepParams {
     const WorldDesc* worlds;
     const uint32_t* world_list;  // worlds handled by this launch
@@ -201,6 +210,7 @@ struct StepParams {
     float4* warm_vals;
     uint32_t* warm_cur;          // [nworlds] which of a world's two tables holds last frame
     uint32_t* sleep;             // [nworlds] consecutive still frames (sleeping mode, r2d_sleep.h), else null
+    const ExtIO* ext;            // this call's host rows (device copy, read per call), else null
     float dt;
     uint32_t sub_steps, iters;
     float cell;

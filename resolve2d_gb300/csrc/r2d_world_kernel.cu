@@ -300,8 +300,11 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
     // A world that failed earlier in this batch of calls stays frozen (its
     // state untouched) until the host replays it with larger capacities.
     if (P.world_fail_call[w] != 0xFFFFFFFFu) return;
-    // a sleeping world is not stepped (r2d_sleep.h)
+    // a sleeping world is not stepped (r2d_sleep.h); a frame call still gets its pose
     if (P.sleep && P.sleep[w] >= R2D_SLEEP_FRAMES) {
+        float* out = P.ext ? P.ext->out : nullptr;
+        for (uint32_t i = tid; out && i < n; i += NT)
+            for (int f = 0; f < 6; ++f) out[(size_t)f * NB + base + i] = P.state[(size_t)f * NB + base + i];
         if (tid == 0) P.world_status[w] = DS_OK;
         return;
     }
@@ -393,6 +396,9 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
     const bool disc_rot = (wd.flags & W_DISC_ROTATION) != 0;
     const float* __restrict__ st = P.state;
     const float* __restrict__ pr = P.props;
+    // a frame call's host rows (r2d_*_process_io), read over the CPU-GPU link
+    const float* ext_force = P.ext ? P.ext->force : nullptr;
+    float* ext_out = P.ext ? P.ext->out : nullptr;
 
     // ---------------- load the world ----------------
     for (uint32_t i = tid; i < n; i += NT) {
@@ -826,9 +832,15 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
                 const uint8_t k = s.kind[i];
                 float fx = 0.f, fy = 0.f, tq = 0.f;
                 if (sub == 0) {  // user-set force / torque (RigidBody.Props, RigidBody.zig:73,78)
-                    fx = st[(size_t)S_FORCE_X * NB + g];
-                    fy = st[(size_t)S_FORCE_Y * NB + g];
-                    tq = st[(size_t)S_TORQUE * NB + g];
+                    if (ext_force) {
+                        fx = ext_force[g];
+                        fy = ext_force[(size_t)NB + g];
+                        tq = ext_force[2 * (size_t)NB + g];
+                    } else {
+                        fx = st[(size_t)S_FORCE_X * NB + g];
+                        fy = st[(size_t)S_FORCE_Y * NB + g];
+                        tq = st[(size_t)S_TORQUE * NB + g];
+                    }
                     // a dynamic body's force / torque is cleared after integration (lib.zig:247-248)
                     if (!(k & K_STATIC) && (fx != 0.f || fy != 0.f || tq != 0.f)) s.kind[i] = k | K_FORCED;
                 }
@@ -987,10 +999,26 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
             P.state[(size_t)S_MOM_X * NB + g] = s.mx[i];
             P.state[(size_t)S_MOM_Y * NB + g] = s.my[i];
             P.state[(size_t)S_ANG_MOM * NB + g] = s.L[i];
-            if (s.kind[i] & K_FORCED) {
+            // consumed forces are cleared (lib.zig:247-248); a frame call's
+            // forces replace the state's rows as if written before the step:
+            // cleared for a dynamic body, kept (unused) for a static one
+            if (ext_force) {
+                const bool keep = (s.kind[i] & K_STATIC) != 0;
+                P.state[(size_t)S_FORCE_X * NB + g] = keep ? ext_force[g] : 0.f;
+                P.state[(size_t)S_FORCE_Y * NB + g] = keep ? ext_force[(size_t)NB + g] : 0.f;
+                P.state[(size_t)S_TORQUE * NB + g] = keep ? ext_force[2 * (size_t)NB + g] : 0.f;
+            } else if (s.kind[i] & K_FORCED) {
                 P.state[(size_t)S_FORCE_X * NB + g] = 0.f;
                 P.state[(size_t)S_FORCE_Y * NB + g] = 0.f;
                 P.state[(size_t)S_TORQUE * NB + g] = 0.f;
+            }
+            if (ext_out) {
+                ext_out[g] = s.px[i];
+                ext_out[(size_t)NB + g] = s.py[i];
+                ext_out[2 * (size_t)NB + g] = s.ang[i];
+                ext_out[3 * (size_t)NB + g] = s.mx[i];
+                ext_out[4 * (size_t)NB + g] = s.my[i];
+                ext_out[5 * (size_t)NB + g] = s.L[i];
             }
             if (P.sleep && !(s.kind[i] & K_STATIC))
                 moving = moving || !r2d_body_still(s.mx[i], s.my[i], s.L[i], s.inv_m[i], s.inv_i[i]);

@@ -12,6 +12,20 @@ from . import _native as N
 from .scenes import NSTATE, Scene, derive_props_state
 
 
+def _rows(a, k: int, n: int) -> np.ndarray:
+    """`a` as the contiguous float32 [k][n] rows the library reads (no copy
+    when it already is: a pinned buffer stays pinned)."""
+    if isinstance(a, np.ndarray) and a.dtype == np.float32 and a.flags.c_contiguous and a.shape == (k, n):
+        return a
+    return np.ascontiguousarray(np.asarray(a, np.float32).reshape(k, n))
+
+
+def _out_rows(a: np.ndarray, k: int, n: int) -> np.ndarray:
+    if not (isinstance(a, np.ndarray) and a.dtype == np.float32 and a.flags.c_contiguous and a.shape == (k, n)):
+        raise ValueError(f"out must be a C-contiguous float32 array of shape ({k}, {n})")
+    return a
+
+
 def _config(cell: float, mult: int, debug: bool, stream, capacity_scale: float = 0.0,
             grid: bool = False, fp64_positions: bool = False, warm_start: bool = False,
             sleep: bool = False) -> N.Config:
@@ -96,6 +110,15 @@ class World:
 
     def process(self, dt: float, sub_steps: int = 1, iters: int = 8):
         N.check(self._lib.r2d_solver_process(self._h, float(dt), int(sub_steps), int(iters)), "r2d_solver_process")
+
+    def process_io(self, dt: float, sub_steps: int, iters: int, forces=None, out=None):
+        """One frame: force/torque rows [3][n] in, step, pose and momentum rows
+        [6][n] out (written into `out`, a C-contiguous float32 array; pinned
+        buffers are accessed by the step directly)."""
+        fp = N.ptr(_rows(forces, 3, self.n), C.c_float) if forces is not None else None
+        op = N.ptr(_out_rows(out, 6, self.n), C.c_float) if out is not None else None
+        N.check(self._lib.r2d_solver_process_io(self._h, float(dt), int(sub_steps), int(iters), fp, op),
+                "r2d_solver_process_io")
 
     def sync(self):
         N.check(self._lib.r2d_solver_sync(self._h), "r2d_solver_sync")
@@ -200,6 +223,13 @@ class Batch:
 
     def process(self, dt: float, sub_steps: int = 1, iters: int = 8):
         N.check(self._lib.r2d_batch_process(self._h, float(dt), int(sub_steps), int(iters)), "r2d_batch_process")
+
+    def process_io(self, dt: float, sub_steps: int, iters: int, forces=None, out=None):
+        """One frame over all worlds (see World.process_io)."""
+        fp = N.ptr(_rows(forces, 3, self.n), C.c_float) if forces is not None else None
+        op = N.ptr(_out_rows(out, 6, self.n), C.c_float) if out is not None else None
+        N.check(self._lib.r2d_batch_process_io(self._h, float(dt), int(sub_steps), int(iters), fp, op),
+                "r2d_batch_process_io")
 
     def sync(self):
         N.check(self._lib.r2d_batch_sync(self._h), "r2d_batch_sync")
