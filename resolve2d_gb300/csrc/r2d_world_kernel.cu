@@ -396,9 +396,7 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
     const bool disc_rot = (wd.flags & W_DISC_ROTATION) != 0;
     const float* __restrict__ st = P.state;
     const float* __restrict__ pr = P.props;
-    // a frame call's host rows (r2d_*_process_io), read over the CPU-GPU link
-    const float* ext_force = P.ext ? P.ext->force : nullptr;
-    float* ext_out = P.ext ? P.ext->out : nullptr;
+
 
     // ---------------- load the world ----------------
     for (uint32_t i = tid; i < n; i += NT) {
@@ -832,6 +830,8 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
                 const uint8_t k = s.kind[i];
                 float fx = 0.f, fy = 0.f, tq = 0.f;
                 if (sub == 0) {  // user-set force / torque (RigidBody.Props, RigidBody.zig:73,78)
+                    // a frame call's host rows (r2d_*_process_io), read over the CPU-GPU link
+                    const float* ext_force = P.ext ? P.ext->force : nullptr;
                     if (ext_force) {
                         fx = ext_force[g];
                         fy = ext_force[(size_t)NB + g];
@@ -991,6 +991,8 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
         PHASE(5);
         // ---------------- write back ----------------
         bool moving = false;
+        const float* ext_force = P.ext ? P.ext->force : nullptr;
+        float* ext_out = P.ext ? P.ext->out : nullptr;
         for (uint32_t i = tid; i < n; i += NT) {
             const uint32_t g = base + i;
             P.state[(size_t)S_POS_X * NB + g] = s.px[i];
