@@ -68,6 +68,25 @@ LARGE = {
 }
 
 
+def max_over_ranks(x: float, device: str = "cuda") -> float:
+    """The largest of every rank's `x` (the timed region of the slowest rank);
+    `x` itself with one process."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_seed(rank: int) -> int:
+    """Each rank steps its own 4,096-world replica (weak scaling): the
+    headline scene's seed 3, shifted by the rank."""
+    return 3 + rank
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -349,7 +368,7 @@ def main():
     from resolve2d_gb300.engine import Batch, World
 
     B.build_library()
-    sc = scenes.config3(seed=3 + rank)
+    sc = scenes.config3(seed=replica_seed(rank))
     # a dedicated stream: the library launches on it and the CUDA events below
     # are recorded on it (the legacy default stream has handle 0, which the
     # library would replace with a stream of its own)
@@ -396,10 +415,7 @@ def main():
     batch.sync()
     ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     dev_s = sum(ms) / 1e3
-    if world > 1:
-        t = torch.tensor([dev_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dev_s = float(t.item())
+    dev_s = max_over_ranks(dev_s)
     clk = clocks.stop()
     value = nb * args.steps * world / dev_s
     launches = batch.launches_per_step() * args.steps
