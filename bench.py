@@ -53,6 +53,10 @@ import numpy as np
 
 REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
+# The library runs the size classes of a step on up to 16 streams at once;
+# CUDA's default of 8 hardware work queues would serialise some of them.  It
+# only takes effect before CUDA starts in this process.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 SETTLE_STEPS = 300
 BYTES_READ = 77   # pos 8, angle 4, momentum 8, ang. momentum 4, force+torque 12, AABB 16, mass/inertia/mu/dims 20, kind 1, id 4
@@ -493,6 +497,7 @@ def main():
                    "l2": "flushed between timed steps (256 MiB write outside the events)",
                    "tiles": "threads per CTA of each size class autotuned on the settled worlds"
                    if not args.no_autotune else "default threads per size class",
+                   "cuda_device_max_connections": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS"),
                    "parallelism": f"replicas x{world}"},
         "gpu_launches": launches,
         "wall_s_timed_loop": wall,
