@@ -340,7 +340,7 @@ def run_large(args):
     print(json.dumps(line), flush=True)
 
 
-def main():
+def arg_parser() -> argparse.ArgumentParser:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=30)
@@ -353,7 +353,11 @@ def main():
                     help="worlds stepped one per launch for the plain-path comparison")
     ap.add_argument("--workload", default="config3", choices=["config3", *LARGE],
                     help="config3 (the headline batch) or one large world on the grid pipeline")
-    args = ap.parse_args()
+    return ap
+
+
+def main():
+    args = arg_parser().parse_args()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload in LARGE:
