@@ -1,0 +1,33 @@
+"""The reference-style ``Solver`` over the GPU engine, against the oracle.
+
+The scene of ``test_solver_api.py`` is built through the factory: discs and
+rectangles by density and by mass, a static ground set through
+``body_unwrap().static``, gravity, all four joint types and an exclusion.  It
+is stepped on the GPU through ``engine.World``, and every five frames it must
+equal the same scene given to the oracle, bit for bit.
+"""
+
+import pytest
+
+from oracle import Oracle
+from test_solver_api import add_joints_to_oracle, add_to_oracle, body_specs, build, make_joints, spec_arrays, step_both
+from resolve2d_gb300.solver import Solver
+
+pytestmark = pytest.mark.gpu
+
+
+def test_factory_scene_on_the_gpu_equals_the_oracle():
+    specs = body_specs(11)
+    s = Solver.init(4.0, 2)
+    hs = build(s, specs)
+    fac = s.entityFactory()
+    fac.makeDownwardsGravity(9.81)
+    make_joints(fac, hs)
+    fac.excludeCollisionPair(hs[1], hs[2])
+    o = Oracle()
+    add_to_oracle(o, *spec_arrays(specs))
+    o.lib.r2o_add_gravity(o.h, 9.81)
+    add_joints_to_oracle(o)
+    o.lib.r2o_exclude_pair(o.h, 1, 2)
+    step_both(s, o, 30, "factory scene on the GPU")
+    s.deinit()

@@ -1,0 +1,394 @@
+"""The reference-style ``Solver`` / ``EntityFactory`` (resolve2d_gb300/solver.py).
+
+Scenes are built through the factory exactly as the reference's examples build
+them (src/examples/*.zig): options, handles, ``body_unwrap().static = true``,
+joints by handle, exclusions.  They are compared with the same scene handed to
+the oracle directly.  The engine is replaced here by ``OracleBackend``, a test
+stand-in with ``engine.World``'s methods that steps the oracle.  These tests
+therefore check the solver's own bookkeeping on any host: map order,
+``swapRemove``, AABBs of new and old bodies, state write-back and errors.
+``tests/test_gpu_solver_api.py`` runs the same scene on the GPU.
+"""
+
+import math
+
+import numpy as np
+import pytest
+
+from oracle import ORDER_COLOUR, Oracle, _p
+from parity import assert_state_equal
+from resolve2d_gb300 import _native as N
+from resolve2d_gb300 import scenes as S
+from resolve2d_gb300.solver import (
+    BodyOptions, Density, DiscOptions, InvalidRigidBodyId, Mass, NoSuchIdExists, Parameters, RectangleOptions,
+    Solver,
+)
+import ctypes as C
+
+
+class OracleBackend:
+    """engine.World's interface over the oracle, for host-only tests.  Every
+    setter rebuilds the oracle from what it was given, carrying the current
+    state across."""
+
+    def __init__(self):
+        self.o = None
+        self.bodies = None
+        self.g = []
+        self.joints = (np.zeros(0, np.uint8), np.zeros(0, np.uint32), np.zeros(0, np.uint32),
+                       np.zeros((0, S.JOINT_PARAMS), np.float32))
+        self.x = np.zeros((0, 2), np.uint32)
+        self.calls = []
+
+    def _build(self, state, init_aabb):
+        ids, kind, props = self.bodies
+        n = ids.shape[0]
+        opt = np.zeros((S.NOPT, n), np.float32)
+        opt[S.POS_X], opt[S.POS_Y], opt[S.ANGLE] = state[S.S_POS_X], state[S.S_POS_Y], state[S.S_ANGLE]
+        opt[S.MU], opt[S.MASS_PROP] = props[S.P_MU], props[S.P_MASS]
+        opt[S.DIM0], opt[S.DIM1] = props[S.P_DIM0], props[S.P_DIM1]
+        o = Oracle()
+        k = np.ascontiguousarray(kind & 3, np.uint8)
+        o.lib.r2o_add_bodies(o.h, n, _p(np.ascontiguousarray(ids, np.uint32), C.c_uint32), _p(k, C.c_uint8),
+                             _p(opt, C.c_float))
+        np.testing.assert_array_equal(o.props(), props)  # mass given: the oracle derives the same inertia
+        st = o.state()
+        if init_aabb:
+            st[: S.S_AABB_X] = state[: S.S_AABB_X]
+        else:
+            st = np.array(state, np.float32)
+        o.set_state(np.ascontiguousarray(st))
+        for g in self.g:
+            o.lib.r2o_add_gravity(o.h, g)
+        t, a, b, prm = self.joints
+        if t.size:
+            o.lib.r2o_add_joints(o.h, t.shape[0], _p(t, C.c_uint8), _p(a, C.c_uint32), _p(b, C.c_uint32),
+                                 _p(prm, C.c_float))
+        o.nj = int(t.size)
+        for x, y in self.x:
+            o.lib.r2o_exclude_pair(o.h, int(x), int(y))
+        self.o = o
+
+    def _rebuild(self):
+        if self.bodies is not None:
+            self._build(self.o.state(), False)
+
+    def set_bodies(self, ids, kind, props, state, init_aabb):
+        self.calls.append(("set_bodies", int(ids.shape[0]), bool(init_aabb)))
+        self.bodies = (np.array(ids, np.uint32), np.array(kind, np.uint8), np.array(props, np.float32))
+        self._build(np.asarray(state, np.float32), init_aabb)
+
+    def set_gravity(self, g):
+        self.calls.append(("set_gravity", len(g)))
+        self.g = [float(v) for v in g]
+        self._rebuild()
+
+    def set_joints(self, t, a, b, prm):
+        self.calls.append(("set_joints", len(t)))
+        self.joints = (np.array(t, np.uint8), np.array(a, np.uint32), np.array(b, np.uint32),
+                       np.ascontiguousarray(prm, np.float32).reshape(-1, S.JOINT_PARAMS))
+        self._rebuild()
+
+    def set_exclusions(self, pairs):
+        self.calls.append(("set_exclusions", len(pairs)))
+        self.x = np.array(pairs, np.uint32).reshape(-1, 2)
+        self._rebuild()
+
+    def write_state(self, state):
+        self.calls.append(("write_state",))
+        self.o.set_state(np.ascontiguousarray(state, np.float32))
+
+    def read_state(self):
+        return self.o.state()
+
+    def process(self, dt, sub, iters):
+        self.calls.append(("process",))
+        have = set(self.bodies[0].tolist())
+        t, a, b, _ = self.joints
+        two = (t == S.JOINT_DISTANCE) | (t == S.JOINT_OFFSET_DISTANCE)
+        if any(x not in have for x in a.tolist()) or any(y not in have for y in b[two].tolist()):
+            raise N.R2DError(-2, "r2d_solver_process", "a joint names an unknown body id")
+        assert self.o.process(dt, sub, iters, ORDER_COLOUR) == 0
+
+    def sync(self):
+        pass
+
+    def close(self):
+        self.o = None
+
+
+# ---------------------------------------------------------------------------
+# one scene, two ways
+# ---------------------------------------------------------------------------
+def body_specs(seed, n=36):
+    """Bodies as the factory takes them: (shape, BodyOptions, geometry, static)."""
+    rng = np.random.default_rng(seed)
+    specs = [("rect", BodyOptions(pos=(0.0, -0.5), mass_prop=Density(5.0), mu=0.4), RectangleOptions(60.0, 1.0), True)]
+    for _ in range(n):
+        pos = (float(rng.uniform(-6, 6)), float(rng.uniform(0.2, 6)))
+        mp = Density(float(rng.uniform(0.5, 3))) if rng.random() < 0.7 else Mass(float(rng.uniform(0.5, 4)))
+        bo = BodyOptions(pos=pos, mass_prop=mp, vel=(float(rng.normal()), float(rng.normal())),
+                         angle=float(rng.uniform(-math.pi, math.pi)), omega=float(rng.normal()),
+                         mu=float(rng.uniform(0.1, 0.9)))
+        static = bool(rng.random() < 0.08)
+        if rng.random() < 0.5:
+            specs.append(("rect", bo, RectangleOptions(float(rng.uniform(0.3, 1.6)), float(rng.uniform(0.3, 1.6))),
+                          static))
+        else:
+            specs.append(("disc", bo, DiscOptions(float(rng.uniform(0.2, 0.8))), static))
+    return specs
+
+
+def spec_arrays(specs, first_id=0):
+    """The same bodies as the oracle's (ids, kind, opt) arrays."""
+    n = len(specs)
+    ids = np.arange(first_id, first_id + n, dtype=np.uint32)
+    kind = np.zeros(n, np.uint8)
+    opt = np.zeros((S.NOPT, n), np.float32)
+    for i, (shape, bo, go, static) in enumerate(specs):
+        k = (S.KIND_RECT if shape == "rect" else 0) | (S.KIND_STATIC if static else 0)
+        if isinstance(bo.mass_prop, Density):
+            k |= S.KIND_DENSITY
+            opt[S.MASS_PROP, i] = bo.mass_prop.density
+        else:
+            opt[S.MASS_PROP, i] = bo.mass_prop.mass
+        kind[i] = k
+        opt[S.POS_X, i], opt[S.POS_Y, i] = bo.pos
+        opt[S.ANGLE, i], opt[S.OMEGA, i], opt[S.MU, i] = bo.angle, bo.omega, bo.mu
+        opt[S.VEL_X, i], opt[S.VEL_Y, i] = bo.vel
+        if shape == "rect":
+            opt[S.DIM0, i], opt[S.DIM1, i] = go.width, go.height
+        else:
+            opt[S.DIM0, i] = go.radius
+    return ids, kind, opt
+
+
+def add_to_oracle(o, ids, kind, opt):
+    o.lib.r2o_add_bodies(o.h, ids.shape[0], _p(ids, C.c_uint32), _p(kind, C.c_uint8),
+                         _p(np.ascontiguousarray(opt), C.c_float))
+
+
+def build(solver, specs):
+    fac = solver.entityFactory()
+    handles = []
+    for shape, bo, go, static in specs:
+        h = fac.makeRectangleBody(bo, go) if shape == "rect" else fac.makeDiscBody(bo, go)
+        if static:
+            h.body_unwrap().static = True
+        handles.append(h)
+    return handles
+
+
+JOINTS = [  # (type, body a, body b, params, extra)
+    (S.JOINT_DISTANCE, 3, 4, Parameters(beta=8.0), [1.5]),
+    (S.JOINT_OFFSET_DISTANCE, 5, 6, Parameters(power_max=40.0, power_min=-40.0), [0.1, -0.2, 0.0, 0.15, 1.2]),
+    (S.JOINT_FIXED_POSITION, 7, 7, Parameters(beta=4.0), [1.0, 3.0]),
+    (S.JOINT_MOTOR, 8, 8, Parameters(power_max=25.0, power_min=-25.0), [3.0]),
+]
+
+
+def make_joints(fac, hs):
+    for t, a, b, prm, extra in JOINTS:
+        if t == S.JOINT_DISTANCE:
+            fac.makeDistanceJoint(prm, hs[a], hs[b], extra[0])
+        elif t == S.JOINT_OFFSET_DISTANCE:
+            fac.makeOffsetDistanceJoint(prm, hs[a], hs[b], extra[0:2], extra[2:4], extra[4])
+        elif t == S.JOINT_FIXED_POSITION:
+            fac.makeFixedPositionJoint(prm, hs[a], extra)
+        else:
+            fac.makeMotorJoint(prm, hs[a], extra[0])
+
+
+def add_joints_to_oracle(o):
+    t = np.array([j[0] for j in JOINTS], np.uint8)
+    a = np.array([j[1] for j in JOINTS], np.uint32)
+    b = np.array([j[2] for j in JOINTS], np.uint32)
+    prm = np.zeros((len(JOINTS), S.JOINT_PARAMS), np.float32)
+    for i, (_, _, _, p, extra) in enumerate(JOINTS):
+        prm[i, :3] = p.power_max, p.power_min, p.beta
+        prm[i, 3 : 3 + len(extra)] = extra
+    o.lib.r2o_add_joints(o.h, len(JOINTS), _p(t, C.c_uint8), _p(a, C.c_uint32), _p(b, C.c_uint32),
+                         _p(prm, C.c_float))
+    o.nj = len(JOINTS)
+
+
+DT, SUB, ITERS = 1 / 60, 2, 8
+
+
+def step_both(s, o, frames, what):
+    for f in range(frames):
+        s.process(DT, SUB, ITERS)
+        assert o.process(DT, SUB, ITERS, ORDER_COLOUR) == 0
+        if f % 5 == 4 or f == frames - 1:
+            assert_state_equal(s.read_state(), o.state(), f"{what}, frame {f + 1}")
+
+
+def test_factory_scene_steps_like_the_same_scene_given_to_the_oracle():
+    specs = body_specs(11)
+    s = Solver(backend=OracleBackend)
+    hs = build(s, specs)
+    fac = s.entityFactory()
+    fac.makeDownwardsGravity(9.81)
+    make_joints(fac, hs)
+    fac.excludeCollisionPair(hs[1], hs[2])
+    fac.excludeCollisionPair(hs[2], hs[1])  # the same pair
+    o = Oracle()
+    add_to_oracle(o, *spec_arrays(specs))
+    o.lib.r2o_add_gravity(o.h, 9.81)
+    add_joints_to_oracle(o)
+    o.lib.r2o_exclude_pair(o.h, 1, 2)
+    step_both(s, o, 30, "factory scene")
+    assert s.ids().tolist() == list(range(len(specs)))
+    assert s._dev.calls[:5] == [("set_gravity", 1), ("set_bodies", len(specs), True), ("set_joints", len(JOINTS)),
+                                ("set_exclusions", 1), ("process",)]
+    assert sum(c[0] == "set_bodies" for c in s._dev.calls) == 1  # nothing re-uploaded between frames
+
+
+def test_handles_and_views_read_the_reference_fields():
+    specs = body_specs(12, n=6)
+    s = Solver(backend=OracleBackend)
+    hs = build(s, specs)
+    shape, bo, go, static = specs[3]
+    b = hs[3].body_unwrap()
+    assert b.id == 3 and b.type == ("rectangle" if shape == "rect" else "disc") and b.static == static
+    m = np.float32(bo.mass_prop.mass) if isinstance(bo.mass_prop, Mass) else None
+    if m is not None:
+        assert b.props.mass == m
+    assert b.props.pos == (np.float32(bo.pos[0]), np.float32(bo.pos[1]))
+    assert b.props.momentum.x == np.float32(np.float32(bo.vel[0]) * np.float32(b.props.mass))
+    assert b.props.ang_momentum == np.float32(np.float32(bo.omega) * np.float32(b.props.inertia))
+    assert s.bodyHandle(999).body() is None
+    with pytest.raises(LookupError):
+        s.bodyHandle(999).body_unwrap()
+    s.process(DT, 1, ITERS)  # the engine computes the first AABBs
+    aabb = hs[0].body_unwrap().aabb
+    assert aabb.half_width == np.float32(30.0) and aabb.half_height == np.float32(0.5)
+
+
+def test_bodies_added_mid_run_get_a_first_aabb_and_the_others_keep_theirs():
+    specs = body_specs(13)
+    first, second = specs[:20], specs[20:]
+    s = Solver(backend=OracleBackend)
+    build(s, first)
+    s.entityFactory().makeDownwardsGravity(9.81)
+    o = Oracle()
+    add_to_oracle(o, *spec_arrays(first))
+    o.lib.r2o_add_gravity(o.h, 9.81)
+    step_both(s, o, 10, "before the additions")
+    build(s, second)
+    add_to_oracle(o, *spec_arrays(second, first_id=len(first)))
+    # the stored AABBs only feed the next broadphase, so compare them before stepping
+    s._flush()
+    assert_state_equal(s.read_state(), o.state(), "right after the additions")
+    step_both(s, o, 15, "after the additions")
+    assert ("set_bodies", len(specs), True) in s._dev.calls
+
+
+def test_remove_rigid_body_moves_the_last_body_into_its_slot():
+    specs = body_specs(14)
+    n = len(specs)
+    s = Solver(backend=OracleBackend)
+    build(s, specs)
+    s.entityFactory().makeDownwardsGravity(9.81)
+    o = Oracle()
+    ids, kind, opt = spec_arrays(specs)
+    add_to_oracle(o, ids, kind, opt)
+    o.lib.r2o_add_gravity(o.h, 9.81)
+    step_both(s, o, 6, "before the removal")
+    s.removeRigidBody(5)
+    with pytest.raises(NoSuchIdExists):
+        s.removeRigidBody(5)
+    order = list(range(n))
+    order[5] = n - 1
+    order.pop()
+    assert s.ids().tolist() == ids[order].tolist()
+    st = o.state()[:, order]
+    o2 = Oracle()
+    add_to_oracle(o2, ids[order], kind[order], np.ascontiguousarray(opt[:, order]))
+    o2.lib.r2o_add_gravity(o2.h, 9.81)
+    o2.set_state(np.ascontiguousarray(st))
+    assert_state_equal(s.read_state(), o2.state(), "right after the removal")
+    step_both(s, o2, 10, "after the removal")
+    assert ("set_bodies", n - 1, False) in s._dev.calls
+
+
+def test_writes_through_a_view_reach_the_next_frame():
+    specs = body_specs(15)
+    s = Solver(backend=OracleBackend)
+    hs = build(s, specs)
+    s.entityFactory().makeDownwardsGravity(9.81)
+    o = Oracle()
+    add_to_oracle(o, *spec_arrays(specs))
+    o.lib.r2o_add_gravity(o.h, 9.81)
+    step_both(s, o, 5, "before the writes")
+    p = hs[9].body_unwrap().props
+    p.momentum = (3.0, -2.0)
+    p.force = (10.0, 40.0)
+    p.torque = -5.0
+    st = o.state()
+    st[S.S_MOM_X, 9], st[S.S_MOM_Y, 9] = 3.0, -2.0
+    st[S.S_FORCE_X, 9], st[S.S_FORCE_Y, 9], st[S.S_TORQUE, 9] = 10.0, 40.0, -5.0
+    o.set_state(st)
+    assert ("write_state",) not in s._dev.calls  # written at the next frame, once
+    step_both(s, o, 10, "after the writes")
+    assert s._dev.calls.count(("write_state",)) == 1
+
+
+def test_a_joint_to_a_removed_body_is_invalid_rigid_body_id():
+    specs = body_specs(16, n=8)
+    s = Solver(backend=OracleBackend)
+    hs = build(s, specs)
+    s.entityFactory().makeDistanceJoint(Parameters(), hs[3], hs[4], 1.0)
+    s.process(DT, 1, ITERS)
+    before = s.read_state()
+    s.removeRigidBody(4)
+    with pytest.raises(InvalidRigidBodyId):
+        s.process(DT, 1, ITERS)
+    assert np.array_equal(s.read_state()[:, :4], before[:, :4])
+
+
+def test_clear_drops_everything_and_ids_keep_counting():
+    s = Solver(backend=OracleBackend)
+    hs = build(s, body_specs(17, n=5))
+    fac = s.entityFactory()
+    fac.makeDownwardsGravity(9.81)
+    fac.makeMotorJoint(Parameters(), hs[2], 1.0)
+    fac.excludeCollisionPair(hs[1], hs[2])
+    s.process(DT, 1, ITERS)
+    s.clear()
+    assert s.num_bodies == 0 and s.current_body_id == 6
+    s.process(DT, 1, ITERS)  # nothing to step
+    h = fac.makeDiscBody(BodyOptions(pos=(0.0, 2.0), mass_prop=Mass(1.0)), DiscOptions(0.5))
+    assert h.id == 6
+    s.process(DT, 1, ITERS)
+    tail = s._dev.calls[-5:]
+    assert ("set_gravity", 0) in tail and ("set_joints", 0) in tail and ("set_exclusions", 0) in tail
+    assert hs[0].body() is None and h.body_unwrap().props.pos.y < 2.0 + 1e-6
+
+
+def test_without_bodies_no_engine_is_made_and_gravity_is_capped():
+    made = []
+    s = Solver(backend=lambda: made.append(1) or OracleBackend())
+    s.process(DT, 1, ITERS)
+    assert not made
+    fac = s.entityFactory()
+    for _ in range(4):
+        fac.makeDownwardsGravity(9.81)
+    with pytest.raises(ValueError):
+        fac.makeDownwardsGravity(9.81)
+    with pytest.raises(TypeError):
+        fac.makeDiscBody(BodyOptions(pos=(0.0, 0.0), mass_prop=2.0))
+
+
+def test_the_default_engine_is_the_gpu_library():
+    """No stand-in: the solver drives the CUDA library, which reports a
+    missing device instead of falling back to anything."""
+    from conftest import gpu_available
+
+    if gpu_available():
+        pytest.skip("a GPU is present; tests/test_gpu_solver_api.py covers this path")
+    s = Solver()
+    build(s, body_specs(18, n=3))
+    with pytest.raises(N.R2DError) as e:
+        s.process(DT, 1, ITERS)
+    assert e.value.code == -8
