@@ -392,3 +392,28 @@ def test_the_default_engine_is_the_gpu_library():
     with pytest.raises(N.R2DError) as e:
         s.process(DT, 1, ITERS)
     assert e.value.code == -8
+
+
+def test_the_integration_guide_example_runs(monkeypatch):
+    """The reference-style example in INTEGRATION.md runs as written (engine
+    replaced by the oracle stand-in), and the disc it follows falls onto the ground."""
+    import re
+    from pathlib import Path
+
+    from conftest import REPO
+    import resolve2d_gb300.solver as mod
+
+    text = Path(REPO, "INTEGRATION.md").read_text()
+    block = next(b for b in re.findall(r"```python\n(.*?)```", text, flags=re.S) if "Solver.init(" in b)
+
+    class OracleSolver(mod.Solver):
+        def __init__(self, *a, **kw):
+            super().__init__(*a, backend=OracleBackend, **kw)
+
+    monkeypatch.setattr(mod, "Solver", OracleSolver)
+    env = {"print": lambda *a: None}
+    exec(block, env)
+    a, solver = env["a"], env["solver"]
+    assert solver.num_bodies == 2 and env["b"].body() is None
+    y = a.body_unwrap().props.pos.y
+    assert 0.0 < y < 4.0  # resting on the ground's top face (y = 0), below where it started
