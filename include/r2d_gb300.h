@@ -149,7 +149,8 @@ R2D_API int r2d_solver_destroy(r2d_solver* s);
  * order.  props [R2D_PROP_FIELDS][n], state [R2D_STATE_FIELDS][n].  With
  * init_aabb != 0 every AABB is computed as RigidBody.updateAABB does when a
  * body is created (Disc.zig:63-66, Rectangle.zig:71-86) and the AABB fields
- * of `state` are ignored. */
+ * of `state` are ignored.  Ids are unique (the store is a map keyed by id):
+ * two bodies with one id return R2D_ERR_INVALID_ARGUMENT. */
 R2D_API int r2d_solver_set_bodies(r2d_solver* s, uint32_t n, const uint32_t* ids, const uint8_t* kind,
                                   const float* props, const float* state, int init_aabb);
 /* Per-frame mirror of the dynamic state (host -> device, device -> host). */
@@ -217,7 +218,8 @@ R2D_API int r2d_batch_create(const r2d_config* cfg, r2d_batch** out);
 R2D_API int r2d_batch_destroy(r2d_batch* b);
 /* Bodies of world w are [body_off[w], body_off[w+1]) of the concatenated
  * arrays (same layouts as r2d_solver_set_bodies); gravity [nworlds] is one
- * DownwardsGravity per world (0 = none). */
+ * DownwardsGravity per world (0 = none).  Ids are unique within a world and
+ * may repeat across worlds. */
 R2D_API int r2d_batch_set_worlds(r2d_batch* b, uint32_t nworlds, const uint32_t* body_off, const uint32_t* ids,
                                  const uint8_t* kind, const float* props, const float* state,
                                  const float* gravity, int init_aabb);

@@ -26,6 +26,7 @@
 #include "r2d_device.cuh"
 #include "r2d_large.h"
 #include "r2d_sincos.h"
+#include "r2d_validate.h"
 #include "r2d_world.cuh"
 
 namespace r2d {
@@ -281,6 +282,11 @@ struct Engine {
         const uint32_t n = body_off[nw];
         for (uint32_t w = 0; w < nw; ++w)
             if (body_off[w + 1] < body_off[w]) return fail(R2D_ERR_INVALID_ARGUMENT, "body_off not monotonic");
+        uint32_t dup = 0;
+        const int64_t dw = r2d_first_duplicate_id(nw, body_off, ids, &dup);
+        if (dw >= 0)
+            return fail(R2D_ERR_INVALID_ARGUMENT,
+                        "world " + std::to_string(dw) + " holds two bodies with id " + std::to_string(dup));
         nworlds = nw;
         nbodies = n;
         ids_h.assign(ids, ids + n);
