@@ -9,12 +9,19 @@ Two reuses would skip work without changing any result:
     the AABB-intersecting pairs until some body's AABB leaves its grown box, so
     the binning could be skipped until then and only the exact filter run.
 
-This script measures how often each would apply: it settles the batch for 300
+(c) fewer colours would mean fewer barrier-separated solve phases.  A world's
+    contact colouring is an edge colouring of its dynamic bodies, so it needs
+    at least the largest number of contacts on one dynamic body; the script
+    compares the shipped hashed greedy order with that floor and with a
+    degree-first greedy order.
+
+This script measures all three: it settles the batch for 300
 steps (the benchmark's settling), steps a seeded sample of worlds for a number
 of frames, and prints (a) the fraction of world-frames whose key set is
 unchanged (plain, weighted by body count, and by world size), and (b) per
 delta, the fraction of world-frames that would rebuild and the candidate count
-relative to the exact pair count.  CPU only.
+relative to the exact pair count, and (c) the mean contact colours per
+world-frame under each rule.  CPU only.
 
     python tests/coherence_study.py [--worlds 256] [--frames 60] [--threads 8]
 """
@@ -46,6 +53,47 @@ def overlapping(x0, x1, y0, y1, static):
     return np.triu(ov, 1)
 
 
+M32 = 0xFFFFFFFF
+
+
+def colour_mix(a, b):
+    """r2d_colour_mix (resolve2d_gb300/csrc/r2d_colour.h) in Python integers."""
+    h = (a * 0x9E3779B1 + b * 0x85EBCA77 + 0x165667B1) & M32
+    h ^= h >> 16
+    h = (h * 0x7FEB352D) & M32
+    h ^= h >> 15
+    h = (h * 0x846CA68B) & M32
+    return h ^ (h >> 16)
+
+
+def greedy_colours(edges, dyn, order):
+    """Colours first-fit greedy uses over `edges` taken in `order`; only dynamic bodies conflict."""
+    used, top = {}, 0
+    for e in order:
+        ends = [b for b in edges[e] if dyn[b]]
+        taken = set().union(*(used.get(b, set()) for b in ends)) if ends else set()
+        c = 0
+        while c in taken:
+            c += 1
+        for b in ends:
+            used.setdefault(b, set()).add(c)
+        top = max(top, c + 1)
+    return top
+
+
+def colour_counts(keys, dyn):
+    """(floor, hashed greedy, degree-first greedy) for one frame's manifold keys."""
+    edges = [(int(min(a, b)), int(max(a, b))) for a, b in keys]
+    deg = np.zeros(dyn.shape[0], int)
+    for lo, hi in edges:
+        deg[lo] += dyn[lo]
+        deg[hi] += dyn[hi]
+    hashed = sorted(range(len(edges)), key=lambda e: (colour_mix(*edges[e]), edges[e]))
+    by_degree = sorted(range(len(edges)), key=lambda e: (-(deg[edges[e][0]] + deg[edges[e][1]]),
+                                                          colour_mix(*edges[e]), edges[e]))
+    return int(deg.max()), greedy_colours(edges, dyn, hashed), greedy_colours(edges, dyn, by_degree)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--worlds", type=int, default=256)
@@ -67,6 +115,7 @@ def main():
     rebuilds = dict.fromkeys(DELTAS, 0)
     cands = dict.fromkeys(DELTAS, 0)
     exact = manifolds = 0
+    colours = []
     for w in worlds:
         sub = sc.world(int(w))
         b0, b1 = int(sc.body_off[w]), int(sc.body_off[w + 1])
@@ -92,6 +141,11 @@ def main():
             assert o.process(sub.dt, sub.sub_steps, sub.iters, ORDER_COLOUR) == 0
             k, _ = o.manifolds()
             manifolds += len(k)
+            if len(k):
+                floor, hashed, by_degree = colour_counts(k, ~static)
+                cc, _ = o.colours()
+                assert hashed == int(cc.max()) + 1  # the restated rule is the oracle's
+                colours.append((n, floor, hashed, by_degree))
             keys = set(map(tuple, np.sort(k, axis=1).tolist()))
             if prev is not None:
                 hit = keys == prev
@@ -113,6 +167,12 @@ def main():
     for d in DELTAS:
         print(f"(b) delta {d:4.2f}: rebuild in {rebuilds[d] / frames:.3f} of world-frames, "
               f"candidates {cands[d] / max(exact, 1):.2f} x the exact pairs")
+    c = np.array(colours, float)
+    big = c[:, 0] > 192
+    for name, rows in (("all worlds", c), (">192 bodies", c[big])):
+        print(f"(c) {name} ({len(rows)} world-frames): contact colours: floor {rows[:, 1].mean():.2f}, "
+              f"hashed greedy {rows[:, 2].mean():.2f}, degree-first greedy {rows[:, 3].mean():.2f}")
+    print(f"    hashed greedy above floor + 1 in {np.mean(c[:, 2] > c[:, 1] + 1):.3f} of world-frames")
 
 
 if __name__ == "__main__":
