@@ -67,7 +67,7 @@ def zig_decls():
 
 def test_zig_externs_match_the_header():
     h, z = header_decls(), zig_decls()
-    assert len(z) >= 12
+    assert set(z) == set(h), f"not bound in Zig: {sorted(set(h) - set(z))}"
     for name, (ret, params) in z.items():
         assert name in h, f"{name} is bound in Zig but not declared"
         assert ret == h[name][0], f"{name}: return type"
@@ -87,3 +87,11 @@ def test_config_layouts_agree():
             z_fields.append((name.strip(), zig_type(rest.split("=")[0])))
     assert z_fields == c_fields
     assert [f for f, _ in N.Config._fields_] == [f for f, _ in c_fields]
+
+
+def test_status_codes_agree():
+    text = Path(REPO, "include", "r2d_gb300.h").read_text()
+    header = {f"R2D_{n}": int(v) for n, v in re.findall(r"R2D_(OK|ERR_\w+)\s*=\s*(-?\d+)", text)}
+    zig = {f"R2D_{n}": int(v) for n, v in re.findall(r"pub const (OK|ERR_\w+): Status = (-?\d+);", zig_block())}
+    assert zig == header
+    assert {v: k for k, v in header.items()} == N.STATUS_NAMES
