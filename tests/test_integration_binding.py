@@ -10,6 +10,8 @@ the test reads text.
 import re
 from pathlib import Path
 
+import pytest
+
 from conftest import REPO
 from resolve2d_gb300 import _native as N
 
@@ -95,3 +97,29 @@ def test_status_codes_agree():
     zig = {f"R2D_{n}": int(v) for n, v in re.findall(r"pub const (OK|ERR_\w+): Status = (-?\d+);", zig_block())}
     assert zig == header
     assert {v: k for k, v in header.items()} == N.STATUS_NAMES
+
+
+def test_the_c_example_compiles_and_links(tmp_path):
+    """The C example of the guide, wrapped in a function that supplies its
+    arrays, compiles as C99 against the header and links against the library."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc")
+    if cc is None:
+        pytest.skip("no gcc")
+    text = Path(REPO, "INTEGRATION.md").read_text()
+    block = next(b for b in re.findall(r"```c\n(.*?)```", text, flags=re.S) if "r2d_solver_create" in b)
+    body = "\n".join(line for line in block.splitlines() if not line.startswith("#include"))
+    src = tmp_path / "example.c"
+    src.write_text(
+        '#include <stdio.h>\n#include "r2d_gb300.h"\n'
+        "int run(uint32_t n, const uint32_t* ids, const uint8_t* kind, const float* props, float* state) {\n"
+        f"{body}\n    return st;\n}}\n"
+        "int main(void) { return 0; }\n"
+    )
+    lib_dir = str(Path(N.LIB_PATH).parent)
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-I", str(Path(REPO, "include")), str(src),
+                        "-o", str(tmp_path / "example"), "-L", lib_dir, "-lr2d_gb300", f"-Wl,-rpath,{lib_dir}"],
+                       stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    assert r.returncode == 0, r.stdout
