@@ -193,18 +193,20 @@ R2D_API int r2d_solver_read_state_fields(r2d_solver* s, uint32_t first, uint32_t
  * writing the f32 state restarts it from that state.  No counterpart in the
  * reference. */
 R2D_API int r2d_solver_read_positions_f64(r2d_solver* s, double* pose);
-/* Debug taps (need R2D_FLAG_DEBUG_TAPS): the last frame's manifolds
- * (Solver.manifolds, lib.zig:137) with their contact colours.  keys [cap][2]
- * are (reference, incident) body indices; data [cap][R2D_MANIFOLD_FLOATS]. */
 /* Consecutive still steps of the solver's world (R2D_FLAG_SLEEP); from 60 on
  * the world sleeps.  0 when sleeping is off. */
 R2D_API int r2d_solver_sleep_frames(r2d_solver* s, uint32_t* frames);
 /* Kernel launches of the solver's latest step (a world on the grid pipeline
  * launches per phase and per colouring; a fused world launches one kernel). */
 R2D_API int r2d_solver_launches_per_step(r2d_solver* s, uint32_t* out);
+/* Debug taps (need R2D_FLAG_DEBUG_TAPS): the last frame's manifolds
+ * (Solver.manifolds, lib.zig:137) with their contact colours.  keys [cap][2]
+ * are (reference, incident) body indices; data [cap][R2D_MANIFOLD_FLOATS]. */
 R2D_API int r2d_solver_num_manifolds(r2d_solver* s, uint32_t* out);
 R2D_API int r2d_solver_get_manifolds(r2d_solver* s, uint32_t cap, uint32_t* keys, float* data,
                                      uint32_t* colours);
+/* Debug taps: the colour of each of the first `cap` joints, in insertion order,
+ * from the last frame (the solve runs joint colours in ascending order). */
 R2D_API int r2d_solver_get_joint_colours(r2d_solver* s, uint32_t cap, uint32_t* colours);
 
 /* ---------------------------------------------------------------------------
