@@ -4,7 +4,9 @@ Mirrors src/core/lib.zig with the same names, argument meaning and errors, so
 a scene written against the reference reads the same here:
 
 - ``Solver.init``, ``deinit``, ``clear``, ``process``, ``bodyHandle``,
-  ``removeRigidBody`` and ``entityFactory`` (lib.zig:131-314);
+  ``removeRigidBody`` and ``entityFactory`` (lib.zig:131-314), and the
+  ``bodies`` and ``manifolds`` fields (lib.zig:135-137) as a read-only map of
+  body views and the last frame's manifolds keyed by id;
 - ``EntityFactory.makeDiscBody``, ``makeRectangleBody``,
   ``makeDownwardsGravity``, ``makeOffsetDistanceJoint``, ``makeDistanceJoint``,
   ``makeFixedPositionJoint``, ``makeMotorJoint`` and ``excludeCollisionPair``
@@ -37,6 +39,7 @@ from __future__ import annotations
 
 import dataclasses
 import math
+from collections.abc import Iterator, Mapping
 from typing import Callable, NamedTuple, Sequence
 
 import numpy as np
@@ -262,6 +265,71 @@ class BodyHandle:
         return b
 
 
+class ContactPoint(NamedTuple):
+    """CollisionPoint (collision.zig:22-51): lever arms from the two bodies'
+    centres at the start of the frame, depths and accumulated impulses."""
+
+    ref_r: Vector2
+    inc_r: Vector2
+    depth: float
+    original_depth: float
+    mass_n: float
+    mass_t: float
+    accumulated_pn: float
+    accumulated_pt: float
+
+
+class Manifold(NamedTuple):
+    """CollisionManifold (collision.zig:53-69) of the last frame, keyed by body
+    ids, with the colour its constraint was solved in."""
+
+    ref_id: int
+    inc_id: int
+    normal: Vector2
+    tangent: Vector2
+    friction: float
+    points: tuple[ContactPoint, ...]
+    colour: int
+
+
+_P0, _PF = 9, 12  # first float of point 0 in a manifold row, floats per point
+
+
+def _manifold(ids: np.ndarray, key, row, colour) -> Manifold:
+    pts = []
+    for p in range(2):
+        if row[5 + p]:
+            b = _P0 + _PF * p
+            pts.append(ContactPoint(Vector2(float(row[b + 2]), float(row[b + 3])),
+                                    Vector2(float(row[b + 4]), float(row[b + 5])),
+                                    *(float(v) for v in row[b + 6: b + 12])))
+    return Manifold(int(ids[key[0]]), int(ids[key[1]]), Vector2(float(row[0]), float(row[1])),
+                    Vector2(float(row[2]), float(row[3])), float(row[4]), tuple(pts), int(colour))
+
+
+class BodyMap(Mapping):
+    """Solver.bodies (lib.zig:135): id -> RigidBody view, in map order."""
+
+    def __init__(self, solver: "Solver"):
+        self._solver = solver
+
+    def __getitem__(self, id) -> RigidBody:
+        slot = self._solver._slot_of.get(int(id))
+        if slot is None:
+            raise KeyError(id)
+        return RigidBody(self._solver, slot)
+
+    def __iter__(self) -> Iterator[int]:
+        return iter(self._solver._ids[: self._solver._n].tolist())
+
+    def __len__(self) -> int:
+        return self._solver._n
+
+    def count(self) -> int:
+        """AutoArrayHashMap.count."""
+        return len(self)
+
+
 def _id(h) -> int:
     return int(h.id) if isinstance(h, BodyHandle) else int(h)
 
@@ -382,6 +450,7 @@ class Solver:
         self._excl: dict[tuple[int, int], None] = {}
         self._bodies_dirty = self._state_dirty = self._host_stale = False
         self._gravity_dirty = self._joints_dirty = self._excl_dirty = True
+        self._frame_ids = None
 
     def deinit(self) -> None:
         """Solver.deinit (lib.zig:159-179): releases the device engine too."""
@@ -425,6 +494,19 @@ class Solver:
     def num_bodies(self) -> int:
         return self._n
 
+    @property
+    def bodies(self) -> BodyMap:
+        """The bodies by id, in map order (insertion order, ``swapRemove`` on removal)."""
+        return BodyMap(self)
+
+    def manifolds(self) -> list[Manifold]:
+        """Solver.manifolds (lib.zig:137) of the last frame.  Needs the engine's
+        debug taps: ``Solver(debug=True)``."""
+        if self._dev is None or self._frame_ids is None:
+            return []
+        keys, data, colours = self._dev.manifolds()
+        return [_manifold(self._frame_ids, keys[m], data[m], colours[m]) for m in range(keys.shape[0])]
+
     def ids(self) -> np.ndarray:
         """Body ids in map order."""
         return self._ids[: self._n].copy()
@@ -446,6 +528,7 @@ class Solver:
                 raise InvalidRigidBodyId(e.code, "Solver.process", str(e)) from e
             raise
         self._host_stale = True
+        self._frame_ids = self._ids[: self._n].copy()  # the order the frame's manifold keys index
 
     def sync(self) -> None:
         """Waits for the frames in flight and raises the first device-side error."""

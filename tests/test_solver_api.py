@@ -110,6 +110,11 @@ class OracleBackend:
             raise N.R2DError(-2, "r2d_solver_process", "a joint names an unknown body id")
         assert self.o.process(dt, sub, iters, ORDER_COLOUR) == 0
 
+    def manifolds(self):
+        k, d = self.o.manifolds()
+        c, _ = self.o.colours()
+        return k, d, c[: k.shape[0]]
+
     def sync(self):
         pass
 
@@ -417,3 +422,34 @@ def test_the_integration_guide_example_runs(monkeypatch):
     assert solver.num_bodies == 2 and env["b"].body() is None
     y = a.body_unwrap().props.pos.y
     assert 0.0 < y < 4.0  # resting on the ground's top face (y = 0), below where it started
+
+
+def test_bodies_map_and_last_frame_manifolds_are_keyed_by_id():
+    specs = body_specs(19)
+    n = len(specs)
+    s = Solver(backend=OracleBackend)
+    build(s, specs)
+    s.entityFactory().makeDownwardsGravity(9.81)
+    assert s.manifolds() == []  # nothing stepped yet
+    for _ in range(3):
+        s.process(DT, 1, ITERS)
+    s.removeRigidBody(2)  # the last body takes slot 2: ids and slots now differ
+    bodies = s.bodies
+    assert len(bodies) == bodies.count() == n - 1 and 2 not in bodies
+    assert list(bodies) == s.ids().tolist() and list(bodies)[2] == n - 1
+    assert bodies[n - 1].id == n - 1
+    with pytest.raises(KeyError):
+        bodies[2]
+    s.process(DT, 1, ITERS)
+    ms = s.manifolds()
+    k, d, c = s._dev.manifolds()
+    assert len(ms) == k.shape[0] > 0
+    ids = s.ids()
+    for m, key, row, col in zip(ms, k, d, c):
+        assert (m.ref_id, m.inc_id) == (ids[key[0]], ids[key[1]]) and m.colour == col
+        assert len(m.points) == int(row[5]) + int(row[6])
+        assert m.normal == (row[0], row[1]) and m.points[0].depth == row[9 + 6]
+    # ids of manifolds name bodies that exist; the removed id never appears
+    assert all(m.ref_id in bodies and m.inc_id in bodies for m in ms)
+    s.removeRigidBody(5)
+    assert {(m.ref_id, m.inc_id) for m in s.manifolds()} == {(m.ref_id, m.inc_id) for m in ms}
