@@ -85,10 +85,30 @@ def max_over_ranks(x: float, device: str = "cuda") -> float:
     return float(t.item())
 
 
-def replica_seed(rank: int) -> int:
-    """Each rank steps its own 4,096-world replica (weak scaling): the
-    headline scene's seed 3, shifted by the rank."""
-    return 3 + rank
+def sum_over_ranks(x: float, device: str = "cuda") -> float:
+    """The sum of every rank's `x`; `x` itself with one process."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def rank_scene(rank: int, world: int, per_rank: int = 4096):
+    """The worlds one rank steps.  One process: the headline batch (seed 3,
+    4,096 worlds).  N processes: the N x 4,096 worlds of the same generator and
+    seed, dealt out by body count (weak scaling, nothing exchanged while
+    stepping).  Every rank builds the same global batch and keeps its share."""
+    from resolve2d_gb300 import scenes
+    from resolve2d_gb300.shard import balanced_shards
+
+    if world == 1:
+        return scenes.config3(nworlds=per_rank)
+    full = scenes.config3(nworlds=per_rank * world)
+    return full.select(balanced_shards(np.diff(full.body_off), world)[rank])
 
 
 def dist_env():
@@ -376,7 +396,7 @@ def main():
     from resolve2d_gb300.engine import Batch, World
 
     B.build_library()
-    sc = scenes.config3(seed=replica_seed(rank))
+    sc = rank_scene(rank, world)
     # a dedicated stream: the library launches on it and the CUDA events below
     # are recorded on it (the legacy default stream has handle 0, which the
     # library would replace with a stream of its own)
@@ -425,7 +445,9 @@ def main():
     dev_s = sum(ms) / 1e3
     dev_s = max_over_ranks(dev_s)
     clk = clocks.stop()
-    value = nb * args.steps * world / dev_s
+    nb_all = int(round(sum_over_ranks(nb)))  # bodies stepped by all ranks together
+    nw_all = int(round(sum_over_ranks(sc.nworlds)))
+    value = nb_all * args.steps / dev_s
     launches = batch.launches_per_step() * args.steps
 
     # End to end through the C ABI with pinned host buffers.  Each step
@@ -443,7 +465,7 @@ def main():
         for _ in range(e2e_steps):
             step_fn()
         batch.sync()
-        return nb * e2e_steps / (time.perf_counter() - t1)
+        return nb_all * e2e_steps / max_over_ranks(time.perf_counter() - t1)
 
     forces_in = torch.zeros((3, nb), dtype=torch.float32).pin_memory().numpy()
     pose_out = torch.empty((6, nb), dtype=torch.float32).pin_memory().numpy()
@@ -497,21 +519,24 @@ def main():
         "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * step_s, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-        "config": {"workload": HEADLINE, "bodies": nb, "worlds": sc.nworlds,
+        "config": {"workload": HEADLINE, "bodies": nb_all, "worlds": nw_all,
                    "l2": "flushed between timed steps (256 MiB write outside the events)",
                    "tiles": "threads per CTA of each size class autotuned on the settled worlds"
                    if not args.no_autotune else "default threads per size class",
                    "cuda_device_max_connections": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS"),
-                   "parallelism": f"replicas x{world}"},
+                   "parallelism": (f"worlds dealt to {world} GPUs by body count, {nb} bodies on rank 0"
+                                   if world > 1 else "one GPU")},
         "gpu_launches": launches,
         "wall_s_timed_loop": wall,
-        "e2e": {"value": e2e_v, "unit": "body-steps/s", "h2d_bytes_per_step": 12 * nb, "d2h_bytes_per_step": 24 * nb,
+        "e2e": {"value": e2e_v, "unit": "body-steps/s", "h2d_bytes_per_step": 12 * nb_all,
+                "d2h_bytes_per_step": 24 * nb_all,
                 "inputs": "force and torque rows (pinned)", "results": "pose and momenta rows (pinned)",
                 "call": "r2d_batch_process_io (the step reads and writes the pinned rows over the CPU-GPU link)",
                 "three_calls": {"value": e2e_three, "call": "write_state_fields, process, read_state_fields"},
-                "full_state": {"value": e2e_full, "h2d_bytes_per_step": 52 * nb, "d2h_bytes_per_step": 52 * nb}},
+                "full_state": {"value": e2e_full, "h2d_bytes_per_step": 52 * nb_all,
+                               "d2h_bytes_per_step": 52 * nb_all}},
         "plain_one_world_per_launch": {"value": plain, "unit": "body-steps/s", "worlds": args.plain_worlds,
-                                       "batched_over_plain": (value / world) / plain if plain else None},
+                                       "batched_over_plain": (value * nb / nb_all) / plain if plain else None},
         "roofline": {"bound": "hbm", "kernel": "world_step_kernel (the size-class launches of one step)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_src,

@@ -98,6 +98,24 @@ class Scene:
             dt=self.dt, sub_steps=self.sub_steps, iters=self.iters, steps=self.steps,
         )
 
+    def select(self, worlds) -> "Scene":
+        """The worlds at the given indices, in that order, as their own
+        (joint-free) scene."""
+        assert self.jtype.size == 0 and self.xpairs.size == 0, "joint-free scenes only"
+        worlds = np.asarray(worlds, np.int64)
+        spans = [np.arange(self.body_off[w], self.body_off[w + 1]) for w in worlds]
+        rows = np.concatenate(spans) if spans else np.zeros(0, np.int64)
+        sizes = np.array([len(sp) for sp in spans], np.int64)
+        return Scene(
+            name=f"{self.name}[{len(worlds)} worlds]",
+            ids=self.ids[rows].copy(),
+            kind=self.kind[rows].copy(),
+            opt=np.ascontiguousarray(self.opt[:, rows]),
+            body_off=np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint32),
+            gravity=self.gravity[worlds].copy(),
+            dt=self.dt, sub_steps=self.sub_steps, iters=self.iters, steps=self.steps,
+        )
+
     def body_radius(self) -> np.ndarray:
         """Size of each body for error figures: a disc's radius, half the
         shorter side of a rectangle."""

@@ -1,10 +1,14 @@
-"""The benchmark's multi-rank host logic on two CPU processes (gloo): every
-rank reports the slowest rank's time, and each rank steps its own replica."""
+"""The benchmark's multi-rank host logic on two CPU processes (gloo).
+
+Every rank reports the slowest rank's time and the sum of the ranks' bodies.
+The ranks step disjoint shares of one global batch, dealt out by body count.
+"""
 
 import os
 import socket
 import sys
 
+import numpy as np
 import pytest
 
 torch = pytest.importorskip("torch")
@@ -12,6 +16,7 @@ import torch.distributed as dist  # noqa: E402
 import torch.multiprocessing as mp  # noqa: E402
 
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PER_RANK = 48
 
 
 def _free_port() -> int:
@@ -27,12 +32,16 @@ def _rank(rank: int, world: int, port: int, out):
     dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
     try:
         t = bench.max_over_ranks(1.0 + rank * 0.25, device="cpu")
-        out.put((rank, t, bench.replica_seed(rank)))
+        sc = bench.rank_scene(rank, world, per_rank=PER_RANK)
+        total = bench.sum_over_ranks(sc.nbodies, device="cpu")
+        out.put((rank, t, sc.nworlds, sc.nbodies, total, sc.gravity.tolist()))
     finally:
         dist.destroy_process_group()
 
 
-def test_two_ranks_agree_on_the_slowest_time():
+def test_two_ranks_agree_on_time_and_bodies_and_share_one_batch():
+    from resolve2d_gb300 import scenes
+
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     port = _free_port()
@@ -43,13 +52,23 @@ def test_two_ranks_agree_on_the_slowest_time():
         p.join(timeout=120)
         assert p.exitcode == 0
     got = sorted(q.get(timeout=10) for _ in procs)
-    assert [g[1] for g in got] == [1.25, 1.25]
-    assert got[0][2] != got[1][2]  # every rank its own replica
+    assert [g[1] for g in got] == [1.25, 1.25]  # the slowest rank's time, everywhere
+    full = scenes.config3(nworlds=2 * PER_RANK)
+    assert got[0][4] == got[1][4] == full.nbodies  # the bodies of all ranks together
+    assert got[0][2] + got[1][2] == full.nworlds
+    assert abs(got[0][3] - got[1][3]) <= int(np.diff(full.body_off).max())  # balanced to one world
+    # the two shares are disjoint: every world's gravity (a per-world draw) appears once
+    g = sorted(got[0][5] + got[1][5])
+    np.testing.assert_array_equal(g, np.sort(full.gravity))
 
 
 def test_one_process_needs_no_group():
     sys.path.insert(0, REPO)
     import bench
+    from resolve2d_gb300 import scenes
 
     assert bench.max_over_ranks(2.5, device="cpu") == 2.5
-    assert bench.replica_seed(0) == 3
+    assert bench.sum_over_ranks(7.0, device="cpu") == 7.0
+    one = bench.rank_scene(0, 1, per_rank=PER_RANK)
+    ref = scenes.config3(nworlds=PER_RANK)
+    np.testing.assert_array_equal(one.opt, ref.opt)  # one process steps the headline batch itself
