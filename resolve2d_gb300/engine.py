@@ -88,7 +88,8 @@ class World:
 
     @classmethod
     def from_scene(cls, sc: Scene, debug: bool = False, stream=None, **kw) -> "World":
-        assert sc.nworlds == 1
+        if sc.nworlds != 1:
+            raise ValueError(f"World.from_scene takes one world; this scene has {sc.nworlds} (use Batch)")
         w = cls(debug=debug, stream=stream, **kw)
         props, state = derive_props_state(sc.kind, sc.opt)
         w.set_gravity(sc.gravity[sc.gravity != 0] if sc.gravity.size else np.zeros(0, np.float32))
@@ -205,7 +206,8 @@ class Batch:
 
     @classmethod
     def from_scene(cls, sc: Scene, debug: bool = False, stream=None, **kw) -> "Batch":
-        assert sc.jtype.size == 0 and sc.xpairs.size == 0, "the batch entry points take worlds without joints"
+        if sc.jtype.size or sc.xpairs.size:
+            raise ValueError("the batch entry points take worlds without joints or exclusions (use World)")
         b = cls(debug=debug, stream=stream, **kw)
         props, state = derive_props_state(sc.kind, sc.opt)
         b.set_worlds(sc.body_off, sc.ids, sc.kind & 3, props, state, sc.gravity, init_aabb=True)

@@ -81,3 +81,13 @@ def test_static_step_refuses_bad_arguments_before_launching():
     assert static_step(lib, ngrav=1, gravity=None) == INVALID
     assert static_step(lib, sub_steps=0) == INVALID
     assert "sub_steps" in last_error(lib)
+
+
+def test_scene_shapes_the_handles_refuse_before_any_device_work():
+    from resolve2d_gb300 import scenes
+    from resolve2d_gb300.engine import Batch, World
+
+    with pytest.raises(ValueError, match="one world"):
+        World.from_scene(scenes.config3(nworlds=2))
+    with pytest.raises(ValueError, match="without joints"):
+        Batch.from_scene(scenes.random_scene(1, n=6, joints=True))
