@@ -86,7 +86,8 @@ class Scene:
 
     def worlds(self, w0: int, w1: int) -> "Scene":
         """Worlds ``w0 .. w1-1`` as their own (joint-free) scene."""
-        assert self.jtype.size == 0 and self.xpairs.size == 0, "joint-free scenes only"
+        if self.jtype.size or self.xpairs.size:
+            raise ValueError("joint-free scenes only")
         b0, b1 = int(self.body_off[w0]), int(self.body_off[w1])
         return Scene(
             name=f"{self.name}[{w0}:{w1}]",
@@ -101,7 +102,8 @@ class Scene:
     def select(self, worlds) -> "Scene":
         """The worlds at the given indices, in that order, as their own
         (joint-free) scene."""
-        assert self.jtype.size == 0 and self.xpairs.size == 0, "joint-free scenes only"
+        if self.jtype.size or self.xpairs.size:
+            raise ValueError("joint-free scenes only")
         worlds = np.asarray(worlds, np.int64)
         spans = [np.arange(self.body_off[w], self.body_off[w + 1]) for w in worlds]
         rows = np.concatenate(spans) if spans else np.zeros(0, np.int64)
