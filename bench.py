@@ -26,8 +26,8 @@ pos_error_vs_fp64  stated from the committed precision study
            (tests/precision_study.py: the long-horizon workload against the
            FP64 oracle, position error in body radii).
 cpu_baseline  the CPU oracle (the C++ restatement of the reference's step,
-           replaying the same constraint order) on this host's cores, from
-           the same settled state, for about ten seconds.
+           in the reference's own constraint order) on this host's cores,
+           from the same settled state, for about ten seconds.
 
 --impl reference times that CPU step alone (the reference is Zig and cannot
 be built here) and prints its own line.
@@ -196,21 +196,26 @@ def cpu_threads() -> int:
 
 
 def settle_scene(sc, steps):
-    """Advance the scene `steps` steps on the CPU oracle (all host threads)."""
+    """Advance the scene `steps` steps on the CPU oracle (all host threads), in
+    the reference's own constraint order."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle as O
 
-    _, state, st = O.batch_run(sc, steps, cpu_threads())
+    _, state, st = O.batch_run(sc, steps, cpu_threads(), order=O.ORDER_REFERENCE)
     if st:
         raise RuntimeError(f"the oracle returned status {st}")
     return state.reshape(13, sc.nbodies)
 
 
 def oracle_time(sc, state, steps, threads):
+    """Seconds the oracle takes for `steps` steps of every world from `state`,
+    in the reference's own constraint order (joints, then manifolds, in
+    insertion and discovery order, lib.zig:226-236): the reference's step,
+    without the colouring that the colour-major order adds."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle as O
 
-    secs, _, st = O.batch_run(sc, steps, threads, state_in=state)
+    secs, _, st = O.batch_run(sc, steps, threads, state_in=state, order=O.ORDER_REFERENCE)
     if st:
         raise RuntimeError(f"the oracle returned status {st}")
     return secs
@@ -262,7 +267,8 @@ def run_reference(args):
         "config": {"workload": workload, "bodies": sc.nbodies, "worlds": sc.nworlds},
         "cpu_baseline": {"value": v, "unit": "body-steps/s", "cores": threads, "kind": "port",
                          "sample": f"all {sc.nworlds} worlds x {args.steps} steps from the settled state; "
-                                   "C++ restatement of Solver.process (Zig toolchain absent)"},
+                                   "C++ restatement of Solver.process in the reference's own constraint order "
+                                   "(Zig toolchain absent)"},
         "e2e": {"value": v, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -358,7 +364,8 @@ def run_large(args):
         line["cpu_baseline"] = {"value": nb * cpu_steps / secs, "unit": "body-steps/s", "cores": 1,
                                 "kind": "port", "seconds": secs,
                                 "sample": f"the world x {cpu_steps} steps from the settled state on one core (the "
-                                          "oracle threads over worlds; C++ restatement of Solver.process)"}
+                                          "oracle threads over worlds; C++ restatement of Solver.process in the "
+                                          "reference's own constraint order)"}
     print(json.dumps(line), flush=True)
 
 
@@ -555,7 +562,8 @@ def main():
         line["cpu_baseline"] = {"value": nb * cpu_steps / secs, "unit": "body-steps/s", "cores": threads,
                                 "kind": "port", "seconds": secs,
                                 "sample": f"all {sc.nworlds} worlds x {cpu_steps} steps from the settled state "
-                                          "(C++ restatement of Solver.process; Zig toolchain absent)"}
+                                          "(C++ restatement of Solver.process in the reference's own constraint order; "
+                                          "Zig toolchain absent)"}
         # the same step on one core (the reference itself is single-threaded), on a bounded
         # sample: the first worlds holding about a tenth of the bodies, for about five seconds
         sub_w = int(np.searchsorted(sc.body_off, nb // 10)) + 1

@@ -34,6 +34,8 @@ _SIG = {
     "r2o_set_hash_config": ([_P, C.c_float, C.c_uint32], None),
     "r2o_set_warm_start": ([_P, C.c_int], None),
     "r2o_set_sleep": ([_P, C.c_int], None),
+    "r2o_set_phase_timing": ([_P, C.c_int], None),
+    "r2o_phase_seconds": ([_P, _f64p], None),
     "r2o_sleep_frames": ([_P], C.c_uint32),
     "r2o_get_state": ([_P, _f32p], None),
     "r2o_get_state_f64": ([_P, _f64p], None),
@@ -52,6 +54,10 @@ _SIG = {
 }
 
 _lib = None
+
+
+# Phases of Solver::step, in r2o::Phase order (r2d_oracle.hpp)
+PHASES = ("manifolds", "colouring", "forces", "prestep", "solve", "integrate")
 
 
 def load() -> C.CDLL:
@@ -129,6 +135,15 @@ class Oracle:
         """Sleeping (r2d_sleep.h): a world still for R2D_SLEEP_FRAMES
         consecutive steps is not stepped until its state is written."""
         self.lib.r2o_set_sleep(self.h, int(bool(on)))
+
+    def set_phase_timing(self, on: bool = True):
+        """Time each phase of the step (PHASES order); clears the sums."""
+        self.lib.r2o_set_phase_timing(self.h, int(bool(on)))
+
+    def phase_seconds(self) -> np.ndarray:
+        out = np.zeros(len(PHASES), np.float64)
+        self.lib.r2o_phase_seconds(self.h, _p(out, C.c_double))
+        return out
 
     def sleep_frames(self) -> int:
         return int(self.lib.r2o_sleep_frames(self.h))

@@ -18,6 +18,7 @@
  */
 #include <atomic>
 #include <chrono>
+#include <iterator>
 #include <cstring>
 #include <memory>
 #include <thread>
@@ -244,6 +245,18 @@ void r2o_get_state_f64(void* hp, double* out) {
 void r2o_set_state(void* hp, const float* in) {
     Handle* h = (Handle*)hp;
     DISPATCH(h, (set_state(S, in), S.sleep_frames = 0u));  // a write wakes the world
+}
+
+/* Per-phase wall time of the step (a measurement aid; r2o::Phase order).
+ * Switching it on or off clears the sums. */
+void r2o_set_phase_timing(void* hp, int on) {
+    Handle* h = (Handle*)hp;
+    DISPATCH(h, (S.time_phases = on != 0, std::fill(std::begin(S.phase_seconds), std::end(S.phase_seconds), 0.0)));
+}
+
+void r2o_phase_seconds(void* hp, double* out) {
+    Handle* h = (Handle*)hp;
+    DISPATCH(h, std::copy(std::begin(S.phase_seconds), std::end(S.phase_seconds), out));
 }
 
 void r2o_set_sleep(void* hp, int on) {

@@ -42,6 +42,7 @@
 
 #include <algorithm>
 #include <array>
+#include <chrono>
 #include <cmath>
 #include <cstdint>
 #include <limits>
@@ -70,6 +71,21 @@ enum Status : int {
 constexpr int64_t MAX_CELLS = 64ll << 20;
 
 enum Order : int { ORDER_REFERENCE = 0, ORDER_COLOUR = 1 };
+
+// Phases of one step, for the optional wall-clock split (Solver::time_phases):
+// updateManifolds (broadphase and narrowphase, lib.zig:194, 253-299), the
+// colouring of the colour-major order, forces and velocities (lib.zig:199-216),
+// the TGS update and preStep (lib.zig:218-224), the iterations
+// (lib.zig:226-236) and integration (lib.zig:238-249).
+enum Phase : int {
+    PH_MANIFOLDS = 0,
+    PH_COLOURING,
+    PH_FORCES,
+    PH_PRESTEP,
+    PH_SOLVE,
+    PH_INTEGRATE,
+    PH_COUNT
+};
 
 // ---------------------------------------------------------------------------
 // Constants (src/core/simulation_constants.zig:3-22)
@@ -525,6 +541,11 @@ public:
     // until its state is written again.
     bool sleep_enabled = false;
     uint32_t sleep_frames = 0;
+
+    // A measurement aid: with time_phases set, step() adds each phase's wall
+    // time to phase_seconds.  Off, it reads no clock.
+    bool time_phases = false;
+    double phase_seconds[PH_COUNT] = {};
 
     std::vector<Body<R>> bodies;  // insertion order
     std::unordered_map<uint32_t, size_t> index_of_id;
@@ -1155,6 +1176,14 @@ public:
     int step(R dt, size_t sub_steps, size_t collision_iters, int order) {
         const R f32_sub = R(sub_steps);
         const R sub_dt = dt / f32_sub;
+        using clock = std::chrono::steady_clock;
+        clock::time_point t_mark = time_phases ? clock::now() : clock::time_point{};
+        auto mark = [&](int phase) {  // charge the time since the last mark to `phase`
+            if (!time_phases) return;
+            const clock::time_point now = clock::now();
+            phase_seconds[phase] += std::chrono::duration<double>(now - t_mark).count();
+            t_mark = now;
+        };
 
         // joints resolve their ids on every solve in the reference; validate
         // once up front so that an invalid id leaves the state untouched.
@@ -1167,11 +1196,13 @@ public:
 
         int st = update_manifolds();
         if (st != OK) return st;
+        mark(PH_MANIFOLDS);
         if (order == ORDER_COLOUR) {
             st = compute_colouring();
             if (st != OK) return st;
         }
         if (warm_start) warm_load();
+        mark(PH_COLOURING);
 
         for (size_t s = 0; s < sub_steps; ++s) {
             for (R g : gravity) {  // DownwardsGravity.apply (DownwardsGravity.zig:35-39)
@@ -1189,10 +1220,12 @@ public:
                 b.props.momentum.y += b.props.force.y * sub_dt;
                 b.props.ang_momentum += b.props.torque * sub_dt;
             }
+            mark(PH_FORCES);
             for (auto& km : manifolds) {  // lib.zig:218-224
                 update_tgs_depth(km.second, km.first);
                 pre_step(km.second, km.first);
             }
+            mark(PH_PRESTEP);
             if (warm_start && s == 0) {
                 if (order == ORDER_COLOUR) {
                     for (size_t m : contact_order) warm_apply(manifolds[m].second, manifolds[m].first);
@@ -1216,6 +1249,7 @@ public:
                     for (auto& km : manifolds) calculate_impulses(km.second, km.first, sub_dt);
                 }
             }
+            mark(PH_SOLVE);
             for (Body<R>& b : bodies) {  // lib.zig:238-249
                 if (b.is_static) continue;
                 R sm = sub_dt / b.props.mass;
@@ -1225,8 +1259,10 @@ public:
                 b.props.force = V2<R>{};
                 b.props.torque = 0;
             }
+            mark(PH_INTEGRATE);
         }
         if (warm_start) warm_store();
+        mark(PH_INTEGRATE);
         return OK;
     }
 };

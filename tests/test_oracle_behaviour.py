@@ -196,3 +196,21 @@ def test_sleeping_rule():
     for _ in range(80):
         assert moving.process(1 / 60, 1, 8, ORDER_COLOUR) == 0
     assert moving.sleep_frames() < 60
+
+
+def test_phase_timing_measures_without_changing_results():
+    from oracle import PHASES
+
+    sc = scenes.random_scene(8, n=40, joints=True)
+    timed, plain = Oracle.from_scene(sc), Oracle.from_scene(sc)
+    timed.set_phase_timing(True)
+    for _ in range(10):
+        assert timed.process(1 / 60, 2, 8, ORDER_COLOUR) == 0
+        assert plain.process(1 / 60, 2, 8, ORDER_COLOUR) == 0
+    np.testing.assert_array_equal(timed.state(), plain.state())
+    ph = timed.phase_seconds()
+    assert ph.shape == (len(PHASES),) and (ph >= 0).all() and ph.sum() > 0
+    assert ph[PHASES.index("solve")] > 0 and ph[PHASES.index("colouring")] > 0
+    assert not plain.phase_seconds().any()  # off: nothing is read or added
+    timed.set_phase_timing(False)
+    assert not timed.phase_seconds().any()  # switching clears the sums
