@@ -175,7 +175,9 @@ def _prop_scalar(f: int):
 
 class Props:
     """RigidBody.Props (RigidBody.zig:67-81) of one body, read from and
-    written to the solver's state.  Values are float32, as the reference's."""
+    written to the solver's state.  Values are float32, as the reference's.
+    Reads see the last frame; writes reach the engine at the next ``process``,
+    all of a frame's writes in one upload."""
 
     def __init__(self, solver: "Solver", slot: int):
         self._solver = solver
