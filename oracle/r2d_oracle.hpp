@@ -31,6 +31,16 @@
  *   ORDER_COLOUR:    the same per-constraint arithmetic replayed in the GPU's
  *                    colour-major order (r2d_colour.h defines the colouring).
  *
+ * What pins it.  The reference ships two unit tests, the Vector2 operations
+ * (nmath.zig:157-176) and three AABB overlaps (aabb.zig:34-45); the oracle
+ * reproduces both (tests/test_oracle_reference_tests.py).  Contacts,
+ * rectangle manifolds and joints are also checked on cases worked by hand
+ * from the reference source (tests/test_oracle_behaviour.py,
+ * test_oracle_manifolds.py, test_oracle_joints.py).  The reference cannot be
+ * built or run here and ships no golden outputs, so beyond those cases parity
+ * is unpinned: the oracle is trusted because it follows the source line by
+ * line.
+ *
  * Deviations, all documented where they occur:
  *   - body ids are u32 (the reference's RigidBody.Id is u16,
  *     RigidBody.zig:15), so scenes above 65,536 bodies are representable;
