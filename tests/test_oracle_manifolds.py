@@ -107,3 +107,40 @@ def test_boxes_apart_by_more_than_the_margin_make_no_manifold():
     assert o.update_manifolds() == 0
     k, _ = o.manifolds()
     assert k.shape[0] == 0
+
+
+def test_disc_over_a_box_corner_becomes_the_reference():
+    # Box 2x2 at the origin (id 0, static), disc r = 0.5 at (1.3, 1.3) (id 1).  The
+    # box's faces overlap the disc by 0.2.  The disc's one axis runs from its
+    # centre to the box's closest point, which for a rectangle is its nearest
+    # vertex (1, 1) (Rectangle.zig:114-130).  Along that axis the overlap is
+    # 0.5 - 0.3*sqrt(2) = 0.0757, smaller, so the disc is the reference
+    # (collision.zig:281-286).  Its single point is that vertex, at depth
+    # |c - v| - r (Disc.zig:99-123), stored half the depth along the normal.
+    o = world([("rect", 0.0, 0.0, 2.0, 2.0, 0.5, 1.0, 0.0, 0.0, 0.0, 0.0, True), ("disc", 1.3, 1.3, 0.5, 0.5)])
+    assert o.update_manifolds() == 0
+    k, d = o.manifolds()
+    assert k.tolist() == [[1, 0]]
+    s = math.sqrt(0.5)
+    np.testing.assert_allclose(d[0, :2], [-s, -s], atol=1e-6)
+    pts = points(d[0])
+    assert len(pts) == 1
+    depth = 0.3 * math.sqrt(2.0) - 0.5
+    assert abs(pts[0]["depth"][0] - depth) < 1e-6
+    np.testing.assert_allclose(pts[0]["pos"], [1.0 + s * depth / 2, 1.0 + s * depth / 2], atol=1e-6)
+
+
+def test_disc_beside_a_box_face_meets_the_face():
+    # Disc r = 0.5 at (1.3, 0.0): the box's right face (overlap 0.2) beats the
+    # disc's axis toward the vertex (1, 1), so the box is the reference.  The
+    # disc's incident point is its centre minus r along the normal (Disc.zig:125-130):
+    # (0.8, 0), depth -0.2, stored at (0.9, 0).
+    o = world([("rect", 0.0, 0.0, 2.0, 2.0, 0.5, 1.0, 0.0, 0.0, 0.0, 0.0, True), ("disc", 1.3, 0.0, 0.5, 0.5)])
+    assert o.update_manifolds() == 0
+    k, d = o.manifolds()
+    assert k.tolist() == [[0, 1]]
+    np.testing.assert_allclose(d[0, :2], [1.0, 0.0], atol=1e-6)
+    pts = points(d[0])
+    assert len(pts) == 1
+    assert abs(pts[0]["depth"][0] + 0.2) < 1e-6
+    np.testing.assert_allclose(pts[0]["pos"], [0.9, 0.0], atol=1e-6)
