@@ -35,11 +35,12 @@
  * (nmath.zig:157-176) and three AABB overlaps (aabb.zig:34-45); the oracle
  * reproduces both (tests/test_oracle_reference_tests.py).  Contacts,
  * rectangle and disc manifolds, friction and joints are also checked on
- * cases worked by hand from the reference source (tests/test_oracle_behaviour.py,
- * test_oracle_manifolds.py, test_oracle_friction.py, test_oracle_joints.py).  The reference cannot be
- * built or run here and ships no golden outputs, so beyond those cases parity
- * is unpinned: the oracle is trusted because it follows the source line by
- * line.
+ * cases worked by hand from the reference source
+ * (tests/test_oracle_behaviour.py, test_oracle_manifolds.py,
+ * test_oracle_friction.py, test_oracle_joints.py).  The reference cannot be
+ * built or run here and ships no golden outputs, so beyond those cases
+ * parity is unpinned: the oracle is trusted because it follows the source
+ * line by line.
  *
  * Deviations, all documented where they occur:
  *   - body ids are u32 (the reference's RigidBody.Id is u16,
