@@ -37,7 +37,7 @@
  * rectangle and disc manifolds, friction and joints are also checked on
  * cases worked by hand from the reference source
  * (tests/test_oracle_behaviour.py, test_oracle_manifolds.py,
- * test_oracle_friction.py, test_oracle_joints.py).  The reference cannot be
+ * test_oracle_friction.py, test_oracle_joints.py, test_oracle_quirks.py).  The reference cannot be
  * built or run here and ships no golden outputs, so beyond those cases
  * parity is unpinned: the oracle is trusted because it follows the source
  * line by line.
