@@ -8,7 +8,8 @@ Each follows from a line of the reference and is checked here on the CPU:
 - a point whose normal impulse is below 1e-4 is skipped whole, friction
   included (collision.zig:176), so a body too light to ever reach that
   impulse gets no support at all;
-- the narrowphase runs once a frame, not once a substep (lib.zig:194).
+- the narrowphase runs once a frame, not once a substep (lib.zig:194);
+- the TGS depth update writes no depth (collision.zig:73-100).
 """
 
 import math
@@ -85,3 +86,23 @@ def test_the_narrowphase_runs_once_a_frame():
     assert o.process(float(DT), 4, 8, ORDER_COLOUR) == 0
     k, _ = o.manifolds()
     assert k.shape[0] == 1  # found at the next frame's start
+
+
+def test_the_tgs_depth_update_changes_no_depth():
+    # updateTGSDepth skips a point whose depth still equals its original depth
+    # (collision.zig:80), and that depth is only written after the check, so over
+    # any number of substeps every point keeps the narrowphase's depth
+    sc = S.random_scene(31, n=50)
+    o = Oracle.from_scene(sc)
+    for _ in range(20):
+        assert o.process(sc.dt, 1, sc.iters, ORDER_COLOUR) == 0
+    assert o.process(sc.dt, 4, sc.iters, ORDER_COLOUR) == 0
+    _, d = o.manifolds()
+    seen = 0
+    for row in d:
+        for p in range(2):
+            if row[5 + p]:
+                base = 9 + 12 * p
+                assert row[base + 6] == row[base + 7]  # depth == original_depth
+                seen += 1
+    assert seen > 20
