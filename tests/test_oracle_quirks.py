@@ -9,7 +9,8 @@ Each follows from a line of the reference and is checked here on the CPU:
   included (collision.zig:176), so a body too light to ever reach that
   impulse gets no support at all;
 - the narrowphase runs once a frame, not once a substep (lib.zig:194);
-- the TGS depth update writes no depth (collision.zig:73-100).
+- the TGS depth update writes no depth (collision.zig:73-100);
+- both points of a manifold read the same start velocities (collision.zig:145-149).
 """
 
 import math
@@ -106,3 +107,19 @@ def test_the_tgs_depth_update_changes_no_depth():
                 assert row[base + 6] == row[base + 7]  # depth == original_depth
                 seen += 1
     assert seen > 20
+
+
+def test_both_points_of_a_manifold_read_the_same_start_velocities():
+    # calculateImpulses reads the bodies' velocities once per manifold and applies
+    # the summed impulses after its point loop (collision.zig:145-149, 208-217).
+    # A flat box landing on the ground meets it with two mirror-image points:
+    # one iteration gives them bit-identical normal impulses.  Read point by point,
+    # point 0's impulse would start the box turning and change point 1's.
+    o = world([("rect", 0.0, -0.5, 40.0, 1.0, 0.5, 1.0, 0.0, 0.0, 0.0, 0.0, True),
+               ("rect", 0.0, 0.49, 1.0, 1.0, 0.5, 1.0, 0.0, -1.0)])
+    assert o.process(float(DT), 1, 1, ORDER_COLOUR) == 0
+    _, d = o.manifolds()
+    assert d.shape[0] == 1 and d[0, 5] == 1 and d[0, 6] == 1
+    pn0, pn1 = d[0, 9 + 10], d[0, 9 + 12 + 10]
+    assert pn0 > 0.0 and pn0 == pn1
+    assert o.state()[S.S_ANG_MOM, 1] == 0.0  # the pair's torques cancel exactly
