@@ -1,6 +1,6 @@
 """The reference-style ``Solver`` over the GPU engine, against the oracle.
 
-The scene of ``test_solver_api.py`` is built through the factory: discs and
+The scene of ``solver_scenes.py`` is built through the factory: discs and
 rectangles by density and by mass, a static ground set through
 ``body_unwrap().static``, gravity, all four joint types and an exclusion.  It
 is stepped on the GPU through ``engine.World``, and every five frames it must
@@ -10,7 +10,7 @@ equal the same scene given to the oracle, bit for bit.
 import pytest
 
 from oracle import Oracle
-from test_solver_api import add_joints_to_oracle, add_to_oracle, body_specs, build, make_joints, spec_arrays, step_both
+from solver_scenes import add_joints_to_oracle, add_to_oracle, body_specs, build, make_joints, spec_arrays, step_both
 from resolve2d_gb300.solver import Solver
 
 pytestmark = pytest.mark.gpu
