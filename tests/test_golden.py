@@ -10,7 +10,7 @@ import sys
 import numpy as np
 import pytest
 
-from oracle import ORDER_COLOUR, Oracle
+from oracle import ORDER_COLOUR
 from parity import assert_manifolds_equal, assert_state_equal
 
 HERE = os.path.dirname(os.path.abspath(__file__))

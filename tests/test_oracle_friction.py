@@ -9,7 +9,6 @@ on the CPU:
 - every point of a settled scene lies inside its Coulomb cone.
 """
 
-import math
 
 import numpy as np
 
