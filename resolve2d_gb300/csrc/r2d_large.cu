@@ -11,7 +11,7 @@
  *   cells, entries, bucket sort    SpatialHash.zig:19-137 (a counting sort)
  *   candidate pairs                lib.zig:264-282 (bucket sharing, filters,
  *                                  "manifold already exists" as a hash set)
- *   narrowphase + manifolds        collision.zig:299-363, Bodies/*.zig
+ *   narrowphase + manifolds        collision.zig:299-363, Bodies/{Disc,Rectangle,RigidBody}.zig
  *   colouring                      Jones-Plassmann rounds: a constraint takes
  *                                  its colour once every neighbour that comes
  *                                  before it in priority order has one, which

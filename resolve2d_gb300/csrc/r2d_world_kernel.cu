@@ -2,7 +2,7 @@
  * r2d_world_kernel.cu -- one CTA steps one whole world: the body state is
  * loaded into shared memory once, and the spatial-hash broadphase
  * (src/core/SpatialHash.zig), the SAT narrowphase and manifold build
- * (src/core/collision.zig:221-363, Bodies/*.zig), the constraint colouring,
+ * (src/core/collision.zig:221-363, Bodies/{Disc,Rectangle,RigidBody}.zig), the constraint colouring,
  * the substep loop of Solver.process (src/core/lib.zig:189-251: forces,
  * velocities, prestep, joint + contact impulses, integration) and the state
  * write-back all run from shared memory.  HBM sees each body's state once in
