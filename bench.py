@@ -221,6 +221,20 @@ def oracle_time(sc, state, steps, threads):
     return secs
 
 
+def one_core_baseline(sc, state) -> dict:
+    """The oracle's step on one thread (the reference itself is single-threaded),
+    on a bounded sample: the first worlds holding about a tenth of the bodies,
+    for about five seconds."""
+    sub_w = int(np.searchsorted(sc.body_off, sc.nbodies // 10)) + 1
+    sub = sc.worlds(0, min(sub_w, sc.nworlds))
+    sub_state = np.ascontiguousarray(state[:, : sub.nbodies])
+    one = oracle_time(sub, sub_state, 1, 1)
+    steps = max(1, min(50, int(5.0 / max(one, 1e-3))))
+    secs = oracle_time(sub, sub_state, steps, 1)
+    return {"value": sub.nbodies * steps / secs, "unit": "body-steps/s", "seconds": secs,
+            "sample": f"worlds 0..{sub.nworlds - 1} ({sub.nbodies} bodies) x {steps} steps on one thread"}
+
+
 def stated_pos_error():
     """The f32-vs-FP64 position error the metric is stated at, from the
     committed precision study (tests/precision_study.py on the 16,384-world
@@ -271,6 +285,8 @@ def run_reference(args):
                                    "(Zig toolchain absent)"},
         "e2e": {"value": v, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if sc.nworlds > 1:
+        line["cpu_baseline"]["one_core"] = one_core_baseline(sc, state)
     print(json.dumps(line), flush=True)
 
 
@@ -564,17 +580,7 @@ def main():
                                 "sample": f"all {sc.nworlds} worlds x {cpu_steps} steps from the settled state "
                                           "(C++ restatement of Solver.process in the reference's own constraint order; "
                                           "Zig toolchain absent)"}
-        # the same step on one core (the reference itself is single-threaded), on a bounded
-        # sample: the first worlds holding about a tenth of the bodies, for about five seconds
-        sub_w = int(np.searchsorted(sc.body_off, nb // 10)) + 1
-        sub = sc.worlds(0, min(sub_w, sc.nworlds))
-        sub_state = np.ascontiguousarray(settled[:, : sub.nbodies])
-        one1 = oracle_time(sub, sub_state, 1, 1)
-        steps1 = max(1, min(50, int(5.0 / max(one1, 1e-3))))
-        secs1 = oracle_time(sub, sub_state, steps1, 1)
-        line["cpu_baseline"]["one_core"] = {
-            "value": sub.nbodies * steps1 / secs1, "unit": "body-steps/s", "seconds": secs1,
-            "sample": f"worlds 0..{sub.nworlds - 1} ({sub.nbodies} bodies) x {steps1} steps on one thread"}
+        line["cpu_baseline"]["one_core"] = one_core_baseline(sc, settled)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
