@@ -15,6 +15,9 @@ a scene written against the reference reads the same here:
   ``RigidBody`` fields (``id``, ``static``, ``type``, ``props``, ``aabb``;
   RigidBody.zig:67-90).
 
+``batch(solvers)`` steps many such scenes together, one world each, on the
+batched engine (``engine.Batch``).
+
 Bodies are kept on the host in the reference's map order: insertion order,
 with ``swapRemove`` on removal (lib.zig:308-310).  They are handed to the
 engine (``engine.World``, the C ABI's ``r2d_solver_*``) at the next
@@ -637,3 +640,49 @@ class Solver:
         if self._excl_dirty:
             d.set_exclusions(np.array(list(self._excl), np.uint32).reshape(-1, 2))
             self._excl_dirty = False
+
+
+# ---------------------------------------------------------------------------
+# many scenes at once
+# ---------------------------------------------------------------------------
+def batch_arrays(solvers: Sequence[Solver]):
+    """The bodies of several solvers as one batch's arrays: (body_off, ids,
+    kind, props, state, gravity).  Each solver becomes one world; worlds keep
+    the solvers' order and their own ids.
+
+    The batch entry points take one DownwardsGravity per world and no joints or
+    exclusions, and they compute every first AABB or none.  So each solver must
+    have at most one gravity generator, no joints and no exclusions, and either
+    all the solvers have stepped or none has."""
+    fresh = set()
+    for s in solvers:
+        if len(s._gravity) > 1 or s._jtype or s._excl:
+            raise ValueError("a batched world has at most one gravity generator and no joints or exclusions")
+        s._pull()
+        if s._n:
+            fresh.add(bool(s._fresh[: s._n].all()))
+            if s._fresh[: s._n].any() and not s._fresh[: s._n].all():
+                raise ValueError("a solver holds both new and stepped bodies; step it once first")
+    if len(fresh) > 1:
+        raise ValueError("either every solver has stepped or none has")
+    counts = [s._n for s in solvers]
+    body_off = np.concatenate([[0], np.cumsum(counts)]).astype(np.uint32)
+    ids = np.concatenate([s._ids[: s._n] for s in solvers]) if solvers else np.zeros(0, np.uint32)
+    kind = np.concatenate([s._kind[: s._n] for s in solvers]) if solvers else np.zeros(0, np.uint8)
+    props = np.concatenate([s._props[:, : s._n] for s in solvers], axis=1) if solvers else np.zeros((NPROP, 0))
+    state = np.concatenate([s._state[:, : s._n] for s in solvers], axis=1) if solvers else np.zeros((NSTATE, 0))
+    gravity = np.array([s._gravity[0] if s._gravity else 0.0 for s in solvers], np.float32)
+    return (body_off, ids.astype(np.uint32), kind.astype(np.uint8), np.ascontiguousarray(props, np.float32),
+            np.ascontiguousarray(state, np.float32), gravity, fresh == {True})
+
+
+def batch(solvers: Sequence[Solver], **engine_options):
+    """Independent worlds built with the reference's API, stepped together:
+    an ``engine.Batch`` holding one world per solver (see ``batch_arrays``).
+    The solvers themselves are not changed."""
+    from .engine import Batch
+
+    body_off, ids, kind, props, state, gravity, init_aabb = batch_arrays(solvers)
+    b = Batch(**engine_options)
+    b.set_worlds(body_off, ids, kind, props, state, gravity, init_aabb=init_aabb)
+    return b

@@ -346,3 +346,64 @@ def test_bodies_map_and_last_frame_manifolds_are_keyed_by_id():
     assert all(m.ref_id in bodies and m.inc_id in bodies for m in ms)
     s.removeRigidBody(5)
     assert {(m.ref_id, m.inc_id) for m in s.manifolds()} == {(m.ref_id, m.inc_id) for m in ms}
+
+
+def test_batch_arrays_are_the_scene_arrays_a_batch_takes():
+    from resolve2d_gb300.solver import batch_arrays
+
+    groups = [body_specs(40 + k, n=5 + 7 * k) for k in range(3)]
+    gravity = [9.81, 0.0, 4.5]
+    solvers = []
+    for specs, g in zip(groups, gravity):
+        s = Solver(backend=OracleBackend)
+        build(s, specs)
+        if g:
+            s.entityFactory().makeDownwardsGravity(g)
+        solvers.append(s)
+    body_off, ids, kind, props, state, grav, init_aabb = batch_arrays(solvers)
+    sc = S._concat("three", [spec_arrays(specs) for specs in groups], gravity, DT, 1, ITERS, 1)
+    want_props, want_state = S.derive_props_state(sc.kind, sc.opt)
+    np.testing.assert_array_equal(body_off, sc.body_off)
+    np.testing.assert_array_equal(ids, sc.ids)
+    np.testing.assert_array_equal(kind, sc.kind & 3)
+    np.testing.assert_array_equal(props, want_props)
+    np.testing.assert_array_equal(state, want_state)
+    np.testing.assert_array_equal(grav, np.float32(gravity))
+    assert init_aabb  # nothing has stepped: the engine computes every first AABB
+
+
+def test_batch_arrays_of_stepped_solvers_carry_their_states():
+    from resolve2d_gb300.solver import batch_arrays
+
+    solvers = []
+    for k in range(2):
+        s = Solver(backend=OracleBackend)
+        build(s, body_specs(50 + k, n=8))
+        s.entityFactory().makeDownwardsGravity(9.81)
+        for _ in range(3):
+            s.process(DT, 1, ITERS)
+        solvers.append(s)
+    body_off, _, _, _, state, _, init_aabb = batch_arrays(solvers)
+    assert not init_aabb
+    for k, s in enumerate(solvers):
+        np.testing.assert_array_equal(state[:, body_off[k]: body_off[k + 1]], s.read_state())
+    # a new body beside stepped ones: the batch cannot give only it a first AABB
+    solvers[1].entityFactory().makeDiscBody(BodyOptions(pos=(0.0, 9.0), mass_prop=Mass(1.0)), DiscOptions(0.3))
+    with pytest.raises(ValueError):
+        batch_arrays(solvers)
+
+
+def test_batch_arrays_refuse_what_a_batch_cannot_hold():
+    from resolve2d_gb300.solver import batch_arrays
+
+    s = Solver(backend=OracleBackend)
+    hs = build(s, body_specs(60, n=4))
+    s.entityFactory().makeDistanceJoint(Parameters(), hs[1], hs[2], 1.0)
+    with pytest.raises(ValueError, match="joints"):
+        batch_arrays([s])
+    t = Solver(backend=OracleBackend)
+    build(t, body_specs(61, n=4))
+    t.entityFactory().makeDownwardsGravity(9.81)
+    t.entityFactory().makeDownwardsGravity(1.0)
+    with pytest.raises(ValueError, match="gravity"):
+        batch_arrays([t])
