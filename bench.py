@@ -7,6 +7,11 @@ dt = 1/60, 8 solver iterations, one sub-step.  The scene is first advanced
 full contact load, not bodies in free fall.  One "step" = one
 Solver.process-equivalent pass over all 4,096 worlds.
 
+Under torchrun with N ranks (one GPU each), every rank builds the same
+N x 4,096 worlds, keeps the share dealt to it by body count
+(resolve2d_gb300/shard.py) and steps it with nothing exchanged (weak
+scaling); value is all ranks' bodies over the slowest rank's time.
+
 value      body-steps/s with the state resident in HBM, CUDA events around
            each step on the library's stream, L2 flushed (256 MiB write)
            between steps outside the timed events.
