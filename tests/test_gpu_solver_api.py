@@ -31,3 +31,39 @@ def test_factory_scene_on_the_gpu_equals_the_oracle():
     o.lib.r2o_exclude_pair(o.h, 1, 2)
     step_both(s, o, 30, "factory scene on the GPU")
     s.deinit()
+
+
+def run_batched_reference_scenes():
+    """Three reference-style scenes stepped as one batch (``solver.batch``),
+    each world against its own oracle; returns nothing, asserts bit equality."""
+    from oracle import ORDER_COLOUR
+    from parity import assert_state_equal
+    from resolve2d_gb300.solver import batch
+    from solver_scenes import DT, ITERS
+
+    groups = [body_specs(70 + k, n=6 + 9 * k) for k in range(3)]
+    solvers, oracles = [], []
+    for specs in groups:
+        s = Solver.init(4.0, 2)  # its own engine is made at its first process, which never comes
+        build(s, specs)
+        s.entityFactory().makeDownwardsGravity(9.81)
+        solvers.append(s)
+        o = Oracle()
+        add_to_oracle(o, *spec_arrays(specs))
+        o.lib.r2o_add_gravity(o.h, 9.81)
+        oracles.append(o)
+    b = batch(solvers)
+    off = [0]
+    for specs in groups:
+        off.append(off[-1] + len(specs))
+    for _ in range(20):
+        b.process(DT, 1, ITERS)
+        for o in oracles:
+            assert o.process(DT, 1, ITERS, ORDER_COLOUR) == 0
+    st = b.read_state()
+    for k, o in enumerate(oracles):
+        assert_state_equal(st[:, off[k]: off[k + 1]], o.state(), f"batched world {k}")
+
+
+def test_reference_scenes_batched_on_the_gpu_equal_the_oracle():
+    run_batched_reference_scenes()
