@@ -200,12 +200,37 @@ def cpu_threads() -> int:
         return os.cpu_count() or 1
 
 
+def _with_constraints(sc) -> bool:
+    """The oracle's batch runner steps bodies only; a scene with joints or
+    exclusions (one world) steps through a whole oracle solver instead."""
+    return bool(sc.jtype.size or sc.xpairs.size)
+
+
+def _solver_run(sc, state, steps):
+    """(seconds, final state) of `steps` oracle steps of a one-world scene with
+    its joints and exclusions, on one thread, in the reference's order."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+
+    o = O.Oracle.from_scene(sc)
+    if state is not None:
+        o.set_state(np.ascontiguousarray(state, np.float32))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        st = o.process(sc.dt, sc.sub_steps, sc.iters, O.ORDER_REFERENCE)
+        if st:
+            raise RuntimeError(f"the oracle returned status {st}")
+    return time.perf_counter() - t0, o.state()
+
+
 def settle_scene(sc, steps):
     """Advance the scene `steps` steps on the CPU oracle (all host threads), in
     the reference's own constraint order."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle as O
 
+    if _with_constraints(sc):
+        return _solver_run(sc, None, steps)[1]
     _, state, st = O.batch_run(sc, steps, cpu_threads(), order=O.ORDER_REFERENCE)
     if st:
         raise RuntimeError(f"the oracle returned status {st}")
@@ -220,6 +245,8 @@ def oracle_time(sc, state, steps, threads):
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle as O
 
+    if _with_constraints(sc):
+        return _solver_run(sc, state, steps)[0]
     secs, _, st = O.batch_run(sc, steps, threads, state_in=state, order=O.ORDER_REFERENCE)
     if st:
         raise RuntimeError(f"the oracle returned status {st}")
@@ -284,7 +311,8 @@ def run_reference(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded)",
         "config": {"workload": workload, "bodies": sc.nbodies, "worlds": sc.nworlds},
-        "cpu_baseline": {"value": v, "unit": "body-steps/s", "cores": threads, "kind": "port",
+        "cpu_baseline": {"value": v, "unit": "body-steps/s", "cores": 1 if _with_constraints(sc) else threads,
+                         "kind": "port",
                          "sample": f"all {sc.nworlds} worlds x {args.steps} steps from the settled state; "
                                    "C++ restatement of Solver.process in the reference's own constraint order "
                                    "(Zig toolchain absent)"},
