@@ -191,7 +191,11 @@ class Oracle:
 def batch_run(sc, steps: int, nthreads: int, precision: int = 32, order: int = ORDER_COLOUR, state_in=None):
     """Step every world of a scene on host threads, optionally from a given
     state ([13][n] field-major over all worlds); returns (seconds, state
-    [13][n], status)."""
+    [13][n], status).  The worlds are stepped with their bodies and gravity
+    only, so a scene with joints or exclusions is refused: step it through
+    Oracle.from_scene."""
+    if sc.jtype.size or sc.xpairs.size:
+        raise ValueError("batch_run steps bodies only; use Oracle.from_scene for joints or exclusions")
     lib = load()
     off = np.ascontiguousarray(sc.body_off, np.uint32)
     ids = np.ascontiguousarray(sc.ids, np.uint32)

@@ -214,3 +214,11 @@ def test_phase_timing_measures_without_changing_results():
     assert not plain.phase_seconds().any()  # off: nothing is read or added
     timed.set_phase_timing(False)
     assert not timed.phase_seconds().any()  # switching clears the sums
+
+
+def test_the_batch_runner_refuses_what_it_would_drop():
+    import pytest
+    from oracle import batch_run
+
+    with pytest.raises(ValueError, match="joints"):
+        batch_run(scenes.random_scene(3, n=8, joints=True), 1, 1)
