@@ -1,7 +1,9 @@
-"""The benchmark's multi-rank host logic on two CPU processes (gloo).
+"""The benchmark's host logic, on the CPU.
 
-Every rank reports the slowest rank's time and the sum of the ranks' bodies.
-The ranks step disjoint shares of one global batch, dealt out by body count.
+On two gloo processes, every rank reports the slowest rank's time and the sum
+of the ranks' bodies.  The ranks step disjoint shares of one global batch,
+dealt out by body count.  The CPU baseline steps a constrained scene with its
+joints and exclusions.
 """
 
 import os
@@ -72,3 +74,21 @@ def test_one_process_needs_no_group():
     one = bench.rank_scene(0, 1, per_rank=PER_RANK)
     ref = scenes.config3(nworlds=PER_RANK)
     np.testing.assert_array_equal(one.opt, ref.opt)  # one process steps the headline batch itself
+
+
+def test_the_cpu_baseline_steps_a_scene_with_its_joints():
+    """A scene with joints and exclusions is settled and timed through a whole
+    oracle solver, never by the body-only batch runner."""
+    sys.path.insert(0, REPO)
+    import bench
+    from oracle import ORDER_REFERENCE, Oracle
+    from resolve2d_gb300 import scenes
+
+    sc = scenes.config2(n_bodies=1200, n_chains=20, chain_links=10, n_motors=10, box_w=120.0, box_h=40.0)
+    assert sc.jtype.size and sc.xpairs.size and bench._with_constraints(sc)
+    got = bench.settle_scene(sc, 3)
+    o = Oracle.from_scene(sc)
+    for _ in range(3):
+        assert o.process(sc.dt, sc.sub_steps, sc.iters, ORDER_REFERENCE) == 0
+    np.testing.assert_array_equal(got, o.state())
+    assert bench.oracle_time(sc, got, 1, 4) > 0.0
