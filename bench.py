@@ -212,6 +212,8 @@ def _solver_run(sc, state, steps):
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle as O
 
+    if sc.nworlds != 1:  # Oracle.from_scene takes world 0 only
+        raise ValueError(f"a scene with joints or exclusions is timed as one world, not {sc.nworlds}")
     o = O.Oracle.from_scene(sc)
     if state is not None:
         o.set_state(np.ascontiguousarray(state, np.float32))

@@ -181,6 +181,8 @@ struct Engine {
     // memory, step through the grid-wide pipeline of r2d_large.cu on their
     // own stream while the fused classes run.
     static constexpr uint32_t FUSED_MAX_BODIES = 520;
+    // Largest spatial-hash table (table_mult x bodies) of one world.
+    static constexpr unsigned long long MAX_TABLE_BUCKETS = 1ull << 31;
     std::vector<uint8_t> world_large;                 // [nworlds] routed to the large path
     std::vector<uint32_t> large_list;                 // those worlds, in index order
     std::vector<std::unique_ptr<LargeWorld>> large;   // [nworlds] scratch of each large world
@@ -218,6 +220,7 @@ struct Engine {
     float g_dt = 0.f;
     uint32_t g_sub = 0, g_iters = 0;
     bool use_graph = true;
+    uint32_t colour_round_limit = 0;  // R2D_COLOUR_ROUND_LIMIT (0 = the colouring's own bound)
 
     ~Engine() {
         large.clear();
@@ -268,6 +271,10 @@ struct Engine {
         verbose = v && v[0] && v[0] != '0';
         const char* ng = getenv("R2D_NO_GRAPH");
         use_graph = !(ng && ng[0] && ng[0] != '0');
+        // Test hook: a small limit on the grid pipeline's colouring rounds
+        // makes its one bounded device loop give up (R2D_ERR_TIMEOUT).
+        const char* rl = getenv("R2D_COLOUR_ROUND_LIMIT");
+        colour_round_limit = rl ? (uint32_t)strtoul(rl, nullptr, 10) : 0u;
         CUDA_TRY(dalloc(d_call, 1));
         CUDA_TRY(dalloc(d_ext, 1));
         CUDA_TRY(cudaMemsetAsync(d_ext, 0, sizeof(ExtIO), stream));
@@ -282,6 +289,15 @@ struct Engine {
         const uint32_t n = body_off[nw];
         for (uint32_t w = 0; w < nw; ++w)
             if (body_off[w + 1] < body_off[w]) return fail(R2D_ERR_INVALID_ARGUMENT, "body_off not monotonic");
+        // the bucket count table_mult x n is 32-bit on the device: refuse a
+        // product that would wrap before anything is uploaded
+        for (uint32_t w = 0; w < nw; ++w) {
+            const unsigned long long T = (unsigned long long)table_mult * (body_off[w + 1] - body_off[w]);
+            if (T > MAX_TABLE_BUCKETS)
+                return fail(R2D_ERR_CAPACITY, "world " + std::to_string(w) + ": a spatial-hash table of " +
+                                                  std::to_string(T) + " buckets exceeds the maximum of " +
+                                                  std::to_string(MAX_TABLE_BUCKETS));
+        }
         uint32_t dup = 0;
         const int64_t dw = r2d_first_duplicate_id(nw, body_off, ids, &dup);
         if (dw >= 0)
@@ -572,7 +588,9 @@ struct Engine {
         c.np = sz(3.25 * nb + 32.0, 3);
         c.hs = c.np;
         c.nj = max_nj;
-        c.nt = table_mult * nb;
+        // a class bound times a large multiplier may pass 32 bits: such a
+        // layout cannot fit shared memory, and the world takes the grid pipeline
+        c.nt = (uint32_t)std::min<unsigned long long>((unsigned long long)table_mult * nb, 1ull << 28);
         return c;
     }
 
@@ -1022,6 +1040,7 @@ struct Engine {
         in.warm = warm_start();
         in.verbose = verbose;
         in.sleep = d_sleep ? d_sleep + w : nullptr;
+        in.colour_round_limit = colour_round_limit;
         return in;
     }
 

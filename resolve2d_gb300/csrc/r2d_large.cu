@@ -393,6 +393,9 @@ struct Colouring {
     uint32_t* npred;  // earlier neighbours of each constraint (null: rounds walk the adjacency)
     uint32_t* preds;  // their indices, PRED_ROW a constraint (those with more walk the adjacency)
     uint32_t* wl[2];  // worklists of the constraints a round left uncoloured (null: rounds scan all)
+    // Rounds allowed before the colouring gives up (LC_STUCK); 0 = count + 1,
+    // more than the count ever needs, since every round colours at least one.
+    uint32_t round_limit;
 
     __device__ void ends(uint32_t i, uint32_t* a, uint32_t* b) const {
         *a = NO_NODE;
@@ -597,6 +600,7 @@ __global__ void __launch_bounds__(CT, 1) lk_colour_cluster(Colouring C) {
     const bool listed = C.wl[0] != nullptr && C.npred != nullptr;
     uint32_t* cnt = C.cnt;
     uint32_t held = C.count > t0 ? (C.count - t0 - 1) / nt + 1 : 0u;  // constraints this thread holds
+    const uint32_t limit = C.round_limit ? C.round_limit : C.count + 1u;
     for (uint32_t round = 0;; ++round) {
         if (t0 == 0) cnt[LC_PEND0 + (round + 1) % 3] = 0u;
         bool open = false;
@@ -619,8 +623,9 @@ __global__ void __launch_bounds__(CT, 1) lk_colour_cluster(Colouring C) {
             if (t0 == 0) cnt[LC_ROUNDS] = round + 1;
             break;
         }
-        // each round colours at least the highest-priority uncoloured constraint
-        if (round >= C.count) {
+        // each round colours at least the highest-priority uncoloured
+        // constraint, so only a limit below the count can end here
+        if (round + 1u >= limit) {
             if (t0 == 0) cnt[LC_STUCK] = 1u;
             break;
         }
@@ -1675,6 +1680,7 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
         C.adj = adj; C.adjl = adjl; C.prio = prio; C.cursor = I.cursor; C.cnt = cnt;
         C.npred = npred; C.preds = preds;
         C.wl[0] = wl0; C.wl[1] = wl1;
+        C.round_limit = in.colour_round_limit;
         LTRY(cudaMemsetAsync(adj, 0, sizeof(uint32_t) * ((size_t)n + 1), st));
         LAUNCH(lk_col_count, blocks(count), C);
         SCAN(adj, n);
@@ -1719,8 +1725,8 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
             return DS_CAPACITY;
         }
         if (h[LC_STUCK]) {
-            *msg = "the colouring did not finish";
-            return -4;
+            *msg = "the colouring did not finish within its round limit";
+            return DS_TIMEOUT;
         }
         rounds[j] = h[LC_ROUNDS];
     }
@@ -2007,12 +2013,14 @@ int static_world_step(const StaticStepArgs& in, cudaStream_t st, std::string* ms
         *msg = std::to_string(n) + " bodies exceed the static-scratch maximum of " + std::to_string(SX_BODIES);
         return DS_CAPACITY;
     }
-    const uint32_t T = in.table_mult * n;
-    if (in.table_mult == 0 || T > SX_BUCKETS) {
-        *msg = "spatial-hash table of " + std::to_string(T) + " buckets exceeds the static-scratch maximum of " +
+    // table_mult x n in 64 bits: a product that wraps 32 bits must not pass the check
+    const unsigned long long T64 = (unsigned long long)in.table_mult * n;
+    if (T64 == 0 || T64 > SX_BUCKETS) {
+        *msg = "spatial-hash table of " + std::to_string(T64) + " buckets exceeds the static-scratch maximum of " +
                std::to_string(SX_BUCKETS);
         return DS_CAPACITY;
     }
+    const uint32_t T = (uint32_t)T64;
     unsigned char* base = nullptr;
     if (int r = static_scratch_address(&base, msg)) return r;
 #define SP(T_, field) reinterpret_cast<T_*>(base + SL.field)
@@ -2135,8 +2143,8 @@ int static_world_step(const StaticStepArgs& in, cudaStream_t st, std::string* ms
             return DS_CAPACITY;
         }
         if (h[LC_STUCK]) {
-            *msg = "the colouring did not finish";
-            return -4;
+            *msg = "the colouring did not finish within its round limit";
+            return DS_TIMEOUT;
         }
         ncol = h[LC_N];
     }

@@ -39,6 +39,7 @@ struct LargeInputs {
     bool warm;             // warm starting (the world keeps its impulses across calls)
     bool verbose;          // print each step's phase times and counts to stderr
     uint32_t* sleep;       // this world's still-frame counter (sleeping mode, r2d_sleep.h), else null
+    uint32_t colour_round_limit;  // colouring rounds before R2D_ERR_TIMEOUT (0 = never reached)
 };
 
 class LargeWorld {

@@ -3,7 +3,7 @@
  * CUDA kernels and the CPU oracle so that both see the same rotation values.
  *
  * The reference rotates every vector through nmath.rotate2
- * (src/core/nmath.zig:367-374), which calls Zig's std.math.cos / std.math.sin
+ * (src/core/nmath.zig:129-136), which calls Zig's std.math.cos / std.math.sin
  * on an f32 angle.  Those come from the toolchain's libm, so the engine's
  * results depend on one transcendental implementation; the broadphase AABBs,
  * SAT axes, projections and contact points of every rectangle go through it.

@@ -233,6 +233,7 @@ enum CapBits : uint32_t {
 enum DeviceStatus : int {
     DS_OK = 0,
     DS_CAPACITY = -5,
+    DS_TIMEOUT = -6,   // a bounded device-side loop gave up (R2D_ERR_TIMEOUT)
     DS_NONFINITE = -7,
 };
 

@@ -83,6 +83,20 @@ def test_static_step_refuses_bad_arguments_before_launching():
     assert "sub_steps" in last_error(lib)
 
 
+def test_static_step_refuses_a_table_size_that_wraps_32_bits():
+    # 4,096 bodies x 2^20 = 2^32 buckets: 0 in 32-bit arithmetic.  The check
+    # runs in 64 bits, before the device is touched (the buffers are never read).
+    lib = N.load()
+    f = (C.c_float * 16)()
+    u8 = (C.c_uint8 * 4)()
+    u32 = (C.c_uint32 * 4)()
+    for mult in (1 << 20, (1 << 32) - 1, 3):
+        rc = lib.r2d_world_step_static(C.cast(f, N._f32p), C.cast(f, N._f32p), C.cast(u8, N._u8p),
+                                       C.cast(u32, N._u32p), 4096, None, 0, 1.0 / 60.0, 1, 8, 0.0, mult, None)
+        assert rc == -5, mult
+        assert "buckets exceeds" in last_error(lib)
+
+
 def test_scene_shapes_the_handles_refuse_before_any_device_work():
     from resolve2d_gb300 import scenes
     from resolve2d_gb300.engine import Batch, World
