@@ -92,7 +92,7 @@ enum { R2D_JOINT_PARAMS = 8 };
 enum { R2D_MANIFOLD_FLOATS = 33 };
 
 enum {
-    R2D_FLAG_DEBUG_TAPS = 1u, /* keep manifolds and colours for r2d_*_get_manifolds */
+    R2D_FLAG_DEBUG_TAPS = 1u, /* keep manifolds, colours and candidate pairs for r2d_*_get_manifolds / _get_pairs */
     /* Step every world through the grid-wide pipeline that worlds above 520
      * bodies always use (global scratch, one kernel per phase and colour)
      * instead of the fused one-CTA-per-world kernel.  Same results. */
@@ -208,6 +208,13 @@ R2D_API int r2d_solver_get_manifolds(r2d_solver* s, uint32_t cap, uint32_t* keys
 /* Debug taps: the colour of each of the first `cap` joints, in insertion order,
  * from the last frame (the solve runs joint colours in ascending order). */
 R2D_API int r2d_solver_get_joint_colours(r2d_solver* s, uint32_t cap, uint32_t* colours);
+/* Debug taps: the last frame's candidate pairs, the pairs that reach SAT in
+ * Solver.updateManifolds (src/core/lib.zig:264-282): two bodies sharing a
+ * spatial-hash bucket, not both static, not excluded, AABBs intersecting.
+ * pairs [cap][2] are (lower, higher) body indices in the store's order,
+ * sorted ascending; each pair once. */
+R2D_API int r2d_solver_num_pairs(r2d_solver* s, uint32_t* out);
+R2D_API int r2d_solver_get_pairs(r2d_solver* s, uint32_t cap, uint32_t* pairs);
 
 /* ---------------------------------------------------------------------------
  * Many independent worlds stepped by one launch per kernel class.  No
@@ -256,6 +263,9 @@ R2D_API int r2d_batch_world_status(r2d_batch* b, int* status);
 R2D_API int r2d_batch_num_manifolds(r2d_batch* b, uint32_t w, uint32_t* out);
 R2D_API int r2d_batch_get_manifolds(r2d_batch* b, uint32_t w, uint32_t cap, uint32_t* keys, float* data,
                                     uint32_t* colours);
+/* The candidate pairs of world w (see the solver's), world-local indices. */
+R2D_API int r2d_batch_num_pairs(r2d_batch* b, uint32_t w, uint32_t* out);
+R2D_API int r2d_batch_get_pairs(r2d_batch* b, uint32_t w, uint32_t cap, uint32_t* pairs);
 
 /* ---------------------------------------------------------------------------
  * One world stepped with no allocation.  No counterpart in the reference.

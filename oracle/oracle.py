@@ -46,6 +46,8 @@ _SIG = {
     "r2o_num_manifolds": ([_P], C.c_uint32),
     "r2o_get_manifolds": ([_P, _u32p, _f32p], None),
     "r2o_get_colours": ([_P, C.c_uint32, _u32p, C.c_uint32, _u32p], C.c_uint32),
+    "r2o_set_record_pairs": ([_P, C.c_int], None),
+    "r2o_get_pairs": ([_P, C.c_uint32, _u32p], C.c_uint32),
     "r2o_nmath_kat": ([_f32p, _f32p, _f32p], None),
     "r2o_aabb_intersects": ([C.c_float] * 8, C.c_int),
     "r2o_sincosf": ([C.c_uint32, _f32p, _f32p, _f32p], None),
@@ -179,6 +181,19 @@ class Oracle:
         d = np.zeros((m, MF), np.float32)
         self.lib.r2o_get_manifolds(self.h, _p(k, C.c_uint32), _p(d, C.c_float))
         return k, d
+
+    def record_pairs(self, on: bool = True):
+        """Keep each narrowphase's candidate pairs (see pairs)."""
+        self.lib.r2o_set_record_pairs(self.h, int(bool(on)))
+
+    def pairs(self) -> np.ndarray:
+        """The pairs the last narrowphase passed to performNarrowSAT
+        (lib.zig:264-284): [k][2] (lower, higher) body indices, sorted."""
+        n = int(self.lib.r2o_get_pairs(self.h, 0, None))
+        out = np.zeros((n, 2), np.uint32)
+        if n:
+            self.lib.r2o_get_pairs(self.h, n, _p(out, C.c_uint32))
+        return out
 
     def colours(self):
         m = int(self.lib.r2o_num_manifolds(self.h))

@@ -313,6 +313,25 @@ void r2o_get_manifolds(void* hp, uint32_t* keys, float* data) {
     DISPATCH(h, get_manifolds(S, keys, data));
 }
 
+/* Candidate pairs of the last narrowphase (recorded once enabled): (lower,
+ * higher) body indices, sorted; at most cap pairs written, count returned. */
+void r2o_set_record_pairs(void* hp, int on) {
+    Handle* h = (Handle*)hp;
+    DISPATCH(h, S.record_pairs = on != 0);
+}
+
+uint32_t r2o_get_pairs(void* hp, uint32_t cap, uint32_t* out) {
+    Handle* h = (Handle*)hp;
+    uint32_t n = 0;
+    DISPATCH(h, (n = (uint32_t)S.candidate_pairs.size(), [&] {
+                     for (uint32_t q = 0; q < n && q < cap; ++q) {
+                         out[2 * q] = (uint32_t)(S.candidate_pairs[q] >> 32);
+                         out[2 * q + 1] = (uint32_t)S.candidate_pairs[q];
+                     }
+                 }()));
+    return n;
+}
+
 /* Colours of the manifolds (discovery order) and joints (insertion order)
  * from the last colouring; at most ncap / jcap entries are written.
  * Returns the number of manifold colours available. */

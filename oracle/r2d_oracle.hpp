@@ -565,6 +565,11 @@ public:
     std::unordered_set<uint64_t> exclude_collision_pairs;
     std::vector<std::pair<Key, Manifold<R>>> manifolds;  // discovery order
     std::unordered_set<uint64_t> manifold_keys;
+    // A checking aid: with record_pairs set, update_manifolds keeps every
+    // pair that reaches performNarrowSAT (lib.zig:282-284) as (lower, higher)
+    // body indices, sorted and unique.  Off, it records nothing.
+    bool record_pairs = false;
+    std::vector<uint64_t> candidate_pairs;
     R cell_size = R(4);        // lib.zig:255 hard-codes 4.0
     size_t table_mult = 2;     // lib.zig:255 hard-codes 2 * bodies.count()
 
@@ -722,6 +727,7 @@ public:
         manifold_keys.clear();
         contact_colour.clear();
         contact_order.clear();
+        candidate_pairs.clear();
         if (n == 0) return OK;
 
         // SpatialHash.init (SpatialHash.zig:19-71)
@@ -778,6 +784,7 @@ public:
                 if (manifold_keys.count(pair_key(b1, b2))) continue;
                 if (manifold_keys.count(pair_key(b2, b1))) continue;
                 if (!body1.aabb.intersects(body2.aabb)) continue;
+                if (record_pairs) candidate_pairs.push_back(pair_key(std::min(b1, b2), std::max(b1, b2)));
                 SATResult<R> sat = perform_narrow_sat(b1, b2);
                 if (!sat.collides) continue;
                 Manifold<R> m;
@@ -789,6 +796,10 @@ public:
                 manifolds.push_back({Key{sat.ref, sat.inc}, m});
                 manifold_keys.insert(pair_key(sat.ref, sat.inc));
             }
+        }
+        if (record_pairs) {
+            std::sort(candidate_pairs.begin(), candidate_pairs.end());
+            candidate_pairs.erase(std::unique(candidate_pairs.begin(), candidate_pairs.end()), candidate_pairs.end());
         }
         return OK;
     }

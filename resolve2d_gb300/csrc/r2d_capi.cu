@@ -156,6 +156,8 @@ struct Engine {
     float* d_dbg_data = nullptr;
     uint32_t* d_dbg_col = nullptr;
     uint32_t* d_dbg_jcol = nullptr;
+    uint32_t* d_dbg_npairs = nullptr;
+    uint32_t* d_dbg_pairs = nullptr;
 
     std::vector<int> status_h;
     bool pending = false;
@@ -235,6 +237,7 @@ struct Engine {
         dfree(d_jtype); dfree(d_jb1); dfree(d_jb2); dfree(d_jprm); dfree(d_excl);
         for (auto& c : classes) dfree(c.d_list);
         dfree(d_dbg_nman); dfree(d_dbg_keys); dfree(d_dbg_data); dfree(d_dbg_col); dfree(d_dbg_jcol);
+        dfree(d_dbg_npairs); dfree(d_dbg_pairs);
         dfree(d_fail_call); dfree(d_one); dfree(d_capbits); dfree(d_timers);
         for (int a = 0; a < NAUX; ++a) {
             if (aux[a]) cudaStreamDestroy(aux[a]);
@@ -852,11 +855,18 @@ struct Engine {
         // debug taps
         dbg = DebugOut{};
         if (cfg.flags & R2D_FLAG_DEBUG_TAPS) {
-            uint32_t cap = 0, jcap = 0;
+            uint32_t cap = 0, jcap = 0, pcap = 0;
             for (auto& c : classes) {
                 cap = std::max(cap, c.caps.nm);
                 jcap = std::max(jcap, c.caps.nj);
+                pcap = std::max(pcap, c.caps.np);
             }
+            CUDA_TRY(dalloc(d_dbg_npairs, nworlds));
+            CUDA_TRY(dalloc(d_dbg_pairs, (size_t)nworlds * (pcap ? pcap : 1) * 2));
+            CUDA_TRY(cudaMemsetAsync(d_dbg_npairs, 0, 4 * nworlds, stream));
+            dbg.pcap = pcap;
+            dbg.npairs = d_dbg_npairs;
+            dbg.pairs = d_dbg_pairs;
             CUDA_TRY(dalloc(d_dbg_nman, nworlds));
             CUDA_TRY(dalloc(d_dbg_keys, (size_t)nworlds * cap * 2));
             CUDA_TRY(dalloc(d_dbg_data, (size_t)nworlds * cap * DEBUG_MF));
@@ -1345,6 +1355,45 @@ struct Engine {
         return R2D_OK;
     }
 
+    int num_pairs(uint32_t w, uint32_t* out) {
+        if (!debug_taps()) return fail(R2D_ERR_INVALID_ARGUMENT, "debug taps are off (R2D_FLAG_DEBUG_TAPS)");
+        if (w >= nworlds) return fail(R2D_ERR_INVALID_ARGUMENT, "world index out of range");
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        if (world_large[w]) {
+            *out = large[w] ? large[w]->num_pairs() : 0u;
+            return R2D_OK;
+        }
+        CUDA_TRY(cudaMemcpy(out, d_dbg_npairs + w, 4, cudaMemcpyDeviceToHost));
+        return R2D_OK;
+    }
+
+    // The last frame's candidate pairs of world w, (lower, higher) world-local
+    // body indices, sorted ascending (the device finds them in no fixed order).
+    int get_pairs(uint32_t w, uint32_t cap, uint32_t* out) {
+        uint32_t m = 0;
+        if (int st = num_pairs(w, &m)) return st;
+        if (world_large[w]) {
+            m = std::min(m, cap);
+            if (large[w] && m) {
+                std::string msg;
+                if (const int r = large[w]->dump_pairs(m, out, stream, &msg)) return fail(r, msg);
+            }
+        } else {
+            m = std::min(m, std::min(cap, dbg.pcap));
+            if (m)
+                CUDA_TRY(cudaMemcpy(out, d_dbg_pairs + 2 * (size_t)w * dbg.pcap, 8 * (size_t)m,
+                                    cudaMemcpyDeviceToHost));
+        }
+        std::vector<unsigned long long> k(m);
+        for (uint32_t q = 0; q < m; ++q) k[q] = ((unsigned long long)out[2 * q] << 32) | out[2 * q + 1];
+        std::sort(k.begin(), k.end());
+        for (uint32_t q = 0; q < m; ++q) {
+            out[2 * q] = (uint32_t)(k[q] >> 32);
+            out[2 * q + 1] = (uint32_t)k[q];
+        }
+        return R2D_OK;
+    }
+
     int get_joint_colours(uint32_t w, uint32_t cap, uint32_t* colours) {
         if (!debug_taps()) return fail(R2D_ERR_INVALID_ARGUMENT, "debug taps are off (R2D_FLAG_DEBUG_TAPS)");
         if (w >= nworlds) return fail(R2D_ERR_INVALID_ARGUMENT, "world index out of range");
@@ -1563,6 +1612,16 @@ R2D_API int r2d_solver_read_positions_f64(r2d_solver* s, double* pose) {
     return guarded([&] { return s->eng.read_pose64(pose); });
 }
 
+R2D_API int r2d_solver_num_pairs(r2d_solver* s, uint32_t* out) {
+    if (!s || !out) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL handle or out pointer");
+    return guarded([&] { return s->eng.num_pairs(0, out); });
+}
+
+R2D_API int r2d_solver_get_pairs(r2d_solver* s, uint32_t cap, uint32_t* pairs) {
+    if (!s || (cap && !pairs)) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL handle or pairs buffer");
+    return guarded([&] { return s->eng.get_pairs(0, cap, pairs); });
+}
+
 R2D_API int r2d_solver_get_joint_colours(r2d_solver* s, uint32_t cap, uint32_t* colours) {
     if (!s || !colours) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL argument");
     return guarded([&] { return s->eng.get_joint_colours(0, cap, colours); });
@@ -1712,6 +1771,16 @@ R2D_API int r2d_batch_get_manifolds(r2d_batch* b, uint32_t w, uint32_t cap, uint
                                     uint32_t* colours) {
     if (!b) return fail(R2D_ERR_INVALID_ARGUMENT, "batch is NULL");
     return guarded([&] { return b->eng.get_manifolds(w, cap, keys, data, colours); });
+}
+
+R2D_API int r2d_batch_num_pairs(r2d_batch* b, uint32_t w, uint32_t* out) {
+    if (!b || !out) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL handle or out pointer");
+    return guarded([&] { return b->eng.num_pairs(w, out); });
+}
+
+R2D_API int r2d_batch_get_pairs(r2d_batch* b, uint32_t w, uint32_t cap, uint32_t* pairs) {
+    if (!b || (cap && !pairs)) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL handle or pairs buffer");
+    return guarded([&] { return b->eng.get_pairs(w, cap, pairs); });
 }
 
 // The allocation-free world step: validation here, the pipeline over the

@@ -1453,7 +1453,7 @@ struct LargeWorld::Impl {
     int wcur = 0;
 
     double pair_scale = 1.0;  // grows when the candidate-pair set overflows
-    uint32_t nman = 0, nj = 0, nlaunch = 0;
+    uint32_t nman = 0, nj = 0, nlaunch = 0, npairs = 0;
     std::vector<uint32_t> coff, joff;
 
     ~Impl() {
@@ -1549,6 +1549,7 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
     I.nman = 0;
     I.nj = 0;
     I.nlaunch = 0;
+    I.npairs = 0;
     I.coff.assign(1, 0u);
     I.joff.assign(1, 0u);
     if (n == 0) return 0;
@@ -1642,6 +1643,7 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
                  LB(I.apn), LB(I.apt), LB(I.bias), LB(I.r1x2), LB(I.r1y2), LB(I.r2x2), LB(I.r2y2), LB(I.depth2),
                  LB(I.odepth2), LB(I.apn2), LB(I.apt2)}));
     A.s = I.views(in);
+    I.npairs = npairs;
     A.nm = npairs;
     A.npt = 2 * npairs;
     LTRY(cudaMemsetAsync(I.cnt, 0, sizeof(uint32_t) * LC_N, st));
@@ -1880,6 +1882,28 @@ int LargeWorld::dump(uint32_t cap, uint32_t* keys, float* data, uint32_t* colour
     if (keys) LTRY(cudaMemcpy(keys, I.dk, 8ull * m, cudaMemcpyDeviceToHost));
     if (data) LTRY(cudaMemcpy(data, I.dd, sizeof(float) * DEBUG_MF * (size_t)m, cudaMemcpyDeviceToHost));
     if (colours) LTRY(cudaMemcpy(colours, I.dc, 4ull * m, cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+uint32_t LargeWorld::num_pairs() const { return impl->npairs; }
+
+// the 64-bit (lower << 32 | higher) pair keys as two 32-bit indices each
+__global__ void lk_split_pairs(const unsigned long long* keys, uint32_t n, uint32_t* out) {
+    const uint32_t i = blockIdx.x * LT + threadIdx.x;
+    if (i >= n) return;
+    const unsigned long long k = keys[i];
+    out[2 * i] = (uint32_t)(k >> 32);
+    out[2 * i + 1] = (uint32_t)k;
+}
+
+int LargeWorld::dump_pairs(uint32_t cap, uint32_t* pairs, cudaStream_t st, std::string* msg) {
+    Impl& I = *impl;
+    const uint32_t m = std::min(cap, I.npairs);
+    if (m == 0) return 0;
+    LTRY(regrow(I.cap_d, 2 * (size_t)m, {LB(I.dk), LB(I.dc)}));
+    lk_split_pairs<<<blocks(m), LT, 0, st>>>(I.pairs, m, I.dk);
+    LTRY(cudaStreamSynchronize(st));
+    LTRY(cudaMemcpy(pairs, I.dk, 8ull * m, cudaMemcpyDeviceToHost));
     return 0;
 }
 

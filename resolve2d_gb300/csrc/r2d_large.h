@@ -56,6 +56,10 @@ public:
     uint32_t num_manifolds() const;
     int dump(uint32_t cap, uint32_t* keys, float* data, uint32_t* colours, cudaStream_t st, std::string* msg);
     int joint_colours(uint32_t cap, uint32_t* colours, cudaStream_t st, std::string* msg);
+    // Candidate pairs of the last step (debug tap): (lower, higher) world-local
+    // indices [min(cap, count)][2], in no particular order.
+    uint32_t num_pairs() const;
+    int dump_pairs(uint32_t cap, uint32_t* pairs, cudaStream_t st, std::string* msg);
     // Kernel launches of the last step.
     uint32_t launches() const;
     // Warm starting: take over another table of last frame's impulses

@@ -173,6 +173,11 @@ struct DebugOut {
     uint32_t* colour;    // [world][cap]
     uint32_t* jcolour;   // [world][jcap]
     uint32_t jcap;
+    // candidate pairs: the pairs that reach the narrowphase (every filter of
+    // updateManifolds passed, lib.zig:264-282), in no particular order
+    uint32_t pcap;       // pairs per world slot
+    uint32_t* npairs;    // [world]
+    uint32_t* pairs;     // [world][pcap][2]  (lower, higher) world-local indices
 };
 
 // Host rows a frame call reads and writes directly over the coherent

@@ -615,6 +615,16 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
         SUBPHASE(17);
     }
     __syncthreads();
+    if (P.dbg.pcap) {  // debug tap: the candidate pairs, before the narrowphase reuses nothing of them
+        const uint32_t found = s_cnt[0];
+        if (tid == 0) P.dbg.npairs[w] = found;
+        uint32_t* out = P.dbg.pairs + 2 * (size_t)w * P.dbg.pcap;
+        for (uint32_t q = tid; q < found && q < P.dbg.pcap; q += NT) {
+            const uint32_t key = pairs[q];
+            out[2 * q] = key >> 16;
+            out[2 * q + 1] = key & 0xFFFFu;
+        }
+    }
 
     PHASE(1);
     // ---------------- narrowphase (collision.zig:299-320, lib.zig:284-294) ----------------

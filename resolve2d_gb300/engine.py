@@ -164,6 +164,15 @@ class World:
                 "r2d_solver_read_positions_f64")
         return out
 
+    def pairs(self) -> np.ndarray:
+        """The last frame's candidate pairs [k][2] (lower, higher body index),
+        sorted: the pairs that reached the narrowphase."""
+        m = C.c_uint32()
+        N.check(self._lib.r2d_solver_num_pairs(self._h, C.byref(m)), "r2d_solver_num_pairs")
+        out = np.zeros((m.value, 2), np.uint32)
+        N.check(self._lib.r2d_solver_get_pairs(self._h, m.value, N.ptr(out, C.c_uint32)), "r2d_solver_get_pairs")
+        return out
+
     def joint_colours(self, nj: int):
         c = np.zeros(nj, np.uint32)
         N.check(self._lib.r2d_solver_get_joint_colours(self._h, nj, N.ptr(c, C.c_uint32)), "r2d_solver_get_joint_colours")
@@ -285,3 +294,11 @@ class Batch:
         N.check(self._lib.r2d_batch_get_manifolds(self._h, w, m.value, N.ptr(k, C.c_uint32), N.ptr(d, C.c_float),
                                                   N.ptr(c, C.c_uint32)), "r2d_batch_get_manifolds")
         return k, d, c
+
+    def pairs(self, w: int) -> np.ndarray:
+        """World w's candidate pairs of the last frame (see World.pairs)."""
+        m = C.c_uint32()
+        N.check(self._lib.r2d_batch_num_pairs(self._h, w, C.byref(m)), "r2d_batch_num_pairs")
+        out = np.zeros((m.value, 2), np.uint32)
+        N.check(self._lib.r2d_batch_get_pairs(self._h, w, m.value, N.ptr(out, C.c_uint32)), "r2d_batch_get_pairs")
+        return out

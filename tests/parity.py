@@ -63,6 +63,16 @@ def assert_manifolds_equal(gk, gd, gc, ok, od, oc):
         assert cg == co, f"manifold {k}: colour gpu {cg} oracle {co}"
 
 
+def assert_pairs_equal(got: np.ndarray, want: np.ndarray, what: str = "pairs"):
+    """Candidate pair sets (the pairs that reached the narrowphase), both
+    sorted (lower, higher) index rows: identical, each pair once."""
+    g = set(map(tuple, np.asarray(got).tolist()))
+    o = set(map(tuple, np.asarray(want).tolist()))
+    assert len(g) == len(got), f"{what}: the GPU reported a pair twice"
+    assert g == o, f"{what}: gpu-only {sorted(g - o)[:5]} oracle-only {sorted(o - g)[:5]}"
+    np.testing.assert_array_equal(np.asarray(got, np.uint32).reshape(-1, 2), np.asarray(want, np.uint32).reshape(-1, 2))
+
+
 def run_pair(sc, steps, check_every=1, debug=True, sub_steps=None, iters=None, warm=False, **world_kw):
     """Step scene `sc` on the GPU (one world through the C ABI) and on the
     oracle in colour-major order; compare state, manifolds and colours every
@@ -77,6 +87,7 @@ def run_pair(sc, steps, check_every=1, debug=True, sub_steps=None, iters=None, w
     w = World.from_scene(sc, debug=debug, warm_start=warm, **world_kw)
     o = Oracle.from_scene(sc)
     o.set_warm_start(warm)
+    o.record_pairs(debug)
     assert_state_equal(w.read_state(), o.state(), "initial state")
     for s in range(steps):
         want = o.process(sc.dt, S, I, ORDER_COLOUR)
@@ -94,6 +105,7 @@ def run_pair(sc, steps, check_every=1, debug=True, sub_steps=None, iters=None, w
         if (s + 1) % check_every == 0 or s + 1 == steps:
             assert_state_equal(w.read_state(), o.state(), f"{sc.name} step {s + 1}")
             if debug:
+                assert_pairs_equal(w.pairs(), o.pairs(), f"{sc.name} step {s + 1}")
                 gk, gd, gc = w.manifolds()
                 ok, od = o.manifolds()
                 oc, _ = o.colours()

@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 from oracle import ORDER_COLOUR, Oracle
-from parity import assert_manifolds_equal, assert_state_equal, run_pair
+from parity import assert_manifolds_equal, assert_pairs_equal, assert_state_equal, run_pair
 from resolve2d_gb300 import _native as N
 from resolve2d_gb300 import scenes
 from resolve2d_gb300.engine import Batch, World
@@ -46,6 +46,8 @@ def test_batch_matches_oracle_per_world():
     sc = scenes.batched_worlds("batch-small", seed=3, nworlds=24, steps=40, lo=16, hi=512)
     b = Batch.from_scene(sc, debug=True)
     oracles = [Oracle.from_scene(sc.world(w)) for w in range(sc.nworlds)]
+    for o in oracles:
+        o.record_pairs()
     for s in range(sc.steps):
         b.process(sc.dt, sc.sub_steps, sc.iters)
         b.sync()
@@ -55,6 +57,7 @@ def test_batch_matches_oracle_per_world():
     for w, o in enumerate(oracles):
         b0, b1 = sc.body_off[w], sc.body_off[w + 1]
         assert_state_equal(st[:, b0:b1], o.state(), f"world {w}")
+        assert_pairs_equal(b.pairs(w), o.pairs(), f"world {w}")
         gk, gd, gc = b.manifolds(w)
         ok, od = o.manifolds()
         oc, _ = o.colours()
@@ -246,16 +249,46 @@ def test_pairs_across_cell_boundaries_with_and_without_bucket_collisions(grid):
     w = World.from_scene(sc, debug=True, mult=mult, grid=grid)
     o = Oracle.from_scene(sc)
     o.set_hash(4.0, mult)
+    o.record_pairs()
     for s in range(2):
         assert o.process(sc.dt, 1, 8, ORDER_COLOUR) == 0
         w.process(sc.dt, 1, 8)
         w.sync()
         assert_state_equal(w.read_state(), o.state(), f"boundary step {s + 1}")
+        assert_pairs_equal(w.pairs(), o.pairs(), f"boundary step {s + 1}")
         gk, gd, gc = w.manifolds()
         ok, od = o.manifolds()
         oc, _ = o.colours()
         assert_manifolds_equal(gk, gd, gc, ok, od, oc)
     assert len(ok) == n_pairs // 2  # only the colliding rows pair up
+    assert len(o.pairs()) == n_pairs // 2  # the other rows share no bucket: not even candidates
+
+
+@pytest.mark.parametrize("grid", [False, True])
+def test_candidate_pairs_include_aabb_overlaps_that_sat_rejects(grid):
+    # Discs of radius 0.5 on a checkerboard of 0.8 spacing: every
+    # diagonal neighbour's AABB overlaps (|dx| = 0.8 < 1.01) while the discs
+    # are 1.13 apart, so SAT rejects them.  Those pairs reach the narrowphase
+    # (lib.zig:282-284) without making a manifold; the tap must list them.
+    # Two discs excluded from colliding and two static boxes that overlap
+    # each other must not appear.
+    b = scenes._Builder()
+    for i in range(8):
+        for j in range(8):
+            if (i + j) % 2 == 0:  # a checkerboard: only diagonal neighbours' AABBs overlap
+                b.disc(0.8 * i, 0.8 * j + 1.0, 0.5, 0.5)
+    b.rect(2.0, -0.5, 20.0, 1.0, 0.5, static=True)
+    b.rect(2.5, -0.5, 20.0, 1.0, 0.5, static=True)
+    ids, kind, opt = b.arrays()
+    sc = scenes._concat("diagonal", [(ids, kind, opt)], [0.0], 1 / 60, 1, 8, 1,
+                        excl=(np.zeros(1, np.uint32), np.array([[ids[0], ids[4]]], np.uint32)))
+    w, o = run_pair(sc, steps=1, grid=grid)
+    pairs = set(map(tuple, w.pairs().tolist()))
+    keys = {tuple(sorted(k)) for k in w.manifolds()[0].tolist()}
+    assert keys < pairs and len(pairs - keys) >= 40
+    assert (0, 4) not in pairs  # diagonal neighbours, excluded
+    nb = len(ids)
+    assert (nb - 2, nb - 1) not in pairs
 
 
 @pytest.mark.parametrize("grid", [False, True])

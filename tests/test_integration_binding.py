@@ -1,4 +1,5 @@
-"""The Zig binding written out in INTEGRATION.md agrees with include/r2d_gb300.h.
+"""The Zig binding (zig/r2d.zig) agrees with include/r2d_gb300.h, and the C
+example (examples/frame_loop.c) compiles and links against the library.
 
 Each `pub extern "r2d_gb300" fn` there must name an entry point the header
 declares, with the same parameters in the same order (pointer depth, constness
@@ -54,9 +55,7 @@ def header_decls():
 
 
 def zig_block():
-    text = Path(REPO, "INTEGRATION.md").read_text()
-    blocks = re.findall(r"```zig\n(.*?)```", text, flags=re.S)
-    return next(b for b in blocks if 'pub extern "r2d_gb300"' in b)
+    return Path(REPO, "zig", "r2d.zig").read_text()
 
 
 def zig_decls():
@@ -100,24 +99,16 @@ def test_status_codes_agree():
 
 
 def test_the_c_example_compiles_and_links(tmp_path):
-    """The C example of the guide, wrapped in a function that supplies its
-    arrays, compiles as C99 against the header and links against the library."""
+    """examples/frame_loop.c compiles as C99 against the header and links
+    against the library."""
     import shutil
     import subprocess
 
     cc = shutil.which("gcc")
     if cc is None:
         pytest.skip("no gcc")
-    text = Path(REPO, "INTEGRATION.md").read_text()
-    block = next(b for b in re.findall(r"```c\n(.*?)```", text, flags=re.S) if "r2d_solver_create" in b)
-    body = "\n".join(line for line in block.splitlines() if not line.startswith("#include"))
     src = tmp_path / "example.c"
-    src.write_text(
-        '#include <stdio.h>\n#include "r2d_gb300.h"\n'
-        "int run(uint32_t n, const uint32_t* ids, const uint8_t* kind, const float* props, float* state) {\n"
-        f"{body}\n    return st;\n}}\n"
-        "int main(void) { return 0; }\n"
-    )
+    src.write_text(Path(REPO, "examples", "frame_loop.c").read_text() + "\nint main(void) { return 0; }\n")
     lib_dir = str(Path(N.LIB_PATH).parent)
     r = subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-I", str(Path(REPO, "include")), str(src),
                         "-o", str(tmp_path / "example"), "-L", lib_dir, "-lr2d_gb300", f"-Wl,-rpath,{lib_dir}"],

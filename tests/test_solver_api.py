@@ -292,17 +292,16 @@ def test_the_default_engine_is_the_gpu_library():
     assert e.value.code == -8
 
 
-def test_the_integration_guide_example_runs(monkeypatch):
-    """The reference-style example in INTEGRATION.md runs as written (engine
-    replaced by the oracle stand-in), and the disc it follows falls onto the ground."""
-    import re
+def test_the_solver_scene_example_runs(monkeypatch):
+    """examples/solver_scene.py, a scene written against the reference's API,
+    runs as written (engine replaced by the oracle stand-in), and the disc it
+    follows falls onto the ground."""
     from pathlib import Path
 
     from conftest import REPO
     import resolve2d_gb300.solver as mod
 
-    text = Path(REPO, "INTEGRATION.md").read_text()
-    block = next(b for b in re.findall(r"```python\n(.*?)```", text, flags=re.S) if "Solver.init(" in b)
+    block = Path(REPO, "examples", "solver_scene.py").read_text()
 
     class OracleSolver(mod.Solver):
         def __init__(self, *a, **kw):
