@@ -171,18 +171,6 @@ def test_overflowing_pile_moves_to_grid_pipeline():
     run_pair(sc, steps=4, check_every=1)
 
 
-def test_config1_pyramid_first_steps():
-    sc = scenes.config1()
-    run_pair(sc, steps=40, check_every=20, debug=False)
-
-
-def test_config2_chains_and_motors_first_steps():
-    sc = scenes.config2()
-    w, o = run_pair(sc, steps=6, check_every=3)
-    _, oj = o.colours()
-    np.testing.assert_array_equal(w.joint_colours(len(sc.jtype)), oj)
-
-
 def test_new_joints_midrun_are_recoloured():
     """A grid-pipeline world keeps its joint colouring from step to step; new
     joints (here the same joints in reverse insertion order, which changes their
