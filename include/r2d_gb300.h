@@ -104,12 +104,15 @@ enum {
      * drift over long horizons (r2d_*_read_positions_f64 reads the pose). */
     R2D_FLAG_FP64_POSITIONS = 4u,
     /* Warm starting (no counterpart in the reference, whose manifolds are
-     * cleared every frame, src/core/lib.zig:261): a manifold whose
-     * (reference, incident) pair had one last frame starts from last frame's
-     * accumulated impulses, applied to the bodies after the first substep's
-     * preStep; and since such a sum must be able to shrink, impulses below
-     * the reference's 1e-4 skip threshold are applied (clamped at zero)
-     * instead of skipped. */
+     * cleared every frame, src/core/lib.zig:261; its roadmap asks for it,
+     * README.md:60-61): a manifold whose (reference, incident) pair of body
+     * ids had one last frame starts from last frame's accumulated impulses,
+     * applied to the bodies after the first substep's preStep; and since
+     * such a sum must be able to shrink, impulses below the reference's
+     * 1e-4 skip threshold are applied (clamped at zero) instead of skipped.
+     * The impulses are keyed by the stable body ids, so they survive
+     * r2d_*_set_bodies / set_worlds: pairs whose two ids are still in the
+     * world (world w of a batch keeps world w's) start warm. */
     R2D_FLAG_WARM_START = 8u,
     /* Sleeping (no counterpart in the reference; its roadmap lists it,
      * README.md:64-67): a world whose every non-static body ends 60
@@ -117,7 +120,15 @@ enum {
      * stepped again until the host writes to the engine (state, fields,
      * bodies, gravity, joints or exclusions), which wakes every world.
      * r2d_*_sleep_frames reads the per-world counters. */
-    R2D_FLAG_SLEEP = 16u
+    R2D_FLAG_SLEEP = 16u,
+    /* Compensated (Kahan) accumulation of each contact point's normal and
+     * tangent impulse sums (no counterpart in the reference, which adds them
+     * in plain f32, src/core/collision.zig:182-190): the rounding remainder of
+     * every addition is kept in a second word and carried into later ones;
+     * the bodies receive the changes of the rounded sum, as in the reference.
+     * With R2D_FLAG_WARM_START the remainders travel with the sums from
+     * frame to frame. */
+    R2D_FLAG_COMPENSATED = 32u
 };
 
 typedef struct r2d_config {

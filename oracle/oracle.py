@@ -33,6 +33,9 @@ _SIG = {
     "r2o_add_joints": ([_P, C.c_uint32, _u8p, _u32p, _u32p, _f32p], None),
     "r2o_set_hash_config": ([_P, C.c_float, C.c_uint32], None),
     "r2o_set_warm_start": ([_P, C.c_int], None),
+    "r2o_set_compensated": ([_P, C.c_int], None),
+    "r2o_acc_sum": ([C.c_uint32, _f32p, C.c_float, C.c_float, C.c_float, _f32p], None),
+    "r2o_copy_warm": ([_P, _P], C.c_int),
     "r2o_set_sleep": ([_P, C.c_int], None),
     "r2o_set_phase_timing": ([_P, C.c_int], None),
     "r2o_phase_seconds": ([_P, _f64p], None),
@@ -132,6 +135,40 @@ class Oracle:
         """Warm starting (off in reference mode): manifolds found again start
         from last frame's accumulated impulses."""
         self.lib.r2o_set_warm_start(self.h, int(bool(on)))
+
+    def add_bodies_raw(self, ids, kind, props, state):
+        """Appends bodies given as an engine takes them: ids, kind bits
+        (rectangle 1, static 2), props [5][n] (mass, inertia, mu, dims) and a
+        full state [13][n], AABBs included.  The oracle derives the inertia
+        from the mass as EntityFactory does; it must equal props[1]."""
+        ids = np.ascontiguousarray(ids, np.uint32)
+        kind = np.ascontiguousarray(np.asarray(kind) & 3, np.uint8)
+        props = np.asarray(props, np.float32)
+        state = np.asarray(state, np.float32)
+        n = ids.shape[0]
+        first = int(self.lib.r2o_num_bodies(self.h))
+        opt = np.zeros((10, n), np.float32)
+        opt[0], opt[1], opt[2] = state[0], state[1], state[2]
+        opt[6], opt[7] = props[2], props[0]
+        opt[8], opt[9] = props[3], props[4]
+        if self.lib.r2o_add_bodies(self.h, n, _p(ids, C.c_uint32), _p(kind, C.c_uint8), _p(opt, C.c_float)) != 0:
+            raise ValueError("the oracle refused the bodies")
+        st = self.state()
+        if not np.array_equal(self.props()[:, first:], props):
+            raise ValueError("the oracle derives other masses or inertias from these props")
+        st[:, first:] = state
+        self.set_state(np.ascontiguousarray(st))
+
+    def set_compensated(self, on: bool = True):
+        """Compensated (Kahan) accumulation of each point's impulses (off in
+        reference mode; r2d_accum.h)."""
+        self.lib.r2o_set_compensated(self.h, int(bool(on)))
+
+    def take_warm(self, other: "Oracle"):
+        """Carry `other`'s last-frame warm-start table (keyed by body ids)
+        into this solver, as an engine keeps it across body uploads."""
+        if self.lib.r2o_copy_warm(self.h, other.h) != 0:
+            raise ValueError("the two oracles differ in precision")
 
     def set_sleep(self, on: bool = True):
         """Sleeping (r2d_sleep.h): a world still for R2D_SLEEP_FRAMES
@@ -246,3 +283,14 @@ def sincosf(x) -> tuple[np.ndarray, np.ndarray]:
     c = np.empty_like(x)
     load().r2o_sincosf(x.size, _p(x, C.c_float), _p(s, C.c_float), _p(c, C.c_float))
     return s, c
+
+
+def acc_sum(x, s0: float = 0.0, lo: float = 0.0, hi: float | None = None):
+    """Accumulates increments `x` from s0 with r2d_accum.h's clamped
+    compensated update (lower bound lo; upper bound hi when given):
+    returns (s, c, sum of the applied changes) as float32."""
+    x = np.ascontiguousarray(x, np.float32)
+    out = np.zeros(3, np.float32)
+    load().r2o_acc_sum(x.shape[0], _p(x, C.c_float), float(s0), float(lo),
+                       float("nan") if hi is None else float(hi), _p(out, C.c_float))
+    return out

@@ -226,6 +226,36 @@ void r2o_set_warm_start(void* hp, int on) {
     DISPATCH(h, (S.warm_start = on != 0, S.warm_prev.clear()));
 }
 
+/* n increments x[k] accumulated from (s, c) = (s0, 0) with the clamped
+ * compensated update of r2d_accum.h (lower bound lo, no upper bound when
+ * hi is NaN); out = {s, c, sum of the applied changes}. */
+void r2o_acc_sum(uint32_t n, const float* x, float s0, float lo, float hi, float* out) {
+    float s = s0, c = 0.f, applied = 0.f;
+    for (uint32_t k = 0; k < n; ++k)
+        applied += (hi == hi) ? r2d_acc_add_clamp(&s, &c, x[k], lo, hi) : r2d_acc_add_max(&s, &c, x[k], lo);
+    out[0] = s;
+    out[1] = c;
+    out[2] = applied;
+}
+
+void r2o_set_compensated(void* hp, int on) {
+    Handle* h = (Handle*)hp;
+    DISPATCH(h, S.compensated = on != 0);
+}
+
+/* Hands src's last-frame warm-start table (keyed by body ids) to dst, as an
+ * engine keeps it when its body store is replaced.  Both of one precision. */
+int r2o_copy_warm(void* dst, const void* src) {
+    Handle* d = (Handle*)dst;
+    const Handle* s = (const Handle*)src;
+    if (d->precision != s->precision) return -1;
+    if (d->precision == 64)
+        d->d->warm_prev = s->d->warm_prev;
+    else
+        d->f->warm_prev = s->f->warm_prev;
+    return 0;
+}
+
 void r2o_get_state(void* hp, float* out) {
     Handle* h = (Handle*)hp;
     if (h->precision == 64)

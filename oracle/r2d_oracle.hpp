@@ -63,6 +63,7 @@
 #include <utility>
 #include <vector>
 
+#include "../resolve2d_gb300/csrc/r2d_accum.h"
 #include "../resolve2d_gb300/csrc/r2d_colour.h"
 #include "../resolve2d_gb300/csrc/r2d_sincos.h"
 #include "../resolve2d_gb300/csrc/r2d_sleep.h"
@@ -360,6 +361,7 @@ void project_along_axis(const Body<R>& b, V2<R> normal, R out[2]) {
 template <class R>
 struct CollisionPoint {  // collision.zig:22-36
     R accumulated_pn = 0, accumulated_pt = 0;
+    R comp_pn = 0, comp_pt = 0;  // compensation words (compensated mode, r2d_accum.h)
     V2<R> ref_r, inc_r, pos;
     R depth = 0, original_depth = 0;
     R mass_n = 0, mass_t = 0;
@@ -543,9 +545,15 @@ public:
     // Warm starting (an extension, off in reference mode): a manifold found
     // again the next frame with the same (reference, incident) pair starts
     // from last frame's accumulated impulses, which are applied to the
-    // bodies once, after the first substep's preStep.
+    // bodies once, after the first substep's preStep.  Pairs are keyed by
+    // the bodies' stable ids, so the table survives changes to the body
+    // store (r2o_copy_warm hands it to a rebuilt solver).
     bool warm_start = false;
-    std::unordered_map<uint64_t, std::array<R, 4>> warm_prev;  // (ref << 32 | inc) -> pn0, pt0, pn1, pt1
+    // (ref id << 32 | inc id) -> pn0, pt0, pn1, pt1, then their compensation words
+    std::unordered_map<uint64_t, std::array<R, 8>> warm_prev;
+    // Compensated accumulation of every point's impulses (an extension, off
+    // in reference mode): r2d_accum.h.
+    bool compensated = false;
 
     // Sleeping (an extension, off in reference mode; r2d_sleep.h): after
     // R2D_SLEEP_FRAMES consecutive still frames the world is not stepped
@@ -867,6 +875,8 @@ public:
             if (point.depth >= R(0)) {
                 point.accumulated_pn = 0;
                 point.accumulated_pt = 0;
+                point.comp_pn = 0;
+                point.comp_pt = 0;
                 continue;
             }
             V2<R> r1 = point.ref_r, r2 = point.inc_r;
@@ -885,13 +895,20 @@ public:
             if (!warm_start && pn < C<R>::MIN_MANIFOLD_IMPULSE) continue;
             num = dot2(dv, m.tangent);
             R pt = num * point.mass_t;
-            R new_accumulated_pn = zmax(R(0), point.accumulated_pn + pn);
-            R applied_pn = new_accumulated_pn - point.accumulated_pn;
-            point.accumulated_pn = new_accumulated_pn;
-            R max_pt = m.friction * std::fabs(point.accumulated_pn);
-            R new_accumulated_pt = zclamp(point.accumulated_pt + pt, -max_pt, max_pt);
-            R applied_pt = new_accumulated_pt - point.accumulated_pt;
-            point.accumulated_pt = new_accumulated_pt;
+            R applied_pn, applied_pt;
+            if (compensated) {  // r2d_accum.h: the same clamps on s + c
+                applied_pn = r2d_acc_add_max(&point.accumulated_pn, &point.comp_pn, pn, R(0));
+                R max_pt = m.friction * std::fabs(point.accumulated_pn);
+                applied_pt = r2d_acc_add_clamp(&point.accumulated_pt, &point.comp_pt, pt, -max_pt, max_pt);
+            } else {
+                R new_accumulated_pn = zmax(R(0), point.accumulated_pn + pn);
+                applied_pn = new_accumulated_pn - point.accumulated_pn;
+                point.accumulated_pn = new_accumulated_pn;
+                R max_pt = m.friction * std::fabs(point.accumulated_pn);
+                R new_accumulated_pt = zclamp(point.accumulated_pt + pt, -max_pt, max_pt);
+                applied_pt = new_accumulated_pt - point.accumulated_pt;
+                point.accumulated_pt = new_accumulated_pt;
+            }
             V2<R> pn_vec = scale2(m.normal, applied_pn);
             V2<R> pt_vec = scale2(m.tangent, applied_pt);
             V2<R> dp = add2(pn_vec, pt_vec);
@@ -915,14 +932,20 @@ public:
     }
 
     // ---- warm starting ----
+    uint64_t warm_key(const Key& k) const {
+        return ((uint64_t)bodies[k.ref].id << 32) | (uint64_t)bodies[k.inc].id;
+    }
+
     void warm_load() {
         for (auto& km : manifolds) {
-            auto it = warm_prev.find(((uint64_t)km.first.ref << 32) | (uint64_t)km.first.inc);
+            auto it = warm_prev.find(warm_key(km.first));
             if (it == warm_prev.end()) continue;
             for (int i = 0; i < 2; ++i) {
                 if (!km.second.has_point[i]) continue;
                 km.second.points[i].accumulated_pn = it->second[2 * i];
                 km.second.points[i].accumulated_pt = it->second[2 * i + 1];
+                km.second.points[i].comp_pn = it->second[4 + 2 * i];
+                km.second.points[i].comp_pt = it->second[4 + 2 * i + 1];
             }
         }
     }
@@ -940,6 +963,8 @@ public:
             if (point.depth >= R(0)) {
                 point.accumulated_pn = 0;
                 point.accumulated_pt = 0;
+                point.comp_pn = 0;
+                point.comp_pt = 0;
                 continue;
             }
             V2<R> dp = add2(scale2(m.normal, point.accumulated_pn), scale2(m.tangent, point.accumulated_pt));
@@ -965,13 +990,15 @@ public:
     void warm_store() {
         warm_prev.clear();
         for (auto& km : manifolds) {
-            std::array<R, 4> a{R(0), R(0), R(0), R(0)};
+            std::array<R, 8> a{};
             for (int i = 0; i < 2; ++i) {
                 if (!km.second.has_point[i]) continue;
                 a[2 * i] = km.second.points[i].accumulated_pn;
                 a[2 * i + 1] = km.second.points[i].accumulated_pt;
+                a[4 + 2 * i] = km.second.points[i].comp_pn;
+                a[4 + 2 * i + 1] = km.second.points[i].comp_pt;
             }
-            warm_prev[((uint64_t)km.first.ref << 32) | (uint64_t)km.first.inc] = a;
+            warm_prev[warm_key(km.first)] = a;
         }
     }
 

@@ -35,6 +35,7 @@ FLAG_GRID_PIPELINE = 2
 FLAG_FP64_POSITIONS = 4
 FLAG_WARM_START = 8
 FLAG_SLEEP = 16
+FLAG_COMPENSATED = 32
 MANIFOLD_FLOATS = 33
 
 

@@ -51,22 +51,29 @@ def _stale(target: Path, deps: list[Path]) -> bool:
 TIMERS_LIB = BUILD / "libr2d_timers.so"
 
 
-def build_library(force: bool = False, verbose: bool = False, timers: bool = False) -> Path:
+def build_library(force: bool = False, verbose: bool = False, timers: bool = False,
+                  defines: dict | None = None, name: str | None = None) -> Path:
     """Compile the translation units in parallel and link libr2d_gb300.so.
     timers=True builds libr2d_timers.so instead: the same library with the
     fused kernel's per-phase cycle counters (R2D_PHASE_TIMERS), for
-    resolve2d_gb300.phase_timers."""
+    resolve2d_gb300.phase_timers.  `defines` (e.g. {"R2D_REG_TARGET": 80})
+    with `name` builds a tuning variant as lib<name>.so beside it."""
     BUILD.mkdir(exist_ok=True)
     deps = _deps()
     lib = TIMERS_LIB if timers else LIB
+    tag = "_timers" if timers else ""
+    if name:
+        lib = BUILD / f"lib{name}.so"
+        tag = "_" + name
     if not force and not _stale(lib, deps):
         return lib
     cc = nvcc()
     procs = []
     objs = []
     extra = ["-DR2D_PHASE_TIMERS"] if timers else []
+    extra += [f"-D{k}={v}" for k, v in (defines or {}).items()]
     for src in SOURCES:
-        obj = BUILD / (Path(src).stem + ("_timers.o" if timers else ".o"))
+        obj = BUILD / (Path(src).stem + tag + ".o")
         objs.append(obj)
         cmd = [cc, *ARCH, *NVCC_FLAGS, *extra, "-I", str(INCLUDE), "-c", str(CSRC / src), "-o", str(obj)]
         if verbose:

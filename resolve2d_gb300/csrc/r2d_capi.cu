@@ -20,12 +20,14 @@
 #include <cstring>
 #include <string>
 #include <unordered_map>
+#include <unordered_set>
 #include <vector>
 
 #include "../../include/r2d_gb300.h"
 #include "r2d_device.cuh"
 #include "r2d_large.h"
 #include "r2d_sincos.h"
+#include "r2d_solve.cuh"
 #include "r2d_validate.h"
 #include "r2d_world.cuh"
 
@@ -34,10 +36,8 @@ cudaError_t launch_world_step(const StepParams& P, const Caps& C, int threads, c
                               cudaStream_t stream);
 cudaError_t allow_world_step_smem(int bytes);
 cudaError_t launch_count_call(uint32_t* counter, cudaStream_t stream);
-cudaError_t launch_migrate_warm(uint32_t nworlds, const uint32_t* old_keys, const float4* old_vals,
-                                const uint32_t* old_off, const uint32_t* old_hs, const uint32_t* old_cur,
-                                uint32_t* new_keys, float4* new_vals, const uint32_t* new_off, const uint32_t* new_hs,
-                                cudaStream_t stream);
+cudaError_t launch_migrate_warm(uint32_t nworlds, const WarmTables& old_t, const uint32_t* old_cur,
+                                const WarmTables& new_t, cudaStream_t stream);
 }  // namespace r2d
 
 using namespace r2d;
@@ -207,9 +207,18 @@ struct Engine {
     // Warm starting (R2D_FLAG_WARM_START): each fused world's two tables of
     // warm_hs slots (WorldDesc::warm_off), sized from its class's manifold
     // capacity; d_warm_cur[w] names the table holding last frame.
-    uint32_t* d_warm_keys = nullptr;
+    unsigned long long* d_warm_keys = nullptr;
     float4* d_warm_vals = nullptr;
+    float4* d_warm_cvals = nullptr;  // compensation words (R2D_FLAG_COMPENSATED)
     uint32_t* d_warm_cur = nullptr;
+    // Last frame's warm-start entries of each world, taken when the body
+    // store is replaced and put into the new tables at the next plan: keys
+    // are body ids, so they stay valid; entries naming a vanished id are dropped.
+    struct WarmEntry {
+        unsigned long long key;
+        float4 val, cval;
+    };
+    std::vector<std::vector<WarmEntry>> warm_carry;
     uint32_t* d_sleep = nullptr;  // [nworlds] consecutive still frames (R2D_FLAG_SLEEP)
     // A frame call's host rows (process_io): the device copy the kernels read
     // (StepParams::ext) and the value last copied there.
@@ -229,7 +238,8 @@ struct Engine {
         if (gexec) cudaGraphExecDestroy(gexec);
         dfree(d_call);
         dfree(d_ext);
-        dfree(d_warm_keys); dfree(d_warm_vals); dfree(d_warm_cur); dfree(d_warm_off); dfree(d_warm_hs);
+        dfree(d_warm_keys); dfree(d_warm_vals); dfree(d_warm_cvals); dfree(d_warm_cur); dfree(d_warm_off);
+        dfree(d_warm_hs);
         dfree(d_sleep);
         dfree(d_state); dfree(d_pos64); dfree(d_props); dfree(d_kind); dfree(d_ids); dfree(d_worlds);
         dfree(d_status); dfree(d_err);
@@ -306,6 +316,22 @@ struct Engine {
         if (dw >= 0)
             return fail(R2D_ERR_INVALID_ARGUMENT,
                         "world " + std::to_string(dw) + " holds two bodies with id " + std::to_string(dup));
+        // warm starting: last frame's impulses outlive the body store (their
+        // keys are ids); world w of the new store takes world w's
+        if (warm_start()) {
+            if (int st = take_warm_entries()) return st;
+            warm_carry.resize(nw);
+            for (uint32_t w = 0; w < nw; ++w) {
+                std::unordered_set<uint32_t> live(ids + body_off[w], ids + body_off[w + 1]);
+                auto& v = warm_carry[w];
+                v.erase(std::remove_if(v.begin(), v.end(),
+                                       [&](const WarmEntry& e) {
+                                           return !live.count((uint32_t)(e.key >> 32)) ||
+                                                  !live.count((uint32_t)e.key);
+                                       }),
+                        v.end());
+            }
+        }
         nworlds = nw;
         nbodies = n;
         ids_h.assign(ids, ids + n);
@@ -353,7 +379,8 @@ struct Engine {
         large.resize(nw);
         large_status.assign(nw, 0);
         large_frozen.assign(nw, 0);
-        dfree(d_warm_keys); dfree(d_warm_vals); dfree(d_warm_cur); dfree(d_warm_off); dfree(d_warm_hs);
+        dfree(d_warm_keys); dfree(d_warm_vals); dfree(d_warm_cvals); dfree(d_warm_cur); dfree(d_warm_off);
+        dfree(d_warm_hs);
         warm_hs_h.assign(nw, 0);
         warm_off_h.assign(nw, 0);
         if (warm_start()) {
@@ -438,6 +465,7 @@ struct Engine {
     bool fp64_positions() const { return (cfg.flags & R2D_FLAG_FP64_POSITIONS) != 0; }
     bool warm_start() const { return (cfg.flags & R2D_FLAG_WARM_START) != 0; }
     bool sleeping() const { return (cfg.flags & R2D_FLAG_SLEEP) != 0; }
+    bool compensated() const { return (cfg.flags & R2D_FLAG_COMPENSATED) != 0; }
 
     static uint32_t pow2_at_least(uint32_t v) {
         uint32_t p = 1;
@@ -457,21 +485,25 @@ struct Engine {
             total += 2ull * hs[w];
         }
         if (hs == warm_hs_h && d_warm_keys) return R2D_OK;
-        uint32_t *keys = nullptr, *doff = nullptr, *dhs = nullptr;
-        float4* vals = nullptr;
+        unsigned long long* keys = nullptr;
+        uint32_t *doff = nullptr, *dhs = nullptr;
+        float4 *vals = nullptr, *cvals = nullptr;
         CUDA_TRY(dalloc(keys, std::max<size_t>(total, 1)));
         CUDA_TRY(dalloc(vals, std::max<size_t>(total, 1)));
+        if (compensated()) CUDA_TRY(dalloc(cvals, std::max<size_t>(total, 1)));
         CUDA_TRY(dalloc(doff, nworlds));
         CUDA_TRY(dalloc(dhs, nworlds));
         CUDA_TRY(cudaMemcpyAsync(doff, off.data(), 4 * nworlds, cudaMemcpyHostToDevice, stream));
         CUDA_TRY(cudaMemcpyAsync(dhs, hs.data(), 4 * nworlds, cudaMemcpyHostToDevice, stream));
-        CUDA_TRY(launch_migrate_warm(nworlds, d_warm_keys, d_warm_vals, d_warm_off, d_warm_keys ? d_warm_hs : nullptr,
-                                     d_warm_cur, keys, vals, doff, dhs, stream));
+        const WarmTables old_t{d_warm_keys, d_warm_vals, d_warm_cvals, d_warm_off, d_warm_keys ? d_warm_hs : nullptr};
+        const WarmTables new_t{keys, vals, cvals, doff, dhs};
+        CUDA_TRY(launch_migrate_warm(nworlds, old_t, d_warm_cur, new_t, stream));
         CUDA_TRY(cudaMemsetAsync(d_warm_cur, 0, sizeof(uint32_t) * nworlds, stream));
         CUDA_TRY(cudaStreamSynchronize(stream));
-        dfree(d_warm_keys); dfree(d_warm_vals); dfree(d_warm_off); dfree(d_warm_hs);
+        dfree(d_warm_keys); dfree(d_warm_vals); dfree(d_warm_cvals); dfree(d_warm_off); dfree(d_warm_hs);
         d_warm_keys = keys;
         d_warm_vals = vals;
+        d_warm_cvals = cvals;
         d_warm_off = doff;
         d_warm_hs = dhs;
         warm_hs_h = hs;
@@ -480,6 +512,110 @@ struct Engine {
             worlds_h[w].warm_hs = hs[w];
             worlds_h[w].warm_off = off[w];
         }
+        return R2D_OK;
+    }
+
+    // Every world's last-frame warm-start entries, from the device tables
+    // of the current store (fused tables and grid-pipeline worlds alike),
+    // into warm_carry[w] (world w of the current store).
+    int take_warm_entries() {
+        // entries taken at an earlier upload and not yet placed (no step
+        // since) are still the last frame's: keep them
+        if (!warm_carry.empty()) return R2D_OK;
+        warm_carry.assign(nworlds, {});
+        if (nworlds == 0) return R2D_OK;
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        std::vector<unsigned long long> k;
+        std::vector<float4> v, c;
+        std::vector<uint32_t> cur(nworlds, 0);
+        if (d_warm_keys && d_warm_cur) {
+            size_t total = 0;
+            for (uint32_t w = 0; w < nworlds; ++w) total = std::max<size_t>(total, (size_t)warm_off_h[w] + 2ull * warm_hs_h[w]);
+            k.resize(total);
+            v.resize(total);
+            c.assign(total, make_float4(0.f, 0.f, 0.f, 0.f));
+            CUDA_TRY(cudaMemcpy(cur.data(), d_warm_cur, 4 * nworlds, cudaMemcpyDeviceToHost));
+            CUDA_TRY(cudaMemcpy(k.data(), d_warm_keys, 8 * total, cudaMemcpyDeviceToHost));
+            CUDA_TRY(cudaMemcpy(v.data(), d_warm_vals, 16 * total, cudaMemcpyDeviceToHost));
+            if (d_warm_cvals) CUDA_TRY(cudaMemcpy(c.data(), d_warm_cvals, 16 * total, cudaMemcpyDeviceToHost));
+        }
+        for (uint32_t w = 0; w < nworlds; ++w) {
+            auto& out = warm_carry[w];
+            if (w < world_large.size() && world_large[w]) {
+                if (!large[w]) continue;
+                std::vector<unsigned long long> lk;
+                std::vector<float4> lv, lc;
+                std::string msg;
+                if (const int r = large[w]->read_warm(&lk, &lv, &lc, stream, &msg)) return fail(r, msg);
+                for (size_t q = 0; q < lk.size(); ++q)
+                    if (lk[q] != ~0ull) out.push_back(WarmEntry{lk[q], lv[q], lc[q]});
+            } else if (w < warm_hs_h.size() && warm_hs_h[w] && !k.empty()) {
+                const size_t at = (size_t)warm_off_h[w] + (size_t)cur[w] * warm_hs_h[w];
+                for (size_t q = at; q < at + warm_hs_h[w]; ++q)
+                    if (k[q] != ~0ull) out.push_back(WarmEntry{k[q], v[q], c[q]});
+            }
+        }
+        return R2D_OK;
+    }
+
+    // The carried entries into the new store's tables (after plan has laid
+    // them out, table 0 current): a fused world's are inserted on the host
+    // with the device's hash and probing and uploaded; a grid-pipeline
+    // world's are seeded into its own tables.
+    int put_warm_entries() {
+        if (warm_carry.empty()) return R2D_OK;
+        auto build = [](const std::vector<WarmEntry>& es, uint32_t hs, std::vector<unsigned long long>& k,
+                        std::vector<float4>& v, std::vector<float4>& c) {
+            k.assign(hs, ~0ull);
+            v.assign(hs, make_float4(0.f, 0.f, 0.f, 0.f));
+            c.assign(hs, make_float4(0.f, 0.f, 0.f, 0.f));
+            uint32_t taken = 0;
+            for (const WarmEntry& e : es) {
+                if (2 * (taken + 1) > hs) break;  // at most half full, as the device keeps it
+                const uint32_t mask = hs - 1u;
+                for (uint32_t probe = 0, h = warm_hash(e.key); probe < hs; ++probe) {
+                    const uint32_t slot = (h + probe) & mask;
+                    if (k[slot] != ~0ull) continue;
+                    k[slot] = e.key;
+                    v[slot] = e.val;
+                    c[slot] = e.cval;
+                    ++taken;
+                    break;
+                }
+            }
+        };
+        std::vector<unsigned long long> k;
+        std::vector<float4> v, c;
+        for (uint32_t w = 0; w < nworlds && w < warm_carry.size(); ++w) {
+            const auto& es = warm_carry[w];
+            if (es.empty()) continue;
+            if (world_large[w]) {
+                const uint32_t hs = pow2_at_least(2u * (uint32_t)es.size() + 2u);
+                build(es, hs, k, v, c);
+                unsigned long long* dk = nullptr;
+                float4 *dv = nullptr, *dc = nullptr;
+                CUDA_TRY(dalloc(dk, hs));
+                CUDA_TRY(dalloc(dv, hs));
+                CUDA_TRY(dalloc(dc, hs));
+                CUDA_TRY(cudaMemcpy(dk, k.data(), 8ull * hs, cudaMemcpyHostToDevice));
+                CUDA_TRY(cudaMemcpy(dv, v.data(), 16ull * hs, cudaMemcpyHostToDevice));
+                CUDA_TRY(cudaMemcpy(dc, c.data(), 16ull * hs, cudaMemcpyHostToDevice));
+                std::string msg;
+                const int r = large[w]->seed_warm(dk, dv, compensated() ? dc : nullptr, hs, stream, &msg);
+                dfree(dk);
+                dfree(dv);
+                dfree(dc);
+                if (r) return fail(r, msg);
+            } else if (warm_hs_h[w] && d_warm_keys) {
+                const uint32_t hs = warm_hs_h[w];
+                build(es, hs, k, v, c);
+                const size_t at = warm_off_h[w];  // table 0: plan left every world's current table at 0
+                CUDA_TRY(cudaMemcpy(d_warm_keys + at, k.data(), 8ull * hs, cudaMemcpyHostToDevice));
+                CUDA_TRY(cudaMemcpy(d_warm_vals + at, v.data(), 16ull * hs, cudaMemcpyHostToDevice));
+                if (d_warm_cvals) CUDA_TRY(cudaMemcpy(d_warm_cvals + at, c.data(), 16ull * hs, cudaMemcpyHostToDevice));
+            }
+        }
+        warm_carry.clear();
         return R2D_OK;
     }
 
@@ -637,7 +773,7 @@ struct Engine {
     LayoutOpts layout_opts(bool lean, bool multi_substep) const {
         const bool debug = (cfg.flags & R2D_FLAG_DEBUG_TAPS) != 0;
         // debug taps report lever arms after integration: keep frame-start positions
-        return LayoutOpts{lean, debug, multi_substep || debug, debug};
+        return LayoutOpts{lean, debug, multi_substep || debug, debug, compensated()};
     }
 
     // Shared memory a CTA may have (opt-in maximum) ...
@@ -848,6 +984,7 @@ struct Engine {
             for (const auto& c : classes)
                 for (uint32_t w : c.worlds) nm[w] = c.caps.nm;
             if (int st = layout_warm(nm)) return st;
+            if (int st = put_warm_entries()) return st;
         }
         for (auto& d : worlds_h) d.bucket_recip = bucket_recip(table_mult * d.n);
         CUDA_TRY(dalloc(d_worlds, nworlds));
@@ -1048,6 +1185,7 @@ struct Engine {
         in.disc_rot = (d.flags & W_DISC_ROTATION) != 0;
         in.pos64 = d_pos64;
         in.warm = warm_start();
+        in.comp = compensated();
         in.verbose = verbose;
         in.sleep = d_sleep ? d_sleep + w : nullptr;
         in.colour_round_limit = colour_round_limit;
@@ -1114,6 +1252,7 @@ struct Engine {
         if (warm_start()) {
             P.warm_keys = d_warm_keys;
             P.warm_vals = d_warm_vals;
+            P.warm_cvals = d_warm_cvals;
             P.warm_cur = d_warm_cur;
         }
         return P;
@@ -1299,7 +1438,8 @@ struct Engine {
             CUDA_TRY(cudaMemcpy(&cur, d_warm_cur + w, sizeof(uint32_t), cudaMemcpyDeviceToHost));
             const size_t at = (size_t)warm_off_h[w] + (size_t)cur * warm_hs_h[w];
             std::string msg;
-            const int r = large[w]->seed_warm(d_warm_keys + at, d_warm_vals + at, warm_hs_h[w], stream, &msg);
+            const int r = large[w]->seed_warm(d_warm_keys + at, d_warm_vals + at,
+                                              d_warm_cvals ? d_warm_cvals + at : nullptr, warm_hs_h[w], stream, &msg);
             if (r) return fail(r, msg);
         }
         for (uint32_t k = from; k < calls.size(); ++k) {

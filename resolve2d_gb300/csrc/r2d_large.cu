@@ -369,6 +369,10 @@ __global__ void lk_narrow(Phase1 A, uint32_t npairs) {
         s.odepth[p] = pts[k].depth;
         s.apn[p] = 0.f;
         s.apt[p] = 0.f;
+        if (s.cpn) {
+            s.cpn[p] = 0.f;
+            s.cpt[p] = 0.f;
+        }
     }
 }
 
@@ -728,6 +732,10 @@ __global__ void lk_permute(SWT<uint32_t> src, SWT<uint32_t> dst, const uint32_t*
         dst.odepth[q] = src.odepth[p];
         dst.apn[q] = src.apn[p];
         dst.apt[q] = src.apt[p];
+        if (src.cpn) {
+            dst.cpn[q] = src.cpn[p];
+            dst.cpt[q] = src.cpt[p];
+        }
     }
 }
 
@@ -744,6 +752,7 @@ __global__ void lk_permute(SWT<uint32_t> src, SWT<uint32_t> dst, const uint32_t*
 struct Packed {
     float4 *v0, *v1, *v2, *v3, *v4, *v5, *v6;
     float4* mom4;
+    float4* v7;  // compensated mode: the accumulators' compensation words, as v5; else null
 };
 constexpr uint32_t PK_NP = 0xFFu, PK_STATIC_A = 0x100u, PK_STATIC_B = 0x200u;  // v1.y bits
 
@@ -772,6 +781,8 @@ __device__ __forceinline__ void solve_contact_rec(const Packed& pk, const MRec& 
     const f2 r1s[2] = {{v2.x, v2.y}, {v3.x, v3.y}}, r2s[2] = {{v2.z, v2.w}, {v3.z, v3.w}};
     const float mn[2] = {v4.x, v4.z}, mt[2] = {v4.y, v4.w};
     float apn[2] = {v5.x, v5.z}, apt[2] = {v5.y, v5.w};
+    float4 v7 = pk.v7 ? pk.v7[m] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float cpn[2] = {v7.x, v7.z}, cpt[2] = {v7.y, v7.w};
     const float inv_m1 = v6.x, inv_i1 = v6.y, inv_m2 = v6.z, inv_i2 = v6.w;
     float4 ma4, mb4;
     if (MOM4) {
@@ -801,15 +812,22 @@ __device__ __forceinline__ void solve_contact_rec(const Packed& pk, const MRec& 
         if (!warm && pn < MIN_MANIFOLD_IMPULSE) continue;
         num = dot2(dv, t);
         const float pt = num * mt[k];
-        const float acc = apn[k];
-        const float nacc = zmax(0.0f, acc + pn);
-        const float applied_pn = nacc - acc;
-        apn[k] = nacc;
-        const float max_pt = fr * fabsf(nacc);
-        const float acct = apt[k];
-        const float nacct = zclamp(acct + pt, -max_pt, max_pt);
-        const float applied_pt = nacct - acct;
-        apt[k] = nacct;
+        float applied_pn, applied_pt;
+        if (pk.v7) {  // compensated (r2d_accum.h), as accumulate() in r2d_solve.cuh
+            applied_pn = r2d_acc_add_max(&apn[k], &cpn[k], pn, 0.0f);
+            const float max_pt = fr * fabsf(apn[k]);
+            applied_pt = r2d_acc_add_clamp(&apt[k], &cpt[k], pt, -max_pt, max_pt);
+        } else {
+            const float acc = apn[k];
+            const float nacc = zmax(0.0f, acc + pn);
+            applied_pn = nacc - acc;
+            apn[k] = nacc;
+            const float max_pt = fr * fabsf(nacc);
+            const float acct = apt[k];
+            const float nacct = zclamp(acct + pt, -max_pt, max_pt);
+            applied_pt = nacct - acct;
+            apt[k] = nacct;
+        }
         const f2 dp = add2(scale2(n, applied_pn), scale2(t, applied_pt));
         if (!sa) {
             alp1 = sub2(alp1, dp);
@@ -821,6 +839,7 @@ __device__ __forceinline__ void solve_contact_rec(const Packed& pk, const MRec& 
         }
     }
     pk.v5[m] = make_float4(apn[0], apt[0], apn[1], apt[1]);
+    if (pk.v7) pk.v7[m] = make_float4(cpn[0], cpt[0], cpn[1], cpt[1]);
     if (!sa) {
         if (MOM4) {
             pk.mom4[a] = make_float4(ma4.x + alp1.x, ma4.y + alp1.y, ma4.z + arp1, 0.f);
@@ -984,6 +1003,9 @@ __device__ __forceinline__ void pack_one(const Phase2& A, uint32_t m, bool first
         const bool z0 = b0 < 0.0f, z1 = b1 < 0.0f;
         A.pk.v5[m] = make_float4(z0 ? 0.f : s.apn[p], z0 ? 0.f : s.apt[p], z1 ? 0.f : s.apn[p + 1],
                                  z1 ? 0.f : s.apt[p + 1]);
+        if (A.pk.v7)
+            A.pk.v7[m] = make_float4(z0 ? 0.f : s.cpn[p], z0 ? 0.f : s.cpt[p], z1 ? 0.f : s.cpn[p + 1],
+                                     z1 ? 0.f : s.cpt[p + 1]);
     }
 }
 
@@ -996,6 +1018,15 @@ __device__ __forceinline__ void unpack_one(const Phase2& A, uint32_t m) {
     if (np > 1) {
         A.s.apn[p + 1] = v.z;
         A.s.apt[p + 1] = v.w;
+    }
+    if (A.pk.v7) {
+        const float4 c = A.pk.v7[m];
+        A.s.cpn[p] = c.x;
+        A.s.cpt[p] = c.y;
+        if (np > 1) {
+            A.s.cpn[p + 1] = c.z;
+            A.s.cpt[p + 1] = c.w;
+        }
     }
 }
 
@@ -1018,15 +1049,12 @@ __global__ void lk_contacts(Phase2 A) {
 }
 
 // ---- warm starting: the world's tables of last frame's impulses ----
-__device__ __forceinline__ unsigned long long warm_key64(uint32_t ref, uint32_t inc) {
-    return ((unsigned long long)ref << 32) | inc;
-}
-
-__global__ void lk_warm_load(SWT<uint32_t> s, uint32_t M, const unsigned long long* keys, const float4* vals,
-                             uint32_t hs) {
+// Keys are the bodies' stable ids (warm_key_ids); `ids` is this world's id array.
+__global__ void lk_warm_load(SWT<uint32_t> s, const uint32_t* ids, uint32_t M, const unsigned long long* keys,
+                             const float4* vals, const float4* cvals, uint32_t hs) {
     const uint32_t m = blockIdx.x * LT + threadIdx.x;
     if (m >= M) return;
-    const int slot = warm_find(keys, hs, warm_key64(s.ma[m], s.mb[m]));
+    const int slot = warm_find(keys, hs, warm_key_ids(__ldg(ids + s.ma[m]), __ldg(ids + s.mb[m])));
     if (slot < 0) return;
     const float4 v = vals[slot];
     const uint32_t p0 = s.mp0[m], np = s.mnp[m];
@@ -1037,6 +1065,17 @@ __global__ void lk_warm_load(SWT<uint32_t> s, uint32_t M, const unsigned long lo
     if (np > 1) {
         s.apn[p0 + 1] = v.z;
         s.apt[p0 + 1] = v.w;
+    }
+    if (s.cpn && cvals) {
+        const float4 c = cvals[slot];
+        if (np > 0) {
+            s.cpn[p0] = c.x;
+            s.cpt[p0] = c.y;
+        }
+        if (np > 1) {
+            s.cpn[p0 + 1] = c.z;
+            s.cpt[p0 + 1] = c.w;
+        }
     }
 }
 
@@ -1051,22 +1090,33 @@ __global__ void lk_warm_clear(unsigned long long* keys, uint32_t hs) {
     if (q < hs) keys[q] = ~0ull;
 }
 
-__global__ void lk_warm_store(SWT<uint32_t> s, uint32_t M, unsigned long long* keys, float4* vals, uint32_t hs) {
+__global__ void lk_warm_store(SWT<uint32_t> s, const uint32_t* ids, uint32_t M, unsigned long long* keys,
+                              float4* vals, float4* cvals, uint32_t hs) {
     const uint32_t m = blockIdx.x * LT + threadIdx.x;
     if (m >= M) return;
     const uint32_t p0 = s.mp0[m], np = s.mnp[m];
-    const float4 v = make_float4(np > 0 ? s.apn[p0] : 0.f, np > 0 ? s.apt[p0] : 0.f, np > 1 ? s.apn[p0 + 1] : 0.f,
-                                 np > 1 ? s.apt[p0 + 1] : 0.f);
-    warm_insert(keys, vals, hs, warm_key64(s.ma[m], s.mb[m]), v);
+    const int slot = warm_claim(keys, hs, warm_key_ids(__ldg(ids + s.ma[m]), __ldg(ids + s.mb[m])));
+    if (slot < 0) return;
+    vals[slot] = make_float4(np > 0 ? s.apn[p0] : 0.f, np > 0 ? s.apt[p0] : 0.f, np > 1 ? s.apn[p0 + 1] : 0.f,
+                             np > 1 ? s.apt[p0 + 1] : 0.f);
+    if (cvals)
+        cvals[slot] = s.cpn ? make_float4(np > 0 ? s.cpn[p0] : 0.f, np > 0 ? s.cpt[p0] : 0.f,
+                                          np > 1 ? s.cpn[p0 + 1] : 0.f, np > 1 ? s.cpt[p0 + 1] : 0.f)
+                            : make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
-// a fused-kernel table (16-bit reference << 16 | incident keys) into this path's
-__global__ void lk_warm_copy(const uint32_t* keys, const float4* vals, uint32_t hs, unsigned long long* nkeys,
-                             float4* nvals, uint32_t nhs) {
+// another table of the same format (a fused world's, or one the host built)
+// into this path's
+__global__ void lk_warm_copy(const unsigned long long* keys, const float4* vals, const float4* cvals, uint32_t hs,
+                             unsigned long long* nkeys, float4* nvals, float4* ncvals, uint32_t nhs) {
     const uint32_t q = blockIdx.x * LT + threadIdx.x;
     if (q >= hs) return;
-    const uint32_t key = keys[q];
-    if (key != 0xFFFFFFFFu) warm_insert(nkeys, nvals, nhs, warm_key64(key >> 16, key & 0xFFFFu), vals[q]);
+    const unsigned long long key = keys[q];
+    if (key == ~0ull) return;
+    const int slot = warm_claim(nkeys, nhs, key);
+    if (slot < 0) return;
+    nvals[slot] = vals[q];
+    if (ncvals) ncvals[slot] = cvals ? cvals[q] : make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
 // the joint at colour-major position k (one coalesced head, 32 B of parameters)
@@ -1412,14 +1462,15 @@ struct LargeWorld::Impl {
     float *nx = nullptr, *ny = nullptr, *fric = nullptr;
     float *r1x = nullptr, *r1y = nullptr, *r2x = nullptr, *r2y = nullptr, *depth = nullptr, *odepth = nullptr;
     float *mn = nullptr, *mt = nullptr, *apn = nullptr, *apt = nullptr, *bias = nullptr;
-    float4* pk[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // Packed records
+    float *cpn = nullptr, *cpt = nullptr;  // compensation words (compensated mode)
+    float4* pk[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // Packed records
     float4* mom4 = nullptr;
     // the permutation's second copy of the fields it moves (swapped with the first after each step's permutation)
     uint32_t *ma2 = nullptr, *mb2 = nullptr, *mp02 = nullptr;
     uint8_t *mnp2 = nullptr, *mcol2 = nullptr;
     float *nx2 = nullptr, *ny2 = nullptr;
     float *r1x2 = nullptr, *r1y2 = nullptr, *r2x2 = nullptr, *r2y2 = nullptr, *depth2 = nullptr, *odepth2 = nullptr,
-          *apn2 = nullptr, *apt2 = nullptr;
+          *apn2 = nullptr, *apt2 = nullptr, *cpn2 = nullptr, *cpt2 = nullptr;
     // colouring
     uint32_t *adjl = nullptr, *prio = nullptr;
     uint32_t *jadj = nullptr, *jadjl = nullptr, *jprio = nullptr;  // the joints' own adjacency
@@ -1448,6 +1499,7 @@ struct LargeWorld::Impl {
     // warm starting: two tables (last frame's = wcur), sizes in slots
     unsigned long long* wkeys[2] = {nullptr, nullptr};
     float4* wvals[2] = {nullptr, nullptr};
+    float4* wcvals[2] = {nullptr, nullptr};  // compensated mode
     size_t wcap[2] = {0, 0};
     uint32_t whs[2] = {0, 0};
     int wcur = 0;
@@ -1462,13 +1514,14 @@ struct LargeWorld::Impl {
                       nx, ny, fric, r1x, r1y, r2x, r2y, depth, odepth, mn, mt, apn, apt, bias, adjl, prio,
                       jcol, jorder, cnt, entries, hist, tsum, dk, dc, dd, ma2, mb2, mp02, mnp2, mcol2, nx2, ny2,
                       r1x2, r1y2, r2x2, r2y2, depth2, odepth2, apn2, apt2, jadj, jadjl, jprio, npred, jnpred,
-                      preds, jpreds, pk[0], pk[1], pk[2], pk[3], pk[4], pk[5], pk[6], mom4, wl0, wl1, jwl0, jwl1,
-                      jhead, jprm_cm};
+                      preds, jpreds, pk[0], pk[1], pk[2], pk[3], pk[4], pk[5], pk[6], pk[7], mom4, wl0, wl1, jwl0,
+                      jwl1, jhead, jprm_cm, cpn, cpt, cpn2, cpt2};
         for (void* p : ps)
             if (p) cudaFree(p);
         for (int b = 0; b < 2; ++b) {
             if (wkeys[b]) cudaFree(wkeys[b]);
             if (wvals[b]) cudaFree(wvals[b]);
+            if (wcvals[b]) cudaFree(wcvals[b]);
         }
         if (h_cnt) cudaFreeHost(h_cnt);
     }
@@ -1492,6 +1545,8 @@ struct LargeWorld::Impl {
         s.nx = nx; s.ny = ny; s.fric = fric;
         s.r1x = r1x; s.r1y = r1y; s.r2x = r2x; s.r2y = r2y;
         s.depth = depth; s.odepth = odepth; s.mn = mn; s.mt = mt; s.apn = apn; s.apt = apt; s.bias = bias;
+        s.cpn = in.comp ? cpn : nullptr;
+        s.cpt = in.comp ? cpt : nullptr;
         return s;
     }
     // the permutation's destination: views() with the second copies
@@ -1500,13 +1555,15 @@ struct LargeWorld::Impl {
         s.ma = ma2; s.mb = mb2; s.mp0 = mp02; s.mnp = mnp2; s.mcol = mcol2; s.nx = nx2; s.ny = ny2;
         s.r1x = r1x2; s.r1y = r1y2; s.r2x = r2x2; s.r2y = r2y2; s.depth = depth2; s.odepth = odepth2;
         s.apn = apn2; s.apt = apt2;
+        s.cpn = in.comp ? cpn2 : nullptr;
+        s.cpt = in.comp ? cpt2 : nullptr;
         return s;
     }
     void swap_shadow() {
         std::swap(ma, ma2); std::swap(mb, mb2); std::swap(mp0, mp02); std::swap(mnp, mnp2); std::swap(mcol, mcol2);
         std::swap(nx, nx2); std::swap(ny, ny2); std::swap(r1x, r1x2); std::swap(r1y, r1y2); std::swap(r2x, r2x2);
         std::swap(r2y, r2y2); std::swap(depth, depth2); std::swap(odepth, odepth2); std::swap(apn, apn2);
-        std::swap(apt, apt2);
+        std::swap(apt, apt2); std::swap(cpn, cpn2); std::swap(cpt, cpt2);
     }
 };
 
@@ -1637,11 +1694,12 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
     LTRY(regrow(I.cap_m, (size_t)npairs + 1,
                 {LB(I.ma), LB(I.mb), LB(I.mp0), LB(I.corder), LB(I.mnp), LB(I.mcol), LB(I.nx), LB(I.ny),
                  LB(I.fric), LB(I.ma2), LB(I.mb2), LB(I.mp02), LB(I.mnp2), LB(I.mcol2), LB(I.nx2), LB(I.ny2),
-                 LB(I.pk[0]), LB(I.pk[1]), LB(I.pk[2]), LB(I.pk[3]), LB(I.pk[4]), LB(I.pk[5]), LB(I.pk[6])}));
+                 LB(I.pk[0]), LB(I.pk[1]), LB(I.pk[2]), LB(I.pk[3]), LB(I.pk[4]), LB(I.pk[5]), LB(I.pk[6]),
+                 LB(I.pk[7])}));
     LTRY(regrow(I.cap_pt, 2 * (size_t)npairs + 1,
                 {LB(I.r1x), LB(I.r1y), LB(I.r2x), LB(I.r2y), LB(I.depth), LB(I.odepth), LB(I.mn), LB(I.mt),
                  LB(I.apn), LB(I.apt), LB(I.bias), LB(I.r1x2), LB(I.r1y2), LB(I.r2x2), LB(I.r2y2), LB(I.depth2),
-                 LB(I.odepth2), LB(I.apn2), LB(I.apt2)}));
+                 LB(I.odepth2), LB(I.apn2), LB(I.apt2), LB(I.cpn), LB(I.cpt), LB(I.cpn2), LB(I.cpt2)}));
     A.s = I.views(in);
     I.npairs = npairs;
     A.nm = npairs;
@@ -1754,15 +1812,17 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
     }
     mark(3);
 
+    const uint32_t* wids = in.ids + in.base;
     if (in.warm && M && I.whs[I.wcur]) {
-        LAUNCH(lk_warm_load, blocks(M), I.views(in), M, I.wkeys[I.wcur], I.wvals[I.wcur], I.whs[I.wcur]);
+        LAUNCH(lk_warm_load, blocks(M), I.views(in), wids, M, I.wkeys[I.wcur], I.wvals[I.wcur],
+               in.comp ? I.wcvals[I.wcur] : nullptr, I.whs[I.wcur]);
     }
     // the table this call writes, sized for its manifolds (at most half full)
     const int wnext = 1 - I.wcur;
     uint32_t whs_next = 1;
     while (whs_next < 2u * M + 2u) whs_next <<= 1;
     if (in.warm) {
-        LTRY(regrow(I.wcap[wnext], whs_next, {LB(I.wkeys[wnext]), LB(I.wvals[wnext])}));
+        LTRY(regrow(I.wcap[wnext], whs_next, {LB(I.wkeys[wnext]), LB(I.wvals[wnext]), LB(I.wcvals[wnext])}));
     }
 
     // ---- substeps: the world's state changes from here on ----
@@ -1777,7 +1837,7 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
     S.pos64 = in.pos64;
     S.warm = in.warm;
     S.pk = Packed{I.pk[0], I.pk[1], I.pk[2], I.pk[3], I.pk[4], I.pk[5], I.pk[6],
-                  in.nj == 0 && !in.warm ? I.mom4 : nullptr};
+                  in.nj == 0 && !in.warm ? I.mom4 : nullptr, in.comp ? I.pk[7] : nullptr};
     const bool resident = use_resident_substeps(largest, I.cl_solve);
     // on the per-colour path, an iteration's contact colours may still share one cluster launch
     const bool contacts_clustered = !resident && M && I.coff.size() > 2 &&
@@ -1825,7 +1885,9 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
     if (!resident && M) LAUNCH(lk_unpack, blocks(M), S);
     if (in.warm) {  // this call's impulses become the next call's start
         LAUNCH(lk_warm_clear, blocks(whs_next), I.wkeys[wnext], whs_next);
-        if (M) LAUNCH(lk_warm_store, blocks(M), S.s, M, I.wkeys[wnext], I.wvals[wnext], whs_next);
+        if (M)
+            LAUNCH(lk_warm_store, blocks(M), S.s, wids, M, I.wkeys[wnext], I.wvals[wnext],
+                   in.comp ? I.wcvals[wnext] : nullptr, whs_next);
         I.whs[wnext] = whs_next;
         I.wcur = wnext;
     }
@@ -1850,15 +1912,31 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
     return 0;
 }
 
-int LargeWorld::seed_warm(const uint32_t* keys, const float4* vals, uint32_t hs, cudaStream_t st, std::string* msg) {
+int LargeWorld::seed_warm(const unsigned long long* keys, const float4* vals, const float4* cvals, uint32_t hs,
+                          cudaStream_t st, std::string* msg) {
     Impl& I = *impl;
-    LTRY(regrow(I.wcap[0], hs, {LB(I.wkeys[0]), LB(I.wvals[0])}));
+    LTRY(regrow(I.wcap[0], hs, {LB(I.wkeys[0]), LB(I.wvals[0]), LB(I.wcvals[0])}));
     lk_warm_clear<<<blocks(hs), LT, 0, st>>>(I.wkeys[0], hs);
-    lk_warm_copy<<<blocks(hs), LT, 0, st>>>(keys, vals, hs, I.wkeys[0], I.wvals[0], hs);
+    lk_warm_copy<<<blocks(hs), LT, 0, st>>>(keys, vals, cvals, hs, I.wkeys[0], I.wvals[0], I.wcvals[0], hs);
     LTRY(cudaStreamSynchronize(st));
     I.whs[0] = hs;
     I.whs[1] = 0;
     I.wcur = 0;
+    return 0;
+}
+
+int LargeWorld::read_warm(std::vector<unsigned long long>* keys, std::vector<float4>* vals,
+                          std::vector<float4>* cvals, cudaStream_t st, std::string* msg) {
+    Impl& I = *impl;
+    const uint32_t hs = I.whs[I.wcur];
+    keys->assign(hs, ~0ull);
+    vals->assign(hs, make_float4(0.f, 0.f, 0.f, 0.f));
+    cvals->assign(hs, make_float4(0.f, 0.f, 0.f, 0.f));
+    if (hs == 0) return 0;
+    LTRY(cudaStreamSynchronize(st));
+    LTRY(cudaMemcpy(keys->data(), I.wkeys[I.wcur], 8ull * hs, cudaMemcpyDeviceToHost));
+    LTRY(cudaMemcpy(vals->data(), I.wvals[I.wcur], 16ull * hs, cudaMemcpyDeviceToHost));
+    if (I.wcvals[I.wcur]) LTRY(cudaMemcpy(cvals->data(), I.wcvals[I.wcur], 16ull * hs, cudaMemcpyDeviceToHost));
     return 0;
 }
 

@@ -9,6 +9,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 #include "r2d_world.cuh"
 
@@ -37,6 +38,7 @@ struct LargeInputs {
     bool disc_rot;         // some joint reads disc orientations
     double* pos64;         // [3][NB] f64 pose (FP64-positions mode), else null
     bool warm;             // warm starting (the world keeps its impulses across calls)
+    bool comp;             // compensated accumulation of the impulses (r2d_accum.h)
     bool verbose;          // print each step's phase times and counts to stderr
     uint32_t* sleep;       // this world's still-frame counter (sleeping mode, r2d_sleep.h), else null
     uint32_t colour_round_limit;  // colouring rounds before R2D_ERR_TIMEOUT (0 = never reached)
@@ -63,9 +65,15 @@ public:
     // Kernel launches of the last step.
     uint32_t launches() const;
     // Warm starting: take over another table of last frame's impulses
-    // (keys / values of `hs` slots in device memory, the fused kernel's
-    // layout) when a world moves to this path.
-    int seed_warm(const uint32_t* keys, const float4* vals, uint32_t hs, cudaStream_t st, std::string* msg);
+    // (keys / values / compensation words (may be null) of `hs` slots in
+    // device memory, the fused kernel's layout) when a world moves to this
+    // path or its body store is replaced.
+    int seed_warm(const unsigned long long* keys, const float4* vals, const float4* cvals, uint32_t hs,
+                  cudaStream_t st, std::string* msg);
+    // This path's last-frame table, copied to the host: keys, values and
+    // compensation words (zeros when none are kept), `hs` slots.
+    int read_warm(std::vector<unsigned long long>* keys, std::vector<float4>* vals, std::vector<float4>* cvals,
+                  cudaStream_t st, std::string* msg);
 
     struct Impl;
 

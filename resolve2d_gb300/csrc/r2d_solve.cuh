@@ -8,6 +8,7 @@
 
 #include <stdint.h>
 
+#include "r2d_accum.h"
 #include "r2d_device.cuh"
 #include "r2d_world.cuh"
 
@@ -26,6 +27,7 @@ struct SWT {
     uint8_t *mnp, *mcol;
     float *nx, *ny, *fric;
     float *r1x, *r1y, *r2x, *r2y, *depth, *odepth, *mn, *mt, *apn, *apt, *bias;
+    float *cpn, *cpt;  // compensation words of apn / apt (compensated mode, r2d_accum.h), else null
 
     __device__ __forceinline__ float mass(uint32_t i) const { return __ldg(gmass + i); }
     __device__ __forceinline__ float inertia(uint32_t i) const { return __ldg(ginertia + i); }
@@ -46,6 +48,35 @@ struct SWT {
         }
     }
 };
+
+// The accumulation of calculateImpulses (collision.zig:182-190): point p's
+// normal impulse sum clamped at zero, its tangent sum to +-friction times
+// the normal sum; the changes go to the bodies.  Compensated mode keeps each
+// sum's rounding remainder in a second word (r2d_accum.h).
+template <class IDX>
+__device__ __forceinline__ void accumulate(const SWT<IDX>& s, uint32_t p, float pn, float pt, float fr,
+                                           float* applied_pn, float* applied_pt) {
+    if (s.cpn) {
+        float an = s.apn[p], cn = s.cpn[p], at = s.apt[p], ct = s.cpt[p];
+        *applied_pn = r2d_acc_add_max(&an, &cn, pn, 0.0f);
+        const float max_pt = fr * fabsf(an);
+        *applied_pt = r2d_acc_add_clamp(&at, &ct, pt, -max_pt, max_pt);
+        s.apn[p] = an;
+        s.cpn[p] = cn;
+        s.apt[p] = at;
+        s.cpt[p] = ct;
+        return;
+    }
+    const float acc = s.apn[p];
+    const float nacc = zmax(0.0f, acc + pn);
+    *applied_pn = nacc - acc;
+    s.apn[p] = nacc;
+    const float max_pt = fr * fabsf(nacc);
+    const float acct = s.apt[p];
+    const float nacct = zclamp(acct + pt, -max_pt, max_pt);
+    *applied_pt = nacct - acct;
+    s.apt[p] = nacct;
+}
 
 // CollisionManifold.calculateImpulses (collision.zig:135-218).  `warm`:
 // warm-starting mode, where an increment below MIN_MANIFOLD_IMPULSE is not
@@ -82,15 +113,8 @@ __device__ __forceinline__ void solve_contact(const SWT<IDX>& s, uint32_t m, boo
         if (!warm && pn < MIN_MANIFOLD_IMPULSE) continue;
         num = dot2(dv, t);
         const float pt = num * s.mt[p];
-        const float acc = s.apn[p];
-        const float nacc = zmax(0.0f, acc + pn);
-        const float applied_pn = nacc - acc;
-        s.apn[p] = nacc;
-        const float max_pt = fr * fabsf(nacc);
-        const float acct = s.apt[p];
-        const float nacct = zclamp(acct + pt, -max_pt, max_pt);
-        const float applied_pt = nacct - acct;
-        s.apt[p] = nacct;
+        float applied_pn, applied_pt;
+        accumulate(s, p, pn, pt, fr, &applied_pn, &applied_pt);
         const f2 dp = add2(scale2(n, applied_pn), scale2(t, applied_pt));
         if (!sa) {
             alp1 = sub2(alp1, dp);
@@ -156,15 +180,8 @@ __device__ __forceinline__ void solve_contact_lanes(const SWT<IDX>& s, uint32_t 
                 if (warm || !(pn < MIN_MANIFOLD_IMPULSE)) {  // as solve_contact's skip, NaN included
                     num = dot2(dv, t);
                     const float pt = num * s.mt[p];
-                    const float acc = s.apn[p];
-                    const float nacc = zmax(0.0f, acc + pn);
-                    const float applied_pn = nacc - acc;
-                    s.apn[p] = nacc;
-                    const float max_pt = s.fric[m] * fabsf(nacc);
-                    const float acct = s.apt[p];
-                    const float nacct = zclamp(acct + pt, -max_pt, max_pt);
-                    const float applied_pt = nacct - acct;
-                    s.apt[p] = nacct;
+                    float applied_pn, applied_pt;
+                    accumulate(s, p, pn, pt, s.fric[m], &applied_pn, &applied_pt);
                     dp = add2(scale2(n, applied_pn), scale2(t, applied_pt));
                     c1 = cross2(r1, dp);
                     c2 = cross2(r2, dp);
@@ -217,8 +234,10 @@ __device__ __forceinline__ void solve_contact_lanes(const SWT<IDX>& s, uint32_t 
 
 // ---- warm starting (an extension; off in reference mode) ----
 // Each world keeps last frame's accumulated impulses in an open-addressing
-// table in HBM: key (reference << 16 | incident), value (pn0, pt0, pn1, pt1).
-__device__ __forceinline__ uint32_t warm_hash(uint32_t k) {
+// table in HBM: key (reference id << 32 | incident id), the bodies' stable
+// ids, so the table outlives changes to the body store; value (pn0, pt0,
+// pn1, pt1), and in compensated mode their compensation words beside it.
+__host__ __device__ __forceinline__ uint32_t warm_hash(uint32_t k) {
     k ^= k >> 16;
     k *= 0x7FEB352Du;
     k ^= k >> 15;
@@ -228,7 +247,7 @@ __device__ __forceinline__ uint32_t warm_hash(uint32_t k) {
 }
 
 // 64-bit keys (the grid pipeline: reference << 32 | incident)
-__device__ __forceinline__ uint32_t warm_hash(unsigned long long k) {
+__host__ __device__ __forceinline__ uint32_t warm_hash(unsigned long long k) {
     return warm_hash((uint32_t)k ^ (warm_hash((uint32_t)(k >> 32)) * 0x9E3779B1u));
 }
 
@@ -246,18 +265,22 @@ __device__ __forceinline__ int warm_find(const K* __restrict__ keys, uint32_t hs
     return -1;
 }
 
-// Inserts a key that is not in the table yet (keys are unique per frame);
-// the table holds at most half its slots, so a free slot is always found.
+// Claims the slot of a key that is not in the table yet (keys are unique
+// per frame) and returns it; the table holds at most half its slots, so a
+// free slot is always found (-1 only for a full table).
 template <class K>
-__device__ __forceinline__ void warm_insert(K* keys, float4* vals, uint32_t hs, K key, float4 v) {
+__device__ __forceinline__ int warm_claim(K* keys, uint32_t hs, K key) {
     const uint32_t mask = hs - 1u, h = warm_hash(key);
     for (uint32_t probe = 0; probe < hs; ++probe) {
         const uint32_t slot = (h + probe) & mask;
-        if (atomicCAS(&keys[slot], ~K(0), key) == ~K(0)) {
-            vals[slot] = v;
-            return;
-        }
+        if (atomicCAS(&keys[slot], ~K(0), key) == ~K(0)) return (int)slot;
     }
+    return -1;
+}
+
+// The warm-start key of a manifold: its bodies' stable ids.
+__device__ __forceinline__ unsigned long long warm_key_ids(uint32_t ref_id, uint32_t inc_id) {
+    return ((unsigned long long)ref_id << 32) | inc_id;
 }
 
 // Applies a manifold's (warm-started) accumulated impulses to its bodies,
@@ -277,6 +300,10 @@ __device__ __forceinline__ void warm_apply_contact(const SWT<IDX>& s, uint32_t m
         if (s.bias[p] < 0.0f) {
             s.apn[p] = 0.f;
             s.apt[p] = 0.f;
+            if (s.cpn) {
+                s.cpn[p] = 0.f;
+                s.cpt[p] = 0.f;
+            }
             continue;
         }
         f2 r1, r2;

@@ -64,12 +64,13 @@ struct Layout {
     // manifolds + points (narrowphase .. end) -- aliased by the broadphase scratch
     uint32_t ma, mb, mp0, mnp, mcol, nx, ny, fric;
     uint32_t r1x, r1y, r2x, r2y, depth, odepth, mn, mt, apn, apt, bias;
+    uint32_t cpn, cpt;  // compensation words (compensated mode; offset 0 = absent)
     // broadphase scratch (inside the manifold region)
     uint32_t ax, ay, ahw, ahh, rx0, ry0, rx1, ry1, fx0, fy0, fx1, fy1, bcnt, ebucket, ebody, eslot, sbody, table, hset;
     // colouring scratch: sort keys, per-body colour masks
     uint32_t skey, cmask;
     // optional arrays (offset 0 = absent)
-    bool has_depth, has_pos0, has_prev;
+    bool has_depth, has_pos0, has_prev, has_comp;
     // orders
     uint32_t corder, coff, jorder, joff, jcol;
     // pairs
@@ -88,8 +89,10 @@ __host__ __device__ inline uint32_t r2d_align(uint32_t x, uint32_t a) { return (
 //   pos0:  keep frame-start positions (lean with more than one substep;
 //          with one substep the positions do not move before integration)
 //   prev:  keep each body's previous-substep angle (full layout, debug taps)
+//   comp:  keep a compensation word beside each accumulated impulse
+//          (R2D_FLAG_COMPENSATED)
 struct LayoutOpts {
-    bool lean, depth, pos0, prev;
+    bool lean, depth, pos0, prev, comp;
 };
 
 __host__ __device__ inline Layout make_layout(const Caps& c, const LayoutOpts& f) {
@@ -104,6 +107,7 @@ __host__ __device__ inline Layout make_layout(const Caps& c, const LayoutOpts& f
     L.has_depth = f.depth || !f.lean;
     L.has_pos0 = f.lean && f.pos0;
     L.has_prev = f.prev || !f.lean;
+    L.has_comp = f.comp;
     L.px = take(nb4); L.py = take(nb4); L.ang = take(nb4);
     L.mx = take(nb4); L.my = take(nb4); L.L = take(nb4);
     L.inv_m = take(nb4); L.inv_i = take(nb4);
@@ -129,9 +133,13 @@ __host__ __device__ inline Layout make_layout(const Caps& c, const LayoutOpts& f
     }
     if (L.has_depth) L.depth = take(np4);
     L.bias = take(np4);
-    // mn .. apt are contiguous: the colouring sorts its keys there
+    // mn .. apt (.. cpt) are contiguous: the colouring sorts its keys there
     L.mn = take(np4); L.mt = take(np4);
     L.apn = take(np4); L.apt = take(np4);
+    if (L.has_comp) {
+        L.cpn = take(np4);
+        L.cpt = take(np4);
+    }
     const uint32_t xend_m = o;
     o = xbase;
     L.ax = take(nb4); L.ay = take(nb4); L.ahw = take(nb4); L.ahh = take(nb4);
@@ -160,10 +168,20 @@ __host__ __device__ inline Layout make_layout(const Caps& c, const LayoutOpts& f
     const uint32_t ncon = c.nm > c.nj ? c.nm : c.nj;
     uint32_t n2 = 1;
     while (n2 < ncon) n2 <<= 1;
-    L.skey = (8 * n2 <= 4 * np4) ? L.mn : take(8 * n2);
+    L.skey = (8 * n2 <= (L.has_comp ? 6u : 4u) * np4) ? L.mn : take(8 * n2);
     L.total = o;
     return L;
 }
+
+// Every fused world's warm-start tables: world w owns slots
+// [off[w], off[w] + 2 * hs[w]) (two tables of hs[w] slots, a power of two).
+struct WarmTables {
+    unsigned long long* keys;  // (ref id << 32 | inc id); all ones = empty
+    float4* vals;              // (pn0, pt0, pn1, pt1)
+    float4* cvals;             // their compensation words, or null
+    const uint32_t* off;       // [nworlds]
+    const uint32_t* hs;        // [nworlds]
+};
 
 struct DebugOut {
     uint32_t cap;        // manifolds per world slot (0 = no dump)
@@ -211,8 +229,9 @@ struct StepParams {
     const uint32_t* call_counter;  // ... or, when set, *call_counter - 1 (bumped on the device per call)
     unsigned long long* timers;  // [nworlds][PHASE_SLOTS] when built with R2D_PHASE_TIMERS
     double* pos64;               // [3][nbodies] x, y, angle in f64 (FP64-positions mode), else null
-    uint32_t* warm_keys;         // warm-start tables (WorldDesc::warm_off), else null
-    float4* warm_vals;
+    unsigned long long* warm_keys;  // warm-start tables (WorldDesc::warm_off): (ref id << 32 | inc id), else null
+    float4* warm_vals;           // (pn0, pt0, pn1, pt1)
+    float4* warm_cvals;          // their compensation words (compensated mode), else null
     uint32_t* warm_cur;          // [nworlds] which of a world's two tables holds last frame
     uint32_t* sleep;             // [nworlds] consecutive still frames (sleeping mode, r2d_sleep.h), else null
     const ExtIO* ext;            // this call's host rows (device copy, read per call), else null

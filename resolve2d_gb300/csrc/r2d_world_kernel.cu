@@ -271,13 +271,19 @@ __device__ bool colour_greedy_sorted(uint32_t count, uint32_t n, Ends ends, Mix 
 
 using SW = SWT<uint16_t>;
 
+// Bodies with more spatial-hash entries than this are emitted by the whole
+// block (up to MAX_BIG_BODIES of them; more fall back to their own thread).
+constexpr uint32_t BIG_BODY_ENTRIES = 16, MAX_BIG_BODIES = 16;
+
 // Register budget per thread: low enough that several worlds share an SM
 // (the kernel is latency-bound; concurrency hides it).
 #ifndef R2D_REG_TARGET
 #define R2D_REG_TARGET 96
 #endif
+// One-warp CTAs keep 96 registers: below that they spill.
+constexpr int reg_target_for(int nt) { return nt <= 32 ? 96 : R2D_REG_TARGET; }
 constexpr int min_blocks_for(int nt) {
-    return 65536 / (nt * R2D_REG_TARGET) > 0 ? 65536 / (nt * R2D_REG_TARGET) : 1;
+    return 65536 / (nt * reg_target_for(nt)) > 0 ? 65536 / (nt * reg_target_for(nt)) : 1;
 }
 
 template <int NT, bool LEAN>
@@ -290,6 +296,8 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
     __shared__ uint32_t s_capbits;
     __shared__ uint32_t s_cnt[4];  // pairs, manifolds, points
     __shared__ unsigned long long s_wsum64[32];
+    __shared__ uint32_t s_big[MAX_BIG_BODIES];  // bodies whose cell entries the whole block emits
+    __shared__ uint32_t s_nbig;
 
     const int tid = threadIdx.x;
     if (blockIdx.x >= P.nlist) return;
@@ -377,6 +385,8 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
     s.r1x = SMF(Lo.r1x); s.r1y = SMF(Lo.r1y); s.r2x = SMF(Lo.r2x); s.r2y = SMF(Lo.r2y);
     s.depth = SMF(Lo.depth); s.odepth = SMF(Lo.odepth); s.mn = SMF(Lo.mn); s.mt = SMF(Lo.mt);
     s.apn = SMF(Lo.apn); s.apt = SMF(Lo.apt); s.bias = SMF(Lo.bias);
+    s.cpn = Lo.has_comp ? SMF(Lo.cpn) : nullptr;
+    s.cpt = Lo.has_comp ? SMF(Lo.cpt) : nullptr;
 
     float *ax = SMF(Lo.ax), *ay = SMF(Lo.ay), *ahw = SMF(Lo.ahw), *ahh = SMF(Lo.ahh);
     int32_t *rx0 = SMI32(Lo.rx0), *ry0 = SMI32(Lo.ry0), *rx1 = SMI32(Lo.rx1), *ry1 = SMI32(Lo.ry1);
@@ -486,7 +496,21 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
             goto fail;
         }
         const BucketMod bmod = {wd.bucket_recip, T};
+        // A body's entries, row by row over its cells; a body with many
+        // (a static ground or wall spans dozens of cells) is left to the
+        // whole block below, so that no thread walks a long row alone while
+        // the others wait at the barrier.
+        if (tid == 0) s_nbig = 0u;
+        __syncthreads();
         for (uint32_t i = tid; i < n; i += NT) {
+            const uint32_t wx = (uint32_t)(fx1[i] - fx0[i] + 1);
+            if (fx1[i] >= fx0[i] && fy1[i] >= fy0[i] && wx * (uint32_t)(fy1[i] - fy0[i] + 1) > BIG_BODY_ENTRIES) {
+                const uint32_t q = atomicAdd(&s_nbig, 1u);
+                if (q < MAX_BIG_BODIES) {
+                    s_big[q] = i;
+                    continue;
+                }
+            }
             uint32_t k = bcnt[i];
             for (int32_t yi = fy0[i]; yi <= fy1[i]; ++yi)
                 for (int32_t xi = fx0[i]; xi <= fx1[i]; ++xi) {
@@ -496,6 +520,18 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
                     atomicAdd(&table[bk], 1u);
                     ++k;
                 }
+        }
+        __syncthreads();
+        const uint32_t nbig = min(s_nbig, (uint32_t)MAX_BIG_BODIES);
+        for (uint32_t q = 0; q < nbig; ++q) {
+            const uint32_t i = s_big[q], k0 = bcnt[i];
+            const uint32_t wx = (uint32_t)(fx1[i] - fx0[i] + 1), cnt = wx * (uint32_t)(fy1[i] - fy0[i] + 1);
+            for (uint32_t t = tid; t < cnt; t += NT) {  // entry t: row t / wx, column t % wx
+                const uint32_t bk = cell_bucket(fx0[i] + (int32_t)(t % wx), fy0[i] + (int32_t)(t / wx), bmod);
+                ebucket[k0 + t] = bk;
+                ebody[k0 + t] = (uint16_t)i;
+                atomicAdd(&table[bk], 1u);
+            }
         }
         __syncthreads();
         block_scan_excl<NT>(table, T, s_wsum);  // table[b] = first slot of bucket b
@@ -803,18 +839,23 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
         for (uint32_t p = tid; p < s_cnt[2] && p < C.npt; p += NT) {
             s.apn[p] = 0.f;
             s.apt[p] = 0.f;
+            if (Lo.has_comp) {
+                s.cpn[p] = 0.f;
+                s.cpt[p] = 0.f;
+            }
         }
         const bool warm = P.warm_keys != nullptr;
         const uint32_t wcur = warm ? P.warm_cur[w] : 0u;
         if (warm) {
             // a manifold of last frame's pair starts from its impulses
             __syncthreads();
-            const uint32_t* keys = P.warm_keys + wd.warm_off + wcur * wd.warm_hs;
-            const float4* vals = P.warm_vals + wd.warm_off + wcur * wd.warm_hs;
+            const size_t at = (size_t)wd.warm_off + (size_t)wcur * wd.warm_hs;
+            const unsigned long long* keys = P.warm_keys + at;
             for (uint32_t m = tid; m < M; m += NT) {
-                const int slot = warm_find(keys, wd.warm_hs, ((uint32_t)s.ma[m] << 16) | s.mb[m]);
+                const unsigned long long key = warm_key_ids(__ldg(P.ids + base + s.ma[m]), __ldg(P.ids + base + s.mb[m]));
+                const int slot = warm_find(keys, wd.warm_hs, key);
                 if (slot < 0) continue;
-                const float4 v = vals[slot];
+                const float4 v = P.warm_vals[at + slot];
                 const uint32_t p0 = s.mp0[m], np = s.mnp[m];
                 if (np > 0) {
                     s.apn[p0] = v.x;
@@ -823,6 +864,17 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
                 if (np > 1) {
                     s.apn[p0 + 1] = v.z;
                     s.apt[p0 + 1] = v.w;
+                }
+                if (Lo.has_comp && P.warm_cvals) {
+                    const float4 c = P.warm_cvals[at + slot];
+                    if (np > 0) {
+                        s.cpn[p0] = c.x;
+                        s.cpt[p0] = c.y;
+                    }
+                    if (np > 1) {
+                        s.cpn[p0 + 1] = c.z;
+                        s.cpt[p0 + 1] = c.w;
+                    }
                 }
             }
         }
@@ -984,15 +1036,22 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
         if (warm) {
             // this frame's impulses go to the world's other table, which then
             // becomes the one the next frame reads
-            uint32_t* keys = P.warm_keys + wd.warm_off + (1u - wcur) * wd.warm_hs;
-            float4* vals = P.warm_vals + wd.warm_off + (1u - wcur) * wd.warm_hs;
-            for (uint32_t q = tid; q < wd.warm_hs; q += NT) keys[q] = 0xFFFFFFFFu;
+            const size_t at = (size_t)wd.warm_off + (size_t)(1u - wcur) * wd.warm_hs;
+            unsigned long long* keys = P.warm_keys + at;
+            for (uint32_t q = tid; q < wd.warm_hs; q += NT) keys[q] = ~0ull;
             __syncthreads();
             for (uint32_t m = tid; m < M; m += NT) {
                 const uint32_t p0 = s.mp0[m], np = s.mnp[m];
-                const float4 v = make_float4(np > 0 ? s.apn[p0] : 0.f, np > 0 ? s.apt[p0] : 0.f,
-                                             np > 1 ? s.apn[p0 + 1] : 0.f, np > 1 ? s.apt[p0 + 1] : 0.f);
-                warm_insert(keys, vals, wd.warm_hs, ((uint32_t)s.ma[m] << 16) | s.mb[m], v);
+                const unsigned long long key = warm_key_ids(__ldg(P.ids + base + s.ma[m]), __ldg(P.ids + base + s.mb[m]));
+                const int slot = warm_claim(keys, wd.warm_hs, key);
+                if (slot < 0) continue;
+                P.warm_vals[at + slot] = make_float4(np > 0 ? s.apn[p0] : 0.f, np > 0 ? s.apt[p0] : 0.f,
+                                                     np > 1 ? s.apn[p0 + 1] : 0.f, np > 1 ? s.apt[p0 + 1] : 0.f);
+                if (P.warm_cvals)
+                    P.warm_cvals[at + slot] =
+                        Lo.has_comp ? make_float4(np > 0 ? s.cpn[p0] : 0.f, np > 0 ? s.cpt[p0] : 0.f,
+                                                  np > 1 ? s.cpn[p0 + 1] : 0.f, np > 1 ? s.cpt[p0 + 1] : 0.f)
+                                    : make_float4(0.f, 0.f, 0.f, 0.f);
             }
             __syncthreads();
             if (tid == 0) P.warm_cur[w] = 1u - wcur;
@@ -1150,31 +1209,33 @@ cudaError_t allow_world_step_smem(int bytes) {
 
 // Moves each world's last-frame warm-start table into a new layout (one CTA
 // per world): entries of the old table `old_cur[w]` are inserted into table 0
-// of the new one.  Old offsets/sizes of 0 slots mean "no table".
-__global__ void migrate_warm_kernel(const uint32_t* old_keys, const float4* old_vals, const uint32_t* old_off,
-                                    const uint32_t* old_hs, const uint32_t* old_cur, uint32_t* new_keys,
-                                    float4* new_vals, const uint32_t* new_off, const uint32_t* new_hs) {
+// of the new one, at most half its slots.  Old sizes of 0 slots mean "no
+// table"; compensation words move when both layouts keep them.
+__global__ void migrate_warm_kernel(WarmTables o, const uint32_t* old_cur, WarmTables n) {
     const uint32_t w = blockIdx.x;
-    const uint32_t nh = new_hs[w], oh = old_hs ? old_hs[w] : 0u;
-    uint32_t* nk = new_keys + new_off[w];
-    float4* nv = new_vals + new_off[w];
-    for (uint32_t q = threadIdx.x; q < 2u * nh; q += blockDim.x) nk[q] = 0xFFFFFFFFu;
+    const uint32_t nh = n.hs[w], oh = o.hs ? o.hs[w] : 0u;
+    unsigned long long* nk = n.keys + n.off[w];
+    for (uint32_t q = threadIdx.x; q < 2u * nh; q += blockDim.x) nk[q] = ~0ull;
     __syncthreads();
     if (!oh || !nh) return;
-    const uint32_t base = old_off[w] + old_cur[w] * oh;
+    const size_t base = (size_t)o.off[w] + (size_t)old_cur[w] * oh;
+    __shared__ uint32_t taken;
+    if (threadIdx.x == 0) taken = 0u;
+    __syncthreads();
     for (uint32_t q = threadIdx.x; q < oh; q += blockDim.x) {
-        const uint32_t key = old_keys[base + q];
-        if (key != 0xFFFFFFFFu) warm_insert(nk, nv, nh, key, old_vals[base + q]);
+        const unsigned long long key = o.keys[base + q];
+        if (key == ~0ull || atomicAdd(&taken, 1u) >= nh / 2u) continue;
+        const int slot = warm_claim(nk, nh, key);
+        if (slot < 0) continue;
+        n.vals[n.off[w] + slot] = o.vals[base + q];
+        if (n.cvals) n.cvals[n.off[w] + slot] = o.cvals ? o.cvals[base + q] : make_float4(0.f, 0.f, 0.f, 0.f);
     }
 }
 
-cudaError_t launch_migrate_warm(uint32_t nworlds, const uint32_t* old_keys, const float4* old_vals,
-                                const uint32_t* old_off, const uint32_t* old_hs, const uint32_t* old_cur,
-                                uint32_t* new_keys, float4* new_vals, const uint32_t* new_off, const uint32_t* new_hs,
-                                cudaStream_t stream) {
+cudaError_t launch_migrate_warm(uint32_t nworlds, const WarmTables& old_t, const uint32_t* old_cur,
+                                const WarmTables& new_t, cudaStream_t stream) {
     if (nworlds == 0) return cudaSuccess;
-    migrate_warm_kernel<<<nworlds, 256, 0, stream>>>(old_keys, old_vals, old_off, old_hs, old_cur, new_keys, new_vals,
-                                                     new_off, new_hs);
+    migrate_warm_kernel<<<nworlds, 256, 0, stream>>>(old_t, old_cur, new_t);
     return cudaGetLastError();
 }
 

@@ -28,14 +28,14 @@ def _out_rows(a: np.ndarray, k: int, n: int) -> np.ndarray:
 
 def _config(cell: float, mult: int, debug: bool, stream, capacity_scale: float = 0.0,
             grid: bool = False, fp64_positions: bool = False, warm_start: bool = False,
-            sleep: bool = False) -> N.Config:
+            sleep: bool = False, compensated: bool = False) -> N.Config:
     cfg = N.Config()
     cfg.capacity_scale = float(capacity_scale)
     cfg.spatialhash_cell_width = float(cell)
     cfg.spatialhash_table_size_mult = int(mult)
     cfg.flags = ((N.FLAG_DEBUG_TAPS if debug else 0) | (N.FLAG_GRID_PIPELINE if grid else 0)
                  | (N.FLAG_FP64_POSITIONS if fp64_positions else 0) | (N.FLAG_WARM_START if warm_start else 0)
-                 | (N.FLAG_SLEEP if sleep else 0))
+                 | (N.FLAG_SLEEP if sleep else 0) | (N.FLAG_COMPENSATED if compensated else 0))
     cfg.stream = int(stream) if stream else None
     return cfg
 
@@ -46,10 +46,11 @@ class World:
 
     def __init__(self, cell: float = 0.0, mult: int = 0, debug: bool = False, stream=None, capacity_scale: float = 0.0,
                  grid: bool = False, fp64_positions: bool = False, warm_start: bool = False,
-                 sleep: bool = False):
+                 sleep: bool = False, compensated: bool = False):
         self._lib = N.load()
         self._h = C.c_void_p()
-        cfg = _config(cell, mult, debug, stream, capacity_scale, grid, fp64_positions, warm_start, sleep)
+        cfg = _config(cell, mult, debug, stream, capacity_scale, grid, fp64_positions, warm_start, sleep,
+                      compensated)
         N.check(self._lib.r2d_solver_create(C.byref(cfg), C.byref(self._h)), "r2d_solver_create")
         self.n = 0
 
@@ -184,10 +185,11 @@ class Batch:
 
     def __init__(self, cell: float = 0.0, mult: int = 0, debug: bool = False, stream=None, capacity_scale: float = 0.0,
                  grid: bool = False, fp64_positions: bool = False, warm_start: bool = False,
-                 sleep: bool = False):
+                 sleep: bool = False, compensated: bool = False):
         self._lib = N.load()
         self._h = C.c_void_p()
-        cfg = _config(cell, mult, debug, stream, capacity_scale, grid, fp64_positions, warm_start, sleep)
+        cfg = _config(cell, mult, debug, stream, capacity_scale, grid, fp64_positions, warm_start, sleep,
+                      compensated)
         N.check(self._lib.r2d_batch_create(C.byref(cfg), C.byref(self._h)), "r2d_batch_create")
         self.n = 0
         self.nworlds = 0

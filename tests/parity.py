@@ -73,7 +73,7 @@ def assert_pairs_equal(got: np.ndarray, want: np.ndarray, what: str = "pairs"):
     np.testing.assert_array_equal(np.asarray(got, np.uint32).reshape(-1, 2), np.asarray(want, np.uint32).reshape(-1, 2))
 
 
-def run_pair(sc, steps, check_every=1, debug=True, sub_steps=None, iters=None, warm=False, **world_kw):
+def run_pair(sc, steps, check_every=1, debug=True, sub_steps=None, iters=None, warm=False, comp=False, **world_kw):
     """Step scene `sc` on the GPU (one world through the C ABI) and on the
     oracle in colour-major order; compare state, manifolds and colours every
     `check_every` steps.  Returns (world, oracle), or (None, None) when the
@@ -84,9 +84,10 @@ def run_pair(sc, steps, check_every=1, debug=True, sub_steps=None, iters=None, w
 
     S = sc.sub_steps if sub_steps is None else sub_steps
     I = sc.iters if iters is None else iters
-    w = World.from_scene(sc, debug=debug, warm_start=warm, **world_kw)
+    w = World.from_scene(sc, debug=debug, warm_start=warm, compensated=comp, **world_kw)
     o = Oracle.from_scene(sc)
     o.set_warm_start(warm)
+    o.set_compensated(comp)
     o.record_pairs(debug)
     assert_state_equal(w.read_state(), o.state(), "initial state")
     for s in range(steps):

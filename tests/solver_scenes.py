@@ -7,8 +7,9 @@ import math
 
 import numpy as np
 
-from oracle import ORDER_COLOUR, _p
+from oracle import ORDER_COLOUR, Oracle, _p
 from parity import assert_state_equal
+from resolve2d_gb300 import _native as N
 from resolve2d_gb300 import scenes as S
 from resolve2d_gb300.solver import BodyOptions, Density, DiscOptions, Mass, Parameters, RectangleOptions
 
@@ -114,3 +115,105 @@ def step_both(s, o, frames, what):
         assert o.process(DT, SUB, ITERS, ORDER_COLOUR) == 0
         if f % 5 == 4 or f == frames - 1:
             assert_state_equal(s.read_state(), o.state(), f"{what}, frame {f + 1}")
+
+
+class OracleBackend:
+    """engine.World's interface over the oracle, for host-only tests.  Every
+    setter rebuilds the oracle from what it was given, carrying the current
+    state across, and in warm-start mode last frame's impulses (keyed by body
+    ids), as the engine keeps them across body uploads."""
+
+    def __init__(self, warm_start=False, compensated=False, carry_warm=True):
+        self.warm_start, self.compensated, self.carry_warm = warm_start, compensated, carry_warm
+        self.o = None
+        self.bodies = None
+        self.g = []
+        self.joints = (np.zeros(0, np.uint8), np.zeros(0, np.uint32), np.zeros(0, np.uint32),
+                       np.zeros((0, S.JOINT_PARAMS), np.float32))
+        self.x = np.zeros((0, 2), np.uint32)
+        self.calls = []
+
+    def _build(self, state, init_aabb):
+        ids, kind, props = self.bodies
+        n = ids.shape[0]
+        opt = np.zeros((S.NOPT, n), np.float32)
+        opt[S.POS_X], opt[S.POS_Y], opt[S.ANGLE] = state[S.S_POS_X], state[S.S_POS_Y], state[S.S_ANGLE]
+        opt[S.MU], opt[S.MASS_PROP] = props[S.P_MU], props[S.P_MASS]
+        opt[S.DIM0], opt[S.DIM1] = props[S.P_DIM0], props[S.P_DIM1]
+        o = Oracle()
+        k = np.ascontiguousarray(kind & 3, np.uint8)
+        o.lib.r2o_add_bodies(o.h, n, _p(np.ascontiguousarray(ids, np.uint32), C.c_uint32), _p(k, C.c_uint8),
+                             _p(opt, C.c_float))
+        np.testing.assert_array_equal(o.props(), props)  # mass given: the oracle derives the same inertia
+        st = o.state()
+        if init_aabb:
+            st[: S.S_AABB_X] = state[: S.S_AABB_X]
+        else:
+            st = np.array(state, np.float32)
+        o.set_state(np.ascontiguousarray(st))
+        for g in self.g:
+            o.lib.r2o_add_gravity(o.h, g)
+        t, a, b, prm = self.joints
+        if t.size:
+            o.lib.r2o_add_joints(o.h, t.shape[0], _p(t, C.c_uint8), _p(a, C.c_uint32), _p(b, C.c_uint32),
+                                 _p(prm, C.c_float))
+        o.nj = int(t.size)
+        for x, y in self.x:
+            o.lib.r2o_exclude_pair(o.h, int(x), int(y))
+        o.set_warm_start(self.warm_start)
+        o.set_compensated(self.compensated)
+        if self.warm_start and self.carry_warm and self.o is not None:
+            o.take_warm(self.o)
+        self.o = o
+
+    def _rebuild(self):
+        if self.bodies is not None:
+            self._build(self.o.state(), False)
+
+    def set_bodies(self, ids, kind, props, state, init_aabb):
+        self.calls.append(("set_bodies", int(ids.shape[0]), bool(init_aabb)))
+        self.bodies = (np.array(ids, np.uint32), np.array(kind, np.uint8), np.array(props, np.float32))
+        self._build(np.asarray(state, np.float32), init_aabb)
+
+    def set_gravity(self, g):
+        self.calls.append(("set_gravity", len(g)))
+        self.g = [float(v) for v in g]
+        self._rebuild()
+
+    def set_joints(self, t, a, b, prm):
+        self.calls.append(("set_joints", len(t)))
+        self.joints = (np.array(t, np.uint8), np.array(a, np.uint32), np.array(b, np.uint32),
+                       np.ascontiguousarray(prm, np.float32).reshape(-1, S.JOINT_PARAMS))
+        self._rebuild()
+
+    def set_exclusions(self, pairs):
+        self.calls.append(("set_exclusions", len(pairs)))
+        self.x = np.array(pairs, np.uint32).reshape(-1, 2)
+        self._rebuild()
+
+    def write_state(self, state):
+        self.calls.append(("write_state",))
+        self.o.set_state(np.ascontiguousarray(state, np.float32))
+
+    def read_state(self):
+        return self.o.state()
+
+    def process(self, dt, sub, iters):
+        self.calls.append(("process",))
+        have = set(self.bodies[0].tolist())
+        t, a, b, _ = self.joints
+        two = (t == S.JOINT_DISTANCE) | (t == S.JOINT_OFFSET_DISTANCE)
+        if any(x not in have for x in a.tolist()) or any(y not in have for y in b[two].tolist()):
+            raise N.R2DError(-2, "r2d_solver_process", "a joint names an unknown body id")
+        assert self.o.process(dt, sub, iters, ORDER_COLOUR) == 0
+
+    def manifolds(self):
+        k, d = self.o.manifolds()
+        c, _ = self.o.colours()
+        return k, d, c[: k.shape[0]]
+
+    def sync(self):
+        pass
+
+    def close(self):
+        self.o = None

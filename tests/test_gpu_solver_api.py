@@ -7,6 +7,7 @@ is stepped on the GPU through ``engine.World``, and every five frames it must
 equal the same scene given to the oracle, bit for bit.
 """
 
+import numpy as np
 import pytest
 
 from oracle import Oracle
@@ -67,3 +68,40 @@ def run_batched_reference_scenes():
 
 def test_reference_scenes_batched_on_the_gpu_equal_the_oracle():
     run_batched_reference_scenes()
+
+
+def test_warm_start_survives_an_addition_and_a_swap_remove():
+    """Warm starting through the reference-style API: the engine keys last
+    frame's impulses by body id, so a body added mid-run and a swapRemove
+    (which moves the last body into the hole) keep every surviving pair's
+    impulses.  The GPU equals the oracle stand-in that carries its table
+    across the rebuild, and differs from one that drops it."""
+    from solver_scenes import DT, ITERS, OracleBackend
+    from resolve2d_gb300.solver import BodyOptions, Density, DiscOptions
+
+    from parity import assert_state_equal
+
+    specs = body_specs(12)
+    gpu = Solver.init(4.0, 2, warm_start=True)
+    ref = Solver(backend=lambda: OracleBackend(warm_start=True))
+    cold = Solver(backend=lambda: OracleBackend(warm_start=True, carry_warm=False))
+    solvers = (gpu, ref, cold)
+    for s in solvers:
+        build(s, specs)
+        s.entityFactory().makeDownwardsGravity(9.81)
+    for _ in range(60):
+        for s in solvers:
+            s.process(DT, 1, ITERS)
+    assert_state_equal(gpu.read_state(), ref.read_state(), "before the changes")
+    for s in solvers:
+        s.entityFactory().makeDiscBody(BodyOptions(pos=(40.0, 5.0), mass_prop=Density(1.0)), DiscOptions(radius=0.5))
+        s.removeRigidBody(5)
+    assert gpu.ids().tolist() == ref.ids().tolist()
+    for f in range(20):
+        for s in solvers:
+            s.process(DT, 1, ITERS)
+        if f in (0, 19):
+            assert_state_equal(gpu.read_state(), ref.read_state(), f"frame {f + 1} after the changes")
+    assert not np.array_equal(gpu.read_state(), cold.read_state())
+    for s in solvers:
+        s.deinit()

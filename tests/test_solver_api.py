@@ -21,104 +21,9 @@ from resolve2d_gb300 import _native as N
 from resolve2d_gb300 import scenes as S
 from resolve2d_gb300.solver import BodyOptions, DiscOptions, InvalidRigidBodyId, Mass, NoSuchIdExists, Parameters, Solver
 from solver_scenes import (
-    DT, ITERS, JOINTS, add_joints_to_oracle, add_to_oracle, body_specs, build, make_joints, spec_arrays, step_both,
+    DT, ITERS, JOINTS, OracleBackend, add_joints_to_oracle, add_to_oracle, body_specs, build, make_joints, spec_arrays,
+    step_both,
 )
-
-
-class OracleBackend:
-    """engine.World's interface over the oracle, for host-only tests.  Every
-    setter rebuilds the oracle from what it was given, carrying the current
-    state across."""
-
-    def __init__(self):
-        self.o = None
-        self.bodies = None
-        self.g = []
-        self.joints = (np.zeros(0, np.uint8), np.zeros(0, np.uint32), np.zeros(0, np.uint32),
-                       np.zeros((0, S.JOINT_PARAMS), np.float32))
-        self.x = np.zeros((0, 2), np.uint32)
-        self.calls = []
-
-    def _build(self, state, init_aabb):
-        ids, kind, props = self.bodies
-        n = ids.shape[0]
-        opt = np.zeros((S.NOPT, n), np.float32)
-        opt[S.POS_X], opt[S.POS_Y], opt[S.ANGLE] = state[S.S_POS_X], state[S.S_POS_Y], state[S.S_ANGLE]
-        opt[S.MU], opt[S.MASS_PROP] = props[S.P_MU], props[S.P_MASS]
-        opt[S.DIM0], opt[S.DIM1] = props[S.P_DIM0], props[S.P_DIM1]
-        o = Oracle()
-        k = np.ascontiguousarray(kind & 3, np.uint8)
-        o.lib.r2o_add_bodies(o.h, n, _p(np.ascontiguousarray(ids, np.uint32), C.c_uint32), _p(k, C.c_uint8),
-                             _p(opt, C.c_float))
-        np.testing.assert_array_equal(o.props(), props)  # mass given: the oracle derives the same inertia
-        st = o.state()
-        if init_aabb:
-            st[: S.S_AABB_X] = state[: S.S_AABB_X]
-        else:
-            st = np.array(state, np.float32)
-        o.set_state(np.ascontiguousarray(st))
-        for g in self.g:
-            o.lib.r2o_add_gravity(o.h, g)
-        t, a, b, prm = self.joints
-        if t.size:
-            o.lib.r2o_add_joints(o.h, t.shape[0], _p(t, C.c_uint8), _p(a, C.c_uint32), _p(b, C.c_uint32),
-                                 _p(prm, C.c_float))
-        o.nj = int(t.size)
-        for x, y in self.x:
-            o.lib.r2o_exclude_pair(o.h, int(x), int(y))
-        self.o = o
-
-    def _rebuild(self):
-        if self.bodies is not None:
-            self._build(self.o.state(), False)
-
-    def set_bodies(self, ids, kind, props, state, init_aabb):
-        self.calls.append(("set_bodies", int(ids.shape[0]), bool(init_aabb)))
-        self.bodies = (np.array(ids, np.uint32), np.array(kind, np.uint8), np.array(props, np.float32))
-        self._build(np.asarray(state, np.float32), init_aabb)
-
-    def set_gravity(self, g):
-        self.calls.append(("set_gravity", len(g)))
-        self.g = [float(v) for v in g]
-        self._rebuild()
-
-    def set_joints(self, t, a, b, prm):
-        self.calls.append(("set_joints", len(t)))
-        self.joints = (np.array(t, np.uint8), np.array(a, np.uint32), np.array(b, np.uint32),
-                       np.ascontiguousarray(prm, np.float32).reshape(-1, S.JOINT_PARAMS))
-        self._rebuild()
-
-    def set_exclusions(self, pairs):
-        self.calls.append(("set_exclusions", len(pairs)))
-        self.x = np.array(pairs, np.uint32).reshape(-1, 2)
-        self._rebuild()
-
-    def write_state(self, state):
-        self.calls.append(("write_state",))
-        self.o.set_state(np.ascontiguousarray(state, np.float32))
-
-    def read_state(self):
-        return self.o.state()
-
-    def process(self, dt, sub, iters):
-        self.calls.append(("process",))
-        have = set(self.bodies[0].tolist())
-        t, a, b, _ = self.joints
-        two = (t == S.JOINT_DISTANCE) | (t == S.JOINT_OFFSET_DISTANCE)
-        if any(x not in have for x in a.tolist()) or any(y not in have for y in b[two].tolist()):
-            raise N.R2DError(-2, "r2d_solver_process", "a joint names an unknown body id")
-        assert self.o.process(dt, sub, iters, ORDER_COLOUR) == 0
-
-    def manifolds(self):
-        k, d = self.o.manifolds()
-        c, _ = self.o.colours()
-        return k, d, c[: k.shape[0]]
-
-    def sync(self):
-        pass
-
-    def close(self):
-        self.o = None
 
 
 def test_factory_scene_steps_like_the_same_scene_given_to_the_oracle():
@@ -406,3 +311,25 @@ def test_batch_arrays_refuse_what_a_batch_cannot_hold():
     t.entityFactory().makeDownwardsGravity(1.0)
     with pytest.raises(ValueError, match="gravity"):
         batch_arrays([t])
+
+
+def test_warm_table_carries_across_a_rebuild_on_the_cpu():
+    """The oracle stand-in's warm carry (what the GPU test of the same name
+    compares against) changes the trajectory: a body added and a swapRemove
+    mid-run, with and without last frame's impulses."""
+    from resolve2d_gb300.solver import BodyOptions, Density, DiscOptions
+
+    specs = body_specs(12)
+    runs = []
+    for carry in (True, False):
+        s = Solver(backend=lambda carry=carry: OracleBackend(warm_start=True, carry_warm=carry))
+        build(s, specs)
+        s.entityFactory().makeDownwardsGravity(9.81)
+        for _ in range(60):
+            s.process(DT, 1, ITERS)
+        s.entityFactory().makeDiscBody(BodyOptions(pos=(40.0, 5.0), mass_prop=Density(1.0)), DiscOptions(radius=0.5))
+        s.removeRigidBody(5)
+        for _ in range(5):
+            s.process(DT, 1, ITERS)
+        runs.append(s.read_state())
+    assert not np.array_equal(runs[0], runs[1])
