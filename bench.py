@@ -66,6 +66,10 @@ os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 SETTLE_STEPS = 300
 BYTES_READ = 77   # pos 8, angle 4, momentum 8, ang. momentum 4, force+torque 12, AABB 16, mass/inertia/mu/dims 20, kind 1, id 4
 BYTES_WRITE = 40  # pos 8, angle 4, momentum 8, ang. momentum 4, AABB 16
+# The compulsory-traffic model of the hot-path scope (pose, momenta, mass,
+# inertia, mu, shape and type read; pose and momenta written), without the
+# stored AABB and the force rows this layout keeps in HBM.
+BYTES_MODEL_72 = 72
 METRIC = "body-steps/sec on 1 GB300, batched FP32 vs plain, at stated pos error vs FP64"
 HEADLINE = "config3: 4096 worlds, counts log-uniform [16,512], dt 1/60, 8 iterations, settled 300 steps"
 # single large worlds: (scene name, description, settle steps)
@@ -114,6 +118,55 @@ def rank_scene(rank: int, world: int, per_rank: int = 4096):
         return scenes.config3(nworlds=per_rank)
     full = scenes.config3(nworlds=per_rank * world)
     return full.select(balanced_shards(np.diff(full.body_off), world)[rank])
+
+
+def headline_config(bodies: int, worlds: int, ranks: int, rank0_bodies: int) -> dict:
+    """The workload both arms print (the driver compares them key for key)."""
+    return {"workload": HEADLINE, "bodies": int(bodies), "worlds": int(worlds),
+            "settle": f"{SETTLE_STEPS} steps in the GPU's colour-major constraint order before timing; the CPU "
+                      "arm settles on the oracle, bit-identical to the GPU's settled state",
+            "l2": "GPU arm: flushed between timed steps (256 MiB write outside the events)",
+            "parallelism": (f"worlds dealt to {ranks} GPUs by body count, {rank0_bodies} bodies on rank 0"
+                            if ranks > 1 else "one GPU")}
+
+
+def spawn_command(n: int, argv: list[str], port: int) -> list[str]:
+    """This script under torch.distributed.run with n local ranks (one GPU
+    each), as `bench.py --gpus n` starts itself when no launcher set
+    WORLD_SIZE."""
+    return [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+            "--master-addr", "127.0.0.1", f"--master-port={port}", os.path.abspath(__file__), *argv]
+
+
+def free_port() -> int:
+    import socket
+
+    with socket.socket() as so:
+        so.bind(("127.0.0.1", 0))
+        return so.getsockname()[1]
+
+
+def dry_run(args):
+    """--dry-run: the rank logic alone, on the host (gloo): every rank builds
+    its share of the global batch and the ranks reduce their body counts and
+    a stand-in time as the timed run does; rank 0 prints the totals.  No
+    GPU is touched; it checks a multi-rank launch before spending GPUs."""
+    rank, world, _ = dist_env()
+    import torch.distributed as dist
+
+    if world > 1:
+        dist.init_process_group("gloo")
+    try:
+        sc = rank_scene(rank, world, per_rank=args.dry_run_worlds)
+        t = max_over_ranks(1.0 + 0.5 * rank, device="cpu")
+        nb_all = int(round(sum_over_ranks(sc.nbodies, device="cpu")))
+        nw_all = int(round(sum_over_ranks(sc.nworlds, device="cpu")))
+        if rank == 0:
+            print(json.dumps({"dry_run": True, "n_gpus": world, "worlds": nw_all, "bodies": nb_all,
+                              "rank0_bodies": sc.nbodies, "slowest_rank_time": t}), flush=True)
+    finally:
+        if world > 1:
+            dist.destroy_process_group()
 
 
 def dist_env():
@@ -206,9 +259,10 @@ def _with_constraints(sc) -> bool:
     return bool(sc.jtype.size or sc.xpairs.size)
 
 
-def _solver_run(sc, state, steps):
+def _solver_run(sc, state, steps, order=None):
     """(seconds, final state) of `steps` oracle steps of a one-world scene with
-    its joints and exclusions, on one thread, in the reference's order."""
+    its joints and exclusions, on one thread, in the reference's order (or
+    `order`)."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle as O
 
@@ -219,21 +273,22 @@ def _solver_run(sc, state, steps):
         o.set_state(np.ascontiguousarray(state, np.float32))
     t0 = time.perf_counter()
     for _ in range(steps):
-        st = o.process(sc.dt, sc.sub_steps, sc.iters, O.ORDER_REFERENCE)
+        st = o.process(sc.dt, sc.sub_steps, sc.iters, O.ORDER_REFERENCE if order is None else order)
         if st:
             raise RuntimeError(f"the oracle returned status {st}")
     return time.perf_counter() - t0, o.state()
 
 
 def settle_scene(sc, steps):
-    """Advance the scene `steps` steps on the CPU oracle (all host threads), in
-    the reference's own constraint order."""
+    """Advance the scene `steps` steps on the CPU oracle (all host threads) in
+    the GPU's colour-major constraint order, which the GPU reproduces bit for
+    bit: both arms then time the same settled state."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle as O
 
     if _with_constraints(sc):
-        return _solver_run(sc, None, steps)[1]
-    _, state, st = O.batch_run(sc, steps, cpu_threads(), order=O.ORDER_REFERENCE)
+        return _solver_run(sc, None, steps, order=O.ORDER_COLOUR)[1]
+    _, state, st = O.batch_run(sc, steps, cpu_threads(), order=O.ORDER_COLOUR)
     if st:
         raise RuntimeError(f"the oracle returned status {st}")
     return state.reshape(13, sc.nbodies)
@@ -296,9 +351,16 @@ def run_reference(args):
     if args.workload in LARGE:
         sc = getattr(scenes, args.workload)()
         workload, settle = LARGE[args.workload]
+        config = {"workload": workload, "bodies": sc.nbodies, "worlds": sc.nworlds}
     else:
+        # the GPU arm's workload: N x 4,096 worlds under N ranks; the CPU arm
+        # times the first 4,096 of them (the same generator and seed), a
+        # bounded sample with the same per-world distribution
         sc = scenes.config3(seed=3)
-        workload, settle = HEADLINE, SETTLE_STEPS
+        settle = SETTLE_STEPS
+        full_bodies = sc.nbodies if world == 1 else scenes.config3(nworlds=4096 * world).nbodies
+        rank0 = rank_scene(0, world).nbodies if world > 1 else sc.nbodies
+        config = headline_config(full_bodies, 4096 * world, world, rank0)
     threads = cpu_threads()
     state = settle_scene(sc, settle)
     # each step: one full pass over all 4,096 worlds
@@ -312,12 +374,12 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded)",
-        "config": {"workload": workload, "bodies": sc.nbodies, "worlds": sc.nworlds},
+        "config": config,
         "cpu_baseline": {"value": v, "unit": "body-steps/s", "cores": 1 if _with_constraints(sc) else threads,
                          "kind": "port",
-                         "sample": f"all {sc.nworlds} worlds x {args.steps} steps from the settled state; "
-                                   "C++ restatement of Solver.process in the reference's own constraint order "
-                                   "(Zig toolchain absent)"},
+                         "sample": f"{sc.nworlds} worlds ({sc.nbodies} bodies) x {args.steps} steps from the settled "
+                                   "state; C++ restatement of Solver.process in the reference's own constraint "
+                                   "order (Zig toolchain absent)"},
         "e2e": {"value": v, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     if sc.nworlds > 1:
@@ -420,6 +482,47 @@ def run_large(args):
     print(json.dumps(line), flush=True)
 
 
+def plain_drop_in(name: str, stream, no_cpu: bool) -> dict:
+    """One large world (config 1 or 2) through the single-world entry points
+    (r2d_solver_*), the drop-in for Solver.process, which steps it on the
+    grid pipeline: settled as in --workload, then 10 steps timed by CUDA
+    events on the library's stream (the pipeline's host round trips inside
+    them), L2 flushed between steps.  Beside it, one step of the CPU oracle
+    from the same settled state on one core, in the reference's order."""
+    import torch
+    from resolve2d_gb300 import scenes
+    from resolve2d_gb300.engine import World
+
+    sc = getattr(scenes, name)()
+    desc, settle = LARGE[name]
+    w = World.from_scene(sc, stream=stream.cuda_stream)
+    for _ in range(settle):
+        w.process(sc.dt, sc.sub_steps, sc.iters)
+    w.sync()
+    settled = w.read_state()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    steps = 10
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    torch.cuda.synchronize()
+    for a, b in ev:
+        flush.zero_()
+        a.record(stream)
+        w.process(sc.dt, sc.sub_steps, sc.iters)
+        b.record(stream)
+    w.sync()
+    torch.cuda.synchronize()
+    secs = sum(a.elapsed_time(b) for a, b in ev) / 1e3
+    out = {"workload": desc, "bodies": sc.nbodies, "joints": int(sc.jtype.size), "steps": steps,
+           "ms_per_step": 1e3 * secs / steps, "value": sc.nbodies * steps / secs, "unit": "body-steps/s",
+           "call": "r2d_solver_process (grid pipeline)", "launches_per_step": w.launches_per_step()}
+    w.close()
+    if not no_cpu:
+        cpu = oracle_time(sc, settled, 1, 1)
+        out["cpu_one_core"] = {"value": sc.nbodies / cpu, "unit": "body-steps/s", "seconds": cpu,
+                               "sample": "one step from the settled state on one core, reference order"}
+    return out
+
+
 def arg_parser() -> argparse.ArgumentParser:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -433,11 +536,24 @@ def arg_parser() -> argparse.ArgumentParser:
                     help="worlds stepped one per launch for the plain-path comparison")
     ap.add_argument("--workload", default="config3", choices=["config3", *LARGE],
                     help="config3 (the headline batch) or one large world on the grid pipeline")
+    ap.add_argument("--no-plain-drop-in", action="store_true",
+                    help="skip the config 1 / config 2 single-world lines inside the headline line")
+    ap.add_argument("--dry-run", action="store_true",
+                    help="the multi-rank logic alone on the host (gloo), no GPU: prints the ranks' totals")
+    ap.add_argument("--dry-run-worlds", type=int, default=64, help="worlds per rank in --dry-run")
     return ap
 
 
 def main():
     args = arg_parser().parse_args()
+    rank, world, _ = dist_env()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # one process per GPU: start this script under torch.distributed.run
+        sys.exit(subprocess.call(spawn_command(args.gpus, sys.argv[1:], free_port())))
+    if "WORLD_SIZE" in os.environ and world != args.gpus:
+        raise SystemExit(f"--gpus {args.gpus} but the launcher started {world} ranks")
+    if args.dry_run:
+        return dry_run(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.workload in LARGE:
@@ -579,13 +695,10 @@ def main():
         "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * step_s, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-        "config": {"workload": HEADLINE, "bodies": nb_all, "worlds": nw_all,
-                   "l2": "flushed between timed steps (256 MiB write outside the events)",
-                   "tiles": "threads per CTA of each size class autotuned on the settled worlds"
+        "config": headline_config(nb_all, nw_all, world, nb),
+        "tuning": {"tiles": "threads per CTA of each size class autotuned on the settled worlds"
                    if not args.no_autotune else "default threads per size class",
-                   "cuda_device_max_connections": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS"),
-                   "parallelism": (f"worlds dealt to {world} GPUs by body count, {nb} bodies on rank 0"
-                                   if world > 1 else "one GPU")},
+                   "cuda_device_max_connections": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS")},
         "gpu_launches": launches,
         "wall_s_timed_loop": wall,
         "e2e": {"value": e2e_v, "unit": "body-steps/s", "h2d_bytes_per_step": 12 * nb_all,
@@ -601,10 +714,15 @@ def main():
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_src,
                      "traffic": None if traffic is None else traffic * nb,
-                     "bytes_per_body_step": BYTES_READ + BYTES_WRITE},
+                     "bytes_per_body_step": BYTES_READ + BYTES_WRITE,
+                     "model_72": {"bytes_per_body_step": BYTES_MODEL_72,
+                                  "achieved": BYTES_MODEL_72 * nb / step_s / 1e9,
+                                  "frac": BYTES_MODEL_72 * nb / step_s / 1e9 / peak}},
         "clocks": clk,
     }
     line["pos_error_vs_fp64"] = stated_pos_error()
+    if rank == 0 and world == 1 and not args.no_plain_drop_in:
+        line["plain_drop_in"] = {w: plain_drop_in(w, stream, args.no_cpu_baseline) for w in LARGE}
     if rank == 0 and not args.no_cpu_baseline:
         threads = cpu_threads()
         one = oracle_time(sc, settled, 1, threads)

@@ -51,6 +51,8 @@ _SIG = {
     "r2o_get_colours": ([_P, C.c_uint32, _u32p, C.c_uint32, _u32p], C.c_uint32),
     "r2o_set_record_pairs": ([_P, C.c_int], None),
     "r2o_get_pairs": ([_P, C.c_uint32, _u32p], C.c_uint32),
+    "r2o_batch_run_checkpoints": ([C.c_int, C.c_uint32, _u32p, _u32p, _u8p, _f32p, _f32p, C.c_float, C.c_uint32,
+                                   C.c_uint32, C.c_int, C.c_int, C.c_int, C.c_uint32, _u32p, _f64p], C.c_int),
     "r2o_nmath_kat": ([_f32p, _f32p, _f32p], None),
     "r2o_aabb_intersects": ([C.c_float] * 8, C.c_int),
     "r2o_sincosf": ([C.c_uint32, _f32p, _f32p, _f32p], None),
@@ -262,6 +264,32 @@ def batch_run(sc, steps: int, nthreads: int, precision: int = 32, order: int = O
                              int(steps), int(order), int(nthreads), None if sin is None else _p(sin, C.c_float),
                              _p(state, C.c_float), C.byref(status))
     return float(secs), state, int(status.value)
+
+
+# modes of batch_checkpoints
+BR_WARM, BR_COMPENSATED, BR_PERTURB_ULP, BR_PERTURB_F32_ULP = 1, 2, 4, 8
+
+
+def batch_checkpoints(sc, checks, nthreads: int, precision: int = 64, order: int = ORDER_COLOUR, flags: int = 0):
+    """Every world of a bodies-only scene stepped from its start on host
+    threads in the mode `flags` (BR_*: warm starting, compensated sums, the
+    dynamic bodies' x nudged up by one ulp of the precision or one f32 ulp);
+    returns (f64 state [len(checks)][13][n] at each step count, status)."""
+    if sc.jtype.size or sc.xpairs.size:
+        raise ValueError("batch_checkpoints steps bodies only")
+    lib = load()
+    off = np.ascontiguousarray(sc.body_off, np.uint32)
+    ids = np.ascontiguousarray(sc.ids, np.uint32)
+    kind = np.ascontiguousarray(sc.kind, np.uint8)
+    opt = np.ascontiguousarray(sc.opt, np.float32)
+    grav = np.ascontiguousarray(sc.gravity, np.float32)
+    ck = np.ascontiguousarray(sorted(int(c) for c in checks), np.uint32)
+    out = np.zeros((ck.shape[0], NSTATE, sc.nbodies), np.float64)
+    st = lib.r2o_batch_run_checkpoints(precision, sc.nworlds, _p(off, C.c_uint32), _p(ids, C.c_uint32),
+                                       _p(kind, C.c_uint8), _p(opt, C.c_float), _p(grav, C.c_float), float(sc.dt),
+                                       sc.sub_steps, sc.iters, int(order), int(nthreads), int(flags), ck.shape[0],
+                                       _p(ck, C.c_uint32), _p(out, C.c_double))
+    return out, int(st)
 
 
 def nmath_kat(a, b) -> np.ndarray:

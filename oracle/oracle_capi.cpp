@@ -172,6 +172,24 @@ void get_manifolds(const Solver<R>& s, uint32_t* keys, float* data) {
 
 }  // namespace
 
+/* Flags of r2o_batch_run_checkpoints. */
+enum { BR_WARM = 1, BR_COMPENSATED = 2, BR_PERTURB_ULP = 4, BR_PERTURB_F32_ULP = 8 };
+
+/* Perturbs every dynamic body's x by one ulp of the solver's own precision
+ * (BR_PERTURB_ULP) or by one f32 ulp (BR_PERTURB_F32_ULP), upwards. */
+template <class R>
+void perturb_x(Solver<R>& s, int flags) {
+    for (auto& b : s.bodies) {
+        if (b.is_static) continue;
+        if (flags & BR_PERTURB_F32_ULP) {
+            const float x = (float)b.props.pos.x;
+            b.props.pos.x = R(std::nextafter(x, std::numeric_limits<float>::infinity()));
+        } else if (flags & BR_PERTURB_ULP) {
+            b.props.pos.x = std::nextafter(b.props.pos.x, std::numeric_limits<R>::infinity());
+        }
+    }
+}
+
 extern "C" {
 
 void* r2o_create(int precision) {
@@ -435,6 +453,56 @@ double r2o_batch_run(int precision, uint32_t nworlds, const uint32_t* body_off, 
     }
     if (status_out) *status_out = first_err.load();
     return std::chrono::duration<double>(t1 - t0).count();
+}
+
+/* Every world of a scene stepped on host threads from its initial state
+ * (r2o_batch_run without state_in), in the given mode (flags above), and
+ * its full state kept in f64 at each of the ncheck ascending step counts:
+ * out [ncheck][NSTATE][ntot].  Returns the first non-zero status. */
+int r2o_batch_run_checkpoints(int precision, uint32_t nworlds, const uint32_t* body_off, const uint32_t* ids,
+                              const uint8_t* kind, const float* opt_all, const float* gravity, float dt,
+                              uint32_t sub_steps, uint32_t iters, int order, int nthreads, int flags,
+                              uint32_t ncheck, const uint32_t* checks, double* out) {
+    const uint32_t ntot = body_off[nworlds];
+    std::atomic<uint32_t> next(0);
+    std::atomic<int> first_err(0);
+    auto work = [&]() {
+        for (;;) {
+            const uint32_t w = next.fetch_add(1);
+            if (w >= nworlds) break;
+            const uint32_t b0 = body_off[w], n = body_off[w + 1] - b0;
+            std::vector<float> opt((size_t)NOPT * n);
+            for (int f = 0; f < NOPT; ++f)
+                for (uint32_t i = 0; i < n; ++i) opt[(size_t)f * n + i] = opt_all[(size_t)f * ntot + b0 + i];
+            std::unique_ptr<Handle> h((Handle*)r2o_create(precision));
+            r2o_add_bodies(h.get(), n, ids + b0, kind + b0, opt.data());
+            if (gravity[w] != 0.f) r2o_add_gravity(h.get(), gravity[w]);
+            DISPATCH(h, (S.warm_start = (flags & BR_WARM) != 0, S.compensated = (flags & BR_COMPENSATED) != 0,
+                         perturb_x(S, flags)));
+            std::vector<double> st((size_t)NSTATE * n);
+            uint32_t done = 0;
+            for (uint32_t c = 0; c < ncheck; ++c) {
+                for (; done < checks[c]; ++done) {
+                    const int e = r2o_process(h.get(), dt, sub_steps, iters, order);
+                    if (e != 0) {
+                        int z = 0;
+                        first_err.compare_exchange_strong(z, e);
+                        break;
+                    }
+                }
+                r2o_get_state_f64(h.get(), st.data());
+                for (int f = 0; f < NSTATE; ++f)
+                    for (uint32_t i = 0; i < n; ++i)
+                        out[((size_t)c * NSTATE + f) * ntot + b0 + i] = st[(size_t)f * n + i];
+            }
+        }
+    };
+    if (nthreads < 1) nthreads = 1;
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nthreads; ++t) pool.emplace_back(work);
+    work();
+    for (auto& t : pool) t.join();
+    return first_err.load();
 }
 
 /* Known-answer hooks for the reference's own unit tests:

@@ -5,11 +5,25 @@ batched distribution, seed 4, 3,600 steps at dt 1/60).
         [--checkpoints 1,10,60,120,300,600] [--oracle-worlds 256]
         [--out profiles/precision_config4.json]
 
-Two GPU modes step every world from the same start: f32 throughout (the
-reference's arithmetic, bit-identical to the f32 oracle) and f32 with the
-pose integrated in f64 (R2D_FLAG_FP64_POSITIONS).  The first
-`--oracle-worlds` worlds are also stepped by the FP64 oracle (the same
-algorithm in double) on the host threads.  Reported, at the checkpoints:
+GPU modes step every world from the same start:
+
+* f32: the reference's arithmetic, bit-identical to the f32 oracle;
+* f32+f64 pose: the pose integrated in f64 (R2D_FLAG_FP64_POSITIONS);
+* f32 warm: warm starting (R2D_FLAG_WARM_START);
+* f32 warm+Kahan: warm starting with compensated impulse sums
+  (R2D_FLAG_COMPENSATED);
+* f32 warm+Kahan+f64 pose: all three.
+
+The first `--oracle-worlds` worlds are also stepped by the FP64 oracle (the
+same algorithm in double) on the host threads, in reference mode and in warm
+mode; each GPU mode is compared with the FP64 run of its own algorithm.
+The chaos floor: the FP64 oracle run again with every dynamic body's x
+nudged up by one f64 ulp (and, separately, by one f32 ulp: the size of one
+f32 rounding) at step 0, compared with the unperturbed FP64 run.  A
+difference that small reaching the same error as f32 does means the error
+is the scenes' sensitivity to any perturbation, not the f32 arithmetic.
+
+Reported, at the checkpoints:
 
 * position error against the FP64 oracle, in body radii (a disc's radius,
   half the shorter side of a rectangle): max, p99, median;
@@ -107,19 +121,37 @@ def main():
     res = {"workload": f"config4: {sc.nworlds} worlds, {sc.nbodies} bodies, seed 4, dt 1/60, {a.steps} steps",
            "oracle_worlds": a.oracle_worlds, "oracle_bodies": sub.nbodies, "checkpoints": {}}
 
-    # FP64 oracle on the subset; each checkpoint is its own run from the
-    # start (the oracle returns f32 state, which must not be fed back)
+    # FP64 oracle runs of the subset, every checkpoint's state in f64
     t0 = time.time()
     ref = {}
-    for c in checks:
-        _, state, st = O.batch_run(sub, c, a.threads, precision=64)
-        assert st == 0, st
-        ref[c] = state
+    for name, flags in (("fp64", 0), ("fp64 warm", O.BR_WARM),
+                        ("fp64 +1 ulp", O.BR_PERTURB_ULP), ("fp64 +1 f32 ulp", O.BR_PERTURB_F32_ULP),
+                        ("fp64 warm +1 ulp", O.BR_WARM | O.BR_PERTURB_ULP)):
+        out, st = O.batch_checkpoints(sub, checks, a.threads, precision=64, flags=flags)
+        assert st == 0, (name, st)
+        ref[name] = {c: out[k] for k, c in enumerate(checks)}
     res["oracle_seconds"] = time.time() - t0
+    # the chaos floor: perturbed FP64 against FP64
+    for name, base in (("fp64 +1 ulp", "fp64"), ("fp64 +1 f32 ulp", "fp64"), ("fp64 warm +1 ulp", "fp64 warm")):
+        for c in checks:
+            p_a, e_a = world_energy(sub, ref[name][c], sprops, sub.gravity)
+            p_b, e_b = world_energy(sub, ref[base][c], sprops, sub.gravity)
+            res["checkpoints"].setdefault(str(c), {})[name] = {
+                "pos_error_vs_fp64_radii": pos_error(sub, ref[name][c], ref[base][c]),
+                "momentum_vs_fp64_rel": rel(p_a, p_b),
+                "energy_vs_fp64_rel": rel(e_a, e_b),
+            }
 
-    for mode, fp64 in (("f32", False), ("f32+f64 pose", True)):
-        b = Batch.from_scene(sc, fp64_positions=fp64)
-        bsub = Batch.from_scene(sub, fp64_positions=fp64, debug=True)
+    modes = (("f32", {}, "fp64"),
+             ("f32+f64 pose", {"fp64_positions": True}, "fp64"),
+             ("f32 warm", {"warm_start": True}, "fp64 warm"),
+             ("f32 warm+Kahan", {"warm_start": True, "compensated": True}, "fp64 warm"),
+             ("f32 warm+Kahan+f64 pose", {"warm_start": True, "compensated": True, "fp64_positions": True},
+              "fp64 warm"))
+    for mode, kw, base in modes:
+        fp64 = kw.get("fp64_positions", False)
+        b = Batch.from_scene(sc, **kw)
+        bsub = Batch.from_scene(sub, debug=True, **kw)
         s0 = b.read_state()
         _, e0 = world_energy(sc, s0, props, sc.gravity)
         done = 0
@@ -136,12 +168,13 @@ def main():
             if fp64:
                 ss = ss.astype(np.float64)
                 ss[:3] = bsub.read_positions_f64()
-            p_all, e_all = world_energy(sc, st, props, sc.gravity)
+            _, e_all = world_energy(sc, st, props, sc.gravity)
             p_sub, e_sub = world_energy(sub, ss, sprops, sub.gravity)
-            p_ref, e_ref = world_energy(sub, ref[c], sprops, sub.gravity)
+            p_ref, e_ref = world_energy(sub, ref[base][c], sprops, sub.gravity)
             entry = res["checkpoints"].setdefault(str(c), {})
             entry[mode] = {
-                "pos_error_vs_fp64_radii": pos_error(sub, ss, ref[c]),
+                "against": base,
+                "pos_error_vs_fp64_radii": pos_error(sub, ss, ref[base][c]),
                 "momentum_vs_fp64_rel": rel(p_sub, p_ref),
                 "energy_vs_fp64_rel": rel(e_sub, e_ref),
                 "energy_drift_all_worlds": rel(e_all, e0),

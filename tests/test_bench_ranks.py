@@ -77,11 +77,12 @@ def test_one_process_needs_no_group():
 
 
 def test_the_cpu_baseline_steps_a_scene_with_its_joints():
-    """A scene with joints and exclusions is settled and timed through a whole
+    """A scene with joints and exclusions is settled (in the GPU's colour-major
+    order, which the GPU reproduces bit for bit) and timed through a whole
     oracle solver, never by the body-only batch runner."""
     sys.path.insert(0, REPO)
     import bench
-    from oracle import ORDER_REFERENCE, Oracle
+    from oracle import ORDER_COLOUR, Oracle
     from resolve2d_gb300 import scenes
 
     sc = scenes.config2(n_bodies=1200, n_chains=20, chain_links=10, n_motors=10, box_w=120.0, box_h=40.0)
@@ -89,6 +90,46 @@ def test_the_cpu_baseline_steps_a_scene_with_its_joints():
     got = bench.settle_scene(sc, 3)
     o = Oracle.from_scene(sc)
     for _ in range(3):
-        assert o.process(sc.dt, sc.sub_steps, sc.iters, ORDER_REFERENCE) == 0
+        assert o.process(sc.dt, sc.sub_steps, sc.iters, ORDER_COLOUR) == 0
     np.testing.assert_array_equal(got, o.state())
     assert bench.oracle_time(sc, got, 1, 4) > 0.0
+
+
+def test_bench_gpus_n_starts_n_ranks_itself():
+    """`bench.py --gpus 2` without a launcher starts itself under
+    torch.distributed.run with two local ranks; with --dry-run the ranks run
+    the rank logic over gloo and rank 0 alone prints the totals."""
+    import json
+    import subprocess
+
+    env = dict(os.environ)
+    for k in ("RANK", "WORLD_SIZE", "LOCAL_RANK", "MASTER_ADDR", "MASTER_PORT"):
+        env.pop(k, None)
+    r = subprocess.run([sys.executable, os.path.join(REPO, "bench.py"), "--gpus", "2", "--dry-run",
+                        "--dry-run-worlds", str(PER_RANK)], env=env, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    lines = [json.loads(x) for x in r.stdout.splitlines() if x.startswith("{")]
+    assert len(lines) == 1
+    from resolve2d_gb300 import scenes
+
+    full = scenes.config3(nworlds=2 * PER_RANK)
+    assert lines[0]["n_gpus"] == 2 and lines[0]["worlds"] == full.nworlds and lines[0]["bodies"] == full.nbodies
+    assert lines[0]["slowest_rank_time"] == 1.5
+
+
+def test_bench_refuses_a_rank_count_other_than_gpus():
+    import subprocess
+
+    env = dict(os.environ, WORLD_SIZE="3", RANK="0", LOCAL_RANK="0")
+    r = subprocess.run([sys.executable, os.path.join(REPO, "bench.py"), "--gpus", "2", "--dry-run"], env=env,
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode != 0 and "--gpus 2" in (r.stdout + r.stderr)
+
+
+def test_both_arms_print_one_config():
+    sys.path.insert(0, REPO)
+    import bench
+
+    a = bench.headline_config(589_055, 4096, 1, 589_055)
+    b = bench.headline_config(589_055, 4096, 1, 589_055)
+    assert a == b and {"workload", "bodies", "worlds", "l2", "parallelism"} <= set(a)
