@@ -232,6 +232,10 @@ struct Engine {
     uint32_t g_sub = 0, g_iters = 0;
     bool use_graph = true;
     uint32_t colour_round_limit = 0;  // R2D_COLOUR_ROUND_LIMIT (0 = the colouring's own bound)
+    // Tuning: the binning grid's cell as a multiple of the largest dynamic
+    // body's diameter (R2D_FINE_CELL_SCALE, default 1).  Pairs do not depend
+    // on it; candidates and entries per body do.
+    float fine_scale = 1.0f;
 
     ~Engine() {
         large.clear();
@@ -288,6 +292,8 @@ struct Engine {
         // makes its one bounded device loop give up (R2D_ERR_TIMEOUT).
         const char* rl = getenv("R2D_COLOUR_ROUND_LIMIT");
         colour_round_limit = rl ? (uint32_t)strtoul(rl, nullptr, 10) : 0u;
+        const char* fs = getenv("R2D_FINE_CELL_SCALE");
+        if (fs && strtof(fs, nullptr) > 0.f) fine_scale = strtof(fs, nullptr);
         CUDA_TRY(dalloc(d_call, 1));
         CUDA_TRY(dalloc(d_ext, 1));
         CUDA_TRY(cudaMemsetAsync(d_ext, 0, sizeof(ExtIO), stream));
@@ -748,7 +754,7 @@ struct Engine {
             if (dia > dmax) dmax = dia;
         }
         if (!(dmax > 0.f)) return cell;
-        return std::min(cell, std::max(cell / 16.0f, dmax + 0.05f));
+        return std::min(cell, std::max(cell / 16.0f, fine_scale * (dmax + 0.05f)));
     }
 
     // Expected binning-grid cells of world w: a dynamic body covers 1-4
