@@ -156,6 +156,27 @@ template <int NT, class Mix, class Tie>
 __device__ void priority_order(uint32_t count, Mix mix, Tie tie, unsigned long long* skey, uint32_t* bucket,
                                uint32_t* wsum) {
     const int tid = threadIdx.x;
+    if (count <= 128u && count <= (uint32_t)NT) {
+        // Few constraints: each thread ranks its own against all the others
+        // (the keys are distinct), one pass and two barriers instead of the
+        // counting sort's scans.  The 256-word bucket array holds the keys.
+        unsigned long long* keys = reinterpret_cast<unsigned long long*>(bucket);
+        uint32_t h = 0, tv = 0;
+        if ((uint32_t)tid < count) {
+            h = mix((uint32_t)tid);
+            tv = tie((uint32_t)tid);
+            keys[tid] = ((unsigned long long)h << 32) | tv;
+        }
+        __syncthreads();
+        if ((uint32_t)tid < count) {
+            const unsigned long long mine = ((unsigned long long)h << 32) | tv;
+            uint32_t rank = 0;
+            for (uint32_t j = 0; j < count; ++j) rank += keys[j] < mine ? 1u : 0u;
+            skey[rank] = ((unsigned long long)h << 32) | (uint32_t)tid;
+        }
+        __syncthreads();
+        return;
+    }
     for (uint32_t b = tid; b < 256; b += NT) bucket[b] = 0u;
     __syncthreads();
     for (uint32_t i = tid; i < count; i += NT) atomicAdd(&bucket[mix(i) >> 24], 1u);
@@ -271,6 +292,12 @@ __device__ bool colour_greedy_sorted(uint32_t count, uint32_t n, Ends ends, Mix 
 
 using SW = SWT<uint16_t>;
 
+// Worlds of at most this many bodies test every pair of bodies directly
+// instead of binning them (the same pairs; fewer scans and barriers).
+#ifndef R2D_BRUTE_MAX_BODIES
+#define R2D_BRUTE_MAX_BODIES 64
+#endif
+
 // Bodies with more spatial-hash entries than this are emitted by the whole
 // block (up to MAX_BIG_BODIES of them; more fall back to their own thread).
 constexpr uint32_t BIG_BODY_ENTRIES = 16, MAX_BIG_BODIES = 16;
@@ -294,7 +321,10 @@ constexpr uint32_t BIG_BODY_ENTRIES = 16, MAX_BIG_BODIES = 16;
 // world is frozen with R2D_ERR_TIMEOUT (no interleaving can reach it: the
 // earliest unfinished manifold never waits).
 #ifndef R2D_DATAFLOW
-#define R2D_DATAFLOW 1
+#define R2D_DATAFLOW 0
+#endif
+#ifndef R2D_DATAFLOW_SLEEP
+#define R2D_DATAFLOW_SLEEP 1
 #endif
 constexpr uint32_t DATAFLOW_SPIN_LIMIT = 1u << 22;
 
@@ -324,7 +354,7 @@ __device__ __forceinline__ bool dataflow_wait(const uint32_t* upd, uint32_t x, u
             *abort = 1u;
             return false;
         }
-        if (spin >= 16u) __nanosleep(32);
+        if (R2D_DATAFLOW_SLEEP && spin >= 16u) __nanosleep(32);
     }
     return true;
 }
@@ -406,7 +436,7 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
                                                                                const Layout Lo) {
     extern __shared__ __align__(16) unsigned char sm[];
     __shared__ uint32_t s_wsum[32];
-    __shared__ uint32_t s_ccnt[256];
+    __shared__ __align__(16) uint32_t s_ccnt[256];  // also 128 u64 sort keys (priority_order)
     __shared__ int s_err;
     __shared__ uint32_t s_capbits;
     __shared__ uint32_t s_cnt[4];  // pairs, manifolds, points
@@ -600,7 +630,46 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
     }
     if (err) set_err(&s_err, err);
     if (__syncthreads_or(err != 0)) goto fail;
-    {
+    if (n <= (uint32_t)R2D_BRUTE_MAX_BODIES) {
+        // Few bodies: every pair is tested directly, in equal shares of the
+        // n(n-1)/2 pairs per thread, with the filters and the shared-bucket
+        // test below -- the same pair set without the binning grid's scans.
+        const BucketMod bmod = {wd.bucket_recip, T};
+        const uint32_t total = n * (n - 1u) / 2u;
+        const uint32_t per = (total + NT - 1) / NT;
+        const uint32_t p0 = min(total, (uint32_t)tid * per), p1 = min(total, p0 + per);
+        if (p0 < p1) {
+            uint32_t i = 0, rem = p0;  // pair p0 = (i, i + 1 + rem), rows of decreasing length
+            while (rem >= n - 1u - i) {
+                rem -= n - 1u - i;
+                ++i;
+            }
+            uint32_t j = i + 1u + rem;
+            f2 pi = {ax[i], ay[i]};
+            float hwi = ahw[i], hhi = ahh[i];
+            bool sti = (s.kind[i] & K_STATIC) != 0;
+            for (uint32_t q = p0; q < p1; ++q, ++j) {
+                if (j >= n) {  // next row
+                    ++i;
+                    j = i + 1u;
+                    pi = f2{ax[i], ay[i]};
+                    hwi = ahw[i];
+                    hhi = ahh[i];
+                    sti = (s.kind[i] & K_STATIC) != 0;
+                }
+                if (sti && (s.kind[j] & K_STATIC)) continue;
+                if (!aabb_intersects(pi, hwi, hhi, f2{ax[j], ay[j]}, ahw[j], ahh[j])) continue;
+                if (!shares_bucket(i, j, rx0, ry0, rx1, ry1, bmod)) continue;
+                if (wd.nexcl && excluded(P.excl + wd.excl_off, wd.nexcl, ((unsigned long long)i << 32) | j)) continue;
+                const cg::coalesced_group g = cg::coalesced_threads();
+                uint32_t at = 0;
+                if (g.thread_rank() == 0) at = atomicAdd(&s_cnt[0], g.size());
+                const uint32_t slot = g.shfl(at, 0) + g.thread_rank();
+                if (slot < C.hs) cand[slot] = (i << 16) | j;
+            }
+        }
+        __syncthreads();
+    } else {
         SUBPHASE(12);
         const uint32_t E = block_scan_excl<NT>(bcnt, n, s_wsum);
         if (E > C.ne) {
@@ -731,9 +800,11 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
             P.timers[(size_t)w * PHASE_SLOTS + 19] += E;
         }
 #endif
-        // The pair list, grouped by shape type (disc-disc, disc-rectangle,
-        // rectangle-rectangle) so that the narrowphase's warps mostly follow
-        // one code path.
+    }
+    {
+        // The pair list, grouped by shape type (rectangle-rectangle,
+        // disc-rectangle, disc-disc) so that the narrowphase's warps mostly
+        // follow one code path.
         {
             const uint32_t found = s_cnt[0];
             if (found > C.np) {
@@ -754,9 +825,11 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
             unsigned long long total = 0;
             const unsigned long long before = block_scan_value_u64<NT>(mine, s_wsum64, &total);
             constexpr unsigned long long F = (1ull << 21) - 1ull;
-            const uint32_t t0 = (uint32_t)(total & F), t1 = (uint32_t)((total >> 21) & F);
-            uint32_t at[3] = {(uint32_t)(before & F), t0 + (uint32_t)((before >> 21) & F),
-                              t0 + t1 + (uint32_t)(before >> 42)};
+            // heaviest first: rectangle-rectangle, disc-rectangle, disc-disc,
+            // so that the warps drawing the costly SAT pairs start with them
+            const uint32_t t1 = (uint32_t)((total >> 21) & F), t2 = (uint32_t)(total >> 42);
+            uint32_t at[3] = {t2 + t1 + (uint32_t)(before & F), t2 + (uint32_t)((before >> 21) & F),
+                              (uint32_t)(before >> 42)};
             for (uint32_t q = s0; q < s1; ++q) {
                 const uint32_t key = cand[q];
                 const uint32_t t = (s.kind[key >> 16] & K_RECT) + (s.kind[key & 0xFFFFu] & K_RECT);
@@ -791,6 +864,7 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
             bool hit = false;
             int npt = 0;
             uint32_t ref = 0, inc = 0;
+            float mulo = 0.f, muhi = 0.f;  // friction coefficients of the pair's lower and higher body
             SatState sat;
             NewPoint pts[2];
             if (pi < npairs) {
@@ -802,6 +876,8 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
                 const float blo = __ldg(pr + (size_t)P_DIM1 * NB + base + lo);
                 const float ahi = __ldg(pr + (size_t)P_DIM0 * NB + base + hi);
                 const float bhi = __ldg(pr + (size_t)P_DIM1 * NB + base + hi);
+                mulo = __ldg(pr + (size_t)P_MU * NB + base + lo);
+                muhi = __ldg(pr + (size_t)P_MU * NB + base + hi);
                 const bool lo_first = idlo < idhi;
                 const uint32_t o1 = lo_first ? lo : hi;
                 const uint32_t o2 = lo_first ? hi : lo;
@@ -851,6 +927,8 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
             s.mnp[m] = (uint8_t)npt;
             s.nx[m] = sat.normal.x;
             s.ny[m] = sat.normal.y;
+            // the preStep's friction, sqrt(mu_ref * mu_inc) (collision.zig:114), fixed for the frame
+            s.fric[m] = sqrtf(mulo * muhi);
 #pragma unroll
             for (int k = 0; k < 2; ++k) {
                 if (k >= npt) break;
@@ -1081,7 +1159,6 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
                 const float inv_mass = inv_m1 + inv_m2;
                 const float inv_i1 = s.inv_i[a], inv_i2 = s.inv_i[b];
                 const f2 t2 = cw90(n2);
-                s.fric[m] = sqrtf(__ldg(pr + (size_t)P_MU * NB + base + a) * __ldg(pr + (size_t)P_MU * NB + base + b));
                 for (uint32_t k = 0; k < np; ++k) {
                     const uint32_t p = p0 + k;
                     f2 r1, r2;
