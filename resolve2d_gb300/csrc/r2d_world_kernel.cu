@@ -259,24 +259,26 @@ __device__ bool colour_greedy_sorted(uint32_t count, uint32_t n, Ends ends, Mix 
                     // the lowest free colour, reading a mask word only when
                     // every colour below it is taken (colours are nearly
                     // always below 32)
-                    auto word = [&](uint32_t q) {
-                        return (na ? cmask[q * n + a] : 0u) | (nb2 ? cmask[q * n + b] : 0u);
-                    };
-                    uint32_t c = 128u;
+                    // (the words read are current -- no other lane of this
+                    // round names a or b -- so they are written back without
+                    // being read again)
+                    uint32_t c = 128u, wa = 0u, wb = 0u;
                     for (uint32_t q = 0; q < 4; ++q) {
-                        const uint32_t wq = word(q);
-                        if (wq != 0xFFFFFFFFu) {
-                            c = 32u * q + (uint32_t)__ffs(~wq) - 1u;
+                        wa = na ? cmask[q * n + a] : 0u;
+                        wb = nb2 ? cmask[q * n + b] : 0u;
+                        if ((wa | wb) != 0xFFFFFFFFu) {
+                            c = 32u * q + (uint32_t)__ffs(~(wa | wb)) - 1u;
                             break;
                         }
                     }
                     if (c >= (uint32_t)MAX_COLOURS) {
                         overflow = 1;
-                        c = 0u;
+                        colour[ci] = 0u;
+                    } else {
+                        colour[ci] = (uint8_t)c;
+                        if (na) cmask[(c >> 5) * n + a] = wa | (1u << (c & 31u));
+                        if (nb2) cmask[(c >> 5) * n + b] = wb | (1u << (c & 31u));
                     }
-                    colour[ci] = (uint8_t)c;
-                    if (na) cmask[(c >> 5) * n + a] |= 1u << (c & 31u);
-                    if (nb2) cmask[(c >> 5) * n + b] |= 1u << (c & 31u);
                     done = true;
                 }
                 __syncwarp();
