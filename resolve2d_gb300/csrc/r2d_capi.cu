@@ -236,7 +236,6 @@ struct Engine {
     // body's diameter (R2D_FINE_CELL_SCALE, default 1).  Pairs do not depend
     // on it; candidates and entries per body do.
     float fine_scale = 1.0f;
-    uint32_t dataflow_skew = 0;  // R2D_DATAFLOW_TEST_SKEW
 
     ~Engine() {
         large.clear();
@@ -293,10 +292,6 @@ struct Engine {
         // makes its one bounded device loop give up (R2D_ERR_TIMEOUT).
         const char* rl = getenv("R2D_COLOUR_ROUND_LIMIT");
         colour_round_limit = rl ? (uint32_t)strtoul(rl, nullptr, 10) : 0u;
-        // Test hook: the barrier-free contact solve's waits never see their
-        // targets (R2D_ERR_TIMEOUT).
-        const char* dk = getenv("R2D_DATAFLOW_TEST_SKEW");
-        dataflow_skew = dk ? (uint32_t)strtoul(dk, nullptr, 10) : 0u;
         const char* fs = getenv("R2D_FINE_CELL_SCALE");
         if (fs && strtof(fs, nullptr) > 0.f) fine_scale = strtof(fs, nullptr);
         CUDA_TRY(dalloc(d_call, 1));
@@ -1253,7 +1248,6 @@ struct Engine {
         P.cell = cell;
         P.table_mult = table_mult;
         P.dbg = dbg;
-        P.dataflow_skew = dataflow_skew;
         P.world_fail_call = d_fail_call;
         P.world_capbits = d_capbits;
         P.call_index = call_index;

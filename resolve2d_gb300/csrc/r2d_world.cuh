@@ -240,9 +240,6 @@ struct StepParams {
     float cell;
     uint32_t table_mult;
     DebugOut dbg;
-    // Test hook: added to every target of the barrier-free contact solve's
-    // waits, so that they run out (0 in use).
-    uint32_t dataflow_skew;
 };
 
 // Phase timer slots (cycles, R2D_PHASE_TIMERS builds only): load,

@@ -297,7 +297,7 @@ using SW = SWT<uint16_t>;
 // Worlds of at most this many bodies test every pair of bodies directly
 // instead of binning them (the same pairs; fewer scans and barriers).
 #ifndef R2D_BRUTE_MAX_BODIES
-#define R2D_BRUTE_MAX_BODIES 64
+#define R2D_BRUTE_MAX_BODIES 96
 #endif
 
 // Bodies with more spatial-hash entries than this are emitted by the whole
@@ -309,124 +309,6 @@ constexpr uint32_t BIG_BODY_ENTRIES = 16, MAX_BIG_BODIES = 16;
 #ifndef R2D_REG_TARGET
 #define R2D_REG_TARGET 96
 #endif
-// ---- the contact solve without block barriers ----
-// Within a colour no two manifolds share a non-static body, so a manifold of
-// colour c only has to wait for its own two bodies to have taken every update
-// of the earlier colours (and earlier iterations), not for the whole block.
-// upd[x] counts the contact updates body x has taken in this substep; body
-// x's colours are the bits of its colouring mask, so the manifold of colour
-// c in iteration `it` finds body x ready when
-//     upd[x] == it * popcount(mask_x) + popcount(mask_x & bits below c),
-// and counts one more once it has written x.  Every body then sees its
-// updates in the barrier version's order, so the results are the same bits.
-// Every wait is bounded: on the limit the colour reports failure and the
-// world is frozen with R2D_ERR_TIMEOUT (no interleaving can reach it: the
-// earliest unfinished manifold never waits).
-#ifndef R2D_DATAFLOW
-#define R2D_DATAFLOW 0
-#endif
-#ifndef R2D_DATAFLOW_SLEEP
-#define R2D_DATAFLOW_SLEEP 1
-#endif
-constexpr uint32_t DATAFLOW_SPIN_LIMIT = 1u << 22;
-
-// Updates body x must have taken before colour c of iteration it.
-__device__ __forceinline__ uint32_t dataflow_target(const uint32_t* cmask, uint32_t n, uint32_t x, uint32_t c,
-                                                    uint32_t it, bool one_word) {
-    const uint32_t w0 = cmask[x];
-    if (one_word) return it * (uint32_t)__popc(w0) + (uint32_t)__popc(w0 & ((1u << c) - 1u));
-    uint32_t cnt = 0, pos = 0;
-#pragma unroll
-    for (uint32_t q = 0; q < 4; ++q) {
-        const uint32_t wq = cmask[q * n + x];
-        cnt += (uint32_t)__popc(wq);
-        const uint32_t lo = q * 32u;
-        pos += c >= lo + 32u ? (uint32_t)__popc(wq) : (c > lo ? (uint32_t)__popc(wq & ((1u << (c - lo)) - 1u)) : 0u);
-    }
-    return it * cnt + pos;
-}
-
-// Waits until upd[x] == target.  A wait that runs out sets *abort, which
-// ends every other wait of the block at once.
-__device__ __forceinline__ bool dataflow_wait(const uint32_t* upd, uint32_t x, uint32_t target, uint32_t* abort) {
-    const volatile uint32_t* v = upd;
-    const volatile uint32_t* ab = abort;
-    for (uint32_t spin = 0; v[x] != target; ++spin) {
-        if (spin >= DATAFLOW_SPIN_LIMIT || *ab) {
-            *abort = 1u;
-            return false;
-        }
-        if (R2D_DATAFLOW_SLEEP && spin >= 16u) __nanosleep(32);
-    }
-    return true;
-}
-
-__device__ __forceinline__ void dataflow_done(uint32_t* upd, uint32_t x, uint32_t target) {
-    volatile uint32_t* v = upd;
-    v[x] = target + 1u;
-}
-
-// One colour of one iteration (see above).  Returns false when a wait ran
-// out.  Every lane of the block calls it for every colour, in order.
-template <int NT, bool LEAN>
-__device__ __forceinline__ bool contact_colour_dataflow(const SWT<uint16_t>& s, const uint16_t* corder, uint32_t k0,
-                                                        uint32_t k1, uint32_t c, uint32_t it, const uint32_t* cmask,
-                                                        uint32_t n, bool one_word, uint32_t* upd, bool warm,
-                                                        uint32_t skew, uint32_t* abort) {
-    const uint32_t tid = threadIdx.x, lane = tid & 31u;
-    bool ok = true;
-    if (k1 - k0 <= (uint32_t)(NT / 2)) {  // two lanes a manifold, one per contact point
-        const uint32_t k = k0 + (tid >> 1);
-        const bool valid = k < k1;
-        if (__ballot_sync(0xffffffffu, valid) == 0u) return true;  // none of this colour in this warp
-        uint32_t m = 0, a = 0, b = 0, ta = 0, tb = 0;
-        bool da = false, db = false;
-        if (valid) {
-            m = corder[k];
-            a = s.ma[m];
-            b = s.mb[m];
-            da = !(s.kind[a] & K_STATIC);
-            db = !(s.kind[b] & K_STATIC);
-            if (da) {
-                ta = dataflow_target(cmask, n, a, c, it, one_word);
-                ok = dataflow_wait(upd, a, ta + skew, abort) && ok;
-            }
-            if (db) {
-                tb = dataflow_target(cmask, n, b, c, it, one_word);
-                ok = dataflow_wait(upd, b, tb + skew, abort) && ok;
-            }
-        }
-        __syncwarp();
-        __threadfence_block();
-        solve_contact_lanes<LEAN>(s, m, valid, lane, warm);
-        if (valid && !(lane & 1u)) {
-            __threadfence_block();
-            if (da) dataflow_done(upd, a, ta);
-            if (db) dataflow_done(upd, b, tb);
-        }
-    } else {
-        for (uint32_t k = k0 + tid; k < k1; k += NT) {
-            const uint32_t m = corder[k], a = s.ma[m], b = s.mb[m];
-            const bool da = !(s.kind[a] & K_STATIC), db = !(s.kind[b] & K_STATIC);
-            uint32_t ta = 0, tb = 0;
-            if (da) {
-                ta = dataflow_target(cmask, n, a, c, it, one_word);
-                ok = dataflow_wait(upd, a, ta + skew, abort) && ok;
-            }
-            if (db) {
-                tb = dataflow_target(cmask, n, b, c, it, one_word);
-                ok = dataflow_wait(upd, b, tb + skew, abort) && ok;
-            }
-            __threadfence_block();
-            solve_contact<LEAN>(s, m, warm);
-            __threadfence_block();
-            if (da) dataflow_done(upd, a, ta);
-            if (db) dataflow_done(upd, b, tb);
-        }
-    }
-    return ok;
-}
-
 // One-warp CTAs keep 96 registers: below that they spill.
 constexpr int reg_target_for(int nt) { return nt <= 32 ? 96 : R2D_REG_TARGET; }
 constexpr int min_blocks_for(int nt) {
@@ -445,7 +327,6 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
     __shared__ unsigned long long s_wsum64[32];
     __shared__ uint32_t s_big[MAX_BIG_BODIES];  // bodies whose cell entries the whole block emits
     __shared__ uint32_t s_nbig;
-    __shared__ uint32_t s_df_abort;  // a barrier-free solve's wait ran out
 
     const int tid = threadIdx.x;
     if (blockIdx.x >= P.nlist) return;
@@ -1184,18 +1065,7 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
                     __syncthreads();
                 }
             }
-            // impulse iterations (lib.zig:226-236): joints, then contacts.
-            // A world without joints still holds its contact colouring masks
-            // (the joint colouring would reuse them) and solves its contacts
-            // without block barriers (contact_colour_dataflow).
-            const bool dataflow = R2D_DATAFLOW && NJ == 0 && ncol > 0;
-            uint32_t* upd = cmask + 4 * n;  // the colouring's lane bits, dead after it
-            bool df_ok = true;
-            if (dataflow) {
-                for (uint32_t i = tid; i < n; i += NT) upd[i] = 0u;
-                if (tid == 0) s_df_abort = 0u;
-                __syncthreads();
-            }
+            // impulse iterations (lib.zig:226-236): joints, then contacts
             for (uint32_t it = 0; it < P.iters; ++it) {
                 for (uint32_t c = 0; c < njcol; ++c) {
                     const uint32_t k0 = joff[c], k1 = joff[c + 1];
@@ -1211,12 +1081,6 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
                 // manifold (one per contact point); a larger one, one lane.
                 for (uint32_t c = 0; c < ncol; ++c) {
                     const uint32_t k0 = coff[c], k1 = coff[c + 1];
-                    if (dataflow) {
-                        df_ok = contact_colour_dataflow<NT, LEAN>(s, corder, k0, k1, c, it, cmask, n, ncol <= 32u,
-                                                                  upd, warm, P.dataflow_skew, &s_df_abort) &&
-                                df_ok;
-                        continue;
-                    }
                     if (k1 - k0 <= (uint32_t)(NT / 2)) {
                         const uint32_t k = k0 + ((uint32_t)tid >> 1);
                         solve_contact_lanes<LEAN>(s, k < k1 ? (uint32_t)corder[k] : 0u, k < k1, (uint32_t)tid & 31u,
@@ -1226,11 +1090,6 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
                     }
                     __syncthreads();
                 }
-            }
-            if (dataflow && __syncthreads_or(!df_ok)) {
-                if (tid == 0) s_err = DS_TIMEOUT;
-                __syncthreads();
-                goto fail;
             }
             // integration (lib.zig:238-249)
             for (uint32_t i = tid; i < n; i += NT) {

@@ -1,9 +1,9 @@
-"""The benchmark line recorded from a GB300 run (profiles/bench_config3.md)
-carries every key of the bench contract, with sane values, and the keys the
-bench writes today are the ones recorded.  CPU only: it reads text."""
+"""The benchmark line recorded from a GB300 run (profiles/bench_config3.json,
+the line bench.py printed) carries every key of the bench contract, with sane
+values, and the keys the bench writes today are the ones recorded.  CPU only:
+it reads the recorded file."""
 
 import json
-import re
 from pathlib import Path
 
 from conftest import REPO
@@ -14,9 +14,7 @@ TOP = {"metric": str, "value": float, "unit": str, "n_gpus": int, "steps": int, 
 
 
 def recorded_line() -> dict:
-    text = Path(REPO, "profiles", "bench_config3.md").read_text()
-    block = re.search(r"```json\n(.*?)```", text, flags=re.S).group(1)
-    return json.loads(block)
+    return json.loads(Path(REPO, "profiles", "bench_config3.json").read_text())
 
 
 def test_the_recorded_line_keeps_the_contract():

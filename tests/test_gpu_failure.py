@@ -9,12 +9,6 @@ runs out on an ordinary pile: the kernel stops, flags the colouring as stuck
 and returns, the call reports R2D_ERR_TIMEOUT, and the world keeps the state
 it had before the call, because the colouring runs before any substep.
 
-The fused kernel's contact solve waits, instead of at block barriers, on
-per-body update counters, each wait bounded.  The R2D_DATAFLOW_TEST_SKEW hook
-shifts every target out of reach: the first wait runs out, ends the others,
-and the world reports R2D_ERR_TIMEOUT with its pose and momenta untouched
-(the last substep has already refreshed the stored AABBs by then).
-
 A spatial-hash table whose bucket count (multiplier x bodies) would wrap 32
 bits is refused at upload with R2D_ERR_CAPACITY, before anything reaches the
 device.
@@ -70,30 +64,6 @@ def test_colouring_round_limit_reports_timeout_and_leaves_the_state():
     w2.sync()
     assert not np.array_equal(w2.read_state(), state)
     w.close()
-    w2.close()
-
-
-def test_barrier_free_solve_wait_reports_timeout():
-    sc, state = _settled_config0()
-    os.environ["R2D_DATAFLOW_TEST_SKEW"] = "1000000"
-    try:
-        w = World.from_scene(sc)
-    finally:
-        del os.environ["R2D_DATAFLOW_TEST_SKEW"]
-    w.write_state(state)
-    w.sync()
-    w.process(sc.dt, sc.sub_steps, sc.iters)
-    with pytest.raises(N.R2DError) as e:
-        w.sync()
-    assert e.value.code == TIMEOUT
-    assert_state_equal(w.read_state()[:6], state[:6], "pose and momenta after the timed-out call")
-    w.close()
-    # a solver without the hook steps the same state on the same context
-    w2 = World.from_scene(sc)
-    w2.write_state(state)
-    w2.process(sc.dt, sc.sub_steps, sc.iters)
-    w2.sync()
-    assert not np.array_equal(w2.read_state(), state)
     w2.close()
 
 
