@@ -161,6 +161,24 @@ R2D_DF void geo_make(Geo& g, f2 pos, bool rect, float d0, float d1, float c, flo
     for (int i = 0; i < 4; ++i) g.en[i] = ccw90(normalize2(sub2(g.wv[(i + 1) & 3], g.wv[i])));
 }
 
+// geo_make with a rectangle's edge normals taken from `en` (two float4:
+// normals 0, 1 then 2, 3) as geo_make computed them for the same pose, so
+// the values are the same bits; the vertices are recomputed (no division).
+R2D_DF void geo_make_cached(Geo& g, f2 pos, bool rect, float d0, float d1, float c, float s, const float4* en) {
+    g.pos = pos;
+    g.rect = rect;
+    g.radius = d0;
+    if (!rect) return;
+    const float w = d0 / 2.0f, h = d1 / 2.0f;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) g.wv[i] = add2(rot(rect_local(i, w, h), c, s), pos);
+    const float4 a = en[0], b = en[1];
+    g.en[0] = f2{a.x, a.y};
+    g.en[1] = f2{a.z, a.w};
+    g.en[2] = f2{b.x, b.y};
+    g.en[3] = f2{b.z, b.w};
+}
+
 // closestPoint (Disc.zig:80-84; Rectangle.zig:114-130 -- the nearest vertex)
 R2D_DF f2 closest_point(const Geo& g, f2 p) {
     if (!g.rect) {

@@ -438,35 +438,62 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
 
 
     // ---------------- load the world ----------------
-    for (uint32_t i = tid; i < n; i += NT) {
+    // Two bodies a thread per round, every global load of both issued before
+    // either is used, so a round waits for memory once.
+    struct RawBody {
+        uint8_t k;
+        float px, py, a, mx, my, L, m, I, ax, ay, ahw, ahh;
+    };
+    auto fetch = [&](uint32_t i) {
         const uint32_t g = base + i;
-        const uint8_t k = __ldg(P.kind + g);
-        const float a = st[(size_t)S_ANGLE * NB + g];
-        s.px[i] = st[(size_t)S_POS_X * NB + g];
-        s.py[i] = st[(size_t)S_POS_Y * NB + g];
-        s.ang[i] = a;
-        s.mx[i] = st[(size_t)S_MOM_X * NB + g];
-        s.my[i] = st[(size_t)S_MOM_Y * NB + g];
-        s.L[i] = st[(size_t)S_ANG_MOM * NB + g];
-        const float m = __ldg(pr + (size_t)P_MASS * NB + g);
-        const float I = __ldg(pr + (size_t)P_INERTIA * NB + g);
+        RawBody r;
+        r.k = __ldg(P.kind + g);
+        r.a = st[(size_t)S_ANGLE * NB + g];
+        r.px = st[(size_t)S_POS_X * NB + g];
+        r.py = st[(size_t)S_POS_Y * NB + g];
+        r.mx = st[(size_t)S_MOM_X * NB + g];
+        r.my = st[(size_t)S_MOM_Y * NB + g];
+        r.L = st[(size_t)S_ANG_MOM * NB + g];
+        r.m = __ldg(pr + (size_t)P_MASS * NB + g);
+        r.I = __ldg(pr + (size_t)P_INERTIA * NB + g);
+        r.ax = st[(size_t)S_AABB_X * NB + g];
+        r.ay = st[(size_t)S_AABB_Y * NB + g];
+        r.ahw = st[(size_t)S_AABB_HW * NB + g];
+        r.ahh = st[(size_t)S_AABB_HH * NB + g];
+        return r;
+    };
+    auto put = [&](uint32_t i, const RawBody& r) {
+        s.px[i] = r.px;
+        s.py[i] = r.py;
+        s.ang[i] = r.a;
+        s.mx[i] = r.mx;
+        s.my[i] = r.my;
+        s.L[i] = r.L;
         if (Lo.has_pos0) {
-            s.px0[i] = s.px[i];
-            s.py0[i] = s.py[i];
+            s.px0[i] = r.px;
+            s.py0[i] = r.py;
         }
-        s.inv_m[i] = (k & K_STATIC) ? 0.f : 1.0f / m;
-        s.inv_i[i] = (k & K_STATIC) ? 0.f : 1.0f / I;
-        s.kind[i] = k;
+        s.inv_m[i] = (r.k & K_STATIC) ? 0.f : 1.0f / r.m;
+        s.inv_i[i] = (r.k & K_STATIC) ? 0.f : 1.0f / r.I;
+        s.kind[i] = r.k;
         float c = 1.f, sn = 0.f;
-        if ((k & K_RECT) || disc_rot) r2d_sincosf(a, &sn, &c);
+        if ((r.k & K_RECT) || disc_rot) r2d_sincosf(r.a, &sn, &c);
         s.cs[i] = c;
         s.sn[i] = sn;
-        if (Lo.has_prev) s.ang_prev[i] = a;
+        if (Lo.has_prev) s.ang_prev[i] = r.a;
         s.tq[i] = 0.f;
-        ax[i] = st[(size_t)S_AABB_X * NB + g];
-        ay[i] = st[(size_t)S_AABB_Y * NB + g];
-        ahw[i] = st[(size_t)S_AABB_HW * NB + g];
-        ahh[i] = st[(size_t)S_AABB_HH * NB + g];
+        ax[i] = r.ax;
+        ay[i] = r.ay;
+        ahw[i] = r.ahw;
+        ahh[i] = r.ahh;
+    };
+    for (uint32_t i = tid; i < n; i += 2 * NT) {
+        const bool two = i + NT < n;
+        const RawBody r0 = fetch(i);
+        RawBody r1 = r0;
+        if (two) r1 = fetch(i + NT);
+        put(i, r0);
+        if (two) put(i + NT, r1);
     }
     for (uint32_t b = tid; b < T + 1; b += NT) table[b] = 0u;
     __syncthreads();
@@ -737,6 +764,23 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
     PHASE(1);
     // ---------------- narrowphase (collision.zig:299-320, lib.zig:284-294) ----------------
     {
+        // Each rectangle's edge normals (a square root and two divisions per
+        // edge), once per body instead of once per pair it is in: held in the
+        // point arrays mn .. apt, which the narrowphase leaves alone (they
+        // hold 16 B a point, at least 2.4 points a body; 32 B a body needed).
+        float4* gen = reinterpret_cast<float4*>(sm + Lo.mn);
+        const bool en_cached = 32u * n <= 16u * C.npt;
+        if (en_cached) {
+            for (uint32_t i = tid; i < n; i += NT) {
+                if (!(s.kind[i] & K_RECT)) continue;
+                Geo g;
+                geo_make(g, f2{s.px[i], s.py[i]}, true, __ldg(pr + (size_t)P_DIM0 * NB + base + i),
+                         __ldg(pr + (size_t)P_DIM1 * NB + base + i), s.cs[i], s.sn[i]);
+                gen[2 * i] = make_float4(g.en[0].x, g.en[0].y, g.en[1].x, g.en[1].y);
+                gen[2 * i + 1] = make_float4(g.en[2].x, g.en[2].y, g.en[3].x, g.en[3].y);
+            }
+            __syncthreads();
+        }
         const float h = P.dt / (float)P.sub_steps;
         const uint32_t npairs = s_cnt[0];
         const uint32_t lane = tid & 31u;
@@ -765,10 +809,17 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
                 const uint32_t o1 = lo_first ? lo : hi;
                 const uint32_t o2 = lo_first ? hi : lo;
                 Geo g1, g2;
-                geo_make(g1, f2{s.px[o1], s.py[o1]}, s.kind[o1] & K_RECT, lo_first ? alo : ahi, lo_first ? blo : bhi,
-                         s.cs[o1], s.sn[o1]);
-                geo_make(g2, f2{s.px[o2], s.py[o2]}, s.kind[o2] & K_RECT, lo_first ? ahi : alo, lo_first ? bhi : blo,
-                         s.cs[o2], s.sn[o2]);
+                if (en_cached) {
+                    geo_make_cached(g1, f2{s.px[o1], s.py[o1]}, s.kind[o1] & K_RECT, lo_first ? alo : ahi,
+                                    lo_first ? blo : bhi, s.cs[o1], s.sn[o1], gen + 2 * o1);
+                    geo_make_cached(g2, f2{s.px[o2], s.py[o2]}, s.kind[o2] & K_RECT, lo_first ? ahi : alo,
+                                    lo_first ? bhi : blo, s.cs[o2], s.sn[o2], gen + 2 * o2);
+                } else {
+                    geo_make(g1, f2{s.px[o1], s.py[o1]}, s.kind[o1] & K_RECT, lo_first ? alo : ahi,
+                             lo_first ? blo : bhi, s.cs[o1], s.sn[o1]);
+                    geo_make(g2, f2{s.px[o2], s.py[o2]}, s.kind[o2] & K_RECT, lo_first ? ahi : alo,
+                             lo_first ? bhi : blo, s.cs[o2], s.sn[o2]);
+                }
                 hit = perform_narrow_sat(g1, g2, sat);
                 if (hit) {
                     ref = sat.ref_is_first ? o1 : o2;
