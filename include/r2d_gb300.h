@@ -64,8 +64,13 @@ enum {
  * (Disc.zig:8, Rectangle.zig:17-18). */
 enum { R2D_P_MASS = 0, R2D_P_INERTIA, R2D_P_MU, R2D_P_DIM0, R2D_P_DIM1, R2D_PROP_FIELDS };
 
-/* kind bits per body: RigidBody.Type (RigidBody.zig:28-31) and the static flag (:85) */
-enum { R2D_KIND_RECTANGLE = 1, R2D_KIND_STATIC = 2 };
+/* kind bits per body: RigidBody.Type (RigidBody.zig:28-31) and the static flag (:85).
+ * R2D_KIND_POLYGON: a convex polygon, the roadmap's next shape (README.md:64-67)
+ * behind the same vtable (RigidBody.zig:33-42); its vertices come with
+ * r2d_*_set_polygons, its props are mass, inertia, mu and two free dims. */
+enum { R2D_KIND_RECTANGLE = 1, R2D_KIND_STATIC = 2, R2D_KIND_POLYGON = 4 };
+/* Vertices a polygon may have (3 .. R2D_POLY_MAX_VERTS). */
+enum { R2D_POLY_MAX_VERTS = 8 };
 
 /* Constraint.Type (src/core/Constraints/Constraint.zig:15-20) */
 enum {
@@ -164,6 +169,15 @@ R2D_API int r2d_solver_destroy(r2d_solver* s);
  * two bodies with one id return R2D_ERR_INVALID_ARGUMENT. */
 R2D_API int r2d_solver_set_bodies(r2d_solver* s, uint32_t n, const uint32_t* ids, const uint8_t* kind,
                                   const float* props, const float* state, int init_aabb);
+/* The vertices of the store's R2D_KIND_POLYGON bodies (after set_bodies):
+ * for each of n bodies (store indices `body`), nverts[k] (3..8) local
+ * vertices about the body's origin, verts [n][R2D_POLY_MAX_VERTS][2],
+ * clockwise as the rectangle's (Rectangle.zig:40), convex.  A body uploaded
+ * with init_aabb gets its first AABB here.  A world holding a polygon steps
+ * on the grid pipeline.  No counterpart in the reference (polygons are on
+ * its roadmap, README.md:64-67). */
+R2D_API int r2d_solver_set_polygons(r2d_solver* s, uint32_t n, const uint32_t* body, const uint8_t* nverts,
+                                    const float* verts);
 /* Per-frame mirror of the dynamic state (host -> device, device -> host). */
 R2D_API int r2d_solver_write_state(r2d_solver* s, const float* state);
 R2D_API int r2d_solver_read_state(r2d_solver* s, float* state);
@@ -243,6 +257,9 @@ R2D_API int r2d_batch_destroy(r2d_batch* b);
 R2D_API int r2d_batch_set_worlds(r2d_batch* b, uint32_t nworlds, const uint32_t* body_off, const uint32_t* ids,
                                  const uint8_t* kind, const float* props, const float* state,
                                  const float* gravity, int init_aabb);
+/* r2d_solver_set_polygons for a batch: `body` indexes the concatenated bodies. */
+R2D_API int r2d_batch_set_polygons(r2d_batch* b, uint32_t n, const uint32_t* body, const uint8_t* nverts,
+                                   const float* verts);
 R2D_API int r2d_batch_write_state(r2d_batch* b, const float* state);
 R2D_API int r2d_batch_read_state(r2d_batch* b, float* state);
 R2D_API int r2d_batch_process(r2d_batch* b, float dt, uint32_t sub_steps, uint32_t collision_iters);

@@ -28,6 +28,7 @@ _SIG = {
     "r2o_destroy": ([_P], None),
     "r2o_add_bodies": ([_P, C.c_uint32, _u32p, _u8p, _f32p], C.c_int),
     "r2o_num_bodies": ([_P], C.c_uint32),
+    "r2o_add_bodies_poly": ([_P, C.c_uint32, _u32p, _u8p, _f32p, _u8p, _f32p], C.c_int),
     "r2o_add_gravity": ([_P, C.c_float], None),
     "r2o_exclude_pair": ([_P, C.c_uint32, C.c_uint32], None),
     "r2o_add_joints": ([_P, C.c_uint32, _u8p, _u32p, _u32p, _f32p], None),
@@ -110,7 +111,14 @@ class Oracle:
         ids = np.ascontiguousarray(sc.ids, np.uint32)
         kind = np.ascontiguousarray(sc.kind, np.uint8)
         opt = np.ascontiguousarray(sc.opt, np.float32)
-        o.lib.r2o_add_bodies(o.h, ids.shape[0], _p(ids, C.c_uint32), _p(kind, C.c_uint8), _p(opt, C.c_float))
+        if getattr(sc, "has_polygons", False):
+            nv = np.ascontiguousarray(sc.poly_nv, np.uint8)
+            pv = np.ascontiguousarray(sc.poly_v, np.float32)
+            if o.lib.r2o_add_bodies_poly(o.h, ids.shape[0], _p(ids, C.c_uint32), _p(kind, C.c_uint8),
+                                         _p(opt, C.c_float), _p(nv, C.c_uint8), _p(pv, C.c_float)) != 0:
+                raise ValueError("a polygon needs 3 to 8 vertices")
+        else:
+            o.lib.r2o_add_bodies(o.h, ids.shape[0], _p(ids, C.c_uint32), _p(kind, C.c_uint8), _p(opt, C.c_float))
         for g in np.atleast_1d(sc.gravity):
             if g != 0:
                 o.lib.r2o_add_gravity(o.h, float(g))

@@ -37,15 +37,20 @@ struct Handle {
     std::unique_ptr<Solver<double>> d;
 };
 
+// kind bits: 1 rectangle, 2 static, 4 mass by density, 8 polygon (mass
+// MASS_PROP, inertia DIM1, vertices nverts[i] pairs at verts[i][MAX_POLY_VERTS][2]).
 template <class R>
 void add_bodies(Solver<R>& s, uint32_t n, const uint32_t* ids, const uint8_t* kind,
-                const float* opt) {
+                const float* opt, const uint8_t* nverts = nullptr, const float* verts = nullptr) {
     for (uint32_t i = 0; i < n; ++i) {
         auto o = [&](int f) { return R(opt[(size_t)f * n + i]); };
         V2<R> pos{o(0), o(1)}, vel{o(3), o(4)};
         bool by_density = (kind[i] & 4) != 0;
         size_t idx;
-        if (kind[i] & 1)
+        if ((kind[i] & 8) && nverts && verts)
+            idx = s.make_polygon(ids[i], pos, vel, o(2), o(5), o(6), o(7), o(9), nverts[i],
+                                 verts + (size_t)i * 2 * MAX_POLY_VERTS, o(8), o(9));
+        else if (kind[i] & 1)
             idx = s.make_rectangle(ids[i], pos, vel, o(2), o(5), o(6), by_density, o(7), o(8), o(9));
         else
             idx = s.make_disc(ids[i], pos, vel, o(2), o(5), o(6), by_density, o(7), o(8));
@@ -208,6 +213,17 @@ int r2o_add_bodies(void* hp, uint32_t n, const uint32_t* ids, const uint8_t* kin
                    const float* opt) {
     Handle* h = (Handle*)hp;
     DISPATCH(h, add_bodies(S, n, ids, kind, opt));
+    return 0;
+}
+
+/* r2o_add_bodies with polygons among them (kind bit 8): nverts [n],
+ * verts [n][MAX_POLY_VERTS][2]. */
+int r2o_add_bodies_poly(void* hp, uint32_t n, const uint32_t* ids, const uint8_t* kind, const float* opt,
+                        const uint8_t* nverts, const float* verts) {
+    Handle* h = (Handle*)hp;
+    for (uint32_t i = 0; i < n; ++i)
+        if ((kind[i] & 8) && (nverts[i] < 3 || nverts[i] > MAX_POLY_VERTS)) return -1;
+    DISPATCH(h, add_bodies(S, n, ids, kind, opt, nverts, verts));
     return 0;
 }
 

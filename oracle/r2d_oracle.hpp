@@ -218,7 +218,14 @@ struct AABB {
 // ---------------------------------------------------------------------------
 // Bodies (src/core/Bodies/{RigidBody,Disc,Rectangle}.zig)
 // ---------------------------------------------------------------------------
-enum BodyType : uint8_t { DISC = 0, RECTANGLE = 1 };  // RigidBody.zig:28-31
+// RigidBody.zig:28-31, plus a convex polygon: the roadmap's next shape
+// (README.md:64-67), behind the same vtable (RigidBody.zig:33-42).  A
+// polygon is the rectangle's code over its own vertex ring: local vertices
+// about its origin in the rectangle's winding (Rectangle.zig:40 lists
+// (-w,-h), (-w,h), (w,h), (w,-h): clockwise, so that the counter-clockwise
+// turn of an edge points outwards), 3 to MAX_POLY_VERTS of them.
+enum BodyType : uint8_t { DISC = 0, RECTANGLE = 1, POLYGON = 2 };
+constexpr uint32_t MAX_POLY_VERTS = 8;
 
 template <class R>
 struct Props {  // RigidBody.zig:69-81
@@ -237,8 +244,9 @@ struct Body {  // RigidBody.zig:83-91 with the Disc / Rectangle payloads inlined
     BodyType type = DISC;
     Props<R> props;
     R radius = 0;                // Disc.zig:8
-    R width = 0, height = 0;     // Rectangle.zig:17-18
-    V2<R> local_vertices[4];     // Rectangle.zig:20
+    R width = 0, height = 0;     // Rectangle.zig:17-18 (a polygon: the two dims it was given)
+    uint32_t nverts = 4;         // vertices of a rectangle or polygon
+    V2<R> local_vertices[MAX_POLY_VERTS];  // Rectangle.zig:20
 };
 
 template <class R>
@@ -272,9 +280,9 @@ void update_aabb(Body<R>& b) {
         b.aabb = AABB<R>{b.props.pos, b.radius, b.radius};
         return;
     }
-    // Rectangle.zig:71-86
+    // Rectangle.zig:71-86 (a polygon: over its vertices)
     R width = 0, height = 0;
-    for (int i = 0; i < 4; ++i) {
+    for (uint32_t i = 0; i < b.nverts; ++i) {
         V2<R> rot = rotate2(b.local_vertices[i], b.props.angle);
         if (rot.x > width) width = rot.x;
         if (rot.y > height) height = rot.y;
@@ -283,8 +291,8 @@ void update_aabb(Body<R>& b) {
 }
 
 template <class R>
-void world_vertices(const Body<R>& b, V2<R> out[4]) {  // Rectangle.zig:88-98
-    for (int i = 0; i < 4; ++i) {
+void world_vertices(const Body<R>& b, V2<R> out[MAX_POLY_VERTS]) {  // Rectangle.zig:88-98
+    for (uint32_t i = 0; i < b.nverts; ++i) {
         V2<R> r = rotate2(b.local_vertices[i], b.props.angle);
         out[i] = add2(r, b.props.pos);
     }
@@ -299,9 +307,9 @@ V2<R> closest_point(const Body<R>& b, V2<R> pos) {
     // Rectangle.zig:114-130: the nearest VERTEX, not the nearest surface point.
     R best_dist2 = std::numeric_limits<R>::infinity();
     V2<R> best_pos = pos;
-    V2<R> wv[4];
+    V2<R> wv[MAX_POLY_VERTS];
     world_vertices(b, wv);
-    for (int i = 0; i < 4; ++i) {
+    for (uint32_t i = 0; i < b.nverts; ++i) {
         V2<R> d = sub2(wv[i], pos);
         R dist2 = dot2(d, d);
         if (dist2 < best_dist2) {
@@ -321,7 +329,7 @@ Edge<R> get_normal(const Body<R>& self, const Body<R>& other, uint32_t iter) {
         return e;
     }
     // Rectangle.zig:132-151
-    uint32_t next_iter = iter == 3 ? 0 : iter + 1;
+    uint32_t next_iter = iter + 1 == self.nverts ? 0 : iter + 1;
     V2<R> r1 = rotate2(self.local_vertices[iter], self.props.angle);
     V2<R> a1 = add2(r1, self.props.pos);
     V2<R> r2 = rotate2(self.local_vertices[next_iter], self.props.angle);
@@ -344,7 +352,7 @@ void project_along_axis(const Body<R>& b, V2<R> normal, R out[2]) {
     // Rectangle.zig:153-169
     R best_low = std::numeric_limits<R>::infinity();
     R best_high = -std::numeric_limits<R>::infinity();
-    for (int i = 0; i < 4; ++i) {
+    for (uint32_t i = 0; i < b.nverts; ++i) {
         V2<R> r = rotate2(b.local_vertices[i], b.props.angle);
         V2<R> world = add2(r, b.props.pos);
         R dot = dot2(world, normal);
@@ -430,8 +438,8 @@ Incident<R> clip_against_edge(const Body<R>& self, Line<R> edge, V2<R> normal) {
     bool found = false;
     R best_dot = std::numeric_limits<R>::infinity();
     V2<R> curr_world = local_to_world(self, self.local_vertices[0]);
-    for (int i = 0; i < 4; ++i) {
-        int next_idx = i == 3 ? 0 : i + 1;
+    for (uint32_t i = 0; i < self.nverts; ++i) {
+        uint32_t next_idx = i + 1 == self.nverts ? 0 : i + 1;
         V2<R> next_world = local_to_world(self, self.local_vertices[next_idx]);
         V2<R> tangent = normalize2(sub2(next_world, curr_world));
         V2<R> tentative_normal = rotate90counterclockwise(tangent);
@@ -630,6 +638,31 @@ public:
         update_aabb(b);
         b.props.momentum = scale2(vel, mass);
         b.props.ang_momentum = omega * b.props.inertia;
+        return append(b);
+    }
+
+    // A convex polygon (no counterpart in the reference; its roadmap's next
+    // shape): `nverts` local vertices (x, y pairs, clockwise about the body's
+    // origin, as the rectangle's), with its mass and inertia given (the
+    // caller integrates them over its shape); d0, d1 are kept as its dims.
+    size_t make_polygon(uint32_t id, V2<R> pos, V2<R> vel, R angle, R omega, R mu, R mass, R inertia,
+                        uint32_t nverts, const float* verts, R d0, R d1) {
+        Body<R> b;
+        b.id = id;
+        b.type = POLYGON;
+        b.nverts = nverts;
+        b.num_normals = nverts;
+        b.width = d0;
+        b.height = d1;
+        for (uint32_t k = 0; k < nverts; ++k) b.local_vertices[k] = {R(verts[2 * k]), R(verts[2 * k + 1])};
+        b.props.pos = pos;
+        b.props.angle = angle;
+        b.props.mass = mass;
+        b.props.inertia = inertia;
+        b.props.mu = mu;
+        update_aabb(b);
+        b.props.momentum = scale2(vel, mass);
+        b.props.ang_momentum = omega * inertia;
         return append(b);
     }
 

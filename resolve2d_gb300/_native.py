@@ -36,6 +36,8 @@ FLAG_FP64_POSITIONS = 4
 FLAG_WARM_START = 8
 FLAG_SLEEP = 16
 FLAG_COMPENSATED = 32
+KIND_POLYGON = 4
+POLY_MAX_VERTS = 8
 MANIFOLD_FLOATS = 33
 
 
@@ -82,6 +84,7 @@ SIGNATURES = {
     "r2d_batch_sleep_frames": ([_P, _u32p], C.c_int),
     "r2d_solver_get_manifolds": ([_P, C.c_uint32, _u32p, _f32p, _u32p], C.c_int),
     "r2d_solver_get_joint_colours": ([_P, C.c_uint32, _u32p], C.c_int),
+    "r2d_solver_set_polygons": ([_P, C.c_uint32, _u32p, _u8p, _f32p], C.c_int),
     "r2d_solver_num_pairs": ([_P, _u32p], C.c_int),
     "r2d_solver_get_pairs": ([_P, C.c_uint32, _u32p], C.c_int),
     "r2d_batch_create": ([C.POINTER(Config), C.POINTER(_P)], C.c_int),
@@ -96,6 +99,7 @@ SIGNATURES = {
     "r2d_batch_world_status": ([_P, _i32p], C.c_int),
     "r2d_batch_num_manifolds": ([_P, C.c_uint32, _u32p], C.c_int),
     "r2d_batch_get_manifolds": ([_P, C.c_uint32, C.c_uint32, _u32p, _f32p, _u32p], C.c_int),
+    "r2d_batch_set_polygons": ([_P, C.c_uint32, _u32p, _u8p, _f32p], C.c_int),
     "r2d_batch_num_pairs": ([_P, C.c_uint32, _u32p], C.c_int),
     "r2d_batch_get_pairs": ([_P, C.c_uint32, C.c_uint32, _u32p], C.c_int),
     "r2d_solver_write_state_fields": ([_P, C.c_uint32, C.c_uint32, _f32p], C.c_int),

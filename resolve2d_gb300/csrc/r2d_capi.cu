@@ -97,6 +97,25 @@ void init_aabb(uint8_t kind, float x, float y, float angle, float d0, float d1, 
     out[3] = eh;
 }
 
+// A polygon's first AABB: its largest rotated vertex in x and y, from 0
+// (Rectangle.updateAABB over its vertices, Rectangle.zig:71-86).
+void init_aabb_polygon(float x, float y, float angle, const float* verts, uint32_t nv, float out[4]) {
+    float s, c;
+    r2d_sincosf(angle, &s, &c);
+    float ew = 0.f, eh = 0.f;
+    for (uint32_t i = 0; i < nv; ++i) {
+        const float lx = verts[2 * i], ly = verts[2 * i + 1];
+        const float rx = lx * c - ly * s;
+        const float ry = lx * s + ly * c;
+        if (rx > ew) ew = rx;
+        if (ry > eh) eh = ry;
+    }
+    out[0] = x;
+    out[1] = y;
+    out[2] = ew;
+    out[3] = eh;
+}
+
 struct KClass {
     Caps caps{};
     int threads = 128;
@@ -125,6 +144,14 @@ struct Engine {
     std::vector<uint8_t> kind_h;
     std::vector<float> props_h;
     std::vector<float> state_h;  // last uploaded (for capacity planning)
+    // Convex polygons (K_POLY bodies, stepped by the grid pipeline): vertex
+    // counts [nbodies] and local vertices [nbodies][MAX_POLY_VERTS][2]; the
+    // bodies whose first AABB waits for their vertices.
+    bool has_poly = false;
+    std::vector<uint8_t> poly_nv_h, poly_aabb_pending;
+    std::vector<float> poly_v_h;
+    uint8_t* d_poly_nv = nullptr;
+    float2* d_poly_v = nullptr;
 
     float* d_state = nullptr;
     double* d_pos64 = nullptr;  // [3][nbodies] f64 x, y, angle (R2D_FLAG_FP64_POSITIONS)
@@ -246,6 +273,7 @@ struct Engine {
         dfree(d_warm_hs);
         dfree(d_sleep);
         dfree(d_state); dfree(d_pos64); dfree(d_props); dfree(d_kind); dfree(d_ids); dfree(d_worlds);
+        dfree(d_poly_nv); dfree(d_poly_v);
         dfree(d_status); dfree(d_err);
         if (h_err) cudaFreeHost(h_err);
         dfree(d_jtype); dfree(d_jb1); dfree(d_jb2); dfree(d_jprm); dfree(d_excl);
@@ -338,6 +366,9 @@ struct Engine {
                         v.end());
             }
         }
+        for (uint32_t i = 0; i < n; ++i)
+            if ((kind[i] & K_RECT) && (kind[i] & K_POLY))
+                return fail(R2D_ERR_INVALID_ARGUMENT, "body " + std::to_string(i) + " is both a rectangle and a polygon");
         nworlds = nw;
         nbodies = n;
         ids_h.assign(ids, ids + n);
@@ -381,6 +412,21 @@ struct Engine {
         world_large.assign(nw, 0);
         const bool grid_all = (cfg.flags & R2D_FLAG_GRID_PIPELINE) != 0;
         for (uint32_t w = 0; w < nw; ++w) world_large[w] = grid_all || worlds_h[w].n > FUSED_MAX_BODIES;
+        // polygons: a world holding one steps on the grid pipeline; vertices
+        // come with r2d_*_set_polygons, and so do their first AABBs
+        has_poly = false;
+        poly_nv_h.assign(n, 0);
+        poly_aabb_pending.assign(n, 0);
+        poly_v_h.assign((size_t)n * 2 * MAX_POLY_VERTS, 0.f);
+        dfree(d_poly_nv);
+        dfree(d_poly_v);
+        for (uint32_t w = 0; w < nw; ++w)
+            for (uint32_t i = body_off[w]; i < body_off[w + 1]; ++i)
+                if (kind_h[i] & K_POLY) {
+                    has_poly = true;
+                    world_large[w] = 1;
+                    poly_aabb_pending[i] = do_init_aabb ? 1 : 0;
+                }
         large.clear();
         large.resize(nw);
         large_status.assign(nw, 0);
@@ -410,6 +456,49 @@ struct Engine {
         CUDA_TRY(cudaMemcpyAsync(d_ids, ids_h.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice, stream));
         CUDA_TRY(cudaStreamSynchronize(stream));
         plan_dirty = true;
+        return R2D_OK;
+    }
+
+    // Vertices of polygon bodies (global body indices): nverts 3..8 local
+    // vertices each, clockwise; a body whose first AABB was asked for at
+    // upload gets it now.
+    int set_polygons(uint32_t n, const uint32_t* body, const uint8_t* nverts, const float* verts) {
+        if (!d_state) return fail(R2D_ERR_INVALID_ARGUMENT, "no bodies");
+        for (uint32_t k = 0; k < n; ++k) {
+            const uint32_t i = body[k];
+            if (i >= nbodies) return fail(R2D_ERR_INVALID_ARGUMENT, "polygon body index " + std::to_string(i) + " out of range");
+            if (!(kind_h[i] & K_POLY))
+                return fail(R2D_ERR_INVALID_ARGUMENT, "body " + std::to_string(i) + " is not a polygon (R2D_KIND_POLYGON)");
+            if (nverts[k] < 3 || nverts[k] > MAX_POLY_VERTS)
+                return fail(R2D_ERR_INVALID_ARGUMENT, "a polygon has 3 to 8 vertices, body " + std::to_string(i));
+        }
+        CUDA_TRY(wake());
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        for (uint32_t k = 0; k < n; ++k) {
+            const uint32_t i = body[k];
+            poly_nv_h[i] = nverts[k];
+            std::copy(verts + (size_t)k * 2 * MAX_POLY_VERTS, verts + (size_t)(k + 1) * 2 * MAX_POLY_VERTS,
+                      poly_v_h.begin() + (size_t)i * 2 * MAX_POLY_VERTS);
+            if (poly_aabb_pending[i]) {
+                float ab[4];
+                const size_t N = nbodies;
+                init_aabb_polygon(state_h[(size_t)S_POS_X * N + i], state_h[(size_t)S_POS_Y * N + i],
+                                  state_h[(size_t)S_ANGLE * N + i], verts + (size_t)k * 2 * MAX_POLY_VERTS, nverts[k],
+                                  ab);
+                for (int f = 0; f < 4; ++f) {
+                    state_h[(size_t)(S_AABB_X + f) * N + i] = ab[f];
+                    CUDA_TRY(cudaMemcpy(d_state + (size_t)(S_AABB_X + f) * N + i, &ab[f], sizeof(float),
+                                        cudaMemcpyHostToDevice));
+                }
+                poly_aabb_pending[i] = 0;
+            }
+        }
+        if (!d_poly_nv) {
+            CUDA_TRY(dalloc(d_poly_nv, nbodies));
+            CUDA_TRY(dalloc(d_poly_v, (size_t)nbodies * MAX_POLY_VERTS));
+        }
+        CUDA_TRY(cudaMemcpy(d_poly_nv, poly_nv_h.data(), nbodies, cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaMemcpy(d_poly_v, poly_v_h.data(), sizeof(float) * poly_v_h.size(), cudaMemcpyHostToDevice));
         return R2D_OK;
     }
 
@@ -1085,6 +1174,11 @@ struct Engine {
     int process_step(float dt, uint32_t sub_steps, uint32_t iters) {
         if (sub_steps == 0) return fail(R2D_ERR_INVALID_ARGUMENT, "sub_steps must be >= 1");
         if (!d_state) return fail(R2D_ERR_INVALID_ARGUMENT, "no bodies");
+        if (has_poly)
+            for (uint32_t i = 0; i < nbodies; ++i)
+                if ((kind_h[i] & K_POLY) && poly_nv_h[i] < 3)
+                    return fail(R2D_ERR_INVALID_ARGUMENT,
+                                "polygon body " + std::to_string(i) + " has no vertices (r2d_*_set_polygons)");
         if ((sub_steps > 1) != plan_multi_substep) {
             plan_multi_substep = sub_steps > 1;
             plan_dirty = true;
@@ -1195,6 +1289,8 @@ struct Engine {
         in.verbose = verbose;
         in.sleep = d_sleep ? d_sleep + w : nullptr;
         in.colour_round_limit = colour_round_limit;
+        in.poly_v = has_poly ? d_poly_v : nullptr;
+        in.poly_nv = has_poly ? d_poly_nv : nullptr;
         return in;
     }
 
@@ -1758,6 +1854,12 @@ R2D_API int r2d_solver_read_positions_f64(r2d_solver* s, double* pose) {
     return guarded([&] { return s->eng.read_pose64(pose); });
 }
 
+R2D_API int r2d_solver_set_polygons(r2d_solver* s, uint32_t n, const uint32_t* body, const uint8_t* nverts,
+                                    const float* verts) {
+    if (!s || (n && (!body || !nverts || !verts))) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL handle or array");
+    return guarded([&] { return s->eng.set_polygons(n, body, nverts, verts); });
+}
+
 R2D_API int r2d_solver_num_pairs(r2d_solver* s, uint32_t* out) {
     if (!s || !out) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL handle or out pointer");
     return guarded([&] { return s->eng.num_pairs(0, out); });
@@ -1917,6 +2019,12 @@ R2D_API int r2d_batch_get_manifolds(r2d_batch* b, uint32_t w, uint32_t cap, uint
                                     uint32_t* colours) {
     if (!b) return fail(R2D_ERR_INVALID_ARGUMENT, "batch is NULL");
     return guarded([&] { return b->eng.get_manifolds(w, cap, keys, data, colours); });
+}
+
+R2D_API int r2d_batch_set_polygons(r2d_batch* b, uint32_t n, const uint32_t* body, const uint8_t* nverts,
+                                   const float* verts) {
+    if (!b || (n && (!body || !nverts || !verts))) return fail(R2D_ERR_INVALID_ARGUMENT, "NULL handle or array");
+    return guarded([&] { return b->eng.set_polygons(n, body, nverts, verts); });
 }
 
 R2D_API int r2d_batch_num_pairs(r2d_batch* b, uint32_t w, uint32_t* out) {

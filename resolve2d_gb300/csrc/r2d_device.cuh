@@ -129,28 +129,40 @@ R2D_DF void rect_half_extents(float width, float height, float c, float s, float
 }
 
 // a[i] for a runtime i without dynamic indexing (keeps a[] in registers)
-R2D_DF f2 sel4(const f2 a[4], uint32_t i) {
+template <int N>
+R2D_DF f2 selv(const f2 (&a)[N], uint32_t i) {
     f2 r = a[0];
-    r = i == 1u ? a[1] : r;
-    r = i == 2u ? a[2] : r;
-    r = i == 3u ? a[3] : r;
+#pragma unroll
+    for (int k = 1; k < N; ++k) r = i == (uint32_t)k ? a[k] : r;
     return r;
 }
 
 // ---- narrowphase geometry ----
-// One body as the SAT sees it.  For a rectangle the world vertices
-// (Rectangle.zig:88-98) and edge normals (Rectangle.zig:132-151) are
-// computed once; the reference recomputes the same values at every use.
-struct Geo {
+// One body as the SAT sees it.  For a rectangle (or, on the grid pipeline, a
+// convex polygon of up to MAXV vertices) the world vertices
+// (Rectangle.zig:88-98) and edge normals (Rectangle.zig:132-151) are computed
+// once; the reference recomputes the same values at every use.  A polygon is
+// the rectangle's code over its own vertex ring, the rectangle's winding
+// (clockwise, so that the counter-clockwise turn of an edge points out).
+template <int MAXV>
+struct GeoT {
     f2 pos;
     float radius;  // disc
-    bool rect;
-    f2 wv[4];      // rectangle world vertices
-    f2 en[4];      // rectangle edge normals (ccw90 of the normalised edge)
+    bool rect;     // has vertices: a rectangle or a polygon
+    uint32_t nv_;  // vertices (MAXV > 4 only)
+    f2 wv[MAXV];   // world vertices
+    f2 en[MAXV];   // edge normals (ccw90 of the normalised edge)
+    R2D_DF uint32_t nv() const { return MAXV == 4 ? 4u : nv_; }
+    R2D_DF uint32_t next(uint32_t i) const { return i + 1u == nv() ? 0u : i + 1u; }
 };
+using Geo = GeoT<4>;
+constexpr int MAX_POLY_VERTS = 8;
+using GeoPoly = GeoT<MAX_POLY_VERTS>;
 
-R2D_DF void geo_make(Geo& g, f2 pos, bool rect, float d0, float d1, float c, float s) {
+template <int MAXV>
+R2D_DF void geo_make(GeoT<MAXV>& g, f2 pos, bool rect, float d0, float d1, float c, float s) {
     g.pos = pos;
+    g.nv_ = 4u;
     g.rect = rect;
     g.radius = d0;
     if (!rect) return;
@@ -161,11 +173,46 @@ R2D_DF void geo_make(Geo& g, f2 pos, bool rect, float d0, float d1, float c, flo
     for (int i = 0; i < 4; ++i) g.en[i] = ccw90(normalize2(sub2(g.wv[(i + 1) & 3], g.wv[i])));
 }
 
+// A convex polygon of nv (3..MAX_POLY_VERTS) local vertices `local`.
+R2D_DF void geo_make_polygon(GeoPoly& g, f2 pos, const float2* __restrict__ local, uint32_t nv, float c, float s) {
+    g.pos = pos;
+    g.rect = true;
+    g.radius = 0.f;
+    g.nv_ = nv;
+#pragma unroll
+    for (int i = 0; i < MAX_POLY_VERTS; ++i) {
+        if ((uint32_t)i >= nv) break;
+        const float2 v = local[i];
+        g.wv[i] = add2(rot(f2{v.x, v.y}, c, s), pos);
+    }
+#pragma unroll
+    for (int i = 0; i < MAX_POLY_VERTS; ++i) {
+        if ((uint32_t)i >= nv) break;
+        g.en[i] = ccw90(normalize2(sub2(selv(g.wv, g.next(i)), g.wv[i])));
+    }
+}
+
+// A polygon's AABB half extents: Rectangle.updateAABB (Rectangle.zig:71-86)
+// over its vertices, from 0.
+R2D_DF void polygon_half_extents(const float2* __restrict__ local, uint32_t nv, float c, float s, float* hw,
+                                 float* hh) {
+    float ew = 0.f, eh = 0.f;
+    for (uint32_t i = 0; i < nv; ++i) {
+        const float2 v = local[i];
+        const f2 r = rot(f2{v.x, v.y}, c, s);
+        if (r.x > ew) ew = r.x;
+        if (r.y > eh) eh = r.y;
+    }
+    *hw = ew;
+    *hh = eh;
+}
+
 // geo_make with a rectangle's edge normals taken from `en` (two float4:
 // normals 0, 1 then 2, 3) as geo_make computed them for the same pose, so
 // the values are the same bits; the vertices are recomputed (no division).
 R2D_DF void geo_make_cached(Geo& g, f2 pos, bool rect, float d0, float d1, float c, float s, const float4* en) {
     g.pos = pos;
+    g.nv_ = 4u;
     g.rect = rect;
     g.radius = d0;
     if (!rect) return;
@@ -180,7 +227,8 @@ R2D_DF void geo_make_cached(Geo& g, f2 pos, bool rect, float d0, float d1, float
 }
 
 // closestPoint (Disc.zig:80-84; Rectangle.zig:114-130 -- the nearest vertex)
-R2D_DF f2 closest_point(const Geo& g, f2 p) {
+template <int MAXV>
+R2D_DF f2 closest_point(const GeoT<MAXV>& g, f2 p) {
     if (!g.rect) {
         f2 n = normalize2(sub2(p, g.pos));
         return addmult2(g.pos, n, g.radius);
@@ -188,7 +236,8 @@ R2D_DF f2 closest_point(const Geo& g, f2 p) {
     float best = __int_as_float(0x7f800000);
     f2 bp = p;
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
+    for (int i = 0; i < MAXV; ++i) {
+        if ((uint32_t)i >= g.nv()) break;
         f2 d = sub2(g.wv[i], p);
         float d2 = dot2(d, d);
         if (d2 < best) {
@@ -200,7 +249,8 @@ R2D_DF f2 closest_point(const Geo& g, f2 p) {
 }
 
 // projectAlongAxis (Disc.zig:92-97; Rectangle.zig:153-169)
-R2D_DF void project(const Geo& g, f2 n, float* lo, float* hi) {
+template <int MAXV>
+R2D_DF void project(const GeoT<MAXV>& g, f2 n, float* lo, float* hi) {
     if (!g.rect) {
         float mid = dot2(g.pos, n);
         *lo = mid - g.radius;
@@ -209,7 +259,8 @@ R2D_DF void project(const Geo& g, f2 n, float* lo, float* hi) {
     }
     float l = __int_as_float(0x7f800000), h = __int_as_float(0xff800000);
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
+    for (int i = 0; i < MAXV; ++i) {
+        if ((uint32_t)i >= g.nv()) break;
         float d = dot2(g.wv[i], n);
         if (d < l) l = d;
         if (d > h) h = d;
@@ -226,13 +277,14 @@ struct SatState {
 };
 
 // overlapSAT (collision.zig:228-289) with `reference` = R, `incident` = I.
-R2D_DF bool overlap_sat(SatState& ret, const Geo& R, const Geo& I, bool r_is_o1) {
+template <int MAXV>
+R2D_DF bool overlap_sat(SatState& ret, const GeoT<MAXV>& R, const GeoT<MAXV>& I, bool r_is_o1) {
     const float EPS = SAT_OVERLAP_THRESHOLD;
-    const int nn = R.rect ? 4 : 1;
+    const int nn = R.rect ? (int)R.nv() : 1;
     f2 disc_axis = {0.f, 0.f};
     if (!R.rect) disc_axis = normalize2(sub2(closest_point(I, R.pos), R.pos));  // Disc.zig:86-90
 #pragma unroll
-    for (int it = 0; it < 4; ++it) {
+    for (int it = 0; it < MAXV; ++it) {
         if (it >= nn) break;
         f2 normal = R.rect ? R.en[it] : disc_axis;
         bool flipped = false;
@@ -279,7 +331,8 @@ R2D_DF bool overlap_sat(SatState& ret, const Geo& R, const Geo& I, bool r_is_o1)
 // performNarrowSAT (collision.zig:299-320): o1 = lower id.  The reference
 // leaves ret.normal/key undefined until the first axis writes them; the
 // start value here is normal (0,0), reference = o1, edge 0.
-R2D_DF bool perform_narrow_sat(const Geo& o1, const Geo& o2, SatState& ret) {
+template <int MAXV>
+R2D_DF bool perform_narrow_sat(const GeoT<MAXV>& o1, const GeoT<MAXV>& o2, SatState& ret) {
     ret.normal = {0.f, 0.f};
     ret.penetration = __int_as_float(0x7f800000);
     ret.refid = 0;
@@ -336,7 +389,8 @@ R2D_DF void clip_line_to_line(f2 aa, f2 ab, f2 ba, f2 bb, f2* p1o, f2* p2o) {
 // identifyCollisionPoints (Disc.zig:99-123; Rectangle.zig:171-211 with
 // clipAgainstEdge Disc.zig:125-130 / Rectangle.zig:213-238).  Returns the
 // number of points written (0..2).
-R2D_DF int identify_points(const Geo& ref, const Geo& inc, uint32_t refid, NewPoint out[2]) {
+template <int MAXV>
+R2D_DF int identify_points(const GeoT<MAXV>& ref, const GeoT<MAXV>& inc, uint32_t refid, NewPoint out[2]) {
     if (!ref.rect) {
         f2 pos = closest_point(inc, ref.pos);
         f2 normal = normalize2(sub2(pos, ref.pos));  // Disc.getNormal recomputes the same point
@@ -346,9 +400,9 @@ R2D_DF int identify_points(const Geo& ref, const Geo& inc, uint32_t refid, NewPo
         out[0] = make_point(pos, depth, ref.pos, inc.pos, normal);
         return 1;
     }
-    const f2 ea = sel4(ref.wv, refid);
-    const f2 eb = sel4(ref.wv, (refid + 1) & 3);
-    const f2 ndir = sel4(ref.en, refid);
+    const f2 ea = selv(ref.wv, refid);
+    const f2 eb = selv(ref.wv, ref.next(refid));
+    const f2 ndir = selv(ref.en, refid);
     if (!inc.rect) {
         f2 pos = addmult2(inc.pos, ndir, -inc.radius);
         float dot = dot2(sub2(pos, ea), ndir);
@@ -359,7 +413,8 @@ R2D_DF int identify_points(const Geo& ref, const Geo& inc, uint32_t refid, NewPo
     bool found = false;
     float best_dot = __int_as_float(0x7f800000);
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
+    for (int i = 0; i < MAXV; ++i) {
+        if ((uint32_t)i >= inc.nv()) break;
         float d = dot2(ndir, inc.en[i]);
         if (d < best_dot) {
             best_dot = d;
@@ -369,7 +424,7 @@ R2D_DF int identify_points(const Geo& ref, const Geo& inc, uint32_t refid, NewPo
     }
     if (!found) best = 0;  // every dot NaN: the reference reads an undefined edge
     f2 pa, pb;
-    clip_line_to_line(ea, eb, sel4(inc.wv, best), sel4(inc.wv, (best + 1) & 3), &pa, &pb);
+    clip_line_to_line(ea, eb, selv(inc.wv, best), selv(inc.wv, inc.next(best)), &pa, &pb);
     const float dot_a = dot2(sub2(pa, ea), ndir);
     const float dot_b = dot2(sub2(pb, eb), ndir);
     const bool ha = dot_a < COLLISION_MARGIN, hb = dot_b < COLLISION_MARGIN;

@@ -68,6 +68,7 @@ enum LargeCounter : int {
     LC_ROUNDS,         // the rounds that colouring needed
     LC_MOVING,         // some non-static body ended the step moving (sleeping mode)
     LC_STUCK,          // a colouring ran more rounds than it has constraints (cannot happen)
+    LC_NOPOLY,         // a polygon body where no vertices are given (the allocation-free step)
     LC_N
 };
 
@@ -185,6 +186,10 @@ struct Phase1 {
     uint32_t nexcl;
     uint32_t* cnt;
     unsigned long long* entries;  // total cell entries (64-bit)
+    // convex polygons of the engine (K_POLY bodies): local vertices
+    // [NB][MAX_POLY_VERTS] and counts [NB]; null when it has none
+    const float2* poly_v;
+    const uint8_t* poly_nv;
 
     __device__ float st(int f, uint32_t i) const { return state[(size_t)f * NB + base + i]; }
     __device__ float pr(int f, uint32_t i) const { return __ldg(props + (size_t)f * NB + base + i); }
@@ -196,12 +201,13 @@ __device__ __forceinline__ uint32_t load_body(const Phase1& A, uint32_t i) {
     const uint8_t k = __ldg(A.kind_in + A.base + i);
     const float a = A.st(S_ANGLE, i);
     A.s.kind[i] = k;
+    if ((k & K_POLY) && !A.poly_v) atomicExch(&A.cnt[LC_NOPOLY], 1u);
     const float inv_m = (k & K_STATIC) ? 0.f : 1.0f / A.pr(P_MASS, i);
     const float inv_i = (k & K_STATIC) ? 0.f : 1.0f / A.pr(P_INERTIA, i);
     A.s.inv_m[i] = inv_m;
     A.s.inv_i[i] = inv_i;
     float c = 1.f, sn = 0.f;
-    if ((k & K_RECT) || A.disc_rot) r2d_sincosf(a, &sn, &c);
+    if ((k & (K_RECT | K_POLY)) || A.disc_rot) r2d_sincosf(a, &sn, &c);
     A.s.cs[i] = c;
     A.s.sn[i] = sn;
     A.s.ang_prev[i] = a;
@@ -331,6 +337,19 @@ __global__ void lk_pairs(Phase1 A, uint32_t E) {
     }
 }
 
+// Body i as the polygon-capable SAT sees it: a disc, a rectangle (its four
+// vertices) or a polygon (its own ring).
+__device__ __forceinline__ void narrow_geo(const Phase1& A, uint32_t i, GeoPoly& g) {
+    const SWT<uint32_t>& s = A.s;
+    const uint8_t k = s.kind[i];
+    if (k & K_POLY) {
+        const size_t gi = (size_t)A.base + i;
+        geo_make_polygon(g, f2{s.px[i], s.py[i]}, A.poly_v + gi * MAX_POLY_VERTS, A.poly_nv[gi], s.cs[i], s.sn[i]);
+    } else {
+        geo_make(g, f2{s.px[i], s.py[i]}, k & K_RECT, A.pr(P_DIM0, i), A.pr(P_DIM1, i), s.cs[i], s.sn[i]);
+    }
+}
+
 // performNarrowSAT + manifold build (collision.zig:299-320, lib.zig:284-294)
 __global__ void lk_narrow(Phase1 A, uint32_t npairs) {
     const uint32_t pi = blockIdx.x * LT + threadIdx.x;
@@ -340,14 +359,25 @@ __global__ void lk_narrow(Phase1 A, uint32_t npairs) {
     const uint32_t lo = (uint32_t)(key >> 32), hi = (uint32_t)key;
     const uint32_t o1 = __ldg(A.ids + A.base + lo) < __ldg(A.ids + A.base + hi) ? lo : hi;
     const uint32_t o2 = o1 == lo ? hi : lo;
-    Geo g1, g2;
-    geo_make(g1, f2{s.px[o1], s.py[o1]}, s.kind[o1] & K_RECT, A.pr(P_DIM0, o1), A.pr(P_DIM1, o1), s.cs[o1], s.sn[o1]);
-    geo_make(g2, f2{s.px[o2], s.py[o2]}, s.kind[o2] & K_RECT, A.pr(P_DIM0, o2), A.pr(P_DIM1, o2), s.cs[o2], s.sn[o2]);
     SatState sat;
-    if (!perform_narrow_sat(g1, g2, sat)) return;
-    const uint32_t ref = sat.ref_is_first ? o1 : o2, inc = sat.ref_is_first ? o2 : o1;
     NewPoint pts[2];
-    const int npt = sat.ref_is_first ? identify_points(g1, g2, sat.refid, pts) : identify_points(g2, g1, sat.refid, pts);
+    int npt = 0;
+    if (A.poly_v) {  // an engine with polygons: every pair through the polygon-capable geometry
+        GeoPoly g1, g2;
+        narrow_geo(A, o1, g1);
+        narrow_geo(A, o2, g2);
+        if (!perform_narrow_sat(g1, g2, sat)) return;
+        npt = sat.ref_is_first ? identify_points(g1, g2, sat.refid, pts) : identify_points(g2, g1, sat.refid, pts);
+    } else {
+        Geo g1, g2;
+        geo_make(g1, f2{s.px[o1], s.py[o1]}, s.kind[o1] & K_RECT, A.pr(P_DIM0, o1), A.pr(P_DIM1, o1), s.cs[o1],
+                 s.sn[o1]);
+        geo_make(g2, f2{s.px[o2], s.py[o2]}, s.kind[o2] & K_RECT, A.pr(P_DIM0, o2), A.pr(P_DIM1, o2), s.cs[o2],
+                 s.sn[o2]);
+        if (!perform_narrow_sat(g1, g2, sat)) return;
+        npt = sat.ref_is_first ? identify_points(g1, g2, sat.refid, pts) : identify_points(g2, g1, sat.refid, pts);
+    }
+    const uint32_t ref = sat.ref_is_first ? o1 : o2, inc = sat.ref_is_first ? o2 : o1;
     const uint32_t m = atomicAdd(&A.cnt[LC_MANIFOLDS], 1u);
     const uint32_t p0 = atomicAdd(&A.cnt[LC_POINTS], (uint32_t)npt);
     if (m >= A.nm || p0 + npt > A.npt) return;  // cannot happen: sized from the pair count
@@ -888,6 +918,8 @@ struct Phase2 {
     const float* jprm_cm;   // and their parameters, [k][JOINT_PARAMS]
     uint32_t k0, k1;        // the colour-major constraints one per-colour launch solves
     double* pos64;          // f64 pose (FP64-positions mode), else null
+    const float2* poly_v;   // polygons (as Phase1), else null
+    const uint8_t* poly_nv;
     bool warm;              // warm starting
 
     __device__ float& st(int f, uint32_t i) const { return state[(size_t)f * NB + base + i]; }
@@ -914,7 +946,10 @@ __device__ __forceinline__ void forces_one(const Phase2& A, uint32_t i, bool fir
     }
     if (last) {
         float hw, hh;
-        if (k & K_RECT) {
+        if (k & K_POLY) {
+            const size_t gi = (size_t)A.base + i;
+            polygon_half_extents(A.poly_v + gi * MAX_POLY_VERTS, A.poly_nv[gi], s.cs[i], s.sn[i], &hw, &hh);
+        } else if (k & K_RECT) {
             rect_half_extents(A.pr(P_DIM0, i), A.pr(P_DIM1, i), s.cs[i], s.sn[i], &hw, &hh);
         } else {
             hw = hh = A.pr(P_DIM0, i);
@@ -1165,7 +1200,7 @@ __device__ __forceinline__ void integrate_one(const Phase2& A, uint32_t i, bool 
         s.ang[i] += s.L[i] * A.h / s.inertia(i);
     }
     s.tq[i] = 0.f;
-    if (!last && ((k & K_RECT) || A.disc_rot)) {
+    if (!last && ((k & (K_RECT | K_POLY)) || A.disc_rot)) {
         float c, sn;
         r2d_sincosf(s.ang[i], &sn, &c);
         s.cs[i] = c;
@@ -1629,6 +1664,7 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
     Phase1 A{};
     A.s = I.views(in);
     A.state = in.state; A.props = in.props; A.kind_in = in.kind; A.ids = in.ids;
+    A.poly_v = in.poly_v; A.poly_nv = in.poly_nv;
     A.NB = in.NB; A.base = in.base; A.n = n; A.cell = in.cell;
     A.bmod = BucketMod{bucket_recip(T), T};
     A.disc_rot = in.disc_rot;
@@ -1829,6 +1865,7 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
     Phase2 S{};
     S.s = I.views(in);
     S.state = in.state; S.props = in.props; S.NB = in.NB; S.base = in.base; S.n = n; S.nman = M;
+    S.poly_v = in.poly_v; S.poly_nv = in.poly_nv;
     S.h = dt / (float)sub_steps;
     S.disc_rot = in.disc_rot;
     S.ngrav = in.ngrav;
@@ -2175,6 +2212,10 @@ int static_world_step(const StaticStepArgs& in, cudaStream_t st, std::string* ms
     if (h[LC_NONFINITE]) {
         *msg = "a body's AABB is not finite (it has no spatial-hash cell)";
         return DS_NONFINITE;
+    }
+    if (h[LC_NOPOLY]) {
+        *msg = "a polygon body (R2D_KIND_POLYGON): this step takes discs and rectangles only";
+        return -1;  // R2D_ERR_INVALID_ARGUMENT
     }
     unsigned long long E64 = 0;
     memcpy(&E64, h + LC_N, sizeof(E64));

@@ -42,6 +42,8 @@ struct LargeInputs {
     bool verbose;          // print each step's phase times and counts to stderr
     uint32_t* sleep;       // this world's still-frame counter (sleeping mode, r2d_sleep.h), else null
     uint32_t colour_round_limit;  // colouring rounds before R2D_ERR_TIMEOUT (0 = never reached)
+    const float2* poly_v;  // [NB][MAX_POLY_VERTS] local vertices of the engine's polygons, else null
+    const uint8_t* poly_nv;  // [NB] their vertex counts
 };
 
 class LargeWorld {

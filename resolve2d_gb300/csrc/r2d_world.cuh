@@ -15,7 +15,8 @@ enum StateField : int {
     S_NFIELDS
 };
 enum PropField : int { P_MASS = 0, P_INERTIA, P_MU, P_DIM0, P_DIM1, P_NFIELDS };
-enum KindBits : uint8_t { K_RECT = 1, K_STATIC = 2, K_FORCED = 0x80 /* device-only: force/torque to clear */ };
+// K_POLY: a convex polygon (grid pipeline only; its vertices live beside the props)
+enum KindBits : uint8_t { K_RECT = 1, K_STATIC = 2, K_POLY = 4, K_FORCED = 0x80 /* device-only: force/torque to clear */ };
 enum JointTypes : uint8_t { J_DISTANCE = 0, J_OFFSET = 1, J_FIXED = 2, J_MOTOR = 3 };
 enum WorldFlags : uint32_t { W_DISC_ROTATION = 2u };
 

@@ -9,7 +9,20 @@ import ctypes as C
 import numpy as np
 
 from . import _native as N
-from .scenes import NSTATE, Scene, derive_props_state
+from .scenes import KIND_POLY, NSTATE, Scene, derive_props_state
+
+
+def device_kind(kind) -> np.ndarray:
+    """A scene's kind bits as the library takes them: rectangle 1, static 2,
+    polygon 4 (the scene's mass-by-density bit stays on the host)."""
+    k = np.asarray(kind).astype(np.uint8)
+    return ((k & 3) | ((k & KIND_POLY) >> 1)).astype(np.uint8)
+
+
+def _polygon_rows(sc: Scene):
+    """(body indices, vertex counts, vertices [k][8][2]) of a scene's polygons."""
+    idx = np.flatnonzero(sc.poly_nv).astype(np.uint32)
+    return idx, np.ascontiguousarray(sc.poly_nv[idx], np.uint8), np.ascontiguousarray(sc.poly_v[idx], np.float32)
 
 
 def _rows(a, k: int, n: int) -> np.ndarray:
@@ -72,6 +85,15 @@ class World:
                                                 N.ptr(props, C.c_float), N.ptr(state, C.c_float), int(init_aabb)),
                 "r2d_solver_set_bodies")
 
+    def set_polygons(self, body, nverts, verts):
+        """Vertices of the polygon bodies at store indices `body`
+        (r2d_solver_set_polygons): nverts [k], verts [k][8][2]."""
+        body, nverts = N.u32(body), N.u8(nverts)
+        verts = np.ascontiguousarray(np.asarray(verts, np.float32).reshape(-1, N.POLY_MAX_VERTS, 2))
+        N.check(self._lib.r2d_solver_set_polygons(self._h, int(body.shape[0]), N.ptr(body, C.c_uint32),
+                                                  N.ptr(nverts, C.c_uint8), N.ptr(verts, C.c_float)),
+                "r2d_solver_set_polygons")
+
     def set_gravity(self, g):
         g = N.f32(np.atleast_1d(g))
         N.check(self._lib.r2d_solver_set_gravity(self._h, int(g.shape[0]), N.ptr(g, C.c_float)), "r2d_solver_set_gravity")
@@ -94,7 +116,9 @@ class World:
         w = cls(debug=debug, stream=stream, **kw)
         props, state = derive_props_state(sc.kind, sc.opt)
         w.set_gravity(sc.gravity[sc.gravity != 0] if sc.gravity.size else np.zeros(0, np.float32))
-        w.set_bodies(sc.ids, sc.kind & 3, props, state, init_aabb=True)
+        w.set_bodies(sc.ids, device_kind(sc.kind), props, state, init_aabb=True)
+        if sc.has_polygons:
+            w.set_polygons(*_polygon_rows(sc))
         if sc.jtype.size:
             w.set_joints(sc.jtype, sc.jid1, sc.jid2, sc.jprm)
         if sc.xpairs.size:
@@ -215,13 +239,24 @@ class Batch:
                                                N.ptr(props, C.c_float), N.ptr(state, C.c_float),
                                                N.ptr(gravity, C.c_float), int(init_aabb)), "r2d_batch_set_worlds")
 
+    def set_polygons(self, body, nverts, verts):
+        """Vertices of the polygon bodies at indices `body` of the
+        concatenated store (r2d_batch_set_polygons)."""
+        body, nverts = N.u32(body), N.u8(nverts)
+        verts = np.ascontiguousarray(np.asarray(verts, np.float32).reshape(-1, N.POLY_MAX_VERTS, 2))
+        N.check(self._lib.r2d_batch_set_polygons(self._h, int(body.shape[0]), N.ptr(body, C.c_uint32),
+                                                 N.ptr(nverts, C.c_uint8), N.ptr(verts, C.c_float)),
+                "r2d_batch_set_polygons")
+
     @classmethod
     def from_scene(cls, sc: Scene, debug: bool = False, stream=None, **kw) -> "Batch":
         if sc.jtype.size or sc.xpairs.size:
             raise ValueError("the batch entry points take worlds without joints or exclusions (use World)")
         b = cls(debug=debug, stream=stream, **kw)
         props, state = derive_props_state(sc.kind, sc.opt)
-        b.set_worlds(sc.body_off, sc.ids, sc.kind & 3, props, state, sc.gravity, init_aabb=True)
+        b.set_worlds(sc.body_off, sc.ids, device_kind(sc.kind), props, state, sc.gravity, init_aabb=True)
+        if sc.has_polygons:
+            b.set_polygons(*_polygon_rows(sc))
         return b
 
     def write_state(self, state):

@@ -23,8 +23,10 @@ import numpy as np
 # body option fields, float32 field-major [NOPT][n]
 POS_X, POS_Y, ANGLE, VEL_X, VEL_Y, OMEGA, MU, MASS_PROP, DIM0, DIM1 = range(10)
 NOPT = 10
-# kind bits
-KIND_RECT, KIND_STATIC, KIND_DENSITY = 1, 2, 4
+# kind bits (KIND_POLY: a convex polygon, whose vertices are Scene.poly_v;
+# its opt MASS_PROP is its mass and DIM1 its inertia, DIM0 its bounding radius)
+KIND_RECT, KIND_STATIC, KIND_DENSITY, KIND_POLY = 1, 2, 4, 8
+MAX_POLY_VERTS = 8
 # state / prop fields (include/r2d_gb300.h)
 NSTATE, NPROP = 13, 5
 S_POS_X, S_POS_Y, S_ANGLE, S_MOM_X, S_MOM_Y, S_ANG_MOM = range(6)
@@ -57,6 +59,20 @@ class Scene:
     jprm: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros((0, JOINT_PARAMS), np.float32))
     xworld: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros(0, np.uint32))
     xpairs: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros((0, 2), np.uint32))
+    # convex polygons: vertex counts [n] (0 for other bodies) and local
+    # vertices [n][MAX_POLY_VERTS][2], clockwise about the body's origin;
+    # empty arrays when the scene has none
+    poly_nv: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros(0, np.uint8))
+    poly_v: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros((0, MAX_POLY_VERTS, 2), np.float32))
+
+    @property
+    def has_polygons(self) -> bool:
+        return bool(self.poly_nv.size) and bool((self.poly_nv > 0).any())
+
+    def _poly_rows(self, rows):
+        if not self.poly_nv.size:
+            return {}
+        return {"poly_nv": self.poly_nv[rows].copy(), "poly_v": self.poly_v[rows].copy()}
 
     @property
     def nworlds(self) -> int:
@@ -82,6 +98,7 @@ class Scene:
             jworld=np.zeros(int(jm.sum()), np.uint32), jtype=self.jtype[jm], jid1=self.jid1[jm],
             jid2=self.jid2[jm], jprm=self.jprm[jm],
             xworld=np.zeros(int(xm.sum()), np.uint32), xpairs=self.xpairs[xm],
+            **self._poly_rows(slice(b0, b1)),
         )
 
     def worlds(self, w0: int, w1: int) -> "Scene":
@@ -97,6 +114,7 @@ class Scene:
             body_off=(self.body_off[w0 : w1 + 1] - self.body_off[w0]).astype(np.uint32),
             gravity=self.gravity[w0:w1].copy(),
             dt=self.dt, sub_steps=self.sub_steps, iters=self.iters, steps=self.steps,
+            **self._poly_rows(slice(b0, b1)),
         )
 
     def select(self, worlds) -> "Scene":
@@ -116,13 +134,19 @@ class Scene:
             body_off=np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint32),
             gravity=self.gravity[worlds].copy(),
             dt=self.dt, sub_steps=self.sub_steps, iters=self.iters, steps=self.steps,
+            **self._poly_rows(rows),
         )
 
     def body_radius(self) -> np.ndarray:
         """Size of each body for error figures: a disc's radius, half the
         shorter side of a rectangle."""
         rect = (self.kind & KIND_RECT) != 0
-        return np.where(rect, 0.5 * np.minimum(self.opt[DIM0], self.opt[DIM1]), self.opt[DIM0]).astype(np.float64)
+        r = np.where(rect, 0.5 * np.minimum(self.opt[DIM0], self.opt[DIM1]), self.opt[DIM0]).astype(np.float64)
+        if self.has_polygons:  # a polygon: its smallest vertex distance
+            for i in np.flatnonzero(self.poly_nv):
+                v = self.poly_v[i, : self.poly_nv[i]].astype(np.float64)
+                r[i] = float(np.min(np.hypot(v[:, 0], v[:, 1])))
+        return r
 
 
 def derive_props_state(kind: np.ndarray, opt: np.ndarray):
@@ -138,22 +162,23 @@ def derive_props_state(kind: np.ndarray, opt: np.ndarray):
     """
     f = np.float32
     n = kind.shape[0]
-    rect = (kind & KIND_RECT) != 0
+    poly = (kind & KIND_POLY) != 0
+    rect = ((kind & KIND_RECT) != 0) & ~poly
     dens = (kind & KIND_DENSITY) != 0
     d0, d1, mp = opt[DIM0].astype(f), opt[DIM1].astype(f), opt[MASS_PROP].astype(f)
     pi32 = f(math.pi)
     disc_mass = ((pi32 * d0) * d0) * mp
     rect_mass = (d0 * d1) * mp
-    mass = np.where(dens, np.where(rect, rect_mass, disc_mass), mp).astype(f)
+    mass = np.where(dens & ~poly, np.where(rect, rect_mass, disc_mass), mp).astype(f)
     disc_i = ((f(0.5) * mass) * d0) * d0
     rect_i = (mass * ((d0 * d0) + (d1 * d1))) / f(12)
-    inertia = np.where(rect, rect_i, disc_i).astype(f)
+    inertia = np.where(poly, d1, np.where(rect, rect_i, disc_i)).astype(f)
     props = np.zeros((NPROP, n), f)
     props[P_MASS] = mass
     props[P_INERTIA] = inertia
     props[P_MU] = opt[MU]
     props[P_DIM0] = d0
-    props[P_DIM1] = np.where(rect, d1, f(0))
+    props[P_DIM1] = np.where(rect | poly, d1, f(0))
     state = np.zeros((NSTATE, n), f)
     state[S_POS_X] = opt[POS_X]
     state[S_POS_Y] = opt[POS_Y]
@@ -169,6 +194,7 @@ class _Builder:
 
     def __init__(self):
         self.rows: list[tuple] = []
+        self.polys: dict[int, tuple] = {}
 
     def disc(self, x, y, r, mu, density=1.0, vx=0.0, vy=0.0, angle=0.0, omega=0.0, static=False):
         k = KIND_DENSITY | (KIND_STATIC if static else 0)
@@ -180,6 +206,47 @@ class _Builder:
         self.rows.append((k, x, y, angle, vx, vy, omega, mu, density, w, h))
         return len(self.rows) - 1
 
+    def polygon(self, x, y, verts, mu, density=1.0, vx=0.0, vy=0.0, angle=0.0, omega=0.0, static=False):
+        """A convex polygon of uniform density: `verts` (k x 2, 3 <= k <= 8)
+        about any point; they are shifted to the centroid, ordered
+        clockwise, and the mass and inertia integrated over the shape
+        (float64, then float32)."""
+        v = np.asarray(verts, np.float64).reshape(-1, 2)
+        k = v.shape[0]
+        if not 3 <= k <= MAX_POLY_VERTS:
+            raise ValueError(f"a polygon has 3 to {MAX_POLY_VERTS} vertices, not {k}")
+        c = v.mean(axis=0)
+        v = v[np.argsort(-np.arctan2(v[:, 1] - c[1], v[:, 0] - c[0]), kind="stable")]  # clockwise
+        x0, y0, x1, y1 = v[:, 0], v[:, 1], np.roll(v[:, 0], -1), np.roll(v[:, 1], -1)
+        cr = x0 * y1 - x1 * y0
+        area = 0.5 * cr.sum()
+        cx = ((x0 + x1) * cr).sum() / (6.0 * area)
+        cy = ((y0 + y1) * cr).sum() / (6.0 * area)
+        v = v - np.array([cx, cy])
+        x0, y0, x1, y1 = v[:, 0], v[:, 1], np.roll(v[:, 0], -1), np.roll(v[:, 1], -1)
+        cr = x0 * y1 - x1 * y0
+        area = abs(0.5 * cr.sum())
+        second = abs((cr * (x0 * x0 + x0 * x1 + x1 * x1 + y0 * y0 + y0 * y1 + y1 * y1)).sum()) / 12.0
+        mass = density * area
+        inertia = density * second
+        bound = float(np.max(np.hypot(v[:, 0], v[:, 1])))
+        kd = KIND_POLY | (KIND_STATIC if static else 0)
+        self.rows.append((kd, x, y, angle, vx, vy, omega, mu, mass, bound, inertia))
+        pv = np.zeros((MAX_POLY_VERTS, 2), np.float32)
+        pv[:k] = v
+        self.polys[len(self.rows) - 1] = (k, pv)
+        return len(self.rows) - 1
+
+    def polygon_arrays(self):
+        """(poly_nv [n], poly_v [n][8][2]) of the bodies added so far."""
+        n = len(self.rows)
+        nv = np.zeros(n, np.uint8)
+        pv = np.zeros((n, MAX_POLY_VERTS, 2), np.float32)
+        for i, (k, v) in self.polys.items():
+            nv[i] = k
+            pv[i] = v
+        return nv, pv
+
     def arrays(self):
         n = len(self.rows)
         kind = np.array([r[0] for r in self.rows], np.uint8).reshape(n)
@@ -187,7 +254,7 @@ class _Builder:
         return np.arange(n, dtype=np.uint32), kind, np.ascontiguousarray(opt)
 
 
-def _concat(name, worlds, gravity, dt, sub_steps, iters, steps, joints=None, excl=None) -> Scene:
+def _concat(name, worlds, gravity, dt, sub_steps, iters, steps, joints=None, excl=None, polys=None) -> Scene:
     ids, kinds, opts, off = [], [], [], [0]
     for (i, k, o) in worlds:
         ids.append(i)
@@ -207,6 +274,9 @@ def _concat(name, worlds, gravity, dt, sub_steps, iters, steps, joints=None, exc
         sc.jworld, sc.jtype, sc.jid1, sc.jid2, sc.jprm = joints
     if excl is not None:
         sc.xworld, sc.xpairs = excl
+    if polys is not None:  # one (poly_nv, poly_v) per world
+        sc.poly_nv = np.concatenate([p[0] for p in polys]).astype(np.uint8)
+        sc.poly_v = np.ascontiguousarray(np.concatenate([p[1] for p in polys]).astype(np.float32))
     return sc
 
 
@@ -398,6 +468,44 @@ def random_scene(seed: int, n: int = 40, rect_p: float = 0.5, box: float = 8.0, 
         js = (np.zeros(len(jt), np.uint32), np.array(jt, np.uint8), np.array(j1, np.uint32),
               np.array(j2, np.uint32), np.array(jp, np.float32).reshape(-1, JOINT_PARAMS))
     return _concat(f"random{seed}", [b.arrays()], [9.81], 1 / 60, 1, 8, 60, joints=js)
+
+
+def random_polygon(rng, r_lo=0.3, r_hi=1.0):
+    """A random convex polygon of 3 to 8 vertices: points at jittered, evenly
+    spaced angles on a circle (so every vertex is a corner of the hull)."""
+    k = int(rng.integers(3, MAX_POLY_VERTS + 1))
+    r = rng.uniform(r_lo, r_hi)
+    a = (np.arange(k) + rng.uniform(-0.3, 0.3, k)) * (2.0 * math.pi / k)
+    return np.stack([r * np.cos(a), r * np.sin(a)], axis=1)
+
+
+def polygon_scene(seed: int, n: int = 40, box: float = 8.0, poly_p: float = 0.4, rect_p: float = 0.3,
+                  static_p: float = 0.1, worlds: int = 1) -> Scene:
+    """Random worlds mixing convex polygons (3-8 vertices) with discs and
+    rectangles over a static ground, with random angles and velocities:
+    every pair type (polygon-polygon, -rectangle, -disc) meets."""
+    rng = np.random.default_rng(seed)
+    parts, polys = [], []
+    for _ in range(worlds):
+        b = _Builder()
+        b.rect(0.0, -0.5, 3 * box, 1.0, 0.5, static=True)
+        for _ in range(n):
+            x, y = rng.uniform(-box, box), rng.uniform(0.0, box)
+            st = rng.random() < static_p
+            vx, vy = (0.0, 0.0) if st else (rng.normal(), rng.normal())
+            ang, om, mu = rng.uniform(-math.pi, math.pi), rng.normal(), rng.uniform(0.1, 0.9)
+            u = rng.random()
+            if u < poly_p:
+                b.polygon(x, y, random_polygon(rng), mu, vx=vx, vy=vy, angle=ang, omega=om, static=st)
+            elif u < poly_p + rect_p:
+                b.rect(x, y, rng.uniform(0.3, 2.0), rng.uniform(0.3, 2.0), mu, vx=vx, vy=vy, angle=ang, omega=om,
+                       static=st)
+            else:
+                b.disc(x, y, rng.uniform(0.2, 1.0), mu, vx=vx, vy=vy, angle=ang, omega=om, static=st)
+        parts.append(b.arrays())
+        polys.append(b.polygon_arrays())
+    g = [9.81] * worlds
+    return _concat(f"polygons{seed}", parts, g, 1 / 60, 1, 8, 60, polys=polys)
 
 
 CONFIGS = {0: config0, 1: config1, 2: config2, 3: config3, 4: config4}

@@ -127,6 +127,30 @@ def test_static_step_refuses_too_many_candidate_pairs():
     _refused_unchanged(torch, sc, b"candidate pairs")
 
 
+def test_static_step_refuses_polygon_bodies():
+    # the allocation-free step takes no polygon vertices: a polygon body is
+    # refused with R2D_ERR_INVALID_ARGUMENT, the state untouched
+    torch = pytest.importorskip("torch")
+    from resolve2d_gb300.engine import device_kind
+
+    sc = scenes.polygon_scene(2, n=12)
+    w = World.from_scene(sc)
+    start = w.read_state()
+    dev = torch.device("cuda:0")
+    props, _ = derive_props_state(sc.kind, sc.opt)
+    bufs = (torch.from_numpy(np.ascontiguousarray(start, np.float32)).to(dev),
+            torch.from_numpy(np.ascontiguousarray(props, np.float32)).to(dev),
+            torch.from_numpy(device_kind(sc.kind)).to(dev),
+            torch.from_numpy(np.ascontiguousarray(sc.ids, np.uint32).view(np.int32)).to(dev))
+    g = np.ascontiguousarray(sc.gravity[sc.gravity != 0], np.float32)
+    lib = N.load()
+    rc = _static_step(lib, torch, bufs, start.shape[1], g, sc.dt, sc.sub_steps, sc.iters)
+    assert rc == -1
+    assert b"polygon" in lib.r2d_last_error_string()
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(bufs[0].cpu().numpy(), start)
+
+
 def test_static_step_rejects_worlds_beyond_its_maximum():
     torch = pytest.importorskip("torch")
     sc = scenes.batched_worlds("w5000", seed=6, nworlds=1, steps=1, lo=5000, hi=5000)

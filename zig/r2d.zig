@@ -28,6 +28,8 @@ pub extern "r2d_gb300" fn r2d_solver_create(cfg: *const Config, out: *?*Solver) 
 pub extern "r2d_gb300" fn r2d_solver_destroy(s: *Solver) Status;
 pub extern "r2d_gb300" fn r2d_solver_set_bodies(s: *Solver, n: u32, ids: [*]const u32, kind: [*]const u8,
     props: [*]const f32, state: [*]const f32, init_aabb: c_int) Status;
+pub extern "r2d_gb300" fn r2d_solver_set_polygons(s: *Solver, n: u32, body: [*]const u32, nverts: [*]const u8,
+    verts: [*]const f32) Status;
 pub extern "r2d_gb300" fn r2d_solver_write_state(s: *Solver, state: [*]const f32) Status;
 pub extern "r2d_gb300" fn r2d_solver_read_state(s: *Solver, state: [*]f32) Status;
 pub extern "r2d_gb300" fn r2d_solver_set_gravity(s: *Solver, n: u32, g: [*]const f32) Status;
@@ -57,6 +59,8 @@ pub extern "r2d_gb300" fn r2d_batch_create(cfg: *const Config, out: *?*Batch) St
 pub extern "r2d_gb300" fn r2d_batch_destroy(b: *Batch) Status;
 pub extern "r2d_gb300" fn r2d_batch_set_worlds(b: *Batch, nworlds: u32, body_off: [*]const u32, ids: [*]const u32,
     kind: [*]const u8, props: [*]const f32, state: [*]const f32, gravity: [*]const f32, init_aabb: c_int) Status;
+pub extern "r2d_gb300" fn r2d_batch_set_polygons(b: *Batch, n: u32, body: [*]const u32, nverts: [*]const u8,
+    verts: [*]const f32) Status;
 pub extern "r2d_gb300" fn r2d_batch_write_state(b: *Batch, state: [*]const f32) Status;
 pub extern "r2d_gb300" fn r2d_batch_read_state(b: *Batch, state: [*]f32) Status;
 pub extern "r2d_gb300" fn r2d_batch_process(b: *Batch, dt: f32, sub_steps: u32, iters: u32) Status;
