@@ -1421,7 +1421,86 @@ struct Engine {
                     acc[15] / steps, acc[16] / steps, acc[4] / steps, acc[5] / steps, acc[6] / steps,
                     acc[19] / steps, acc[18] / steps, acc[7] / steps, acc[8] / steps, acc[9] / steps);
         }
+        dump_timeline(t);
         cudaMemset(d_timers, 0, 8 * t.size());
+    }
+
+    // The last step's CTA timeline: when each size class started and ended,
+    // how busy the SMs were over the step, and how long its tail was.
+    void dump_timeline(const std::vector<unsigned long long>& t) {
+        struct Cta {
+            unsigned long long s, e;
+            uint32_t sm;
+        };
+        std::vector<Cta> ctas;
+        unsigned long long t0 = ~0ull, t1 = 0;
+        for (uint32_t w = 0; w < nworlds; ++w) {
+            const unsigned long long* r = &t[(size_t)w * PHASE_SLOTS];
+            if (r[PT_END] <= r[PT_START] || !r[PT_START]) continue;
+            ctas.push_back({r[PT_START], r[PT_END], (uint32_t)r[PT_SM]});
+            t0 = std::min(t0, r[PT_START]);
+            t1 = std::max(t1, r[PT_END]);
+        }
+        if (ctas.empty()) return;
+        const double span = (double)(t1 - t0) * 1e-3;  // us
+        for (auto& c : classes) {
+            unsigned long long fs = ~0ull, ls = 0, le = 0;
+            double dur = 0;
+            size_t k = 0;
+            for (uint32_t w : c.worlds) {
+                const unsigned long long* r = &t[(size_t)w * PHASE_SLOTS];
+                if (r[PT_END] <= r[PT_START] || !r[PT_START]) continue;
+                fs = std::min(fs, r[PT_START]);
+                ls = std::max(ls, r[PT_START]);
+                le = std::max(le, r[PT_END]);
+                dur += (double)(r[PT_END] - r[PT_START]);
+                ++k;
+            }
+            if (!k) continue;
+            fprintf(stderr, "r2d timeline nb=%u thr=%d worlds=%zu | first start %.1f us, last start %.1f, last end %.1f, "
+                            "mean CTA %.1f us\n",
+                    c.caps.nb, c.threads, k, (fs - t0) * 1e-3, (ls - t0) * 1e-3, (le - t0) * 1e-3, dur / k * 1e-3);
+        }
+        int nsm = 0;
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        // per SM: the union of its CTAs' intervals, and its last end
+        std::vector<std::vector<std::pair<unsigned long long, unsigned long long>>> per((size_t)std::max(nsm, 1));
+        for (const Cta& c : ctas)
+            if (c.sm < per.size()) per[c.sm].push_back({c.s, c.e});
+        double busy = 0;
+        std::vector<double> last;
+        for (auto& v : per) {
+            if (v.empty()) {
+                last.push_back(0);
+                continue;
+            }
+            std::sort(v.begin(), v.end());
+            unsigned long long cs = v[0].first, ce = v[0].second, le = 0;
+            for (auto& iv : v) {
+                le = std::max(le, iv.second);
+                if (iv.first > ce) {
+                    busy += (double)(ce - cs);
+                    cs = iv.first;
+                    ce = iv.second;
+                } else {
+                    ce = std::max(ce, iv.second);
+                }
+            }
+            busy += (double)(ce - cs);
+            last.push_back((le - t0) * 1e-3);
+        }
+        std::sort(last.begin(), last.end());
+        std::vector<double> ends;
+        for (const Cta& c : ctas) ends.push_back((c.e - t0) * 1e-3);
+        std::sort(ends.begin(), ends.end());
+        const auto q = [](const std::vector<double>& v, double f) { return v[(size_t)(f * (v.size() - 1))]; };
+        fprintf(stderr, "r2d timeline step: %.1f us from first CTA start to last end, %zu CTAs on %d SMs | SM busy %.1f %% "
+                        "of SM-time | SM last end min %.1f median %.1f max %.1f us | 90 %% of CTAs ended by %.1f us, "
+                        "99 %% by %.1f\n",
+                span, ctas.size(), nsm, 100.0 * busy * 1e-3 / (span * std::max(nsm, 1)), last.front(),
+                q(last, 0.5), last.back(), q(ends, 0.9), q(ends, 0.99));
     }
 #endif
 

@@ -246,7 +246,11 @@ struct StepParams {
 // Phase timer slots (cycles, R2D_PHASE_TIMERS builds only): load,
 // broadphase, narrowphase, contact colouring, joint colouring, solve,
 // write-back, then counts: pairs, manifolds, colours, colouring rounds.
-constexpr int PHASE_SLOTS = 20;  // 12..: sub-phases (cells, bucket sort, colour sort, colour walk)
+// 12..19: sub-phases (cells, bucket sort, colour sort, colour walk) and
+// counts.  20..22: the CTA's timeline in the last step (not summed):
+// %globaltimer at its start and end, in ns, and the SM it ran on.
+constexpr int PHASE_SLOTS = 23;
+constexpr int PT_START = 20, PT_END = 21, PT_SM = 22;
 
 // Which per-world buffer overflowed (reported with DS_CAPACITY).
 enum CapBits : uint32_t {

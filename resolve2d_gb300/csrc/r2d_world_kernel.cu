@@ -361,6 +361,14 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
     }
     int err = 0;
 #ifdef R2D_PHASE_TIMERS
+    if (tid == 0 && P.timers) {
+        unsigned long long gt;
+        uint32_t sm;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(gt));
+        asm volatile("mov.u32 %0, %%smid;" : "=r"(sm));
+        P.timers[(size_t)w * PHASE_SLOTS + PT_START] = gt;
+        P.timers[(size_t)w * PHASE_SLOTS + PT_SM] = sm;
+    }
     long long t_mark = clock64();
     const uint32_t jp_rounds = 0;
     long long t_sub = t_mark;
@@ -1284,6 +1292,9 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
             t[9] += ncol;
             t[10] += jp_rounds;
             t[11] += 1;
+            unsigned long long gt;
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(gt));
+            t[PT_END] = gt;
         }
 #endif
         if (tid == 0) P.world_status[w] = DS_OK;
