@@ -33,7 +33,7 @@
 
 namespace r2d {
 cudaError_t launch_world_step(const StepParams& P, const Caps& C, int threads, const LayoutOpts& opts,
-                              cudaStream_t stream);
+                              cudaStream_t stream, int priority = 0);
 cudaError_t allow_world_step_smem(int bytes);
 cudaError_t launch_count_call(uint32_t* counter, cudaStream_t stream);
 cudaError_t launch_migrate_warm(uint32_t nworlds, const WarmTables& old_t, const uint32_t* old_cur,
@@ -123,7 +123,17 @@ struct KClass {
     std::vector<uint32_t> worlds;
     uint32_t* d_list = nullptr;
     uint32_t smem = 0;
+    int priority = 0;  // launch priority: larger worlds (longer CTAs) higher
 };
+
+// Size-class launch priorities on (R2D_CLASS_PRIORITY=0 leaves them all at
+// the default) and auxiliary streams, one per class.
+#ifndef R2D_CLASS_PRIORITY
+#define R2D_CLASS_PRIORITY 1
+#endif
+#ifndef R2D_NAUX
+#define R2D_NAUX 32
+#endif
 
 struct Engine {
     r2d_config cfg{};
@@ -131,7 +141,10 @@ struct Engine {
     bool own_stream = false;
     // Size classes run concurrently on auxiliary streams forked from and
     // joined back into `stream`, so one class's tail overlaps the others.
-    static constexpr int NAUX = 16;
+    // Classes sharing a stream would run one after the other, so there is a
+    // stream for each of the 11 body bounds x 3 capacity boosts a step
+    // normally has.
+    static constexpr int NAUX = R2D_NAUX;
     cudaStream_t aux[NAUX] = {};
     cudaEvent_t ev_fork = nullptr, ev_join[NAUX] = {};
     bool verbose = false;
@@ -1068,6 +1081,26 @@ struct Engine {
         }
         std::stable_sort(classes.begin(), classes.end(),
                          [](const KClass& a, const KClass& b) { return a.caps.nb > b.caps.nb; });
+        // The block scheduler hands out every CTA of one launch before the
+        // next launch's, in an order of its own, unless priorities say
+        // otherwise.  Larger worlds run longer, so their CTAs go first
+        // (longest tasks first) and the short small-world CTAs fill the end
+        // of the step: body bounds ranked largest first, spread over the
+        // device's priority levels.
+        {
+            int least = 0, greatest = 0;
+            if (R2D_CLASS_PRIORITY && cudaDeviceGetStreamPriorityRange(&least, &greatest) == cudaSuccess &&
+                least > greatest) {
+                std::vector<uint32_t> nbs;
+                for (const auto& c : classes)
+                    if (nbs.empty() || nbs.back() != c.caps.nb) nbs.push_back(c.caps.nb);
+                const int levels = least - greatest + 1, D = (int)nbs.size();
+                for (auto& c : classes) {
+                    const int r = (int)(std::find(nbs.begin(), nbs.end(), c.caps.nb) - nbs.begin());
+                    c.priority = greatest + (r * levels) / std::max(D, 1);
+                }
+            }
+        }
         large_list.clear();
         for (uint32_t w = 0; w < nworlds; ++w) {
             if (!world_large[w]) continue;
@@ -1203,7 +1236,7 @@ struct Engine {
                     return st;
                 }
                 CUDA_TRY(ec);
-                const cudaError_t ei = cudaGraphInstantiate(&gexec, graph, 0);
+                const cudaError_t ei = cudaGraphInstantiate(&gexec, graph, cudaGraphInstantiateFlagUseNodePriority);
                 cudaGraphDestroy(graph);
                 CUDA_TRY(ei);
                 g_dt = dt;
@@ -1240,7 +1273,8 @@ struct Engine {
         if (classes.size() == 1) {
             P.world_list = classes[0].d_list;
             P.nlist = (uint32_t)classes[0].worlds.size();
-            cudaError_t e = launch_world_step(P, classes[0].caps, classes[0].threads, classes[0].opts, stream);
+            cudaError_t e =
+                launch_world_step(P, classes[0].caps, classes[0].threads, classes[0].opts, stream, classes[0].priority);
             if (e != cudaSuccess) return fail(R2D_ERR_CUDA, std::string("world step launch: ") + cudaGetErrorString(e));
         } else if (nused > 1) {
             for (int a = 0; a < nused; ++a) CUDA_TRY(cudaStreamWaitEvent(aux[a], ev_fork, 0));
@@ -1249,7 +1283,7 @@ struct Engine {
                 const KClass& c = classes[i];
                 P.world_list = c.d_list;
                 P.nlist = (uint32_t)c.worlds.size();
-                cudaError_t e = launch_world_step(P, c.caps, c.threads, c.opts, aux[i % NAUX]);
+                cudaError_t e = launch_world_step(P, c.caps, c.threads, c.opts, aux[i % NAUX], c.priority);
                 if (e != cudaSuccess) return fail(R2D_ERR_CUDA, std::string("world step launch: ") + cudaGetErrorString(e));
             }
             for (int a = 0; a < nused; ++a) {

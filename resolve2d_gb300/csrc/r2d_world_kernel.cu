@@ -1322,11 +1322,21 @@ __global__ void count_call_kernel(uint32_t* counter) { *counter += 1u; }
 // host-side launch helpers
 // ---------------------------------------------------------------------------
 template <int NT, bool LEAN>
-cudaError_t launch_world_step_nt(const StepParams& P, const Caps& C, const LayoutOpts& opts, cudaStream_t stream) {
+cudaError_t launch_world_step_nt(const StepParams& P, const Caps& C, const LayoutOpts& opts, cudaStream_t stream,
+                                 int priority) {
     const Layout L = make_layout(C, opts);
     if (P.nlist == 0) return cudaSuccess;
-    world_step_kernel<NT, LEAN><<<P.nlist, NT, L.total, stream>>>(P, C, L);
-    return cudaGetLastError();
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(P.nlist);
+    cfg.blockDim = dim3(NT);
+    cfg.dynamicSmemBytes = L.total;
+    cfg.stream = stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributePriority;
+    at[0].val.priority = priority;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, world_step_kernel<NT, LEAN>, P, C, L);
 }
 
 template <int NT, bool LEAN>
@@ -1389,11 +1399,14 @@ cudaError_t launch_count_call(uint32_t* counter, cudaStream_t stream) {
     return cudaGetLastError();
 }
 
+// `priority` is the launch's stream priority (cudaDeviceGetStreamPriorityRange):
+// when several size classes run at once, the block scheduler hands out the
+// CTAs of a higher-priority launch first.
 cudaError_t launch_world_step(const StepParams& P, const Caps& C, int threads, const LayoutOpts& opts,
-                              cudaStream_t stream) {
-#define R2D_LAUNCH(NT)                                                        \
-    return opts.lean ? launch_world_step_nt<NT, true>(P, C, opts, stream) \
-                     : launch_world_step_nt<NT, false>(P, C, opts, stream)
+                              cudaStream_t stream, int priority) {
+#define R2D_LAUNCH(NT)                                                                  \
+    return opts.lean ? launch_world_step_nt<NT, true>(P, C, opts, stream, priority) \
+                     : launch_world_step_nt<NT, false>(P, C, opts, stream, priority)
     switch (threads) {
     case 32: R2D_LAUNCH(32);
     case 64: R2D_LAUNCH(64);
