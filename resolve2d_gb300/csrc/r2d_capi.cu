@@ -276,6 +276,10 @@ struct Engine {
     // body's diameter (R2D_FINE_CELL_SCALE, default 1).  Pairs do not depend
     // on it; candidates and entries per body do.
     float fine_scale = 1.0f;
+    // Tuning: launch priorities by body bound (R2D_CLASS_PRIORITIES, e.g.
+    // "520:-5,448:-4"; bounds not named get 0), in place of the ranking.
+    std::vector<std::pair<uint32_t, int>> priority_map;
+    bool priority_map_set = false;
 
     ~Engine() {
         large.clear();
@@ -335,6 +339,20 @@ struct Engine {
         colour_round_limit = rl ? (uint32_t)strtoul(rl, nullptr, 10) : 0u;
         const char* fs = getenv("R2D_FINE_CELL_SCALE");
         if (fs && strtof(fs, nullptr) > 0.f) fine_scale = strtof(fs, nullptr);
+        if (const char* pm = getenv("R2D_CLASS_PRIORITIES")) {
+            priority_map_set = true;
+            const char* q = pm;
+            while (*q) {
+                char* e1 = nullptr;
+                const unsigned long nb = strtoul(q, &e1, 10);
+                if (e1 == q || *e1 != ':') break;
+                char* e2 = nullptr;
+                const long pr = strtol(e1 + 1, &e2, 10);
+                if (e2 == e1 + 1) break;
+                priority_map.push_back({(uint32_t)nb, (int)pr});
+                q = *e2 == ',' ? e2 + 1 : e2;
+            }
+        }
         CUDA_TRY(dalloc(d_call, 1));
         CUDA_TRY(dalloc(d_ext, 1));
         CUDA_TRY(cudaMemsetAsync(d_ext, 0, sizeof(ExtIO), stream));
@@ -1089,8 +1107,14 @@ struct Engine {
         // device's priority levels.
         {
             int least = 0, greatest = 0;
-            if (R2D_CLASS_PRIORITY && cudaDeviceGetStreamPriorityRange(&least, &greatest) == cudaSuccess &&
-                least > greatest) {
+            if (priority_map_set) {
+                for (auto& c : classes) {
+                    c.priority = 0;
+                    for (const auto& kv : priority_map)
+                        if (kv.first == c.caps.nb) c.priority = kv.second;
+                }
+            } else if (R2D_CLASS_PRIORITY && cudaDeviceGetStreamPriorityRange(&least, &greatest) == cudaSuccess &&
+                       least > greatest) {
                 std::vector<uint32_t> nbs;
                 for (const auto& c : classes)
                     if (nbs.empty() || nbs.back() != c.caps.nb) nbs.push_back(c.caps.nb);

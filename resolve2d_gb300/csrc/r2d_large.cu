@@ -419,124 +419,6 @@ __global__ void lk_narrow(Phase1 A, uint32_t npairs) {
     narrow_pair(A, pi);
 }
 
-// Lanes per pair in the narrowphase: 1 (lk_narrow), or 8 (lk_narrow_lanes).
-#ifndef R2D_NARROW_LANES
-#define R2D_NARROW_LANES 1
-#endif
-
-// A rectangle's position and world vertices, as geo_make computes them; the
-// edge normals are left zero.
-__device__ void rect_geo_vertices(const Phase1& A, uint32_t o, Geo& g) {
-    const SWT<uint32_t>& s = A.s;
-    const f2 pos = f2{s.px[o], s.py[o]};
-    const float w = A.pr(P_DIM0, o) / 2.0f, h = A.pr(P_DIM1, o) / 2.0f, c = s.cs[o], sn = s.sn[o];
-    g.pos = pos;
-    g.nv_ = 4u;
-    g.rect = true;
-    g.radius = A.pr(P_DIM0, o);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        g.wv[i] = add2(rot(rect_local(i, w, h), c, sn), pos);
-        g.en[i] = f2{0.f, 0.f};
-    }
-}
-
-// The narrowphase with eight lanes per pair.  For a rectangle-rectangle pair
-// lane k evaluates SAT axis k (edge k & 3 of o1 for k < 4, of o2 otherwise:
-// the order overlapSAT visits them, collision.zig:228-289): the possibly
-// flipped edge normal and the two projections' overlap, with the arithmetic
-// of overlap_sat.  Every lane then replays overlapSAT's sequential choice
-// over the eight axes from shuffled values, so the result has the same bits;
-// the group's first lane clips the contact points and writes the manifold.
-// Other pairs (and engines with polygons) run whole on the first lane.
-__global__ void lk_narrow_lanes(Phase1 A, uint32_t npairs) {
-    const uint32_t t = blockIdx.x * LT + threadIdx.x;
-    const uint32_t pi = t >> 3, k = t & 7u;
-    if (pi >= npairs) return;  // the group's eight lanes leave together (LT is a multiple of 8)
-    const unsigned gm = 0xFFu << (threadIdx.x & 24u);
-    const SWT<uint32_t>& s = A.s;
-    const unsigned long long key = A.pairs[pi];
-    const uint32_t lo = (uint32_t)(key >> 32), hi = (uint32_t)key;
-    const bool rr = (s.kind[lo] & K_RECT) && (s.kind[hi] & K_RECT);
-    if (A.poly_v || !rr) {
-        if (k == 0) narrow_pair(A, pi);
-        return;
-    }
-    const uint32_t o1 = __ldg(A.ids + A.base + lo) < __ldg(A.ids + A.base + hi) ? lo : hi;
-    const uint32_t o2 = o1 == lo ? hi : lo;
-    Geo g0, g1;
-    rect_geo_vertices(A, o1, g0);
-    rect_geo_vertices(A, o2, g1);
-    // this lane's axis: edge e of body b (geo_make's edge normal)
-    const uint32_t b = k >> 2, e = k & 3u;
-    const Geo R = b ? g1 : g0;
-    const Geo I = b ? g0 : g1;
-    const f2 en = ccw90(normalize2(sub2(selv(R.wv, (e + 1u) & 3u), selv(R.wv, e))));
-    f2 normal = en;
-    bool flipped = false;
-    if (dot2(normal, sub2(I.pos, R.pos)) < 0.0f) {  // normalShouldFlipSAT (:221-226)
-        normal = neg_by_mul(normal);
-        flipped = true;
-    }
-    float p1lo, p1hi, p2lo, p2hi;
-    project(R, normal, &p1lo, &p1hi);
-    project(I, normal, &p2lo, &p2hi);
-    const float dk = zmin(p1hi - p2lo, p2hi - p1lo);
-    // overlapSAT's choice over the axes in order, on every lane
-    const float EPS = SAT_OVERLAP_THRESHOLD;
-    SatState ret;
-    ret.normal = {0.f, 0.f};
-    ret.penetration = __int_as_float(0x7f800000);
-    ret.refid = 0;
-    ret.ref_is_first = true;
-#pragma unroll
-    for (int it = 0; it < 8; ++it) {
-        const float d = __shfl_sync(gm, dk, it, 8);
-        const f2 nrm = f2{__shfl_sync(gm, normal.x, it, 8), __shfl_sync(gm, normal.y, it, 8)};
-        const bool fl = __shfl_sync(gm, (int)flipped, it, 8) != 0;
-        if (d <= -COLLISION_MARGIN) return;  // no contact (every lane sees the same axis)
-        const bool r_is_o1 = it < 4;
-        const Geo& Ri = r_is_o1 ? g0 : g1;
-        const Geo& Ii = r_is_o1 ? g1 : g0;
-        if (!fl && approx_eql2(nrm, ret.normal, EPS)) {
-            const float tref = dot2(Ri.pos, nrm);
-            const float tinc = dot2(Ii.pos, nrm);
-            if (tref < tinc - EPS) {
-                ret.penetration = d;
-                ret.normal = nrm;
-                ret.refid = (uint32_t)(it & 3);
-                ret.ref_is_first = r_is_o1;
-            }
-        }
-        if (!fl && approx_eql2(nrm, negate2(ret.normal), EPS)) {
-            const f2 diff = sub2(Ii.pos, Ri.pos);
-            if (dot2(diff, nrm) > dot2(diff, ret.normal) + EPS) {
-                ret.penetration = d;
-                ret.normal = nrm;
-                ret.refid = (uint32_t)(it & 3);
-                ret.ref_is_first = r_is_o1;
-            }
-        }
-        if (d + EPS < ret.penetration) {
-            ret.penetration = d;
-            ret.normal = nrm;
-            ret.refid = (uint32_t)(it & 3);
-            ret.ref_is_first = r_is_o1;
-        }
-    }
-    // every edge normal to the first lane, which clips and writes
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-        const f2 v = f2{__shfl_sync(gm, en.x, q, 8), __shfl_sync(gm, en.y, q, 8)};
-        if (q < 4) g0.en[q] = v;
-        else g1.en[q - 4] = v;
-    }
-    if (k != 0) return;
-    NewPoint pts[2];
-    const int npt = ret.ref_is_first ? identify_points(g0, g1, ret.refid, pts) : identify_points(g1, g0, ret.refid, pts);
-    narrow_write(A, o1, o2, ret, pts, npt);
-}
-
 // ---------------------------------------------------------------------------
 // colouring (r2d_colour.h) by Jones-Plassmann rounds
 // ---------------------------------------------------------------------------
@@ -1872,10 +1754,7 @@ int LargeWorld::step(const LargeInputs& in, float dt, uint32_t sub_steps, uint32
     A.nm = npairs;
     A.npt = 2 * npairs;
     LTRY(cudaMemsetAsync(I.cnt, 0, sizeof(uint32_t) * LC_N, st));
-    if (R2D_NARROW_LANES == 8)
-        LAUNCH(lk_narrow_lanes, blocks(8 * (uint64_t)npairs), A, npairs);
-    else
-        LAUNCH(lk_narrow, blocks(npairs), A, npairs);
+    LAUNCH(lk_narrow, blocks(npairs), A, npairs);
     LTRY(cudaMemcpyAsync(I.h_cnt, I.cnt, sizeof(uint32_t) * LC_N, cudaMemcpyDeviceToHost, st));
     LTRY(cudaStreamSynchronize(st));
     const uint32_t M = I.h_cnt[LC_MANIFOLDS];
