@@ -123,7 +123,7 @@ struct KClass {
     std::vector<uint32_t> worlds;
     uint32_t* d_list = nullptr;
     uint32_t smem = 0;
-    int priority = 0;  // launch priority: larger worlds (longer CTAs) higher
+    int priority = 0;  // launch priority (plan(): large and small bounds paired, from the top)
 };
 
 // Size-class launch priorities on (R2D_CLASS_PRIORITY=0 leaves them all at
@@ -277,7 +277,7 @@ struct Engine {
     // on it; candidates and entries per body do.
     float fine_scale = 1.0f;
     // Tuning: launch priorities by body bound (R2D_CLASS_PRIORITIES, e.g.
-    // "520:-5,448:-4"; bounds not named get 0), in place of the ranking.
+    // "520:-5,448:-4"; bounds not named get 0), in place of the pairing.
     std::vector<std::pair<uint32_t, int>> priority_map;
     bool priority_map_set = false;
 
@@ -927,7 +927,7 @@ struct Engine {
     // Picks each size class's threads per CTA by timing whole steps (all
     // classes running together, as in use) from the current state, which is
     // restored after every trial and at the end: one coordinate-descent pass
-    // over the classes, candidates 32..256 threads, a candidate replacing the
+    // over the classes, candidates 32..512 threads, a candidate replacing the
     // standing choice only when 1.5 % faster.  Results do not depend on the
     // choice (the colouring, scans and solve order do not), only speed.
     int autotune(float dt, uint32_t sub_steps, uint32_t iters, uint32_t trial_steps) {
@@ -976,7 +976,7 @@ struct Engine {
             status = fail(R2D_ERR_CUDA, "autotune events");
         } else {
             static constexpr uint32_t bnd[] = {32, 64, 96, 128, 160, 192, 256, 320, 384, 448, 520};
-            static constexpr int cand[] = {32, 64, 128, 256};
+            static constexpr int cand[] = {32, 64, 128, 256, 512};
             std::vector<int> used(11, 0);
             for (const auto& c : classes)
                 for (int k = 0; k < 11; ++k)
@@ -989,7 +989,9 @@ struct Engine {
                 float best_t = time_steps();
                 int best = start;
                 for (int nt : cand) {
-                    if (nt == start || (bnd[k] > 192 && nt < 64) || (bnd[k] <= 64 && nt > 128)) continue;
+                    if (nt == start || (bnd[k] > 192 && nt < 64) || (bnd[k] <= 64 && nt > 128) ||
+                        (bnd[k] <= 256 && nt > 256))
+                        continue;
                     thread_override[k] = nt;
                     plan_dirty = true;
                     const float t = time_steps();
@@ -1101,10 +1103,11 @@ struct Engine {
                          [](const KClass& a, const KClass& b) { return a.caps.nb > b.caps.nb; });
         // The block scheduler hands out every CTA of one launch before the
         // next launch's, in an order of its own, unless priorities say
-        // otherwise.  Larger worlds run longer, so their CTAs go first
-        // (longest tasks first) and the short small-world CTAs fill the end
-        // of the step: body bounds ranked largest first, spread over the
-        // device's priority levels.
+        // otherwise.  Each priority level pairs a large body bound (the
+        // longest CTAs, 70-150 KB of shared memory) with a small one (short
+        // CTAs of 10-30 KB that fill the shared memory the large CTAs leave
+        // on an SM): bounds ranked largest first, k-th and k-th from last on
+        // level k, from the device's highest priority down.
         {
             int least = 0, greatest = 0;
             if (priority_map_set) {
@@ -1118,10 +1121,10 @@ struct Engine {
                 std::vector<uint32_t> nbs;
                 for (const auto& c : classes)
                     if (nbs.empty() || nbs.back() != c.caps.nb) nbs.push_back(c.caps.nb);
-                const int levels = least - greatest + 1, D = (int)nbs.size();
+                const int D = (int)nbs.size();
                 for (auto& c : classes) {
                     const int r = (int)(std::find(nbs.begin(), nbs.end(), c.caps.nb) - nbs.begin());
-                    c.priority = greatest + (r * levels) / std::max(D, 1);
+                    c.priority = std::min(greatest + std::min(r, D - 1 - r), least);
                 }
             }
         }
@@ -1473,10 +1476,12 @@ struct Engine {
             const double steps = acc[11] > 0 ? acc[11] : 1;
             fprintf(stderr, "r2d timers nb=%u thr=%d worlds=%zu smem=%u | load %.0f bp %.0f [cells %.0f sort %.0f "
                             "cand %.0f compact %.0f] np %.0f col %.0f [sort %.0f walk %.0f] jcol %.0f solve %.0f "
-                            "wb %.0f | entries %.1f candidates %.1f pairs %.1f man %.1f colours %.1f\n",
+                            "[forces %.0f prestep %.0f] wb %.0f | entries %.1f candidates %.1f pairs %.1f man %.1f "
+                            "colours %.1f\n",
                     c.caps.nb, c.threads, c.worlds.size(), c.smem, acc[0] / steps, acc[1] / steps, acc[12] / steps,
                     acc[13] / steps, acc[14] / steps, acc[17] / steps, acc[2] / steps, acc[3] / steps,
-                    acc[15] / steps, acc[16] / steps, acc[4] / steps, acc[5] / steps, acc[6] / steps,
+                    acc[15] / steps, acc[16] / steps, acc[4] / steps, acc[5] / steps, acc[PT_FORCES] / steps,
+                    acc[PT_PRESTEP] / steps, acc[6] / steps,
                     acc[19] / steps, acc[18] / steps, acc[7] / steps, acc[8] / steps, acc[9] / steps);
         }
         dump_timeline(t);

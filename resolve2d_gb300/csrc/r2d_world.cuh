@@ -164,12 +164,10 @@ __host__ __device__ inline Layout make_layout(const Caps& c, const LayoutOpts& f
     // per-body colour masks reuse them
     L.pairs = take(4 * c.np);
     L.cmask = (20 * c.nb <= 4 * c.np) ? L.pairs : take(20 * c.nb);  // 4 colour words + lane bits
-    // sort keys of the colouring (8 B each, a power-of-two count): the
-    // point arrays mn .. apt are not live until after the colouring
+    // sort keys of the colouring (8 B a constraint): the point arrays mn ..
+    // apt are not live until after the colouring
     const uint32_t ncon = c.nm > c.nj ? c.nm : c.nj;
-    uint32_t n2 = 1;
-    while (n2 < ncon) n2 <<= 1;
-    L.skey = (8 * n2 <= (L.has_comp ? 6u : 4u) * np4) ? L.mn : take(8 * n2);
+    L.skey = (8 * ncon <= (L.has_comp ? 6u : 4u) * np4) ? L.mn : take(8 * ncon);
     L.total = o;
     return L;
 }
@@ -248,9 +246,10 @@ struct StepParams {
 // write-back, then counts: pairs, manifolds, colours, colouring rounds.
 // 12..19: sub-phases (cells, bucket sort, colour sort, colour walk) and
 // counts.  20..22: the CTA's timeline in the last step (not summed):
-// %globaltimer at its start and end, in ns, and the SM it ran on.
-constexpr int PHASE_SLOTS = 23;
-constexpr int PT_START = 20, PT_END = 21, PT_SM = 22;
+// %globaltimer at its start and end, in ns, and the SM it ran on.  23, 24:
+// the solve phase's forces and prestep passes (cycles).
+constexpr int PHASE_SLOTS = 25;
+constexpr int PT_START = 20, PT_END = 21, PT_SM = 22, PT_FORCES = 23, PT_PRESTEP = 24;
 
 // Which per-world buffer overflowed (reported with DS_CAPACITY).
 enum CapBits : uint32_t {

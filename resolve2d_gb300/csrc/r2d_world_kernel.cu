@@ -215,17 +215,19 @@ __device__ void priority_order(uint32_t count, Mix mix, Tie tie, unsigned long l
 // computed with warp shuffles instead of block-wide rounds.  ends(i, &a, &b)
 // names constraint i's conflict nodes (values >= 0x10000 mean "no node").
 // Returns true on every thread when some constraint would need more than
-// MAX_COLOURS colours.  bucket: 256 words of shared scratch.
+// MAX_COLOURS colours; *ncolours (shared) gets the number of colours used.
+// bucket: 256 words of shared scratch.
 template <int NT, class Ends, class Mix, class Tie, class Hook>
 __device__ bool colour_greedy_sorted(uint32_t count, uint32_t n, Ends ends, Mix mix, Tie tie, uint8_t* colour,
                                      unsigned long long* skey, uint32_t* cmask, uint32_t* bucket, uint32_t* wsum,
-                                     Hook SUBPHASE_HOOK) {
+                                     uint32_t* ncolours, Hook SUBPHASE_HOOK) {
     const int tid = threadIdx.x, lane = tid & 31;
     for (uint32_t i = tid; i < 5 * n; i += NT) cmask[i] = 0u;
     priority_order<NT>(count, mix, tie, skey, bucket, wsum);
     SUBPHASE_HOOK();
     int overflow = 0;
     if (tid < 32) {
+        uint32_t used = 0;  // colours this lane handed out: the highest + 1
         uint32_t* lanebits = cmask + 4 * n;  // per node: lanes of this chunk that name it
         auto fetch = [&](uint32_t base, uint32_t* ci, uint32_t* a, uint32_t* b, bool* valid) {
             const uint32_t i = base + lane;
@@ -278,6 +280,7 @@ __device__ bool colour_greedy_sorted(uint32_t count, uint32_t n, Ends ends, Mix 
                         colour[ci] = (uint8_t)c;
                         if (na) cmask[(c >> 5) * n + a] = wa | (1u << (c & 31u));
                         if (nb2) cmask[(c >> 5) * n + b] = wb | (1u << (c & 31u));
+                        used = max(used, c + 1u);
                     }
                     done = true;
                 }
@@ -288,6 +291,8 @@ __device__ bool colour_greedy_sorted(uint32_t count, uint32_t n, Ends ends, Mix 
             b = nxb;
             valid = nvalid;
         }
+        used = __reduce_max_sync(0xffffffffu, used);
+        if (lane == 0) *ncolours = used;
     }
     return __syncthreads_or(overflow) != 0;
 }
@@ -327,6 +332,7 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
     __shared__ unsigned long long s_wsum64[32];
     __shared__ uint32_t s_big[MAX_BIG_BODIES];  // bodies whose cell entries the whole block emits
     __shared__ uint32_t s_nbig;
+    __shared__ uint32_t s_ncol;  // colours of the last colouring
 
     const int tid = threadIdx.x;
     if (blockIdx.x >= P.nlist) return;
@@ -922,7 +928,7 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
             return (min(x, y) << 16) | max(x, y);
         };
         if (colour_greedy_sorted<NT>(M, n, contact_ends, contact_mix, contact_tie, s.mcol, skey, cmask, s_ccnt,
-                                     s_wsum, [&]() { SUBPHASE(15); })) {
+                                     s_wsum, &s_ncol, [&]() { SUBPHASE(15); })) {
             if (tid == 0) {
                 s_err = DS_CAPACITY;
                 s_capbits |= CAP_COLOURS;
@@ -932,13 +938,12 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
         }
         SUBPHASE(16);
         // colour-major order
-        for (uint32_t c = tid; c < 256; c += NT) s_ccnt[c] = 0u;
+        ncol = s_ncol;
+        for (uint32_t c = tid; c < ncol; c += NT) s_ccnt[c] = 0u;
         __syncthreads();
         for (uint32_t m = tid; m < M; m += NT) atomicAdd(&s_ccnt[s.mcol[m]], 1u);
         __syncthreads();
-        for (uint32_t c = 0; c < (uint32_t)MAX_COLOURS; ++c)
-            if (s_ccnt[c]) ncol = c + 1;
-        block_scan_excl<NT>(s_ccnt, 256, s_wsum);
+        block_scan_excl<NT>(s_ccnt, ncol, s_wsum);
         for (uint32_t c = tid; c <= ncol; c += NT) coff[c] = (uint16_t)(c < ncol ? s_ccnt[c] : M);
         __syncthreads();
         for (uint32_t m = tid; m < M; m += NT) corder[atomicAdd(&s_ccnt[s.mcol[m]], 1u)] = (uint16_t)m;
@@ -958,7 +963,7 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
             auto joint_mix = [&](uint32_t j) { return r2d_colour_mix(j, R2D_COLOUR_JOINT_SALT); };
             auto joint_tie = [&](uint32_t j) { return j; };
             if (colour_greedy_sorted<NT>(NJ, n, joint_ends, joint_mix, joint_tie, jcol, skey, cmask, s_ccnt, s_wsum,
-                                         [&]() {})) {
+                                         &s_ncol, [&]() {})) {
                 if (tid == 0) {
                     s_err = DS_CAPACITY;
                     s_capbits |= CAP_COLOURS;
@@ -966,13 +971,12 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
                 __syncthreads();
                 goto fail;
             }
-            for (uint32_t c = tid; c < 256; c += NT) s_ccnt[c] = 0u;
+            njcol = s_ncol;
+            for (uint32_t c = tid; c < njcol; c += NT) s_ccnt[c] = 0u;
             __syncthreads();
             for (uint32_t j = tid; j < NJ; j += NT) atomicAdd(&s_ccnt[jcol[j]], 1u);
             __syncthreads();
-            for (uint32_t c = 0; c < (uint32_t)MAX_COLOURS; ++c)
-                if (s_ccnt[c]) njcol = c + 1;
-            block_scan_excl<NT>(s_ccnt, 256, s_wsum);
+            block_scan_excl<NT>(s_ccnt, njcol, s_wsum);
             for (uint32_t c = tid; c <= njcol; c += NT) joff[c] = (uint16_t)(c < njcol ? s_ccnt[c] : NJ);
             __syncthreads();
             for (uint32_t j = tid; j < NJ; j += NT) jorder[atomicAdd(&s_ccnt[jcol[j]], 1u)] = (uint16_t)j;
@@ -1075,6 +1079,7 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
                 s.tq[i] = tq;
             }
             __syncthreads();
+            SUBPHASE(PT_FORCES);
             // updateTGSDepth + preStep (collision.zig:73-133)
             for (uint32_t m = tid; m < M; m += NT) {
                 const uint32_t a = s.ma[m], b = s.mb[m];
@@ -1118,6 +1123,7 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
                 }
             }
             __syncthreads();
+            SUBPHASE(PT_PRESTEP);
             if (warm && sub == 0) {  // the warm-started impulses, colour by colour
                 for (uint32_t c = 0; c < ncol; ++c) {
                     for (uint32_t k = coff[c] + tid; k < coff[c + 1]; k += NT) warm_apply_contact<LEAN>(s, corder[k]);

@@ -7,7 +7,8 @@ clock64() at its phase boundaries), steps the 4,096 benchmark worlds
 (seed 3) `--settle` steps, then `--steps` more with the counters on, and the
 library prints one line per size class to stderr: mean cycles per
 world-step of load, broadphase (cells, bucket sort, candidates, pair list),
-narrowphase, colouring (sort, walk), joint colouring, solve, write-back, and
+narrowphase, colouring (sort, walk), joint colouring, solve (of which the
+forces and prestep passes), write-back, and
 mean counts of entries, candidates, pairs, manifolds and colours.  Cycles are
 wall-clock cycles of the SM the world ran on, so co-resident worlds inflate
 them; they rank phases, they do not time the step (bench.py does).
