@@ -922,11 +922,13 @@ struct Engine {
     // Threads per CTA for a class of `nb` bodies: a world's phases rarely
     // have more parallel items than this, and smaller CTAs let more worlds
     // share an SM.
-    static int default_threads(uint32_t nb) { return nb <= 64 ? 64 : (nb <= 256 ? 128 : 256); }
+    // Threads per CTA of a size class before autotuning: small worlds run
+    // fastest as many small CTAs an SM (registers, not work, limit them).
+    static int default_threads(uint32_t nb) { return nb <= 64 ? 32 : (nb <= 128 ? 64 : (nb <= 256 ? 128 : 256)); }
 
     // Picks each size class's threads per CTA by timing whole steps (all
     // classes running together, as in use) from the current state, which is
-    // restored after every trial and at the end: one coordinate-descent pass
+    // restored after every trial and at the end: two coordinate-descent passes
     // over the classes, candidates 32..512 threads, a candidate replacing the
     // standing choice only when 1.5 % faster.  Results do not depend on the
     // choice (the colouring, scans and solve order do not), only speed.
@@ -981,6 +983,9 @@ struct Engine {
             for (const auto& c : classes)
                 for (int k = 0; k < 11; ++k)
                     if (c.caps.nb == bnd[k]) used[k] = 1;
+            // two passes: a class's best tile depends on the others' (they
+            // share the SMs), so the second pass revisits every class
+            for (int pass = 0; pass < 2; ++pass)
             for (int k = 0; k < 11 && status == R2D_OK; ++k) {
                 if (!used[k]) continue;
                 const int start = thread_override[k] ? thread_override[k] : default_threads(bnd[k]);
