@@ -89,10 +89,14 @@ __device__ __forceinline__ void solve_contact(const SWT<IDX>& s, uint32_t m, boo
     const bool sa = s.kind[a] & K_STATIC, sb = s.kind[b] & K_STATIC;
     const float inv_m1 = s.inv_m[a], inv_m2 = s.inv_m[b];
     const float inv_i1 = s.inv_i[a], inv_i2 = s.inv_i[b];
-    const f2 vlinear_1 = scale2(f2{s.mx[a], s.my[a]}, inv_m1);
-    const float omega1 = s.L[a] * inv_i1;
-    const f2 vlinear_2 = scale2(f2{s.mx[b], s.my[b]}, inv_m2);
-    const float omega2 = s.L[b] * inv_i2;
+    // the momenta, read once: no other constraint of this colour moves a or
+    // b, so the sums below are the read-modify-writes the reference does
+    const float mx1 = s.mx[a], my1 = s.my[a], L1 = s.L[a];
+    const float mx2 = s.mx[b], my2 = s.my[b], L2 = s.L[b];
+    const f2 vlinear_1 = scale2(f2{mx1, my1}, inv_m1);
+    const float omega1 = L1 * inv_i1;
+    const f2 vlinear_2 = scale2(f2{mx2, my2}, inv_m2);
+    const float omega2 = L2 * inv_i2;
     const f2 n = {s.nx[m], s.ny[m]};
     const f2 t = cw90(n);
     const float fr = s.fric[m];
@@ -127,14 +131,14 @@ __device__ __forceinline__ void solve_contact(const SWT<IDX>& s, uint32_t m, boo
     }
     // A static body receives exactly +0 in the reference; its state is left alone.
     if (!sa) {
-        s.mx[a] += alp1.x;
-        s.my[a] += alp1.y;
-        s.L[a] += arp1;
+        s.mx[a] = mx1 + alp1.x;
+        s.my[a] = my1 + alp1.y;
+        s.L[a] = L1 + arp1;
     }
     if (!sb) {
-        s.mx[b] += alp2.x;
-        s.my[b] += alp2.y;
-        s.L[b] += arp2;
+        s.mx[b] = mx2 + alp2.x;
+        s.my[b] = my2 + alp2.y;
+        s.L[b] = L2 + arp2;
     }
 }
 
@@ -153,21 +157,30 @@ __device__ __forceinline__ void solve_contact_lanes(const SWT<IDX>& s, uint32_t 
     bool sa = true, sb = true, hit = false;
     f2 dp = {0.f, 0.f};
     float c1 = 0.f, c2 = 0.f;
+    // the momenta, read once (no other constraint of this colour moves a or
+    // b): the even lane's write-back below adds to these values
+    float mx1 = 0.f, my1 = 0.f, L1 = 0.f, mx2 = 0.f, my2 = 0.f, L2 = 0.f;
     if (valid) {
         a = s.ma[m];
         b = s.mb[m];
         sa = s.kind[a] & K_STATIC;
         sb = s.kind[b] & K_STATIC;
+        mx1 = s.mx[a];
+        my1 = s.my[a];
+        L1 = s.L[a];
+        mx2 = s.mx[b];
+        my2 = s.my[b];
+        L2 = s.L[b];
         if (half < (uint32_t)s.mnp[m]) {
             const uint32_t p = s.mp0[m] + half;
             const float bias = s.bias[p];
             if (!(bias < 0.0f)) {  // bias < 0: depth >= 0, accumulators stay 0 (collision.zig:154-158)
                 const float inv_m1 = s.inv_m[a], inv_m2 = s.inv_m[b];
                 const float inv_i1 = s.inv_i[a], inv_i2 = s.inv_i[b];
-                const f2 vlinear_1 = scale2(f2{s.mx[a], s.my[a]}, inv_m1);
-                const float omega1 = s.L[a] * inv_i1;
-                const f2 vlinear_2 = scale2(f2{s.mx[b], s.my[b]}, inv_m2);
-                const float omega2 = s.L[b] * inv_i2;
+                const f2 vlinear_1 = scale2(f2{mx1, my1}, inv_m1);
+                const float omega1 = L1 * inv_i1;
+                const f2 vlinear_2 = scale2(f2{mx2, my2}, inv_m2);
+                const float omega2 = L2 * inv_i2;
                 const f2 n = {s.nx[m], s.ny[m]};
                 const f2 t = cw90(n);
                 f2 r1, r2;
@@ -221,14 +234,14 @@ __device__ __forceinline__ void solve_contact_lanes(const SWT<IDX>& s, uint32_t 
     }
     // A static body receives exactly +0 in the reference; its state is left alone.
     if (!sa) {
-        s.mx[a] += alp1.x;
-        s.my[a] += alp1.y;
-        s.L[a] += arp1;
+        s.mx[a] = mx1 + alp1.x;
+        s.my[a] = my1 + alp1.y;
+        s.L[a] = L1 + arp1;
     }
     if (!sb) {
-        s.mx[b] += alp2.x;
-        s.my[b] += alp2.y;
-        s.L[b] += arp2;
+        s.mx[b] = mx2 + alp2.x;
+        s.my[b] = my2 + alp2.y;
+        s.L[b] = L2 + arp2;
     }
 }
 
