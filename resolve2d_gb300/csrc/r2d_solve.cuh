@@ -15,10 +15,13 @@
 namespace r2d {
 
 // Views of one world's arrays: shared memory in the fused kernel (16-bit
-// manifold indices), global memory in the large-world path (32-bit).
-template <class IDX>
+// manifold indices), global memory in the large-world path (32-bit).  PK:
+// a body's momenta and inverse mass share one 16-byte word (mom4), so that
+// the constraint loops fetch them with one load; else four arrays.
+template <class IDX, bool PK = false>
 struct SWT {
     float *px, *py, *ang, *mx, *my, *L, *inv_m, *inv_i, *cs, *sn, *ang_prev, *tq, *px0, *py0;
+    float4* mom4;  // PK: (mx, my, L, inv_m) of each body
     bool pos0;                           // px0/py0 hold frame-start positions
     const float* __restrict__ gmass;     // this world's masses (global, read-only)
     const float* __restrict__ ginertia;  // this world's inertias
@@ -29,6 +32,37 @@ struct SWT {
     float *r1x, *r1y, *r2x, *r2y, *depth, *odepth, *mn, *mt, *apn, *apt, *bias;
     float *cpn, *cpt;  // compensation words of apn / apt (compensated mode, r2d_accum.h), else null
 
+    __device__ __forceinline__ float& MX(uint32_t i) const {
+        if constexpr (PK) return mom4[i].x;
+        else return mx[i];
+    }
+    __device__ __forceinline__ float& MY(uint32_t i) const {
+        if constexpr (PK) return mom4[i].y;
+        else return my[i];
+    }
+    __device__ __forceinline__ float& AM(uint32_t i) const {  // angular momentum
+        if constexpr (PK) return mom4[i].z;
+        else return L[i];
+    }
+    __device__ __forceinline__ float& IM(uint32_t i) const {  // inverse mass
+        if constexpr (PK) return mom4[i].w;
+        else return inv_m[i];
+    }
+    // (mx, my, L, inv_m) of body i
+    __device__ __forceinline__ float4 mom(uint32_t i) const {
+        if constexpr (PK) return mom4[i];
+        else return make_float4(mx[i], my[i], L[i], inv_m[i]);
+    }
+    // body i's momenta, with its inverse mass `im` (unchanged)
+    __device__ __forceinline__ void put_mom(uint32_t i, float x, float y, float l, float im) const {
+        if constexpr (PK) {
+            mom4[i] = make_float4(x, y, l, im);
+        } else {
+            mx[i] = x;
+            my[i] = y;
+            L[i] = l;
+        }
+    }
     __device__ __forceinline__ float mass(uint32_t i) const { return __ldg(gmass + i); }
     __device__ __forceinline__ float inertia(uint32_t i) const { return __ldg(ginertia + i); }
     // Lever arms of point p between bodies a (reference) and b (incident).
@@ -53,8 +87,8 @@ struct SWT {
 // normal impulse sum clamped at zero, its tangent sum to +-friction times
 // the normal sum; the changes go to the bodies.  Compensated mode keeps each
 // sum's rounding remainder in a second word (r2d_accum.h).
-template <class IDX>
-__device__ __forceinline__ void accumulate(const SWT<IDX>& s, uint32_t p, float pn, float pt, float fr,
+template <class S>
+__device__ __forceinline__ void accumulate(const S& s, uint32_t p, float pn, float pt, float fr,
                                            float* applied_pn, float* applied_pt) {
     if (s.cpn) {
         float an = s.apn[p], cn = s.cpn[p], at = s.apt[p], ct = s.cpt[p];
@@ -83,16 +117,16 @@ __device__ __forceinline__ void accumulate(const SWT<IDX>& s, uint32_t p, float 
 // skipped (the reference's skip keeps an accumulated impulse from ever
 // decreasing, which a warm-started one must be able to); the sum is clamped
 // at zero as written.
-template <bool LEAN, class IDX>
-__device__ __forceinline__ void solve_contact(const SWT<IDX>& s, uint32_t m, bool warm = false) {
+template <bool LEAN, class S>
+__device__ __forceinline__ void solve_contact(const S& s, uint32_t m, bool warm = false) {
     const uint32_t a = s.ma[m], b = s.mb[m];
     const bool sa = s.kind[a] & K_STATIC, sb = s.kind[b] & K_STATIC;
-    const float inv_m1 = s.inv_m[a], inv_m2 = s.inv_m[b];
-    const float inv_i1 = s.inv_i[a], inv_i2 = s.inv_i[b];
     // the momenta, read once: no other constraint of this colour moves a or
     // b, so the sums below are the read-modify-writes the reference does
-    const float mx1 = s.mx[a], my1 = s.my[a], L1 = s.L[a];
-    const float mx2 = s.mx[b], my2 = s.my[b], L2 = s.L[b];
+    const float4 q1 = s.mom(a), q2 = s.mom(b);
+    const float mx1 = q1.x, my1 = q1.y, L1 = q1.z, inv_m1 = q1.w;
+    const float mx2 = q2.x, my2 = q2.y, L2 = q2.z, inv_m2 = q2.w;
+    const float inv_i1 = s.inv_i[a], inv_i2 = s.inv_i[b];
     const f2 vlinear_1 = scale2(f2{mx1, my1}, inv_m1);
     const float omega1 = L1 * inv_i1;
     const f2 vlinear_2 = scale2(f2{mx2, my2}, inv_m2);
@@ -130,16 +164,8 @@ __device__ __forceinline__ void solve_contact(const SWT<IDX>& s, uint32_t m, boo
         }
     }
     // A static body receives exactly +0 in the reference; its state is left alone.
-    if (!sa) {
-        s.mx[a] = mx1 + alp1.x;
-        s.my[a] = my1 + alp1.y;
-        s.L[a] = L1 + arp1;
-    }
-    if (!sb) {
-        s.mx[b] = mx2 + alp2.x;
-        s.my[b] = my2 + alp2.y;
-        s.L[b] = L2 + arp2;
-    }
+    if (!sa) s.put_mom(a, mx1 + alp1.x, my1 + alp1.y, L1 + arp1, inv_m1);
+    if (!sb) s.put_mom(b, mx2 + alp2.x, my2 + alp2.y, L2 + arp2, inv_m2);
 }
 
 // calculateImpulses with two lanes per manifold: lane 2q + h of a warp takes
@@ -149,8 +175,8 @@ __device__ __forceinline__ void solve_contact(const SWT<IDX>& s, uint32_t m, boo
 // order, point 0 then point 1, which keeps every sum bit-identical to
 // solve_contact.  Every lane of the warp must call this (it shuffles);
 // `valid` says whether the lane pair holds a manifold.
-template <bool LEAN, class IDX>
-__device__ __forceinline__ void solve_contact_lanes(const SWT<IDX>& s, uint32_t m, bool valid, uint32_t lane,
+template <bool LEAN, class S>
+__device__ __forceinline__ void solve_contact_lanes(const S& s, uint32_t m, bool valid, uint32_t lane,
                                                     bool warm = false) {
     const uint32_t half = lane & 1u;
     uint32_t a = 0, b = 0;
@@ -159,23 +185,25 @@ __device__ __forceinline__ void solve_contact_lanes(const SWT<IDX>& s, uint32_t 
     float c1 = 0.f, c2 = 0.f;
     // the momenta, read once (no other constraint of this colour moves a or
     // b): the even lane's write-back below adds to these values
-    float mx1 = 0.f, my1 = 0.f, L1 = 0.f, mx2 = 0.f, my2 = 0.f, L2 = 0.f;
+    float mx1 = 0.f, my1 = 0.f, L1 = 0.f, inv_m1 = 0.f, mx2 = 0.f, my2 = 0.f, L2 = 0.f, inv_m2 = 0.f;
     if (valid) {
         a = s.ma[m];
         b = s.mb[m];
         sa = s.kind[a] & K_STATIC;
         sb = s.kind[b] & K_STATIC;
-        mx1 = s.mx[a];
-        my1 = s.my[a];
-        L1 = s.L[a];
-        mx2 = s.mx[b];
-        my2 = s.my[b];
-        L2 = s.L[b];
+        const float4 q1 = s.mom(a), q2 = s.mom(b);
+        mx1 = q1.x;
+        my1 = q1.y;
+        L1 = q1.z;
+        inv_m1 = q1.w;
+        mx2 = q2.x;
+        my2 = q2.y;
+        L2 = q2.z;
+        inv_m2 = q2.w;
         if (half < (uint32_t)s.mnp[m]) {
             const uint32_t p = s.mp0[m] + half;
             const float bias = s.bias[p];
             if (!(bias < 0.0f)) {  // bias < 0: depth >= 0, accumulators stay 0 (collision.zig:154-158)
-                const float inv_m1 = s.inv_m[a], inv_m2 = s.inv_m[b];
                 const float inv_i1 = s.inv_i[a], inv_i2 = s.inv_i[b];
                 const f2 vlinear_1 = scale2(f2{mx1, my1}, inv_m1);
                 const float omega1 = L1 * inv_i1;
@@ -233,16 +261,8 @@ __device__ __forceinline__ void solve_contact_lanes(const SWT<IDX>& s, uint32_t 
         }
     }
     // A static body receives exactly +0 in the reference; its state is left alone.
-    if (!sa) {
-        s.mx[a] = mx1 + alp1.x;
-        s.my[a] = my1 + alp1.y;
-        s.L[a] = L1 + arp1;
-    }
-    if (!sb) {
-        s.mx[b] = mx2 + alp2.x;
-        s.my[b] = my2 + alp2.y;
-        s.L[b] = L2 + arp2;
-    }
+    if (!sa) s.put_mom(a, mx1 + alp1.x, my1 + alp1.y, L1 + arp1, inv_m1);
+    if (!sb) s.put_mom(b, mx2 + alp2.x, my2 + alp2.y, L2 + arp2, inv_m2);
 }
 
 // ---- warm starting (an extension; off in reference mode) ----
@@ -299,8 +319,8 @@ __device__ __forceinline__ unsigned long long warm_key_ids(uint32_t ref_id, uint
 // Applies a manifold's (warm-started) accumulated impulses to its bodies,
 // summed as calculateImpulses sums its applied ones; a point with depth >= 0
 // (bias < 0) starts from zero instead.
-template <bool LEAN, class IDX>
-__device__ __forceinline__ void warm_apply_contact(const SWT<IDX>& s, uint32_t m) {
+template <bool LEAN, class S>
+__device__ __forceinline__ void warm_apply_contact(const S& s, uint32_t m) {
     const uint32_t a = s.ma[m], b = s.mb[m];
     const bool sa = s.kind[a] & K_STATIC, sb = s.kind[b] & K_STATIC;
     const f2 n = {s.nx[m], s.ny[m]};
@@ -332,20 +352,20 @@ __device__ __forceinline__ void warm_apply_contact(const SWT<IDX>& s, uint32_t m
         }
     }
     if (!sa) {
-        s.mx[a] += alp1.x;
-        s.my[a] += alp1.y;
-        s.L[a] += arp1;
+        s.MX(a) += alp1.x;
+        s.MY(a) += alp1.y;
+        s.AM(a) += arp1;
     }
     if (!sb) {
-        s.mx[b] += alp2.x;
-        s.my[b] += alp2.y;
-        s.L[b] += arp2;
+        s.MX(b) += alp2.x;
+        s.MY(b) += alp2.y;
+        s.AM(b) += arp2;
     }
 }
 
 // Constraint solve functions (src/core/Constraints/*.zig).
-template <class IDX>
-__device__ __forceinline__ void solve_joint(const SWT<IDX>& s, uint8_t type, uint32_t i1, uint32_t i2,
+template <class S>
+__device__ __forceinline__ void solve_joint(const S& s, uint8_t type, uint32_t i1, uint32_t i2,
                                             const float* __restrict__ prm, float h) {
     const float pmax = __ldg(prm + 0), pmin = __ldg(prm + 1), beta = __ldg(prm + 2);
     if (type == J_DISTANCE) {  // DistanceJoint.zig:40-75
@@ -354,8 +374,8 @@ __device__ __forceinline__ void solve_joint(const SWT<IDX>& s, uint8_t type, uin
         const bool st1 = s.kind[i1] & K_STATIC, st2 = s.kind[i2] & K_STATIC;
         const float w1 = st1 ? 0.f : 1.0f / s.mass(i1);
         const float w2 = st2 ? 0.f : 1.0f / s.mass(i2);
-        const f2 v1 = scale2(f2{s.mx[i1], s.my[i1]}, w1);
-        const f2 v2 = scale2(f2{s.mx[i2], s.my[i2]}, w2);
+        const f2 v1 = scale2(f2{s.MX(i1), s.MY(i1)}, w1);
+        const f2 v2 = scale2(f2{s.MX(i2), s.MY(i2)}, w2);
         const f2 rel = sub2(v2, v1);
         const f2 d = sub2(f2{s.px[i2], s.py[i2]}, f2{s.px[i1], s.py[i1]});
         const f2 normal = normalize2(d);
@@ -366,10 +386,10 @@ __device__ __forceinline__ void solve_joint(const SWT<IDX>& s, uint8_t type, uin
         const float den = 1.0f / zmax(fabsf(ndv), epsilon);
         J = zclamp(J, pmin * den, pmax * den);
         const f2 dp = scale2(normal, J);
-        s.mx[i1] -= dp.x;
-        s.my[i1] -= dp.y;
-        s.mx[i2] += dp.x;
-        s.my[i2] += dp.y;
+        s.MX(i1) -= dp.x;
+        s.MY(i1) -= dp.y;
+        s.MX(i2) += dp.x;
+        s.MY(i2) += dp.y;
     } else if (type == J_OFFSET) {  // OffsetDistanceJoint.zig:44-105
         const float epsilon = CONSTRAINT_GRADIENT_DIVISION_LIMIT;
         const f2 r1 = {__ldg(prm + 3), __ldg(prm + 4)}, r2 = {__ldg(prm + 5), __ldg(prm + 6)};
@@ -384,10 +404,10 @@ __device__ __forceinline__ void solve_joint(const SWT<IDX>& s, uint8_t type, uin
         const float inv_m2 = st2 ? 0.f : 1.0f / s.mass(i2);
         const float inv_i1 = st1 ? 0.f : 1.0f / s.inertia(i1);
         const float inv_i2 = st2 ? 0.f : 1.0f / s.inertia(i2);
-        const f2 vl1 = scale2(f2{s.mx[i1], s.my[i1]}, inv_m1);
-        const float om1 = s.L[i1] * inv_i1;
-        const f2 vl2 = scale2(f2{s.mx[i2], s.my[i2]}, inv_m2);
-        const float om2 = s.L[i2] * inv_i2;
+        const f2 vl1 = scale2(f2{s.MX(i1), s.MY(i1)}, inv_m1);
+        const float om1 = s.AM(i1) * inv_i1;
+        const f2 vl2 = scale2(f2{s.MX(i2), s.MY(i2)}, inv_m2);
+        const float om2 = s.AM(i2) * inv_i2;
         const f2 v1 = add2(vl1, f2{-rr1.y * om1, rr1.x * om1});
         const f2 v2 = add2(vl2, f2{-rr2.y * om2, rr2.x * om2});
         const f2 dv = sub2(v2, v1);
@@ -402,18 +422,18 @@ __device__ __forceinline__ void solve_joint(const SWT<IDX>& s, uint8_t type, uin
         const float den2 = 1.0f / zmax(fabsf(ndv), epsilon);
         J = zclamp(J, pmin * den2, pmax * den2);
         const f2 dp = scale2(normal, J);
-        s.mx[i1] -= dp.x;
-        s.my[i1] -= dp.y;
-        s.L[i1] -= J * r1xn;
-        s.mx[i2] += dp.x;
-        s.my[i2] += dp.y;
-        s.L[i2] += J * r2xn;
+        s.MX(i1) -= dp.x;
+        s.MY(i1) -= dp.y;
+        s.AM(i1) -= J * r1xn;
+        s.MX(i2) += dp.x;
+        s.MY(i2) += dp.y;
+        s.AM(i2) += J * r2xn;
     } else if (type == J_FIXED) {  // FixedPositionJoint.zig:38-72
         if (s.kind[i1] & K_STATIC) return;
         const float epsilon = ALLOWED_CONSTRAINT_VALUE;
         const f2 target = {__ldg(prm + 3), __ldg(prm + 4)};
         const float w = 1.0f / s.mass(i1);
-        const f2 v = scale2(f2{s.mx[i1], s.my[i1]}, w);
+        const f2 v = scale2(f2{s.MX(i1), s.MY(i1)}, w);
         const f2 delta = sub2(target, f2{s.px[i1], s.py[i1]});
         const float dist = length2(delta);
         if (dist < ALLOWED_CONSTRAINT_VALUE) return;
@@ -424,14 +444,14 @@ __device__ __forceinline__ void solve_joint(const SWT<IDX>& s, uint8_t type, uin
         const float den = 1.0f / zmax(fabsf(relv), epsilon);
         J = zclamp(J, pmin * den, pmax * den);
         const f2 dp = scale2(normal, J);
-        s.mx[i1] += dp.x;
-        s.my[i1] += dp.y;
+        s.MX(i1) += dp.x;
+        s.MY(i1) += dp.y;
     } else {  // MotorJoint.zig:38-64
         if (s.kind[i1] & K_STATIC) return;
         const float epsilon = ALLOWED_CONSTRAINT_VALUE;
         const float target = __ldg(prm + 3);
         const float I = s.inertia(i1);
-        const float omega = s.L[i1] / I;
+        const float omega = s.AM(i1) / I;
         const float C = omega - target;
         if (fabsf(C) < ALLOWED_CONSTRAINT_VALUE) return;
         const float bias = beta * C;
@@ -440,7 +460,7 @@ __device__ __forceinline__ void solve_joint(const SWT<IDX>& s, uint8_t type, uin
         const float relv = torque / I;
         const float den = 1.0f / zmax(fabsf(relv), epsilon);
         J = zclamp(J, pmin * den, pmax * den);
-        s.L[i1] += J * h;
+        s.AM(i1) += J * h;
     }
 }
 

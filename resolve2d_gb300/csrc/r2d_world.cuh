@@ -61,7 +61,7 @@ struct Caps {
 // Byte offsets into the dynamic shared memory of one CTA.
 struct Layout {
     // bodies (whole step)
-    uint32_t px, py, ang, mx, my, L, inv_m, inv_i, cs, sn, ang_prev, tq, px0, py0, kind;
+    uint32_t px, py, ang, mom, inv_i, cs, sn, ang_prev, tq, px0, py0, kind;  // mom: (mx, my, L, inv_m) float4
     // manifolds + points (narrowphase .. end) -- aliased by the broadphase scratch
     uint32_t ma, mb, mp0, mnp, mcol, nx, ny, fric;
     uint32_t r1x, r1y, r2x, r2y, depth, odepth, mn, mt, apn, apt, bias;
@@ -110,8 +110,7 @@ __host__ __device__ inline Layout make_layout(const Caps& c, const LayoutOpts& f
     L.has_prev = f.prev || !f.lean;
     L.has_comp = f.comp;
     L.px = take(nb4); L.py = take(nb4); L.ang = take(nb4);
-    L.mx = take(nb4); L.my = take(nb4); L.L = take(nb4);
-    L.inv_m = take(nb4); L.inv_i = take(nb4);
+    L.mom = take(4 * nb4); L.inv_i = take(nb4);
     L.cs = take(nb4); L.sn = take(nb4); L.tq = take(nb4);
     if (L.has_prev) L.ang_prev = take(nb4);
     if (L.has_pos0) {

@@ -297,7 +297,7 @@ __device__ bool colour_greedy_sorted(uint32_t count, uint32_t n, Ends ends, Mix 
     return __syncthreads_or(overflow) != 0;
 }
 
-using SW = SWT<uint16_t>;
+using SW = SWT<uint16_t, true>;
 
 // Worlds of at most this many bodies test every pair of bodies directly
 // instead of binning them (the same pairs; fewer scans and barriers).
@@ -414,8 +414,9 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
 
     SW s;
     s.px = SMF(Lo.px); s.py = SMF(Lo.py); s.ang = SMF(Lo.ang);
-    s.mx = SMF(Lo.mx); s.my = SMF(Lo.my); s.L = SMF(Lo.L);
-    s.inv_m = SMF(Lo.inv_m); s.inv_i = SMF(Lo.inv_i);
+    s.mx = s.my = s.L = s.inv_m = nullptr;
+    s.mom4 = reinterpret_cast<float4*>(sm + Lo.mom);
+    s.inv_i = SMF(Lo.inv_i);
     s.cs = SMF(Lo.cs); s.sn = SMF(Lo.sn); s.ang_prev = SMF(Lo.ang_prev); s.tq = SMF(Lo.tq);
     s.px0 = SMF(Lo.px0); s.py0 = SMF(Lo.py0);
     s.pos0 = Lo.has_pos0;
@@ -480,14 +481,11 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
         s.px[i] = r.px;
         s.py[i] = r.py;
         s.ang[i] = r.a;
-        s.mx[i] = r.mx;
-        s.my[i] = r.my;
-        s.L[i] = r.L;
+        s.put_mom(i, r.mx, r.my, r.L, (r.k & K_STATIC) ? 0.f : 1.0f / r.m);
         if (Lo.has_pos0) {
             s.px0[i] = r.px;
             s.py0[i] = r.py;
         }
-        s.inv_m[i] = (r.k & K_STATIC) ? 0.f : 1.0f / r.m;
         s.inv_i[i] = (r.k & K_STATIC) ? 0.f : 1.0f / r.I;
         s.kind[i] = r.k;
         float c = 1.f, sn = 0.f;
@@ -679,6 +677,7 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
             f2 pi = {ax[i], ay[i]};
             float hwi = ahw[i], hhi = ahh[i];
             bool sti = (s.kind[i] & K_STATIC) != 0;
+            uint32_t sb0 = (uint32_t)eslot[e] + 1u - first;  // candidate k pairs e with sorted entry sb0 + k
             for (uint32_t k = k0; k < k1; ++k) {
                 if (k >= next) {
                     do {
@@ -694,18 +693,24 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
                     hwi = ahw[i];
                     hhi = ahh[i];
                     sti = (s.kind[i] & K_STATIC) != 0;
+                    sb0 = (uint32_t)eslot[e] + 1u - first;
                 }
-                const uint32_t e2 = sbody[(uint32_t)eslot[e] + 1u + (k - first)];
+                const uint32_t e2 = sbody[sb0 + k];
                 const uint32_t j = ebody[e2];
-                const int32_t fx0j = fx0[j], fy0j = fy0[j];
+                // everything the tests below read of j, in one round of loads
+                const int32_t fx0j = fx0[j], fy0j = fy0[j], fx1j = fx1[j];
+                const uint32_t bj = bcnt[j];
+                const f2 pj = {ax[j], ay[j]};
+                const float hwj = ahw[j], hhj = ahh[j];
+                const bool stj = (s.kind[j] & K_STATIC) != 0;
                 // a pair is reported from the first cell the two cover in common
                 if (max(fx0i, fx0j) != cxe || max(fy0i, fy0j) != cye) continue;
                 int32_t cx2, cy2;
-                entry_cell(e2, bcnt[j], fx0j, fx1[j], fy0j, &cx2, &cy2);
+                entry_cell(e2, bj, fx0j, fx1j, fy0j, &cx2, &cy2);
                 if (cx2 != cxe || cy2 != cye) continue;  // another cell hashed to this bucket
-                if (sti && (s.kind[j] & K_STATIC)) continue;
+                if (sti && stj) continue;
                 // symmetric in the two bodies: |dx|, |dy| and the sums commute
-                if (!aabb_intersects(pi, hwi, hhi, f2{ax[j], ay[j]}, ahw[j], ahh[j])) continue;
+                if (!aabb_intersects(pi, hwi, hhi, pj, hwj, hhj)) continue;
                 if (!shares_bucket(i, j, rx0, ry0, rx1, ry1, bmod)) continue;
                 const uint32_t plo = min(i, j), phi = max(i, j);
                 if (wd.nexcl && excluded(P.excl + wd.excl_off, wd.nexcl, ((unsigned long long)plo << 32) | phi)) continue;
@@ -1073,9 +1078,9 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
                     P.state[(size_t)S_AABB_HH * NB + g] = hh;
                 }
                 if (k & K_STATIC) continue;
-                s.mx[i] += fx * h;
-                s.my[i] += fy * h;
-                s.L[i] += tq * h;
+                s.MX(i) += fx * h;
+                s.MY(i) += fy * h;
+                s.AM(i) += tq * h;
                 s.tq[i] = tq;
             }
             __syncthreads();
@@ -1102,7 +1107,7 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
                     s.r2x[p] = rr2.x;
                     s.r2y[p] = rr2.y;
                 }
-                const float inv_m1 = s.inv_m[a], inv_m2 = s.inv_m[b];
+                const float inv_m1 = s.IM(a), inv_m2 = s.IM(b);
                 const float inv_mass = inv_m1 + inv_m2;
                 const float inv_i1 = s.inv_i[a], inv_i2 = s.inv_i[b];
                 const f2 t2 = cw90(n2);
@@ -1162,13 +1167,13 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
                 const uint8_t k = s.kind[i];
                 if (k & K_STATIC) continue;
                 if (P.pos64) {
-                    integrate_pose64(P.pos64, NB, base + i, s.mx[i], s.my[i], s.L[i], h, s.mass(i), s.inertia(i),
+                    integrate_pose64(P.pos64, NB, base + i, s.MX(i), s.MY(i), s.AM(i), h, s.mass(i), s.inertia(i),
                                      &s.px[i], &s.py[i], &s.ang[i]);
                 } else {
                     const float sm_ = h / s.mass(i);
-                    s.px[i] += s.mx[i] * sm_;
-                    s.py[i] += s.my[i] * sm_;
-                    s.ang[i] += s.L[i] * h / s.inertia(i);
+                    s.px[i] += s.MX(i) * sm_;
+                    s.py[i] += s.MY(i) * sm_;
+                    s.ang[i] += s.AM(i) * h / s.inertia(i);
                 }
                 s.tq[i] = 0.f;
                 if (!last && ((k & K_RECT) || disc_rot)) {
@@ -1215,9 +1220,9 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
             P.state[(size_t)S_POS_X * NB + g] = s.px[i];
             P.state[(size_t)S_POS_Y * NB + g] = s.py[i];
             P.state[(size_t)S_ANGLE * NB + g] = s.ang[i];
-            P.state[(size_t)S_MOM_X * NB + g] = s.mx[i];
-            P.state[(size_t)S_MOM_Y * NB + g] = s.my[i];
-            P.state[(size_t)S_ANG_MOM * NB + g] = s.L[i];
+            P.state[(size_t)S_MOM_X * NB + g] = s.MX(i);
+            P.state[(size_t)S_MOM_Y * NB + g] = s.MY(i);
+            P.state[(size_t)S_ANG_MOM * NB + g] = s.AM(i);
             // consumed forces are cleared (lib.zig:247-248); a frame call's
             // forces replace the state's rows as if written before the step:
             // cleared for a dynamic body, kept (unused) for a static one
@@ -1235,12 +1240,12 @@ __global__ void __launch_bounds__(NT, min_blocks_for(NT)) world_step_kernel(cons
                 ext_out[g] = s.px[i];
                 ext_out[(size_t)NB + g] = s.py[i];
                 ext_out[2 * (size_t)NB + g] = s.ang[i];
-                ext_out[3 * (size_t)NB + g] = s.mx[i];
-                ext_out[4 * (size_t)NB + g] = s.my[i];
-                ext_out[5 * (size_t)NB + g] = s.L[i];
+                ext_out[3 * (size_t)NB + g] = s.MX(i);
+                ext_out[4 * (size_t)NB + g] = s.MY(i);
+                ext_out[5 * (size_t)NB + g] = s.AM(i);
             }
             if (P.sleep && !(s.kind[i] & K_STATIC))
-                moving = moving || !r2d_body_still(s.mx[i], s.my[i], s.L[i], s.inv_m[i], s.inv_i[i]);
+                moving = moving || !r2d_body_still(s.MX(i), s.MY(i), s.AM(i), s.IM(i), s.inv_i[i]);
         }
         if (P.sleep) {
             const bool any_moving = __syncthreads_or(moving) != 0;
