@@ -87,29 +87,44 @@ struct SWT {
 // normal impulse sum clamped at zero, its tangent sum to +-friction times
 // the normal sum; the changes go to the bodies.  Compensated mode keeps each
 // sum's rounding remainder in a second word (r2d_accum.h).
-template <class S>
-__device__ __forceinline__ void accumulate(const S& s, uint32_t p, float pn, float pt, float fr,
-                                           float* applied_pn, float* applied_pt) {
-    if (s.cpn) {
-        float an = s.apn[p], cn = s.cpn[p], at = s.apt[p], ct = s.cpt[p];
+// The accumulator update of calculateImpulses (collision.zig:182-190) on a
+// point's accumulated impulses an, at (and, compensated, their words cn, ct)
+// held in registers; *applied_pn / *applied_pt get the changes.
+__device__ __forceinline__ void acc_update(bool comp, float& an, float& at, float& cn, float& ct, float pn, float pt,
+                                           float fr, float* applied_pn, float* applied_pt) {
+    if (comp) {
         *applied_pn = r2d_acc_add_max(&an, &cn, pn, 0.0f);
         const float max_pt = fr * fabsf(an);
         *applied_pt = r2d_acc_add_clamp(&at, &ct, pt, -max_pt, max_pt);
-        s.apn[p] = an;
-        s.cpn[p] = cn;
-        s.apt[p] = at;
-        s.cpt[p] = ct;
         return;
     }
-    const float acc = s.apn[p];
-    const float nacc = zmax(0.0f, acc + pn);
-    *applied_pn = nacc - acc;
-    s.apn[p] = nacc;
+    const float nacc = zmax(0.0f, an + pn);
+    *applied_pn = nacc - an;
+    an = nacc;
     const float max_pt = fr * fabsf(nacc);
-    const float acct = s.apt[p];
-    const float nacct = zclamp(acct + pt, -max_pt, max_pt);
-    *applied_pt = nacct - acct;
-    s.apt[p] = nacct;
+    const float nacct = zclamp(at + pt, -max_pt, max_pt);
+    *applied_pt = nacct - at;
+    at = nacct;
+}
+
+// acc_update on point p's accumulators in the world's arrays; every load
+// comes before the first store.
+template <class S>
+__device__ __forceinline__ void accumulate(const S& s, uint32_t p, float pn, float pt, float fr,
+                                           float* applied_pn, float* applied_pt) {
+    const bool comp = s.cpn != nullptr;
+    float an = s.apn[p], at = s.apt[p], cn = 0.f, ct = 0.f;
+    if (comp) {
+        cn = s.cpn[p];
+        ct = s.cpt[p];
+    }
+    acc_update(comp, an, at, cn, ct, pn, pt, fr, applied_pn, applied_pt);
+    s.apn[p] = an;
+    s.apt[p] = at;
+    if (comp) {
+        s.cpn[p] = cn;
+        s.cpt[p] = ct;
+    }
 }
 
 // CollisionManifold.calculateImpulses (collision.zig:135-218).  `warm`:
@@ -134,33 +149,59 @@ __device__ __forceinline__ void solve_contact(const S& s, uint32_t m, bool warm 
     const f2 n = {s.nx[m], s.ny[m]};
     const f2 t = cw90(n);
     const float fr = s.fric[m];
+    const uint32_t p0 = s.mp0[m], np = s.mnp[m];
+    const bool comp = s.cpn != nullptr;
+    // Both points start from the velocities above (collision.zig:145-149),
+    // so their inputs are all read before either point's accumulators are
+    // written back; the impulses reach the bodies in the reference's order.
+    float bias[2], mnp_[2], mtp[2], an[2], at[2], cn[2] = {0.f, 0.f}, ct[2] = {0.f, 0.f};
+    f2 r1[2], r2[2];
+#pragma unroll
+    for (uint32_t k = 0; k < 2; ++k) {
+        bias[k] = -1.f;
+        if (k >= np) continue;
+        const uint32_t p = p0 + k;
+        bias[k] = s.bias[p];
+        s.template arms<LEAN>(p, a, b, &r1[k], &r2[k]);
+        mnp_[k] = s.mn[p];
+        mtp[k] = s.mt[p];
+        an[k] = s.apn[p];
+        at[k] = s.apt[p];
+        if (comp) {
+            cn[k] = s.cpn[p];
+            ct[k] = s.cpt[p];
+        }
+    }
     f2 alp1 = {0.f, 0.f}, alp2 = {0.f, 0.f};
     float arp1 = 0.f, arp2 = 0.f;
-    const uint32_t p0 = s.mp0[m], np = s.mnp[m];
-    for (uint32_t k = 0; k < np; ++k) {
-        const uint32_t p = p0 + k;
-        const float bias = s.bias[p];
-        if (bias < 0.0f) continue;  // depth >= 0: accumulators stay 0 (collision.zig:154-158)
-        f2 r1, r2;
-        s.template arms<LEAN>(p, a, b, &r1, &r2);
-        const f2 v1 = add2(vlinear_1, f2{-r1.y * omega1, r1.x * omega1});
-        const f2 v2 = add2(vlinear_2, f2{-r2.y * omega2, r2.x * omega2});
+#pragma unroll
+    for (uint32_t k = 0; k < 2; ++k) {
+        if (bias[k] < 0.0f) continue;  // depth >= 0 (or no point): accumulators stay 0 (collision.zig:154-158)
+        const f2 v1 = add2(vlinear_1, f2{-r1[k].y * omega1, r1[k].x * omega1});
+        const f2 v2 = add2(vlinear_2, f2{-r2[k].y * omega2, r2[k].x * omega2});
         const f2 dv = sub2(v1, v2);
-        float num = dot2(dv, n) + bias;  // BAUMGARTE*max(0,-depth-SLOP)/h (collision.zig:172)
-        const float pn = num * s.mn[p];
+        float num = dot2(dv, n) + bias[k];  // BAUMGARTE*max(0,-depth-SLOP)/h (collision.zig:172)
+        const float pn = num * mnp_[k];
         if (!warm && pn < MIN_MANIFOLD_IMPULSE) continue;
         num = dot2(dv, t);
-        const float pt = num * s.mt[p];
+        const float pt = num * mtp[k];
         float applied_pn, applied_pt;
-        accumulate(s, p, pn, pt, fr, &applied_pn, &applied_pt);
+        acc_update(comp, an[k], at[k], cn[k], ct[k], pn, pt, fr, &applied_pn, &applied_pt);
+        const uint32_t p = p0 + k;
+        s.apn[p] = an[k];
+        s.apt[p] = at[k];
+        if (comp) {
+            s.cpn[p] = cn[k];
+            s.cpt[p] = ct[k];
+        }
         const f2 dp = add2(scale2(n, applied_pn), scale2(t, applied_pt));
         if (!sa) {
             alp1 = sub2(alp1, dp);
-            arp1 -= cross2(r1, dp);
+            arp1 -= cross2(r1[k], dp);
         }
         if (!sb) {
             alp2 = add2(alp2, dp);
-            arp2 += cross2(r2, dp);
+            arp2 += cross2(r2[k], dp);
         }
     }
     // A static body receives exactly +0 in the reference; its state is left alone.
