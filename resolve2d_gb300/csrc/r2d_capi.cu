@@ -142,7 +142,7 @@ struct Engine {
     // Size classes run concurrently on auxiliary streams forked from and
     // joined back into `stream`, so one class's tail overlaps the others.
     // Classes sharing a stream would run one after the other, so there is a
-    // stream for each of the 11 body bounds x 3 capacity boosts a step
+    // stream for each of the size classes (body bounds x capacity boosts) a step
     // normally has.
     static constexpr int NAUX = R2D_NAUX;
     cudaStream_t aux[NAUX] = {};
@@ -223,6 +223,10 @@ struct Engine {
     // memory, step through the grid-wide pipeline of r2d_large.cu on their
     // own stream while the fused classes run.
     static constexpr uint32_t FUSED_MAX_BODIES = 520;
+    // Size classes of the fused kernel, by body count (a class's shared
+    // memory is sized for its bound).
+    static constexpr uint32_t CLASS_BOUNDS[] = {32, 64, 96, 128, 160, 192, 256, 320, 384, 448, 520};
+    static constexpr int NBOUNDS = sizeof(CLASS_BOUNDS) / sizeof(CLASS_BOUNDS[0]);
     // Largest spatial-hash table (table_mult x bodies) of one world.
     static constexpr unsigned long long MAX_TABLE_BUCKETS = 1ull << 31;
     std::vector<uint8_t> world_large;                 // [nworlds] routed to the large path
@@ -977,16 +981,16 @@ struct Engine {
         if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
             status = fail(R2D_ERR_CUDA, "autotune events");
         } else {
-            static constexpr uint32_t bnd[] = {32, 64, 96, 128, 160, 192, 256, 320, 384, 448, 520};
+            const uint32_t* bnd = CLASS_BOUNDS;
             static constexpr int cand[] = {32, 64, 128, 256, 512};
-            std::vector<int> used(11, 0);
+            std::vector<int> used(NBOUNDS, 0);
             for (const auto& c : classes)
-                for (int k = 0; k < 11; ++k)
+                for (int k = 0; k < NBOUNDS; ++k)
                     if (c.caps.nb == bnd[k]) used[k] = 1;
             // two passes: a class's best tile depends on the others' (they
             // share the SMs), so the second pass revisits every class
             for (int pass = 0; pass < 2; ++pass)
-            for (int k = 0; k < 11 && status == R2D_OK; ++k) {
+            for (int k = 0; k < NBOUNDS && status == R2D_OK; ++k) {
                 if (!used[k]) continue;
                 const int start = thread_override[k] ? thread_override[k] : default_threads(bnd[k]);
                 thread_override[k] = start;
@@ -1032,9 +1036,9 @@ struct Engine {
         for (auto& c : classes) dfree(c.d_list);
         classes.clear();
         // size classes by body count: bounds in bodies
-        static constexpr uint32_t bounds[] = {32, 64, 96, 128, 160, 192, 256, 320, 384, 448, 520};
-        constexpr int nbnd = sizeof(bounds) / sizeof(bounds[0]);
-        static_assert(bounds[nbnd - 1] == FUSED_MAX_BODIES, "largest fused class");
+        const uint32_t* bounds = CLASS_BOUNDS;
+        constexpr int nbnd = NBOUNDS;
+        static_assert(CLASS_BOUNDS[NBOUNDS - 1] == FUSED_MAX_BODIES, "largest fused class");
         auto bound_of = [&](uint32_t n) {
             int k = 0;
             while (k < nbnd - 1 && n > bounds[k]) ++k;
