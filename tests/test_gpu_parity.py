@@ -376,3 +376,32 @@ def test_autotune_restores_state_and_keeps_results():
     st = b.read_state()
     for w, o in enumerate(oracles):
         assert_state_equal(st[:, sc.body_off[w]:sc.body_off[w + 1]], o.state(), f"world {w}")
+
+
+def test_launch_paths_agree():
+    # graph replay (the default), kernel-by-kernel launches (R2D_NO_GRAPH=1,
+    # read when a batch is created) and the launch priorities left at the
+    # default level (R2D_CLASS_PRIORITIES="") step a batch of every size
+    # class to the same bits
+    import os
+
+    sc = scenes.batched_worlds("paths", seed=14, nworlds=48, steps=5, lo=16, hi=512)
+    states = []
+    for env in ({}, {"R2D_NO_GRAPH": "1"}, {"R2D_CLASS_PRIORITIES": ""}):
+        old = {k: os.environ.get(k) for k in env}
+        os.environ.update(env)
+        try:
+            b = Batch.from_scene(sc)
+        finally:
+            for k, v in old.items():
+                if v is None:
+                    del os.environ[k]
+                else:
+                    os.environ[k] = v
+        for _ in range(sc.steps):
+            b.process(sc.dt, sc.sub_steps, sc.iters)
+        b.sync()
+        states.append(b.read_state())
+        b.close()
+    for s in states[1:]:
+        np.testing.assert_array_equal(s.view(np.uint32), states[0].view(np.uint32))
