@@ -123,7 +123,8 @@ struct KClass {
     std::vector<uint32_t> worlds;
     uint32_t* d_list = nullptr;
     uint32_t smem = 0;
-    int priority = 0;  // launch priority (plan(): large and small bounds paired, from the top)
+    uint32_t boost = 0;  // the capacity boosts its worlds carry
+    int priority = 0;    // launch priority (plan(): large and small bounds paired, from the top)
 };
 
 // Size-class launch priorities on (R2D_CLASS_PRIORITY=0 leaves them all at
@@ -343,19 +344,34 @@ struct Engine {
         colour_round_limit = rl ? (uint32_t)strtoul(rl, nullptr, 10) : 0u;
         const char* fs = getenv("R2D_FINE_CELL_SCALE");
         if (fs && strtof(fs, nullptr) > 0.f) fine_scale = strtof(fs, nullptr);
-        if (const char* pm = getenv("R2D_CLASS_PRIORITIES")) {
-            priority_map_set = true;
-            const char* q = pm;
+        // "bound:value,bound:value,..." lists (bounds in bodies)
+        auto parse_map = [](const char* q, std::vector<std::pair<uint32_t, int>>* out) {
             while (*q) {
                 char* e1 = nullptr;
                 const unsigned long nb = strtoul(q, &e1, 10);
                 if (e1 == q || *e1 != ':') break;
                 char* e2 = nullptr;
-                const long pr = strtol(e1 + 1, &e2, 10);
+                const long v = strtol(e1 + 1, &e2, 10);
                 if (e2 == e1 + 1) break;
-                priority_map.push_back({(uint32_t)nb, (int)pr});
+                out->push_back({(uint32_t)nb, (int)v});
                 q = *e2 == ',' ? e2 + 1 : e2;
             }
+        };
+        if (const char* pm = getenv("R2D_CLASS_PRIORITIES")) {
+            priority_map_set = true;
+            parse_map(pm, &priority_map);
+        }
+        // Tuning: threads per CTA by body bound (R2D_CLASS_THREADS, e.g.
+        // "448:128,520:256"), as if the autotuner had chosen them.
+        if (const char* tm = getenv("R2D_CLASS_THREADS")) {
+            std::vector<std::pair<uint32_t, int>> tmap;
+            parse_map(tm, &tmap);
+            for (const auto& kv : tmap)
+                for (int k = 0; k < NBOUNDS; ++k)
+                    if (CLASS_BOUNDS[k] == kv.first &&
+                        (kv.second == 32 || kv.second == 64 || kv.second == 128 || kv.second == 256 ||
+                         kv.second == 512))
+                        thread_override[k] = kv.second;
         }
         CUDA_TRY(dalloc(d_call, 1));
         CUDA_TRY(dalloc(d_ext, 1));
@@ -1090,6 +1106,7 @@ struct Engine {
                 if (d.n) rect_frac = std::max(rect_frac, (float)rects / (float)d.n);
             }
             kc.caps = caps_for(bounds[k], max_nj, rect_frac, max_cells, boost);
+            kc.boost = boost;
             kc.opts = layout_opts(!(boost & BOOST_FULL), plan_multi_substep);
             // A world's phases rarely have more parallel items than this many
             // threads; smaller CTAs let more worlds share an SM.
@@ -1136,6 +1153,13 @@ struct Engine {
                     c.priority = std::min(greatest + std::min(r, D - 1 - r), least);
                 }
             }
+        }
+        if (verbose) {
+            fprintf(stderr, "r2d: plan: %zu classes (bound/boost: worlds, threads, shared B, priority):", classes.size());
+            for (const auto& c : classes)
+                fprintf(stderr, " %u/%u: %zu %d %u %d;", c.caps.nb, c.boost, c.worlds.size(), c.threads, c.smem,
+                        c.priority);
+            fprintf(stderr, "\n");
         }
         large_list.clear();
         for (uint32_t w = 0; w < nworlds; ++w) {
